@@ -1,0 +1,341 @@
+"""Python binding of libcolo (ctypes over the C ABI in include/colo.h).
+
+The product path is libcolo.so: hand-written sm_103a CUDA kernels plus the
+C++ level loop.  There is no CPU fallback -- importing works without a GPU,
+but every mining call fails with ColoError(COLO_ERR_NO_DEVICE) when no CUDA
+device is present.
+
+Mirrors the reference's colocationFinder entry points
+(Codes/colocationFinder.h:138-183): LoadParameter -> read_params,
+populateData -> Dataset.from_csv, Begin's level loop -> Context.mine.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _build
+
+OK = 0
+STATUS = {0: "COLO_OK", 1: "COLO_ERR_ARG", 2: "COLO_ERR_IO", 3: "COLO_ERR_PARSE", 4: "COLO_ERR_INPUT",
+          5: "COLO_ERR_CUDA", 6: "COLO_ERR_NOMEM", 7: "COLO_ERR_TIMEOUT", 8: "COLO_ERR_CAPACITY",
+          9: "COLO_ERR_NO_DEVICE", 10: "COLO_ERR_INTERNAL"}
+MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
+
+# Every symbol declared in include/colo.h (checked by the CPU tests).
+EXPORTS = [
+    "colo_status_string", "colo_create", "colo_destroy", "colo_last_error", "colo_params_default",
+    "colo_read_params", "colo_read_config", "colo_dataset_from_csv", "colo_dataset_from_host",
+    "colo_dataset_write_csv", "colo_dataset_upload", "colo_dataset_evict", "colo_dataset_num_points",
+    "colo_dataset_num_features", "colo_dataset_feature_name", "colo_dataset_free", "colo_mine",
+    "colo_mine_batch", "colo_result_num_levels", "colo_result_level_size", "colo_result_level_candidates",
+    "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
+    "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
+    "colo_stage_filter", "colo_stage_sqdist",
+]
+
+
+class ColoError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+
+
+class Params(C.Structure):
+    _fields_ = [("distance", C.c_float), ("pi_threshold", C.c_float), ("filter_flag", C.c_uint32),
+                ("max_size", C.c_uint32), ("mode", C.c_int32), ("keep_tables", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
+
+
+_P = C.c_void_p
+_u64p = C.POINTER(C.c_uint64)
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+_f32p = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int32)
+_lib = None
+
+
+def _ptr(a: Optional[np.ndarray], t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def load(build: bool = True) -> C.CDLL:
+    """Load libcolo.so (building it first when sources changed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build:
+        _build.build()
+    path = _build.lib_path("libcolo.so")
+    if not path.exists():
+        raise ColoError(9, f"{path} is missing: run __graft_entry__.build()")
+    lib = C.CDLL(str(path))
+    sig = {
+        "colo_status_string": (C.c_char_p, [C.c_int]),
+        "colo_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+        "colo_destroy": (C.c_int, [_P]),
+        "colo_last_error": (C.c_char_p, [_P]),
+        "colo_params_default": (None, [C.POINTER(Params)]),
+        "colo_read_params": (C.c_int, [C.c_char_p, C.POINTER(Params)]),
+        "colo_read_config": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                       C.c_size_t]),
+        "colo_dataset_from_csv": (C.c_int, [_P, C.c_char_p, C.POINTER(_P)]),
+        "colo_dataset_from_host": (C.c_int, [_P, _f32p, _f32p, _i32p, C.c_uint64, _f32p, C.POINTER(_P)]),
+        "colo_dataset_write_csv": (C.c_int, [_P, C.c_char_p]),
+        "colo_dataset_upload": (C.c_int, [_P]),
+        "colo_dataset_evict": (C.c_int, [_P]),
+        "colo_dataset_num_points": (C.c_uint64, [_P]),
+        "colo_dataset_num_features": (C.c_uint32, [_P]),
+        "colo_dataset_feature_name": (C.c_char_p, [_P, C.c_uint32]),
+        "colo_dataset_free": (None, [_P]),
+        "colo_mine": (C.c_int, [_P, _P, C.POINTER(Params), C.POINTER(_P)]),
+        "colo_mine_batch": (C.c_int, [_P, C.POINTER(_P), C.POINTER(Params), C.c_uint32, C.POINTER(_P)]),
+        "colo_result_num_levels": (C.c_uint32, [_P]),
+        "colo_result_level_size": (C.c_uint32, [_P, C.c_uint32]),
+        "colo_result_level_candidates": (C.c_uint64, [_P, C.c_uint32]),
+        "colo_result_level": (C.c_int, [_P, C.c_uint32, _u32p, _u64p, _u8p, _u64p, _u64p, _f32p, _u8p, _u32p]),
+        "colo_result_table": (C.c_uint64, [_P, C.c_uint32, C.c_uint64, _u32p]),
+        "colo_result_write_patterns": (C.c_int, [_P, _P, C.c_char_p]),
+        "colo_result_times": (C.c_int, [_P, C.POINTER(C.c_double)]),
+        "colo_result_counters": (C.c_int, [_P, _u64p]),
+        "colo_result_free": (None, [_P]),
+        "colo_stage_cells": (C.c_int, [_P, _P, C.c_float, _u64p, _u64p, _u32p, _u32p, _u64p]),
+        "colo_stage_neighbors": (C.c_int, [_P, _P, C.c_float, _u64p, _u32p, _u64p]),
+        "colo_stage_filter": (C.c_int, [_P, _P, C.c_float, C.c_float, _u32p, C.c_uint64, C.c_uint32, _u64p, _u8p]),
+        "colo_stage_sqdist": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, _f32p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHED, max_size: int = 0,
+                   keep_tables: bool = False) -> Params:
+    p = Params()
+    load().colo_params_default(C.byref(p))
+    p.distance = distance
+    p.pi_threshold = pi_threshold
+    p.mode = mode
+    p.max_size = max_size
+    p.keep_tables = 1 if keep_tables else 0
+    return p
+
+
+def read_params(path: str) -> Params:
+    """LoadParameter (colocationFinder.cpp:57-74)."""
+    p = Params()
+    lib = load()
+    lib.colo_params_default(C.byref(p))
+    st = lib.colo_read_params(str(path).encode(), C.byref(p))
+    if st != OK:
+        raise ColoError(st, str(path))
+    return p
+
+
+def read_config(path: str) -> List[str]:
+    """Begin's five-line config file (colocationFinder.cpp:1077-1092)."""
+    bufs = [C.create_string_buffer(4096) for _ in range(5)]
+    st = load().colo_read_config(str(path).encode(), *bufs, 4096)
+    if st != OK:
+        raise ColoError(st, str(path))
+    return [b.value.decode() for b in bufs]
+
+
+@dataclass
+class Level:
+    k: int
+    cand: np.ndarray        # (C, k) feature indices
+    ub: np.ndarray          # (C, k) filter upper bounds
+    passed: np.ndarray      # (C,) filter verdict
+    rows: np.ndarray        # (C,) instance-table rows
+    num: np.ndarray         # (C, k) participation numerators
+    pi: np.ndarray          # (C,) float PI (-1: not refined)
+    prevalent: np.ndarray   # (C,)
+    argmin: np.ndarray      # (C,)
+    tables: dict = field(default_factory=dict)
+
+    def patterns(self):
+        return [tuple(int(v) for v in self.cand[c]) for c in np.nonzero(self.prevalent)[0]]
+
+
+class Result:
+    def __init__(self, lib, handle):
+        self._lib = lib
+        self.h = handle
+        self.levels: List[Level] = []
+        for li in range(lib.colo_result_num_levels(handle)):
+            k = lib.colo_result_level_size(handle, li)
+            n = lib.colo_result_level_candidates(handle, li)
+            cand = np.zeros((n, k), np.uint32)
+            ub = np.zeros((n, k), np.uint64)
+            pas = np.zeros(n, np.uint8)
+            rows = np.zeros(n, np.uint64)
+            num = np.zeros((n, k), np.uint64)
+            pi = np.zeros(n, np.float32)
+            prev = np.zeros(n, np.uint8)
+            am = np.zeros(n, np.uint32)
+            lib.colo_result_level(handle, li, _ptr(cand, _u32p), _ptr(ub, _u64p), _ptr(pas, _u8p), _ptr(rows, _u64p),
+                                  _ptr(num, _u64p), _ptr(pi, _f32p), _ptr(prev, _u8p), _ptr(am, _u32p))
+            lev = Level(k, cand, ub, pas, rows, num, pi, prev, am)
+            for c in range(n):
+                r = lib.colo_result_table(handle, li, c, None)
+                if r != 2 ** 64 - 1:
+                    t = np.zeros((r, k), np.uint32)
+                    lib.colo_result_table(handle, li, c, _ptr(t, _u32p))
+                    lev.tables[c] = t
+            self.levels.append(lev)
+        t = (C.c_double * 8)()
+        lib.colo_result_times(handle, t)
+        self.times = dict(zip(["total", "upload", "bucket", "join", "filter", "refine", "fill", "apriori"], list(t)))
+        c = np.zeros(8, np.uint64)
+        lib.colo_result_counters(handle, _ptr(c, _u64p))
+        self.counters = dict(zip(["launches", "npl_points", "neighbors", "rows_written", "fallbacks"], c[:5].tolist()))
+
+    def patterns(self):
+        out = []
+        for lev in self.levels:
+            out.extend(lev.patterns())
+        return out
+
+    def num_candidates(self) -> int:
+        return int(sum(len(l.cand) for l in self.levels))
+
+    def write_patterns(self, ds: "Dataset", location: str):
+        st = self._lib.colo_result_write_patterns(self.h, ds.h, str(location).encode())
+        if st != OK:
+            raise ColoError(st, location)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._lib.colo_result_free(self.h)
+            self.h = None
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = _P()
+        st = self.lib.colo_create(C.byref(h), device)
+        if st != OK:
+            raise ColoError(st, "colo_create")
+        self.h = h
+
+    def error(self) -> str:
+        return self.lib.colo_last_error(self.h).decode()
+
+    def check(self, st: int, what: str):
+        if st != OK:
+            raise ColoError(st, f"{what}: {self.error()}")
+
+    def dataset(self, x, y, fid, bounds) -> "Dataset":
+        return Dataset.from_arrays(self, x, y, fid, bounds)
+
+    def mine(self, ds: "Dataset", params: Params) -> Result:
+        out = _P()
+        self.check(self.lib.colo_mine(self.h, ds.h, C.byref(params), C.byref(out)), "colo_mine")
+        return Result(self.lib, out)
+
+    def mine_batch(self, dss: Sequence["Dataset"], params: Sequence[Params]) -> List[Result]:
+        n = len(dss)
+        hs = (_P * n)(*[d.h for d in dss])
+        ps = (Params * n)(*params)
+        outs = (_P * n)()
+        self.check(self.lib.colo_mine_batch(self.h, hs, ps, n, outs), "colo_mine_batch")
+        return [Result(self.lib, outs[i]) for i in range(n)]
+
+    def stage_neighbors(self, ds: "Dataset", R: float):
+        tot = C.c_uint64(0)
+        self.check(self.lib.colo_stage_neighbors(self.h, ds.h, R, None, None, C.byref(tot)), "stage_neighbors")
+        offs = np.zeros(ds.n + 1, np.uint64)
+        nbr = np.zeros(max(int(tot.value), 1), np.uint32)
+        tot2 = C.c_uint64(len(nbr))
+        self.check(self.lib.colo_stage_neighbors(self.h, ds.h, R, _ptr(offs, _u64p), _ptr(nbr, _u32p),
+                                                 C.byref(tot2)), "stage_neighbors")
+        return offs, nbr[: int(tot2.value)]
+
+    def stage_cells(self, ds: "Dataset", R: float):
+        nr = C.c_uint64(0)
+        self.check(self.lib.colo_stage_cells(self.h, ds.h, R, None, None, None, None, C.byref(nr)), "stage_cells")
+        cell = np.zeros(ds.n, np.uint64)
+        rc = np.zeros(max(nr.value, 1), np.uint64)
+        rf = np.zeros(max(nr.value, 1), np.uint32)
+        rn = np.zeros(max(nr.value, 1), np.uint32)
+        nr2 = C.c_uint64(len(rc))
+        self.check(self.lib.colo_stage_cells(self.h, ds.h, R, _ptr(cell, _u64p), _ptr(rc, _u64p), _ptr(rf, _u32p),
+                                             _ptr(rn, _u32p), C.byref(nr2)), "stage_cells")
+        n = int(nr2.value)
+        return cell, rc[:n], rf[:n], rn[:n]
+
+    def stage_filter(self, ds: "Dataset", R: float, thr: float, cand: np.ndarray):
+        cand = np.ascontiguousarray(cand, np.uint32)
+        n, k = cand.shape
+        ub = np.zeros((n, k), np.uint64)
+        pas = np.zeros(n, np.uint8)
+        self.check(self.lib.colo_stage_filter(self.h, ds.h, R, thr, _ptr(cand, _u32p), n, k, _ptr(ub, _u64p),
+                                              _ptr(pas, _u8p)), "stage_filter")
+        return ub, pas
+
+    def stage_sqdist(self, x1, y1, x2, y2) -> np.ndarray:
+        a = [np.ascontiguousarray(v, np.float32) for v in (x1, y1, x2, y2)]
+        out = np.zeros(len(a[0]), np.float32)
+        self.check(self.lib.colo_stage_sqdist(self.h, *[_ptr(v, _f32p) for v in a], len(out), _ptr(out, _f32p)),
+                   "stage_sqdist")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.colo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Dataset:
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.h = handle
+        self.n = int(ctx.lib.colo_dataset_num_points(handle))
+        self.nfeat = int(ctx.lib.colo_dataset_num_features(handle))
+
+    @classmethod
+    def from_csv(cls, ctx: Context, path: str) -> "Dataset":
+        h = _P()
+        ctx.check(ctx.lib.colo_dataset_from_csv(ctx.h, str(path).encode(), C.byref(h)), "dataset_from_csv")
+        return cls(ctx, h)
+
+    @classmethod
+    def from_arrays(cls, ctx: Context, x, y, fid, bounds) -> "Dataset":
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        fid = np.ascontiguousarray(fid, np.int32)
+        b = np.ascontiguousarray(bounds, np.float32)
+        h = _P()
+        ctx.check(ctx.lib.colo_dataset_from_host(ctx.h, _ptr(x, _f32p), _ptr(y, _f32p), _ptr(fid, _i32p), len(x),
+                                                 _ptr(b, _f32p), C.byref(h)), "dataset_from_host")
+        return cls(ctx, h)
+
+    def names(self) -> List[str]:
+        return [self.ctx.lib.colo_dataset_feature_name(self.h, f).decode() for f in range(self.nfeat)]
+
+    def upload(self):
+        self.ctx.check(self.ctx.lib.colo_dataset_upload(self.h), "dataset_upload")
+
+    def evict(self):
+        self.ctx.lib.colo_dataset_evict(self.h)
+
+    def write_csv(self, path: str):
+        self.ctx.check(self.ctx.lib.colo_dataset_write_csv(self.h, str(path).encode()), "dataset_write_csv")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.colo_dataset_free(self.h)
+            self.h = None

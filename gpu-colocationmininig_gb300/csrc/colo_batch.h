@@ -1,0 +1,122 @@
+// colo_batch.h -- device state of one mining batch and the stage launchers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "colo_internal.h"
+
+namespace colo {
+
+// Host description of one job inside a batch.
+struct JobHost {
+    JobGrid grid;
+    uint64_t p0 = 0, np = 0;     // point range
+};
+
+struct Batch {
+    cudaStream_t s = 0;
+    int sms = 148;
+    // sizes
+    uint64_t N = 0;              // points
+    uint32_t F = 0;              // features (global)
+    uint32_t J = 0;              // jobs
+    uint32_t W = 1;              // mask words per cell (max local feature count / 32)
+    uint32_t Fmax_local = 0;
+    uint64_t M = 0;              // occupied cells
+    uint64_t Rn = 0;             // (cell, feature) runs
+    uint64_t key_bits = 1;
+    // host copies of small arrays
+    std::vector<JobHost> jobs;
+    std::vector<uint32_t> h_fstart, h_fcount, h_fjob, h_frun_off;
+    // points (by id)
+    const float* x = nullptr;    // borrowed (dataset device copy)
+    const float* y = nullptr;
+    const uint32_t* feat = nullptr;
+    DevBuf<uint32_t> fstart, fcount, fjob;
+    DevBuf<JobGrid> grids;
+    DevBuf<DevFlags> flags;
+    // bucketed (sorted by cell key, then id)
+    DevBuf<uint32_t> sid, sfeat, scell;
+    DevBuf<float> sx, sy;
+    // cells
+    DevBuf<uint64_t> ckey;
+    DevBuf<uint32_t> cstart, crun, cjob;
+    DevBuf<int32_t> nb9;
+    DevBuf<uint32_t> cmask;
+    // runs
+    DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
+    DevBuf<uint32_t> frun_off, frun;
+    // neighbourhood lists
+    DevBuf<uint64_t> nrl_off, npl_off;
+    DevBuf<uint32_t> nrl_feat;
+    DevBuf<uint64_t> nrl_pos;
+    DevBuf<uint32_t> npl_id;
+    DevBuf<float> npl_x, npl_y;
+    uint64_t nrl_total = 0, npl_total = 0;
+    // neighbour CSR
+    DevBuf<uint64_t> nb_off;
+    DevBuf<uint32_t> nb;
+    uint64_t E = 0;
+    uint64_t join_pairs = 0;     // pair distance evaluations in the join (count pass)
+    int join_group = 8;          // lanes per anchor in the join (autotuned)
+};
+
+// colo_bucket.cu
+void bucket_points(Batch& b);            // cells, runs, masks, nb9, frun
+void build_neighborhoods(Batch& b);      // NRL / NPL
+// colo_join.cu
+void join_neighbors(Batch& b);           // neighbour CSR
+// colo_filter.cu
+// Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
+// bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.
+void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_off);
+// Level-k upper bounds for candidates cand[c*k + j] (global features):
+// ub[c*k + j].  driver[c] is the member whose runs drive the enumeration.
+void filter_level(Batch& b, const uint32_t* d_cand, const uint32_t* d_driver,
+                  const uint64_t* d_item_off, uint64_t ncand, uint64_t nitems, uint32_t k,
+                  uint32_t* d_ub);
+
+// colo_level.cu --------------------------------------------------------------
+// One candidate's view for the level kernels.
+struct CandDesc {
+    const uint32_t* parent;      // column-major parent table (k-1 columns); nullptr: implicit (k=2)
+    uint64_t prow;               // parent rows (k=2: anchors of member 0)
+    uint64_t pstride;            // parent column stride (>= prow)
+    uint32_t m[kMaxK];           // member features
+    uint32_t* slots;             // per parent row counts (count pass output)
+    const uint64_t* offs;        // per parent row output offsets (fill pass input)
+    uint32_t* out;               // column-major output table (k columns, rows = total)
+    uint64_t out_rows;           // rows of the output table (column stride)
+    uint64_t out_cap;            // capacity (single-pass mode)
+    unsigned long long* cursor;  // single-pass mode: rows reserved so far
+    unsigned long long* rows;    // count pass: rows of this candidate (atomic sum)
+    uint32_t* bitmap;            // member bitmaps, word offsets in bm_off
+    uint64_t bm_off[kMaxK + 1];
+    uint32_t job;
+    uint32_t k;
+};
+
+struct LevelWork {
+    const CandDesc* cands;       // device array
+    const uint64_t* chunk_off;   // device: prefix of 32-row chunks per candidate (ncand+1)
+    uint64_t ncand;
+    uint64_t nchunks;
+    unsigned long long* next;    // device work counter (persistent kernels)
+};
+
+// count pass: slots + bitmaps; fill pass: rows; single pass: rows at
+// reserved positions + slots + bitmaps (overflow recorded per candidate).
+void level_count(Batch& b, const LevelWork& w, uint32_t k, bool persistent);
+void level_fill(Batch& b, const LevelWork& w, uint32_t k, bool persistent);
+void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow);
+// Participation statistics per candidate and member: [A, last, first, full]
+// (A = set bits in [0, n-2]).
+void level_pi(Batch& b, const CandDesc* d_cands, uint64_t ncand, uint32_t k, uint64_t* d_stats);
+
+// Squared-distance evaluation of the reference expression for n pairs.
+void eval_sqdist(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,
+                 float* out, cudaStream_t s);
+
+}  // namespace colo

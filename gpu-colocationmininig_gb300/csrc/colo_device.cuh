@@ -1,0 +1,57 @@
+// colo_device.cuh -- device helpers shared by the kernels of libcolo.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "colo_internal.h"
+
+namespace colo {
+
+// Squared distance with the reference's own expression
+// (Codes/Utility_Inline.h:25-33: x1,y1 = first instance, x2,y2 = second).
+// The text is kept alike on purpose: the neighbour relation must be
+// bit-identical, and the device pow(float, int) it calls is CUDA's.
+__device__ __forceinline__ float ref_sqdist(float x1, float y1, float x2, float y2) {
+    float squareDistance = pow((x2 - x1), 2) + pow((y2 - y1), 2);
+    return squareDistance;
+}
+
+// Cell of a point (Codes/DeviceProcess_Kernel.h:615-625): float subtract,
+// float divide, float->u32 conversion (saturating on the device).
+__device__ __forceinline__ uint64_t ref_cell(const JobGrid& g, float x, float y) {
+    float rx = x - g.min_x;
+    float ry = y - g.min_y;
+    rx /= g.w;
+    ry /= g.w;
+    uint32_t i = (uint32_t)rx;
+    uint32_t j = (uint32_t)ry;
+    uint64_t c = (uint64_t)g.gx * j + i;
+    if (g.compat32) c = (uint32_t)c;
+    return c;
+}
+
+// The reference's neighbour-cell rule (Codes/Utility_Inline.h:35-53 with the
+// stencil loops): an in-range geometric neighbour (nx, ny) of cell column cx
+// is visited unless the column-wrap tests drop it.  Out-of-range neighbours
+// are never visited.
+__device__ __forceinline__ bool ref_adjacent_col(uint32_t cx, uint32_t nx, uint32_t gx) {
+    if (cx == 0) return nx != gx - 1;
+    if (cx == gx - 1) return nx != 0;
+    return true;
+}
+
+template <class T>
+__device__ __forceinline__ uint64_t lower_bound_dev(const T* a, uint64_t lo, uint64_t hi, T v) {
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+}  // namespace colo

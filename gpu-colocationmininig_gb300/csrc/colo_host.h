@@ -1,0 +1,94 @@
+// colo_host.h -- host-side structures of libcolo (datasets, results, I/O).
+#pragma once
+#include <stdint.h>
+
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "colo.h"
+#include "colo_internal.h"
+
+namespace colo {
+
+// Points as read from a CSV or given by the caller (raw feature ids).
+struct HostPoints {
+    std::vector<float> x, y;
+    std::vector<int32_t> raw;
+    std::vector<std::string> first_token;   // the id token as written (names)
+    float bounds[4] = {0, 0, 0, 0};
+    void clear() {
+        x.clear();
+        y.clear();
+        raw.clear();
+        first_token.clear();
+    }
+};
+
+// Per-level trace of one job (features are global batch indices; f0 is the
+// job's first feature so cand - f0 is the feature index inside the job).
+struct LevelTrace {
+    uint32_t k = 0;
+    uint32_t f0 = 0;
+    std::vector<uint32_t> cand;
+    std::vector<uint64_t> ub, num, rows;
+    std::vector<uint8_t> pass, prevalent;
+    std::vector<float> pi;
+    std::vector<uint32_t> argmin;
+    std::vector<std::vector<uint32_t>> tables;   // row-major, kept on request
+    std::vector<uint8_t> has_table;
+};
+
+struct MineResult {
+    std::vector<LevelTrace> levels;
+    double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint64_t counters[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+struct BatchStorage;   // owned device copies for multi-job batches
+
+colo_status read_params_file(const char* path, colo_params* p, std::string& err);
+colo_status read_config_file(const char* path, std::string out[5], std::string& err);
+colo_status parse_points_csv(const char* path, HostPoints& hp, std::string& err);
+colo_status write_points_csv(const HostPoints& hp, const std::vector<std::string>& names,
+                             const std::vector<uint32_t>& feat, const char* path, std::string& err);
+colo_status write_patterns(const MineResult& r, const std::vector<std::string>& names,
+                           const char* location, std::string& err);
+
+}  // namespace colo
+
+// ---------------------------------------------------------------------------
+// Opaque C-ABI objects
+// ---------------------------------------------------------------------------
+struct colo_ctx {
+    int device = 0;
+    cudaStream_t s = nullptr;
+    int sms = 0;
+    std::string err;
+};
+
+struct colo_dataset {
+    colo_ctx* ctx = nullptr;
+    colo::HostPoints hp;
+    std::vector<uint32_t> feat;              // feature index per point
+    std::vector<std::string> names;
+    std::vector<uint32_t> fstart, fcount;
+    colo::DevBuf<float> dx, dy;
+    colo::DevBuf<uint32_t> dfeat;
+    bool resident = false;
+};
+
+struct colo_result {
+    colo::MineResult r;
+};
+
+namespace colo {
+struct Batch;
+colo_status set_err(colo_ctx* ctx, colo_status st, const std::string& msg);
+colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn);
+void upload_dataset(colo_dataset* ds, cudaStream_t s);
+// Points, features, job grids and the bucketed/joined device state of a batch.
+// `own` keeps the concatenated device copies of multi-job batches alive.
+void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J, Batch& b,
+                 std::vector<DevBuf<float>>& ownf, std::vector<DevBuf<uint32_t>>& ownu, double* t_upload);
+}  // namespace colo

@@ -1,0 +1,137 @@
+// colo_internal.h -- shared types of libcolo (device layout, launch helpers).
+//
+// Device layout of one mining batch (one or more independent jobs):
+//   points      x[N], y[N] f32, feat[N] u32 (global feature index; features of
+//               a job are contiguous and a job's points are contiguous)
+//   features    fstart[F], fcount[F], fjob[F]
+//   jobs        JobGrid[J] (the reference grid of each job, R^2, threshold)
+//   bucketed    points sorted by (job cell key, point id): sid/sx/sy/sfeat/scell
+//   cells       occupied cells ckey[M], cstart[M+1] (sorted positions),
+//               crun[M+1] (run ranges), nb9[M*9] (geometric 3x3 neighbours),
+//               cmask[M*W] (feature bit masks, local feature index)
+//   runs        (cell, feature) runs rfeat/rstart/rcnt/rcell[Rn], feature-major
+//               index frun_off[F+1]/frun[Rn]
+//   NPL         per cell, the points of its adjacent cells ordered by
+//               (feature, cell, id): npl_off[M+1], npl_id/npl_x/npl_y
+//   NRL         per cell, the runs behind its NPL: nrl_off[M+1], nrl_feat,
+//               nrl_pos (NPL offset of each run)
+//   neighbours  CSR N+(a) indexed by point id: nb_off[N+1] (u64), nb[E]
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "colo.h"
+
+namespace colo {
+
+constexpr int kMaxK = 32;          // largest pattern size handled by the level kernels
+constexpr int kMaxMembersFiltered = 8;  // filter counts members j < 8 (block (8,2,2) in the reference)
+
+struct JobGrid {
+    float min_x, min_y, w;       // grid origin and cell width (= R)
+    float R2;                    // R*R in float
+    float thr;                   // PI threshold
+    uint32_t gx, gy;
+    uint64_t total;              // gx*gy
+    uint64_t key_base;           // first cell key of this job in the batch
+    int32_t compat32;            // 32-bit reference cell arithmetic is exact
+    uint32_t f0, nf;             // global feature range of the job
+    uint32_t pad;
+};
+
+// Error carrier for kernels: bounded waits and range checks record here.
+struct DevFlags {
+    uint32_t out_of_grid;        // points whose cell is outside [0, total)
+    uint32_t overflow;           // capacity overflows (learned presize)
+    uint32_t timeout;            // a bounded wait gave up
+    uint32_t internal;           // consistency checks
+};
+
+__host__ __device__ inline uint32_t ceil_div_u32(uint64_t a, uint64_t b) {
+    return (uint32_t)((a + b - 1) / b);
+}
+
+// ---------------------------------------------------------------------------
+// Host-side helpers
+// ---------------------------------------------------------------------------
+
+struct CudaError {
+    cudaError_t err;
+    std::string where;
+};
+
+#define COLO_CUDA(call)                                                          \
+    do {                                                                         \
+        cudaError_t e__ = (call);                                                \
+        if (e__ != cudaSuccess) throw ::colo::CudaError{e__, std::string(#call) + " @ " + __FILE__ + ":" + std::to_string(__LINE__)}; \
+    } while (0)
+
+#define COLO_LAUNCH_CHECK()                                                      \
+    do {                                                                         \
+        cudaError_t e__ = cudaGetLastError();                                    \
+        if (e__ != cudaSuccess) throw ::colo::CudaError{e__, std::string("kernel launch @ ") + __FILE__ + ":" + std::to_string(__LINE__)}; \
+    } while (0)
+
+struct StatusError {
+    colo_status st;
+    std::string msg;
+};
+
+// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept { swap(o); }
+    DevBuf& operator=(DevBuf&& o) noexcept { release(); swap(o); return *this; }
+    ~DevBuf() { release(); }
+    void swap(DevBuf& o) { std::swap(p, o.p); std::swap(n, o.n); std::swap(s, o.s); }
+    void alloc(size_t count, cudaStream_t st) {
+        release();
+        s = st;
+        n = count;
+        if (count == 0) return;
+        cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), st);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            n = 0;
+            cudaGetLastError();
+            throw StatusError{COLO_ERR_NOMEM, "device allocation of " + std::to_string(count * sizeof(T)) + " bytes failed"};
+        }
+    }
+    void zero(cudaStream_t st) {
+        if (n) COLO_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    T* get() const { return p; }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// Launch counter (kernels of this library launched by the current mine).
+extern thread_local uint64_t g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches += n; }
+
+// ---------------------------------------------------------------------------
+// Primitives (colo_prims.cu)
+// ---------------------------------------------------------------------------
+
+// out[i] = sum(in[0..i)) ; returns total (synchronises to read it back if total_host != nullptr).
+void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
+                     uint64_t* total_host);
+void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t s,
+                     uint32_t* total_host);
+// Stable LSD radix sort of (key, val) pairs by the low `bits` bits of key.
+// Results land back in keys/vals.
+void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s);
+
+}  // namespace colo

@@ -1,0 +1,311 @@
+// colo_level.cu -- level-wise instance tables and participation bitmaps.
+//
+// Reference semantics (generalInstanceTableSlotCounter_Kernel and
+// generateInstanceTableGeneral_Kernel, Codes/DeviceProcess_Kernel.h:255-385;
+// degree 2: 12-100): for a candidate (c_0..c_{k-1}) with parent table
+// T(c_0..c_{k-2}), row r extends by b when b is an instance of c_{k-1} in a
+// cell adjacent to r[0]'s cell with sq(r[i], b) <= R^2 for every i.  The
+// candidates b of r are exactly N+_{c_{k-1}}(r[0]), a contiguous slice of the
+// neighbour CSR (features ascend along each list), so the cell test and the
+// r[0] distance test are already done; rows check the other k-2 members.
+//
+// Work decomposition: a warp owns 32 parent rows.  Their slices are
+// flattened with a warp prefix sum and the warp walks the flattened items 32
+// at a time, so a row with 10^4 candidates and a row with none cost the same
+// per item (load-balanced expand).  Hits are compacted with one ballot per
+// step; output rows are written column-major (one coalesced stream per
+// column).  Participation bits are set with atomicOr on 32-bit words.
+#include "colo_batch.h"
+#include "colo_device.cuh"
+
+namespace colo {
+namespace {
+
+enum { MODE_COUNT = 0, MODE_FILL = 1, MODE_SINGLE = 2 };
+
+__device__ __forceinline__ void set_bit(uint32_t* words, uint32_t bit) {
+    atomicOr(&words[bit >> 5], 1u << (bit & 31));
+}
+
+// K = pattern size (2..8), or 0 for a runtime size read from the descriptor
+// (members kept in global memory, slower; only reached for k > 8).
+template <int K, int MODE>
+__global__ void __launch_bounds__(256) k_level(
+    const CandDesc* __restrict__ cands, const uint64_t* __restrict__ chunk_off, uint64_t ncand,
+    uint64_t nchunks, const uint64_t* __restrict__ nb_off, const uint32_t* __restrict__ nb,
+    const float* __restrict__ x, const float* __restrict__ y, const uint32_t* __restrict__ fstart,
+    const uint32_t* __restrict__ fcount, const JobGrid* __restrict__ grids,
+    uint32_t* __restrict__ overflow) {
+    constexpr int KR = (K == 0) ? 1 : K;   // register members kept for K > 0
+    const int lane = threadIdx.x & 31;
+    const uint64_t ch = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (ch >= nchunks) return;
+    // candidate of this chunk
+    uint64_t lo = 0, hi = ncand;
+    while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (chunk_off[mid] <= ch) lo = mid;
+        else hi = mid;
+    }
+    const CandDesc& d = cands[lo];
+    const uint32_t k = (K == 0) ? d.k : (uint32_t)K;
+    const uint64_t row = (ch - chunk_off[lo]) * 32 + lane;
+    const bool valid = row < d.prow;
+    const uint32_t flast = d.m[k - 1];
+    const uint32_t last_start = fstart[flast];
+    const uint32_t last_end = last_start + fcount[flast];
+    const float R2 = grids[d.job].R2;
+
+    // row members (ids) and coordinates of members 1..k-2
+    uint32_t rid[KR];
+    float rx[KR], ry[KR];
+#pragma unroll
+    for (int i = 0; i < KR; ++i) {
+        rid[i] = 0;
+        rx[i] = 0.f;
+        ry[i] = 0.f;
+    }
+    uint32_t a0 = 0;
+    uint64_t slo = 0, shi = 0;
+    if (valid) {
+        a0 = d.parent ? d.parent[row] : fstart[d.m[0]] + (uint32_t)row;
+        if (K > 0) {
+            rid[0] = a0;
+#pragma unroll
+            for (int i = 1; i < KR - 1; ++i) {
+                rid[i] = d.parent[(uint64_t)i * d.pstride + row];
+                rx[i] = x[rid[i]];
+                ry[i] = y[rid[i]];
+            }
+        }
+        uint64_t o0 = nb_off[a0], o1 = nb_off[a0 + 1];
+        slo = lower_bound_dev(nb, o0, o1, last_start);
+        shi = lower_bound_dev(nb, slo, o1, last_end);
+    }
+    // flatten the 32 slices
+    uint32_t len = (uint32_t)(shi - slo);
+    uint32_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const uint32_t excl = incl - len;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t mine = 0;               // hits of this lane's row so far
+    uint64_t out0 = 0;
+    if (MODE == MODE_FILL && valid) out0 = d.offs[row] - d.offs[0];   // offsets may be a slice of a longer scan
+    const uint32_t lt = (1u << lane) - 1u;
+    bool ovf = false;
+
+    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        const uint32_t item = t0 + lane;
+        const bool active = item < total;
+        // owner lane: last lane whose slice starts at or before item
+        int j = 0;
+#pragma unroll
+        for (int bstep = 16; bstep > 0; bstep >>= 1) {
+            uint32_t ev = __shfl_sync(0xffffffffu, excl, j + bstep);
+            if (ev <= item) j += bstep;
+        }
+        const uint32_t ex_j = __shfl_sync(0xffffffffu, excl, j);
+        const uint32_t in_j = __shfl_sync(0xffffffffu, incl, j);
+        const uint64_t lo_j = __shfl_sync(0xffffffffu, slo, j);
+        uint32_t b = 0;
+        bool ok = active;
+        if (active) b = nb[lo_j + (item - ex_j)];
+        if (K == 0) {
+            if (active && k > 2) {
+                const float xb = x[b], yb = y[b];
+                const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
+                for (uint32_t i = 1; i + 1 < k && ok; ++i) {
+                    uint32_t ri = d.parent[(uint64_t)i * d.pstride + prow_j];
+                    ok = ref_sqdist(x[ri], y[ri], xb, yb) <= R2;
+                }
+            }
+        } else if (K > 2) {
+            float xb = 0.f, yb = 0.f;
+            if (active) {
+                xb = x[b];
+                yb = y[b];
+            }
+#pragma unroll
+            for (int i = 1; i < KR - 1; ++i) {
+                float xi = __shfl_sync(0xffffffffu, rx[i], j);
+                float yi = __shfl_sync(0xffffffffu, ry[i], j);
+                ok = ok && ref_sqdist(xi, yi, xb, yb) <= R2;
+            }
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+        // lanes of this step that belong to my own row
+        int r0 = (int)excl - (int)t0, r1 = (int)incl - (int)t0;
+        r0 = r0 < 0 ? 0 : r0;
+        r1 = r1 > 32 ? 32 : r1;
+        uint32_t mymask = 0;
+        if (r1 > r0) mymask = (r1 - r0 == 32) ? 0xffffffffu : (((1u << (r1 - r0)) - 1u) << r0);
+        const uint32_t my_hits = __popc(bal & mymask);
+
+        if (MODE == MODE_COUNT || MODE == MODE_SINGLE) {
+            if (ok) set_bit(d.bitmap + d.bm_off[k - 1], b - last_start);
+        }
+        if (MODE == MODE_FILL) {
+            const uint32_t before_j = __shfl_sync(0xffffffffu, mine, j);
+            const uint64_t out_j = __shfl_sync(0xffffffffu, out0, j);
+            int q0 = (int)ex_j - (int)t0, q1 = (int)in_j - (int)t0;
+            q0 = q0 < 0 ? 0 : q0;
+            q1 = q1 > 32 ? 32 : q1;
+            uint32_t jmask = (q1 > q0) ? ((q1 - q0 == 32) ? 0xffffffffu : (((1u << (q1 - q0)) - 1u) << q0)) : 0u;
+            const uint64_t pos = out_j + before_j + __popc(bal & jmask & lt);
+            if (K > 0) {
+#pragma unroll
+                for (int i = 0; i < KR - 1; ++i) {
+                    uint32_t v = __shfl_sync(0xffffffffu, rid[i], j);
+                    if (ok) d.out[(uint64_t)i * d.out_rows + pos] = v;
+                }
+            } else if (ok) {
+                const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
+                d.out[pos] = d.parent ? d.parent[prow_j] : fstart[d.m[0]] + (uint32_t)prow_j;
+                for (uint32_t i = 1; i + 1 < k; ++i)
+                    d.out[(uint64_t)i * d.out_rows + pos] = d.parent[(uint64_t)i * d.pstride + prow_j];
+            }
+            if (ok) d.out[(uint64_t)(k - 1) * d.out_rows + pos] = b;
+        }
+        if (MODE == MODE_SINGLE) {
+            const uint32_t n_ok = __popc(bal);
+            unsigned long long base = 0;
+            if (lane == 0 && n_ok) base = atomicAdd(d.cursor, (unsigned long long)n_ok);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const uint64_t pos = base + __popc(bal & lt);
+            const bool room = pos < d.out_cap;
+            if (ok && !room) ovf = true;
+            if (K > 0) {
+#pragma unroll
+                for (int i = 0; i < KR - 1; ++i) {
+                    uint32_t v = __shfl_sync(0xffffffffu, rid[i], j);
+                    if (ok && room) d.out[(uint64_t)i * d.out_cap + pos] = v;
+                }
+            } else if (ok && room) {
+                const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
+                d.out[pos] = d.parent ? d.parent[prow_j] : fstart[d.m[0]] + (uint32_t)prow_j;
+                for (uint32_t i = 1; i + 1 < k; ++i)
+                    d.out[(uint64_t)i * d.out_cap + pos] = d.parent[(uint64_t)i * d.pstride + prow_j];
+            }
+            if (ok && room) d.out[(uint64_t)(k - 1) * d.out_cap + pos] = b;
+        }
+        mine += my_hits;
+    }
+    if (MODE == MODE_SINGLE) {
+        if (__any_sync(0xffffffffu, ovf) && lane == 0) atomicOr(&overflow[lo], 1u);
+    }
+    if (MODE == MODE_COUNT || MODE == MODE_SINGLE) {
+        const uint32_t wsum = __reduce_add_sync(0xffffffffu, mine);
+        if (lane == 0 && wsum) atomicAdd(d.rows, (unsigned long long)wsum);
+    }
+    if ((MODE == MODE_COUNT || MODE == MODE_SINGLE) && valid) {
+        d.slots[row] = mine;
+        if (mine) {
+            set_bit(d.bitmap + d.bm_off[0], a0 - fstart[d.m[0]]);
+            if (K > 0) {
+#pragma unroll
+                for (int q = 1; q < KR - 1; ++q) set_bit(d.bitmap + d.bm_off[q], rid[q] - fstart[d.m[q]]);
+            } else {
+                for (uint32_t i = 1; i + 1 < k; ++i) {
+                    uint32_t ri = d.parent[(uint64_t)i * d.pstride + row];
+                    set_bit(d.bitmap + d.bm_off[i], ri - fstart[d.m[i]]);
+                }
+            }
+        }
+    }
+}
+
+// Participation statistics: per (candidate, member) [A, last, first, full]
+// where A counts set bits in [0, n-2] (the window getParticipationIndex sums,
+// Codes/DeviceProcess.cu:108-132).
+__global__ void k_level_pi(const CandDesc* __restrict__ cands, uint64_t ncand, uint32_t k,
+                           const uint32_t* __restrict__ fcount, uint64_t* __restrict__ stats) {
+    const uint64_t c = blockIdx.x;
+    if (c >= ncand) return;
+    const CandDesc& d = cands[c];
+    __shared__ unsigned long long red[32];
+    for (uint32_t j = 0; j < k; ++j) {
+        const uint32_t n = fcount[d.m[j]];
+        const uint32_t* w = d.bitmap + d.bm_off[j];
+        const uint32_t nw = (n + 31) / 32;
+        unsigned long long cntA = 0, cntFull = 0;
+        for (uint32_t i = threadIdx.x; i < nw; i += blockDim.x) {
+            uint32_t v = w[i];
+            cntFull += __popc(v);
+            // bits [0, n-2]
+            uint32_t lim = n - 1;   // number of bits in the window
+            uint32_t wb = i * 32;
+            uint32_t mask;
+            if (wb + 32 <= lim) mask = 0xffffffffu;
+            else if (wb >= lim) mask = 0u;
+            else mask = (1u << (lim - wb)) - 1u;
+            cntA += __popc(v & mask);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            cntA += __shfl_down_sync(0xffffffffu, cntA, o);
+            cntFull += __shfl_down_sync(0xffffffffu, cntFull, o);
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) red[wid] = cntA | (cntFull << 32);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long A = 0, Fu = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                A += red[q] & 0xffffffffull;
+                Fu += red[q] >> 32;
+            }
+            uint32_t last = (w[(n - 1) >> 5] >> ((n - 1) & 31)) & 1u;
+            uint32_t first = w[0] & 1u;
+            uint64_t* o = stats + (c * k + j) * 4;
+            o[0] = A;
+            o[1] = last;
+            o[2] = first;
+            o[3] = Fu;
+        }
+        __syncthreads();
+    }
+}
+
+template <int MODE>
+void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
+    if (w.nchunks == 0) return;
+    uint64_t threads = w.nchunks * 32;
+    unsigned grid = (unsigned)((threads + 255) / 256);
+#define COLO_LVL(KK)                                                                              \
+    k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_off.get(), \
+                                            b.nb.get(), b.x, b.y, b.fstart.get(), b.fcount.get(),  \
+                                            b.grids.get(), ovf)
+    switch (k) {
+        case 2: COLO_LVL(2); break;
+        case 3: COLO_LVL(3); break;
+        case 4: COLO_LVL(4); break;
+        case 5: COLO_LVL(5); break;
+        case 6: COLO_LVL(6); break;
+        case 7: COLO_LVL(7); break;
+        case 8: COLO_LVL(8); break;
+        default: COLO_LVL(0); break;
+    }
+#undef COLO_LVL
+    COLO_LAUNCH_CHECK();
+    count_launch();
+}
+
+}  // namespace
+
+void level_count(Batch& b, const LevelWork& w, uint32_t k, bool) { launch_level<MODE_COUNT>(b, w, k, nullptr); }
+void level_fill(Batch& b, const LevelWork& w, uint32_t k, bool) { launch_level<MODE_FILL>(b, w, k, nullptr); }
+void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow) {
+    launch_level<MODE_SINGLE>(b, w, k, d_overflow);
+}
+
+void level_pi(Batch& b, const CandDesc* d_cands, uint64_t ncand, uint32_t k, uint64_t* d_stats) {
+    if (ncand == 0) return;
+    k_level_pi<<<(unsigned)ncand, 256, 0, b.s>>>(d_cands, ncand, k, b.fcount.get(), d_stats);
+    COLO_LAUNCH_CHECK();
+    count_launch();
+}
+
+}  // namespace colo

@@ -1,0 +1,943 @@
+// colo_mine.cpp -- the C ABI and the level loop (host orchestration).
+//
+// The level loop follows Begin (colocationFinder.cpp:1068-1147): degree 2
+// (degree2Processing, 256-425), then per level the filter, refinement with
+// participation index (generatePrevalentPatternsGeneral, 736-854), Apriori
+// candidate generation (candidateColocationGeneral, 517-557) and instance
+// tables for the prevalent patterns that prefix a next-level candidate
+// (calcInstanceTablePatternIndexes + generateInstanceTableGeneral, 1042-1066,
+// 856-909).  Instance tables stay in device memory between levels.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "colo_batch.h"
+#include "colo_host.h"
+
+using namespace colo;
+
+namespace colo {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+inline double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+template <class Fn>
+colo_status guarded(colo_ctx* ctx, Fn&& fn) {
+    return run_guarded(ctx, std::function<colo_status()>(fn));
+}
+
+// Feature grouping of populateData (colocationFinder.cpp:168-229): a change of
+// raw id starts a new feature, named by the id token as written.
+void group_features(colo_dataset* ds) {
+    const HostPoints& hp = ds->hp;
+    size_t n = hp.x.size();
+    ds->feat.resize(n);
+    ds->names.clear();
+    ds->fstart.clear();
+    ds->fcount.clear();
+    for (size_t i = 0; i < n; ++i) {
+        if (i == 0 || hp.raw[i] != hp.raw[i - 1]) {
+            ds->names.push_back(hp.first_token.empty() ? std::to_string(hp.raw[i]) : hp.first_token[i]);
+            ds->fstart.push_back((uint32_t)i);
+            ds->fcount.push_back(0);
+        }
+        ds->feat[i] = (uint32_t)(ds->names.size() - 1);
+        ds->fcount.back()++;
+    }
+}
+
+// setGrid (colocationFinder.cpp:102-126).
+JobGrid make_grid(const float bounds[4], float R, float thr) {
+    JobGrid g{};
+    g.min_x = bounds[0];
+    g.min_y = bounds[1];
+    float maxX = bounds[2];
+    float maxYe = bounds[3] + R;
+    g.w = R;
+    float gsx = (maxX - g.min_x) / g.w;
+    float gsy = (maxYe - g.min_y) / g.w;
+    if (!(R > 0.0f) || !std::isfinite(R) || !std::isfinite(gsx) || !std::isfinite(gsy))
+        throw StatusError{COLO_ERR_INPUT, "grid: distance and bounds must be finite with R > 0"};
+    float cx = std::ceil(gsx), cy = std::ceil(gsy);
+    if (!(cx >= 1.0f) || !(cy >= 1.0f) || cx >= 4294967296.0f || cy >= 4294967296.0f)
+        throw StatusError{COLO_ERR_INPUT, "grid: the bounds line gives an empty or oversized grid"};
+    g.gx = (uint32_t)cx;
+    g.gy = (uint32_t)cy;
+    g.total = (uint64_t)g.gx * g.gy;
+    g.compat32 = (g.total + g.gx) < (1ull << 31) ? 1 : 0;
+    g.R2 = R * R;
+    g.thr = thr;
+    return g;
+}
+
+}  // namespace
+
+colo_status set_err(colo_ctx* ctx, colo_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+
+colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn) {
+    try {
+        return fn();
+    } catch (const StatusError& e) {
+        return set_err(ctx, e.st, e.msg);
+    } catch (const CudaError& e) {
+        cudaGetLastError();
+        return set_err(ctx, COLO_ERR_CUDA, std::string(cudaGetErrorString(e.err)) + " in " + e.where);
+    } catch (const std::bad_alloc&) {
+        return set_err(ctx, COLO_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return set_err(ctx, COLO_ERR_INTERNAL, e.what());
+    }
+}
+
+void upload_dataset(colo_dataset* ds, cudaStream_t s) {
+    if (ds->resident) return;
+    uint64_t n = ds->hp.x.size();
+    ds->dx.alloc(n, s);
+    ds->dy.alloc(n, s);
+    ds->dfeat.alloc(n, s);
+    if (n) {
+        COLO_CUDA(cudaMemcpyAsync(ds->dx.get(), ds->hp.x.data(), n * 4, cudaMemcpyHostToDevice, s));
+        COLO_CUDA(cudaMemcpyAsync(ds->dy.get(), ds->hp.y.data(), n * 4, cudaMemcpyHostToDevice, s));
+        COLO_CUDA(cudaMemcpyAsync(ds->dfeat.get(), ds->feat.data(), n * 4, cudaMemcpyHostToDevice, s));
+    }
+    COLO_CUDA(cudaStreamSynchronize(s));
+    ds->resident = true;
+}
+
+namespace {
+
+struct PatternHash {
+    size_t operator()(const std::vector<uint32_t>& v) const {
+        uint64_t h = 1469598103934665603ull;
+        for (uint32_t x : v) h = (h ^ x) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
+struct TableRef {
+    uint32_t* cols = nullptr;   // column-major
+    uint64_t rows = 0;
+    uint64_t stride = 0;
+};
+
+struct JobState {
+    uint32_t f0 = 0, nf = 0;
+    float thr = 0;
+    uint32_t max_size = 0;
+    bool active = true;
+    std::vector<uint32_t> cands;     // this level's candidates (global features)
+    std::unordered_map<std::vector<uint32_t>, TableRef, PatternHash> tables;   // prefixes
+    MineResult* out = nullptr;
+};
+
+// Apriori join (candidateColocationGeneral, colocationFinder.cpp:517-557):
+// patterns i < j with equal (k-2)-prefix are joined; the remaining
+// (k-1)-subsets must all be prevalent (generateandCheckSubsets, 669-679);
+// a failing subset check ends the inner loop ("break", 541-542) and so does
+// a prefix mismatch (551-552).
+std::vector<uint32_t> apriori_next(const std::vector<uint32_t>& prev, uint32_t km1) {
+    std::vector<uint32_t> out;
+    size_t P = prev.size() / km1;
+    if (P < 2) return out;
+    std::unordered_set<std::vector<uint32_t>, PatternHash> have;
+    have.reserve(P * 2);
+    for (size_t i = 0; i < P; ++i) have.emplace(prev.begin() + i * km1, prev.begin() + (i + 1) * km1);
+    const uint32_t k = km1 + 1;
+    std::vector<uint32_t> cand(k), sub(km1);
+    for (size_t i = 0; i < P; ++i) {
+        const uint32_t* pi = &prev[i * km1];
+        for (size_t j = i + 1; j < P; ++j) {
+            const uint32_t* pj = &prev[j * km1];
+            bool same = true;
+            for (uint32_t t = 0; t + 1 < km1; ++t)
+                if (pi[t] != pj[t]) {
+                    same = false;
+                    break;
+                }
+            if (!same || !(pi[km1 - 1] < pj[km1 - 1])) break;
+            for (uint32_t t = 0; t < km1; ++t) cand[t] = pi[t];
+            cand[km1] = pj[km1 - 1];
+            // subsets dropping positions k-3 .. 0 (the two others are pi and pj)
+            bool ok = true;
+            for (int drop = (int)k - 3; drop >= 0 && ok; --drop) {
+                uint32_t q = 0;
+                for (uint32_t t = 0; t < k; ++t)
+                    if ((int)t != drop) sub[q++] = cand[t];
+                if (!have.count(sub)) ok = false;
+            }
+            if (!ok) break;
+            out.insert(out.end(), cand.begin(), cand.end());
+        }
+    }
+    return out;
+}
+
+// threshold_Kernel arithmetic (Codes/DeviceProcess_Kernel.h:545-573).
+bool filter_pass(const uint64_t* ub, const uint32_t* mem, uint32_t k, const std::vector<uint32_t>& fcount,
+                 float thr) {
+    float pi0 = 1.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        float pr = (float)((double)ub[j] / (double)(float)fcount[mem[j]]);
+        if (j == 0) pi0 = pr;
+        else if (pi0 > pr) pi0 = pr;
+    }
+    return pi0 >= thr;
+}
+
+struct LevelArena {
+    DevBuf<uint32_t> slots;
+    DevBuf<uint32_t> bitmap;
+    DevBuf<unsigned long long> rows;
+    DevBuf<CandDesc> descs;
+    DevBuf<uint64_t> chunk_off;
+    DevBuf<uint64_t> stats;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The mining driver for a batch of jobs.
+// ---------------------------------------------------------------------------
+void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J, Batch& b,
+                 std::vector<DevBuf<float>>& ownf, std::vector<DevBuf<uint32_t>>& ownu, double* t_upload) {
+    cudaStream_t s = ctx->s;
+    b.s = s;
+    b.sms = ctx->sms;
+    b.J = J;
+    auto t0 = Clock::now();
+    std::vector<uint32_t> job_f0(J + 1, 0);
+    uint64_t N = 0;
+    for (uint32_t j = 0; j < J; ++j) {
+        job_f0[j + 1] = job_f0[j] + (uint32_t)dsv[j]->names.size();
+        N += dsv[j]->hp.x.size();
+    }
+    if (N >= (1ull << 32) - 1) throw StatusError{COLO_ERR_CAPACITY, "at most 2^32-2 points per batch"};
+    b.N = N;
+    b.F = job_f0[J];
+    if (J == 1) {
+        upload_dataset(dsv[0], s);
+        b.x = dsv[0]->dx.get();
+        b.y = dsv[0]->dy.get();
+        b.feat = dsv[0]->dfeat.get();
+    } else {
+        ownf.resize(2);
+        ownu.resize(1);
+        ownf[0].alloc(N, s);
+        ownf[1].alloc(N, s);
+        ownu[0].alloc(N, s);
+        std::vector<uint32_t> tmp;
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < J; ++j) {
+            colo_dataset* ds = dsv[j];
+            uint64_t n = ds->hp.x.size();
+            if (!n) continue;
+            tmp.resize(n);
+            for (uint64_t i = 0; i < n; ++i) tmp[i] = ds->feat[i] + job_f0[j];
+            COLO_CUDA(cudaMemcpyAsync(ownf[0].get() + off, ds->hp.x.data(), n * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(ownf[1].get() + off, ds->hp.y.data(), n * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(ownu[0].get() + off, tmp.data(), n * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
+            off += n;
+        }
+        b.x = ownf[0].get();
+        b.y = ownf[1].get();
+        b.feat = ownu[0].get();
+    }
+    if (t_upload) *t_upload = ms_since(t0);
+    b.h_fstart.resize(b.F);
+    b.h_fcount.resize(b.F);
+    b.h_fjob.resize(b.F);
+    b.jobs.resize(J);
+    uint64_t key_base = 0, p0 = 0;
+    b.Fmax_local = 1;
+    for (uint32_t j = 0; j < J; ++j) {
+        colo_dataset* ds = dsv[j];
+        for (uint32_t f = 0; f < ds->names.size(); ++f) {
+            b.h_fstart[job_f0[j] + f] = (uint32_t)(p0 + ds->fstart[f]);
+            b.h_fcount[job_f0[j] + f] = ds->fcount[f];
+            b.h_fjob[job_f0[j] + f] = j;
+        }
+        JobGrid g = make_grid(ds->hp.bounds, pv[j].distance, pv[j].pi_threshold);
+        g.key_base = key_base;
+        g.f0 = job_f0[j];
+        g.nf = (uint32_t)ds->names.size();
+        key_base += g.total;
+        b.jobs[j].grid = g;
+        b.jobs[j].p0 = p0;
+        b.jobs[j].np = ds->hp.x.size();
+        p0 += ds->hp.x.size();
+        b.Fmax_local = std::max(b.Fmax_local, g.nf);
+    }
+    b.W = (b.Fmax_local + 31) / 32;
+    b.key_bits = 1;
+    while (b.key_bits < 64 && (1ull << b.key_bits) < key_base) b.key_bits++;
+    b.fstart.alloc(b.F ? b.F : 1, s);
+    b.fcount.alloc(b.F ? b.F : 1, s);
+    b.fjob.alloc(b.F ? b.F : 1, s);
+    b.grids.alloc(J, s);
+    b.flags.alloc(1, s);
+    b.flags.zero(s);
+    std::vector<JobGrid> hg(J);
+    for (uint32_t j = 0; j < J; ++j) hg[j] = b.jobs[j].grid;
+    if (b.F) {
+        COLO_CUDA(cudaMemcpyAsync(b.fstart.get(), b.h_fstart.data(), b.F * 4, cudaMemcpyHostToDevice, s));
+        COLO_CUDA(cudaMemcpyAsync(b.fcount.get(), b.h_fcount.data(), b.F * 4, cudaMemcpyHostToDevice, s));
+        COLO_CUDA(cudaMemcpyAsync(b.fjob.get(), b.h_fjob.data(), b.F * 4, cudaMemcpyHostToDevice, s));
+    }
+    COLO_CUDA(cudaMemcpyAsync(b.grids.get(), hg.data(), J * sizeof(JobGrid), cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaStreamSynchronize(s));
+}
+
+static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J,
+                      MineResult** outs) {
+    cudaStream_t s = ctx->s;
+    const auto t_all = Clock::now();
+    g_launches = 0;
+    Batch b;
+    const int mode = pv[0].mode;
+    const bool plain = (mode == COLO_MODE_PLAIN);
+    std::vector<DevBuf<float>> ownf;
+    std::vector<DevBuf<uint32_t>> ownu;
+    double t_upload = 0;
+    setup_batch(ctx, dsv, pv, J, b, ownf, ownu, &t_upload);
+    const uint64_t N = b.N;
+    std::vector<JobState> js(J);
+    for (uint32_t j = 0; j < J; ++j) {
+        const JobGrid& g = b.jobs[j].grid;
+        js[j].f0 = g.f0;
+        js[j].nf = g.nf;
+        js[j].thr = pv[j].pi_threshold;
+        js[j].max_size = pv[j].max_size;
+        js[j].out = outs[j];
+        js[j].active = g.nf >= 2 && b.jobs[j].np > 0;
+    }
+    auto t0 = Clock::now();
+
+    // ---- bucketing + join ---------------------------------------------------
+    if (N > 0) {
+        bucket_points(b);
+        build_neighborhoods(b);
+    }
+    double t_bucket = ms_since(t0);
+    t0 = Clock::now();
+    if (N > 0) join_neighbors(b);
+    COLO_CUDA(cudaStreamSynchronize(s));
+    double t_join = ms_since(t0);
+
+    double t_filter = 0, t_refine = 0, t_fill = 0, t_apriori = 0;
+    uint64_t rows_written = 0;
+
+    // ---- level loop -----------------------------------------------------------
+    for (uint32_t j = 0; j < J; ++j) {
+        if (!js[j].active) continue;
+        for (uint32_t a = 0; a + 1 < js[j].nf; ++a)          // colocationFinder.cpp:75-82
+            for (uint32_t c = a + 1; c < js[j].nf; ++c) {
+                js[j].cands.push_back(js[j].f0 + a);
+                js[j].cands.push_back(js[j].f0 + c);
+            }
+    }
+    std::unique_ptr<DevBuf<uint32_t>> tables_prev, tables_cur;
+    for (uint32_t k = 2;; ++k) {
+        bool any = false;
+        for (auto& st : js) any |= (st.active && !st.cands.empty());
+        if (!any) break;
+        // ---- filter ----
+        t0 = Clock::now();
+        std::vector<LevelTrace*> tr(J, nullptr);
+        for (uint32_t j = 0; j < J; ++j) {
+            if (!js[j].active || js[j].cands.empty()) continue;
+            js[j].out->levels.emplace_back();
+            LevelTrace& L = js[j].out->levels.back();
+            L.k = k;
+            L.f0 = js[j].f0;
+            L.cand = js[j].cands;
+            size_t C = L.cand.size() / k;
+            L.ub.assign(C * k, 0);
+            L.num.assign(C * k, 0);
+            L.rows.assign(C, 0);
+            L.pass.assign(C, 0);
+            L.prevalent.assign(C, 0);
+            L.pi.assign(C, -1.0f);
+            L.argmin.assign(C, 0);
+            L.has_table.assign(C, 0);
+            tr[j] = &L;
+        }
+        if (k == 2) {
+            DevBuf<uint32_t> ub2;
+            std::vector<uint64_t> job_off;
+            filter_pairs(b, ub2, job_off);
+            std::vector<uint32_t> h(job_off[J]);
+            if (!h.empty())
+                COLO_CUDA(cudaMemcpy(h.data(), ub2.get(), h.size() * 4, cudaMemcpyDeviceToHost));
+            for (uint32_t j = 0; j < J; ++j) {
+                if (!tr[j]) continue;
+                LevelTrace& L = *tr[j];
+                uint32_t nf = js[j].nf;
+                for (size_t c = 0; c < L.cand.size() / 2; ++c) {
+                    uint32_t l0 = L.cand[2 * c] - js[j].f0, l1 = L.cand[2 * c + 1] - js[j].f0;
+                    L.ub[2 * c] = h[job_off[j] + (uint64_t)l0 * nf + l1];
+                    L.ub[2 * c + 1] = h[job_off[j] + (uint64_t)l1 * nf + l0];
+                    L.pass[c] = filter_pass(&L.ub[2 * c], &L.cand[2 * c], 2, b.h_fcount, js[j].thr);
+                }
+            }
+        } else {
+            std::vector<uint32_t> hc, hdrv;
+            std::vector<uint64_t> hoff(1, 0);
+            std::vector<std::pair<uint32_t, size_t>> owner;
+            for (uint32_t j = 0; j < J; ++j) {
+                if (!tr[j]) continue;
+                const LevelTrace& L = *tr[j];
+                for (size_t c = 0; c < L.cand.size() / k; ++c) {
+                    const uint32_t* mem = &L.cand[c * k];
+                    uint32_t m = std::min<uint32_t>(k, kMaxMembersFiltered);
+                    uint32_t best = 0;
+                    uint32_t bestn = UINT32_MAX;
+                    for (uint32_t q = 0; q < m; ++q) {
+                        uint32_t nr = b.h_frun_off[mem[q] + 1] - b.h_frun_off[mem[q]];
+                        if (nr < bestn) {
+                            bestn = nr;
+                            best = q;
+                        }
+                    }
+                    hc.insert(hc.end(), mem, mem + k);
+                    hdrv.push_back(best);
+                    hoff.push_back(hoff.back() + bestn);
+                    owner.push_back({j, c});
+                }
+            }
+            uint64_t ncand = owner.size();
+            DevBuf<uint32_t> dc, dd, dub;
+            DevBuf<uint64_t> doff;
+            dc.alloc(hc.size(), s);
+            dd.alloc(ncand, s);
+            doff.alloc(ncand + 1, s);
+            dub.alloc(ncand * k, s);
+            dub.zero(s);
+            COLO_CUDA(cudaMemcpyAsync(dc.get(), hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(dd.get(), hdrv.data(), ncand * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(doff.get(), hoff.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
+            filter_level(b, dc.get(), dd.get(), doff.get(), ncand, hoff.back(), k, dub.get());
+            std::vector<uint32_t> hub(ncand * k);
+            COLO_CUDA(cudaMemcpyAsync(hub.data(), dub.get(), hub.size() * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
+            for (uint64_t q = 0; q < ncand; ++q) {
+                LevelTrace& L = *tr[owner[q].first];
+                size_t c = owner[q].second;
+                for (uint32_t t = 0; t < k; ++t) L.ub[c * k + t] = hub[q * k + t];
+                L.pass[c] = filter_pass(&L.ub[c * k], &L.cand[c * k], k, b.h_fcount, js[owner[q].first].thr);
+            }
+        }
+        t_filter += ms_since(t0);
+
+        // ---- refinement: count pass + participation ----
+        t0 = Clock::now();
+        std::vector<CandDesc> hd;
+        std::vector<std::pair<uint32_t, size_t>> owner;
+        std::vector<uint64_t> slot_base, chunk_off(1, 0);
+        uint64_t nslots = 0, nwords = 0;
+        for (uint32_t j = 0; j < J; ++j) {
+            if (!tr[j]) continue;
+            LevelTrace& L = *tr[j];
+            for (size_t c = 0; c < L.cand.size() / k; ++c) {
+                if (!L.pass[c]) continue;
+                CandDesc d{};
+                const uint32_t* mem = &L.cand[c * k];
+                if (k == 2) {
+                    d.parent = nullptr;
+                    d.prow = b.h_fcount[mem[0]];
+                    d.pstride = d.prow;
+                } else {
+                    std::vector<uint32_t> pre(mem, mem + k - 1);
+                    auto it = js[j].tables.find(pre);
+                    if (it == js[j].tables.end())
+                        throw StatusError{COLO_ERR_INTERNAL, "missing parent instance table"};
+                    d.parent = it->second.cols;
+                    d.prow = it->second.rows;
+                    d.pstride = it->second.stride;
+                }
+                for (uint32_t t = 0; t < k; ++t) d.m[t] = mem[t];
+                d.job = j;
+                d.k = k;
+                uint64_t w = 0;
+                for (uint32_t t = 0; t < k; ++t) {
+                    d.bm_off[t] = nwords + w;
+                    w += (b.h_fcount[mem[t]] + 31) / 32;
+                }
+                d.bm_off[k] = nwords + w;
+                nwords += w;
+                slot_base.push_back(nslots);
+                nslots += d.prow;
+                chunk_off.push_back(chunk_off.back() + (d.prow + 31) / 32);
+                hd.push_back(d);
+                owner.push_back({j, c});
+            }
+        }
+        const uint64_t ncand = hd.size();
+        LevelArena ar;
+        ar.slots.alloc(nslots ? nslots : 1, s);
+        ar.bitmap.alloc(nwords ? nwords : 1, s);
+        ar.bitmap.zero(s);
+        ar.rows.alloc(ncand ? ncand : 1, s);
+        ar.rows.zero(s);
+        ar.stats.alloc(ncand * k * 4 + 1, s);
+        for (uint64_t q = 0; q < ncand; ++q) {
+            hd[q].slots = ar.slots.get() + slot_base[q];
+            hd[q].bitmap = ar.bitmap.get();
+            hd[q].rows = ar.rows.get() + q;
+        }
+        ar.descs.alloc(ncand ? ncand : 1, s);
+        ar.chunk_off.alloc(ncand + 1, s);
+        std::vector<uint64_t> hstats(ncand * k * 4);
+        if (ncand) {
+            COLO_CUDA(cudaMemcpyAsync(ar.descs.get(), hd.data(), ncand * sizeof(CandDesc), cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(ar.chunk_off.get(), chunk_off.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
+            if (plain) {
+                // per candidate, as the reference refines (one candidate at a time)
+                DevBuf<uint64_t> one_off;
+                one_off.alloc(2 * ncand, s);
+                std::vector<uint64_t> hoff(2 * ncand);
+                for (uint64_t q = 0; q < ncand; ++q) {
+                    hoff[2 * q] = 0;
+                    hoff[2 * q + 1] = chunk_off[q + 1] - chunk_off[q];
+                }
+                COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), 2 * ncand * 8, cudaMemcpyHostToDevice, s));
+                for (uint64_t q = 0; q < ncand; ++q) {
+                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
+                    level_count(b, w, k, false);
+                    level_pi(b, ar.descs.get() + q, 1, k, ar.stats.get() + q * k * 4);
+                    COLO_CUDA(cudaMemcpyAsync(hstats.data() + q * k * 4, ar.stats.get() + q * k * 4, k * 4 * 8,
+                                              cudaMemcpyDeviceToHost, s));
+                    COLO_CUDA(cudaStreamSynchronize(s));
+                }
+            } else {
+                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr};
+                level_count(b, w, k, true);
+                level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
+                COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
+                COLO_CUDA(cudaStreamSynchronize(s));
+            }
+        }
+        // participation index (getParticipationIndex, Codes/DeviceProcess.cu:108-132)
+        std::vector<uint8_t> prev_flag(ncand, 0);
+        for (uint64_t q = 0; q < ncand; ++q) {
+            LevelTrace& L = *tr[owner[q].first];
+            size_t c = owner[q].second;
+            const uint64_t* st = &hstats[q * k * 4];   // [A, last, first, full] per member
+            uint64_t num[kMaxK];
+            if (k == 2) {
+                num[0] = st[0];
+                num[1] = (st[4 + 3] - st[4 + 2]) + ((st[4 + 2] | st[1]) ? 1 : 0);
+            } else {
+                num[0] = st[0];
+                for (uint32_t t = 1; t < k; ++t) num[t] = st[(t - 1) * 4 + 1] + st[t * 4 + 0];
+            }
+            float PI = 1.0f;
+            uint32_t am = 0;
+            for (uint32_t t = 0; t < k; ++t) {
+                L.num[c * k + t] = num[t];
+                float pr = (float)num[t] / (float)b.h_fcount[L.cand[c * k + t]];
+                if (pr < PI) {
+                    PI = pr;
+                    am = t;
+                }
+            }
+            L.pi[c] = PI;
+            L.argmin[c] = am;
+            L.prevalent[c] = !(PI < js[owner[q].first].thr);
+            prev_flag[q] = L.prevalent[c];
+        }
+        // row counts (per-candidate counters of the count pass) and fill offsets
+        std::vector<uint64_t> hrows(ncand);
+        if (ncand)
+            COLO_CUDA(cudaMemcpy(hrows.data(), ar.rows.get(), ncand * 8, cudaMemcpyDeviceToHost));
+        std::vector<uint64_t> gb(ncand + 1, 0);
+        for (uint64_t q = 0; q < ncand; ++q) gb[q + 1] = gb[q] + hrows[q];
+        for (uint64_t q = 0; q < ncand; ++q) tr[owner[q].first]->rows[owner[q].second] = gb[q + 1] - gb[q];
+        t_refine += ms_since(t0);
+
+        // ---- next candidates (Apriori) and the tables they need ----
+        t0 = Clock::now();
+        std::vector<std::unordered_set<std::vector<uint32_t>, PatternHash>> needed(J);
+        for (uint32_t j = 0; j < J; ++j) {
+            if (!tr[j]) continue;
+            LevelTrace& L = *tr[j];
+            std::vector<uint32_t> prev;
+            for (size_t c = 0; c < L.cand.size() / k; ++c)
+                if (L.prevalent[c]) prev.insert(prev.end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+            std::vector<uint32_t> next;
+            bool cap_ok = (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf;
+            if (cap_ok) next = apriori_next(prev, k);
+            js[j].cands = next;
+            for (size_t c = 0; c < next.size() / (k + 1); ++c)
+                needed[j].emplace(next.begin() + c * (k + 1), next.begin() + c * (k + 1) + k);
+        }
+        t_apriori += ms_since(t0);
+
+        // ---- fill pass for the needed prevalent patterns ----
+        t0 = Clock::now();
+        std::vector<uint64_t> fillq;
+        uint64_t total_rows = 0;
+        for (uint64_t q = 0; q < ncand; ++q) {
+            if (!prev_flag[q]) continue;
+            LevelTrace& L = *tr[owner[q].first];
+            size_t c = owner[q].second;
+            std::vector<uint32_t> pat(L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+            if (!needed[owner[q].first].count(pat)) continue;
+            fillq.push_back(q);
+            total_rows += gb[q + 1] - gb[q];
+        }
+        tables_cur.reset(new DevBuf<uint32_t>());
+        tables_cur->alloc(total_rows * k ? total_rows * k : 1, s);
+        // output offsets of every parent row: exclusive scan of the slots
+        DevBuf<uint64_t> G;
+        if (!fillq.empty()) {
+            G.alloc(nslots, s);
+            if (plain) {
+                for (uint64_t q : fillq)   // one scan per candidate, as the reference does
+                    scan_u32_to_u64(ar.slots.get() + slot_base[q], G.get() + slot_base[q], hd[q].prow, s, nullptr);
+            } else {
+                scan_u32_to_u64(ar.slots.get(), G.get(), nslots, s, nullptr);
+            }
+        }
+        std::vector<CandDesc> fd;
+        std::vector<uint64_t> fchunk(1, 0);
+        uint64_t obase = 0;
+        for (uint64_t q : fillq) {
+            CandDesc d = hd[q];
+            uint64_t rows = gb[q + 1] - gb[q];
+            d.offs = G.get() + slot_base[q];
+            d.out = tables_cur->get() + obase;
+            d.out_rows = rows;
+            obase += rows * k;
+            fd.push_back(d);
+            fchunk.push_back(fchunk.back() + (d.prow + 31) / 32);
+            LevelTrace& L = *tr[owner[q].first];
+            size_t c = owner[q].second;
+            L.has_table[c] = 1;
+        }
+        rows_written += total_rows;
+        DevBuf<CandDesc> dfd;
+        DevBuf<uint64_t> dfc;
+        if (!fd.empty()) {
+            dfd.alloc(fd.size(), s);
+            dfc.alloc(fchunk.size(), s);
+            COLO_CUDA(cudaMemcpyAsync(dfd.get(), fd.data(), fd.size() * sizeof(CandDesc), cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(dfc.get(), fchunk.data(), fchunk.size() * 8, cudaMemcpyHostToDevice, s));
+            if (plain) {
+                DevBuf<uint64_t> one_off;
+                one_off.alloc(2 * fd.size(), s);
+                std::vector<uint64_t> hoff(2 * fd.size());
+                for (size_t q = 0; q < fd.size(); ++q) {
+                    hoff[2 * q] = 0;
+                    hoff[2 * q + 1] = fchunk[q + 1] - fchunk[q];
+                }
+                COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), hoff.size() * 8, cudaMemcpyHostToDevice, s));
+                for (size_t q = 0; q < fd.size(); ++q) {
+                    LevelWork w{dfd.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
+                    level_fill(b, w, k, false);
+                    COLO_CUDA(cudaStreamSynchronize(s));
+                }
+            } else {
+                LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr};
+                level_fill(b, w, k, true);
+            }
+        }
+        COLO_CUDA(cudaStreamSynchronize(s));
+        // register the new tables (prefixes of the next level)
+        for (auto& st : js) st.tables.clear();
+        for (size_t i = 0; i < fillq.size(); ++i) {
+            uint64_t q = fillq[i];
+            LevelTrace& L = *tr[owner[q].first];
+            size_t c = owner[q].second;
+            std::vector<uint32_t> pat(L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+            TableRef t{fd[i].out, fd[i].out_rows, fd[i].out_rows};
+            js[owner[q].first].tables[pat] = t;
+            if (pv[owner[q].first].keep_tables) {
+                uint64_t rows = fd[i].out_rows;
+                std::vector<uint32_t> colm(rows * k);
+                if (rows)
+                    COLO_CUDA(cudaMemcpy(colm.data(), fd[i].out, rows * k * 4, cudaMemcpyDeviceToHost));
+                if (L.tables.size() < L.cand.size() / k) L.tables.resize(L.cand.size() / k);
+                std::vector<uint32_t>& rm = L.tables[c];
+                rm.resize(rows * k);
+                for (uint64_t r = 0; r < rows; ++r)
+                    for (uint32_t t = 0; t < k; ++t) rm[r * k + t] = colm[(uint64_t)t * rows + r];
+            }
+        }
+        t_fill += ms_since(t0);
+        tables_prev = std::move(tables_cur);
+        for (auto& st : js)
+            if (st.cands.empty()) st.active = false;
+    }
+    COLO_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t j = 0; j < J; ++j) {
+        MineResult* r = outs[j];
+        r->times[0] = ms_since(t_all);
+        r->times[1] = t_upload;
+        r->times[2] = t_bucket;
+        r->times[3] = t_join;
+        r->times[4] = t_filter;
+        r->times[5] = t_refine;
+        r->times[6] = t_fill;
+        r->times[7] = t_apriori;
+        r->counters[0] = g_launches;
+        r->counters[1] = b.npl_total;
+        r->counters[2] = b.E;
+        r->counters[3] = rows_written;
+    }
+}
+
+}  // namespace colo
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* colo_status_string(colo_status s) {
+    switch (s) {
+        case COLO_OK: return "ok";
+        case COLO_ERR_ARG: return "invalid argument";
+        case COLO_ERR_IO: return "i/o error";
+        case COLO_ERR_PARSE: return "parse error";
+        case COLO_ERR_INPUT: return "input outside the reference's domain";
+        case COLO_ERR_CUDA: return "CUDA error";
+        case COLO_ERR_NOMEM: return "out of memory";
+        case COLO_ERR_TIMEOUT: return "device wait timed out";
+        case COLO_ERR_CAPACITY: return "capacity exceeded";
+        case COLO_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "internal error";
+    }
+}
+
+void colo_params_default(colo_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->distance = 1.0f;
+    p->pi_threshold = 0.5f;
+    p->mode = COLO_MODE_BATCHED;
+}
+
+colo_status colo_create(colo_ctx** out, int device) {
+    if (!out) return COLO_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return COLO_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return COLO_ERR_ARG;
+    std::unique_ptr<colo_ctx> c(new colo_ctx());
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) return COLO_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) return COLO_ERR_CUDA;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    // keep freed blocks in the stream-ordered pool between calls
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    *out = c.release();
+    return COLO_OK;
+}
+
+colo_status colo_destroy(colo_ctx* ctx) {
+    if (!ctx) return COLO_ERR_ARG;
+    if (ctx->s) {
+        cudaStreamSynchronize(ctx->s);
+        cudaStreamDestroy(ctx->s);
+    }
+    delete ctx;
+    return COLO_OK;
+}
+
+const char* colo_last_error(const colo_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+colo_status colo_read_params(const char* path, colo_params* out) {
+    if (!path || !out) return COLO_ERR_ARG;
+    std::string err;
+    return read_params_file(path, out, err);
+}
+
+colo_status colo_read_config(const char* path, char* location, char* param_file, char* dataset,
+                             char* out_location, char* out_file, size_t cap) {
+    if (!path || cap == 0) return COLO_ERR_ARG;
+    std::string lines[5], err;
+    colo_status st = read_config_file(path, lines, err);
+    if (st != COLO_OK) return st;
+    char* dst[5] = {location, param_file, dataset, out_location, out_file};
+    for (int i = 0; i < 5; ++i) {
+        if (!dst[i]) continue;
+        if (lines[i].size() + 1 > cap) return COLO_ERR_CAPACITY;
+        std::memcpy(dst[i], lines[i].c_str(), lines[i].size() + 1);
+    }
+    return COLO_OK;
+}
+
+colo_status colo_dataset_from_csv(colo_ctx* ctx, const char* path, colo_dataset** out) {
+    if (!ctx || !path || !out) return COLO_ERR_ARG;
+    return guarded(ctx, [&]() {
+        std::unique_ptr<colo_dataset> ds(new colo_dataset());
+        ds->ctx = ctx;
+        std::string err;
+        colo_status st = parse_points_csv(path, ds->hp, err);
+        if (st != COLO_OK) return set_err(ctx, st, err);
+        group_features(ds.get());
+        *out = ds.release();
+        return COLO_OK;
+    });
+}
+
+colo_status colo_dataset_from_host(colo_ctx* ctx, const float* x, const float* y, const int32_t* fid,
+                                   uint64_t n, const float bounds[4], colo_dataset** out) {
+    if (!ctx || !out || !bounds || (n && (!x || !y || !fid))) return COLO_ERR_ARG;
+    return guarded(ctx, [&]() {
+        std::unique_ptr<colo_dataset> ds(new colo_dataset());
+        ds->ctx = ctx;
+        ds->hp.x.assign(x, x + n);
+        ds->hp.y.assign(y, y + n);
+        ds->hp.raw.assign(fid, fid + n);
+        for (uint64_t i = 0; i < n; ++i)
+            if (fid[i] == -1) return set_err(ctx, COLO_ERR_INPUT, "feature id -1 is reserved by the reference");
+        std::memcpy(ds->hp.bounds, bounds, 16);
+        group_features(ds.get());
+        *out = ds.release();
+        return COLO_OK;
+    });
+}
+
+colo_status colo_dataset_write_csv(const colo_dataset* ds, const char* path) {
+    if (!ds || !path) return COLO_ERR_ARG;
+    std::string err;
+    return write_points_csv(ds->hp, ds->names, ds->feat, path, err);
+}
+
+colo_status colo_dataset_upload(colo_dataset* ds) {
+    if (!ds) return COLO_ERR_ARG;
+    return guarded(ds->ctx, [&]() {
+        upload_dataset(ds, ds->ctx->s);
+        return COLO_OK;
+    });
+}
+
+colo_status colo_dataset_evict(colo_dataset* ds) {
+    if (!ds) return COLO_ERR_ARG;
+    ds->dx.release();
+    ds->dy.release();
+    ds->dfeat.release();
+    ds->resident = false;
+    return COLO_OK;
+}
+
+uint64_t colo_dataset_num_points(const colo_dataset* ds) { return ds ? ds->hp.x.size() : 0; }
+uint32_t colo_dataset_num_features(const colo_dataset* ds) { return ds ? (uint32_t)ds->names.size() : 0; }
+const char* colo_dataset_feature_name(const colo_dataset* ds, uint32_t f) {
+    return (ds && f < ds->names.size()) ? ds->names[f].c_str() : nullptr;
+}
+void colo_dataset_free(colo_dataset* ds) {
+    if (!ds) return;
+    if (ds->ctx) cudaStreamSynchronize(ds->ctx->s);
+    delete ds;
+}
+
+colo_status colo_mine_batch(colo_ctx* ctx, colo_dataset* const* ds, const colo_params* p, uint32_t njobs,
+                            colo_result** out) {
+    if (!ctx || !ds || !p || !out || njobs == 0) return COLO_ERR_ARG;
+    for (uint32_t j = 0; j < njobs; ++j) {
+        out[j] = nullptr;
+        if (!ds[j] || ds[j]->ctx != ctx) return COLO_ERR_ARG;
+        if (p[j].mode != p[0].mode) return set_err(ctx, COLO_ERR_ARG, "all jobs of a batch use one mode");
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return COLO_ERR_CUDA;
+    std::vector<std::unique_ptr<colo_result>> res(njobs);
+    std::vector<MineResult*> mr(njobs);
+    for (uint32_t j = 0; j < njobs; ++j) {
+        res[j].reset(new colo_result());
+        mr[j] = &res[j]->r;
+    }
+    colo_status st = guarded(ctx, [&]() {
+        if (p[0].mode == COLO_MODE_PLAIN && njobs > 1) {
+            for (uint32_t j = 0; j < njobs; ++j) mine_jobs(ctx, &ds[j], &p[j], 1, &mr[j]);
+        } else {
+            mine_jobs(ctx, ds, p, njobs, mr.data());
+        }
+        return COLO_OK;
+    });
+    if (st != COLO_OK) return st;
+    for (uint32_t j = 0; j < njobs; ++j) out[j] = res[j].release();
+    return COLO_OK;
+}
+
+colo_status colo_mine(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, colo_result** out) {
+    return colo_mine_batch(ctx, &ds, p, 1, out);
+}
+
+uint32_t colo_result_num_levels(const colo_result* r) { return r ? (uint32_t)r->r.levels.size() : 0; }
+uint32_t colo_result_level_size(const colo_result* r, uint32_t li) {
+    return (r && li < r->r.levels.size()) ? r->r.levels[li].k : 0;
+}
+uint64_t colo_result_level_candidates(const colo_result* r, uint32_t li) {
+    return (r && li < r->r.levels.size()) ? r->r.levels[li].cand.size() / r->r.levels[li].k : 0;
+}
+
+colo_status colo_result_level(const colo_result* r, uint32_t li, uint32_t* cand, uint64_t* ub, uint8_t* pass,
+                              uint64_t* rows, uint64_t* num, float* pi, uint8_t* prevalent, uint32_t* argmin) {
+    if (!r || li >= r->r.levels.size()) return COLO_ERR_ARG;
+    const LevelTrace& L = r->r.levels[li];
+    size_t C = L.cand.size() / L.k;
+    if (cand)
+        for (size_t i = 0; i < L.cand.size(); ++i) cand[i] = L.cand[i] - L.f0;
+    if (ub) std::memcpy(ub, L.ub.data(), L.ub.size() * 8);
+    if (pass) std::memcpy(pass, L.pass.data(), C);
+    if (rows) std::memcpy(rows, L.rows.data(), C * 8);
+    if (num) std::memcpy(num, L.num.data(), L.num.size() * 8);
+    if (pi) std::memcpy(pi, L.pi.data(), C * 4);
+    if (prevalent) std::memcpy(prevalent, L.prevalent.data(), C);
+    if (argmin) std::memcpy(argmin, L.argmin.data(), C * 4);
+    return COLO_OK;
+}
+
+uint64_t colo_result_table(const colo_result* r, uint32_t li, uint64_t ci, uint32_t* out) {
+    if (!r || li >= r->r.levels.size()) return UINT64_MAX;
+    const LevelTrace& L = r->r.levels[li];
+    if (ci >= L.has_table.size() || !L.has_table[ci] || ci >= L.tables.size()) return UINT64_MAX;
+    const auto& t = L.tables[ci];
+    if (out) std::memcpy(out, t.data(), t.size() * 4);
+    return t.size() / L.k;
+}
+
+colo_status colo_result_write_patterns(const colo_result* r, const colo_dataset* ds, const char* location) {
+    if (!r || !ds || !location) return COLO_ERR_ARG;
+    std::string err;
+    return write_patterns(r->r, ds->names, location, err);
+}
+
+colo_status colo_result_times(const colo_result* r, double* ms8) {
+    if (!r || !ms8) return COLO_ERR_ARG;
+    std::memcpy(ms8, r->r.times, sizeof(r->r.times));
+    return COLO_OK;
+}
+
+colo_status colo_result_counters(const colo_result* r, uint64_t* c8) {
+    if (!r || !c8) return COLO_ERR_ARG;
+    std::memcpy(c8, r->r.counters, sizeof(r->r.counters));
+    return COLO_OK;
+}
+
+void colo_result_free(colo_result* r) { delete r; }
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// colo_stage.cpp -- stage-level C entry points (one kernel family each), the
+// counterparts of the reference's inner extern "C" API
+// (Codes/DeviceProcess.h:4-36).  They run one stage on a dataset and copy
+// its result to host arrays, so each kernel can be checked in isolation.
+#include <cstring>
+#include <vector>
+
+#include "colo_batch.h"
+#include "colo_host.h"
+
+using namespace colo;
+
+namespace {
+
+colo_params params_for(float R, float thr) {
+    colo_params p;
+    colo_params_default(&p);
+    p.distance = R;
+    p.pi_threshold = thr;
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+colo_status colo_stage_cells(colo_ctx* ctx, colo_dataset* ds, float R, uint64_t* cell_of, uint64_t* run_cell,
+                             uint32_t* run_feat, uint32_t* run_count, uint64_t* nruns) {
+    if (!ctx || !ds || !nruns) return COLO_ERR_ARG;
+    return run_guarded(ctx, [&]() -> colo_status {
+        colo_params p = params_for(R, 0.f);
+        Batch b;
+        std::vector<DevBuf<float>> of;
+        std::vector<DevBuf<uint32_t>> ou;
+        colo_dataset* dsv[1] = {ds};
+        setup_batch(ctx, dsv, &p, 1, b, of, ou, nullptr);
+        if (b.N) bucket_points(b);
+        cudaStream_t s = ctx->s;
+        uint64_t cap = *nruns;
+        *nruns = b.Rn;
+        if (cell_of && b.N) {
+            // per point: cell key of its sorted position
+            std::vector<uint32_t> sid(b.N), scell(b.N);
+            std::vector<uint64_t> ckey(b.M);
+            COLO_CUDA(cudaMemcpyAsync(sid.data(), b.sid.get(), b.N * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(scell.data(), b.scell.get(), b.N * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(ckey.data(), b.ckey.get(), b.M * 8, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
+            for (uint64_t q = 0; q < b.N; ++q) cell_of[sid[q]] = ckey[scell[q]];
+        }
+        if ((run_cell || run_feat || run_count) && b.Rn) {
+            if (cap < b.Rn) return COLO_ERR_CAPACITY;
+            std::vector<uint32_t> rf(b.Rn), rc(b.Rn), rcell(b.Rn);
+            std::vector<uint64_t> ckey(b.M);
+            COLO_CUDA(cudaMemcpyAsync(rf.data(), b.rfeat.get(), b.Rn * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(rc.data(), b.rcnt.get(), b.Rn * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(rcell.data(), b.rcell.get(), b.Rn * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(ckey.data(), b.ckey.get(), b.M * 8, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
+            for (uint64_t r = 0; r < b.Rn; ++r) {
+                if (run_cell) run_cell[r] = ckey[rcell[r]];
+                if (run_feat) run_feat[r] = rf[r];
+                if (run_count) run_count[r] = rc[r];
+            }
+        }
+        return COLO_OK;
+    });
+}
+
+colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint64_t* offs, uint32_t* nbr,
+                                 uint64_t* total) {
+    if (!ctx || !ds || !total) return COLO_ERR_ARG;
+    return run_guarded(ctx, [&]() -> colo_status {
+        colo_params p = params_for(R, 0.f);
+        Batch b;
+        std::vector<DevBuf<float>> of;
+        std::vector<DevBuf<uint32_t>> ou;
+        colo_dataset* dsv[1] = {ds};
+        setup_batch(ctx, dsv, &p, 1, b, of, ou, nullptr);
+        uint64_t cap = *total;
+        if (b.N) {
+            bucket_points(b);
+            build_neighborhoods(b);
+            join_neighbors(b);
+        }
+        *total = b.E;
+        cudaStream_t s = ctx->s;
+        if (offs && b.N) COLO_CUDA(cudaMemcpyAsync(offs, b.nb_off.get(), (b.N + 1) * 8, cudaMemcpyDeviceToHost, s));
+        if (offs && !b.N) offs[0] = 0;
+        if (nbr && b.E) {
+            if (cap < b.E) return COLO_ERR_CAPACITY;
+            COLO_CUDA(cudaMemcpyAsync(nbr, b.nb.get(), b.E * 4, cudaMemcpyDeviceToHost, s));
+        }
+        COLO_CUDA(cudaStreamSynchronize(s));
+        return COLO_OK;
+    });
+}
+
+colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float thr, const uint32_t* cand,
+                              uint64_t ncand, uint32_t k, uint64_t* ub, uint8_t* pass) {
+    if (!ctx || !ds || (ncand && (!cand || !ub))) return COLO_ERR_ARG;
+    if (k < 2 || k > kMaxK) return COLO_ERR_ARG;
+    return run_guarded(ctx, [&]() -> colo_status {
+        colo_params p = params_for(R, thr);
+        Batch b;
+        std::vector<DevBuf<float>> of;
+        std::vector<DevBuf<uint32_t>> ou;
+        colo_dataset* dsv[1] = {ds};
+        setup_batch(ctx, dsv, &p, 1, b, of, ou, nullptr);
+        if (b.N) bucket_points(b);
+        for (uint64_t c = 0; c < ncand * k; ++c)
+            if (cand[c] >= b.F) return COLO_ERR_ARG;
+        cudaStream_t s = ctx->s;
+        std::vector<uint64_t> hub(ncand * k, 0);
+        if (b.N && ncand) {
+            if (k == 2) {
+                DevBuf<uint32_t> ub2;
+                std::vector<uint64_t> job_off;
+                filter_pairs(b, ub2, job_off);
+                std::vector<uint32_t> h(job_off[1]);
+                COLO_CUDA(cudaMemcpy(h.data(), ub2.get(), h.size() * 4, cudaMemcpyDeviceToHost));
+                uint32_t nf = b.F;
+                for (uint64_t c = 0; c < ncand; ++c) {
+                    uint32_t a = cand[2 * c], bb = cand[2 * c + 1];
+                    hub[2 * c] = a == bb ? 0 : h[(uint64_t)a * nf + bb];
+                    hub[2 * c + 1] = a == bb ? 0 : h[(uint64_t)bb * nf + a];
+                }
+            } else {
+                std::vector<uint32_t> drv(ncand);
+                std::vector<uint64_t> off(ncand + 1, 0);
+                for (uint64_t c = 0; c < ncand; ++c) {
+                    uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered, best = 0, bn = UINT32_MAX;
+                    for (uint32_t q = 0; q < m; ++q) {
+                        uint32_t f = cand[c * k + q];
+                        uint32_t nr = b.h_frun_off[f + 1] - b.h_frun_off[f];
+                        if (nr < bn) {
+                            bn = nr;
+                            best = q;
+                        }
+                    }
+                    drv[c] = best;
+                    off[c + 1] = off[c] + bn;
+                }
+                DevBuf<uint32_t> dc, dd, du;
+                DevBuf<uint64_t> doff;
+                dc.alloc(ncand * k, s);
+                dd.alloc(ncand, s);
+                doff.alloc(ncand + 1, s);
+                du.alloc(ncand * k, s);
+                du.zero(s);
+                COLO_CUDA(cudaMemcpyAsync(dc.get(), cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
+                COLO_CUDA(cudaMemcpyAsync(dd.get(), drv.data(), ncand * 4, cudaMemcpyHostToDevice, s));
+                COLO_CUDA(cudaMemcpyAsync(doff.get(), off.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
+                filter_level(b, dc.get(), dd.get(), doff.get(), ncand, off[ncand], k, du.get());
+                std::vector<uint32_t> h(ncand * k);
+                COLO_CUDA(cudaMemcpyAsync(h.data(), du.get(), h.size() * 4, cudaMemcpyDeviceToHost, s));
+                COLO_CUDA(cudaStreamSynchronize(s));
+                for (uint64_t q = 0; q < ncand * k; ++q) hub[q] = h[q];
+            }
+        }
+        std::memcpy(ub, hub.data(), hub.size() * 8);
+        if (pass) {
+            for (uint64_t c = 0; c < ncand; ++c) {
+                float pi0 = 1.0f;
+                for (uint32_t j = 0; j < k; ++j) {
+                    float pr = (float)((double)hub[c * k + j] / (double)(float)b.h_fcount[cand[c * k + j]]);
+                    if (j == 0) pi0 = pr;
+                    else if (pi0 > pr) pi0 = pr;
+                }
+                pass[c] = pi0 >= thr;
+            }
+        }
+        return COLO_OK;
+    });
+}
+
+colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, const float* x2, const float* y2,
+                              uint64_t n, float* out) {
+    if (!ctx || (n && (!x1 || !y1 || !x2 || !y2 || !out))) return COLO_ERR_ARG;
+    return run_guarded(ctx, [&]() -> colo_status {
+        cudaStream_t s = ctx->s;
+        DevBuf<float> a, b, c, d, o;
+        a.alloc(n, s);
+        b.alloc(n, s);
+        c.alloc(n, s);
+        d.alloc(n, s);
+        o.alloc(n, s);
+        if (n) {
+            COLO_CUDA(cudaMemcpyAsync(a.get(), x1, n * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(b.get(), y1, n * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(c.get(), x2, n * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(d.get(), y2, n * 4, cudaMemcpyHostToDevice, s));
+            eval_sqdist(a.get(), b.get(), c.get(), d.get(), n, o.get(), s);
+            COLO_CUDA(cudaMemcpyAsync(out, o.get(), n * 4, cudaMemcpyDeviceToHost, s));
+        }
+        COLO_CUDA(cudaStreamSynchronize(s));
+        return COLO_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+/*
+ * colo.h -- C ABI of the GB300 colocation-mining library (libcolo.so).
+ *
+ * The library replaces the GPU path of GPU-ColocationMininig (Codes/): grid
+ * bucketing, the cell-pair spatial join, the cell-aggregate upper-bound
+ * filter, level-wise instance tables and the participation index.  Every
+ * entry point takes plain pointers and sizes, returns a colo_status, never
+ * prints and never exits.  A context owns one CUDA stream on one device and
+ * all device memory it allocates; use one context per host thread.
+ *
+ * Each declaration names the reference interface it replaces (paths inside
+ * the reference project).
+ */
+#ifndef COLO_H
+#define COLO_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    COLO_OK = 0,
+    COLO_ERR_ARG = 1,        /* bad argument (NULL, size, out of range) */
+    COLO_ERR_IO = 2,         /* file cannot be opened / written */
+    COLO_ERR_PARSE = 3,      /* malformed config, parameter or CSV file */
+    COLO_ERR_INPUT = 4,      /* data the reference cannot represent (point outside the grid, non-finite) */
+    COLO_ERR_CUDA = 5,       /* CUDA runtime error (message in colo_last_error) */
+    COLO_ERR_NOMEM = 6,      /* device or host allocation failed */
+    COLO_ERR_TIMEOUT = 7,    /* a bounded device wait gave up */
+    COLO_ERR_CAPACITY = 8,   /* a fixed-size buffer is too small for the request */
+    COLO_ERR_NO_DEVICE = 9,  /* no CUDA device / library not usable */
+    COLO_ERR_INTERNAL = 10
+} colo_status;
+
+/* Execution form of the level loop. */
+typedef enum {
+    COLO_MODE_PLAIN = 0,     /* per-candidate count -> PI -> fill launches (two-pass) */
+    COLO_MODE_BATCHED = 1,   /* one persistent work-queue launch per level phase, CUDA graph */
+    COLO_MODE_LEARNED = 2    /* batched + cost-model presized single-pass fill with exact fallback */
+} colo_mode;
+
+typedef struct colo_ctx colo_ctx;
+typedef struct colo_dataset colo_dataset;
+typedef struct colo_result colo_result;
+
+/* Mining parameters.  distance / pi_threshold / filter_flag are the three
+ * values of the reference's parameter file (colocationFinder.cpp:57-74);
+ * filter_flag is read and ignored as in the reference. */
+typedef struct {
+    float distance;          /* R; neighbours satisfy squared distance <= R*R (float) */
+    float pi_threshold;      /* prevalent iff !(PI < pi_threshold) */
+    uint32_t filter_flag;
+    uint32_t max_size;       /* 0 = no cap (the reference has none) */
+    int32_t mode;            /* colo_mode */
+    int32_t keep_tables;     /* 1: keep every instance table in the result (tests) */
+    int32_t reserved[6];
+} colo_params;
+
+const char* colo_status_string(colo_status s);
+
+/* ---- context ---------------------------------------------------------- */
+/* Replaces the colocationFinder constructor (colocationFinder.cpp:21-42):
+ * no fixed-size buffers are allocated up front. */
+colo_status colo_create(colo_ctx** out, int device);
+colo_status colo_destroy(colo_ctx* ctx);
+/* Last error message of this context ("" if none). */
+const char* colo_last_error(const colo_ctx* ctx);
+void colo_params_default(colo_params* p);
+
+/* ---- input ------------------------------------------------------------ */
+/* LoadParameter (colocationFinder.cpp:57-74): "R thr flag" whitespace separated. */
+colo_status colo_read_params(const char* path, colo_params* out);
+/* Begin's config file (colocationFinder.cpp:1077-1092): five lines --
+ * location, parameter file, dataset, output location, output file.  Each
+ * out buffer receives a NUL-terminated line (cap bytes each). */
+colo_status colo_read_config(const char* path, char* location, char* param_file, char* dataset,
+                             char* out_location, char* out_file, size_t cap);
+/* populateData (colocationFinder.cpp:139-254): count line, "fid,x,y" lines
+ * grouped by feature until an empty line, then "minX,minY,maxX,maxY". */
+colo_status colo_dataset_from_csv(colo_ctx* ctx, const char* path, colo_dataset** out);
+/* Same data from host arrays: raw feature ids grouped as in populateData
+ * (a change of id starts a new feature, colocationFinder.cpp:168-184). */
+colo_status colo_dataset_from_host(colo_ctx* ctx, const float* x, const float* y,
+                                   const int32_t* fid, uint64_t n, const float bounds[4],
+                                   colo_dataset** out);
+/* Write a dataset in the reference's CSV format (for the CLI and tests). */
+colo_status colo_dataset_write_csv(const colo_dataset* ds, const char* path);
+/* Copy the points to the device now (initializeDeviceMemory,
+ * colocationFinder.cpp:443-464); otherwise colo_mine copies them. */
+colo_status colo_dataset_upload(colo_dataset* ds);
+/* Drop the device copy (the next mine copies again). */
+colo_status colo_dataset_evict(colo_dataset* ds);
+uint64_t colo_dataset_num_points(const colo_dataset* ds);
+uint32_t colo_dataset_num_features(const colo_dataset* ds);
+/* Name (as written in the CSV) of feature f. */
+const char* colo_dataset_feature_name(const colo_dataset* ds, uint32_t f);
+void colo_dataset_free(colo_dataset* ds);
+
+/* ---- mining ----------------------------------------------------------- */
+/* The level loop of Begin (colocationFinder.cpp:1068-1147): degree2Processing
+ * (256-425), then generatePrevalentPatternsGeneral (736-854) and
+ * generateInstanceTableGeneral (856-909) per level, candidateColocationGeneral
+ * (517-557) between levels. */
+colo_status colo_mine(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, colo_result** out);
+/* Many independent jobs; in COLO_MODE_BATCHED/LEARNED every job's level-k
+ * candidates share one launch per level. */
+colo_status colo_mine_batch(colo_ctx* ctx, colo_dataset* const* ds, const colo_params* p,
+                            uint32_t njobs, colo_result** out);
+
+/* ---- results ---------------------------------------------------------- */
+uint32_t colo_result_num_levels(const colo_result* r);
+uint32_t colo_result_level_size(const colo_result* r, uint32_t li);       /* k of level li */
+uint64_t colo_result_level_candidates(const colo_result* r, uint32_t li); /* |C_k| */
+/* Per-candidate trace of one level; arrays sized ncand*k (cand, ub, num) or
+ * ncand (pass, rows, pi, prevalent, argmin); any pointer may be NULL.
+ * ub: filter upper-bound counts; pass: filter verdict; rows: instance-table
+ * rows (0 when not refined); num: participation numerators; pi: float PI
+ * (-1 when not refined); argmin: member giving the minimum. */
+colo_status colo_result_level(const colo_result* r, uint32_t li, uint32_t* cand, uint64_t* ub,
+                              uint8_t* pass, uint64_t* rows, uint64_t* num, float* pi,
+                              uint8_t* prevalent, uint32_t* argmin);
+/* Instance table of candidate ci of level li (kept with keep_tables):
+ * returns rows, copies rows*k point ids row-major into out if non-NULL;
+ * UINT64_MAX if the table was not built. */
+uint64_t colo_result_table(const colo_result* r, uint32_t li, uint64_t ci, uint32_t* out);
+/* savetoFileGen format (colocationFinder.cpp:979-997):
+ * <location>ColocationDegree_<k>.txt with lines "( a | b | c )". */
+colo_status colo_result_write_patterns(const colo_result* r, const colo_dataset* ds,
+                                       const char* location);
+/* Timing of the last mine, milliseconds: [0] total, [1] upload, [2] bucketing,
+ * [3] join, [4] filter, [5] refine, [6] fill, [7] host Apriori. */
+colo_status colo_result_times(const colo_result* r, double* ms8);
+/* Device work counters: [0] kernel launches, [1] join pairs evaluated,
+ * [2] neighbour entries, [3] rows written, [4] fallback candidates. */
+colo_status colo_result_counters(const colo_result* r, uint64_t* c8);
+void colo_result_free(colo_result* r);
+
+/* ---- stage entry points (mirror the reference's inner extern "C" API) ---- */
+/* CountCellFeatures (DeviceProcess.cu:312-369): per-point cell ids and the
+ * (cell, feature) runs of the bucketed dataset.  cell_of[n]; run arrays
+ * sized by *nruns (call with NULL arrays first to get the count). */
+colo_status colo_stage_cells(colo_ctx* ctx, colo_dataset* ds, float R, uint64_t* cell_of,
+                             uint64_t* run_cell, uint32_t* run_feat, uint32_t* run_count,
+                             uint64_t* nruns);
+/* The neighbour relation that degree2TableSlotCounter_Kernel and the level-k
+ * kernels evaluate (DeviceProcess_Kernel.h:12-55, 255-316) as a CSR:
+ * N+(a) = {b : feat(b) > feat(a), cells adjacent, sq(a,b) <= R^2}, each list
+ * ordered by (feature, neighbour cell, b).  offs[n+1], nbr[*total]. */
+colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint64_t* offs,
+                                 uint32_t* nbr, uint64_t* total);
+/* filter2 / threshold_Kernel (DeviceProcess.cu:219-235): upper bounds and
+ * verdicts for ncand candidates of size k (global feature indices). */
+colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float thr,
+                              const uint32_t* cand, uint64_t ncand, uint32_t k, uint64_t* ub,
+                              uint8_t* pass);
+/* Reference squared-distance expression (Utility_Inline.h:25-33) evaluated
+ * on the device for n point pairs: out[i] = sq(x1,y1,x2,y2) bits. */
+colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
+                              const float* y2, uint64_t n, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

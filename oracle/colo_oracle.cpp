@@ -1,0 +1,1101 @@
+/*
+ * colo_oracle.cpp -- CPU restatement of the reference's colocation-mining
+ * semantics.  TEST INFRASTRUCTURE ONLY (see colo_oracle.h): used by tests/,
+ * __graft_entry__.smoke() and bench.py's CPU legs, never by the product.
+ *
+ * Parity status of this oracle
+ *  - Float squared-distance form: pinned against the reference's own device
+ *    expression evaluated on a GB300 (tests/test_gpu_sqdist.py).
+ *  - Integer/host semantics (parse, grid, cells, neighbour-cell rule, filter,
+ *    tables, bitmap windows, PI, Apriori): pinned against golden vectors that
+ *    the reference's own sources produced when compiled and run on the CPU
+ *    (oracle/ref_emu/, fixtures in tests/golden/).
+ *
+ * All citations are paths inside the reference project.
+ */
+#include "colo_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <string>
+#include <unordered_set>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+/* ------------------------------------------------------------------------ */
+/* Float arithmetic                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Codes/Utility_Inline.h:25-33: squareDistance = pow(x2-x1,2) + pow(y2-y1,2)
+ * in float on the device with nvcc defaults.  Measured on a GB300 over every
+ * mantissa of 81 binades, the device pow(d, 2) is the correctly rounded
+ * square except when d*d lies exactly halfway between two floats, where it
+ * may return either neighbour; the two squares are then added with one
+ * correctly rounded float add.  CUDA's pow itself is not restated here.
+ * The host therefore knows the comparison sq <= R^2 exactly unless an exact
+ * tie can flip it; such pairs are "ambiguous" and are resolved by a device
+ * evaluation of the reference expression supplied by the caller. */
+struct SqDecision {
+    bool le;          /* sq <= R2 (for ambiguous pairs: the round-to-even guess) */
+    bool ambiguous;
+};
+
+inline void square_candidates(float d, float* c, int* nc) {
+    double e = (double)d * (double)d;          /* exact for a float d */
+    float rn = (float)e;                       /* round to nearest even */
+    if (e < 1e-36 || e > 3.0e38) {             /* outside the measured range */
+        c[0] = rn;
+        c[1] = rn;
+        *nc = -1;
+        return;
+    }
+    if ((double)rn == e) {
+        c[0] = rn;
+        *nc = 1;
+        return;
+    }
+    float other = (double)rn < e ? std::nextafter(rn, INFINITY) : std::nextafter(rn, 0.0f);
+    if ((double)rn + (double)other == 2.0 * e) {   /* exact tie */
+        c[0] = rn;
+        c[1] = other;
+        *nc = 2;
+        return;
+    }
+    c[0] = rn;
+    *nc = 1;
+}
+
+inline SqDecision sq_decide(float x1, float y1, float x2, float y2, float R2) {
+    float dx = x2 - x1;
+    float dy = y2 - y1;
+    float a[2], b[2];
+    int na, nb;
+    square_candidates(dx, a, &na);
+    square_candidates(dy, b, &nb);
+    SqDecision out;
+    out.le = (a[0] + b[0]) <= R2;
+    out.ambiguous = (na < 0 || nb < 0);
+    if (out.ambiguous) return out;
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j)
+            if (((a[i] + b[j]) <= R2) != out.le) out.ambiguous = true;
+    return out;
+}
+
+/* Squared distance value when no tie is involved (used by oracle_sqdist). */
+inline float sqdist(float x1, float y1, float x2, float y2) {
+    float dx = x2 - x1;
+    float dy = y2 - y1;
+    return (float)((double)dx * dx) + (float)((double)dy * dy);
+}
+
+/* Device float -> u32 conversion (cvt.rzi.u32.f32 clamps to the range). */
+inline uint32_t f2u_sat(float f) {
+    if (!(f > 0.0f)) return 0u;                 /* negative, zero, NaN */
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Grid                                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* colocationFinder.cpp:102-115 (setGrid). */
+int make_grid(float minX, float minY, float maxX, float maxY, float R, oracle_grid* g) {
+    std::memset(g, 0, sizeof(*g));
+    if (!(R > 0.0f) || !std::isfinite(R)) return 1;
+    g->min_x = minX;
+    g->min_y = minY;
+    g->max_x = maxX;
+    g->max_y_ext = maxY + R;              /* computeZone.maxBound.y = maxY + R */
+    g->cell_width = R;
+    float gsx = (g->max_x - g->min_x) / g->cell_width;
+    float gsy = (g->max_y_ext - g->min_y) / g->cell_width;
+    if (!std::isfinite(gsx) || !std::isfinite(gsy)) return 1;
+    float cx = std::ceil(gsx), cy = std::ceil(gsy);
+    if (!(cx >= 1.0f) || !(cy >= 1.0f)) return 1;
+    if (cx >= 4294967296.0f || cy >= 4294967296.0f) return 1;
+    g->gx = (uint32_t)cx;
+    g->gy = (uint32_t)cy;
+    g->total_cells = (uint64_t)g->gx * (uint64_t)g->gy;
+    /* The reference keeps cell ids in u32 and neighbour ids in i32
+     * (Utility_Inline.h:35-37).  Both are exact while total + gx < 2^31. */
+    g->compat32 = (g->total_cells + g->gx) < (1ull << 31) ? 1 : 0;
+    return 0;
+}
+
+/* Codes/DeviceProcess_Kernel.h:615-625 (getCellID), u32 arithmetic. */
+inline uint64_t cell_of(const oracle_grid& g, float x, float y) {
+    float rx = x - g.min_x;
+    float ry = y - g.min_y;
+    rx /= g.cell_width;
+    ry /= g.cell_width;
+    uint64_t i = f2u_sat(rx), j = f2u_sat(ry);
+    uint64_t c = (uint64_t)g.gx * j + i;
+    if (g.compat32) c = (uint32_t)c;      /* const Integer CellID = gx*j + i */
+    return c;
+}
+
+/* Codes/Utility_Inline.h:35-53 (getNeighborCellID) plus the caller's range
+ * check (e.g. DeviceProcess_Kernel.h:28-32).  Returns -1 for "skip". */
+inline int64_t neighbor_cell32(uint32_t x, uint32_t y, uint32_t tid, uint32_t gx,
+                               uint64_t total) {
+    int32_t ncid = (int32_t)(y * gx + x);
+    int32_t r;
+    if (tid % gx == 0) {
+        r = (((uint32_t)ncid + 1u) % gx == 0) ? -1 : ncid;
+    } else if ((tid + 1u) % gx == 0) {
+        r = (((uint32_t)ncid) % gx == 0) ? -1 : ncid;
+    } else {
+        r = ncid;
+    }
+    if (r < 0 || (uint64_t)(uint32_t)r >= total) return -1;
+    return r;
+}
+
+/* The same rule with 64-bit signed arithmetic, used where the reference's
+ * 32-bit ids overflow (total + gx >= 2^31). */
+inline int64_t neighbor_cell64(int64_t x, int64_t y, uint64_t cell, uint32_t gx,
+                               uint64_t total) {
+    int64_t ncid = y * (int64_t)gx + x;
+    if (ncid < 0 || (uint64_t)ncid >= total) return -1;
+    uint64_t cx = cell % gx;
+    if (cx == 0) {
+        if (((uint64_t)ncid + 1) % gx == 0) return -1;
+    } else if (cx == (uint64_t)gx - 1) {
+        if ((uint64_t)ncid % gx == 0) return -1;
+    }
+    return ncid;
+}
+
+/* Visit the up-to-9 neighbour cells of `cell` in the reference's order
+ * (j outer, i inner: DeviceProcess_Kernel.h:24-28). */
+template <class F>
+inline void for_neighbor_cells(const oracle_grid& g, uint64_t cell, F&& fn) {
+    if (g.compat32) {
+        uint32_t cur = (uint32_t)cell;
+        uint32_t cidy = cur / g.gx;
+        uint32_t cidx = cur - g.gx * cidy;
+        for (int j = -1; j <= 1; ++j)
+            for (int i = -1; i <= 1; ++i) {
+                int64_t nc = neighbor_cell32(cidx + (uint32_t)i, cidy + (uint32_t)j, cur,
+                                             g.gx, g.total_cells);
+                if (nc >= 0) fn((uint64_t)nc);
+            }
+    } else {
+        int64_t cidy = (int64_t)(cell / g.gx);
+        int64_t cidx = (int64_t)(cell % g.gx);
+        for (int j = -1; j <= 1; ++j)
+            for (int i = -1; i <= 1; ++i) {
+                int64_t nc = neighbor_cell64(cidx + i, cidy + j, cell, g.gx, g.total_cells);
+                if (nc >= 0) fn((uint64_t)nc);
+            }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Bucketed data (CountCellFeatures, Codes/DeviceProcess.cu:312-369)         */
+/* ------------------------------------------------------------------------ */
+
+struct Data {
+    uint64_t n = 0;
+    uint32_t F = 0;
+    const float* x = nullptr;
+    const float* y = nullptr;
+    const uint32_t* feat = nullptr;
+    std::vector<uint32_t> fstart, fcount;
+    oracle_grid g{};
+    float R2 = 0.0f;
+    float thr = 0.0f;
+    std::vector<uint64_t> cellOf;
+    std::vector<uint32_t> sorted;      /* point ids sorted by (cell, id) */
+    /* (cell, feature) runs in sorted order: key = cell*F + f */
+    std::vector<uint64_t> runKey;
+    std::vector<uint64_t> runStart;
+    std::vector<uint32_t> runCount;
+    std::vector<uint64_t> cellKeys;    /* distinct occupied cells, ascending */
+    std::vector<std::vector<uint32_t>> cellFeatRuns; /* per occupied cell: run indices */
+    /* device outcomes for ambiguous pairs: key = min(a,b) << 32 | max(a,b) */
+    const uint64_t* res_keys = nullptr;
+    const uint8_t* res_le = nullptr;
+    uint64_t nres = 0;
+    mutable std::atomic<uint64_t> unresolved{0};
+
+    /* The reference's neighbour test sq(a, b) <= R^2 (a = first instance). */
+    bool near(uint32_t a, uint32_t b) const {
+        SqDecision dc = sq_decide(x[a], y[a], x[b], y[b], R2);
+        if (!dc.ambiguous) return dc.le;
+        uint64_t key = a < b ? ((uint64_t)a << 32 | b) : ((uint64_t)b << 32 | a);
+        const uint64_t* it = std::lower_bound(res_keys, res_keys + nres, key);
+        if (it != res_keys + nres && *it == key) return res_le[it - res_keys] != 0;
+        unresolved.fetch_add(1, std::memory_order_relaxed);
+        return dc.le;
+    }
+
+    /* run lookup: index of run (cell, f) or -1 */
+    int64_t run(uint64_t cell, uint32_t f) const {
+        uint64_t key = cell * (uint64_t)F + f;
+        auto it = std::lower_bound(runKey.begin(), runKey.end(), key);
+        if (it == runKey.end() || *it != key) return -1;
+        return it - runKey.begin();
+    }
+    uint32_t count(uint64_t cell, uint32_t f) const {
+        int64_t r = run(cell, f);
+        return r < 0 ? 0u : runCount[r];
+    }
+};
+
+int build_data(Data& d, const float* x, const float* y, const uint32_t* feat, uint64_t n,
+               uint32_t F, const float bounds[4], float R, float thr) {
+    d.n = n;
+    d.F = F;
+    d.x = x;
+    d.y = y;
+    d.feat = feat;
+    d.thr = thr;
+    d.R2 = R * R;                        /* colocationFinder.cpp:73 */
+    if (make_grid(bounds[0], bounds[1], bounds[2], bounds[3], R, &d.g)) return 2;
+    d.fstart.assign(F, 0);
+    d.fcount.assign(F, 0);
+    /* featureInstanceStart / Count (colocationFinder.cpp:168-229) */
+    for (uint64_t i = 0; i < n; ++i) {
+        if (feat[i] >= F) return 3;
+        if (i > 0 && feat[i] < feat[i - 1]) return 3;
+        if (d.fcount[feat[i]] == 0) d.fstart[feat[i]] = (uint32_t)i;
+        d.fcount[feat[i]]++;
+    }
+    for (uint32_t f = 0; f < F; ++f)
+        if (d.fcount[f] == 0) return 3;
+    d.cellOf.resize(n);
+    for (uint64_t i = 0; i < n; ++i) {
+        if (!std::isfinite(x[i]) || !std::isfinite(y[i])) return 4;
+        d.cellOf[i] = cell_of(d.g, x[i], y[i]);
+        if (d.cellOf[i] >= d.g.total_cells) return 4;
+    }
+    /* thrust::sort_by_key on cell ids is stable (DeviceProcess.cu:342). */
+    d.sorted.resize(n);
+    for (uint64_t i = 0; i < n; ++i) d.sorted[i] = (uint32_t)i;
+    std::stable_sort(d.sorted.begin(), d.sorted.end(),
+                     [&](uint32_t a, uint32_t b) { return d.cellOf[a] < d.cellOf[b]; });
+    for (uint64_t p = 0; p < n; ++p) {
+        uint32_t id = d.sorted[p];
+        uint64_t key = d.cellOf[id] * (uint64_t)F + feat[id];
+        if (d.runKey.empty() || d.runKey.back() != key) {
+            d.runKey.push_back(key);
+            d.runStart.push_back(p);
+            d.runCount.push_back(0);
+        }
+        d.runCount.back()++;
+    }
+    for (size_t r = 0; r < d.runKey.size(); ++r) {
+        uint64_t cell = d.runKey[r] / F;
+        if (d.cellKeys.empty() || d.cellKeys.back() != cell) {
+            d.cellKeys.push_back(cell);
+            d.cellFeatRuns.emplace_back();
+        }
+        d.cellFeatRuns.back().push_back((uint32_t)r);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Filter: cell-aggregate upper bound (DeviceProcess_Kernel.h:469-509 and    */
+/* threshold_Kernel 545-573).  The reference's degree-2 variant             */
+/* (filter2_2_Kernel, 512-543) reads an uninitialised index; the degree>=3  */
+/* rule is applied to pairs as well.                                        */
+/* ------------------------------------------------------------------------ */
+
+struct FilterOut {
+    std::vector<uint64_t> ub;   /* k entries */
+    bool pass = false;
+};
+
+/* Threshold step, DeviceProcess_Kernel.h:545-573: per member
+ * PI = (float)(countMap * 1.0 / (float)n_j), minimum, compare >= thr.
+ * Only members j < 8 are ever counted (block (8,2,2) in
+ * DeviceProcess.cu:223); the others keep countMap = 0. */
+bool threshold_pass(const Data& d, const uint32_t* c, uint32_t k, const uint64_t* ub) {
+    float pi0 = 1.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        float pr = (float)((double)ub[j] / (double)(float)d.fcount[c[j]]);
+        if (j == 0) pi0 = pr;
+        else if (pi0 > pr) pi0 = pr;
+    }
+    return pi0 >= d.thr;
+}
+
+/* Sparse restatement: a quad can be full only if it holds member 0, so the
+ * quads of member-0 cells are the only ones examined. */
+FilterOut filter_sparse(const Data& d, const uint32_t* c, uint32_t k) {
+    FilterOut out;
+    out.ub.assign(k, 0);
+    const oracle_grid& g = d.g;
+    uint32_t m = k < 8 ? k : 8;
+    if (g.gx >= 2 && g.gy >= 2) {
+        std::unordered_set<uint64_t> quads;   /* key = by*gx + bx */
+        std::unordered_set<uint64_t> cells;
+        for (size_t ci = 0; ci < d.cellKeys.size(); ++ci) {
+            uint64_t cell = d.cellKeys[ci];
+            if (d.count(cell, c[0]) == 0) continue;
+            uint64_t cx = cell % g.gx, cy = cell / g.gx;
+            for (int dy = -1; dy <= 0; ++dy)
+                for (int dx = -1; dx <= 0; ++dx) {
+                    int64_t bx = (int64_t)cx + dx, by = (int64_t)cy + dy;
+                    if (bx < 0 || by < 0 || bx > (int64_t)g.gx - 2 || by > (int64_t)g.gy - 2)
+                        continue;
+                    uint64_t qk = (uint64_t)by * g.gx + (uint64_t)bx;
+                    if (quads.count(qk)) continue;
+                    quads.insert(qk);
+                    bool full = true;
+                    for (uint32_t j = 0; j < m && full; ++j) {
+                        uint64_t s = 0;
+                        for (int yy = 0; yy < 2; ++yy)
+                            for (int xx = 0; xx < 2; ++xx)
+                                s += d.count((uint64_t)(by + yy) * g.gx + (uint64_t)(bx + xx), c[j]);
+                        if (s == 0) full = false;
+                    }
+                    if (!full) continue;
+                    for (int yy = 0; yy < 2; ++yy)
+                        for (int xx = 0; xx < 2; ++xx)
+                            cells.insert((uint64_t)(by + yy) * g.gx + (uint64_t)(bx + xx));
+                }
+        }
+        for (uint64_t cell : cells)
+            for (uint32_t j = 0; j < m; ++j) out.ub[j] += d.count(cell, c[j]);
+    }
+    out.pass = threshold_pass(d, c, k, out.ub.data());
+    return out;
+}
+
+/* Literal dense restatement (every quad of the grid, claim flags per cell). */
+FilterOut filter_dense(const Data& d, const uint32_t* c, uint32_t k) {
+    FilterOut out;
+    out.ub.assign(k, 0);
+    const oracle_grid& g = d.g;
+    uint32_t m = k < 8 ? k : 8;
+    std::vector<uint8_t> processed(g.total_cells, 0);
+    for (uint64_t by = 0; by + 1 < g.gy; ++by)
+        for (uint64_t bx = 0; bx + 1 < g.gx; ++bx) {
+            uint64_t cnt[8][2][2];
+            bool done = false;
+            for (uint32_t j = 0; j < m; ++j) {
+                uint64_t s = 0;
+                for (int yy = 0; yy < 2; ++yy)
+                    for (int xx = 0; xx < 2; ++xx) {
+                        cnt[j][xx][yy] = d.count((by + yy) * g.gx + bx + xx, c[j]);
+                        s += cnt[j][xx][yy];
+                    }
+                if (s == 0) done = true;
+            }
+            if (done) continue;
+            for (int yy = 0; yy < 2; ++yy)
+                for (int xx = 0; xx < 2; ++xx) {
+                    uint64_t cid = (by + yy) * g.gx + bx + xx;
+                    if (processed[cid]) continue;
+                    processed[cid] = 1;
+                    for (uint32_t j = 0; j < m; ++j) out.ub[j] += cnt[j][xx][yy];
+                }
+        }
+    out.pass = threshold_pass(d, c, k, out.ub.data());
+    return out;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Refinement: slot counting with bitmaps and participation index           */
+/* ------------------------------------------------------------------------ */
+
+struct Refined {
+    uint64_t rows = 0;
+    std::vector<uint64_t> num;   /* k numerators as getParticipationIndex sums them */
+    float pi = 1.0f;
+    uint32_t argmin = 0;
+    std::vector<uint32_t> slots; /* per parent row (or per anchor for k = 2) */
+};
+
+/* Codes/DeviceProcess.cu:108-132 (getParticipationIndex): window sums over a
+ * word-per-bit bitmap, float ratio, strict-< minimum starting at 1.0. */
+void participation(const Data& d, const uint32_t* c, uint32_t k, const std::vector<uint8_t>& bm,
+                   Refined& out) {
+    out.num.assign(k, 0);
+    float PI = 1.0f;
+    uint32_t from = 0, to = 0;
+    out.argmin = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+        uint32_t total = d.fcount[c[j]];
+        if (j == 0) {
+            from = 0;
+            to = total;
+        } else {
+            from = to - 1;
+            to = from + total + 1;
+        }
+        uint64_t s = 0;
+        for (uint64_t p = from; p + 1 < (uint64_t)to; ++p) s += bm[p];   /* reduce(from, to-1) */
+        out.num[j] = s;
+        float pr = (float)s / (float)total;
+        if (pr < PI) {
+            PI = pr;
+            out.argmin = j;
+        }
+    }
+    out.pi = PI;
+}
+
+inline void set_bit(std::vector<uint8_t>& bm, uint64_t i) {
+    __atomic_store_n(&bm[i], (uint8_t)1, __ATOMIC_RELAXED);
+}
+
+/* Degree 2: degree2TableSlotCounter_Kernel (DeviceProcess_Kernel.h:12-55).
+ * Bitmap layout: first feature at TID, second at b - secondstart + (n0-1). */
+Refined refine2(const Data& d, uint32_t f0, uint32_t f1) {
+    Refined out;
+    uint32_t start = d.fstart[f0], n0 = d.fcount[f0], n1 = d.fcount[f1];
+    uint32_t secondstart = d.fstart[f1];
+    std::vector<uint8_t> bm((size_t)n0 + n1, 0);
+    out.slots.assign(n0, 0);
+    uint64_t rows = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : rows)
+    for (int64_t tid = 0; tid < (int64_t)n0; ++tid) {
+        uint32_t a = start + (uint32_t)tid;
+        uint32_t cnt = 0;
+        for_neighbor_cells(d.g, d.cellOf[a], [&](uint64_t nc) {
+            int64_t r = d.run(nc, f1);
+            if (r < 0) return;
+            for (uint64_t p = d.runStart[r]; p < d.runStart[r] + d.runCount[r]; ++p) {
+                uint32_t b = d.sorted[p];
+                if (d.near(a, b)) {
+                    cnt++;
+                    set_bit(bm, (uint64_t)tid);
+                    set_bit(bm, (uint64_t)(b - secondstart) + (n0 - 1));
+                }
+            }
+        });
+        out.slots[tid] = cnt;
+        rows += cnt;
+    }
+    out.rows = rows;
+    uint32_t c[2] = {f0, f1};
+    participation(d, c, 2, bm, out);
+    return out;
+}
+
+/* degree2TableGenerator_Kernel (DeviceProcess_Kernel.h:56-100): rows (a,b)
+ * ordered by anchor, neighbour cell, then b. */
+std::vector<uint32_t> fill2(const Data& d, uint32_t f0, uint32_t f1, const Refined& ref) {
+    uint32_t start = d.fstart[f0], n0 = d.fcount[f0];
+    std::vector<uint64_t> off((size_t)n0 + 1, 0);
+    for (uint32_t t = 0; t < n0; ++t) off[t + 1] = off[t] + ref.slots[t];
+    std::vector<uint32_t> tab(off[n0] * 2);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t tid = 0; tid < (int64_t)n0; ++tid) {
+        uint32_t a = start + (uint32_t)tid;
+        uint64_t o = off[tid] * 2;
+        for_neighbor_cells(d.g, d.cellOf[a], [&](uint64_t nc) {
+            int64_t r = d.run(nc, f1);
+            if (r < 0) return;
+            for (uint64_t p = d.runStart[r]; p < d.runStart[r] + d.runCount[r]; ++p) {
+                uint32_t b = d.sorted[p];
+                if (d.near(a, b)) {
+                    tab[o++] = a;
+                    tab[o++] = b;
+                }
+            }
+        });
+    }
+    return tab;
+}
+
+/* Degree k >= 3: generalInstanceTableSlotCounter_Kernel
+ * (DeviceProcess_Kernel.h:255-316).  Bitmap offsets are the running sums of
+ * member counts. */
+Refined refinek(const Data& d, const uint32_t* c, uint32_t k, const std::vector<uint32_t>& parent) {
+    Refined out;
+    uint32_t km1 = k - 1;
+    uint64_t prow = parent.size() / km1;
+    uint64_t bmsize = 0;
+    for (uint32_t j = 0; j < k; ++j) bmsize += d.fcount[c[j]];
+    std::vector<uint8_t> bm(bmsize, 0);
+    std::vector<uint64_t> offs(k, 0);
+    for (uint32_t j = 1; j < k; ++j) offs[j] = offs[j - 1] + d.fcount[c[j - 1]];
+    uint32_t last = c[k - 1];
+    out.slots.assign(prow, 0);
+    uint64_t rows = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : rows)
+    for (int64_t tid = 0; tid < (int64_t)prow; ++tid) {
+        const uint32_t* r = &parent[(size_t)tid * km1];
+        uint32_t cnt = 0;
+        for_neighbor_cells(d.g, d.cellOf[r[0]], [&](uint64_t nc) {
+            int64_t ru = d.run(nc, last);
+            if (ru < 0) return;
+            for (uint64_t p = d.runStart[ru]; p < d.runStart[ru] + d.runCount[ru]; ++p) {
+                uint32_t b = d.sorted[p];
+                bool ok = true;
+                for (uint32_t i = 0; i < km1 && ok; ++i)
+                    if (!d.near(r[i], b)) ok = false;
+                if (!ok) continue;
+                cnt++;
+                for (uint32_t i = 0; i < km1; ++i)
+                    set_bit(bm, (uint64_t)(r[i] - d.fstart[c[i]]) + offs[i]);
+                set_bit(bm, (uint64_t)(b - d.fstart[last]) + offs[km1]);
+            }
+        });
+        out.slots[tid] = cnt;
+        rows += cnt;
+    }
+    out.rows = rows;
+    participation(d, c, k, bm, out);
+    return out;
+}
+
+/* generateInstanceTableGeneral_Kernel (DeviceProcess_Kernel.h:318-385). */
+std::vector<uint32_t> fillk(const Data& d, const uint32_t* c, uint32_t k,
+                            const std::vector<uint32_t>& parent, const Refined& ref) {
+    uint32_t km1 = k - 1;
+    uint64_t prow = parent.size() / km1;
+    std::vector<uint64_t> off(prow + 1, 0);
+    for (uint64_t t = 0; t < prow; ++t) off[t + 1] = off[t] + ref.slots[t];
+    std::vector<uint32_t> tab(off[prow] * k);
+    uint32_t last = c[k - 1];
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t tid = 0; tid < (int64_t)prow; ++tid) {
+        if (ref.slots[tid] == 0) continue;
+        const uint32_t* r = &parent[(size_t)tid * km1];
+        uint64_t o = off[tid] * k;
+        for_neighbor_cells(d.g, d.cellOf[r[0]], [&](uint64_t nc) {
+            int64_t ru = d.run(nc, last);
+            if (ru < 0) return;
+            for (uint64_t p = d.runStart[ru]; p < d.runStart[ru] + d.runCount[ru]; ++p) {
+                uint32_t b = d.sorted[p];
+                bool ok = true;
+                for (uint32_t i = 0; i < km1 && ok; ++i)
+                    if (!d.near(r[i], b)) ok = false;
+                if (!ok) continue;
+                for (uint32_t i = 0; i < km1; ++i) tab[o++] = r[i];
+                tab[o++] = b;
+            }
+        });
+    }
+    return tab;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Apriori candidate generation                                             */
+/* ------------------------------------------------------------------------ */
+
+/* subsetGen (colocationFinder.cpp:598-616) emits the (n-1)-subsets of a
+ * candidate in lexicographic position order: subset i drops position n-1-i. */
+void subsets_lex(const std::vector<uint32_t>& inter, std::vector<std::vector<uint32_t>>& out) {
+    size_t n = inter.size();
+    out.clear();
+    for (size_t i = 0; i < n; ++i) {
+        size_t drop = n - 1 - i;
+        std::vector<uint32_t> s;
+        for (size_t t = 0; t < n; ++t)
+            if (t != drop) s.push_back(inter[t]);
+        out.push_back(s);
+    }
+}
+
+/* checkSubset (colocationFinder.cpp:618-634): linear search. */
+bool check_subset(const std::vector<uint32_t>& prev, size_t nprev, const std::vector<uint32_t>& s) {
+    size_t deg = s.size();
+    for (size_t i = 0; i < nprev; ++i) {
+        bool eq = true;
+        for (size_t j = 0; j < deg; ++j)
+            if (prev[i * deg + j] != s[j]) {
+                eq = false;
+                break;
+            }
+        if (eq) return true;
+    }
+    return nprev == 0;   /* the reference's flag starts true */
+}
+
+/* candidateColocationGeneral (colocationFinder.cpp:517-557): join on equal
+ * (k-2)-prefix, check subsets 2..k-1 (generateandCheckSubsets, 669-679),
+ * and BREAK out of the inner loop on the first failing subset check. */
+std::vector<uint32_t> apriori(const std::vector<uint32_t>& prev, size_t nprev, uint32_t degree) {
+    std::vector<uint32_t> cand;
+    uint32_t lastIndex = degree - 2;
+    std::vector<std::vector<uint32_t>> subs;
+    for (size_t i = 0; i < nprev; ++i) {
+        bool flag = true;
+        for (size_t j = i + 1; j < nprev; ++j) {
+            for (size_t k = 0; k < lastIndex; ++k)
+                if (prev[i * (degree - 1) + k] != prev[j * (degree - 1) + k]) {
+                    flag = false;
+                    break;
+                }
+            if (flag && prev[i * (degree - 1) + lastIndex] < prev[j * (degree - 1) + lastIndex]) {
+                std::vector<uint32_t> inter(prev.begin() + i * (degree - 1),
+                                            prev.begin() + (i + 1) * (degree - 1));
+                inter.push_back(prev[j * (degree - 1) + lastIndex]);
+                subsets_lex(inter, subs);
+                flag = true;
+                for (size_t s = 2; s < degree; ++s) {
+                    flag = check_subset(prev, nprev, subs[s]);
+                    if (!flag) break;
+                }
+                if (!flag) break;
+                cand.insert(cand.end(), inter.begin(), inter.end());
+            } else {
+                break;
+            }
+        }
+    }
+    return cand;
+}
+
+/* getIndex (colocationFinder.cpp:703-718) */
+int64_t find_pattern(const std::vector<uint32_t>& list, size_t cnt, uint32_t deg, const uint32_t* p) {
+    for (size_t i = 0; i < cnt; ++i) {
+        bool eq = true;
+        for (uint32_t j = 0; j < deg; ++j)
+            if (list[i * deg + j] != p[j]) {
+                eq = false;
+                break;
+            }
+        if (eq) return (int64_t)i;
+    }
+    return -1;
+}
+
+}  // namespace
+
+/* ------------------------------------------------------------------------ */
+/* Result                                                                   */
+/* ------------------------------------------------------------------------ */
+
+struct OLevel {
+    uint32_t k = 0;
+    std::vector<uint32_t> cand;
+    std::vector<uint64_t> ub, num, rows;
+    std::vector<uint8_t> pass, prevalent;
+    std::vector<float> pi;
+    std::vector<uint32_t> argmin;
+    std::vector<std::vector<uint32_t>> tables;   /* per candidate (kept on request) */
+    std::vector<uint8_t> has_table;
+};
+
+struct oracle_result {
+    int status = 0;
+    uint64_t unresolved = 0;    /* ambiguous comparisons without a device outcome */
+    std::vector<OLevel> levels;
+};
+
+extern "C" {
+
+int oracle_make_grid(float min_x, float min_y, float max_x, float max_y, float R, oracle_grid* g) {
+    return make_grid(min_x, min_y, max_x, max_y, R, g);
+}
+
+uint64_t oracle_cell_ids(const oracle_grid* g, const float* x, const float* y, uint64_t n,
+                         uint64_t* cell_out) {
+    uint64_t bad = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        cell_out[i] = cell_of(*g, x[i], y[i]);
+        if (cell_out[i] >= g->total_cells) bad++;
+    }
+    return bad;
+}
+
+float oracle_sqdist(float x1, float y1, float x2, float y2) { return sqdist(x1, y1, x2, y2); }
+
+int oracle_cell_adjacent(const oracle_grid* g, uint64_t c, uint64_t nb) {
+    int hit = 0;
+    for_neighbor_cells(*g, c, [&](uint64_t nc) {
+        if (nc == nb) hit = 1;
+    });
+    return hit;
+}
+
+int oracle_mine(const float* x, const float* y, const uint32_t* feat, uint64_t n, uint32_t nfeat,
+                const float bounds[4], float R, float thr, uint32_t max_k, int threads,
+                int keep_tables, const uint64_t* res_keys, const uint8_t* res_le, uint64_t nres,
+                oracle_result** out) {
+    oracle_result* res = new oracle_result();
+    *out = res;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    if (n == 0 || nfeat < 2) return res->status = 0;
+    Data d;
+    int st = build_data(d, x, y, feat, n, nfeat, bounds, R, thr);
+    if (st) return res->status = st;
+    d.res_keys = res_keys;
+    d.res_le = res_le;
+    d.nres = res_keys ? nres : 0;
+    struct Tally {
+        oracle_result* r;
+        const Data& d;
+        ~Tally() { r->unresolved = d.unresolved.load(); }
+    } tally{res, d};
+
+    /* ---- degree 2 (degree2Processing, colocationFinder.cpp:256-425) ---- */
+    std::vector<uint32_t> cands;
+    for (uint32_t i = 0; i + 1 < nfeat; ++i)       /* 75-82 */
+        for (uint32_t j = i + 1; j < nfeat; ++j) {
+            cands.push_back(i);
+            cands.push_back(j);
+        }
+    uint32_t k = 2;
+    std::vector<uint32_t> prev;                    /* prevalent patterns of level k */
+    std::vector<size_t> prevIdx;                   /* their candidate index */
+    std::vector<std::vector<uint32_t>> prevTables; /* table per prevalent pattern (if built) */
+    std::vector<std::vector<uint32_t>> parentTables;
+    std::vector<uint32_t> parentList;              /* prevalent (k-1)-patterns */
+    while (true) {
+        size_t C = cands.size() / k;
+        OLevel L;
+        L.k = k;
+        L.cand = cands;
+        L.ub.assign(C * k, 0);
+        L.num.assign(C * k, 0);
+        L.rows.assign(C, 0);
+        L.pass.assign(C, 0);
+        L.prevalent.assign(C, 0);
+        L.pi.assign(C, -1.0f);
+        L.argmin.assign(C, 0);
+        std::vector<Refined> refs(C);
+        /* filter (2 in the order of the candidates) */
+        std::vector<FilterOut> fo(C);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int64_t c = 0; c < (int64_t)C; ++c) fo[c] = filter_sparse(d, &cands[c * k], k);
+        for (size_t c = 0; c < C; ++c) {
+            for (uint32_t j = 0; j < k; ++j) L.ub[c * k + j] = fo[c].ub[j];
+            L.pass[c] = fo[c].pass;
+        }
+        /* refinement per surviving candidate */
+        prev.clear();
+        prevIdx.clear();
+        for (size_t c = 0; c < C; ++c) {
+            if (!L.pass[c]) continue;
+            const uint32_t* cc = &cands[c * k];
+            if (k == 2) {
+                refs[c] = refine2(d, cc[0], cc[1]);
+            } else {
+                int64_t pi = find_pattern(parentList, parentList.size() / (k - 1), k - 1, cc);
+                if (pi < 0) return res->status = 5;
+                refs[c] = refinek(d, cc, k, parentTables[pi]);
+            }
+            L.rows[c] = refs[c].rows;
+            for (uint32_t j = 0; j < k; ++j) L.num[c * k + j] = refs[c].num[j];
+            L.pi[c] = refs[c].pi;
+            L.argmin[c] = refs[c].argmin;
+            if (!(refs[c].pi < thr)) {                   /* cpp:335, cpp:827 */
+                L.prevalent[c] = 1;
+                prev.insert(prev.end(), cc, cc + k);
+                prevIdx.push_back(c);
+            }
+        }
+        size_t P = prevIdx.size();
+        /* next-level candidates (candidateColocationGeneral(k+1)) */
+        std::vector<uint32_t> next;
+        if (P > 0 && (max_k == 0 || k + 1 <= max_k) && k + 1 <= nfeat) next = apriori(prev, P, k + 1);
+        size_t Cn = next.size() / (k + 1);
+        /* tables for prevalent patterns that prefix a next candidate
+         * (calcInstanceTablePatternIndexes, cpp:1042-1066 / cpp:364-372) */
+        std::vector<uint8_t> need(P, 0);
+        for (size_t i = 0; i < Cn; ++i) {
+            int64_t ix = find_pattern(prev, P, k, &next[i * (k + 1)]);
+            if (ix >= 0) need[ix] = 1;
+        }
+        std::vector<std::vector<uint32_t>> newTables(P);
+        L.tables.assign(keep_tables ? C : 0, {});
+        L.has_table.assign(C, 0);
+        for (size_t p = 0; p < P; ++p) {
+            if (!need[p]) continue;
+            size_t c = prevIdx[p];
+            const uint32_t* cc = &cands[c * k];
+            if (k == 2) {
+                newTables[p] = fill2(d, cc[0], cc[1], refs[c]);
+            } else {
+                int64_t pi = find_pattern(parentList, parentList.size() / (k - 1), k - 1, cc);
+                newTables[p] = fillk(d, cc, k, parentTables[pi], refs[c]);
+            }
+            L.has_table[c] = 1;
+            if (keep_tables) L.tables[c] = newTables[p];
+        }
+        res->levels.push_back(std::move(L));
+        if (Cn == 0) break;
+        parentTables.swap(newTables);
+        parentList = prev;
+        cands = next;
+        k++;
+    }
+    return res->status = 0;
+}
+
+void oracle_free(oracle_result* r) { delete r; }
+int oracle_status(const oracle_result* r) { return r->status; }
+uint64_t oracle_unresolved(const oracle_result* r) { return r->unresolved; }
+uint32_t oracle_num_levels(const oracle_result* r) { return (uint32_t)r->levels.size(); }
+uint32_t oracle_level_k(const oracle_result* r, uint32_t li) { return r->levels[li].k; }
+uint64_t oracle_level_ncand(const oracle_result* r, uint32_t li) {
+    return r->levels[li].cand.size() / r->levels[li].k;
+}
+
+void oracle_level_get(const oracle_result* r, uint32_t li, uint32_t* cand, uint64_t* ub, uint8_t* pass,
+                      uint64_t* rows, uint64_t* num, float* pi, uint8_t* prevalent, uint32_t* argmin) {
+    const OLevel& L = r->levels[li];
+    size_t C = L.cand.size() / L.k;
+    if (cand) std::memcpy(cand, L.cand.data(), L.cand.size() * 4);
+    if (ub) std::memcpy(ub, L.ub.data(), L.ub.size() * 8);
+    if (pass) std::memcpy(pass, L.pass.data(), C);
+    if (rows) std::memcpy(rows, L.rows.data(), C * 8);
+    if (num) std::memcpy(num, L.num.data(), L.num.size() * 8);
+    if (pi) std::memcpy(pi, L.pi.data(), C * 4);
+    if (prevalent) std::memcpy(prevalent, L.prevalent.data(), C);
+    if (argmin) std::memcpy(argmin, L.argmin.data(), C * 4);
+}
+
+uint64_t oracle_table(const oracle_result* r, uint32_t li, uint64_t ci, uint32_t* out) {
+    const OLevel& L = r->levels[li];
+    if (ci >= L.tables.size() || !L.has_table[ci]) return UINT64_MAX;
+    const auto& t = L.tables[ci];
+    if (out) std::memcpy(out, t.data(), t.size() * 4);
+    return t.size() / L.k;
+}
+
+uint64_t oracle_neighbors(const float* x, const float* y, const uint32_t* feat, uint64_t n,
+                          uint32_t nfeat, const float bounds[4], float R, const uint64_t* res_keys,
+                          const uint8_t* res_le, uint64_t nres, uint64_t* offs, uint32_t* nbr,
+                          uint64_t* n_unresolved) {
+    Data d;
+    if (build_data(d, x, y, feat, n, nfeat, bounds, R, 0.0f)) return UINT64_MAX;
+    d.res_keys = res_keys;
+    d.res_le = res_le;
+    d.nres = res_keys ? nres : 0;
+    std::vector<std::vector<uint32_t>> lists(n);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t a = 0; a < (int64_t)n; ++a) {
+        for (uint32_t f = feat[a] + 1; f < nfeat; ++f) {
+            for_neighbor_cells(d.g, d.cellOf[a], [&](uint64_t nc) {
+                int64_t r = d.run(nc, f);
+                if (r < 0) return;
+                for (uint64_t p = d.runStart[r]; p < d.runStart[r] + d.runCount[r]; ++p) {
+                    uint32_t b = d.sorted[p];
+                    if (d.near((uint32_t)a, b)) lists[a].push_back(b);
+                }
+            });
+        }
+    }
+    uint64_t tot = 0;
+    for (uint64_t a = 0; a < n; ++a) {
+        if (offs) offs[a] = tot;
+        if (nbr) std::memcpy(nbr + tot, lists[a].data(), lists[a].size() * 4);
+        tot += lists[a].size();
+    }
+    if (offs) offs[n] = tot;
+    if (n_unresolved) *n_unresolved = d.unresolved.load();
+    return tot;
+}
+
+void oracle_sq_decide_batch(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,
+                            float R2, uint8_t* le, uint8_t* ambiguous, float* value) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        SqDecision dc = sq_decide(x1[i], y1[i], x2[i], y2[i], R2);
+        le[i] = dc.le;
+        ambiguous[i] = dc.ambiguous;
+        if (value) value[i] = sqdist(x1[i], y1[i], x2[i], y2[i]);
+    }
+}
+
+int oracle_sq_decide(float x1, float y1, float x2, float y2, float R2, int* ambiguous) {
+    SqDecision dc = sq_decide(x1, y1, x2, y2, R2);
+    if (ambiguous) *ambiguous = dc.ambiguous ? 1 : 0;
+    return dc.le ? 1 : 0;
+}
+
+/* Every pair of points of different features whose comparison with R^2 an
+ * exact tie could flip.  Candidate pairs come from a uniform grid of cell
+ * size R over the true coordinates (a 5x5 stencil covers every pair at
+ * distance <= 2R), so the set does not depend on the reference grid. */
+uint64_t oracle_ambiguous_pairs(const float* x, const float* y, const uint32_t* feat, uint64_t n,
+                                float R, uint64_t* keys, uint64_t cap) {
+    float R2 = R * R;
+    double w = (double)R;
+    std::vector<std::pair<uint64_t, uint32_t>> cells(n);
+    auto key_of = [&](int64_t cx, int64_t cy) {
+        return ((uint64_t)(cx + (1ll << 31)) << 32) ^ (uint64_t)(cy + (1ll << 31));
+    };
+    std::vector<int64_t> cx(n), cy(n);
+    for (uint64_t i = 0; i < n; ++i) {
+        cx[i] = (int64_t)std::floor((double)x[i] / w);
+        cy[i] = (int64_t)std::floor((double)y[i] / w);
+        cells[i] = {key_of(cx[i], cy[i]), (uint32_t)i};
+    }
+    std::sort(cells.begin(), cells.end());
+    std::vector<uint64_t> found;
+    for (uint64_t i = 0; i < n; ++i) {
+        for (int dy = -2; dy <= 2; ++dy)
+            for (int dx = -2; dx <= 2; ++dx) {
+                uint64_t k = key_of(cx[i] + dx, cy[i] + dy);
+                auto it = std::lower_bound(cells.begin(), cells.end(), std::make_pair(k, 0u));
+                for (; it != cells.end() && it->first == k; ++it) {
+                    uint32_t j = it->second;
+                    if (j <= i || feat[j] == feat[i]) continue;
+                    SqDecision dc = sq_decide(x[i], y[i], x[j], y[j], R2);
+                    if (dc.ambiguous) found.push_back(((uint64_t)i << 32) | j);
+                }
+            }
+    }
+    std::sort(found.begin(), found.end());
+    if (keys) std::memcpy(keys, found.data(), std::min<uint64_t>(found.size(), cap) * 8);
+    return found.size();
+}
+
+int oracle_filter_dense(const float* x, const float* y, const uint32_t* feat, uint64_t n,
+                        uint32_t nfeat, const float bounds[4], float R, float thr,
+                        const uint32_t* cand, uint64_t ncand, uint32_t k, uint64_t* ub,
+                        uint8_t* pass) {
+    Data d;
+    int st = build_data(d, x, y, feat, n, nfeat, bounds, R, thr);
+    if (st) return st;
+    for (uint64_t c = 0; c < ncand; ++c) {
+        FilterOut f = filter_dense(d, cand + c * k, k);
+        for (uint32_t j = 0; j < k; ++j) ub[c * k + j] = f.ub[j];
+        pass[c] = f.pass;
+    }
+    return 0;
+}
+
+uint64_t oracle_apriori(const uint32_t* prev, uint64_t nprev, uint32_t k, uint32_t* out,
+                        uint64_t out_cap) {
+    std::vector<uint32_t> p(prev, prev + nprev * (k - 1));
+    std::vector<uint32_t> c = apriori(p, nprev, k);
+    uint64_t nc = c.size() / k;
+    if (out) std::memcpy(out, c.data(), std::min<uint64_t>(nc, out_cap) * k * 4);
+    return nc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Parsing                                                                  */
+/* ------------------------------------------------------------------------ */
+
+namespace {
+/* boost::escaped_list_separator<char> defaults: separator ',', quote '"',
+ * escape '\\' (the tokenizer used at colocationFinder.cpp:156). */
+std::vector<std::string> split_csv(const std::string& line) {
+    std::vector<std::string> out;
+    std::string cur;
+    bool inq = false;
+    for (size_t i = 0; i < line.size(); ++i) {
+        char ch = line[i];
+        if (ch == '\\' && i + 1 < line.size()) {
+            char nx = line[++i];
+            cur.push_back(nx == 'n' ? '\n' : nx);
+        } else if (ch == '"') {
+            inq = !inq;
+        } else if (ch == ',' && !inq) {
+            out.push_back(cur);
+            cur.clear();
+        } else {
+            cur.push_back(ch);
+        }
+    }
+    out.push_back(cur);
+    return out;
+}
+bool to_float(const std::string& s, float* v) {          /* std::stof */
+    const char* b = s.c_str();
+    char* e = nullptr;
+    *v = std::strtof(b, &e);
+    return e != b;
+}
+bool to_int(const std::string& s, long* v) {             /* std::stoi */
+    const char* b = s.c_str();
+    char* e = nullptr;
+    *v = std::strtol(b, &e, 10);
+    return e != b && *v >= INT32_MIN && *v <= INT32_MAX;
+}
+bool next_line(std::ifstream& in, std::string& line) {
+    bool ok = (bool)std::getline(in, line);
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    return ok;
+}
+}  // namespace
+
+int oracle_parse_csv(const char* path, uint64_t* n, uint32_t* nfeat, float* x, float* y,
+                     uint32_t* feat, float bounds[4], char* names, uint64_t names_cap) {
+    std::ifstream in(path);
+    if (!in.is_open()) return 1;
+    std::string line;
+    next_line(in, line);
+    long N;
+    if (!to_int(line, &N) || N < 0) return 2;
+    uint64_t cnt = 0;
+    uint32_t F = 0;
+    size_t last = (size_t)-1;
+    std::string nm;
+    next_line(in, line);
+    while (!line.empty()) {
+        std::vector<std::string> v = split_csv(line);
+        if (v.size() < 3) return 2;
+        long fid;
+        if (!to_int(v[0], &fid) || fid == -1) return 2;
+        if (last == (size_t)-1 || (size_t)fid != last) {
+            last = (size_t)fid;
+            if (F > 0) nm.push_back('\n');
+            nm += v[0];
+            F++;
+        }
+        float xv, yv;
+        if (!to_float(v[1], &xv) || !to_float(v[2], &yv)) return 2;
+        if (x && cnt < (uint64_t)N) {
+            feat[cnt] = F - 1;
+            x[cnt] = xv;
+            y[cnt] = yv;
+        }
+        cnt++;
+        line.clear();
+        next_line(in, line);
+    }
+    if (cnt != (uint64_t)N) return 3;
+    line.clear();
+    next_line(in, line);
+    std::vector<std::string> v = split_csv(line);
+    if (v.size() < 4) return 2;
+    float bb[4];
+    for (int i = 0; i < 4; ++i)
+        if (!to_float(v[i], &bb[i])) return 2;
+    if (bounds) std::memcpy(bounds, bb, sizeof(bb));
+    *n = cnt;
+    *nfeat = F;
+    if (names && names_cap > 0) {
+        size_t m = std::min<size_t>(nm.size(), names_cap - 1);
+        std::memcpy(names, nm.data(), m);
+        names[m] = 0;
+    }
+    return 0;
+}
+
+int oracle_parse_params(const char* path, float* R, float* thr, uint32_t* filter_flag) {
+    std::ifstream ifs(path);
+    if (!ifs.is_open()) return 1;
+    float r = 0, t = 0;
+    unsigned f = 0;
+    ifs >> r;
+    ifs >> t;
+    ifs >> f;
+    if (ifs.fail() && !ifs.eof()) return 2;
+    *R = r;
+    *thr = t;
+    *filter_flag = f;
+    return 0;
+}
+
+}  // extern "C"

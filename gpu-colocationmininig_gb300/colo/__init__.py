@@ -25,6 +25,9 @@ STATUS = {0: "COLO_OK", 1: "COLO_ERR_ARG", 2: "COLO_ERR_IO", 3: "COLO_ERR_PARSE"
           5: "COLO_ERR_CUDA", 6: "COLO_ERR_NOMEM", 7: "COLO_ERR_TIMEOUT", 8: "COLO_ERR_CAPACITY",
           9: "COLO_ERR_NO_DEVICE", 10: "COLO_ERR_INTERNAL"}
 MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
+COUNTERS = ["launches", "npl_entries", "neighbors", "rows_written", "fallbacks", "points", "cells", "runs",
+            "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
+            "nrl_entries", "refined"]
 
 # Every symbol declared in include/colo.h (checked by the CPU tests).
 EXPORTS = [
@@ -35,7 +38,7 @@ EXPORTS = [
     "colo_mine_batch", "colo_result_num_levels", "colo_result_level_size", "colo_result_level_candidates",
     "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
-    "colo_stage_filter", "colo_stage_sqdist",
+    "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
 ]
 
 
@@ -102,7 +105,10 @@ def load(build: bool = True) -> C.CDLL:
         "colo_result_table": (C.c_uint64, [_P, C.c_uint32, C.c_uint64, _u32p]),
         "colo_result_write_patterns": (C.c_int, [_P, _P, C.c_char_p]),
         "colo_result_times": (C.c_int, [_P, C.POINTER(C.c_double)]),
-        "colo_result_counters": (C.c_int, [_P, _u64p]),
+        "colo_result_counters": (C.c_int, [_P, _u64p, C.c_uint32]),
+        "colo_result_num_kernels": (C.c_uint32, [_P]),
+        "colo_result_kernel": (C.c_int, [_P, C.c_uint32, C.c_char_p, C.c_size_t, _u64p, C.POINTER(C.c_double)]),
+        "colo_ctx_stream": (C.c_void_p, [_P]),
         "colo_result_free": (None, [_P]),
         "colo_stage_cells": (C.c_int, [_P, _P, C.c_float, _u64p, _u64p, _u32p, _u32p, _u64p]),
         "colo_stage_neighbors": (C.c_int, [_P, _P, C.c_float, _u64p, _u32p, _u64p]),
@@ -118,7 +124,7 @@ def load(build: bool = True) -> C.CDLL:
 
 
 def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHED, max_size: int = 0,
-                   keep_tables: bool = False) -> Params:
+                   keep_tables: bool = False, profile: bool = False) -> Params:
     p = Params()
     load().colo_params_default(C.byref(p))
     p.distance = distance
@@ -126,6 +132,7 @@ def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHE
     p.mode = mode
     p.max_size = max_size
     p.keep_tables = 1 if keep_tables else 0
+    p.reserved[0] = 1 if profile else 0
     return p
 
 
@@ -195,9 +202,16 @@ class Result:
         t = (C.c_double * 8)()
         lib.colo_result_times(handle, t)
         self.times = dict(zip(["total", "upload", "bucket", "join", "filter", "refine", "fill", "apriori"], list(t)))
-        c = np.zeros(8, np.uint64)
-        lib.colo_result_counters(handle, _ptr(c, _u64p))
-        self.counters = dict(zip(["launches", "npl_points", "neighbors", "rows_written", "fallbacks"], c[:5].tolist()))
+        c = np.zeros(16, np.uint64)
+        lib.colo_result_counters(handle, _ptr(c, _u64p), 16)
+        self.counters = dict(zip(COUNTERS, c.tolist()))
+        self.kernels = {}
+        for i in range(lib.colo_result_num_kernels(handle)):
+            name = C.create_string_buffer(64)
+            nl = C.c_uint64()
+            ms = C.c_double()
+            lib.colo_result_kernel(handle, i, name, 64, C.byref(nl), C.byref(ms))
+            self.kernels[name.value.decode()] = (int(nl.value), float(ms.value))
 
     def patterns(self):
         out = []
@@ -289,6 +303,9 @@ class Context:
         self.check(self.lib.colo_stage_sqdist(self.h, *[_ptr(v, _f32p) for v in a], len(out), _ptr(out, _f32p)),
                    "stage_sqdist")
         return out
+
+    def stream(self) -> int:
+        return int(self.lib.colo_ctx_stream(self.h) or 0)
 
     def close(self):
         if getattr(self, "h", None):

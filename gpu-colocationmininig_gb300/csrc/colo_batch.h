@@ -104,6 +104,7 @@ struct LevelWork {
     uint64_t ncand;
     uint64_t nchunks;
     unsigned long long* next;    // device work counter (persistent kernels)
+    unsigned long long* items;   // optional: sum of candidate-slice lengths examined
 };
 
 // count pass: slots + bitmaps; fill pass: rows; single pass: rows at

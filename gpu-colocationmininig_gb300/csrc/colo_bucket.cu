@@ -245,10 +245,13 @@ void bucket_points(Batch& b) {
     DevBuf<uint64_t> keys;
     keys.alloc(n, s);
     b.sid.alloc(n, s);
+    {
+    KScope ks("cell_keys");
     k_cell_keys<<<grid_for(n, 256), 256, 0, s>>>(n, b.x, b.y, b.feat, b.fjob.get(), b.grids.get(),
                                                   keys.get(), b.sid.get(), b.flags.get());
     COLO_LAUNCH_CHECK();
     count_launch();
+    }
     radix_sort_u64_u32(keys.get(), b.sid.get(), n, (int)b.key_bits, s);
 
     b.sx.alloc(n, s);
@@ -363,6 +366,7 @@ void build_neighborhoods(Batch& b) {
     b.npl_id.alloc(tp, s);
     b.npl_x.alloc(tp, s);
     b.npl_y.alloc(tp, s);
+    KScope ks("npl_fill");
     k_nl_fill<<<grid_for(M * 32, 256), 256, 0, s>>>(
         M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cstart.get(), b.crun.get(),
         b.rfeat.get(), b.rstart.get(), b.rcnt.get(), b.sid.get(), b.sx.get(), b.sy.get(),

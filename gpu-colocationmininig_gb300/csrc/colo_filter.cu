@@ -230,6 +230,7 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     uint64_t per = (b.M + blocks - 1) / blocks;
     per = (per + kFilterWarps - 1) / kFilterWarps * kFilterWarps;
     blocks = (b.M + per - 1) / per;
+    KScope ks("filter_pairs");
     k_filter_pairs<<<(unsigned)blocks, kFilterThreads, smem, s>>>(
         b.M, b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.W, b.crun.get(),
         b.rfeat.get(), b.rcnt.get(), d_job_off.get(), ub2.get(), acc_dim, per);
@@ -245,6 +246,7 @@ void filter_level(Batch& b, const uint32_t* d_cand, const uint32_t* d_driver, co
     uint64_t blocks = (nitems + 255) / 256;
     uint64_t cap = (uint64_t)b.sms * 16;
     if (blocks > cap) blocks = cap;
+    KScope ks("filter_level");
     k_filter_level<<<(unsigned)blocks, 256, 0, b.s>>>(
         nitems, ncand, k, d_cand, d_driver, d_item_off, b.frun_off.get(), b.frun.get(), b.rcell.get(),
         b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.W, b.crun.get(),

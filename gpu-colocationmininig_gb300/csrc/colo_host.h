@@ -39,10 +39,17 @@ struct LevelTrace {
     std::vector<uint8_t> has_table;
 };
 
+// counters[]: 0 kernel launches, 1 NPL entries, 2 neighbour entries E,
+// 3 table rows written, 4 fallback candidates, 5 points N, 6 occupied cells M,
+// 7 runs, 8 slice entries examined by count passes, 9 parent words read by
+// count passes, 10 table words written, 11 bitmap words, 12 H2D bytes,
+// 13 D2H bytes, 14 NRL entries, 15 refined candidates.
+constexpr int kNumCounters = 16;
 struct MineResult {
     std::vector<LevelTrace> levels;
     double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    uint64_t counters[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint64_t counters[kNumCounters] = {};
+    std::vector<KernelStat> kernels;   // per-kernel CUDA-event timing (when requested)
 };
 
 struct BatchStorage;   // owned device copies for multi-job batches
@@ -76,6 +83,7 @@ struct colo_dataset {
     colo::DevBuf<float> dx, dy;
     colo::DevBuf<uint32_t> dfeat;
     bool resident = false;
+    bool pinned = false;                     // host arrays page-locked for uploads
 };
 
 struct colo_result {

@@ -121,6 +121,86 @@ struct DevBuf {
 extern thread_local uint64_t g_launches;
 inline void count_launch(uint64_t n = 1) { g_launches += n; }
 
+// Optional per-kernel CUDA-event timing on the launching stream (enabled per
+// mine; used by the benchmark for its roofline figures).
+struct KernelStat {
+    std::string name;
+    uint64_t launches = 0;
+    double ms = 0;
+};
+
+struct KTimer {
+    bool on = false;
+    cudaStream_t s = 0;
+    struct Pending {
+        int slot;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pend;
+    std::vector<KernelStat> stats;
+    std::vector<cudaEvent_t> pool;
+    int open_slot = -1;
+    cudaEvent_t open_a = nullptr;
+    cudaEvent_t get() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        COLO_CUDA(cudaEventCreate(&e));
+        return e;
+    }
+    int slot(const char* name) {
+        for (size_t i = 0; i < stats.size(); ++i)
+            if (stats[i].name == name) return (int)i;
+        stats.push_back(KernelStat{name, 0, 0});
+        return (int)stats.size() - 1;
+    }
+    void begin(const char* name) {
+        if (!on) return;
+        open_slot = slot(name);
+        open_a = get();
+        COLO_CUDA(cudaEventRecord(open_a, s));
+    }
+    void end() {
+        if (!on || open_slot < 0) return;
+        cudaEvent_t b = get();
+        COLO_CUDA(cudaEventRecord(b, s));
+        pend.push_back({open_slot, open_a, b});
+        open_slot = -1;
+    }
+    void resolve() {
+        if (pend.empty()) return;
+        COLO_CUDA(cudaStreamSynchronize(s));
+        for (auto& p : pend) {
+            float ms = 0;
+            COLO_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+            stats[p.slot].ms += ms;
+            stats[p.slot].launches++;
+            pool.push_back(p.a);
+            pool.push_back(p.b);
+        }
+        pend.clear();
+    }
+    ~KTimer() {
+        for (auto& p : pend) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+extern thread_local KTimer* g_ktimer;
+struct KScope {
+    explicit KScope(const char* name) {
+        if (g_ktimer) g_ktimer->begin(name);
+    }
+    ~KScope() {
+        if (g_ktimer) g_ktimer->end();
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Primitives (colo_prims.cu)
 // ---------------------------------------------------------------------------

@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(256) k_join(
 template <int T>
 void run_join(Batch& b, bool fill, uint32_t* cnt) {
     const uint64_t n = b.N;
+    KScope ks(fill ? "join_fill" : "join_count");
     uint64_t threads = n * T;
     unsigned grid = (unsigned)((threads + 255) / 256);
     if (grid == 0) grid = 1;

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) k_level(
     uint64_t nchunks, const uint64_t* __restrict__ nb_off, const uint32_t* __restrict__ nb,
     const float* __restrict__ x, const float* __restrict__ y, const uint32_t* __restrict__ fstart,
     const uint32_t* __restrict__ fcount, const JobGrid* __restrict__ grids,
-    uint32_t* __restrict__ overflow) {
+    uint32_t* __restrict__ overflow, unsigned long long* __restrict__ items) {
     constexpr int KR = (K == 0) ? 1 : K;   // register members kept for K > 0
     const int lane = threadIdx.x & 31;
     const uint64_t ch = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(256) k_level(
     }
     const uint32_t excl = incl - len;
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (items && lane == 0 && total && MODE != MODE_FILL) atomicAdd(items, (unsigned long long)total);
     uint32_t mine = 0;               // hits of this lane's row so far
     uint64_t out0 = 0;
     if (MODE == MODE_FILL && valid) out0 = d.offs[row] - d.offs[0];   // offsets may be a slice of a longer scan
@@ -272,12 +273,13 @@ __global__ void k_level_pi(const CandDesc* __restrict__ cands, uint64_t ncand, u
 template <int MODE>
 void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
     if (w.nchunks == 0) return;
+    KScope ks(MODE == MODE_COUNT ? "level_count" : MODE == MODE_FILL ? "level_fill" : "level_single");
     uint64_t threads = w.nchunks * 32;
     unsigned grid = (unsigned)((threads + 255) / 256);
 #define COLO_LVL(KK)                                                                              \
     k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_off.get(), \
                                             b.nb.get(), b.x, b.y, b.fstart.get(), b.fcount.get(),  \
-                                            b.grids.get(), ovf)
+                                            b.grids.get(), ovf, w.items)
     switch (k) {
         case 2: COLO_LVL(2); break;
         case 3: COLO_LVL(3); break;
@@ -303,6 +305,7 @@ void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow
 
 void level_pi(Batch& b, const CandDesc* d_cands, uint64_t ncand, uint32_t k, uint64_t* d_stats) {
     if (ncand == 0) return;
+    KScope ks("level_pi");
     k_level_pi<<<(unsigned)ncand, 256, 0, b.s>>>(d_cands, ncand, k, b.fcount.get(), d_stats);
     COLO_LAUNCH_CHECK();
     count_launch();

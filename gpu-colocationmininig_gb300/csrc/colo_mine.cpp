@@ -105,6 +105,14 @@ colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn) {
 void upload_dataset(colo_dataset* ds, cudaStream_t s) {
     if (ds->resident) return;
     uint64_t n = ds->hp.x.size();
+    if (!ds->pinned && n) {
+        // page-lock the host arrays once so every upload is a direct DMA
+        bool ok = cudaHostRegister(ds->hp.x.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
+        ok = ok && cudaHostRegister(ds->hp.y.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
+        ok = ok && cudaHostRegister(ds->feat.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+        ds->pinned = true;
+    }
     ds->dx.alloc(n, s);
     ds->dy.alloc(n, s);
     ds->dfeat.alloc(n, s);
@@ -306,6 +314,16 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     cudaStream_t s = ctx->s;
     const auto t_all = Clock::now();
     g_launches = 0;
+    KTimer kt;
+    kt.s = s;
+    kt.on = (pv[0].reserved[0] & 1) != 0;
+    g_ktimer = &kt;
+    struct Unset {
+        ~Unset() { g_ktimer = nullptr; }
+    } unset;
+    uint64_t cnt_items = 0, cnt_parent = 0, cnt_fillw = 0, cnt_bmw = 0, cnt_d2h = 0, cnt_refined = 0;
+    DevBuf<unsigned long long> d_items;
+    d_items.alloc(1, s);
     Batch b;
     const int mode = pv[0].mode;
     const bool plain = (mode == COLO_MODE_PLAIN);
@@ -354,6 +372,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         bool any = false;
         for (auto& st : js) any |= (st.active && !st.cands.empty());
         if (!any) break;
+        if (k > (uint32_t)kMaxK)
+            throw StatusError{COLO_ERR_CAPACITY, "patterns larger than 32 features are not supported"};
         // ---- filter ----
         t0 = Clock::now();
         std::vector<LevelTrace*> tr(J, nullptr);
@@ -501,6 +521,10 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         ar.descs.alloc(ncand ? ncand : 1, s);
         ar.chunk_off.alloc(ncand + 1, s);
         std::vector<uint64_t> hstats(ncand * k * 4);
+        d_items.zero(s);
+        cnt_refined += ncand;
+        cnt_bmw += nwords;
+        for (uint64_t q = 0; q < ncand; ++q) cnt_parent += (uint64_t)(k - 1) * hd[q].prow;
         if (ncand) {
             COLO_CUDA(cudaMemcpyAsync(ar.descs.get(), hd.data(), ncand * sizeof(CandDesc), cudaMemcpyHostToDevice, s));
             COLO_CUDA(cudaMemcpyAsync(ar.chunk_off.get(), chunk_off.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
@@ -515,7 +539,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), 2 * ncand * 8, cudaMemcpyHostToDevice, s));
                 for (uint64_t q = 0; q < ncand; ++q) {
-                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
+                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr, d_items.get()};
                     level_count(b, w, k, false);
                     level_pi(b, ar.descs.get() + q, 1, k, ar.stats.get() + q * k * 4);
                     COLO_CUDA(cudaMemcpyAsync(hstats.data() + q * k * 4, ar.stats.get() + q * k * 4, k * 4 * 8,
@@ -523,7 +547,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
             } else {
-                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr};
+                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr, d_items.get()};
                 level_count(b, w, k, true);
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
                 COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
@@ -563,6 +587,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         std::vector<uint64_t> hrows(ncand);
         if (ncand)
             COLO_CUDA(cudaMemcpy(hrows.data(), ar.rows.get(), ncand * 8, cudaMemcpyDeviceToHost));
+        {
+            unsigned long long it = 0;
+            COLO_CUDA(cudaMemcpy(&it, d_items.get(), 8, cudaMemcpyDeviceToHost));
+            cnt_items += it;
+        }
+        cnt_d2h += ncand * 8 + hstats.size() * 8;
         std::vector<uint64_t> gb(ncand + 1, 0);
         for (uint64_t q = 0; q < ncand; ++q) gb[q + 1] = gb[q] + hrows[q];
         for (uint64_t q = 0; q < ncand; ++q) tr[owner[q].first]->rows[owner[q].second] = gb[q + 1] - gb[q];
@@ -629,6 +659,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             L.has_table[c] = 1;
         }
         rows_written += total_rows;
+        cnt_fillw += total_rows * k;
         DevBuf<CandDesc> dfd;
         DevBuf<uint64_t> dfc;
         if (!fd.empty()) {
@@ -646,12 +677,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), hoff.size() * 8, cudaMemcpyHostToDevice, s));
                 for (size_t q = 0; q < fd.size(); ++q) {
-                    LevelWork w{dfd.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
+                    LevelWork w{dfd.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr, nullptr};
                     level_fill(b, w, k, false);
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
             } else {
-                LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr};
+                LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr, nullptr};
                 level_fill(b, w, k, true);
             }
         }
@@ -683,8 +714,22 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             if (st.cands.empty()) st.active = false;
     }
     COLO_CUDA(cudaStreamSynchronize(s));
+    kt.resolve();
     for (uint32_t j = 0; j < J; ++j) {
         MineResult* r = outs[j];
+        r->kernels = kt.stats;
+        r->counters[4] = 0;
+        r->counters[5] = b.N;
+        r->counters[6] = b.M;
+        r->counters[7] = b.Rn;
+        r->counters[8] = cnt_items;
+        r->counters[9] = cnt_parent;
+        r->counters[10] = cnt_fillw;
+        r->counters[11] = cnt_bmw;
+        r->counters[12] = (b.jobs.size() == 1 && t_upload > 0.01) ? 12 * b.N : 0;
+        r->counters[13] = cnt_d2h;
+        r->counters[14] = b.nrl_total;
+        r->counters[15] = cnt_refined;
         r->times[0] = ms_since(t_all);
         r->times[1] = t_upload;
         r->times[2] = t_bucket;
@@ -851,6 +896,12 @@ const char* colo_dataset_feature_name(const colo_dataset* ds, uint32_t f) {
 void colo_dataset_free(colo_dataset* ds) {
     if (!ds) return;
     if (ds->ctx) cudaStreamSynchronize(ds->ctx->s);
+    if (ds->pinned && !ds->hp.x.empty()) {
+        cudaHostUnregister(ds->hp.x.data());
+        cudaHostUnregister(ds->hp.y.data());
+        cudaHostUnregister(ds->feat.data());
+        cudaGetLastError();
+    }
     delete ds;
 }
 
@@ -932,11 +983,29 @@ colo_status colo_result_times(const colo_result* r, double* ms8) {
     return COLO_OK;
 }
 
-colo_status colo_result_counters(const colo_result* r, uint64_t* c8) {
-    if (!r || !c8) return COLO_ERR_ARG;
-    std::memcpy(c8, r->r.counters, sizeof(r->r.counters));
+colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n) {
+    if (!r || !c) return COLO_ERR_ARG;
+    for (uint32_t i = 0; i < n; ++i) c[i] = i < (uint32_t)kNumCounters ? r->r.counters[i] : 0;
     return COLO_OK;
 }
+
+uint32_t colo_result_num_kernels(const colo_result* r) { return r ? (uint32_t)r->r.kernels.size() : 0; }
+
+colo_status colo_result_kernel(const colo_result* r, uint32_t i, char* name, size_t cap, uint64_t* launches,
+                               double* ms) {
+    if (!r || i >= r->r.kernels.size()) return COLO_ERR_ARG;
+    const KernelStat& k = r->r.kernels[i];
+    if (name && cap) {
+        size_t m = std::min(cap - 1, k.name.size());
+        std::memcpy(name, k.name.data(), m);
+        name[m] = 0;
+    }
+    if (launches) *launches = k.launches;
+    if (ms) *ms = k.ms;
+    return COLO_OK;
+}
+
+void* colo_ctx_stream(const colo_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
 
 void colo_result_free(colo_result* r) { delete r; }
 

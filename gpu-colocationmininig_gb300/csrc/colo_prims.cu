@@ -6,6 +6,7 @@
 namespace colo {
 
 thread_local uint64_t g_launches = 0;
+thread_local KTimer* g_ktimer = nullptr;
 
 namespace {
 
@@ -239,6 +240,7 @@ void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cu
     int passes = (bits + kRadixBits - 1) / kRadixBits;
     for (int p = 0; p < passes; ++p) {
         int shift = p * kRadixBits;
+        KScope ks("radix_sort");
         k_radix_hist<<<nblocks, kSortThreads, 0, s>>>(ka, n, shift, hist.get(), nblocks);
         COLO_LAUNCH_CHECK();
         count_launch();

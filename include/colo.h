@@ -55,7 +55,7 @@ typedef struct {
     uint32_t max_size;       /* 0 = no cap (the reference has none) */
     int32_t mode;            /* colo_mode */
     int32_t keep_tables;     /* 1: keep every instance table in the result (tests) */
-    int32_t reserved[6];
+    int32_t reserved[6];     /* reserved[0] bit 0: time every kernel with CUDA events */
 } colo_params;
 
 const char* colo_status_string(colo_status s);
@@ -132,9 +132,21 @@ colo_status colo_result_write_patterns(const colo_result* r, const colo_dataset*
 /* Timing of the last mine, milliseconds: [0] total, [1] upload, [2] bucketing,
  * [3] join, [4] filter, [5] refine, [6] fill, [7] host Apriori. */
 colo_status colo_result_times(const colo_result* r, double* ms8);
-/* Device work counters: [0] kernel launches, [1] join pairs evaluated,
- * [2] neighbour entries, [3] rows written, [4] fallback candidates. */
-colo_status colo_result_counters(const colo_result* r, uint64_t* c8);
+/* Work counters (n entries): [0] kernel launches, [1] neighbourhood-list
+ * entries, [2] neighbour entries E, [3] table rows written, [4] fallback
+ * candidates, [5] points, [6] occupied cells, [7] runs, [8] slice entries
+ * examined by count passes, [9] parent words read by count passes,
+ * [10] table words written, [11] bitmap words, [12] host-to-device bytes,
+ * [13] device-to-host bytes, [14] neighbourhood-run entries, [15] refined
+ * candidates. */
+colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n);
+/* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set). */
+uint32_t colo_result_num_kernels(const colo_result* r);
+colo_status colo_result_kernel(const colo_result* r, uint32_t i, char* name, size_t cap, uint64_t* launches,
+                               double* ms);
+/* The context's CUDA stream (cudaStream_t), for callers that time or order
+ * their own work against the library's. */
+void* colo_ctx_stream(const colo_ctx* ctx);
 void colo_result_free(colo_result* r);
 
 /* ---- stage entry points (mirror the reference's inner extern "C" API) ---- */

@@ -53,10 +53,21 @@ struct SqDecision {
 inline void square_candidates(float d, float* c, int* nc) {
     double e = (double)d * (double)d;          /* exact for a float d */
     float rn = (float)e;                       /* round to nearest even */
-    if (e < 1e-36 || e > 3.0e38) {             /* outside the measured range */
+    if (e == 0.0) {
+        c[0] = 0.0f;
+        *nc = 1;
+        return;
+    }
+    if (e < 1e-36) {                           /* below the measured binades: bracket */
+        c[0] = 0.0f;
+        c[1] = std::nextafter(rn, INFINITY);
+        *nc = 2;
+        return;
+    }
+    if (e > 3.0e38) {                          /* may overflow to infinity */
         c[0] = rn;
-        c[1] = rn;
-        *nc = -1;
+        c[1] = INFINITY;
+        *nc = 2;
         return;
     }
     if ((double)rn == e) {
@@ -84,8 +95,7 @@ inline SqDecision sq_decide(float x1, float y1, float x2, float y2, float R2) {
     square_candidates(dy, b, &nb);
     SqDecision out;
     out.le = (a[0] + b[0]) <= R2;
-    out.ambiguous = (na < 0 || nb < 0);
-    if (out.ambiguous) return out;
+    out.ambiguous = false;
     for (int i = 0; i < na; ++i)
         for (int j = 0; j < nb; ++j)
             if (((a[i] + b[j]) <= R2) != out.le) out.ambiguous = true;

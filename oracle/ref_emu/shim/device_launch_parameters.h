@@ -1,0 +1,2 @@
+#pragma once
+#include "colo_emu.h"

@@ -1,0 +1,2 @@
+#pragma once
+#include "../../thrust_emu.h"

@@ -90,9 +90,11 @@ def test_large_patterns_generic_kernel_path(ctx):
 
 
 def test_dense_cells_and_skewed_sizes(ctx):
+    # one blob where every point neighbours every other: the level-5 table is
+    # the product of the five feature counts (8*16*24*32*40 = 3.9e6 rows)
     rng = np.random.default_rng(6)
-    pts = _cluster_points(rng, 5, 20, 4.0, 200.0, per=6)
-    pts += [(f, rng.normal(100, 2), rng.normal(100, 2)) for f in range(5) for _ in range(80 * (f + 1))]
+    pts = _cluster_points(rng, 5, 20, 4.0, 200.0, per=2)
+    pts += [(f, rng.normal(100, 1), rng.normal(100, 1)) for f in range(5) for _ in range(8 * (f + 1))]
     _check(ctx, _wl("dense", pts, [0, 0, 200, 200], 6.0, 0.2))
 
 

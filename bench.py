@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cpu-frac", type=float, default=0.02)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--forms", default="batched,e2e,plain",
+                    help="comma list of batched (resident), e2e (host buffers), plain")
     args = ap.parse_args()
     rank, world, local = dist_env()
     from colo import gen
@@ -239,12 +241,16 @@ def main():
             ms = float(t.item())
         return ms, results, clk.summary()
 
+    forms = set(args.forms.split(","))
     ms_b, res_b, clocks = timed(colo.MODE_BATCHED, True, profile=True)
     cands = res_b[0].num_candidates()
     value = cands * args.steps * world / (ms_b / 1e3)
-    ms_e, res_e, _ = timed(colo.MODE_BATCHED, False)
+    ms_e, res_e, ms_p, res_p = ms_b, res_b, ms_b, res_b
+    if "e2e" in forms:
+        ms_e, res_e, _ = timed(colo.MODE_BATCHED, False)
     e2e = cands * args.steps * world / (ms_e / 1e3)
-    ms_p, res_p, _ = timed(colo.MODE_PLAIN, True)
+    if "plain" in forms:
+        ms_p, res_p, _ = timed(colo.MODE_PLAIN, True)
     plain = cands * args.steps * world / (ms_p / 1e3)
     # every form mined the same patterns
     same = all(r.patterns() == res_b[0].patterns() for r in res_b + res_e + res_p)

@@ -25,7 +25,7 @@ STATUS = {0: "COLO_OK", 1: "COLO_ERR_ARG", 2: "COLO_ERR_IO", 3: "COLO_ERR_PARSE"
           5: "COLO_ERR_CUDA", 6: "COLO_ERR_NOMEM", 7: "COLO_ERR_TIMEOUT", 8: "COLO_ERR_CAPACITY",
           9: "COLO_ERR_NO_DEVICE", 10: "COLO_ERR_INTERNAL"}
 MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
-COUNTERS = ["launches", "npl_entries", "neighbors", "rows_written", "fallbacks", "points", "cells", "runs",
+COUNTERS = ["launches", "active_anchors", "neighbors", "rows_written", "join_pairs", "points", "cells", "runs",
             "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
             "nrl_entries", "refined"]
 

@@ -13,7 +13,11 @@ config4  1e8 points, 200 features Zipf(1.3), +2% in 50 dense hotspots (sigma 5),
 
 Planted offsets use sigma = 0.3 R (config 0's ratio 15/50) and 0.6 x the
 smallest member count of seeds per pattern (config 0's 1,200/2,000), shared
-between the patterns a feature belongs to.  `scale` shrinks N (tests).
+between the patterns a feature belongs to.  With Zipf-sized features a
+planted pattern can only be prevalent if its members have similar counts
+(PI is the smallest participation ratio), so members are a window of
+consecutive size ranks outside the Zipf head.  Hotspots each belong to one
+feature.  `scale` shrinks N and the domain at constant density (tests).
 """
 from __future__ import annotations
 

@@ -48,18 +48,24 @@ struct Batch {
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
     DevBuf<uint32_t> frun_off, frun;
-    // neighbourhood lists
-    DevBuf<uint64_t> nrl_off, npl_off;
-    DevBuf<uint32_t> nrl_feat;
-    DevBuf<uint64_t> nrl_pos;
-    DevBuf<uint32_t> npl_id;
-    DevBuf<float> npl_x, npl_y;
-    uint64_t nrl_total = 0, npl_total = 0;
-    // neighbour CSR
-    DevBuf<uint64_t> nb_off;
-    DevBuf<uint32_t> nb;
-    uint64_t E = 0;
-    uint64_t join_pairs = 0;     // pair distance evaluations in the join (count pass)
+    // neighbourhood run lists: for cell c, the runs of its adjacent cells
+    // ordered by (feature, cell): nrl_feat/nrl_run[nrl_off[c] .. nrl_off[c+1])
+    DevBuf<uint64_t> nrl_off;
+    DevBuf<uint32_t> nrl_feat, nrl_run;
+    uint64_t nrl_total = 0;
+    // per run: first entry of its cell's list with a higher feature (absolute
+    // index) and the number of target points from there to the list's end
+    DevBuf<uint64_t> run_sfx;
+    DevBuf<uint32_t> run_L;
+    // neighbour lists N+(a) = nb[nb_beg[a] .. nb_beg[a] + nb_cnt[a]), each in
+    // (feature, neighbour cell, id) order
+    DevBuf<uint64_t> nb_beg;
+    DevBuf<uint32_t> nb_cnt, nb;
+    uint64_t E = 0;              // neighbour entries
+    uint64_t nb_cap = 0;         // allocated entries (upper bound in single-pass mode)
+    uint64_t join_pairs = 0;     // pair distance evaluations
+    uint64_t active_anchors = 0; // anchors whose cell has higher-feature neighbours
+    bool join_single = true;     // single pass into per-run upper-bound regions
     int join_group = 8;          // lanes per anchor in the join (autotuned)
 };
 

@@ -1,7 +1,7 @@
 // colo_bucket.cu -- grid bucketing: a stable radix sort of points by cell key
 // into a cell CSR with (cell, feature) runs, per-cell feature masks and the
 // geometric 3x3 occupied-neighbour table; then the per-cell neighbourhood
-// run/point lists (NRL / NPL) that the join streams.
+// run lists that the join walks.
 //
 // Replaces CountCellFeatures (Codes/DeviceProcess.cu:312-369) and
 // kernel_CountCellFeatures (Codes/DeviceProcess_Kernel.h:629-647): instead of
@@ -127,24 +127,28 @@ __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint3
         }
 }
 
-__global__ void k_frun_count(uint64_t Rn, const uint32_t* __restrict__ rfeat, uint32_t* __restrict__ cnt) {
-    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < Rn) atomicAdd(&cnt[rfeat[r]], 1u);
-}
-
-__global__ void k_frun_fill(uint64_t Rn, const uint32_t* __restrict__ rfeat,
-                            const uint32_t* __restrict__ off, uint32_t* __restrict__ cursor,
-                            uint32_t* __restrict__ frun) {
+__global__ void k_frun_keys(uint64_t Rn, const uint32_t* __restrict__ rfeat, uint64_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
     uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= Rn) return;
-    uint32_t f = rfeat[r];
-    frun[off[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)r;
+    keys[r] = rfeat[r];
+    vals[r] = (uint32_t)r;
+}
+
+// frun_off[f] = first position of feature f in the feature-sorted run list
+__global__ void k_frun_off(uint32_t F, uint64_t Rn, const uint64_t* __restrict__ keys,
+                           uint32_t* __restrict__ frun_off) {
+    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f > F) return;
+    frun_off[f] = (uint32_t)lower_bound_dev(keys, (uint64_t)0, Rn, (uint64_t)f);
 }
 
 // ---------------------------------------------------------------------------
-// Neighbourhood lists.  For cell c the adjacent cells A(c) (the reference's
-// stencil, in ascending cell order) contribute their runs; NRL(c) lists them
-// ordered by (feature, cell) and NPL(c) lists their points in that order.
+// Neighbourhood run lists.  For cell c the adjacent cells A(c) (the
+// reference's stencil, ascending cell ids) contribute their runs; NRL(c)
+// orders them by (feature, cell), which is the order the reference's kernels
+// visit candidates of one feature.  For each run of c the list suffix with
+// higher features holds exactly the join targets of the run's points.
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ int adjacent_cells(uint64_t c, const uint64_t* ckey, const uint32_t* cjob,
@@ -165,70 +169,60 @@ __device__ __forceinline__ int adjacent_cells(uint64_t c, const uint64_t* ckey, 
     return cnt;
 }
 
-__global__ void k_nl_count(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                           const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                           const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
-                           uint32_t* __restrict__ nrl_len, uint32_t* __restrict__ npl_len) {
+__global__ void k_nrl_count(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+                            const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
+                            const uint32_t* __restrict__ crun, uint32_t* __restrict__ nrl_len) {
     uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M) return;
     int32_t adj[9];
     int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
-    uint32_t nr = 0, np = 0;
-    for (int s = 0; s < na; ++s) {
-        nr += crun[adj[s] + 1] - crun[adj[s]];
-        np += cstart[adj[s] + 1] - cstart[adj[s]];
-    }
+    uint32_t nr = 0;
+    for (int s = 0; s < na; ++s) nr += crun[adj[s] + 1] - crun[adj[s]];
     nrl_len[c] = nr;
-    npl_len[c] = np;
 }
 
-// One warp per cell.  For a run of feature f in adjacent slot s, its NRL
-// position is sum over slots of (#runs with feature < f) plus the number of
-// earlier slots that also hold f; its NPL position is the same with points.
-__global__ void k_nl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                          const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                          const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
-                          const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
-                          const uint32_t* __restrict__ rcnt, const uint32_t* __restrict__ sid,
-                          const float* __restrict__ sx, const float* __restrict__ sy,
-                          const uint64_t* __restrict__ nrl_off, const uint64_t* __restrict__ npl_off,
-                          uint32_t* __restrict__ nrl_feat, uint64_t* __restrict__ nrl_pos,
-                          uint32_t* __restrict__ npl_id, float* __restrict__ npl_x,
-                          float* __restrict__ npl_y) {
-    const int lane = threadIdx.x & 31;
-    uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// One thread per cell.  A run of feature f in adjacent slot s lands at
+// sum over slots of (#runs with feature < f) plus the number of earlier slots
+// that also hold f.  Then, per run of the cell itself, the first entry with a
+// higher feature and the number of points from there on.
+__global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+                           const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
+                           const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
+                           const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ nrl_off,
+                           uint32_t* __restrict__ nrl_feat, uint32_t* __restrict__ nrl_run,
+                           uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
+    uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M) return;
     int32_t adj[9];
     int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
-    uint64_t rbase = nrl_off[c], pbase = npl_off[c];
+    const uint64_t base = nrl_off[c], end = nrl_off[c + 1];
     for (int s = 0; s < na; ++s) {
         uint32_t r0 = crun[adj[s]], r1 = crun[adj[s] + 1];
         for (uint32_t r = r0; r < r1; ++r) {
             uint32_t f = rfeat[r];
-            uint64_t rpos = 0, ppos = 0;
+            uint64_t pos = 0;
             for (int t = 0; t < na; ++t) {
                 uint32_t q0 = crun[adj[t]], q1 = crun[adj[t] + 1];
                 uint32_t lb = (uint32_t)lower_bound_dev(rfeat, (uint64_t)q0, (uint64_t)q1, f);
-                rpos += lb - q0;
-                uint32_t pts_before = (lb < q1 ? rstart[lb] : cstart[adj[t] + 1]) - cstart[adj[t]];
-                ppos += pts_before;
-                if (t < s && lb < q1 && rfeat[lb] == f) {
-                    rpos += 1;
-                    ppos += rcnt[lb];
-                }
+                pos += lb - q0;
+                if (t < s && lb < q1 && rfeat[lb] == f) pos += 1;
             }
-            if (lane == 0) {
-                nrl_feat[rbase + rpos] = f;
-                nrl_pos[rbase + rpos] = pbase + ppos;
-            }
-            uint32_t st = rstart[r], ct = rcnt[r];
-            for (uint32_t t = lane; t < ct; t += 32) {
-                uint64_t q = pbase + ppos + t;
-                npl_id[q] = sid[st + t];
-                npl_x[q] = sx[st + t];
-                npl_y[q] = sy[st + t];
-            }
+            nrl_feat[base + pos] = f;
+            nrl_run[base + pos] = r;
         }
+    }
+    for (uint32_t r = crun[c]; r < crun[c + 1]; ++r) {
+        uint32_t f = rfeat[r];
+        uint64_t lo = base, hi = end;
+        while (lo < hi) {
+            uint64_t mid = (lo + hi) >> 1;
+            if (nrl_feat[mid] <= f) lo = mid + 1;
+            else hi = mid;
+        }
+        uint32_t L = 0;
+        for (uint64_t q = lo; q < end; ++q) L += rcnt[nrl_run[q]];
+        run_sfx[r] = lo;
+        run_L[r] = L;
     }
 }
 
@@ -312,24 +306,23 @@ void bucket_points(Batch& b) {
     COLO_LAUNCH_CHECK();
     count_launch();
 
-    // feature-major run index
-    DevBuf<uint32_t> fcnt, cursor;
-    fcnt.alloc(b.F, s);
-    fcnt.zero(s);
-    cursor.alloc(b.F, s);
-    cursor.zero(s);
-    b.frun_off.alloc(b.F + 1, s);
-    b.frun.alloc(Rn, s);
-    k_frun_count<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), fcnt.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
-    uint32_t tot = 0;
-    scan_u32_to_u32(fcnt.get(), b.frun_off.get(), b.F, s, &tot);
-    COLO_CUDA(cudaMemcpyAsync(b.frun_off.get() + b.F, &tot, 4, cudaMemcpyHostToDevice, s));
-    k_frun_fill<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), b.frun_off.get(), cursor.get(),
-                                                   b.frun.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    // feature-major run index: runs sorted by feature (stable, cell order kept)
+    {
+        DevBuf<uint64_t> fk;
+        fk.alloc(Rn, s);
+        b.frun.alloc(Rn, s);
+        b.frun_off.alloc(b.F + 1, s);
+        k_frun_keys<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), fk.get(), b.frun.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+        int fbits = 1;
+        while (fbits < 32 && (1ull << fbits) < b.F) fbits++;
+        radix_sort_u64_u32(fk.get(), b.frun.get(), Rn, fbits, s);
+        k_frun_off<<<grid_for(b.F + 1, 128), 128, 0, s>>>(b.F, Rn, fk.get(), b.frun_off.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+        COLO_CUDA(cudaStreamSynchronize(s));
+    }
     b.h_frun_off.resize(b.F + 1);
     COLO_CUDA(cudaMemcpyAsync(b.h_frun_off.data(), b.frun_off.get(), (b.F + 1) * 4,
                               cudaMemcpyDeviceToHost, s));
@@ -344,37 +337,30 @@ void bucket_points(Batch& b) {
 void build_neighborhoods(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t M = b.M;
-    DevBuf<uint32_t> nrl_len, npl_len;
+    DevBuf<uint32_t> nrl_len;
     nrl_len.alloc(M, s);
-    npl_len.alloc(M, s);
-    k_nl_count<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(),
-                                                 b.nb9.get(), b.cstart.get(), b.crun.get(),
-                                                 nrl_len.get(), npl_len.get());
+    k_nrl_count<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
+                                                  b.crun.get(), nrl_len.get());
     COLO_LAUNCH_CHECK();
     count_launch();
     b.nrl_off.alloc(M + 1, s);
-    b.npl_off.alloc(M + 1, s);
-    uint64_t tr = 0, tp = 0;
+    uint64_t tr = 0;
     scan_u32_to_u64(nrl_len.get(), b.nrl_off.get(), M, s, &tr);
-    scan_u32_to_u64(npl_len.get(), b.npl_off.get(), M, s, &tp);
     COLO_CUDA(cudaMemcpyAsync(b.nrl_off.get() + M, &tr, 8, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(b.npl_off.get() + M, &tp, 8, cudaMemcpyHostToDevice, s));
     b.nrl_total = tr;
-    b.npl_total = tp;
     b.nrl_feat.alloc(tr, s);
-    b.nrl_pos.alloc(tr, s);
-    b.npl_id.alloc(tp, s);
-    b.npl_x.alloc(tp, s);
-    b.npl_y.alloc(tp, s);
-    KScope ks("npl_fill");
-    k_nl_fill<<<grid_for(M * 32, 256), 256, 0, s>>>(
-        M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cstart.get(), b.crun.get(),
-        b.rfeat.get(), b.rstart.get(), b.rcnt.get(), b.sid.get(), b.sx.get(), b.sy.get(),
-        b.nrl_off.get(), b.npl_off.get(), b.nrl_feat.get(), b.nrl_pos.get(), b.npl_id.get(),
-        b.npl_x.get(), b.npl_y.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
-    // the tiny host copies above must complete before the temporaries go
+    b.nrl_run.alloc(tr, s);
+    b.run_sfx.alloc(b.Rn, s);
+    b.run_L.alloc(b.Rn, s);
+    {
+        KScope ks("nrl_fill");
+        k_nrl_fill<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
+                                                     b.crun.get(), b.rfeat.get(), b.rcnt.get(), b.nrl_off.get(),
+                                                     b.nrl_feat.get(), b.nrl_run.get(), b.run_sfx.get(),
+                                                     b.run_L.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
     COLO_CUDA(cudaStreamSynchronize(s));
 }
 

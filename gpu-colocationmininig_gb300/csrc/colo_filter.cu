@@ -11,7 +11,7 @@
 //
 // Pairs: if cell C holds feature f, C lies in U_{f,g} exactly when g occurs
 // in the union of the valid quads around C, which is C's clipped 3x3 block.
-// So every pair bound is one pass over the cells: for each run (C, f) and
+// So every pair bound is one pass over the runs: for each run (C, f) and
 // each feature g of the 3x3 block, add count(C, f) to bound(f side of {f,g}).
 // The accumulator is an F x F matrix in shared memory.
 //
@@ -28,30 +28,27 @@ constexpr int kFilterThreads = 256;
 constexpr int kFilterWarps = kFilterThreads / 32;
 constexpr int kMaxW = 8;   // mask words handled in registers (256 features per job)
 
+// One thread per run (C, f); a block owns a contiguous range of runs, so the
+// job changes rarely and the F x F accumulator lives in shared memory.
 __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
-    uint64_t M, const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
-    const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask, uint32_t W,
-    const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
-    const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ job_off,
-    uint32_t* __restrict__ ub2, uint32_t acc_dim, uint64_t cells_per_block) {
+    uint64_t Rn, const uint32_t* __restrict__ rcell, const uint32_t* __restrict__ cjob,
+    const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
+    uint32_t W, const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt,
+    const uint64_t* __restrict__ job_off, uint32_t* __restrict__ ub2, uint32_t acc_dim, uint64_t runs_per_block) {
     extern __shared__ uint32_t acc[];   // acc_dim x acc_dim (acc_dim = 0: no privatisation)
-    __shared__ uint32_t nbm[kFilterWarps][kMaxW];
     __shared__ int32_t cur_job;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint64_t c0 = (uint64_t)blockIdx.x * cells_per_block;
-    const uint64_t c1 = c0 + cells_per_block < M ? c0 + cells_per_block : M;
+    const uint64_t r0 = (uint64_t)blockIdx.x * runs_per_block;
+    const uint64_t r1 = r0 + runs_per_block < Rn ? r0 + runs_per_block : Rn;
     const uint32_t accn = acc_dim * acc_dim;
     for (uint32_t i = threadIdx.x; i < accn; i += blockDim.x) acc[i] = 0;
-    if (threadIdx.x == 0) cur_job = c0 < M ? (int32_t)cjob[c0] : -1;
+    if (threadIdx.x == 0) cur_job = r0 < Rn ? (int32_t)cjob[rcell[r0]] : -1;
     __syncthreads();
-    for (uint64_t base = c0; base < c1; base += kFilterWarps) {
-        // flush on a job change (the round's first cell decides)
-        int32_t jb = (int32_t)cjob[base];
-        if (jb != cur_job) {
+    for (uint64_t base = r0; base < r1; base += blockDim.x) {
+        int32_t jb = (int32_t)cjob[rcell[base]];
+        if (jb != cur_job) {   // flush the accumulator on a job change (uniform branch)
             __syncthreads();
-            const JobGrid gj = grids[cur_job];
-            uint32_t nf = gj.nf;
-            for (uint32_t i = threadIdx.x; i < nf * nf && acc_dim; i += blockDim.x) {
+            uint32_t nf = grids[cur_job].nf;
+            for (uint32_t i = threadIdx.x; acc_dim && i < nf * nf; i += blockDim.x) {
                 uint32_t v = acc[(i / nf) * acc_dim + (i % nf)];
                 if (v) atomicAdd(&ub2[job_off[cur_job] + i], v);
             }
@@ -60,37 +57,29 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
             if (threadIdx.x == 0) cur_job = jb;
             __syncthreads();
         }
-        uint64_t c = base + w;
-        if (c < c1) {
-            uint32_t job = cjob[c];
+        const uint64_t r = base + threadIdx.x;
+        if (r < r1) {
+            const uint32_t c = rcell[r];
+            const uint32_t job = cjob[c];
             const JobGrid g = grids[job];
-            bool priv = acc_dim && (int32_t)job == cur_job && g.nf <= acc_dim;
             if (g.gx >= 2 && g.gy >= 2) {
-                if (lane < (int)W) {
-                    uint32_t m = 0;
-                    for (int q = 0; q < 9; ++q) {
-                        int32_t v = nb9[c * 9 + q];
-                        if (v >= 0) m |= cmask[(uint64_t)v * W + lane];
-                    }
-                    nbm[w][lane] = m;
-                }
-                __syncwarp();
-                uint32_t r0 = crun[c], r1 = crun[c + 1];
-                uint32_t items = (r1 - r0) * W;
-                for (uint32_t it = lane; it < items; it += 32) {
-                    uint32_t r = r0 + it / W, word = it % W;
-                    uint32_t lf = rfeat[r] - g.f0, cnt = rcnt[r];
-                    uint32_t bits = nbm[w][word];
+                const bool priv = acc_dim && (int32_t)job == cur_job && g.nf <= acc_dim;
+                const uint32_t lf = rfeat[r] - g.f0, cnt = rcnt[r];
+                int32_t nb[9];
+                for (int q = 0; q < 9; ++q) nb[q] = nb9[(uint64_t)c * 9 + q];
+                for (uint32_t w = 0; w < W; ++w) {
+                    uint32_t bits = 0;
+                    for (int q = 0; q < 9; ++q)
+                        if (nb[q] >= 0) bits |= cmask[(uint64_t)nb[q] * W + w];
                     while (bits) {
                         int bpos = __ffs(bits) - 1;
                         bits &= bits - 1;
-                        uint32_t lg = word * 32 + bpos;
+                        uint32_t lg = w * 32 + bpos;
                         if (lg == lf) continue;
                         if (priv) atomicAdd(&acc[lf * acc_dim + lg], cnt);
                         else atomicAdd(&ub2[job_off[job] + (uint64_t)lf * g.nf + lg], cnt);
                     }
                 }
-                __syncwarp();
             }
         }
     }
@@ -227,13 +216,13 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     if (smem > 48 * 1024)
         COLO_CUDA(cudaFuncSetAttribute(k_filter_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     uint64_t blocks = (uint64_t)b.sms * (smem > 100 * 1024 ? 1 : 2);
-    uint64_t per = (b.M + blocks - 1) / blocks;
-    per = (per + kFilterWarps - 1) / kFilterWarps * kFilterWarps;
-    blocks = (b.M + per - 1) / per;
+    uint64_t per = (b.Rn + blocks - 1) / blocks;
+    per = (per + kFilterThreads - 1) / kFilterThreads * kFilterThreads;
+    blocks = (b.Rn + per - 1) / per;
     KScope ks("filter_pairs");
     k_filter_pairs<<<(unsigned)blocks, kFilterThreads, smem, s>>>(
-        b.M, b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.W, b.crun.get(),
-        b.rfeat.get(), b.rcnt.get(), d_job_off.get(), ub2.get(), acc_dim, per);
+        b.Rn, b.rcell.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.W, b.rfeat.get(),
+        b.rcnt.get(), d_job_off.get(), ub2.get(), acc_dim, per);
     COLO_LAUNCH_CHECK();
     count_launch();
     COLO_CUDA(cudaStreamSynchronize(s));

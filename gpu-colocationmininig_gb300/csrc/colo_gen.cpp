@@ -107,18 +107,17 @@ int colo_gen_points(const colo_gen_spec* sp, float* x, float* y, int32_t* fid, f
     if (sp->config0) {
         pats = {{0, 1}, {2, 3, 4}, {5, 6, 7, 8}};
     } else {
-        std::vector<uint32_t> use(F, 0);
+        // PI is the smallest member participation ratio, so a planted pattern
+        // is prevalent only when its members have similar counts: members are
+        // a window of consecutive size ranks, away from the Zipf head where
+        // neighbouring ranks differ most.
         for (uint32_t p = 0; p < sp->npat; ++p) {
             uint32_t sz = sp->pat_min + (uint32_t)rng.below(sp->pat_max - sp->pat_min + 1);
             if (sz > F) sz = F;
-            std::vector<uint32_t> order(F);
-            for (uint32_t f = 0; f < F; ++f) order[f] = f;
-            // prefer less used features, random among ties
-            for (uint32_t f = F; f > 1; --f) std::swap(order[f - 1], order[rng.below(f)]);
-            std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return use[a] < use[b]; });
-            std::vector<uint32_t> m(order.begin(), order.begin() + sz);
-            std::sort(m.begin(), m.end());
-            for (uint32_t f : m) use[f]++;
+            uint32_t lo = std::min<uint32_t>(2 * sp->pat_max, F - sz);
+            uint32_t start = lo + (uint32_t)rng.below(F - sz - lo + 1);
+            std::vector<uint32_t> m;
+            for (uint32_t t = 0; t < sz; ++t) m.push_back(start + t);
             pats.push_back(m);
         }
     }

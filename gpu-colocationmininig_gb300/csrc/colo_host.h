@@ -72,6 +72,7 @@ struct colo_ctx {
     cudaStream_t s = nullptr;
     int sms = 0;
     std::string err;
+    int refs = 1;          // the owner plus one per live dataset (freed at zero)
 };
 
 struct colo_dataset {
@@ -93,6 +94,7 @@ struct colo_result {
 namespace colo {
 struct Batch;
 colo_status set_err(colo_ctx* ctx, colo_status st, const std::string& msg);
+void ctx_release(colo_ctx* ctx);
 colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn);
 void upload_dataset(colo_dataset* ds, cudaStream_t s);
 // Points, features, job grids and the bucketed/joined device state of a batch.

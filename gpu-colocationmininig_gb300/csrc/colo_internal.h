@@ -11,11 +11,10 @@
 //               cmask[M*W] (feature bit masks, local feature index)
 //   runs        (cell, feature) runs rfeat/rstart/rcnt/rcell[Rn], feature-major
 //               index frun_off[F+1]/frun[Rn]
-//   NPL         per cell, the points of its adjacent cells ordered by
-//               (feature, cell, id): npl_off[M+1], npl_id/npl_x/npl_y
-//   NRL         per cell, the runs behind its NPL: nrl_off[M+1], nrl_feat,
-//               nrl_pos (NPL offset of each run)
-//   neighbours  CSR N+(a) indexed by point id: nb_off[N+1] (u64), nb[E]
+//   NRL         per cell, the runs of its adjacent cells ordered by
+//               (feature, cell): nrl_off[M+1], nrl_feat, nrl_run; per run the
+//               start of its higher-feature suffix run_sfx and its size run_L
+//   neighbours  N+(a) = nb[nb_beg[a] .. nb_beg[a] + nb_cnt[a]) by point id
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -210,6 +209,8 @@ void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t
                      uint64_t* total_host);
 void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t s,
                      uint32_t* total_host);
+void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
+                     uint64_t* total_host);
 // Stable LSD radix sort of (key, val) pairs by the low `bits` bits of key.
 // Results land back in keys/vals.
 void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s);

@@ -1,112 +1,120 @@
-// colo_join.cu -- cell-pair spatial join producing the neighbour CSR
+// colo_join.cu -- cell-pair spatial join producing the neighbour lists
 //   N+(a) = {b : feat(b) > feat(a), cell(b) adjacent to cell(a), sq(a,b) <= R^2}
-// with each list ordered by (feature, neighbour cell, b): exactly the order in
-// which degree2TableSlotCounter_Kernel / generalInstanceTableSlotCounter_Kernel
+// each ordered by (feature, neighbour cell, b): exactly the order in which
+// degree2TableSlotCounter_Kernel / generalInstanceTableSlotCounter_Kernel
 // visit candidates (Codes/DeviceProcess_Kernel.h:12-55, 255-316).
 //
-// A group of T lanes serves one anchor.  The anchor's targets are a
-// contiguous suffix of its cell's neighbourhood point list (NPL), so loads are
-// coalesced 4-byte streams shared by every anchor of the cell (L1/L2 reuse).
-// The count pass writes |N+(a)|; the fill pass compacts hits with one warp
-// ballot per step (warp-aggregated compaction, no atomics).
+// Work is organised by run (the points of one feature in one cell): a run's
+// targets are the suffix of its cell's neighbourhood run list with higher
+// features, so runs without targets cost nothing and every anchor of a run
+// walks the same target list (L1/L2 reuse).  A group of T lanes serves one
+// anchor; target points are read straight from the cell-sorted coordinate
+// arrays, and hits are compacted with one group ballot per step.
+//
+// Single pass: each anchor owns a region of its run's upper bound L (the
+// number of target points) and writes its hits there, so no counting pass is
+// needed; when the upper bounds would not fit, a count pass + scan + fill
+// pass produces a compact layout instead.
 #include "colo_batch.h"
 #include "colo_device.cuh"
 
 namespace colo {
 namespace {
 
-template <int T, bool FILL>
+enum { J_SINGLE = 0, J_COUNT = 1, J_FILL = 2 };
+
+__global__ void k_run_caps(uint64_t Rn, const uint32_t* __restrict__ rcnt, const uint32_t* __restrict__ run_L,
+                           uint32_t* __restrict__ act, uint64_t* __restrict__ cap) {
+    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= Rn) return;
+    uint32_t L = run_L[r];
+    act[r] = L ? rcnt[r] : 0u;
+    cap[r] = L ? (uint64_t)rcnt[r] * L : 0ull;
+}
+
+// thread per run: list the run's anchors (sorted positions) when it has targets
+__global__ void k_expand_active(uint64_t Rn, const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ rcnt,
+                                const uint32_t* __restrict__ run_L, const uint32_t* __restrict__ act_off,
+                                uint32_t* __restrict__ act_pos, uint32_t* __restrict__ act_run) {
+    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= Rn || run_L[r] == 0) return;
+    uint32_t o = act_off[r], st = rstart[r], n = rcnt[r];
+    for (uint32_t i = 0; i < n; ++i) {
+        act_pos[o + i] = st + i;
+        act_run[o + i] = (uint32_t)r;
+    }
+}
+
+template <int T, int MODE>
 __global__ void __launch_bounds__(256) k_join(
-    uint64_t n, const uint32_t* __restrict__ sid, const uint32_t* __restrict__ scell,
-    const uint32_t* __restrict__ sfeat, const float* __restrict__ sx, const float* __restrict__ sy,
-    const uint64_t* __restrict__ nrl_off, const uint32_t* __restrict__ nrl_feat,
-    const uint64_t* __restrict__ nrl_pos, const uint64_t* __restrict__ npl_off,
-    const uint32_t* __restrict__ npl_id, const float* __restrict__ npl_x,
-    const float* __restrict__ npl_y, const uint32_t* __restrict__ fjob,
-    const JobGrid* __restrict__ grids, uint32_t* __restrict__ cnt,
-    const uint64_t* __restrict__ nb_off, uint32_t* __restrict__ nb) {
+    uint64_t A, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
+    const uint32_t* __restrict__ sid, const uint32_t* __restrict__ scell, const uint32_t* __restrict__ sfeat,
+    const float* __restrict__ sx, const float* __restrict__ sy, const uint32_t* __restrict__ rstart,
+    const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_L,
+    const uint64_t* __restrict__ cap_off, const uint64_t* __restrict__ nrl_off,
+    const uint32_t* __restrict__ nrl_run, const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids,
+    uint64_t* __restrict__ nb_beg, uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb) {
     const int lane = threadIdx.x & 31;
     const int gl = lane % T;
     const int gbase = lane - gl;
-    const uint64_t p = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / T;
-    const bool valid = p < n;
-    uint64_t s = 0, e = 0;
-    float xa = 0.f, ya = 0.f, R2 = 0.f;
-    uint32_t a = 0;
-    if (valid) {
-        uint32_t c = scell[p];
-        uint32_t fa = sfeat[p];
-        a = sid[p];
-        xa = sx[p];
-        ya = sy[p];
-        R2 = grids[fjob[fa]].R2;
-        uint64_t q0 = nrl_off[c], q1 = nrl_off[c + 1];
-        // first run whose feature is above the anchor's
-        uint64_t lo = q0, hi = q1;
-        while (lo < hi) {
-            uint64_t mid = (lo + hi) >> 1;
-            if (nrl_feat[mid] <= fa) lo = mid + 1;
-            else hi = mid;
-        }
-        e = npl_off[c + 1];
-        s = lo < q1 ? nrl_pos[lo] : e;
-    }
-    uint32_t iters = (uint32_t)((e - s + T - 1) / T);
-    uint32_t maxit = __reduce_max_sync(0xffffffffu, iters);
-    const uint32_t gmask_bits = (T == 32) ? 0xffffffffu : ((1u << T) - 1u);
-    uint32_t count = 0;
-    uint64_t out = 0;
-    if (FILL && valid) out = nb_off[a];
-    for (uint32_t it = 0; it < maxit; ++it) {
-        uint64_t t = s + (uint64_t)it * T + gl;
-        bool ok = false;
-        uint32_t bid = 0;
-        if (t < e) {
-            ok = ref_sqdist(xa, ya, npl_x[t], npl_y[t]) <= R2;
-            if (FILL && ok) bid = npl_id[t];
-        }
-        uint32_t bal = __ballot_sync(0xffffffffu, ok);
-        uint32_t gm = (bal >> gbase) & gmask_bits;
-        if (FILL) {
-            if (ok) nb[out + __popc(gm & ((1u << gl) - 1u))] = bid;
-            out += __popc(gm);
-        } else {
-            count += __popc(gm);
+    const uint32_t gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << gbase);
+    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / T;
+    if (i >= A) return;                 // whole groups leave together
+    const uint32_t p = act_pos[i];
+    const uint32_t r = act_run[i];
+    const uint32_t a = sid[p];
+    const float xa = sx[p], ya = sy[p];
+    const float R2 = grids[fjob[sfeat[p]]].R2;
+    const uint64_t qend = nrl_off[scell[p] + 1];
+    uint64_t base = 0;
+    if (MODE == J_SINGLE) base = cap_off[r] + (uint64_t)(p - rstart[r]) * run_L[r];
+    if (MODE == J_FILL) base = nb_beg[a];
+    uint32_t k = 0;
+    for (uint64_t q = run_sfx[r]; q < qend; ++q) {
+        const uint32_t tr = nrl_run[q];
+        const uint32_t ts = rstart[tr], tc = rcnt[tr];
+        for (uint32_t b0 = 0; b0 < tc; b0 += T) {
+            const uint32_t t = b0 + gl;
+            bool ok = false;
+            if (t < tc) ok = ref_sqdist(xa, ya, sx[ts + t], sy[ts + t]) <= R2;
+            const uint32_t bal = (__ballot_sync(gmask, ok) >> gbase) & ((T == 32) ? 0xffffffffu : ((1u << T) - 1u));
+            if (MODE != J_COUNT && ok) nb[base + k + __popc(bal & ((1u << gl) - 1u))] = sid[ts + t];
+            k += __popc(bal);
         }
     }
-    if (!FILL && valid && gl == 0) cnt[a] = count;
+    if (gl == 0) {
+        nb_cnt[a] = k;
+        if (MODE == J_SINGLE) nb_beg[a] = base;
+    }
 }
 
 template <int T>
-void run_join(Batch& b, bool fill, uint32_t* cnt) {
-    const uint64_t n = b.N;
-    KScope ks(fill ? "join_fill" : "join_count");
-    uint64_t threads = n * T;
+void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uint32_t* act_run,
+              const uint64_t* cap_off) {
+    if (A == 0) return;
+    uint64_t threads = A * T;
     unsigned grid = (unsigned)((threads + 255) / 256);
-    if (grid == 0) grid = 1;
-    if (!fill) {
-        k_join<T, false><<<grid, 256, 0, b.s>>>(n, b.sid.get(), b.scell.get(), b.sfeat.get(), b.sx.get(),
-                                                b.sy.get(), b.nrl_off.get(), b.nrl_feat.get(),
-                                                b.nrl_pos.get(), b.npl_off.get(), b.npl_id.get(),
-                                                b.npl_x.get(), b.npl_y.get(), b.fjob.get(),
-                                                b.grids.get(), cnt, nullptr, nullptr);
-    } else {
-        k_join<T, true><<<grid, 256, 0, b.s>>>(n, b.sid.get(), b.scell.get(), b.sfeat.get(), b.sx.get(),
-                                               b.sy.get(), b.nrl_off.get(), b.nrl_feat.get(),
-                                               b.nrl_pos.get(), b.npl_off.get(), b.npl_id.get(),
-                                               b.npl_x.get(), b.npl_y.get(), b.fjob.get(),
-                                               b.grids.get(), nullptr, b.nb_off.get(), b.nb.get());
-    }
+    KScope ks(mode == J_SINGLE ? "join" : mode == J_COUNT ? "join_count" : "join_fill");
+#define COLO_JOIN(MD)                                                                                        \
+    k_join<T, MD><<<grid, 256, 0, b.s>>>(A, act_pos, act_run, b.sid.get(), b.scell.get(), b.sfeat.get(),     \
+                                         b.sx.get(), b.sy.get(), b.rstart.get(), b.rcnt.get(), b.run_sfx.get(), \
+                                         b.run_L.get(), cap_off, b.nrl_off.get(), b.nrl_run.get(),          \
+                                         b.fjob.get(), b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get())
+    if (mode == J_SINGLE) COLO_JOIN(J_SINGLE);
+    else if (mode == J_COUNT) COLO_JOIN(J_COUNT);
+    else COLO_JOIN(J_FILL);
+#undef COLO_JOIN
     COLO_LAUNCH_CHECK();
     count_launch();
 }
 
-void dispatch_join(Batch& b, bool fill, uint32_t* cnt) {
+void dispatch_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uint32_t* act_run,
+                   const uint64_t* cap_off) {
     switch (b.join_group) {
-        case 4: run_join<4>(b, fill, cnt); break;
-        case 16: run_join<16>(b, fill, cnt); break;
-        case 32: run_join<32>(b, fill, cnt); break;
-        default: run_join<8>(b, fill, cnt); break;
+        case 4: run_join<4>(b, mode, A, act_pos, act_run, cap_off); break;
+        case 16: run_join<16>(b, mode, A, act_pos, act_run, cap_off); break;
+        case 32: run_join<32>(b, mode, A, act_pos, act_run, cap_off); break;
+        default: run_join<8>(b, mode, A, act_pos, act_run, cap_off); break;
     }
 }
 
@@ -117,20 +125,68 @@ __global__ void k_sqdist(const float* __restrict__ x1, const float* __restrict__
     if (i < n) out[i] = ref_sqdist(x1[i], y1[i], x2[i], y2[i]);
 }
 
+inline unsigned grid_for(uint64_t n, int threads) {
+    uint64_t g = (n + threads - 1) / threads;
+    return (unsigned)(g == 0 ? 1 : g);
+}
+
 }  // namespace
+
+// Upper bound of the single-pass layout above which the compact two-pass
+// layout is used instead (entries).
+static const uint64_t kSinglePassCap = 1ull << 30;
 
 void join_neighbors(Batch& b) {
     cudaStream_t s = b.s;
-    DevBuf<uint32_t> cnt;
-    cnt.alloc(b.N, s);
-    dispatch_join(b, false, cnt.get());
-    b.nb_off.alloc(b.N + 1, s);
+    const uint64_t Rn = b.Rn;
+    DevBuf<uint32_t> act, act_off;
+    DevBuf<uint64_t> cap, cap_off;
+    act.alloc(Rn, s);
+    cap.alloc(Rn, s);
+    act_off.alloc(Rn, s);
+    cap_off.alloc(Rn, s);
+    k_run_caps<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rcnt.get(), b.run_L.get(), act.get(), cap.get());
+    COLO_LAUNCH_CHECK();
+    count_launch();
+    uint32_t A = 0;
+    scan_u32_to_u32(act.get(), act_off.get(), Rn, s, &A);
+    // upper bound of the single-pass layout = pair evaluations
+    uint64_t U = 0;
+    scan_u64_to_u64(cap.get(), cap_off.get(), Rn, s, &U);
+    b.active_anchors = A;
+    b.join_pairs = U;
+    DevBuf<uint32_t> act_pos, act_run;
+    act_pos.alloc(A, s);
+    act_run.alloc(A, s);
+    if (A) {
+        k_expand_active<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rstart.get(), b.rcnt.get(), b.run_L.get(),
+                                                          act_off.get(), act_pos.get(), act_run.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
+    b.nb_beg.alloc(b.N ? b.N : 1, s);
+    b.nb_cnt.alloc(b.N ? b.N : 1, s);
+    b.nb_beg.zero(s);
+    b.nb_cnt.zero(s);
+    b.join_single = U <= kSinglePassCap;
+    if (b.join_single) {
+        b.nb_cap = U;
+        b.nb.alloc(U ? U : 1, s);
+        dispatch_join(b, J_SINGLE, A, act_pos.get(), act_run.get(), cap_off.get());
+    } else {
+        dispatch_join(b, J_COUNT, A, act_pos.get(), act_run.get(), nullptr);
+        uint64_t E = 0;
+        scan_u32_to_u64(b.nb_cnt.get(), b.nb_beg.get(), b.N, s, &E);
+        b.nb_cap = E;
+        b.nb.alloc(E ? E : 1, s);
+        dispatch_join(b, J_FILL, A, act_pos.get(), act_run.get(), nullptr);
+    }
+    // total entries (statistics)
+    DevBuf<uint64_t> tmp;
+    tmp.alloc(b.N ? b.N : 1, s);
     uint64_t E = 0;
-    scan_u32_to_u64(cnt.get(), b.nb_off.get(), b.N, s, &E);
-    COLO_CUDA(cudaMemcpyAsync(b.nb_off.get() + b.N, &E, 8, cudaMemcpyHostToDevice, s));
+    if (b.N) scan_u32_to_u64(b.nb_cnt.get(), tmp.get(), b.N, s, &E);
     b.E = E;
-    b.nb.alloc(E, s);
-    if (E) dispatch_join(b, true, nullptr);
 }
 
 void eval_sqdist(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,

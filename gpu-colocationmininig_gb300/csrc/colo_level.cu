@@ -32,7 +32,8 @@ __device__ __forceinline__ void set_bit(uint32_t* words, uint32_t bit) {
 template <int K, int MODE>
 __global__ void __launch_bounds__(256) k_level(
     const CandDesc* __restrict__ cands, const uint64_t* __restrict__ chunk_off, uint64_t ncand,
-    uint64_t nchunks, const uint64_t* __restrict__ nb_off, const uint32_t* __restrict__ nb,
+    uint64_t nchunks, const uint64_t* __restrict__ nb_beg, const uint32_t* __restrict__ nb_cnt,
+    const uint32_t* __restrict__ nb,
     const float* __restrict__ x, const float* __restrict__ y, const uint32_t* __restrict__ fstart,
     const uint32_t* __restrict__ fcount, const JobGrid* __restrict__ grids,
     uint32_t* __restrict__ overflow, unsigned long long* __restrict__ items) {
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(256) k_level(
                 ry[i] = y[rid[i]];
             }
         }
-        uint64_t o0 = nb_off[a0], o1 = nb_off[a0 + 1];
+        uint64_t o0 = nb_beg[a0], o1 = o0 + nb_cnt[a0];
         slo = lower_bound_dev(nb, o0, o1, last_start);
         shi = lower_bound_dev(nb, slo, o1, last_end);
     }
@@ -277,7 +278,7 @@ void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
     uint64_t threads = w.nchunks * 32;
     unsigned grid = (unsigned)((threads + 255) / 256);
 #define COLO_LVL(KK)                                                                              \
-    k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_off.get(), \
+    k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_beg.get(), b.nb_cnt.get(), \
                                             b.nb.get(), b.x, b.y, b.fstart.get(), b.fcount.get(),  \
                                             b.grids.get(), ovf, w.items)
     switch (k) {

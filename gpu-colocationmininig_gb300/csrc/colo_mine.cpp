@@ -87,6 +87,18 @@ colo_status set_err(colo_ctx* ctx, colo_status st, const std::string& msg) {
     return st;
 }
 
+// Datasets keep their context alive: callers may free a context before its
+// datasets (garbage-collected bindings do), and a dataset frees its device
+// buffers on the context's stream.
+void ctx_release(colo_ctx* ctx) {
+    if (--ctx->refs > 0) return;
+    if (ctx->s) {
+        cudaStreamSynchronize(ctx->s);
+        cudaStreamDestroy(ctx->s);
+    }
+    delete ctx;
+}
+
 colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn) {
     try {
         return fn();
@@ -718,7 +730,6 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     for (uint32_t j = 0; j < J; ++j) {
         MineResult* r = outs[j];
         r->kernels = kt.stats;
-        r->counters[4] = 0;
         r->counters[5] = b.N;
         r->counters[6] = b.M;
         r->counters[7] = b.Rn;
@@ -729,6 +740,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->counters[12] = (b.jobs.size() == 1 && t_upload > 0.01) ? 12 * b.N : 0;
         r->counters[13] = cnt_d2h;
         r->counters[14] = b.nrl_total;
+        r->counters[4] = b.join_pairs;
         r->counters[15] = cnt_refined;
         r->times[0] = ms_since(t_all);
         r->times[1] = t_upload;
@@ -739,7 +751,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->times[6] = t_fill;
         r->times[7] = t_apriori;
         r->counters[0] = g_launches;
-        r->counters[1] = b.npl_total;
+        r->counters[1] = b.active_anchors;
         r->counters[2] = b.E;
         r->counters[3] = rows_written;
     }
@@ -802,11 +814,7 @@ colo_status colo_create(colo_ctx** out, int device) {
 
 colo_status colo_destroy(colo_ctx* ctx) {
     if (!ctx) return COLO_ERR_ARG;
-    if (ctx->s) {
-        cudaStreamSynchronize(ctx->s);
-        cudaStreamDestroy(ctx->s);
-    }
-    delete ctx;
+    ctx_release(ctx);
     return COLO_OK;
 }
 
@@ -842,6 +850,7 @@ colo_status colo_dataset_from_csv(colo_ctx* ctx, const char* path, colo_dataset*
         colo_status st = parse_points_csv(path, ds->hp, err);
         if (st != COLO_OK) return set_err(ctx, st, err);
         group_features(ds.get());
+        ctx->refs++;
         *out = ds.release();
         return COLO_OK;
     });
@@ -860,6 +869,7 @@ colo_status colo_dataset_from_host(colo_ctx* ctx, const float* x, const float* y
             if (fid[i] == -1) return set_err(ctx, COLO_ERR_INPUT, "feature id -1 is reserved by the reference");
         std::memcpy(ds->hp.bounds, bounds, 16);
         group_features(ds.get());
+        ctx->refs++;
         *out = ds.release();
         return COLO_OK;
     });
@@ -895,7 +905,8 @@ const char* colo_dataset_feature_name(const colo_dataset* ds, uint32_t f) {
 }
 void colo_dataset_free(colo_dataset* ds) {
     if (!ds) return;
-    if (ds->ctx) cudaStreamSynchronize(ds->ctx->s);
+    colo_ctx* ctx = ds->ctx;
+    if (ctx) cudaStreamSynchronize(ctx->s);
     if (ds->pinned && !ds->hp.x.empty()) {
         cudaHostUnregister(ds->hp.x.data());
         cudaHostUnregister(ds->hp.y.data());
@@ -903,6 +914,7 @@ void colo_dataset_free(colo_dataset* ds) {
         cudaGetLastError();
     }
     delete ds;
+    if (ctx) ctx_release(ctx);
 }
 
 colo_status colo_mine_batch(colo_ctx* ctx, colo_dataset* const* ds, const colo_params* p, uint32_t njobs,

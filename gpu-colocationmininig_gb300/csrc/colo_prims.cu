@@ -223,6 +223,11 @@ void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t
     scan_impl<uint32_t, uint32_t>(in, out, n, s, total_host);
 }
 
+void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
+                     uint64_t* total_host) {
+    scan_impl<uint64_t, uint64_t>(in, out, n, s, total_host);
+}
+
 void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};

@@ -85,11 +85,23 @@ colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint6
         }
         *total = b.E;
         cudaStream_t s = ctx->s;
-        if (offs && b.N) COLO_CUDA(cudaMemcpyAsync(offs, b.nb_off.get(), (b.N + 1) * 8, cudaMemcpyDeviceToHost, s));
-        if (offs && !b.N) offs[0] = 0;
-        if (nbr && b.E) {
-            if (cap < b.E) return COLO_ERR_CAPACITY;
-            COLO_CUDA(cudaMemcpyAsync(nbr, b.nb.get(), b.E * 4, cudaMemcpyDeviceToHost, s));
+        if (offs) offs[0] = 0;
+        if ((offs || nbr) && b.N) {
+            // compact the per-anchor lists into a CSR
+            std::vector<uint64_t> beg(b.N);
+            std::vector<uint32_t> cnt(b.N), all(b.nb_cap);
+            COLO_CUDA(cudaMemcpyAsync(beg.data(), b.nb_beg.get(), b.N * 8, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(cnt.data(), b.nb_cnt.get(), b.N * 4, cudaMemcpyDeviceToHost, s));
+            if (b.nb_cap)
+                COLO_CUDA(cudaMemcpyAsync(all.data(), b.nb.get(), b.nb_cap * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
+            if (nbr && cap < b.E) return COLO_ERR_CAPACITY;
+            uint64_t o = 0;
+            for (uint64_t a = 0; a < b.N; ++a) {
+                if (nbr) std::memcpy(nbr + o, all.data() + beg[a], cnt[a] * 4);
+                o += cnt[a];
+                if (offs) offs[a + 1] = o;
+            }
         }
         COLO_CUDA(cudaStreamSynchronize(s));
         return COLO_OK;

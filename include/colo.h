@@ -132,9 +132,9 @@ colo_status colo_result_write_patterns(const colo_result* r, const colo_dataset*
 /* Timing of the last mine, milliseconds: [0] total, [1] upload, [2] bucketing,
  * [3] join, [4] filter, [5] refine, [6] fill, [7] host Apriori. */
 colo_status colo_result_times(const colo_result* r, double* ms8);
-/* Work counters (n entries): [0] kernel launches, [1] neighbourhood-list
- * entries, [2] neighbour entries E, [3] table rows written, [4] fallback
- * candidates, [5] points, [6] occupied cells, [7] runs, [8] slice entries
+/* Work counters (n entries): [0] kernel launches, [1] join anchors with
+ * higher-feature neighbour cells, [2] neighbour entries E, [3] table rows
+ * written, [4] pair distance evaluations in the join, [5] points, [6] occupied cells, [7] runs, [8] slice entries
  * examined by count passes, [9] parent words read by count passes,
  * [10] table words written, [11] bitmap words, [12] host-to-device bytes,
  * [13] device-to-host bytes, [14] neighbourhood-run entries, [15] refined

@@ -115,7 +115,9 @@ def algorithmic_bytes(name: str, c: dict) -> float:
         return 24.0 * N
     if name == "npl_fill":         # read and write (id, x, y) per list entry
         return 24.0 * c["npl_entries"]
-    if name in ("join_count", "join_fill"):   # B_b = 12 N + 4 E + 8 (N + 1), split over the two passes
+    if name == "join":             # B_b = 12 N + 4 E + 8 (N + 1): points once, lists and offsets written
+        return 12.0 * N + 4.0 * E + 8.0 * (N + 1)
+    if name in ("join_count", "join_fill"):   # the same split over the two-pass layout
         return 12.0 * N + 4.0 * N if name == "join_count" else 4.0 * E + 8.0 * (N + 1)
     if name == "level_count":      # parent rows once + candidate slices once
         return 4.0 * c["count_parent_words"] + 4.0 * c["count_items"]
@@ -290,6 +292,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_b / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator; no public dataset exists)",
         "config": {"workload": WORKLOAD, "points": wl.n, "features": wl.nfeat, "candidates_per_step": cands,
+                   "join_active_anchors": int(counters["active_anchors"]), "join_pairs": int(counters["join_pairs"]),
+                   "neighbor_entries": int(counters["neighbors"]),
                    "form": "batched", "l2": "inputs (240 MB) larger than L2 (129 MB); no flush",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": "candidates/s", "ms_per_step": ms_e / args.steps,

@@ -45,6 +45,7 @@ struct Batch {
     DevBuf<uint32_t> cstart, crun, cjob;
     DevBuf<int32_t> nb9;
     DevBuf<uint32_t> cmask;
+    DevBuf<uint32_t> nbmask;     // per cell: feature mask of its geometric 3x3 block
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
     DevBuf<uint32_t> frun_off, frun;

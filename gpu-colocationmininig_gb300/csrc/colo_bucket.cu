@@ -127,6 +127,21 @@ __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint3
         }
 }
 
+// nbmask[c] = union of the feature masks of the occupied cells of c's
+// geometric 3x3 block (every quad containing c lies inside it).
+__global__ void k_nbmask(uint64_t M, uint32_t W, const int32_t* __restrict__ nb9,
+                         const uint32_t* __restrict__ cmask, uint32_t* __restrict__ nbmask) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= M * W) return;
+    uint64_t c = t / W;
+    uint32_t w = (uint32_t)(t % W), m = 0;
+    for (int q = 0; q < 9; ++q) {
+        int32_t v = nb9[c * 9 + q];
+        if (v >= 0) m |= cmask[(uint64_t)v * W + w];
+    }
+    nbmask[t] = m;
+}
+
 __global__ void k_frun_keys(uint64_t Rn, const uint32_t* __restrict__ rfeat, uint64_t* __restrict__ keys,
                             uint32_t* __restrict__ vals) {
     uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -303,6 +318,10 @@ void bucket_points(Batch& b) {
     count_launch();
     b.nb9.alloc((uint64_t)M * 9, s);
     k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get());
+    COLO_LAUNCH_CHECK();
+    count_launch();
+    b.nbmask.alloc((uint64_t)M * b.W, s);
+    k_nbmask<<<grid_for((uint64_t)M * b.W, 256), 256, 0, s>>>(M, b.W, b.nb9.get(), b.cmask.get(), b.nbmask.get());
     COLO_LAUNCH_CHECK();
     count_launch();
 

@@ -32,7 +32,7 @@ constexpr int kMaxW = 8;   // mask words handled in registers (256 features per 
 // job changes rarely and the F x F accumulator lives in shared memory.
 __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
     uint64_t Rn, const uint32_t* __restrict__ rcell, const uint32_t* __restrict__ cjob,
-    const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
+    const JobGrid* __restrict__ grids, const uint32_t* __restrict__ nbmask,
     uint32_t W, const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt,
     const uint64_t* __restrict__ job_off, uint32_t* __restrict__ ub2, uint32_t acc_dim, uint64_t runs_per_block) {
     extern __shared__ uint32_t acc[];   // acc_dim x acc_dim (acc_dim = 0: no privatisation)
@@ -65,12 +65,8 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
             if (g.gx >= 2 && g.gy >= 2) {
                 const bool priv = acc_dim && (int32_t)job == cur_job && g.nf <= acc_dim;
                 const uint32_t lf = rfeat[r] - g.f0, cnt = rcnt[r];
-                int32_t nb[9];
-                for (int q = 0; q < 9; ++q) nb[q] = nb9[(uint64_t)c * 9 + q];
                 for (uint32_t w = 0; w < W; ++w) {
-                    uint32_t bits = 0;
-                    for (int q = 0; q < 9; ++q)
-                        if (nb[q] >= 0) bits |= cmask[(uint64_t)nb[q] * W + w];
+                    uint32_t bits = nbmask[(uint64_t)c * W + w];
                     while (bits) {
                         int bpos = __ffs(bits) - 1;
                         bits &= bits - 1;
@@ -115,8 +111,8 @@ __global__ void k_filter_level(uint64_t nitems, uint64_t ncand, uint32_t k,
                                const uint32_t* __restrict__ frun, const uint32_t* __restrict__ rcell,
                                const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                                const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                               const uint32_t* __restrict__ cmask, uint32_t W,
-                               const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
+                               const uint32_t* __restrict__ cmask, const uint32_t* __restrict__ nbmask,
+                               uint32_t W, const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
                                const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub) {
     for (uint64_t item = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; item < nitems;
          item += (uint64_t)gridDim.x * blockDim.x) {
@@ -141,6 +137,11 @@ __global__ void k_filter_level(uint64_t nitems, uint64_t ncand, uint32_t k,
             uint32_t lf = mem[j] - g.f0;
             need[lf >> 5] |= 1u << (lf & 31);
         }
+        // every quad containing C lies in C's 3x3 block: all members must be there
+        bool present = true;
+        for (uint32_t w = 0; w < W; ++w)
+            if ((nbmask[(uint64_t)C * W + w] & need[w]) != need[w]) present = false;
+        if (!present) continue;
         const uint32_t lfd = fd - g.f0;
         const uint64_t local = ckey[C] - g.key_base;
         const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
@@ -221,7 +222,7 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     blocks = (b.Rn + per - 1) / per;
     KScope ks("filter_pairs");
     k_filter_pairs<<<(unsigned)blocks, kFilterThreads, smem, s>>>(
-        b.Rn, b.rcell.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.W, b.rfeat.get(),
+        b.Rn, b.rcell.get(), b.cjob.get(), b.grids.get(), b.nbmask.get(), b.W, b.rfeat.get(),
         b.rcnt.get(), d_job_off.get(), ub2.get(), acc_dim, per);
     COLO_LAUNCH_CHECK();
     count_launch();
@@ -238,7 +239,7 @@ void filter_level(Batch& b, const uint32_t* d_cand, const uint32_t* d_driver, co
     KScope ks("filter_level");
     k_filter_level<<<(unsigned)blocks, 256, 0, b.s>>>(
         nitems, ncand, k, d_cand, d_driver, d_item_off, b.frun_off.get(), b.frun.get(), b.rcell.get(),
-        b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.W, b.crun.get(),
+        b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.nbmask.get(), b.W, b.crun.get(),
         b.rfeat.get(), b.rcnt.get(), d_ub);
     COLO_LAUNCH_CHECK();
     count_launch();

@@ -37,77 +37,75 @@ namespace {
 /* ------------------------------------------------------------------------ */
 
 /* Codes/Utility_Inline.h:25-33: squareDistance = pow(x2-x1,2) + pow(y2-y1,2)
- * in float on the device with nvcc defaults.  Measured on a GB300 over every
- * mantissa of 81 binades, the device pow(d, 2) is the correctly rounded
- * square except when d*d lies exactly halfway between two floats, where it
- * may return either neighbour; the two squares are then added with one
- * correctly rounded float add.  CUDA's pow itself is not restated here.
- * The host therefore knows the comparison sq <= R^2 exactly unless an exact
- * tie can flip it; such pairs are "ambiguous" and are resolved by a device
- * evaluation of the reference expression supplied by the caller. */
+ * with float differences and the result stored in a float.  Measured on a
+ * GB300 (see tests/test_gpu_sqdist.py), the device value is the correctly
+ * rounded float of the exact sum S = dx^2 + dy^2, except when S lies on (or
+ * within a few double ulps of) a rounding midpoint between two floats, where
+ * either neighbour can come out -- the behaviour of pow evaluated in double
+ * and rounded to float once.  CUDA's pow itself is not restated here: the
+ * host computes S exactly (double-double) and calls a comparison "ambiguous"
+ * when such a midpoint could flip it; ambiguous pairs are resolved by a
+ * device evaluation of the reference expression supplied by the caller. */
 struct SqDecision {
     bool le;          /* sq <= R2 (for ambiguous pairs: the round-to-even guess) */
     bool ambiguous;
 };
 
-inline void square_candidates(float d, float* c, int* nc) {
-    double e = (double)d * (double)d;          /* exact for a float d */
-    float rn = (float)e;                       /* round to nearest even */
-    if (e == 0.0) {
-        c[0] = 0.0f;
-        *nc = 1;
-        return;
+struct ExactSq {
+    float rn;         /* correctly rounded float of S (ties to even) */
+    float other;      /* the other neighbour when S is near a midpoint */
+    bool near_mid;
+};
+
+inline ExactSq exact_sq(float x1, float y1, float x2, float y2) {
+    float dx = x2 - x1;
+    float dy = y2 - y1;
+    double a = (double)dx * (double)dx;          /* exact */
+    double b = (double)dy * (double)dy;          /* exact */
+    double hi = a + b;                           /* TwoSum: S = hi + lo exactly */
+    double bb = hi - a;
+    double lo = (a - (hi - bb)) + (b - bb);
+    ExactSq r;
+    r.near_mid = false;
+    r.rn = (float)hi;
+    r.other = r.rn;
+    if (!(hi < 3.0e38)) return r;                /* overflow range: never near R^2 */
+    /* neighbours of S and their midpoint (exact in double) */
+    float l = (double)r.rn <= hi ? r.rn : std::nextafter(r.rn, -INFINITY);
+    float h = std::nextafter(l, INFINITY);
+    if ((double)l == hi && lo == 0.0) return r;  /* S is a float */
+    double mid = 0.5 * ((double)l + (double)h);
+    double d = hi - mid;                         /* exact (Sterbenz) */
+    /* sign of S - mid = d + lo */
+    bool above = d > 0 || (d == 0 && lo > 0);
+    bool below = d < 0 || (d == 0 && lo < 0);
+    if (above) {
+        r.rn = h;
+    } else if (below) {
+        r.rn = l;
+    } else {                                     /* exact midpoint: ties to even */
+        uint32_t lbits;
+        std::memcpy(&lbits, &l, 4);
+        r.rn = (lbits & 1u) ? h : l;
     }
-    if (e < 1e-36) {                           /* below the measured binades: bracket */
-        c[0] = 0.0f;
-        c[1] = std::nextafter(rn, INFINITY);
-        *nc = 2;
-        return;
+    double gap = std::fabs(d + lo);
+    if (gap <= std::ldexp(hi, -44)) {            /* within ~256 double ulps of the midpoint */
+        r.near_mid = true;
+        r.other = (r.rn == l) ? h : l;
     }
-    if (e > 3.0e38) {                          /* may overflow to infinity */
-        c[0] = rn;
-        c[1] = INFINITY;
-        *nc = 2;
-        return;
-    }
-    if ((double)rn == e) {
-        c[0] = rn;
-        *nc = 1;
-        return;
-    }
-    float other = (double)rn < e ? std::nextafter(rn, INFINITY) : std::nextafter(rn, 0.0f);
-    if ((double)rn + (double)other == 2.0 * e) {   /* exact tie */
-        c[0] = rn;
-        c[1] = other;
-        *nc = 2;
-        return;
-    }
-    c[0] = rn;
-    *nc = 1;
+    return r;
 }
 
 inline SqDecision sq_decide(float x1, float y1, float x2, float y2, float R2) {
-    float dx = x2 - x1;
-    float dy = y2 - y1;
-    float a[2], b[2];
-    int na, nb;
-    square_candidates(dx, a, &na);
-    square_candidates(dy, b, &nb);
+    ExactSq e = exact_sq(x1, y1, x2, y2);
     SqDecision out;
-    out.le = (a[0] + b[0]) <= R2;
-    out.ambiguous = false;
-    for (int i = 0; i < na; ++i)
-        for (int j = 0; j < nb; ++j)
-            if (((a[i] + b[j]) <= R2) != out.le) out.ambiguous = true;
+    out.le = e.rn <= R2;
+    out.ambiguous = e.near_mid && ((e.other <= R2) != out.le);
     return out;
 }
 
-/* Squared distance value when no tie is involved (used by oracle_sqdist). */
-inline float sqdist(float x1, float y1, float x2, float y2) {
-    float dx = x2 - x1;
-    float dy = y2 - y1;
-    return (float)((double)dx * dx) + (float)((double)dy * dy);
-}
+/* Squared distance value away from rounding midpoints (used by oracle_sqdist). */
+inline float sqdist(float x1, float y1, float x2, float y2) { return exact_sq(x1, y1, x2, y2).rn; }
 
 /* Device float -> u32 conversion (cvt.rzi.u32.f32 clamps to the range). */
 inline uint32_t f2u_sat(float f) {
@@ -914,13 +912,15 @@ uint64_t oracle_neighbors(const float* x, const float* y, const uint32_t* feat, 
 }
 
 void oracle_sq_decide_batch(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,
-                            float R2, uint8_t* le, uint8_t* ambiguous, float* value) {
+                            float R2, uint8_t* le, uint8_t* ambiguous, float* value, uint8_t* near_mid) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
         SqDecision dc = sq_decide(x1[i], y1[i], x2[i], y2[i], R2);
         le[i] = dc.le;
         ambiguous[i] = dc.ambiguous;
-        if (value) value[i] = sqdist(x1[i], y1[i], x2[i], y2[i]);
+        ExactSq e = exact_sq(x1[i], y1[i], x2[i], y2[i]);
+        if (value) value[i] = e.rn;
+        if (near_mid) near_mid[i] = e.near_mid;
     }
 }
 

@@ -39,15 +39,18 @@ int oracle_make_grid(float min_x, float min_y, float max_x, float max_y, float R
 uint64_t oracle_cell_ids(const oracle_grid* g, const float* x, const float* y,
                          uint64_t n, uint64_t* cell_out);
 
-/* Squared distance of Codes/Utility_Inline.h:25-33 assuming no exact tie
- * (correctly rounded squares, one float add). */
+/* Squared distance of Codes/Utility_Inline.h:25-33 as the device computes it
+ * away from float rounding midpoints: the correctly rounded float of the
+ * exact dx^2 + dy^2. */
 float oracle_sqdist(float x1, float y1, float x2, float y2);
-/* The comparison sq <= R2 as the device makes it; *ambiguous = 1 when an
- * exact tie in a square could flip it (then the return is a guess). */
+/* The comparison sq <= R2 as the device makes it; *ambiguous = 1 when the
+ * exact sum lies so close to a float rounding midpoint that the device's
+ * rounding could flip it (then the return is the round-to-even guess). */
 int oracle_sq_decide(float x1, float y1, float x2, float y2, float R2, int* ambiguous);
-/* The same for n pairs; value[i] = the tie-free squared distance. */
+/* The same for n pairs; value[i] = correctly rounded squared distance,
+ * near_mid[i] = 1 when the exact sum is within the midpoint window. */
 void oracle_sq_decide_batch(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,
-                            float R2, uint8_t* le, uint8_t* ambiguous, float* value);
+                            float R2, uint8_t* le, uint8_t* ambiguous, float* value, uint8_t* near_mid);
 /* Keys (i << 32 | j, i < j, different features) of every ambiguous pair;
  * returns the count, copies up to cap keys (sorted). */
 uint64_t oracle_ambiguous_pairs(const float* x, const float* y, const uint32_t* feat, uint64_t n,

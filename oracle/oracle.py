@@ -70,7 +70,8 @@ def load():
         "oracle_parse_params": (C.c_int, [C.c_char_p, _f32p, _f32p, _u32p]),
         "oracle_sq_decide": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_int)]),
         "oracle_sqdist": (C.c_float, [C.c_float, C.c_float, C.c_float, C.c_float]),
-        "oracle_sq_decide_batch": (None, [_f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _u8p, _u8p, _f32p]),
+        "oracle_sq_decide_batch": (None, [_f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _u8p, _u8p, _f32p,
+                                          _u8p]),
         "oracle_ambiguous_pairs": (C.c_uint64, [_f32p, _f32p, _u32p, C.c_uint64, C.c_float, _u64p, C.c_uint64]),
         "oracle_cell_adjacent": (C.c_int, [V, C.c_uint64, C.c_uint64]),
         "oracle_make_grid": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, V]),
@@ -274,11 +275,13 @@ def sq_decide(x1, y1, x2, y2, R2):
 
 
 def sq_decide_batch(x1, y1, x2, y2, R2):
-    """(le, ambiguous, tie-free value) for arrays of point pairs."""
+    """(le, ambiguous, value, near_mid) for arrays of point pairs."""
     a = [np.ascontiguousarray(v, np.float32) for v in (x1, y1, x2, y2)]
     n = len(a[0])
     le = np.zeros(n, np.uint8)
     amb = np.zeros(n, np.uint8)
     val = np.zeros(n, np.float32)
-    load().oracle_sq_decide_batch(*[_p(v, _f32p) for v in a], n, R2, _p(le, _u8p), _p(amb, _u8p), _p(val, _f32p))
-    return le.astype(bool), amb.astype(bool), val
+    near = np.zeros(n, np.uint8)
+    load().oracle_sq_decide_batch(*[_p(v, _f32p) for v in a], n, R2, _p(le, _u8p), _p(amb, _u8p), _p(val, _f32p),
+                                  _p(near, _u8p))
+    return le.astype(bool), amb.astype(bool), val, near.astype(bool)

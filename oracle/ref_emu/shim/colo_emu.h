@@ -5,9 +5,8 @@
 // its kernel-launch statements, which build_ref.py rewrites in memory into
 // colo_emu_launch(...) calls.  Device memory is host memory; kernels run
 // block by block; threads of a block run as user-level fibers so that
-// __syncthreads is a real barrier.  pow(float, int) follows the device
-// behaviour measured on a GB300 for squares: the correctly rounded square
-// (golden fixtures use coordinates whose squared differences never tie).
+// __syncthreads is a real barrier.  Golden fixtures use integer coordinates,
+// so every squared distance is exact and no rounding question arises.
 #pragma once
 #include <ucontext.h>
 
@@ -85,12 +84,9 @@ const float DEG_TO_RAD = 0.017453292519943295f;
 const float EARTH_RADIUS_IN_METERS = 6372797.560856f;
 
 // ---- device functions -----------------------------------------------------
-inline float pow(float a, int b) {
-    if (b == 2) return (float)((double)a * (double)a);   // correctly rounded square
-    double r = 1.0;
-    for (int i = 0; i < (b < 0 ? -b : b); ++i) r *= a;
-    return (float)(b < 0 ? 1.0 / r : r);
-}
+// pow(float, int) is left to the host library: C++ promotes it to double, as
+// the device does, so the reference's squared distance is formed in double
+// and rounded to float once on both.
 inline unsigned int atomicInc(unsigned int* a, unsigned int v) {
     unsigned int old = *a;
     *a = (old >= v) ? 0u : old + 1u;

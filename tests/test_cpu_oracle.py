@@ -69,13 +69,18 @@ def test_participation_window_quirk():
     assert lev.pi[0] == 0.0
 
 
-def test_sq_decide_exact_and_tie_cases():
-    # integer coordinates: exact squares, no ambiguity
+def test_sq_decide_exact_and_midpoint_cases():
+    # integer coordinates: the exact sum is a float, no ambiguity
     assert oracle.sq_decide(0, 0, 6, 8, 100.0) == (True, False)
     assert oracle.sq_decide(0, 0, 6, 8.0001, 100.0) == (False, False)
-    le, amb, val = oracle.sq_decide_batch(np.zeros(3), np.zeros(3), np.array([3, 4, 1.5]),
-                                          np.array([4, 3, 2.0]), 25.0)
-    assert le.tolist() == [True, True, True] and not amb.any()
+    le, amb, val, near = oracle.sq_decide_batch(np.zeros(3), np.zeros(3), np.array([3, 4, 1.5]),
+                                                np.array([4, 3, 2.0]), 25.0)
+    assert le.tolist() == [True, True, True] and not amb.any() and not near.any()
+    assert val.tolist() == [25.0, 25.0, 6.25]
+    # a sum exactly halfway between two floats is near a midpoint: 2^24 + 1
+    le, amb, val, near = oracle.sq_decide_batch(np.zeros(1), np.zeros(1), np.array([4096.0]), np.array([1.0]),
+                                                16777216.0)
+    assert near.all() and amb.all()
 
 
 def test_parse_params_and_csv(tmp_path):

@@ -39,6 +39,7 @@ EXPORTS = [
     "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
+    "colo_stage_within",
 ]
 
 
@@ -114,6 +115,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_stage_neighbors": (C.c_int, [_P, _P, C.c_float, _u64p, _u32p, _u64p]),
         "colo_stage_filter": (C.c_int, [_P, _P, C.c_float, C.c_float, _u32p, C.c_uint64, C.c_uint32, _u64p, _u8p]),
         "colo_stage_sqdist": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, _f32p]),
+        "colo_stage_within": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _f32p, _u8p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -306,6 +308,15 @@ class Context:
 
     def stream(self) -> int:
         return int(self.lib.colo_ctx_stream(self.h) or 0)
+
+    def stage_within(self, x1, y1, x2, y2, R2: float):
+        """(reference squared distance, kernels' decision sq <= R2) per pair."""
+        a = [np.ascontiguousarray(v, np.float32) for v in (x1, y1, x2, y2)]
+        out = np.zeros(len(a[0]), np.float32)
+        w = np.zeros(len(a[0]), np.uint8)
+        self.check(self.lib.colo_stage_within(self.h, *[_ptr(v, _f32p) for v in a], len(out), R2, _ptr(out, _f32p),
+                                              _ptr(w, _u8p)), "stage_within")
+        return out, w.astype(bool)
 
     def close(self):
         if getattr(self, "h", None):

@@ -123,8 +123,9 @@ void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow
 // (A = set bits in [0, n-2]).
 void level_pi(Batch& b, const CandDesc* d_cands, uint64_t ncand, uint32_t k, uint64_t* d_stats);
 
-// Squared-distance evaluation of the reference expression for n pairs.
+// Squared-distance evaluation of the reference expression for n pairs; with
+// `within`, also the kernels' decision ref_within(...) for threshold R2.
 void eval_sqdist(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,
-                 float* out, cudaStream_t s);
+                 float* out, cudaStream_t s, float R2 = 0.0f, uint8_t* within = nullptr);
 
 }  // namespace colo

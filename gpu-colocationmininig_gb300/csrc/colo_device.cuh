@@ -16,6 +16,27 @@ __device__ __forceinline__ float ref_sqdist(float x1, float y1, float x2, float 
     return squareDistance;
 }
 
+// The reference's neighbour test ref_sqdist(...) <= R2, decided with two
+// FP32 FMAs whenever the exact squared distance S is clearly away from the
+// boundary, and with the reference expression itself otherwise.
+//
+// The reference value is the float nearest to S (pow is evaluated in double
+// and the sum rounded to float once), so it is <= R2 exactly when S lies
+// below the midpoint R2 + hu between R2 and the next float (hu = half an ulp
+// of R2).  t2 = fma(dx, dx, fma(dy, dy, -R2)) approximates S - R2 with an
+// error below 2^-24 (|t1| + |t2|); eps is that bound with an 8x margin plus
+// the rounding of the comparisons.  Inside the band the expression itself
+// decides, so the result equals ref_sqdist(...) <= R2 for every input.
+__device__ __forceinline__ bool ref_within(float x1, float y1, float x2, float y2, float R2, float hu) {
+    const float dx = x2 - x1, dy = y2 - y1;
+    const float t1 = __fmaf_rn(dy, dy, -R2);
+    const float t2 = __fmaf_rn(dx, dx, t1);
+    const float eps = (fabsf(t1) + fabsf(t2) + hu) * 4.8e-7f + 1e-37f;
+    if (t2 < hu - eps) return true;
+    if (t2 > hu + eps) return false;
+    return ref_sqdist(x1, y1, x2, y2) <= R2;
+}
+
 // Cell of a point (Codes/DeviceProcess_Kernel.h:615-625): float subtract,
 // float divide, float->u32 conversion (saturating on the device).
 __device__ __forceinline__ uint64_t ref_cell(const JobGrid& g, float x, float y) {

@@ -31,13 +31,13 @@ constexpr int kMaxMembersFiltered = 8;  // filter counts members j < 8 (block (8
 struct JobGrid {
     float min_x, min_y, w;       // grid origin and cell width (= R)
     float R2;                    // R*R in float
+    float R2hu;                  // half an ulp of R2 (the rounding gap above R2)
     float thr;                   // PI threshold
     uint32_t gx, gy;
     uint64_t total;              // gx*gy
     uint64_t key_base;           // first cell key of this job in the batch
     int32_t compat32;            // 32-bit reference cell arithmetic is exact
     uint32_t f0, nf;             // global feature range of the job
-    uint32_t pad;
 };
 
 // Error carrier for kernels: bounded waits and range checks record here.

@@ -15,6 +15,8 @@
 // number of target points) and writes its hits there, so no counting pass is
 // needed; when the upper bounds would not fit, a count pass + scan + fill
 // pass produces a compact layout instead.
+#include <cmath>
+
 #include "colo_batch.h"
 #include "colo_device.cuh"
 
@@ -64,7 +66,8 @@ __global__ void __launch_bounds__(256) k_join(
     const uint32_t r = act_run[i];
     const uint32_t a = sid[p];
     const float xa = sx[p], ya = sy[p];
-    const float R2 = grids[fjob[sfeat[p]]].R2;
+    const JobGrid& g = grids[fjob[sfeat[p]]];
+    const float R2 = g.R2, hu = g.R2hu;
     const uint64_t qend = nrl_off[scell[p] + 1];
     uint64_t base = 0;
     if (MODE == J_SINGLE) base = cap_off[r] + (uint64_t)(p - rstart[r]) * run_L[r];
@@ -76,7 +79,7 @@ __global__ void __launch_bounds__(256) k_join(
         for (uint32_t b0 = 0; b0 < tc; b0 += T) {
             const uint32_t t = b0 + gl;
             bool ok = false;
-            if (t < tc) ok = ref_sqdist(xa, ya, sx[ts + t], sy[ts + t]) <= R2;
+            if (t < tc) ok = ref_within(xa, ya, sx[ts + t], sy[ts + t], R2, hu);
             const uint32_t bal = (__ballot_sync(gmask, ok) >> gbase) & ((T == 32) ? 0xffffffffu : ((1u << T) - 1u));
             if (MODE != J_COUNT && ok) nb[base + k + __popc(bal & ((1u << gl) - 1u))] = sid[ts + t];
             k += __popc(bal);
@@ -120,9 +123,11 @@ void dispatch_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, cons
 
 __global__ void k_sqdist(const float* __restrict__ x1, const float* __restrict__ y1,
                          const float* __restrict__ x2, const float* __restrict__ y2, uint64_t n,
-                         float* __restrict__ out) {
+                         float* __restrict__ out, float R2, float hu, uint8_t* __restrict__ within) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = ref_sqdist(x1[i], y1[i], x2[i], y2[i]);
+    if (i >= n) return;
+    out[i] = ref_sqdist(x1[i], y1[i], x2[i], y2[i]);
+    if (within) within[i] = ref_within(x1[i], y1[i], x2[i], y2[i], R2, hu) ? 1 : 0;
 }
 
 inline unsigned grid_for(uint64_t n, int threads) {
@@ -190,9 +195,10 @@ void join_neighbors(Batch& b) {
 }
 
 void eval_sqdist(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,
-                 float* out, cudaStream_t s) {
+                 float* out, cudaStream_t s, float R2, uint8_t* within) {
     if (n == 0) return;
-    k_sqdist<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x1, y1, x2, y2, n, out);
+    float hu = (std::nextafter(R2, INFINITY) - R2) * 0.5f;
+    k_sqdist<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x1, y1, x2, y2, n, out, R2, hu, within);
     COLO_LAUNCH_CHECK();
     count_launch();
 }

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) k_level(
     const uint32_t flast = d.m[k - 1];
     const uint32_t last_start = fstart[flast];
     const uint32_t last_end = last_start + fcount[flast];
-    const float R2 = grids[d.job].R2;
+    const float R2 = grids[d.job].R2, hu = grids[d.job].R2hu;
 
     // row members (ids) and coordinates of members 1..k-2
     uint32_t rid[KR];
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_level(
                 const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
                 for (uint32_t i = 1; i + 1 < k && ok; ++i) {
                     uint32_t ri = d.parent[(uint64_t)i * d.pstride + prow_j];
-                    ok = ref_sqdist(x[ri], y[ri], xb, yb) <= R2;
+                    ok = ref_within(x[ri], y[ri], xb, yb, R2, hu);
                 }
             }
         } else if (K > 2) {
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256) k_level(
             for (int i = 1; i < KR - 1; ++i) {
                 float xi = __shfl_sync(0xffffffffu, rx[i], j);
                 float yi = __shfl_sync(0xffffffffu, ry[i], j);
-                ok = ok && ref_sqdist(xi, yi, xb, yb) <= R2;
+                ok = ok && ref_within(xi, yi, xb, yb, R2, hu);
             }
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, ok);

@@ -76,6 +76,7 @@ JobGrid make_grid(const float bounds[4], float R, float thr) {
     g.total = (uint64_t)g.gx * g.gy;
     g.compat32 = (g.total + g.gx) < (1ull << 31) ? 1 : 0;
     g.R2 = R * R;
+    g.R2hu = (std::nextafter(g.R2, INFINITY) - g.R2) * 0.5f;
     g.thr = thr;
     return g;
 }

@@ -188,10 +188,17 @@ colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float th
 
 colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, const float* x2, const float* y2,
                               uint64_t n, float* out) {
-    if (!ctx || (n && (!x1 || !y1 || !x2 || !y2 || !out))) return COLO_ERR_ARG;
+    return colo_stage_within(ctx, x1, y1, x2, y2, n, 0.0f, out, nullptr);
+}
+
+colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2, const float* y2,
+                              uint64_t n, float R2, float* out, uint8_t* within) {
+    if (!ctx || (n && (!x1 || !y1 || !x2 || !y2 || (!out && !within)))) return COLO_ERR_ARG;
     return run_guarded(ctx, [&]() -> colo_status {
         cudaStream_t s = ctx->s;
         DevBuf<float> a, b, c, d, o;
+        DevBuf<uint8_t> w;
+        if (within) w.alloc(n, s);
         a.alloc(n, s);
         b.alloc(n, s);
         c.alloc(n, s);
@@ -202,8 +209,9 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
             COLO_CUDA(cudaMemcpyAsync(b.get(), y1, n * 4, cudaMemcpyHostToDevice, s));
             COLO_CUDA(cudaMemcpyAsync(c.get(), x2, n * 4, cudaMemcpyHostToDevice, s));
             COLO_CUDA(cudaMemcpyAsync(d.get(), y2, n * 4, cudaMemcpyHostToDevice, s));
-            eval_sqdist(a.get(), b.get(), c.get(), d.get(), n, o.get(), s);
-            COLO_CUDA(cudaMemcpyAsync(out, o.get(), n * 4, cudaMemcpyDeviceToHost, s));
+            eval_sqdist(a.get(), b.get(), c.get(), d.get(), n, o.get(), s, R2, within ? w.get() : nullptr);
+            if (out) COLO_CUDA(cudaMemcpyAsync(out, o.get(), n * 4, cudaMemcpyDeviceToHost, s));
+            if (within) COLO_CUDA(cudaMemcpyAsync(within, w.get(), n, cudaMemcpyDeviceToHost, s));
         }
         COLO_CUDA(cudaStreamSynchronize(s));
         return COLO_OK;

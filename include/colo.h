@@ -171,6 +171,11 @@ colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float th
  * on the device for n point pairs: out[i] = sq(x1,y1,x2,y2) bits. */
 colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
                               const float* y2, uint64_t n, float* out);
+/* The same plus, in within[i], the decision the join and level kernels take
+ * for sq <= R2 (their fast FMA test with the reference expression as the
+ * fallback near the boundary); either output may be NULL. */
+colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
+                              const float* y2, uint64_t n, float R2, float* out, uint8_t* within);
 
 #ifdef __cplusplus
 }

@@ -55,6 +55,18 @@ def test_device_squared_distance_matches_oracle_model(ctx, scale, R, dec):
     assert amb.mean() < 1e-3
 
 
+@pytest.mark.parametrize("scale,R,dec", [(1e6, 10.0, None), (16011.3, 10.0, 2), (1e4, 20.0, 1), (1.0, 0.37, None),
+                                         (2e6, 3.3, 3), (600.0, 10.0, 0)])
+def test_kernel_decision_equals_reference_expression(ctx, scale, R, dec):
+    # the join and level kernels decide sq <= R2 with FMAs and fall back to the
+    # reference expression near the boundary: identical decisions everywhere
+    rng = np.random.default_rng(int(scale) + 7)
+    x1, y1, x2, y2 = _pairs(rng, 2_000_000, scale, R, dec)
+    R2 = float(np.float32(R) * np.float32(R))
+    sq, within = ctx.stage_within(x1, y1, x2, y2, R2)
+    assert np.array_equal(within, sq <= np.float32(R2))
+
+
 def test_symmetric(ctx):
     rng = np.random.default_rng(7)
     x1, y1, x2, y2 = _pairs(rng, 500_000, 1e5, 25.0, 2)

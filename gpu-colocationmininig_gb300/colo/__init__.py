@@ -39,7 +39,7 @@ EXPORTS = [
     "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
-    "colo_stage_within",
+    "colo_stage_within", "colo_table_pi_static",
 ]
 
 
@@ -116,6 +116,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_stage_filter": (C.c_int, [_P, _P, C.c_float, C.c_float, _u32p, C.c_uint64, C.c_uint32, _u64p, _u8p]),
         "colo_stage_sqdist": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, _f32p]),
         "colo_stage_within": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _f32p, _u8p]),
+        "colo_table_pi_static": (C.c_int, [_P, C.c_uint64, C.c_uint32, _u32p, _u32p, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -177,6 +177,35 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
 colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
                               const float* y2, uint64_t n, float R2, float* out, uint8_t* within);
 
+/* ---- allocation-free entry point -------------------------------------- */
+/* No counterpart in the reference (the reference allocates its participation
+ * bitmaps with cudaMalloc per candidate).  For callers that cannot call
+ * cudaMalloc: hosts whose own pool holds the GPU's memory (an allocation
+ * behind the pool's back fails or breaks its accounting) and latency-bound
+ * services that cannot accept cudaFree's device-wide synchronisation.
+ *
+ * Participation numerators and PI of one size-k candidate (2 <= k <= 32)
+ * from its instance table, as colo_mine computes them:
+ *   table  device, rows*k point ids, row-major (colo_result_table's layout)
+ *   fstart, fcount  host, k entries: first point id and instance count of
+ *          each member feature; ids outside [fstart, fstart+fcount) are not
+ *          counted, and then num[] = UINT64_MAX and *pi = NaN
+ *   num    device, k numerators;  pi  device, 1 float (may be NULL)
+ *   stream cudaStream_t on the calling thread's current device (NULL: the
+ *          legacy default stream); the call only enqueues work.
+ * Allocates nothing: the bitmaps live in a fixed device array of
+ * COLO_TABLE_PI_STATIC_WORDS 32-bit words (4 MiB, plus 2 KiB of control
+ * words), held by every GPU where the library is loaded until exit.
+ * COLO_ERR_CAPACITY when the sum over members of ceil(fcount/32) exceeds it.
+ * The first call on a device looks up the array's device address (once per
+ * device); make that first call before any stream capture.  All calls share
+ * the array and each clears what it uses: calls that overlap on the GPU race
+ * and give wrong results. */
+#define COLO_TABLE_PI_STATIC_WORDS (1u << 20)
+colo_status colo_table_pi_static(const uint32_t* table, uint64_t rows, uint32_t k,
+                                 const uint32_t* fstart, const uint32_t* fcount, uint64_t* num,
+                                 float* pi, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

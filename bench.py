@@ -106,15 +106,24 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def algorithmic_bytes(name: str, c: dict) -> float:
-    """Algorithmic bytes of all launches of one kernel family (per-stage formulas)."""
-    N, E = c["points"], c["neighbors"]
-    if name == "radix_sort":       # per pass: read and write (8 B key + 4 B id)
-        return 24.0 * N
+def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
+    """Algorithmic bytes of all launches (per step) of one kernel family.
+
+    `launches` = launches per step, `words` = 32-bit mask words per cell.
+    """
+    N, E, M, Rn = c["points"], c["neighbors"], c["cells"], c["runs"]
+    if name == "radix_sort":       # per digit pass over the points: read and write (8 B key + 4 B id)
+        return 24.0 * N * launches
+    if name == "run_sort":         # per digit pass over the runs
+        return 24.0 * Rn * launches
     if name == "cell_keys":        # read x, y, feature; write key, id
         return 24.0 * N
-    if name == "npl_fill":         # read and write (id, x, y) per list entry
-        return 24.0 * c["npl_entries"]
+    if name == "cell_neighbours":  # read the key, write 9 neighbour indices
+        return 44.0 * M
+    if name == "quad_masks":       # read 9 indices + masks, write 4 quad masks + the 3x3 union
+        return 36.0 * M + 4.0 * words * M * 6
+    if name == "nrl_fill":         # write (feature, run) per list entry + per-run suffix and count
+        return 8.0 * c["nrl_entries"] + 12.0 * Rn
     if name == "join":             # B_b = 12 N + 4 E + 8 (N + 1): points once, lists and offsets written
         return 12.0 * N + 4.0 * E + 8.0 * (N + 1)
     if name in ("join_count", "join_fill"):   # the same split over the two-pass layout
@@ -126,7 +135,9 @@ def algorithmic_bytes(name: str, c: dict) -> float:
     if name == "level_pi":
         return 4.0 * c["bitmap_words"]
     if name == "filter_pairs":
-        return 8.0 * c["runs"] + 4.0 * c["cells"]
+        return 8.0 * Rn + 4.0 * words * M
+    if name == "filter_level":     # per item the driver cell's 4 quad masks; per (cell of U_c, member) one run
+        return 16.0 * words * c["filter_items"] + 8.0 * c["filter_cell_members"]
     return 0.0
 
 
@@ -244,7 +255,7 @@ def main():
         return ms, results, clk.summary()
 
     forms = set(args.forms.split(","))
-    ms_b, res_b, clocks = timed(colo.MODE_BATCHED, True, profile=True)
+    ms_b, res_b, clocks = timed(colo.MODE_BATCHED, True)
     cands = res_b[0].num_candidates()
     value = cands * args.steps * world / (ms_b / 1e3)
     ms_e, res_e, ms_p, res_p = ms_b, res_b, ms_b, res_b
@@ -257,27 +268,36 @@ def main():
     # every form mined the same patterns
     same = all(r.patterns() == res_b[0].patterns() for r in res_b + res_e + res_p)
 
-    # roofline of the dominant kernel (CUDA events on the library's stream)
+    # per-kernel CUDA-event times (a separate profiled pass, so `value` carries no event overhead)
+    ms_k, res_k, _ = timed(colo.MODE_BATCHED, True, profile=True)
     kern = {}
-    for r in res_b:
+    for r in res_k:
         for name, (nl, kms) in r.kernels.items():
             a = kern.setdefault(name, [0, 0.0])
             a[0] += nl
             a[1] += kms
     counters = res_b[0].counters
+    words = (wl.nfeat + 31) // 32
     peak, peak_kind = measured_peak_gbs()
     roof = None
     if kern:
         top = max(kern, key=lambda k: kern[k][1])
         nl, kms = kern[top]
         per_step_launches = nl / args.steps
-        bytes_per_launch = algorithmic_bytes(top, counters) / max(per_step_launches, 1)
+        bytes_per_launch = algorithmic_bytes(top, counters, per_step_launches, words) / max(per_step_launches, 1)
         achieved = bytes_per_launch / (kms / nl / 1e3) / 1e9 if kms > 0 else 0.0
         tr = load_traffic(top)
         roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (burst)",
                 "traffic": tr, "avg_launch_ms": kms / nl, "launches_per_step": per_step_launches,
-                "share_of_step": kms / ms_b}
+                "algorithmic_bytes_per_launch": bytes_per_launch, "share_of_step": kms / ms_k}
+    per_kernel = {}
+    for name, (nl, kms) in sorted(kern.items(), key=lambda kv: -kv[1][1]):
+        ab = algorithmic_bytes(name, counters, nl / args.steps, words)
+        per_kernel[name] = {"ms": round(kms / args.steps, 3), "launches": round(nl / args.steps, 1),
+                            "gbs": round(ab / (kms / args.steps / 1e3) / 1e9, 1) if kms > 0 and ab else None}
+    phases = {k: round(statistics.mean(r.times[k] for r in res_b), 3)
+              for k in ("bucket", "join", "filter", "refine", "fill", "apriori", "total")}
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -286,7 +306,6 @@ def main():
     if not args.no_cpu and world == 1:
         v, cores, sample, _ = run_cpu(wl, args.cpu_frac, 1, 0)
         cpu = {"value": v, "unit": "candidates/s", "cores": cores, "kind": "port", "sample": sample}
-    kernels_ms = {k: round(v[1] / args.steps, 3) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][1])}
     line = {
         "metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_b / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -303,7 +322,8 @@ def main():
         "batched_vs_plain": (ms_p / ms_b),
         "identical_patterns_all_forms": same,
         "gpu_launches": int(sum(r.counters["launches"] for r in res_b)),
-        "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernel_ms_per_step": kernels_ms,
+        "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,
+        "host_phase_ms": phases,
     }
     print(json.dumps(line), flush=True)
     if dist:

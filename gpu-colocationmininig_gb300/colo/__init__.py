@@ -27,7 +27,7 @@ STATUS = {0: "COLO_OK", 1: "COLO_ERR_ARG", 2: "COLO_ERR_IO", 3: "COLO_ERR_PARSE"
 MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
 COUNTERS = ["launches", "active_anchors", "neighbors", "rows_written", "join_pairs", "points", "cells", "runs",
             "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
-            "nrl_entries", "refined"]
+            "nrl_entries", "refined", "filter_items", "single_pass", "single_pass_overflow", "filter_cell_members"]
 
 # Every symbol declared in include/colo.h (checked by the CPU tests).
 EXPORTS = [
@@ -39,8 +39,12 @@ EXPORTS = [
     "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
-    "colo_stage_within", "colo_table_pi_static",
+    "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
+    "colo_ctx_set_model", "colo_result_features",
 ]
+MODEL_FEATURES = 24
+MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
+MODEL_FILE = Path(__file__).resolve().parent / "cost_model.npz"
 
 
 class ColoError(RuntimeError):
@@ -117,6 +121,12 @@ def load(build: bool = True) -> C.CDLL:
         "colo_stage_sqdist": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, _f32p]),
         "colo_stage_within": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _f32p, _u8p]),
         "colo_table_pi_static": (C.c_int, [_P, C.c_uint64, C.c_uint32, _u32p, _u32p, _P, _P, _P]),
+        "colo_model_forward": (C.c_int, [_P, _f32p, _f32p, C.c_uint64, _f32p]),
+        "colo_model_grad": (C.c_int, [_P, _f32p, _f32p, _f32p, C.c_uint64, _f32p, _f32p]),
+        "colo_model_train": (C.c_int, [_P, _f32p, _f32p, _f32p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float,
+                                       C.c_uint64, _f32p]),
+        "colo_ctx_set_model": (C.c_int, [_P, _f32p]),
+        "colo_result_features": (C.c_int, [_P, C.c_uint32, _f32p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -170,6 +180,7 @@ class Level:
     pi: np.ndarray          # (C,) float PI (-1: not refined)
     prevalent: np.ndarray   # (C,)
     argmin: np.ndarray      # (C,)
+    features: np.ndarray = None   # (C, 24) cost-model inputs
     tables: dict = field(default_factory=dict)
 
     def patterns(self):
@@ -194,7 +205,9 @@ class Result:
             am = np.zeros(n, np.uint32)
             lib.colo_result_level(handle, li, _ptr(cand, _u32p), _ptr(ub, _u64p), _ptr(pas, _u8p), _ptr(rows, _u64p),
                                   _ptr(num, _u64p), _ptr(pi, _f32p), _ptr(prev, _u8p), _ptr(am, _u32p))
-            lev = Level(k, cand, ub, pas, rows, num, pi, prev, am)
+            feat = np.zeros((n, MODEL_FEATURES), np.float32)
+            lib.colo_result_features(handle, li, _ptr(feat, _f32p))
+            lev = Level(k, cand, ub, pas, rows, num, pi, prev, am, feat)
             for c in range(n):
                 r = lib.colo_result_table(handle, li, c, None)
                 if r != 2 ** 64 - 1:
@@ -205,8 +218,8 @@ class Result:
         t = (C.c_double * 8)()
         lib.colo_result_times(handle, t)
         self.times = dict(zip(["total", "upload", "bucket", "join", "filter", "refine", "fill", "apriori"], list(t)))
-        c = np.zeros(16, np.uint64)
-        lib.colo_result_counters(handle, _ptr(c, _u64p), 16)
+        c = np.zeros(len(COUNTERS), np.uint64)
+        lib.colo_result_counters(handle, _ptr(c, _u64p), len(COUNTERS))
         self.counters = dict(zip(COUNTERS, c.tolist()))
         self.kernels = {}
         for i in range(lib.colo_result_num_kernels(handle)):
@@ -319,6 +332,47 @@ class Context:
                                               _ptr(w, _u8p)), "stage_within")
         return out, w.astype(bool)
 
+    # ---- learned cost model -------------------------------------------------
+    def model_forward(self, params: np.ndarray, x: np.ndarray) -> np.ndarray:
+        p = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, MODEL_FEATURES)
+        y = np.zeros(len(x), np.float32)
+        self.check(self.lib.colo_model_forward(self.h, _ptr(p, _f32p), _ptr(x, _f32p), len(x), _ptr(y, _f32p)),
+                   "model_forward")
+        return y
+
+    def model_grad(self, params: np.ndarray, x: np.ndarray, t: np.ndarray):
+        p = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, MODEL_FEATURES)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(MODEL_PARAMS, np.float32)
+        loss = C.c_float(0)
+        self.check(self.lib.colo_model_grad(self.h, _ptr(p, _f32p), _ptr(x, _f32p), _ptr(t, _f32p), len(x),
+                                            _ptr(g, _f32p), C.byref(loss)), "model_grad")
+        return g, float(loss.value)
+
+    def model_train(self, params: np.ndarray, x: np.ndarray, t: np.ndarray, epochs: int, batch: int = 4096,
+                    lr: float = 1e-3, seed: int = 0):
+        """GPU training (Adam); returns (trained parameters, per-epoch loss)."""
+        p = np.array(params, np.float32, copy=True)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, MODEL_FEATURES)
+        t = np.ascontiguousarray(t, np.float32)
+        hist = np.zeros(max(epochs, 1), np.float32)
+        self.check(self.lib.colo_model_train(self.h, _ptr(p, _f32p), _ptr(x, _f32p), _ptr(t, _f32p), len(x), epochs,
+                                             batch, lr, seed, _ptr(hist, _f32p)), "model_train")
+        return p, hist[:epochs]
+
+    def set_model(self, params: Optional[np.ndarray]):
+        """Install cost-model parameters for MODE_LEARNED mines (None: remove)."""
+        if params is None:
+            self.check(self.lib.colo_ctx_set_model(self.h, None), "set_model")
+            return
+        p = np.ascontiguousarray(params, np.float32)
+        if p.size != MODEL_PARAMS:
+            raise ValueError(f"expected {MODEL_PARAMS} parameters, got {p.size}")
+        self._model = p
+        self.check(self.lib.colo_ctx_set_model(self.h, _ptr(p, _f32p)), "set_model")
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.colo_destroy(self.h)
@@ -326,6 +380,23 @@ class Context:
 
     def __del__(self):
         self.close()
+
+
+def load_model(path=None) -> np.ndarray:
+    """The committed trained cost model (parameters as float32)."""
+    with np.load(path or MODEL_FILE) as z:
+        return np.ascontiguousarray(z["params"], np.float32)
+
+
+def init_model(seed: int = 0) -> np.ndarray:
+    """He-initialised parameters (input rows 24..31 of W1 zero)."""
+    rng = np.random.default_rng(seed)
+    w1 = np.zeros((32, 64), np.float32)
+    w1[:MODEL_FEATURES] = rng.normal(0, np.sqrt(2.0 / MODEL_FEATURES), (MODEL_FEATURES, 64))
+    w2 = rng.normal(0, np.sqrt(2.0 / 64), (64, 64)).astype(np.float32)
+    w3 = rng.normal(0, np.sqrt(1.0 / 64), 64).astype(np.float32)
+    return np.concatenate([w1.ravel(), np.zeros(64, np.float32), w2.ravel(), np.zeros(64, np.float32), w3,
+                           np.zeros(1, np.float32)]).astype(np.float32)
 
 
 class Dataset:

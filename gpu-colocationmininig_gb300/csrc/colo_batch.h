@@ -46,6 +46,7 @@ struct Batch {
     DevBuf<int32_t> nb9;
     DevBuf<uint32_t> cmask;
     DevBuf<uint32_t> nbmask;     // per cell: feature mask of its geometric 3x3 block
+    DevBuf<uint32_t> qmask;      // per cell: masks of the 4 quads containing it ([M][4][W])
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
     DevBuf<uint32_t> frun_off, frun;
@@ -68,6 +69,7 @@ struct Batch {
     uint64_t active_anchors = 0; // anchors whose cell has higher-feature neighbours
     bool join_single = true;     // single pass into per-run upper-bound regions
     int join_group = 8;          // lanes per anchor in the join (autotuned)
+    uint64_t filter_items = 0;   // (driver cell, candidate) items of the level filters
 };
 
 // colo_bucket.cu
@@ -79,11 +81,11 @@ void join_neighbors(Batch& b);           // neighbour CSR
 // Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
 // bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.
 void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_off);
-// Level-k upper bounds for candidates cand[c*k + j] (global features):
-// ub[c*k + j].  driver[c] is the member whose runs drive the enumeration.
-void filter_level(Batch& b, const uint32_t* d_cand, const uint32_t* d_driver,
-                  const uint64_t* d_item_off, uint64_t ncand, uint64_t nitems, uint32_t k,
-                  uint32_t* d_ub);
+// Level-k upper bounds for host candidates cand[c*k + j] (global features) of
+// jobs job[c]: d_ub[c*k + j] (zeroed by the caller).  d_stats (optional,
+// zeroed, 2 per candidate): full quads and cells of U_c.
+void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint64_t ncand, uint32_t k,
+                  uint32_t* d_ub, unsigned long long* d_stats);
 
 // colo_level.cu --------------------------------------------------------------
 // One candidate's view for the level kernels.

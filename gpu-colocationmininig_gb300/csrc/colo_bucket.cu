@@ -102,44 +102,72 @@ __global__ void k_cell_masks(uint64_t Rn, const uint32_t* __restrict__ rfeat,
 }
 
 // nb9[c*9 + (dy+1)*3 + (dx+1)] = occupied index of the geometric neighbour
-// (cx+dx, cy+dy) inside the job's grid, or -1.
+// (cx+dx, cy+dy) inside the job's grid, or -1.  Keys ascend along a grid row,
+// so the row of the cell itself is read from the adjacent entries and each
+// other row needs one lower_bound (above: after c, below: before c).
 __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                       const JobGrid* __restrict__ grids, int32_t* __restrict__ nb9) {
     uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M) return;
     const JobGrid g = grids[cjob[c]];
-    uint64_t local = ckey[c] - g.key_base;
-    int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
-    for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-            int32_t v = -1;
-            int64_t nx = cx + dx, ny = cy + dy;
-            if (dx == 0 && dy == 0) {
-                v = (int32_t)c;
-            } else if (nx >= 0 && ny >= 0 && nx < (int64_t)g.gx && ny < (int64_t)g.gy) {
-                uint64_t key = g.key_base + (uint64_t)ny * g.gx + (uint64_t)nx;
-                uint64_t lo = 0, hi = M;
-                // neighbours lie within the job's cells; search the whole list
-                lo = lower_bound_dev(ckey, lo, hi, key);
-                if (lo < M && ckey[lo] == key) v = (int32_t)lo;
-            }
-            nb9[c * 9 + (dy + 1) * 3 + (dx + 1)] = v;
+    const uint64_t key = ckey[c];
+    const uint64_t local = key - g.key_base;
+    const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+    const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < (int64_t)g.gx ? cx + 1 : cx;
+    int32_t* out = nb9 + c * 9;
+    for (int dy = -1; dy <= 1; ++dy) {
+        int32_t v[3] = {-1, -1, -1};
+        const int64_t ny = cy + dy;
+        if (dy == 0) {
+            v[1] = (int32_t)c;
+            if (cx > 0 && c > 0 && ckey[c - 1] == key - 1) v[0] = (int32_t)(c - 1);
+            if (cx + 1 < (int64_t)g.gx && c + 1 < M && ckey[c + 1] == key + 1) v[2] = (int32_t)(c + 1);
+        } else if (ny >= 0 && ny < (int64_t)g.gy) {
+            const uint64_t k0 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x0;
+            const uint64_t k1 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x1;
+            uint64_t pos = dy < 0 ? lower_bound_dev(ckey, (uint64_t)0, c, k0) : lower_bound_dev(ckey, c + 1, M, k0);
+            for (; pos < M && ckey[pos] <= k1; ++pos) v[(int64_t)(ckey[pos] - g.key_base - (uint64_t)ny * g.gx) - cx + 1] = (int32_t)pos;
         }
+        out[(dy + 1) * 3 + 0] = v[0];
+        out[(dy + 1) * 3 + 1] = v[1];
+        out[(dy + 1) * 3 + 2] = v[2];
+    }
 }
 
-// nbmask[c] = union of the feature masks of the occupied cells of c's
-// geometric 3x3 block (every quad containing c lies inside it).
-__global__ void k_nbmask(uint64_t M, uint32_t W, const int32_t* __restrict__ nb9,
-                         const uint32_t* __restrict__ cmask, uint32_t* __restrict__ nbmask) {
+// Per cell and mask word: the feature masks of the four quads (2x2 cell
+// blocks) containing the cell, qmask[(c*4 + q)*W + w] with q = (qy+1)*2 +
+// (qx+1) for the quad whose lower-left cell is (cx+qx, cy+qy), qx, qy in
+// {-1, 0} -- q ascends in the quads' (by, bx) order.  A quad outside
+// 0 <= bx <= gx-2, 0 <= by <= gy-2 gets an empty mask, so it is never full.
+// nbmask[c*W + w] = union of the masks of the occupied cells of c's 3x3 block.
+__global__ void k_quad_masks(uint64_t M, uint32_t W, const uint64_t* __restrict__ ckey,
+                             const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
+                             const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
+                             uint32_t* __restrict__ qmask, uint32_t* __restrict__ nbmask) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= M * W) return;
-    uint64_t c = t / W;
-    uint32_t w = (uint32_t)(t % W), m = 0;
+    const uint64_t c = t / W;
+    const uint32_t w = (uint32_t)(t % W);
+    const JobGrid g = grids[cjob[c]];
+    const uint64_t local = ckey[c] - g.key_base;
+    const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+    uint32_t m[9];
+    uint32_t all = 0;
     for (int q = 0; q < 9; ++q) {
         int32_t v = nb9[c * 9 + q];
-        if (v >= 0) m |= cmask[(uint64_t)v * W + w];
+        m[q] = v >= 0 ? cmask[(uint64_t)v * W + w] : 0u;
+        all |= m[q];
     }
-    nbmask[t] = m;
+    nbmask[t] = all;
+    for (int q = 0; q < 4; ++q) {
+        const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
+        const int64_t bx = cx + qx, by = cy + qy;
+        uint32_t qm = 0;
+        if (bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy)
+            qm = m[(qy + 1) * 3 + qx + 1] | m[(qy + 1) * 3 + qx + 2] | m[(qy + 2) * 3 + qx + 1] |
+                 m[(qy + 2) * 3 + qx + 2];
+        qmask[(c * 4 + q) * W + w] = qm;
+    }
 }
 
 __global__ void k_frun_keys(uint64_t Rn, const uint32_t* __restrict__ rfeat, uint64_t* __restrict__ keys,
@@ -317,13 +345,22 @@ void bucket_points(Batch& b) {
     COLO_LAUNCH_CHECK();
     count_launch();
     b.nb9.alloc((uint64_t)M * 9, s);
-    k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("cell_neighbours");
+        k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
     b.nbmask.alloc((uint64_t)M * b.W, s);
-    k_nbmask<<<grid_for((uint64_t)M * b.W, 256), 256, 0, s>>>(M, b.W, b.nb9.get(), b.cmask.get(), b.nbmask.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    b.qmask.alloc((uint64_t)M * 4 * b.W, s);
+    {
+        KScope ks("quad_masks");
+        k_quad_masks<<<grid_for((uint64_t)M * b.W, 256), 256, 0, s>>>(M, b.W, b.ckey.get(), b.cjob.get(),
+                                                                     b.grids.get(), b.nb9.get(), b.cmask.get(),
+                                                                     b.qmask.get(), b.nbmask.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
 
     // feature-major run index: runs sorted by feature (stable, cell order kept)
     {
@@ -336,7 +373,7 @@ void bucket_points(Batch& b) {
         count_launch();
         int fbits = 1;
         while (fbits < 32 && (1ull << fbits) < b.F) fbits++;
-        radix_sort_u64_u32(fk.get(), b.frun.get(), Rn, fbits, s);
+        radix_sort_u64_u32(fk.get(), b.frun.get(), Rn, fbits, s, "run_sort");
         k_frun_off<<<grid_for(b.F + 1, 128), 128, 0, s>>>(b.F, Rn, fk.get(), b.frun_off.get());
         COLO_LAUNCH_CHECK();
         count_launch();

@@ -18,6 +18,8 @@
 // Level k >= 3: quads are enumerated from the cells of a driver member (the
 // one with the fewest cells); each quad is visited once (by its first driver
 // cell) and each cell is counted by its first full quad in (by, bx) order.
+#include <algorithm>
+
 #include "colo_batch.h"
 #include "colo_device.cuh"
 
@@ -89,108 +91,112 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
     }
 }
 
-__device__ __forceinline__ bool quad_full(const int32_t* nbz, int ox, int oy, const uint32_t* cmask,
-                                          uint32_t W, const uint32_t* need) {
-    // quad whose lower-left cell is at offset (ox, oy) from the 3x3 centre Z
-    uint32_t m[kMaxW];
-    for (uint32_t w = 0; w < W; ++w) m[w] = 0;
-    for (int ey = 0; ey < 2; ++ey)
-        for (int ex = 0; ex < 2; ++ex) {
-            int32_t v = nbz[(oy + ey + 1) * 3 + (ox + ex + 1)];
-            if (v < 0) continue;
-            for (uint32_t w = 0; w < W; ++w) m[w] |= cmask[(uint64_t)v * W + w];
-        }
-    for (uint32_t w = 0; w < W; ++w)
-        if ((m[w] & need[w]) != need[w]) return false;
-    return true;
+template <int WT>
+__device__ __forceinline__ bool covers(const uint32_t* __restrict__ qm, const uint32_t (&need)[WT]) {
+    bool ok = true;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) ok &= (qm[w] & need[w]) == need[w];
+    return ok;
 }
 
-__global__ void k_filter_level(uint64_t nitems, uint64_t ncand, uint32_t k,
-                               const uint32_t* __restrict__ cand, const uint32_t* __restrict__ driver,
-                               const uint64_t* __restrict__ item_off, const uint32_t* __restrict__ frun_off,
-                               const uint32_t* __restrict__ frun, const uint32_t* __restrict__ rcell,
-                               const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                               const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                               const uint32_t* __restrict__ cmask, const uint32_t* __restrict__ nbmask,
-                               uint32_t W, const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
-                               const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub) {
+// Level k >= 3.  Items are (driver feature group, driver cell, candidate),
+// candidate fastest: the candidates of a group share a driver feature, so
+// the lanes of a warp read the same cell's quad masks and runs.  For each
+// quad containing the driver cell C (4 masks in qmask[C]):
+//   - it is visited only from its first cell in (ey, ex) order holding the
+//     driver feature (so each quad is seen once per candidate);
+//   - if full, each occupied cell Z of the quad is counted unless an earlier
+//     quad containing Z (in (by, bx) order, qmask[Z][p] for p < q) is full.
+// Counts of one item accumulate in registers; one atomicAdd per member.
+// stats[c*2] = full quads, stats[c*2+1] = cells in U_c.
+template <int WT>
+__global__ void __launch_bounds__(256) k_filter_level(
+    uint64_t nitems, uint32_t ngrp, const uint64_t* __restrict__ grp_item_off, const uint32_t* __restrict__ grp_fd,
+    const uint32_t* __restrict__ grp_lfd, const uint32_t* __restrict__ grp_cand_off,
+    const uint32_t* __restrict__ grp_cands, uint32_t k, const uint32_t* __restrict__ cand,
+    const uint32_t* __restrict__ need_all, const uint32_t* __restrict__ frun_off, const uint32_t* __restrict__ frun,
+    const uint32_t* __restrict__ rcell, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
+    const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ crun,
+    const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub,
+    unsigned long long* __restrict__ stats) {
+    constexpr uint32_t W = WT;
+    const uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered;
     for (uint64_t item = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; item < nitems;
          item += (uint64_t)gridDim.x * blockDim.x) {
-        // candidate owning this item
-        uint64_t lo = 0, hi = ncand;
+        uint32_t lo = 0, hi = ngrp;
         while (hi - lo > 1) {
-            uint64_t mid = (lo + hi) >> 1;
-            if (item_off[mid] <= item) lo = mid;
+            uint32_t mid = (lo + hi) >> 1;
+            if (grp_item_off[mid] <= item) lo = mid;
             else hi = mid;
         }
-        const uint64_t c = lo;
-        const uint32_t* mem = cand + c * k;
-        const uint32_t fd = mem[driver[c]];
-        const uint32_t run = frun[frun_off[fd] + (uint32_t)(item - item_off[c])];
-        const uint32_t C = rcell[run];
-        const JobGrid g = grids[cjob[C]];
-        if (g.gx < 2 || g.gy < 2) continue;
-        const uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered;
-        uint32_t need[kMaxW];
-        for (uint32_t w = 0; w < W; ++w) need[w] = 0;
-        for (uint32_t j = 0; j < m; ++j) {
-            uint32_t lf = mem[j] - g.f0;
-            need[lf >> 5] |= 1u << (lf & 31);
-        }
-        // every quad containing C lies in C's 3x3 block: all members must be there
-        bool present = true;
-        for (uint32_t w = 0; w < W; ++w)
-            if ((nbmask[(uint64_t)C * W + w] & need[w]) != need[w]) present = false;
-        if (!present) continue;
-        const uint32_t lfd = fd - g.f0;
-        const uint64_t local = ckey[C] - g.key_base;
-        const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+        const uint32_t G = grp_cand_off[lo + 1] - grp_cand_off[lo];
+        const uint64_t r = item - grp_item_off[lo];
+        const uint64_t ci = r / G;
+        const uint32_t c = grp_cands[grp_cand_off[lo] + (uint32_t)(r - ci * G)];
+        const uint32_t fd = grp_fd[lo], lfd = grp_lfd[lo];
+        const uint32_t C = rcell[frun[frun_off[fd] + ci]];
+        uint32_t need[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w) need[w] = need_all[(uint64_t)c * W + w];
+        const uint32_t* q4 = qmask + (uint64_t)C * 4 * W;
+        uint32_t full = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (covers<WT>(q4 + q * W, need)) full |= 1u << q;
+        if (!full) continue;
+        const uint32_t* mem = cand + (uint64_t)c * k;
         const int32_t* nbc = nb9 + (uint64_t)C * 9;
-        for (int qy = -1; qy <= 0; ++qy)
-            for (int qx = -1; qx <= 0; ++qx) {
-                int64_t bx = cx + qx, by = cy + qy;
-                if (bx < 0 || by < 0 || bx > (int64_t)g.gx - 2 || by > (int64_t)g.gy - 2) continue;
-                // visit the quad from its first cell (in (ey, ex) order) holding the driver
-                bool first = true;
-                for (int ey = 0; ey < 2 && first; ++ey)
-                    for (int ex = 0; ex < 2; ++ex) {
-                        int ox = qx + ex, oy = qy + ey;
-                        if (ox == 0 && oy == 0) { ey = 2; break; }
-                        int32_t v = nbc[(oy + 1) * 3 + (ox + 1)];
-                        if (v >= 0 && (cmask[(uint64_t)v * W + (lfd >> 5)] >> (lfd & 31) & 1u)) {
-                            first = false;
-                            break;
-                        }
-                    }
-                if (!first) continue;
-                if (!quad_full(nbc, qx, qy, cmask, W, need)) continue;
-                // cells of the quad, each counted by its first full quad
-                for (int ey = 0; ey < 2; ++ey)
-                    for (int ex = 0; ex < 2; ++ex) {
-                        int32_t Z = nbc[(qy + ey + 1) * 3 + (qx + ex + 1)];
-                        if (Z < 0) continue;
-                        const int32_t* nbz = nb9 + (uint64_t)Z * 9;
-                        int64_t zx = bx + ex, zy = by + ey;
-                        bool claimed = true;
-                        for (int py = -1; py <= 0 && claimed; ++py)
-                            for (int px = -1; px <= 0; ++px) {
-                                int64_t ax = zx + px, ay = zy + py;
-                                if (ay > by || (ay == by && ax >= bx)) continue;   // not earlier
-                                if (ax < 0 || ay < 0 || ax > (int64_t)g.gx - 2 || ay > (int64_t)g.gy - 2)
-                                    continue;
-                                if (quad_full(nbz, px, py, cmask, W, need)) {
-                                    claimed = false;
-                                    break;
-                                }
-                            }
-                        if (!claimed) continue;
-                        uint32_t q0 = crun[Z], q1 = crun[Z + 1];
-                        for (uint32_t j = 0; j < m; ++j) {
-                            uint32_t pos = (uint32_t)lower_bound_dev(rfeat, (uint64_t)q0, (uint64_t)q1, mem[j]);
-                            if (pos < q1 && rfeat[pos] == mem[j]) atomicAdd(&ub[c * k + j], rcnt[pos]);
-                        }
-                    }
+        uint32_t acc[kMaxMembersFiltered];
+#pragma unroll
+        for (int j = 0; j < kMaxMembersFiltered; ++j) acc[j] = 0;
+        uint32_t nquads = 0, ncells = 0;
+        for (int q = 0; q < 4; ++q) {
+            if (!(full >> q & 1u)) continue;
+            const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
+            // visit the quad from its first cell (in (ey, ex) order) holding the driver
+            bool first = true;
+            for (int e = 0; e < 4 && first; ++e) {
+                const int ox = qx + (e & 1), oy = qy + (e >> 1);
+                if (ox == 0 && oy == 0) break;
+                const int32_t v = nbc[(oy + 1) * 3 + (ox + 1)];
+                if (v >= 0 && (cmask[(uint64_t)v * W + (lfd >> 5)] >> (lfd & 31) & 1u)) first = false;
             }
+            if (!first) continue;
+            ++nquads;
+            for (int e = 0; e < 4; ++e) {
+                const int ex = e & 1, ey = e >> 1;
+                const int32_t Z = nbc[(qy + ey + 1) * 3 + (qx + ex + 1)];
+                if (Z < 0) continue;
+                // this quad is quad pq of Z; earlier quads of Z are p < pq
+                const int pq = (1 - ey) * 2 + (1 - ex);
+                bool claimed = true;
+                const uint32_t* z4 = qmask + (uint64_t)Z * 4 * W;
+                for (int p = 0; p < pq && claimed; ++p)
+                    if (covers<WT>(z4 + p * W, need)) claimed = false;
+                if (!claimed) continue;
+                ++ncells;
+                const uint32_t q0 = crun[Z], q1 = crun[Z + 1];
+                uint32_t pos = q0, prev = 0;
+#pragma unroll
+                for (int j = 0; j < kMaxMembersFiltered; ++j) {
+                    if ((uint32_t)j < m) {
+                        // runs of a cell ascend by feature; members usually do too
+                        const uint32_t f = mem[j];
+                        if (f < prev) pos = q0;
+                        prev = f;
+                        pos = (uint32_t)lower_bound_dev(rfeat, (uint64_t)pos, (uint64_t)q1, f);
+                        if (pos < q1 && rfeat[pos] == f) acc[j] += rcnt[pos];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxMembersFiltered; ++j)
+            if ((uint32_t)j < m && acc[j]) atomicAdd(&ub[(uint64_t)c * k + j], acc[j]);
+        if (stats && nquads) {
+            atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nquads);
+            atomicAdd(&stats[(uint64_t)c * 2 + 1], (unsigned long long)ncells);
+        }
     }
 }
 
@@ -229,18 +235,86 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     COLO_CUDA(cudaStreamSynchronize(s));
 }
 
-void filter_level(Batch& b, const uint32_t* d_cand, const uint32_t* d_driver, const uint64_t* d_item_off,
-                  uint64_t ncand, uint64_t nitems, uint32_t k, uint32_t* d_ub) {
-    if (nitems == 0) return;
+void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint64_t ncand, uint32_t k,
+                  uint32_t* d_ub, unsigned long long* d_stats) {
+    if (ncand == 0) return;
     if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 256 features per job"};
+    cudaStream_t s = b.s;
+    const uint32_t m = k < kMaxMembersFiltered ? k : (uint32_t)kMaxMembersFiltered;
+    // driver = member with the fewest cells; candidates grouped by driver
+    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0);
+    for (uint64_t c = 0; c < ncand; ++c) {
+        const uint32_t* mem = h_cand + c * k;
+        const uint32_t f0 = b.jobs[h_job[c]].grid.f0;
+        uint32_t best = mem[0], bn = UINT32_MAX;
+        for (uint32_t j = 0; j < m; ++j) {
+            uint32_t nr = b.h_frun_off[mem[j] + 1] - b.h_frun_off[mem[j]];
+            if (nr < bn) {
+                bn = nr;
+                best = mem[j];
+            }
+            uint32_t lf = mem[j] - f0;
+            need[(size_t)c * b.W + (lf >> 5)] |= 1u << (lf & 31);
+        }
+        drv[c] = best;
+    }
+    std::vector<uint32_t> order(ncand);
+    for (uint64_t c = 0; c < ncand; ++c) order[c] = (uint32_t)c;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return drv[a] < drv[c]; });
+    std::vector<uint32_t> gfd, glfd, gcoff;
+    for (uint64_t i = 0; i < ncand; ++i) {
+        const uint32_t c = order[i], fd = drv[c];
+        if (gfd.empty() || gfd.back() != fd) {
+            gfd.push_back(fd);
+            glfd.push_back(fd - b.jobs[h_job[c]].grid.f0);
+            gcoff.push_back((uint32_t)i);
+        }
+    }
+    gcoff.push_back((uint32_t)ncand);
+    std::vector<uint64_t> goff(1, 0);
+    for (size_t g = 0; g < gfd.size(); ++g)
+        goff.push_back(goff.back() + (uint64_t)(b.h_frun_off[gfd[g] + 1] - b.h_frun_off[gfd[g]]) *
+                                         (gcoff[g + 1] - gcoff[g]));
+    const uint32_t ngrp = (uint32_t)gfd.size();
+    const uint64_t nitems = goff.back();
+    b.filter_items += nitems;
+    if (nitems == 0) return;
+    DevBuf<uint32_t> dcand, dneed, dgfd, dglfd, dgcoff, dgc;
+    DevBuf<uint64_t> dgoff;
+    dcand.alloc(ncand * k, s);
+    dneed.alloc(need.size(), s);
+    dgfd.alloc(ngrp, s);
+    dglfd.alloc(ngrp, s);
+    dgcoff.alloc(ngrp + 1, s);
+    dgc.alloc(ncand, s);
+    dgoff.alloc(ngrp + 1, s);
+    COLO_CUDA(cudaMemcpyAsync(dcand.get(), h_cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dneed.get(), need.data(), need.size() * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dgfd.get(), gfd.data(), ngrp * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dglfd.get(), glfd.data(), ngrp * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dgcoff.get(), gcoff.data(), (ngrp + 1) * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dgc.get(), order.data(), ncand * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dgoff.get(), goff.data(), (ngrp + 1) * 8, cudaMemcpyHostToDevice, s));
     uint64_t blocks = (nitems + 255) / 256;
     uint64_t cap = (uint64_t)b.sms * 16;
     if (blocks > cap) blocks = cap;
     KScope ks("filter_level");
-    k_filter_level<<<(unsigned)blocks, 256, 0, b.s>>>(
-        nitems, ncand, k, d_cand, d_driver, d_item_off, b.frun_off.get(), b.frun.get(), b.rcell.get(),
-        b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.nbmask.get(), b.W, b.crun.get(),
-        b.rfeat.get(), b.rcnt.get(), d_ub);
+#define COLO_FL(WW)                                                                                              \
+    k_filter_level<WW><<<(unsigned)blocks, 256, 0, s>>>(                                                         \
+        nitems, ngrp, dgoff.get(), dgfd.get(), dglfd.get(), dgcoff.get(), dgc.get(), k, dcand.get(), dneed.get(), \
+        b.frun_off.get(), b.frun.get(), b.rcell.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(),  \
+        b.rfeat.get(), b.rcnt.get(), d_ub, d_stats)
+    switch (b.W) {
+        case 1: COLO_FL(1); break;
+        case 2: COLO_FL(2); break;
+        case 3: COLO_FL(3); break;
+        case 4: COLO_FL(4); break;
+        case 5: COLO_FL(5); break;
+        case 6: COLO_FL(6); break;
+        case 7: COLO_FL(7); break;
+        default: COLO_FL(8); break;
+    }
+#undef COLO_FL
     COLO_LAUNCH_CHECK();
     count_launch();
 }

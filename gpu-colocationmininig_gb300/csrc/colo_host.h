@@ -35,16 +35,14 @@ struct LevelTrace {
     std::vector<uint8_t> pass, prevalent;
     std::vector<float> pi;
     std::vector<uint32_t> argmin;
+    std::vector<uint64_t> fquads, fcells;       // filter: full quads, cells of U_c (k >= 3)
+    std::vector<float> feat;                    // cost-model features, 24 per candidate
     std::vector<std::vector<uint32_t>> tables;   // row-major, kept on request
     std::vector<uint8_t> has_table;
 };
 
-// counters[]: 0 kernel launches, 1 NPL entries, 2 neighbour entries E,
-// 3 table rows written, 4 fallback candidates, 5 points N, 6 occupied cells M,
-// 7 runs, 8 slice entries examined by count passes, 9 parent words read by
-// count passes, 10 table words written, 11 bitmap words, 12 H2D bytes,
-// 13 D2H bytes, 14 NRL entries, 15 refined candidates.
-constexpr int kNumCounters = 16;
+// counters[]: the list in include/colo.h (colo_result_counters).
+constexpr int kNumCounters = 20;
 struct MineResult {
     std::vector<LevelTrace> levels;
     double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -73,6 +71,7 @@ struct colo_ctx {
     int sms = 0;
     std::string err;
     int refs = 1;          // the owner plus one per live dataset (freed at zero)
+    std::vector<float> model;   // cost-model parameters for LEARNED mines (empty: none)
 };
 
 struct colo_dataset {
@@ -93,6 +92,8 @@ struct colo_result {
 
 namespace colo {
 struct Batch;
+void candidate_features(uint32_t k, const uint32_t* mem, const uint32_t* fcount, const uint64_t* ub,
+                        uint64_t prow, uint64_t fquads, uint64_t fcells, float* x);
 colo_status set_err(colo_ctx* ctx, colo_status st, const std::string& msg);
 void ctx_release(colo_ctx* ctx);
 colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn);

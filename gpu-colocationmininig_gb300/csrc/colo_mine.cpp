@@ -20,6 +20,7 @@
 
 #include "colo_batch.h"
 #include "colo_host.h"
+#include "colo_mlp.h"
 
 using namespace colo;
 
@@ -225,7 +226,16 @@ struct LevelArena {
     DevBuf<CandDesc> descs;
     DevBuf<uint64_t> chunk_off;
     DevBuf<uint64_t> stats;
+    DevBuf<unsigned long long> cursor;   // single pass: rows reserved per candidate
+    DevBuf<uint32_t> overflow;           // single pass: 1 when the table outgrew its capacity
 };
+
+// Capacity of a presized single-pass table from the predicted log1p(rows).
+uint64_t presize_rows(float pred) {
+    double r = std::expm1(std::min<double>(pred, 40.0));
+    if (!(r > 0)) r = 0;
+    return (uint64_t)std::ceil(r * 1.5) + 32;
+}
 
 }  // namespace
 
@@ -334,7 +344,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     struct Unset {
         ~Unset() { g_ktimer = nullptr; }
     } unset;
-    uint64_t cnt_items = 0, cnt_parent = 0, cnt_fillw = 0, cnt_bmw = 0, cnt_d2h = 0, cnt_refined = 0;
+    uint64_t cnt_items = 0, cnt_parent = 0, cnt_fillw = 0, cnt_bmw = 0, cnt_d2h = 0, cnt_refined = 0, cnt_fcm = 0;
+    uint64_t cnt_single = 0, cnt_single_ovf = 0;
     DevBuf<unsigned long long> d_items;
     d_items.alloc(1, s);
     Batch b;
@@ -380,7 +391,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 js[j].cands.push_back(js[j].f0 + c);
             }
     }
-    std::unique_ptr<DevBuf<uint32_t>> tables_prev, tables_cur;
+    std::unique_ptr<DevBuf<uint32_t>> tables_prev, tables_cur, single_prev;
     for (uint32_t k = 2;; ++k) {
         bool any = false;
         for (auto& st : js) any |= (st.active && !st.cands.empty());
@@ -405,6 +416,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             L.prevalent.assign(C, 0);
             L.pi.assign(C, -1.0f);
             L.argmin.assign(C, 0);
+            L.fquads.assign(C, 0);
+            L.fcells.assign(C, 0);
             L.has_table.assign(C, 0);
             tr[j] = &L;
         }
@@ -427,50 +440,59 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
             }
         } else {
-            std::vector<uint32_t> hc, hdrv;
-            std::vector<uint64_t> hoff(1, 0);
+            std::vector<uint32_t> hc, hjob;
             std::vector<std::pair<uint32_t, size_t>> owner;
             for (uint32_t j = 0; j < J; ++j) {
                 if (!tr[j]) continue;
                 const LevelTrace& L = *tr[j];
                 for (size_t c = 0; c < L.cand.size() / k; ++c) {
-                    const uint32_t* mem = &L.cand[c * k];
-                    uint32_t m = std::min<uint32_t>(k, kMaxMembersFiltered);
-                    uint32_t best = 0;
-                    uint32_t bestn = UINT32_MAX;
-                    for (uint32_t q = 0; q < m; ++q) {
-                        uint32_t nr = b.h_frun_off[mem[q] + 1] - b.h_frun_off[mem[q]];
-                        if (nr < bestn) {
-                            bestn = nr;
-                            best = q;
-                        }
-                    }
-                    hc.insert(hc.end(), mem, mem + k);
-                    hdrv.push_back(best);
-                    hoff.push_back(hoff.back() + bestn);
+                    hc.insert(hc.end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+                    hjob.push_back(j);
                     owner.push_back({j, c});
                 }
             }
             uint64_t ncand = owner.size();
-            DevBuf<uint32_t> dc, dd, dub;
-            DevBuf<uint64_t> doff;
-            dc.alloc(hc.size(), s);
-            dd.alloc(ncand, s);
-            doff.alloc(ncand + 1, s);
+            DevBuf<uint32_t> dub;
+            DevBuf<unsigned long long> dfs;
             dub.alloc(ncand * k, s);
             dub.zero(s);
-            COLO_CUDA(cudaMemcpyAsync(dc.get(), hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(dd.get(), hdrv.data(), ncand * 4, cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(doff.get(), hoff.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
-            filter_level(b, dc.get(), dd.get(), doff.get(), ncand, hoff.back(), k, dub.get());
+            dfs.alloc(ncand * 2, s);
+            dfs.zero(s);
+            filter_level(b, hc.data(), hjob.data(), ncand, k, dub.get(), dfs.get());
             std::vector<uint32_t> hub(ncand * k);
+            std::vector<uint64_t> hfs(ncand * 2);
             COLO_CUDA(cudaMemcpyAsync(hub.data(), dub.get(), hub.size() * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(hfs.data(), dfs.get(), hfs.size() * 8, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaStreamSynchronize(s));
+            for (uint64_t q = 0; q < ncand; ++q) {
+                LevelTrace& L = *tr[owner[q].first];
+                size_t c = owner[q].second;
+                L.fquads[c] = hfs[2 * q];
+                L.fcells[c] = hfs[2 * q + 1];
+                cnt_fcm += hfs[2 * q + 1] * std::min<uint32_t>(k, kMaxMembersFiltered);
+            }
             for (uint64_t q = 0; q < ncand; ++q) {
                 LevelTrace& L = *tr[owner[q].first];
                 size_t c = owner[q].second;
                 for (uint32_t t = 0; t < k; ++t) L.ub[c * k + t] = hub[q * k + t];
                 L.pass[c] = filter_pass(&L.ub[c * k], &L.cand[c * k], k, b.h_fcount, js[owner[q].first].thr);
+            }
+        }
+        // cost-model features of every candidate (recorded for training; used by LEARNED)
+        for (uint32_t j = 0; j < J; ++j) {
+            if (!tr[j]) continue;
+            LevelTrace& L = *tr[j];
+            const size_t C = L.cand.size() / k;
+            L.feat.assign(C * kMlpIn, 0.f);
+            for (size_t c = 0; c < C; ++c) {
+                const uint32_t* mem = &L.cand[c * k];
+                uint64_t prow = b.h_fcount[mem[0]];
+                if (k > 2) {
+                    auto it = js[j].tables.find(std::vector<uint32_t>(mem, mem + k - 1));
+                    prow = it == js[j].tables.end() ? 0 : it->second.rows;
+                }
+                candidate_features(k, mem, b.h_fcount.data(), &L.ub[c * k], prow, L.fquads[c], L.fcells[c],
+                                   &L.feat[c * kMlpIn]);
             }
         }
         t_filter += ms_since(t0);
@@ -519,6 +541,45 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
         }
         const uint64_t ncand = hd.size();
+        // LEARNED: predicted rows presize one-pass tables; the queue runs largest first
+        const bool learned = mode == COLO_MODE_LEARNED && !ctx->model.empty() && ncand > 0;
+        std::vector<uint64_t> cap;
+        if (learned) {
+            std::vector<float> X(ncand * kMlpIn), y(ncand);
+            for (uint64_t q = 0; q < ncand; ++q) {
+                const LevelTrace& L = *tr[owner[q].first];
+                std::memcpy(&X[q * kMlpIn], &L.feat[owner[q].second * kMlpIn], kMlpIn * sizeof(float));
+            }
+            DevBuf<float> dparams, dx, dy;
+            dparams.alloc(kMlpParams, s);
+            dx.alloc(X.size(), s);
+            dy.alloc(ncand, s);
+            COLO_CUDA(cudaMemcpyAsync(dparams.get(), ctx->model.data(), kMlpParams * 4, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(dx.get(), X.data(), X.size() * 4, cudaMemcpyHostToDevice, s));
+            mlp_forward(dparams.get(), dx.get(), ncand, dy.get(), s);
+            COLO_CUDA(cudaMemcpyAsync(y.data(), dy.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
+            std::vector<uint64_t> pc(ncand);
+            for (uint64_t q = 0; q < ncand; ++q) pc[q] = presize_rows(y[q]);
+            std::vector<uint64_t> perm(ncand);
+            for (uint64_t q = 0; q < ncand; ++q) perm[q] = q;
+            std::stable_sort(perm.begin(), perm.end(), [&](uint64_t a, uint64_t c) { return pc[a] > pc[c]; });
+            std::vector<CandDesc> hd2(ncand);
+            std::vector<std::pair<uint32_t, size_t>> own2(ncand);
+            std::vector<uint64_t> sb2(ncand);
+            cap.resize(ncand);
+            chunk_off.assign(1, 0);
+            for (uint64_t i = 0; i < ncand; ++i) {
+                hd2[i] = hd[perm[i]];
+                own2[i] = owner[perm[i]];
+                sb2[i] = slot_base[perm[i]];
+                cap[i] = pc[perm[i]];
+                chunk_off.push_back(chunk_off.back() + (hd2[i].prow + 31) / 32);
+            }
+            hd.swap(hd2);
+            owner.swap(own2);
+            slot_base.swap(sb2);
+        }
         LevelArena ar;
         ar.slots.alloc(nslots ? nslots : 1, s);
         ar.bitmap.alloc(nwords ? nwords : 1, s);
@@ -526,10 +587,28 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         ar.rows.alloc(ncand ? ncand : 1, s);
         ar.rows.zero(s);
         ar.stats.alloc(ncand * k * 4 + 1, s);
-        for (uint64_t q = 0; q < ncand; ++q) {
+        std::unique_ptr<DevBuf<uint32_t>> single_cur;
+        uint64_t single_words = 0;
+        if (learned) {
+            for (uint64_t q = 0; q < ncand; ++q) single_words += cap[q] * k;
+            single_cur.reset(new DevBuf<uint32_t>());
+            single_cur->alloc(single_words ? single_words : 1, s);
+            ar.cursor.alloc(ncand, s);
+            ar.cursor.zero(s);
+            ar.overflow.alloc(ncand, s);
+            ar.overflow.zero(s);
+        }
+        for (uint64_t q = 0, o = 0; q < ncand; ++q) {
             hd[q].slots = ar.slots.get() + slot_base[q];
             hd[q].bitmap = ar.bitmap.get();
             hd[q].rows = ar.rows.get() + q;
+            if (learned) {
+                hd[q].out = single_cur->get() + o;
+                hd[q].out_cap = cap[q];
+                hd[q].out_rows = cap[q];
+                hd[q].cursor = ar.cursor.get() + q;
+                o += cap[q] * k;
+            }
         }
         ar.descs.alloc(ncand ? ncand : 1, s);
         ar.chunk_off.alloc(ncand + 1, s);
@@ -559,6 +638,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                                               cudaMemcpyDeviceToHost, s));
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
+            } else if (learned) {
+                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr, d_items.get()};
+                level_single(b, w, k, ar.overflow.get());
+                level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
+                COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
+                COLO_CUDA(cudaStreamSynchronize(s));
             } else {
                 LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr, d_items.get()};
                 level_count(b, w, k, true);
@@ -598,8 +683,14 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         // row counts (per-candidate counters of the count pass) and fill offsets
         std::vector<uint64_t> hrows(ncand);
+        std::vector<uint32_t> hovf(ncand, 0);
         if (ncand)
             COLO_CUDA(cudaMemcpy(hrows.data(), ar.rows.get(), ncand * 8, cudaMemcpyDeviceToHost));
+        if (learned) {
+            COLO_CUDA(cudaMemcpy(hovf.data(), ar.overflow.get(), ncand * 4, cudaMemcpyDeviceToHost));
+            cnt_single += ncand;
+            for (uint64_t q = 0; q < ncand; ++q) cnt_single_ovf += hovf[q] ? 1 : 0;
+        }
         {
             unsigned long long it = 0;
             COLO_CUDA(cudaMemcpy(&it, d_items.get(), 8, cudaMemcpyDeviceToHost));
@@ -631,7 +722,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
 
         // ---- fill pass for the needed prevalent patterns ----
         t0 = Clock::now();
-        std::vector<uint64_t> fillq;
+        std::vector<uint64_t> fillq, keepq;   // keepq: tables the single pass already wrote whole
         uint64_t total_rows = 0;
         for (uint64_t q = 0; q < ncand; ++q) {
             if (!prev_flag[q]) continue;
@@ -639,8 +730,16 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             size_t c = owner[q].second;
             std::vector<uint32_t> pat(L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
             if (!needed[owner[q].first].count(pat)) continue;
+            if (learned && !hovf[q]) {
+                keepq.push_back(q);
+                continue;
+            }
             fillq.push_back(q);
             total_rows += gb[q + 1] - gb[q];
+        }
+        if (learned) {
+            rows_written += gb[ncand];
+            cnt_fillw += single_words;
         }
         tables_cur.reset(new DevBuf<uint32_t>());
         tables_cur->alloc(total_rows * k ? total_rows * k : 1, s);
@@ -702,18 +801,25 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         COLO_CUDA(cudaStreamSynchronize(s));
         // register the new tables (prefixes of the next level)
         for (auto& st : js) st.tables.clear();
-        for (size_t i = 0; i < fillq.size(); ++i) {
-            uint64_t q = fillq[i];
+        std::vector<std::pair<uint64_t, TableRef>> made;
+        for (size_t i = 0; i < fillq.size(); ++i) made.push_back({fillq[i], TableRef{fd[i].out, fd[i].out_rows, fd[i].out_rows}});
+        for (uint64_t q : keepq) {
+            made.push_back({q, TableRef{hd[q].out, gb[q + 1] - gb[q], cap[q]}});
+            tr[owner[q].first]->has_table[owner[q].second] = 1;
+        }
+        for (const auto& mt : made) {
+            const uint64_t q = mt.first;
+            const TableRef& t = mt.second;
             LevelTrace& L = *tr[owner[q].first];
             size_t c = owner[q].second;
             std::vector<uint32_t> pat(L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
-            TableRef t{fd[i].out, fd[i].out_rows, fd[i].out_rows};
             js[owner[q].first].tables[pat] = t;
             if (pv[owner[q].first].keep_tables) {
-                uint64_t rows = fd[i].out_rows;
+                uint64_t rows = t.rows;
                 std::vector<uint32_t> colm(rows * k);
                 if (rows)
-                    COLO_CUDA(cudaMemcpy(colm.data(), fd[i].out, rows * k * 4, cudaMemcpyDeviceToHost));
+                    COLO_CUDA(cudaMemcpy2D(colm.data(), rows * 4, t.cols, t.stride * 4, rows * 4, k,
+                                           cudaMemcpyDeviceToHost));
                 if (L.tables.size() < L.cand.size() / k) L.tables.resize(L.cand.size() / k);
                 std::vector<uint32_t>& rm = L.tables[c];
                 rm.resize(rows * k);
@@ -723,6 +829,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         t_fill += ms_since(t0);
         tables_prev = std::move(tables_cur);
+        single_prev = std::move(single_cur);
         for (auto& st : js)
             if (st.cands.empty()) st.active = false;
     }
@@ -743,6 +850,10 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->counters[14] = b.nrl_total;
         r->counters[4] = b.join_pairs;
         r->counters[15] = cnt_refined;
+        r->counters[16] = b.filter_items;
+        r->counters[17] = cnt_single;
+        r->counters[18] = cnt_single_ovf;
+        r->counters[19] = cnt_fcm;
         r->times[0] = ms_since(t_all);
         r->times[1] = t_upload;
         r->times[2] = t_bucket;

@@ -228,7 +228,7 @@ void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t
     scan_impl<uint64_t, uint64_t>(in, out, n, s, total_host);
 }
 
-void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s) {
+void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
     uint32_t nblocks = (uint32_t)((n + kSortTile - 1) / kSortTile);
@@ -245,7 +245,7 @@ void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cu
     int passes = (bits + kRadixBits - 1) / kRadixBits;
     for (int p = 0; p < passes; ++p) {
         int shift = p * kRadixBits;
-        KScope ks("radix_sort");
+        KScope ks(name);
         k_radix_hist<<<nblocks, kSortThreads, 0, s>>>(ka, n, shift, hist.get(), nblocks);
         COLO_LAUNCH_CHECK();
         count_launch();

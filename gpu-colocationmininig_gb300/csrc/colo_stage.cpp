@@ -138,32 +138,11 @@ colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float th
                     hub[2 * c + 1] = a == bb ? 0 : h[(uint64_t)bb * nf + a];
                 }
             } else {
-                std::vector<uint32_t> drv(ncand);
-                std::vector<uint64_t> off(ncand + 1, 0);
-                for (uint64_t c = 0; c < ncand; ++c) {
-                    uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered, best = 0, bn = UINT32_MAX;
-                    for (uint32_t q = 0; q < m; ++q) {
-                        uint32_t f = cand[c * k + q];
-                        uint32_t nr = b.h_frun_off[f + 1] - b.h_frun_off[f];
-                        if (nr < bn) {
-                            bn = nr;
-                            best = q;
-                        }
-                    }
-                    drv[c] = best;
-                    off[c + 1] = off[c] + bn;
-                }
-                DevBuf<uint32_t> dc, dd, du;
-                DevBuf<uint64_t> doff;
-                dc.alloc(ncand * k, s);
-                dd.alloc(ncand, s);
-                doff.alloc(ncand + 1, s);
+                DevBuf<uint32_t> du;
                 du.alloc(ncand * k, s);
                 du.zero(s);
-                COLO_CUDA(cudaMemcpyAsync(dc.get(), cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
-                COLO_CUDA(cudaMemcpyAsync(dd.get(), drv.data(), ncand * 4, cudaMemcpyHostToDevice, s));
-                COLO_CUDA(cudaMemcpyAsync(doff.get(), off.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
-                filter_level(b, dc.get(), dd.get(), doff.get(), ncand, off[ncand], k, du.get());
+                std::vector<uint32_t> job(ncand, 0);
+                filter_level(b, cand, job.data(), ncand, k, du.get(), nullptr);
                 std::vector<uint32_t> h(ncand * k);
                 COLO_CUDA(cudaMemcpyAsync(h.data(), du.get(), h.size() * 4, cudaMemcpyDeviceToHost, s));
                 COLO_CUDA(cudaStreamSynchronize(s));

@@ -138,7 +138,10 @@ colo_status colo_result_times(const colo_result* r, double* ms8);
  * examined by count passes, [9] parent words read by count passes,
  * [10] table words written, [11] bitmap words, [12] host-to-device bytes,
  * [13] device-to-host bytes, [14] neighbourhood-run entries, [15] refined
- * candidates. */
+ * candidates, [16] (driver cell, candidate) items of the level filters,
+ * [17] candidates filled in one presized pass, [18] of those, overflowed and
+ * refilled by the two-pass fallback, [19] (cell of U_c, member) run lookups
+ * of the level filters. */
 colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n);
 /* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set). */
 uint32_t colo_result_num_kernels(const colo_result* r);
@@ -176,6 +179,37 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
  * fallback near the boundary); either output may be NULL. */
 colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
                               const float* y2, uint64_t n, float R2, float* out, uint8_t* within);
+
+/* ---- learned cost model ----------------------------------------------- */
+/* A 24 -> 64 -> 64 -> 1 ReLU MLP (BF16 weights and activations, FP32
+ * accumulation, hand-written tensor-core kernels) that predicts
+ * log1p(instance-table rows) of a candidate that passed the filter.  In
+ * COLO_MODE_LEARNED it presizes the single-pass table buffers and orders the
+ * level queue; a candidate whose table overflows is refilled by the exact
+ * two-pass fill, so results never depend on it.  No counterpart in the
+ * reference.  Parameters (COLO_MODEL_PARAMS floats): W1[32][64] (input rows
+ * 24..31 zero), b1[64], W2[64][64], b2[64], W3[64], b3. */
+#define COLO_MODEL_FEATURES 24
+#define COLO_MODEL_PARAMS (32 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
+/* y[i] = model(x[i*24 .. i*24+23]) for n rows (host arrays). */
+colo_status colo_model_forward(colo_ctx* ctx, const float* params, const float* x, uint64_t n, float* y);
+/* Gradient of mean_i 0.5*(y_i - t_i)^2 with respect to the parameters. */
+colo_status colo_model_grad(colo_ctx* ctx, const float* params, const float* x, const float* t, uint64_t n,
+                            float* grad, float* loss);
+/* Adam (lr, beta 0.9/0.999) on the GPU over shuffled minibatches; params is
+ * updated in place; epoch_loss[e] (optional) = mean minibatch loss. */
+colo_status colo_model_train(colo_ctx* ctx, float* params, const float* x, const float* t, uint64_t n,
+                             uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float* epoch_loss);
+/* Install a model for COLO_MODE_LEARNED mines on this context (NULL: none;
+ * without a model LEARNED mines run the BATCHED schedule). */
+colo_status colo_ctx_set_model(colo_ctx* ctx, const float* params);
+/* The model's 24 input features of every candidate of level li (ncand*24
+ * floats): [0] k/8, [1..8] log1p(n_j), [9..16] log1p(ub_j) (members j < 8,
+ * else 0), [17] log1p(parent rows), [18] log1p(cells of U_c), [19]
+ * log1p(full quads), [20] log1p(min n_j), [21] log1p(min ub_j), [22]
+ * log1p(parent rows) - log1p(n_last), [23] log1p(ub_last) - log1p(n_last).
+ * Quad statistics are 0 for pairs. */
+colo_status colo_result_features(const colo_result* r, uint32_t li, float* x);
 
 /* ---- allocation-free entry point -------------------------------------- */
 /* No counterpart in the reference (the reference allocates its participation

@@ -187,7 +187,8 @@ def main():
     ap.add_argument("--cpu-frac", type=float, default=0.02)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--forms", default="batched,e2e,plain",
-                    help="comma list of batched (resident), e2e (host buffers), plain")
+                    help="comma list of batched (resident), e2e (host buffers), plain; the headline form "
+                         "(batched+learned) always runs")
     args = ap.parse_args()
     rank, world, local = dist_env()
     from colo import gen
@@ -255,21 +256,32 @@ def main():
         return ms, results, clk.summary()
 
     forms = set(args.forms.split(","))
-    ms_b, res_b, clocks = timed(colo.MODE_BATCHED, True)
+    # headline form: batched + learned presizing (the committed trained cost model)
+    model = None
+    try:
+        model = colo.load_model()
+    except OSError:
+        pass
+    head_mode = colo.MODE_LEARNED if model is not None else colo.MODE_BATCHED
+    ctx.set_model(model)
+    ms_b, res_b, clocks = timed(head_mode, True)
     cands = res_b[0].num_candidates()
     value = cands * args.steps * world / (ms_b / 1e3)
     ms_e, res_e, ms_p, res_p = ms_b, res_b, ms_b, res_b
     if "e2e" in forms:
-        ms_e, res_e, _ = timed(colo.MODE_BATCHED, False)
+        ms_e, res_e, _ = timed(head_mode, False)
     e2e = cands * args.steps * world / (ms_e / 1e3)
+    ms_bt, res_bt = ms_b, res_b
+    if "batched" in forms and head_mode != colo.MODE_BATCHED:
+        ms_bt, res_bt, _ = timed(colo.MODE_BATCHED, True)
     if "plain" in forms:
         ms_p, res_p, _ = timed(colo.MODE_PLAIN, True)
     plain = cands * args.steps * world / (ms_p / 1e3)
     # every form mined the same patterns
-    same = all(r.patterns() == res_b[0].patterns() for r in res_b + res_e + res_p)
+    same = all(r.patterns() == res_b[0].patterns() for r in res_b + res_e + res_p + res_bt)
 
     # per-kernel CUDA-event times (a separate profiled pass, so `value` carries no event overhead)
-    ms_k, res_k, _ = timed(colo.MODE_BATCHED, True, profile=True)
+    ms_k, res_k, _ = timed(head_mode, True, profile=True)
     kern = {}
     for r in res_k:
         for name, (nl, kms) in r.kernels.items():
@@ -313,13 +325,19 @@ def main():
         "config": {"workload": WORKLOAD, "points": wl.n, "features": wl.nfeat, "candidates_per_step": cands,
                    "join_active_anchors": int(counters["active_anchors"]), "join_pairs": int(counters["join_pairs"]),
                    "neighbor_entries": int(counters["neighbors"]),
-                   "form": "batched", "l2": "inputs (240 MB) larger than L2 (129 MB); no flush",
+                   "form": "batched+learned" if head_mode == colo.MODE_LEARNED else "batched",
+                   "l2": "inputs (240 MB) larger than L2 (129 MB); no flush",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": "candidates/s", "ms_per_step": ms_e / args.steps,
                 "h2d_bytes_per_step": int(res_e[0].counters["h2d_bytes"]),
                 "d2h_bytes_per_step": int(res_e[0].counters["d2h_bytes"])},
         "plain": {"value": plain, "unit": "candidates/s", "ms_per_step": ms_p / args.steps},
-        "batched_vs_plain": (ms_p / ms_b),
+        "batched": {"value": cands * args.steps * world / (ms_bt / 1e3), "unit": "candidates/s",
+                    "ms_per_step": ms_bt / args.steps},
+        "headline_vs_plain": (ms_p / ms_b),
+        "learned_presize": ({"single_pass": int(res_b[0].counters["single_pass"]),
+                             "overflow_fallback": int(res_b[0].counters["single_pass_overflow"])}
+                            if head_mode == colo.MODE_LEARNED else None),
         "identical_patterns_all_forms": same,
         "gpu_launches": int(sum(r.counters["launches"] for r in res_b)),
         "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,

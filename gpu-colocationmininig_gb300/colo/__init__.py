@@ -191,7 +191,30 @@ class Result:
     def __init__(self, lib, handle):
         self._lib = lib
         self.h = handle
-        self.levels: List[Level] = []
+        self._levels = None          # parsed on first access
+        t = (C.c_double * 8)()
+        lib.colo_result_times(handle, t)
+        self.times = dict(zip(["total", "upload", "bucket", "join", "filter", "refine", "fill", "apriori"], list(t)))
+        c = np.zeros(len(COUNTERS), np.uint64)
+        lib.colo_result_counters(handle, _ptr(c, _u64p), len(COUNTERS))
+        self.counters = dict(zip(COUNTERS, c.tolist()))
+        self.kernels = {}
+        for i in range(lib.colo_result_num_kernels(handle)):
+            name = C.create_string_buffer(64)
+            nl = C.c_uint64()
+            ms = C.c_double()
+            lib.colo_result_kernel(handle, i, name, 64, C.byref(nl), C.byref(ms))
+            self.kernels[name.value.decode()] = (int(nl.value), float(ms.value))
+
+    @property
+    def levels(self) -> List[Level]:
+        if self._levels is None:
+            self._levels = self._parse_levels()
+        return self._levels
+
+    def _parse_levels(self) -> List[Level]:
+        lib, handle = self._lib, self.h
+        levels = []
         for li in range(lib.colo_result_num_levels(handle)):
             k = lib.colo_result_level_size(handle, li)
             n = lib.colo_result_level_candidates(handle, li)
@@ -214,20 +237,8 @@ class Result:
                     t = np.zeros((r, k), np.uint32)
                     lib.colo_result_table(handle, li, c, _ptr(t, _u32p))
                     lev.tables[c] = t
-            self.levels.append(lev)
-        t = (C.c_double * 8)()
-        lib.colo_result_times(handle, t)
-        self.times = dict(zip(["total", "upload", "bucket", "join", "filter", "refine", "fill", "apriori"], list(t)))
-        c = np.zeros(len(COUNTERS), np.uint64)
-        lib.colo_result_counters(handle, _ptr(c, _u64p), len(COUNTERS))
-        self.counters = dict(zip(COUNTERS, c.tolist()))
-        self.kernels = {}
-        for i in range(lib.colo_result_num_kernels(handle)):
-            name = C.create_string_buffer(64)
-            nl = C.c_uint64()
-            ms = C.c_double()
-            lib.colo_result_kernel(handle, i, name, 64, C.byref(nl), C.byref(ms))
-            self.kernels[name.value.decode()] = (int(nl.value), float(ms.value))
+            levels.append(lev)
+        return levels
 
     def patterns(self):
         out = []
@@ -236,7 +247,8 @@ class Result:
         return out
 
     def num_candidates(self) -> int:
-        return int(sum(len(l.cand) for l in self.levels))
+        lib, h = self._lib, self.h
+        return int(sum(lib.colo_result_level_candidates(h, li) for li in range(lib.colo_result_num_levels(h))))
 
     def write_patterns(self, ds: "Dataset", location: str):
         st = self._lib.colo_result_write_patterns(self.h, ds.h, str(location).encode())

@@ -1,0 +1,111 @@
+"""Training and evaluation of the learned cost model.
+
+The model maps a filtered candidate's 24 cell-aggregate features
+(colo_result_features) to log1p(instance-table rows).  Training pairs come
+from the mining itself: every candidate a mine refines yields (features,
+exact row count).  The training set is mined from seeded datasets of the
+20M-point workload's generator at 200k-2M points (same density), and the
+network is trained on the GPU by the library's own kernels
+(colo_model_train).
+
+    python -m colo.costmodel train --out cost_model.npz   # needs a GPU
+
+`heuristic_log_rows` is the presize the method would use without the
+network (parent rows times the fraction of the last member's instances that
+lie in candidate cells); `evaluate` reports both against the exact counts.
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import time
+
+import numpy as np
+
+from . import MODE_BATCHED, Context, Dataset, default_params, init_model
+from . import gen
+
+TRAIN_SEEDS = range(20270100, 20270150)     # 50 training datasets
+HELDOUT_SEEDS = range(20270200, 20270204)   # never trained on
+MARGIN = 1.5                                # capacity = 1.5 x predicted rows + 32 (as colo_mine.cpp)
+
+
+def dataset_size(seed: int) -> int:
+    rng = np.random.default_rng(seed)
+    return int(math.exp(rng.uniform(math.log(200_000), math.log(2_000_000))))
+
+
+def collect(ctx: Context, seeds, thresholds=(0.15, 0.08), log=None):
+    """(X float32[n, 24], log1p(rows) float32[n], k int[n]) of every refined candidate."""
+    xs, ts, ks = [], [], []
+    for seed in seeds:
+        n = dataset_size(seed)
+        wl = gen.config(3, seed=seed, scale=n / 20_000_000)
+        ds = Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
+        for thr in thresholds:
+            res = ctx.mine(ds, default_params(wl.R, thr, MODE_BATCHED, max_size=wl.max_size))
+            for lev in res.levels:
+                sel = lev.passed.astype(bool)
+                if not sel.any():
+                    continue
+                xs.append(lev.features[sel])
+                ts.append(np.log1p(lev.rows[sel].astype(np.float64)).astype(np.float32))
+                ks.append(np.full(int(sel.sum()), lev.k, np.int32))
+        if log:
+            log(f"seed {seed}: {n} points, {sum(len(t) for t in ts)} samples so far")
+    if not xs:
+        return np.zeros((0, 24), np.float32), np.zeros(0, np.float32), np.zeros(0, np.int32)
+    return np.concatenate(xs), np.concatenate(ts), np.concatenate(ks)
+
+
+def heuristic_log_rows(x: np.ndarray) -> np.ndarray:
+    """Presize without the network: log1p(parent rows) + log1p(ub_last) - log1p(n_last)."""
+    return x[:, 17] + x[:, 23]
+
+
+def errors(pred_log: np.ndarray, t_log: np.ndarray) -> dict:
+    pred = np.expm1(np.clip(pred_log.astype(np.float64), 0, 40))
+    true = np.expm1(t_log.astype(np.float64))
+    rel = np.abs(pred - true) / np.maximum(true, 1.0)
+    cap = np.ceil(pred * MARGIN) + 32
+    return {"median_rel_err": float(np.median(rel)), "p95_rel_err": float(np.percentile(rel, 95)),
+            "overflow_rate": float(np.mean(true > cap)),
+            "alloc_over_needed": float(np.sum(cap) / max(np.sum(true), 1.0))}
+
+
+def evaluate(ctx: Context, params: np.ndarray, x: np.ndarray, t: np.ndarray) -> dict:
+    y = ctx.model_forward(params, x)
+    return {"model": errors(y, t), "heuristic": errors(heuristic_log_rows(x), t), "samples": int(len(t))}
+
+
+def train(ctx: Context, x: np.ndarray, t: np.ndarray, epochs: int = 40, batch: int = 2048, lr: float = 2e-3,
+          seed: int = 0):
+    p0 = init_model(seed)
+    p0[-1] = float(np.mean(t))        # start the output bias at the mean target
+    return ctx.model_train(p0, x, t, epochs, batch, lr, seed)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--epochs", type=int, default=40)
+    args = ap.parse_args()
+    ctx = Context(0)
+    t0 = time.time()
+    x, t, k = collect(ctx, TRAIN_SEEDS, log=print)
+    t_collect = time.time() - t0
+    xh, th, kh = collect(ctx, HELDOUT_SEEDS)
+    t0 = time.time()
+    params, hist = train(ctx, x, t, args.epochs)
+    t_train = time.time() - t0
+    ev = evaluate(ctx, params, xh, th)
+    ev_train = evaluate(ctx, params, x, t)
+    print({"samples": len(t), "collect_s": t_collect, "train_s": t_train, "loss": hist.tolist(),
+           "heldout": ev, "train": ev_train})
+    np.savez(args.out, params=params, loss=hist, samples=len(t), train_seeds=np.array(list(TRAIN_SEEDS)),
+             heldout_median_rel_err=ev["model"]["median_rel_err"], heldout_p95_rel_err=ev["model"]["p95_rel_err"])
+
+
+if __name__ == "__main__":
+    main()

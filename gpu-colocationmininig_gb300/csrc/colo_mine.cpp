@@ -542,8 +542,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         const uint64_t ncand = hd.size();
         // LEARNED: predicted rows presize one-pass tables; the queue runs largest first
-        const bool learned = mode == COLO_MODE_LEARNED && !ctx->model.empty() && ncand > 0;
-        std::vector<uint64_t> cap;
+        bool learned = mode == COLO_MODE_LEARNED && !ctx->model.empty() && ncand > 0;
+        std::vector<uint64_t> cap, pc;
         if (learned) {
             std::vector<float> X(ncand * kMlpIn), y(ncand);
             for (uint64_t q = 0; q < ncand; ++q) {
@@ -559,8 +559,18 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             mlp_forward(dparams.get(), dx.get(), ncand, dy.get(), s);
             COLO_CUDA(cudaMemcpyAsync(y.data(), dy.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaStreamSynchronize(s));
-            std::vector<uint64_t> pc(ncand);
-            for (uint64_t q = 0; q < ncand; ++q) pc[q] = presize_rows(y[q]);
+            // a row extends a parent row by one last-member instance: rows <= prow * n_last
+            pc.resize(ncand);
+            uint64_t words = 0;
+            for (uint64_t q = 0; q < ncand; ++q) {
+                const uint64_t most = hd[q].prow * (uint64_t)b.h_fcount[hd[q].m[k - 1]];
+                pc[q] = std::min(presize_rows(y[q]), std::max<uint64_t>(most, 1));
+                words += pc[q] * k;
+            }
+            // a level whose presized tables would exceed 8 GB takes the exact two-pass form
+            if (words > (1ull << 31)) learned = false;
+        }
+        if (learned) {
             std::vector<uint64_t> perm(ncand);
             for (uint64_t q = 0; q < ncand; ++q) perm[q] = q;
             std::stable_sort(perm.begin(), perm.end(), [&](uint64_t a, uint64_t c) { return pc[a] > pc[c]; });

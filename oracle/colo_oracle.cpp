@@ -1109,3 +1109,95 @@ int oracle_parse_params(const char* path, float* R, float* thr, uint32_t* filter
 }
 
 }  // extern "C"
+
+/* ------------------------------------------------------------------------- */
+/* Cost model: the network of the CUDA kernels (gpu-colocationmininig_gb300/  */
+/* csrc/colo_mlp.cu) restated per row, to check their outputs and gradients. */
+/* With bf16 = 1 the same values are rounded to BF16 (round to nearest even) */
+/* before they enter a product: inputs, weights, H1, H2, dZ2, dZ1; sums are   */
+/* taken in double.  With bf16 = 0 nothing is rounded, so the gradient can   */
+/* be checked against finite differences.                                    */
+/* ------------------------------------------------------------------------- */
+static float bf16_rne(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+namespace {
+constexpr int MI = 24, MIP = 32, MH = 64;
+constexpr int M_W1 = 0, M_B1 = MIP * MH, M_W2 = M_B1 + MH, M_B2 = M_W2 + MH * MH, M_W3 = M_B2 + MH, M_B3 = M_W3 + MH;
+
+struct MlpRow {
+    double xb[MIP], z1[MH], h1[MH], z2[MH], h2[MH], y;
+};
+
+void mlp_row(const float* P, const float* x, int bf16, MlpRow& r) {
+    auto q = [&](double v) { return bf16 ? (double)bf16_rne((float)v) : v; };
+    for (int i = 0; i < MIP; ++i) r.xb[i] = i < MI ? q(x[i]) : 0.0;
+    for (int o = 0; o < MH; ++o) {
+        double a = P[M_B1 + o];
+        for (int i = 0; i < MIP; ++i) a += r.xb[i] * q(P[M_W1 + i * MH + o]);
+        r.z1[o] = a;
+        r.h1[o] = q(a > 0 ? a : 0.0);
+    }
+    for (int o = 0; o < MH; ++o) {
+        double a = P[M_B2 + o];
+        for (int i = 0; i < MH; ++i) a += r.h1[i] * q(P[M_W2 + i * MH + o]);
+        r.z2[o] = a;
+        r.h2[o] = q(a > 0 ? a : 0.0);
+    }
+    double y = P[M_B3];
+    for (int o = 0; o < MH; ++o) y += r.h2[o] * q(P[M_W3 + o]);
+    r.y = y;
+}
+}  // namespace
+
+extern "C" {
+
+void oracle_mlp_forward(const float* P, const float* X, uint64_t n, int bf16, double* Y) {
+    MlpRow r;
+    for (uint64_t i = 0; i < n; ++i) {
+        mlp_row(P, X + i * MI, bf16, r);
+        Y[i] = r.y;
+    }
+}
+
+void oracle_mlp_grad(const float* P, const float* X, const float* T, uint64_t n, int bf16, double* G, double* loss) {
+    auto q = [&](double v) { return bf16 ? (double)bf16_rne((float)v) : v; };
+    const int NP = M_B3 + 1;
+    for (int i = 0; i < NP; ++i) G[i] = 0;
+    double L = 0;
+    MlpRow r;
+    double dz2[MH], dz2b[MH], dz1b[MH];
+    for (uint64_t s = 0; s < n; ++s) {
+        mlp_row(P, X + s * MI, bf16, r);
+        const double d = (r.y - T[s]) / (double)n;
+        L += 0.5 * (r.y - T[s]) * (r.y - T[s]) / (double)n;
+        G[M_B3] += d;
+        for (int o = 0; o < MH; ++o) {
+            G[M_W3 + o] += r.h2[o] * d;
+            dz2[o] = r.z2[o] > 0 ? d * q(P[M_W3 + o]) : 0.0;
+            G[M_B2 + o] += dz2[o];
+            dz2b[o] = q(dz2[o]);
+        }
+        for (int i = 0; i < MH; ++i) {
+            double a = 0;
+            for (int o = 0; o < MH; ++o) a += dz2b[o] * q(P[M_W2 + i * MH + o]);
+            const double dz1 = r.z1[i] > 0 ? a : 0.0;
+            G[M_B1 + i] += dz1;
+            dz1b[i] = q(dz1);
+        }
+        for (int i = 0; i < MH; ++i)
+            for (int o = 0; o < MH; ++o) G[M_W2 + i * MH + o] += r.h1[i] * dz2b[o];
+        for (int i = 0; i < MI; ++i)
+            for (int o = 0; o < MH; ++o) G[M_W1 + i * MH + o] += r.xb[i] * dz1b[o];
+    }
+    if (loss) *loss = L;
+}
+
+}  // extern "C"

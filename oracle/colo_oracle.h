@@ -119,6 +119,13 @@ int oracle_parse_csv(const char* path, uint64_t* n, uint32_t* nfeat, float* x, f
                      uint32_t* feat, float bounds[4], char* names, uint64_t names_cap);
 int oracle_parse_params(const char* path, float* R, float* thr, uint32_t* filter_flag);
 
+/* Cost model (the CUDA kernels' network): predictions and the gradient of
+ * mean 0.5*(y - t)^2 (6337 parameters); bf16 = 1 rounds to BF16 where the
+ * kernels do, bf16 = 0 computes exactly in double. */
+void oracle_mlp_forward(const float* P, const float* X, uint64_t n, int bf16, double* Y);
+void oracle_mlp_grad(const float* P, const float* X, const float* T, uint64_t n, int bf16, double* G,
+                     double* loss);
+
 #ifdef __cplusplus
 }
 #endif

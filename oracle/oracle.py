@@ -23,6 +23,7 @@ _u64p = C.POINTER(C.c_uint64)
 _u32p = C.POINTER(C.c_uint32)
 _u8p = C.POINTER(C.c_uint8)
 _f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
 _lib = None
 
 
@@ -72,6 +73,8 @@ def load():
         "oracle_sqdist": (C.c_float, [C.c_float, C.c_float, C.c_float, C.c_float]),
         "oracle_sq_decide_batch": (None, [_f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _u8p, _u8p, _f32p,
                                           _u8p]),
+        "oracle_mlp_forward": (None, [_f32p, _f32p, C.c_uint64, C.c_int, _f64p]),
+        "oracle_mlp_grad": (None, [_f32p, _f32p, _f32p, C.c_uint64, C.c_int, _f64p, _f64p]),
         "oracle_ambiguous_pairs": (C.c_uint64, [_f32p, _f32p, _u32p, C.c_uint64, C.c_float, _u64p, C.c_uint64]),
         "oracle_cell_adjacent": (C.c_int, [V, C.c_uint64, C.c_uint64]),
         "oracle_make_grid": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, V]),
@@ -285,3 +288,26 @@ def sq_decide_batch(x1, y1, x2, y2, R2):
     load().oracle_sq_decide_batch(*[_p(v, _f32p) for v in a], n, R2, _p(le, _u8p), _p(amb, _u8p), _p(val, _f32p),
                                   _p(near, _u8p))
     return le.astype(bool), amb.astype(bool), val, near.astype(bool)
+
+
+def mlp_forward(params, x, bf16=True) -> np.ndarray:
+    """Cost-model predictions (float64) with the kernels' BF16 rounding points (bf16) or exactly."""
+    lib = load()
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 24)
+    y = np.zeros(len(x), np.float64)
+    lib.oracle_mlp_forward(_p(p, _f32p), _p(x, _f32p), len(x), int(bool(bf16)), _p(y, _f64p))
+    return y
+
+
+def mlp_grad(params, x, t, bf16=True):
+    """(gradient float64[6337], loss) of mean 0.5*(y - t)^2."""
+    lib = load()
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 24)
+    t = np.ascontiguousarray(t, np.float32)
+    g = np.zeros(p.size, np.float64)
+    loss = C.c_double(0)
+    lib.oracle_mlp_grad(_p(p, _f32p), _p(x, _f32p), _p(t, _f32p), len(x), int(bool(bf16)), _p(g, _f64p),
+                        C.byref(loss))
+    return g, float(loss.value)

@@ -40,7 +40,7 @@ EXPORTS = [
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
     "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
-    "colo_ctx_set_model", "colo_result_features",
+    "colo_ctx_set_model", "colo_result_features", "colo_autotune",
 ]
 MODEL_FEATURES = 24
 MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -126,6 +126,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_model_train": (C.c_int, [_P, _f32p, _f32p, _f32p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float,
                                        C.c_uint64, _f32p]),
         "colo_ctx_set_model": (C.c_int, [_P, _f32p]),
+        "colo_autotune": (C.c_int, [_P, _P, C.POINTER(Params), _i32p, C.POINTER(C.c_double)]),
         "colo_result_features": (C.c_int, [_P, C.c_uint32, _f32p]),
     }
     for name, (res, args) in sig.items():
@@ -343,6 +344,13 @@ class Context:
         self.check(self.lib.colo_stage_within(self.h, *[_ptr(v, _f32p) for v in a], len(out), R2, _ptr(out, _f32p),
                                               _ptr(w, _u8p)), "stage_within")
         return out, w.astype(bool)
+
+    def autotune(self, ds: "Dataset", params: Params) -> dict:
+        """Pick the join's lanes per anchor for this dataset (kept for later mines)."""
+        jg = C.c_int32(0)
+        ms = (C.c_double * 4)()
+        self.check(self.lib.colo_autotune(self.h, ds.h, C.byref(params), C.byref(jg), ms), "autotune")
+        return {"join_group": int(jg.value), "join_ms": dict(zip((4, 8, 16, 32), list(ms)))}
 
     # ---- learned cost model -------------------------------------------------
     def model_forward(self, params: np.ndarray, x: np.ndarray) -> np.ndarray:

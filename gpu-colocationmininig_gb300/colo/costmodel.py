@@ -35,8 +35,12 @@ def dataset_size(seed: int) -> int:
     return int(math.exp(rng.uniform(math.log(200_000), math.log(2_000_000))))
 
 
-def collect(ctx: Context, seeds, thresholds=(0.15, 0.08), log=None):
-    """(X float32[n, 24], log1p(rows) float32[n], k int[n]) of every refined candidate."""
+THRESHOLDS = (0.15, 0.1, 0.07, 0.05, 0.035)   # the workload's 0.15 and lower ones (more, larger candidates)
+PER_MINE_CAP = 20_000                          # samples kept per mine (uniform subsample)
+
+
+def collect(ctx: Context, seeds, thresholds=THRESHOLDS, log=None, cap=PER_MINE_CAP):
+    """(X float32[n, 24], log1p(rows) float32[n], k int[n]) of the refined candidates."""
     xs, ts, ks = [], [], []
     for seed in seeds:
         n = dataset_size(seed)
@@ -44,13 +48,23 @@ def collect(ctx: Context, seeds, thresholds=(0.15, 0.08), log=None):
         ds = Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
         for thr in thresholds:
             res = ctx.mine(ds, default_params(wl.R, thr, MODE_BATCHED, max_size=wl.max_size))
+            mx, mt, mk = [], [], []
             for lev in res.levels:
                 sel = lev.passed.astype(bool)
                 if not sel.any():
                     continue
-                xs.append(lev.features[sel])
-                ts.append(np.log1p(lev.rows[sel].astype(np.float64)).astype(np.float32))
-                ks.append(np.full(int(sel.sum()), lev.k, np.int32))
+                mx.append(lev.features[sel])
+                mt.append(np.log1p(lev.rows[sel].astype(np.float64)).astype(np.float32))
+                mk.append(np.full(int(sel.sum()), lev.k, np.int32))
+            if not mx:
+                continue
+            mx, mt, mk = np.concatenate(mx), np.concatenate(mt), np.concatenate(mk)
+            if cap and len(mt) > cap:
+                keep = np.sort(np.random.default_rng(seed * 7 + int(thr * 1000)).choice(len(mt), cap, replace=False))
+                mx, mt, mk = mx[keep], mt[keep], mk[keep]
+            xs.append(mx)
+            ts.append(mt)
+            ks.append(mk)
         if log:
             log(f"seed {seed}: {n} points, {sum(len(t) for t in ts)} samples so far")
     if not xs:
@@ -61,6 +75,20 @@ def collect(ctx: Context, seeds, thresholds=(0.15, 0.08), log=None):
 def heuristic_log_rows(x: np.ndarray) -> np.ndarray:
     """Presize without the network: log1p(parent rows) + log1p(ub_last) - log1p(n_last)."""
     return x[:, 17] + x[:, 23]
+
+
+def heuristic_params() -> np.ndarray:
+    """The same heuristic written as parameters of the network, so the library can run it in place
+    of the trained model: y = relu(x17) - relu(-x23) = x17 + x23 (x17 >= 0, x23 <= 0)."""
+    p = np.zeros(32 * 64 + 64 + 64 * 64 + 64 + 64 + 1, np.float32)
+    w1, w2, w3 = 0, 32 * 64 + 64, 32 * 64 + 64 + 64 * 64 + 64
+    p[w1 + 17 * 64 + 0] = 1.0
+    p[w1 + 23 * 64 + 1] = -1.0
+    p[w2 + 0 * 64 + 0] = 1.0
+    p[w2 + 1 * 64 + 1] = 1.0
+    p[w3 + 0] = 1.0
+    p[w3 + 1] = -1.0
+    return p
 
 
 def errors(pred_log: np.ndarray, t_log: np.ndarray) -> dict:

@@ -13,9 +13,10 @@
 namespace colo {
 namespace {
 
+template <class KT>
 __global__ void k_cell_keys(uint64_t n, const float* __restrict__ x, const float* __restrict__ y,
                             const uint32_t* __restrict__ feat, const uint32_t* __restrict__ fjob,
-                            const JobGrid* __restrict__ grids, uint64_t* __restrict__ keys,
+                            const JobGrid* __restrict__ grids, KT* __restrict__ keys,
                             uint32_t* __restrict__ vals, DevFlags* flags) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -25,7 +26,7 @@ __global__ void k_cell_keys(uint64_t n, const float* __restrict__ x, const float
         atomicAdd(&flags->out_of_grid, 1u);
         c = g.total - 1;
     }
-    keys[i] = g.key_base + c;
+    keys[i] = (KT)(g.key_base + c);
     vals[i] = (uint32_t)i;
 }
 
@@ -41,7 +42,8 @@ __global__ void k_gather_sorted(uint64_t n, const uint32_t* __restrict__ sid,
     sfeat[p] = feat[id];
 }
 
-__global__ void k_heads(uint64_t n, const uint64_t* __restrict__ keys,
+template <class KT>
+__global__ void k_heads(uint64_t n, const KT* __restrict__ keys,
                         const uint32_t* __restrict__ sfeat, uint32_t* __restrict__ cell_head,
                         uint32_t* __restrict__ run_head) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -52,7 +54,8 @@ __global__ void k_heads(uint64_t n, const uint64_t* __restrict__ keys,
     run_head[p] = rh;
 }
 
-__global__ void k_compact(uint64_t n, const uint64_t* __restrict__ keys,
+template <class KT>
+__global__ void k_compact(uint64_t n, const KT* __restrict__ keys,
                           const uint32_t* __restrict__ sfeat, const uint32_t* __restrict__ fjob,
                           const uint32_t* __restrict__ cell_head, const uint32_t* __restrict__ run_head,
                           const uint32_t* __restrict__ cell_ex, const uint32_t* __restrict__ run_ex,
@@ -224,49 +227,109 @@ __global__ void k_nrl_count(uint64_t M, const uint64_t* __restrict__ ckey, const
     nrl_len[c] = nr;
 }
 
-// One thread per cell.  A run of feature f in adjacent slot s lands at
-// sum over slots of (#runs with feature < f) plus the number of earlier slots
-// that also hold f.  Then, per run of the cell itself, the first entry with a
-// higher feature and the number of points from there on.
-__global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                           const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                           const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
-                           const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ nrl_off,
-                           uint32_t* __restrict__ nrl_feat, uint32_t* __restrict__ nrl_run,
-                           uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
-    uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= M) return;
+// The list of cell c (lanes l = 0..G-1 of a group share it).  A run of
+// feature f in adjacent slot s lands at sum over slots of (#runs with feature
+// < f) plus the number of earlier slots that also hold f.  Per own run of
+// the cell: the first entry with a higher feature and the number of target
+// points from there on (the points of each adjacent cell past its runs of
+// features <= f), both from one binary search per slot.
+template <int G>
+__device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __restrict__ ckey,
+                                         const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
+                                         const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cstart,
+                                         const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
+                                         const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ nrl_off,
+                                         uint32_t* __restrict__ nrl_feat, uint32_t* __restrict__ nrl_run,
+                                         uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
     int32_t adj[9];
-    int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
-    const uint64_t base = nrl_off[c], end = nrl_off[c + 1];
-    for (int s = 0; s < na; ++s) {
-        uint32_t r0 = crun[adj[s]], r1 = crun[adj[s] + 1];
-        for (uint32_t r = r0; r < r1; ++r) {
-            uint32_t f = rfeat[r];
-            uint64_t pos = 0;
-            for (int t = 0; t < na; ++t) {
-                uint32_t q0 = crun[adj[t]], q1 = crun[adj[t] + 1];
-                uint32_t lb = (uint32_t)lower_bound_dev(rfeat, (uint64_t)q0, (uint64_t)q1, f);
-                pos += lb - q0;
-                if (t < s && lb < q1 && rfeat[lb] == f) pos += 1;
-            }
-            nrl_feat[base + pos] = f;
-            nrl_run[base + pos] = r;
+    const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+    uint32_t q0[9], q1[9], pre[10];
+    pre[0] = 0;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        if (t < na) {
+            q0[t] = crun[adj[t]];
+            q1[t] = crun[adj[t] + 1];
+        } else {
+            q0[t] = q1[t] = 0;
         }
+        pre[t + 1] = pre[t] + (q1[t] - q0[t]);
     }
-    for (uint32_t r = crun[c]; r < crun[c + 1]; ++r) {
-        uint32_t f = rfeat[r];
-        uint64_t lo = base, hi = end;
-        while (lo < hi) {
-            uint64_t mid = (lo + hi) >> 1;
-            if (nrl_feat[mid] <= f) lo = mid + 1;
-            else hi = mid;
+    const uint64_t base = nrl_off[c];
+    for (uint32_t e = l; e < pre[9]; e += G) {
+        int sl = 0;
+        uint32_t r = 0;
+#pragma unroll
+        for (int t = 0; t < 9; ++t)
+            if (e >= pre[t] && e < pre[t + 1]) {
+                sl = t;
+                r = q0[t] + (e - pre[t]);
+            }
+        const uint32_t f = rfeat[r];
+        uint64_t pos = 0;
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            if (t < na) {
+                const uint32_t lb = (uint32_t)lower_bound_dev(rfeat, (uint64_t)q0[t], (uint64_t)q1[t], f);
+                pos += lb - q0[t];
+                if (t < sl && lb < q1[t] && rfeat[lb] == f) pos += 1;
+            }
         }
+        nrl_feat[base + pos] = f;
+        nrl_run[base + pos] = r;
+    }
+    for (uint32_t r = crun[c] + l; r < crun[c + 1]; r += G) {
+        const uint32_t f = rfeat[r];
+        uint64_t sfx = base;
         uint32_t L = 0;
-        for (uint64_t q = lo; q < end; ++q) L += rcnt[nrl_run[q]];
-        run_sfx[r] = lo;
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            if (t < na) {
+                const uint32_t ub = (uint32_t)lower_bound_dev(rfeat, (uint64_t)q0[t], (uint64_t)q1[t], f + 1);
+                sfx += ub - q0[t];
+                if (ub < q1[t]) L += cstart[adj[t] + 1] - rstart[ub];
+            }
+        }
+        run_sfx[r] = sfx;
         run_L[r] = L;
     }
+}
+
+constexpr uint32_t kBigList = 64;   // cells with longer lists get a warp each
+
+// One thread per cell; cells with lists longer than kBigList are queued for
+// k_nrl_fill_big.
+__global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+                           const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
+                           const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
+                           const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
+                           const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_feat,
+                           uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
+                           uint32_t* __restrict__ run_L, uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
+    uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M) return;
+    if (nrl_off[c + 1] - nrl_off[c] > kBigList) {
+        big[atomicAdd(nbig, 1u)] = (uint32_t)c;
+        return;
+    }
+    nrl_cell<1>(c, 0, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, nrl_off, nrl_feat, nrl_run, run_sfx,
+                run_L);
+}
+
+// A warp per queued cell (grid-stride over the queue).
+__global__ void k_nrl_fill_big(const uint32_t* __restrict__ big, const uint32_t* __restrict__ nbig,
+                               const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+                               const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
+                               const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
+                               const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
+                               const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_feat,
+                               uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
+                               uint32_t* __restrict__ run_L) {
+    const uint32_t n = *nbig;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5)
+        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, nrl_off, nrl_feat, nrl_run,
+                     run_sfx, run_L);
 }
 
 inline unsigned grid_for(uint64_t n, int threads) {
@@ -276,20 +339,27 @@ inline unsigned grid_for(uint64_t n, int threads) {
 
 }  // namespace
 
-void bucket_points(Batch& b) {
+// Cell keys, the stable sort by key, the sorted point copies and the cell /
+// run compaction, with KT = 32-bit keys when every key fits (less traffic per
+// radix pass), else 64-bit.
+template <class KT>
+void sort_and_compact(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t n = b.N;
-    DevBuf<uint64_t> keys;
+    DevBuf<KT> keys;
     keys.alloc(n, s);
     b.sid.alloc(n, s);
     {
     KScope ks("cell_keys");
-    k_cell_keys<<<grid_for(n, 256), 256, 0, s>>>(n, b.x, b.y, b.feat, b.fjob.get(), b.grids.get(),
-                                                  keys.get(), b.sid.get(), b.flags.get());
+    k_cell_keys<KT><<<grid_for(n, 256), 256, 0, s>>>(n, b.x, b.y, b.feat, b.fjob.get(), b.grids.get(),
+                                                      keys.get(), b.sid.get(), b.flags.get());
     COLO_LAUNCH_CHECK();
     count_launch();
     }
-    radix_sort_u64_u32(keys.get(), b.sid.get(), n, (int)b.key_bits, s);
+    if (sizeof(KT) == 4)
+        radix_sort_u32_u32(reinterpret_cast<uint32_t*>(keys.get()), b.sid.get(), n, (int)b.key_bits, s);
+    else
+        radix_sort_u64_u32(reinterpret_cast<uint64_t*>(keys.get()), b.sid.get(), n, (int)b.key_bits, s);
 
     b.sx.alloc(n, s);
     b.sy.alloc(n, s);
@@ -304,7 +374,7 @@ void bucket_points(Batch& b) {
     rh.alloc(n, s);
     cex.alloc(n, s);
     rex.alloc(n, s);
-    k_heads<<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), ch.get(), rh.get());
+    k_heads<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), ch.get(), rh.get());
     COLO_LAUNCH_CHECK();
     count_launch();
     uint32_t M = 0, Rn = 0;
@@ -321,7 +391,7 @@ void bucket_points(Batch& b) {
     b.rcnt.alloc(Rn, s);
     b.rcell.alloc(Rn, s);
     b.scell.alloc(n, s);
-    k_compact<<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), b.fjob.get(), ch.get(),
+    k_compact<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), b.fjob.get(), ch.get(),
                                                 rh.get(), cex.get(), rex.get(), b.ckey.get(),
                                                 b.cstart.get(), b.crun.get(), b.cjob.get(),
                                                 b.rfeat.get(), b.rstart.get(), b.rcell.get(),
@@ -332,11 +402,13 @@ void bucket_points(Batch& b) {
                                                   b.crun.get());
     COLO_LAUNCH_CHECK();
     count_launch();
-    keys.release();
-    ch.release();
-    rh.release();
-    cex.release();
-    rex.release();
+}
+
+void bucket_points(Batch& b) {
+    cudaStream_t s = b.s;
+    if (b.key_bits <= 32) sort_and_compact<uint32_t>(b);
+    else sort_and_compact<uint64_t>(b);
+    const uint64_t M = b.M, Rn = b.Rn;
 
     b.cmask.alloc((uint64_t)M * b.W, s);
     b.cmask.zero(s);
@@ -410,12 +482,22 @@ void build_neighborhoods(Batch& b) {
     b.run_L.alloc(b.Rn, s);
     {
         KScope ks("nrl_fill");
+        DevBuf<uint32_t> big, nbig;
+        big.alloc(M ? M : 1, s);
+        nbig.alloc(1, s);
+        nbig.zero(s);
         k_nrl_fill<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
-                                                     b.crun.get(), b.rfeat.get(), b.rcnt.get(), b.nrl_off.get(),
-                                                     b.nrl_feat.get(), b.nrl_run.get(), b.run_sfx.get(),
-                                                     b.run_L.get());
+                                                     b.cstart.get(), b.crun.get(), b.rfeat.get(), b.rstart.get(),
+                                                     b.nrl_off.get(), b.nrl_feat.get(), b.nrl_run.get(),
+                                                     b.run_sfx.get(), b.run_L.get(), big.get(), nbig.get());
         COLO_LAUNCH_CHECK();
-        count_launch();
+        k_nrl_fill_big<<<(unsigned)(b.sms * 8), 256, 0, s>>>(big.get(), nbig.get(), b.ckey.get(), b.cjob.get(),
+                                                             b.grids.get(), b.nb9.get(), b.cstart.get(), b.crun.get(),
+                                                             b.rfeat.get(), b.rstart.get(), b.nrl_off.get(),
+                                                             b.nrl_feat.get(), b.nrl_run.get(), b.run_sfx.get(),
+                                                             b.run_L.get());
+        COLO_LAUNCH_CHECK();
+        count_launch(2);
     }
     COLO_CUDA(cudaStreamSynchronize(s));
 }

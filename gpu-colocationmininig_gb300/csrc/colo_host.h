@@ -72,6 +72,7 @@ struct colo_ctx {
     std::string err;
     int refs = 1;          // the owner plus one per live dataset (freed at zero)
     std::vector<float> model;   // cost-model parameters for LEARNED mines (empty: none)
+    int join_group = 0;         // lanes per anchor in the join (0: default; set by colo_autotune)
 };
 
 struct colo_dataset {

@@ -215,5 +215,7 @@ void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t
 // Results land back in keys/vals.
 void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s,
                         const char* name = "radix_sort");
+void radix_sort_u32_u32(uint32_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s,
+                        const char* name = "radix_sort");
 
 }  // namespace colo

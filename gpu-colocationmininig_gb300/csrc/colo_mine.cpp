@@ -248,6 +248,7 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     b.s = s;
     b.sms = ctx->sms;
     b.J = J;
+    if (ctx->join_group) b.join_group = ctx->join_group;
     auto t0 = Clock::now();
     std::vector<uint32_t> job_f0(J + 1, 0);
     uint64_t N = 0;

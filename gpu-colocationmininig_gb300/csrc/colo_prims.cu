@@ -144,7 +144,8 @@ constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortRounds = 8;                          // items per lane
 constexpr int kSortTile = kSortThreads * kSortRounds;   // 2048
 
-__global__ void k_radix_hist(const uint64_t* __restrict__ keys, uint64_t n, int shift,
+template <class KT>
+__global__ void k_radix_hist(const KT* __restrict__ keys, uint64_t n, int shift,
                              uint32_t* __restrict__ hist, uint32_t nblocks) {
     __shared__ uint32_t h[kRadix];
     for (int i = threadIdx.x; i < kRadix; i += blockDim.x) h[i] = 0;
@@ -160,8 +161,9 @@ __global__ void k_radix_hist(const uint64_t* __restrict__ keys, uint64_t n, int 
 
 // Stable scatter: items of a tile are ranked in (warp, round, lane) order,
 // which is their input order.
-__global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+template <class KT>
+__global__ void k_radix_scatter(const KT* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                KT* __restrict__ kout, uint32_t* __restrict__ vout,
                                 uint64_t n, int shift, const uint32_t* __restrict__ offs,
                                 uint32_t nblocks) {
     __shared__ uint32_t wh[kSortWarps][kRadix];
@@ -169,7 +171,7 @@ __global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t
     for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&wh[0][0])[i] = 0;
     __syncthreads();
     uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)w * (32 * kSortRounds);
-    uint64_t key[kSortRounds];
+    KT key[kSortRounds];
     uint32_t val[kSortRounds];
     uint32_t rank[kSortRounds];
     const uint32_t lt = (1u << lane) - 1u;
@@ -228,38 +230,51 @@ void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t
     scan_impl<uint64_t, uint64_t>(in, out, n, s, total_host);
 }
 
-void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
+namespace {
+
+template <class KT>
+void radix_sort_impl(KT* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
     uint32_t nblocks = (uint32_t)((n + kSortTile - 1) / kSortTile);
-    DevBuf<uint64_t> k2;
+    DevBuf<KT> k2;
     DevBuf<uint32_t> v2, hist, offs;
     k2.alloc(n, s);
     v2.alloc(n, s);
     hist.alloc((uint64_t)kRadix * nblocks, s);
     offs.alloc((uint64_t)kRadix * nblocks, s);
-    uint64_t* ka = keys;
+    KT* ka = keys;
     uint32_t* va = vals;
-    uint64_t* kb = k2.get();
+    KT* kb = k2.get();
     uint32_t* vb = v2.get();
     int passes = (bits + kRadixBits - 1) / kRadixBits;
     for (int p = 0; p < passes; ++p) {
         int shift = p * kRadixBits;
         KScope ks(name);
-        k_radix_hist<<<nblocks, kSortThreads, 0, s>>>(ka, n, shift, hist.get(), nblocks);
+        k_radix_hist<KT><<<nblocks, kSortThreads, 0, s>>>(ka, n, shift, hist.get(), nblocks);
         COLO_LAUNCH_CHECK();
         count_launch();
         scan_u32_to_u32(hist.get(), offs.get(), (uint64_t)kRadix * nblocks, s, nullptr);
-        k_radix_scatter<<<nblocks, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, offs.get(), nblocks);
+        k_radix_scatter<KT><<<nblocks, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, offs.get(), nblocks);
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);
         std::swap(va, vb);
     }
     if (ka != keys) {
-        COLO_CUDA(cudaMemcpyAsync(keys, ka, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+        COLO_CUDA(cudaMemcpyAsync(keys, ka, n * sizeof(KT), cudaMemcpyDeviceToDevice, s));
         COLO_CUDA(cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     }
+}
+
+}  // namespace
+
+void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
+    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name);
+}
+
+void radix_sort_u32_u32(uint32_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
+    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name);
 }
 
 }  // namespace colo

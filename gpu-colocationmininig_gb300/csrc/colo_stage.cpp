@@ -197,4 +197,51 @@ colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, c
     });
 }
 
+colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, int32_t* join_group,
+                          double* ms) {
+    if (!ctx || !ds || !p) return COLO_ERR_ARG;
+    return run_guarded(ctx, [&]() -> colo_status {
+        static const int widths[4] = {4, 8, 16, 32};
+        Batch b;
+        std::vector<DevBuf<float>> of;
+        std::vector<DevBuf<uint32_t>> ou;
+        colo_dataset* dsv[1] = {ds};
+        setup_batch(ctx, dsv, p, 1, b, of, ou, nullptr);
+        int best = 8;
+        double best_ms = 1e300, t[4] = {0, 0, 0, 0};
+        if (b.N) {
+            bucket_points(b);
+            build_neighborhoods(b);
+            cudaEvent_t e0, e1;
+            COLO_CUDA(cudaEventCreate(&e0));
+            COLO_CUDA(cudaEventCreate(&e1));
+            for (int i = 0; i < 4; ++i) {
+                b.join_group = widths[i];
+                join_neighbors(b);   // warm-up
+                float tot = 0.f;
+                for (int rep = 0; rep < 2; ++rep) {
+                    COLO_CUDA(cudaEventRecord(e0, ctx->s));
+                    join_neighbors(b);
+                    COLO_CUDA(cudaEventRecord(e1, ctx->s));
+                    COLO_CUDA(cudaEventSynchronize(e1));
+                    float v = 0.f;
+                    COLO_CUDA(cudaEventElapsedTime(&v, e0, e1));
+                    tot += v;
+                }
+                t[i] = tot / 2.0;
+                if (t[i] < best_ms) {
+                    best_ms = t[i];
+                    best = widths[i];
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        ctx->join_group = best;
+        if (join_group) *join_group = best;
+        if (ms) std::memcpy(ms, t, sizeof(t));
+        return COLO_OK;
+    });
+}
+
 }  // extern "C"

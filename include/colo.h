@@ -180,6 +180,16 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
 colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
                               const float* y2, uint64_t n, float R2, float* out, uint8_t* within);
 
+/* ---- autotuning ------------------------------------------------------- */
+/* Times the cell-pair join of this dataset at 4, 8, 16 and 32 lanes per
+ * anchor (CUDA events, after a warm-up) and keeps the fastest for later
+ * mines on this context.  The join writes the same lists at every width.
+ * join_group (optional) receives the choice, ms (optional, 4 doubles) the
+ * times.  The cell size is not tuned: it is R, as the reference's neighbour
+ * rule is defined on that grid.  No counterpart in the reference. */
+colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, int32_t* join_group,
+                          double* ms);
+
 /* ---- learned cost model ----------------------------------------------- */
 /* A 24 -> 64 -> 64 -> 1 ReLU MLP (BF16 weights and activations, FP32
  * accumulation, hand-written tensor-core kernels) that predicts

@@ -1,0 +1,31 @@
+"""The join autotuner: it picks one of the lane widths, and the neighbour
+lists and mining results do not depend on the width it picks."""
+import numpy as np
+import pytest
+
+import colo
+from colo import gen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("cfg,scale", [(0, 1.0), (1, 0.02), (3, 0.005)])
+def test_autotuned_join_gives_identical_results(cfg, scale):
+    wl = gen.config(cfg, scale=scale)
+    plain_ctx = colo.Context(0)
+    ds0 = colo.Dataset.from_arrays(plain_ctx, wl.x, wl.y, wl.fid, wl.bounds)
+    params = colo.default_params(wl.R, wl.thr, colo.MODE_BATCHED, max_size=wl.max_size)
+    ref = plain_ctx.mine(ds0, params)
+    offs0, nbr0 = plain_ctx.stage_neighbors(ds0, wl.R)
+
+    ctx = colo.Context(0)
+    ds = colo.Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
+    tuned = ctx.autotune(ds, params)
+    assert tuned["join_group"] in (4, 8, 16, 32)
+    assert all(v > 0 for v in tuned["join_ms"].values())
+    got = ctx.mine(ds, params)
+    assert got.patterns() == ref.patterns()
+    for la, lb in zip(got.levels, ref.levels):
+        assert np.array_equal(la.rows, lb.rows) and np.array_equal(la.num, lb.num)
+    offs, nbr = ctx.stage_neighbors(ds, wl.R)
+    assert np.array_equal(offs, offs0) and np.array_equal(nbr, nbr0)

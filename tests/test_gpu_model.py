@@ -127,3 +127,33 @@ def test_learned_without_model_runs_batched(ctx):
     ref = ctx.mine(ds, colo.default_params(wl.R, wl.thr, colo.MODE_BATCHED, max_size=wl.max_size))
     assert got.patterns() == ref.patterns()
     assert got.counters["single_pass"] == 0
+
+
+def test_trained_model_beats_the_model_free_presize(ctx):
+    """What the network gains over the method without it, on datasets it never saw: prediction
+    error, buffer overflows at the 1.5x presize margin, and two-pass fallbacks in real mines."""
+    from colo import costmodel
+    params = colo.load_model()
+    x, t, _ = costmodel.collect(ctx, costmodel.HELDOUT_SEEDS[:2], thresholds=(0.15, 0.07))
+    ev = costmodel.evaluate(ctx, params, x, t)
+    print("held-out", ev)
+    m, h = ev["model"], ev["heuristic"]
+    assert m["median_rel_err"] < 0.15 and m["p95_rel_err"] < 0.6
+    assert m["median_rel_err"] < h["median_rel_err"] / 3
+    assert m["overflow_rate"] < h["overflow_rate"]
+    # the same comparison through the library: the heuristic written as network parameters
+    hp = costmodel.heuristic_params()
+    assert np.allclose(ctx.model_forward(hp, x), costmodel.heuristic_log_rows(x), atol=0.1)
+    wl = gen.config(3, seed=costmodel.HELDOUT_SEEDS[0], scale=0.05)
+    ds = colo.Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
+    out = {}
+    for name, p in (("trained", params), ("heuristic", hp)):
+        ctx.set_model(p)
+        try:
+            out[name] = ctx.mine(ds, colo.default_params(wl.R, 0.07, colo.MODE_LEARNED))
+        finally:
+            ctx.set_model(None)
+    print({k: (v.counters["single_pass"], v.counters["single_pass_overflow"]) for k, v in out.items()})
+    assert out["trained"].patterns() == out["heuristic"].patterns()
+    assert out["heuristic"].counters["single_pass_overflow"] > 0
+    assert out["trained"].counters["single_pass_overflow"] <= 0.25 * out["heuristic"].counters["single_pass_overflow"]

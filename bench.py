@@ -396,7 +396,10 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator; no public dataset exists)",
         "config": {"workload": WORKLOAD, "points": wl.n, "features": wl.nfeat, "candidates_per_step": cands,
                    "join_active_anchors": int(counters["active_anchors"]), "join_pairs": int(counters["join_pairs"]),
-                   "neighbor_entries": int(counters["neighbors"]),
+                   "neighbor_entries": int(counters["neighbors"]), "cells": int(counters["cells"]),
+                   "runs": int(counters["runs"]), "nrl_entries": int(counters["nrl_entries"]),
+                   "filter_items": int(counters["filter_items"]), "filter_full_quads": int(counters["filter_full_quads"]),
+                   "filter_cells": int(counters["filter_cells"]),
                    "form": "batched+learned" if head_mode == colo.MODE_LEARNED else "batched",
                    "l2": "inputs (240 MB) larger than L2 (129 MB); no flush",
                    "parallelism": f"replicas x{world}", "autotuned": tuned},

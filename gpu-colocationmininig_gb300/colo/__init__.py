@@ -27,7 +27,8 @@ STATUS = {0: "COLO_OK", 1: "COLO_ERR_ARG", 2: "COLO_ERR_IO", 3: "COLO_ERR_PARSE"
 MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
 COUNTERS = ["launches", "active_anchors", "neighbors", "rows_written", "join_pairs", "points", "cells", "runs",
             "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
-            "nrl_entries", "refined", "filter_items", "single_pass", "single_pass_overflow", "filter_cell_members"]
+            "nrl_entries", "refined", "filter_items", "single_pass", "single_pass_overflow", "filter_cell_members",
+            "filter_full_quads", "filter_cells", "reserved22", "reserved23"]
 
 # Every symbol declared in include/colo.h (checked by the CPU tests).
 EXPORTS = [
@@ -138,7 +139,9 @@ def load(build: bool = True) -> C.CDLL:
 
 
 def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHED, max_size: int = 0,
-                   keep_tables: bool = False, profile: bool = False) -> Params:
+                   keep_tables: bool = False, profile: bool = False, features: bool = False) -> Params:
+    """Mining parameters; `profile` times every kernel, `features` records the cost-model
+    features of every candidate (training data)."""
     p = Params()
     load().colo_params_default(C.byref(p))
     p.distance = distance
@@ -146,7 +149,7 @@ def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHE
     p.mode = mode
     p.max_size = max_size
     p.keep_tables = 1 if keep_tables else 0
-    p.reserved[0] = 1 if profile else 0
+    p.reserved[0] = (1 if profile else 0) | (2 if features else 0)
     return p
 
 

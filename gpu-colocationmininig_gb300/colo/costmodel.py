@@ -47,7 +47,7 @@ def collect(ctx: Context, seeds, thresholds=THRESHOLDS, log=None, cap=PER_MINE_C
         wl = gen.config(3, seed=seed, scale=n / 20_000_000)
         ds = Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
         for thr in thresholds:
-            res = ctx.mine(ds, default_params(wl.R, thr, MODE_BATCHED, max_size=wl.max_size))
+            res = ctx.mine(ds, default_params(wl.R, thr, MODE_BATCHED, max_size=wl.max_size, features=True))
             mx, mt, mk = [], [], []
             for lev in res.levels:
                 sel = lev.passed.astype(bool)

@@ -49,7 +49,7 @@ struct Batch {
     DevBuf<uint32_t> qmask;      // per cell: masks of the 4 quads containing it ([M][4][W])
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
-    DevBuf<uint32_t> frun_off, frun;
+    DevBuf<uint32_t> frun_off, frun, frun_cell;   // runs in feature order and their cells
     // neighbourhood run lists: for cell c, the runs of its adjacent cells
     // ordered by (feature, cell): nrl_feat/nrl_run[nrl_off[c] .. nrl_off[c+1])
     DevBuf<uint64_t> nrl_off;
@@ -101,8 +101,8 @@ struct CandDesc {
     uint64_t out_cap;            // capacity (single-pass mode)
     unsigned long long* cursor;  // single-pass mode: rows reserved so far
     unsigned long long* rows;    // count pass: rows of this candidate (atomic sum)
-    uint32_t* bitmap;            // member bitmaps, word offsets in bm_off
-    uint64_t bm_off[kMaxK + 1];
+    uint32_t* bitmap;            // member bitmaps: member j's words start at bm_base plus
+    uint64_t bm_base;            // the sum over i < j of ceil(fcount[m[i]] / 32)
     uint32_t job;
     uint32_t k;
 };

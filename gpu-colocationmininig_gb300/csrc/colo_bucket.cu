@@ -181,6 +181,13 @@ __global__ void k_frun_keys(uint64_t Rn, const uint32_t* __restrict__ rfeat, uin
     vals[r] = (uint32_t)r;
 }
 
+// frun_cell[i] = cell of the i-th run in feature order
+__global__ void k_frun_cell(uint64_t Rn, const uint32_t* __restrict__ frun, const uint32_t* __restrict__ rcell,
+                            uint32_t* __restrict__ frun_cell) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < Rn) frun_cell[i] = rcell[frun[i]];
+}
+
 // frun_off[f] = first position of feature f in the feature-sorted run list
 __global__ void k_frun_off(uint32_t F, uint64_t Rn, const uint64_t* __restrict__ keys,
                            uint32_t* __restrict__ frun_off) {
@@ -238,7 +245,8 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
                                          const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
                                          const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cstart,
                                          const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
-                                         const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ nrl_off,
+                                         const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ cmask,
+                                         uint32_t W, const uint64_t* __restrict__ nrl_off,
                                          uint32_t* __restrict__ nrl_feat, uint32_t* __restrict__ nrl_run,
                                          uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
     int32_t adj[9];
@@ -295,25 +303,85 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
     }
 }
 
-constexpr uint32_t kBigList = 64;   // cells with longer lists get a warp each
+constexpr uint32_t kBigList = 512;   // cells with longer lists get a warp each
 
-// One thread per cell; cells with lists longer than kBigList are queued for
-// k_nrl_fill_big.
+// One thread per cell: the list is the 9-way merge of the adjacent cells'
+// run lists (each ascending by feature) by (feature, slot).  The running
+// point count P gives the suffix counts: the cell's own run of feature f
+// gets sfx = the first position after every entry of feature <= f and
+// L = (total points) - P(sfx).  Cells with lists longer than kBigList are
+// queued for k_nrl_fill_big.
 __global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                            const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
                            const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
                            const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
+                           const uint32_t* __restrict__ rcnt,
                            const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_feat,
                            uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
                            uint32_t* __restrict__ run_L, uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
     uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M) return;
-    if (nrl_off[c + 1] - nrl_off[c] > kBigList) {
+    const uint64_t base = nrl_off[c];
+    if (nrl_off[c + 1] - base > kBigList) {
         big[atomicAdd(nbig, 1u)] = (uint32_t)c;
         return;
     }
-    nrl_cell<1>(c, 0, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, nrl_off, nrl_feat, nrl_run, run_sfx,
-                run_L);
+    int32_t adj[9];
+    const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+    uint32_t h[9], e[9], f[9];
+    int own = 0;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        if (t < na) {
+            h[t] = crun[adj[t]];
+            e[t] = crun[adj[t] + 1];
+            f[t] = h[t] < e[t] ? rfeat[h[t]] : 0xffffffffu;
+            if ((uint64_t)adj[t] == c) own = t;
+        } else {
+            h[t] = e[t] = 0;
+            f[t] = 0xffffffffu;
+        }
+    }
+    uint64_t pos = base;
+    uint32_t P = 0, pend_r = 0, pend_f = 0;
+    bool pend = false;
+    for (;;) {
+        int ts = 0;
+        uint32_t fm = f[0];
+#pragma unroll
+        for (int t = 1; t < 9; ++t)
+            if (f[t] < fm) {
+                fm = f[t];
+                ts = t;
+            }
+        if (fm == 0xffffffffu) break;
+        if (pend && pend_f < fm) {
+            run_sfx[pend_r] = pos;
+            run_L[pend_r] = P;
+            pend = false;
+        }
+        uint32_t r = 0;
+#pragma unroll
+        for (int t = 0; t < 9; ++t)
+            if (t == ts) {
+                r = h[t]++;
+                f[t] = h[t] < e[t] ? rfeat[h[t]] : 0xffffffffu;
+            }
+        nrl_feat[pos] = fm;
+        nrl_run[pos] = r;
+        ++pos;
+        P += rcnt[r];
+        if (ts == own) {
+            pend = true;
+            pend_r = r;
+            pend_f = fm;
+        }
+    }
+    if (pend) {
+        run_sfx[pend_r] = pos;
+        run_L[pend_r] = P;
+    }
+    for (uint32_t r = crun[c]; r < crun[c + 1]; ++r) run_L[r] = P - run_L[r];
 }
 
 // A warp per queued cell (grid-stride over the queue).
@@ -322,14 +390,15 @@ __global__ void k_nrl_fill_big(const uint32_t* __restrict__ big, const uint32_t*
                                const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
                                const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
                                const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
+                               const uint32_t* __restrict__ cmask, uint32_t W,
                                const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_feat,
                                uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
                                uint32_t* __restrict__ run_L) {
     const uint32_t n = *nbig;
     const int lane = threadIdx.x & 31;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5)
-        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, nrl_off, nrl_feat, nrl_run,
-                     run_sfx, run_L);
+        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, cmask, W, nrl_off, nrl_feat,
+                     nrl_run, run_sfx, run_L);
 }
 
 inline unsigned grid_for(uint64_t n, int threads) {
@@ -449,6 +518,10 @@ void bucket_points(Batch& b) {
         k_frun_off<<<grid_for(b.F + 1, 128), 128, 0, s>>>(b.F, Rn, fk.get(), b.frun_off.get());
         COLO_LAUNCH_CHECK();
         count_launch();
+        b.frun_cell.alloc(Rn, s);
+        k_frun_cell<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.frun.get(), b.rcell.get(), b.frun_cell.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
         COLO_CUDA(cudaStreamSynchronize(s));
     }
     b.h_frun_off.resize(b.F + 1);
@@ -488,14 +561,15 @@ void build_neighborhoods(Batch& b) {
         nbig.zero(s);
         k_nrl_fill<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
                                                      b.cstart.get(), b.crun.get(), b.rfeat.get(), b.rstart.get(),
-                                                     b.nrl_off.get(), b.nrl_feat.get(), b.nrl_run.get(),
-                                                     b.run_sfx.get(), b.run_L.get(), big.get(), nbig.get());
+                                                     b.rcnt.get(), b.nrl_off.get(), b.nrl_feat.get(),
+                                                     b.nrl_run.get(), b.run_sfx.get(), b.run_L.get(), big.get(),
+                                                     nbig.get());
         COLO_LAUNCH_CHECK();
         k_nrl_fill_big<<<(unsigned)(b.sms * 8), 256, 0, s>>>(big.get(), nbig.get(), b.ckey.get(), b.cjob.get(),
                                                              b.grids.get(), b.nb9.get(), b.cstart.get(), b.crun.get(),
-                                                             b.rfeat.get(), b.rstart.get(), b.nrl_off.get(),
-                                                             b.nrl_feat.get(), b.nrl_run.get(), b.run_sfx.get(),
-                                                             b.run_L.get());
+                                                             b.rfeat.get(), b.rstart.get(), b.cmask.get(), b.W,
+                                                             b.nrl_off.get(), b.nrl_feat.get(), b.nrl_run.get(),
+                                                             b.run_sfx.get(), b.run_L.get());
         COLO_LAUNCH_CHECK();
         count_launch(2);
     }

@@ -71,6 +71,16 @@ __device__ __forceinline__ uint64_t lower_bound_dev(const T* a, uint64_t lo, uin
     return lo;
 }
 
+// Number of set bits of the W-word mask m below bit b.  A cell's runs ascend
+// by feature and its mask has one bit per feature present, so for local
+// feature b the run index in the cell is crun + mask_rank(mask, b).
+__device__ __forceinline__ uint32_t mask_rank(const uint32_t* __restrict__ m, uint32_t b) {
+    const uint32_t wq = b >> 5;
+    uint32_t r = 0;
+    for (uint32_t w = 0; w < wq; ++w) r += __popc(m[w]);
+    return r + __popc(m[wq] & ((1u << (b & 31)) - 1u));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     return (1u << (threadIdx.x & 31)) - 1u;
 }

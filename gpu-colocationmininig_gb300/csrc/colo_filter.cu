@@ -110,12 +110,12 @@ __device__ __forceinline__ bool covers(const uint32_t* __restrict__ qm, const ui
 // Counts of one item accumulate in registers; one atomicAdd per member.
 // stats[c*2] = full quads, stats[c*2+1] = cells in U_c.
 template <int WT>
-__global__ void __launch_bounds__(256) k_filter_level(
+__global__ void __launch_bounds__(256, 5) k_filter_level(
     uint64_t nitems, uint32_t ngrp, const uint64_t* __restrict__ grp_item_off, const uint32_t* __restrict__ grp_fd,
     const uint32_t* __restrict__ grp_lfd, const uint32_t* __restrict__ grp_cand_off,
     const uint32_t* __restrict__ grp_cands, uint32_t k, const uint32_t* __restrict__ cand,
-    const uint32_t* __restrict__ need_all, const uint32_t* __restrict__ frun_off, const uint32_t* __restrict__ frun,
-    const uint32_t* __restrict__ rcell, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
+    const uint32_t* __restrict__ need_all, const uint32_t* __restrict__ frun_off,
+    const uint32_t* __restrict__ frun_cell, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
     const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ crun,
     const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub,
     unsigned long long* __restrict__ stats) {
@@ -133,8 +133,8 @@ __global__ void __launch_bounds__(256) k_filter_level(
         const uint64_t r = item - grp_item_off[lo];
         const uint64_t ci = r / G;
         const uint32_t c = grp_cands[grp_cand_off[lo] + (uint32_t)(r - ci * G)];
-        const uint32_t fd = grp_fd[lo], lfd = grp_lfd[lo];
-        const uint32_t C = rcell[frun[frun_off[fd] + ci]];
+        const uint32_t fd = grp_fd[lo], lfd = grp_lfd[lo], f0 = fd - lfd;
+        const uint32_t C = frun_cell[frun_off[fd] + ci];
         uint32_t need[WT];
 #pragma unroll
         for (int w = 0; w < WT; ++w) need[w] = need_all[(uint64_t)c * W + w];
@@ -175,17 +175,22 @@ __global__ void __launch_bounds__(256) k_filter_level(
                     if (covers<WT>(z4 + p * W, need)) claimed = false;
                 if (!claimed) continue;
                 ++ncells;
-                const uint32_t q0 = crun[Z], q1 = crun[Z + 1];
-                uint32_t pos = q0, prev = 0;
+                // member j's run in Z: crun[Z] + rank of its bit in Z's feature mask
+                uint32_t zm[WT];
+#pragma unroll
+                for (int w = 0; w < WT; ++w) zm[w] = cmask[(uint64_t)Z * W + w];
+                const uint32_t q0 = crun[Z];
 #pragma unroll
                 for (int j = 0; j < kMaxMembersFiltered; ++j) {
                     if ((uint32_t)j < m) {
-                        // runs of a cell ascend by feature; members usually do too
-                        const uint32_t f = mem[j];
-                        if (f < prev) pos = q0;
-                        prev = f;
-                        pos = (uint32_t)lower_bound_dev(rfeat, (uint64_t)pos, (uint64_t)q1, f);
-                        if (pos < q1 && rfeat[pos] == f) acc[j] += rcnt[pos];
+                        const uint32_t lf = mem[j] - f0, wq = lf >> 5;
+                        uint32_t rk = 0, word = 0;
+#pragma unroll
+                        for (int w = 0; w < WT; ++w) {
+                            if ((uint32_t)w < wq) rk += __popc(zm[w]);
+                            if ((uint32_t)w == wq) word = zm[w];
+                        }
+                        if (word >> (lf & 31) & 1u) acc[j] += rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))];
                     }
                 }
             }
@@ -302,7 +307,7 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
 #define COLO_FL(WW)                                                                                              \
     k_filter_level<WW><<<(unsigned)blocks, 256, 0, s>>>(                                                         \
         nitems, ngrp, dgoff.get(), dgfd.get(), dglfd.get(), dgcoff.get(), dgc.get(), k, dcand.get(), dneed.get(), \
-        b.frun_off.get(), b.frun.get(), b.rcell.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(),  \
+        b.frun_off.get(), b.frun_cell.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(),            \
         b.rfeat.get(), b.rcnt.get(), d_ub, d_stats)
     switch (b.W) {
         case 1: COLO_FL(1); break;

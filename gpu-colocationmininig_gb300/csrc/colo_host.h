@@ -42,7 +42,7 @@ struct LevelTrace {
 };
 
 // counters[]: the list in include/colo.h (colo_result_counters).
-constexpr int kNumCounters = 20;
+constexpr int kNumCounters = 24;
 struct MineResult {
     std::vector<LevelTrace> levels;
     double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};

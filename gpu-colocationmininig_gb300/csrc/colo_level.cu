@@ -27,6 +27,13 @@ __device__ __forceinline__ void set_bit(uint32_t* words, uint32_t bit) {
     atomicOr(&words[bit >> 5], 1u << (bit & 31));
 }
 
+// Word offset of member j's participation bitmap in the level's bitmap arena.
+__device__ __forceinline__ uint64_t bm_offset(const CandDesc& d, uint32_t j, const uint32_t* __restrict__ fcount) {
+    uint64_t o = d.bm_base;
+    for (uint32_t i = 0; i < j; ++i) o += (fcount[d.m[i]] + 31u) / 32u;
+    return o;
+}
+
 // K = pattern size (2..8), or 0 for a runtime size read from the descriptor
 // (members kept in global memory, slower; only reached for k > 8).
 template <int K, int MODE>
@@ -53,6 +60,7 @@ __global__ void __launch_bounds__(256) k_level(
     const uint64_t row = (ch - chunk_off[lo]) * 32 + lane;
     const bool valid = row < d.prow;
     const uint32_t flast = d.m[k - 1];
+    const uint64_t bm_last = (MODE == MODE_FILL) ? 0 : bm_offset(d, k - 1, fcount);
     const uint32_t last_start = fstart[flast];
     const uint32_t last_end = last_start + fcount[flast];
     const float R2 = grids[d.job].R2, hu = grids[d.job].R2hu;
@@ -148,7 +156,7 @@ __global__ void __launch_bounds__(256) k_level(
         const uint32_t my_hits = __popc(bal & mymask);
 
         if (MODE == MODE_COUNT || MODE == MODE_SINGLE) {
-            if (ok) set_bit(d.bitmap + d.bm_off[k - 1], b - last_start);
+            if (ok) set_bit(d.bitmap + bm_last, b - last_start);
         }
         if (MODE == MODE_FILL) {
             const uint32_t before_j = __shfl_sync(0xffffffffu, mine, j);
@@ -206,14 +214,19 @@ __global__ void __launch_bounds__(256) k_level(
     if ((MODE == MODE_COUNT || MODE == MODE_SINGLE) && valid) {
         d.slots[row] = mine;
         if (mine) {
-            set_bit(d.bitmap + d.bm_off[0], a0 - fstart[d.m[0]]);
+            set_bit(d.bitmap + d.bm_base, a0 - fstart[d.m[0]]);
             if (K > 0) {
 #pragma unroll
-                for (int q = 1; q < KR - 1; ++q) set_bit(d.bitmap + d.bm_off[q], rid[q] - fstart[d.m[q]]);
+                uint64_t o = d.bm_base + (fcount[d.m[0]] + 31u) / 32u;
+#pragma unroll
+                for (int q = 1; q < KR - 1; ++q) {
+                    set_bit(d.bitmap + o, rid[q] - fstart[d.m[q]]);
+                    o += (fcount[d.m[q]] + 31u) / 32u;
+                }
             } else {
                 for (uint32_t i = 1; i + 1 < k; ++i) {
                     uint32_t ri = d.parent[(uint64_t)i * d.pstride + row];
-                    set_bit(d.bitmap + d.bm_off[i], ri - fstart[d.m[i]]);
+                    set_bit(d.bitmap + bm_offset(d, i, fcount), ri - fstart[d.m[i]]);
                 }
             }
         }
@@ -231,7 +244,7 @@ __global__ void k_level_pi(const CandDesc* __restrict__ cands, uint64_t ncand, u
     __shared__ unsigned long long red[32];
     for (uint32_t j = 0; j < k; ++j) {
         const uint32_t n = fcount[d.m[j]];
-        const uint32_t* w = d.bitmap + d.bm_off[j];
+        const uint32_t* w = d.bitmap + bm_offset(d, j, fcount);
         const uint32_t nw = (n + 31) / 32;
         unsigned long long cntA = 0, cntFull = 0;
         for (uint32_t i = threadIdx.x; i < nw; i += blockDim.x) {

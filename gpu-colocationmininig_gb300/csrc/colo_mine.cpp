@@ -346,7 +346,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         ~Unset() { g_ktimer = nullptr; }
     } unset;
     uint64_t cnt_items = 0, cnt_parent = 0, cnt_fillw = 0, cnt_bmw = 0, cnt_d2h = 0, cnt_refined = 0, cnt_fcm = 0;
-    uint64_t cnt_single = 0, cnt_single_ovf = 0;
+    uint64_t cnt_single = 0, cnt_single_ovf = 0, cnt_fquads = 0, cnt_fcells = 0;
     DevBuf<unsigned long long> d_items;
     d_items.alloc(1, s);
     Batch b;
@@ -471,6 +471,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 L.fquads[c] = hfs[2 * q];
                 L.fcells[c] = hfs[2 * q + 1];
                 cnt_fcm += hfs[2 * q + 1] * std::min<uint32_t>(k, kMaxMembersFiltered);
+                cnt_fquads += hfs[2 * q];
+                cnt_fcells += hfs[2 * q + 1];
             }
             for (uint64_t q = 0; q < ncand; ++q) {
                 LevelTrace& L = *tr[owner[q].first];
@@ -479,13 +481,19 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 L.pass[c] = filter_pass(&L.ub[c * k], &L.cand[c * k], k, b.h_fcount, js[owner[q].first].thr);
             }
         }
-        // cost-model features of every candidate (recorded for training; used by LEARNED)
+        // cost-model features: of every candidate when the caller records them
+        // (reserved[0] bit 1, training data), else of the candidates a LEARNED
+        // mine refines
+        const bool learned_mode = mode == COLO_MODE_LEARNED && !ctx->model.empty();
         for (uint32_t j = 0; j < J; ++j) {
             if (!tr[j]) continue;
+            const bool all = (pv[j].reserved[0] & 2) != 0;
+            if (!all && !learned_mode) continue;
             LevelTrace& L = *tr[j];
             const size_t C = L.cand.size() / k;
             L.feat.assign(C * kMlpIn, 0.f);
             for (size_t c = 0; c < C; ++c) {
+                if (!all && !L.pass[c]) continue;
                 const uint32_t* mem = &L.cand[c * k];
                 uint64_t prow = b.h_fcount[mem[0]];
                 if (k > 2) {
@@ -528,11 +536,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 d.job = j;
                 d.k = k;
                 uint64_t w = 0;
-                for (uint32_t t = 0; t < k; ++t) {
-                    d.bm_off[t] = nwords + w;
-                    w += (b.h_fcount[mem[t]] + 31) / 32;
-                }
-                d.bm_off[k] = nwords + w;
+                for (uint32_t t = 0; t < k; ++t) w += (b.h_fcount[mem[t]] + 31) / 32;
+                d.bm_base = nwords;
                 nwords += w;
                 slot_base.push_back(nslots);
                 nslots += d.prow;
@@ -865,6 +870,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->counters[17] = cnt_single;
         r->counters[18] = cnt_single_ovf;
         r->counters[19] = cnt_fcm;
+        r->counters[20] = cnt_fquads;
+        r->counters[21] = cnt_fcells;
         r->times[0] = ms_since(t_all);
         r->times[1] = t_upload;
         r->times[2] = t_bucket;

@@ -21,7 +21,7 @@ namespace colo {
 // Features of one candidate (colo_result_features documents the layout).
 void candidate_features(uint32_t k, const uint32_t* mem, const uint32_t* fcount, const uint64_t* ub,
                         uint64_t prow, uint64_t fquads, uint64_t fcells, float* x) {
-    auto lg = [](double v) { return (float)std::log1p(v); };
+    auto lg = [](double v) { return std::log1p((float)v); };
     const uint32_t m = std::min<uint32_t>(k, kMaxMembersFiltered);
     for (int i = 0; i < kMlpIn; ++i) x[i] = 0.f;
     x[0] = (float)k / 8.0f;
@@ -164,6 +164,7 @@ colo_status colo_result_features(const colo_result* r, uint32_t li, float* x) {
     if (!r || !x || li >= r->r.levels.size()) return COLO_ERR_ARG;
     const LevelTrace& L = r->r.levels[li];
     if (!L.feat.empty()) std::memcpy(x, L.feat.data(), L.feat.size() * sizeof(float));
+    else std::memset(x, 0, L.cand.size() / (L.k ? L.k : 1) * kMlpIn * sizeof(float));
     return COLO_OK;
 }
 

@@ -55,7 +55,8 @@ typedef struct {
     uint32_t max_size;       /* 0 = no cap (the reference has none) */
     int32_t mode;            /* colo_mode */
     int32_t keep_tables;     /* 1: keep every instance table in the result (tests) */
-    int32_t reserved[6];     /* reserved[0] bit 0: time every kernel with CUDA events */
+    int32_t reserved[6];     /* reserved[0] bit 0: time every kernel with CUDA events;
+                                bit 1: record cost-model features of every candidate */
 } colo_params;
 
 const char* colo_status_string(colo_status s);
@@ -141,7 +142,8 @@ colo_status colo_result_times(const colo_result* r, double* ms8);
  * candidates, [16] (driver cell, candidate) items of the level filters,
  * [17] candidates filled in one presized pass, [18] of those, overflowed and
  * refilled by the two-pass fallback, [19] (cell of U_c, member) run lookups
- * of the level filters. */
+ * of the level filters, [20] full quads found by the level filters, [21]
+ * cells of U_c summed over candidates, [22..23] reserved. */
 colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n);
 /* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set). */
 uint32_t colo_result_num_kernels(const colo_result* r);
@@ -218,7 +220,9 @@ colo_status colo_ctx_set_model(colo_ctx* ctx, const float* params);
  * else 0), [17] log1p(parent rows), [18] log1p(cells of U_c), [19]
  * log1p(full quads), [20] log1p(min n_j), [21] log1p(min ub_j), [22]
  * log1p(parent rows) - log1p(n_last), [23] log1p(ub_last) - log1p(n_last).
- * Quad statistics are 0 for pairs. */
+ * Quad statistics are 0 for pairs.  Recorded for every candidate when the
+ * mine's colo_params.reserved[0] has bit 1 set (training data), else only
+ * for the candidates a COLO_MODE_LEARNED mine refines (zeros elsewhere). */
 colo_status colo_result_features(const colo_result* r, uint32_t li, float* x);
 
 /* ---- allocation-free entry point -------------------------------------- */

@@ -118,6 +118,8 @@ def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
         return 24.0 * Rn * launches
     if name == "cell_keys":        # read x, y, feature; write key, id
         return 24.0 * N
+    if name == "gather_sorted":    # read the sorted ids, gather x, y, feature, write them in cell order
+        return 28.0 * N
     if name == "cell_neighbours":  # read the key, write 9 neighbour indices
         return 44.0 * M
     if name == "quad_masks":       # read 9 indices + masks, write 4 quad masks + the 3x3 union

@@ -38,8 +38,9 @@ struct Batch {
     DevBuf<JobGrid> grids;
     DevBuf<DevFlags> flags;
     // bucketed (sorted by cell key, then id)
+    DevBuf<float2> xy;           // coordinates by id, packed (built by the cell-key pass)
     DevBuf<uint32_t> sid, sfeat, scell;
-    DevBuf<float> sx, sy;
+    DevBuf<float2> sxy;          // coordinates in cell-sorted order
     // cells
     DevBuf<uint64_t> ckey;
     DevBuf<uint32_t> cstart, crun, cjob;

@@ -17,11 +17,13 @@ template <class KT>
 __global__ void k_cell_keys(uint64_t n, const float* __restrict__ x, const float* __restrict__ y,
                             const uint32_t* __restrict__ feat, const uint32_t* __restrict__ fjob,
                             const JobGrid* __restrict__ grids, KT* __restrict__ keys,
-                            uint32_t* __restrict__ vals, DevFlags* flags) {
+                            uint32_t* __restrict__ vals, float2* __restrict__ xy, DevFlags* flags) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const JobGrid g = grids[fjob[feat[i]]];
-    uint64_t c = ref_cell(g, x[i], y[i]);
+    const float xi = x[i], yi = y[i];
+    xy[i] = make_float2(xi, yi);
+    uint64_t c = ref_cell(g, xi, yi);
     if (c >= g.total) {
         atomicAdd(&flags->out_of_grid, 1u);
         c = g.total - 1;
@@ -30,16 +32,23 @@ __global__ void k_cell_keys(uint64_t n, const float* __restrict__ x, const float
     vals[i] = (uint32_t)i;
 }
 
-__global__ void k_gather_sorted(uint64_t n, const uint32_t* __restrict__ sid,
-                                const float* __restrict__ x, const float* __restrict__ y,
-                                const uint32_t* __restrict__ feat, float* __restrict__ sx,
-                                float* __restrict__ sy, uint32_t* __restrict__ sfeat) {
+// Sorted copies: coordinates gathered as one 8-byte load; the feature of a
+// point id is found in the feature start table (points are grouped by
+// feature), which stays in L1.
+__global__ void k_gather_sorted(uint64_t n, uint32_t F, const uint32_t* __restrict__ sid,
+                                const float2* __restrict__ xy, const uint32_t* __restrict__ fstart,
+                                float2* __restrict__ sxy, uint32_t* __restrict__ sfeat) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    uint32_t id = sid[p];
-    sx[p] = x[id];
-    sy[p] = y[id];
-    sfeat[p] = feat[id];
+    const uint32_t id = sid[p];
+    sxy[p] = xy[id];
+    uint32_t lo = 0, hi = F;   // last feature whose start is <= id
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (fstart[mid] <= id) lo = mid;
+        else hi = mid;
+    }
+    sfeat[p] = lo;
 }
 
 template <class KT>
@@ -420,8 +429,9 @@ void sort_and_compact(Batch& b) {
     b.sid.alloc(n, s);
     {
     KScope ks("cell_keys");
+    b.xy.alloc(n, s);
     k_cell_keys<KT><<<grid_for(n, 256), 256, 0, s>>>(n, b.x, b.y, b.feat, b.fjob.get(), b.grids.get(),
-                                                      keys.get(), b.sid.get(), b.flags.get());
+                                                      keys.get(), b.sid.get(), b.xy.get(), b.flags.get());
     COLO_LAUNCH_CHECK();
     count_launch();
     }
@@ -430,22 +440,27 @@ void sort_and_compact(Batch& b) {
     else
         radix_sort_u64_u32(reinterpret_cast<uint64_t*>(keys.get()), b.sid.get(), n, (int)b.key_bits, s);
 
-    b.sx.alloc(n, s);
-    b.sy.alloc(n, s);
+    b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);
-    k_gather_sorted<<<grid_for(n, 256), 256, 0, s>>>(n, b.sid.get(), b.x, b.y, b.feat, b.sx.get(),
-                                                     b.sy.get(), b.sfeat.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("gather_sorted");
+        k_gather_sorted<<<grid_for(n, 256), 256, 0, s>>>(n, b.F, b.sid.get(), b.xy.get(), b.fstart.get(),
+                                                         b.sxy.get(), b.sfeat.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
 
     DevBuf<uint32_t> ch, rh, cex, rex;
     ch.alloc(n, s);
     rh.alloc(n, s);
     cex.alloc(n, s);
     rex.alloc(n, s);
-    k_heads<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), ch.get(), rh.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("cell_compact");
+        k_heads<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), ch.get(), rh.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
     uint32_t M = 0, Rn = 0;
     scan_u32_to_u32(ch.get(), cex.get(), n, s, &M);
     scan_u32_to_u32(rh.get(), rex.get(), n, s, &Rn);
@@ -460,17 +475,23 @@ void sort_and_compact(Batch& b) {
     b.rcnt.alloc(Rn, s);
     b.rcell.alloc(Rn, s);
     b.scell.alloc(n, s);
-    k_compact<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), b.fjob.get(), ch.get(),
-                                                rh.get(), cex.get(), rex.get(), b.ckey.get(),
-                                                b.cstart.get(), b.crun.get(), b.cjob.get(),
-                                                b.rfeat.get(), b.rstart.get(), b.rcell.get(),
-                                                b.scell.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
-    k_run_tail<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, M, n, b.rstart.get(), b.rcnt.get(), b.cstart.get(),
-                                                  b.crun.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("cell_compact");
+        k_compact<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), b.fjob.get(), ch.get(),
+                                                    rh.get(), cex.get(), rex.get(), b.ckey.get(),
+                                                    b.cstart.get(), b.crun.get(), b.cjob.get(),
+                                                    b.rfeat.get(), b.rstart.get(), b.rcell.get(),
+                                                    b.scell.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
+    {
+        KScope ks("cell_compact");
+        k_run_tail<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, M, n, b.rstart.get(), b.rcnt.get(), b.cstart.get(),
+                                                      b.crun.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
 }
 
 void bucket_points(Batch& b) {
@@ -481,10 +502,13 @@ void bucket_points(Batch& b) {
 
     b.cmask.alloc((uint64_t)M * b.W, s);
     b.cmask.zero(s);
-    k_cell_masks<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), b.rcell.get(), b.cjob.get(),
-                                                    b.grids.get(), b.W, b.cmask.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("cell_masks");
+        k_cell_masks<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), b.rcell.get(), b.cjob.get(),
+                                                        b.grids.get(), b.W, b.cmask.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
     b.nb9.alloc((uint64_t)M * 9, s);
     {
         KScope ks("cell_neighbours");
@@ -509,19 +533,28 @@ void bucket_points(Batch& b) {
         fk.alloc(Rn, s);
         b.frun.alloc(Rn, s);
         b.frun_off.alloc(b.F + 1, s);
-        k_frun_keys<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), fk.get(), b.frun.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
+        {
+            KScope ks("run_index");
+            k_frun_keys<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), fk.get(), b.frun.get());
+            COLO_LAUNCH_CHECK();
+            count_launch();
+        }
         int fbits = 1;
         while (fbits < 32 && (1ull << fbits) < b.F) fbits++;
         radix_sort_u64_u32(fk.get(), b.frun.get(), Rn, fbits, s, "run_sort");
-        k_frun_off<<<grid_for(b.F + 1, 128), 128, 0, s>>>(b.F, Rn, fk.get(), b.frun_off.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
+        {
+            KScope ks("run_index");
+            k_frun_off<<<grid_for(b.F + 1, 128), 128, 0, s>>>(b.F, Rn, fk.get(), b.frun_off.get());
+            COLO_LAUNCH_CHECK();
+            count_launch();
+        }
         b.frun_cell.alloc(Rn, s);
-        k_frun_cell<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.frun.get(), b.rcell.get(), b.frun_cell.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
+        {
+            KScope ks("run_index");
+            k_frun_cell<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.frun.get(), b.rcell.get(), b.frun_cell.get());
+            COLO_LAUNCH_CHECK();
+            count_launch();
+        }
         COLO_CUDA(cudaStreamSynchronize(s));
     }
     b.h_frun_off.resize(b.F + 1);
@@ -540,10 +573,13 @@ void build_neighborhoods(Batch& b) {
     const uint64_t M = b.M;
     DevBuf<uint32_t> nrl_len;
     nrl_len.alloc(M, s);
-    k_nrl_count<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
-                                                  b.crun.get(), nrl_len.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("nrl_count");
+        k_nrl_count<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
+                                                      b.crun.get(), nrl_len.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
     b.nrl_off.alloc(M + 1, s);
     uint64_t tr = 0;
     scan_u32_to_u64(nrl_len.get(), b.nrl_off.get(), M, s, &tr);

@@ -99,108 +99,188 @@ __device__ __forceinline__ bool covers(const uint32_t* __restrict__ qm, const ui
     return ok;
 }
 
-// Level k >= 3.  Items are (driver feature group, driver cell, candidate),
-// candidate fastest: the candidates of a group share a driver feature, so
-// the lanes of a warp read the same cell's quad masks and runs.  For each
-// quad containing the driver cell C (4 masks in qmask[C]):
-//   - it is visited only from its first cell in (ey, ex) order holding the
-//     driver feature (so each quad is seen once per candidate);
-//   - if full, each occupied cell Z of the quad is counted unless an earlier
-//     quad containing Z (in (by, bx) order, qmask[Z][p] for p < q) is full.
-// Counts of one item accumulate in registers; one atomicAdd per member.
+// Level k >= 3.  Items are (driver cell, candidate) pairs taken in run
+// order: a warp owns 32 consecutive (cell, feature) runs -- cell-major, so
+// all warps in flight work on a narrow band of cells whose data stays in L2
+// -- and expands each run whose feature drives G candidates into G items
+// (warp prefix sum; candidates of one driver are adjacent lanes).
+//
+// Phase 1 (a lane per item): the quads containing the driver cell C (masks
+// qmask[C]) that are full for the candidate and are visited from C -- a
+// quad is visited only from its first cell in (ey, ex) order holding the
+// driver feature, so each full quad is seen once per candidate.  Each cell
+// of a visited quad is a task: a 16-bit mask, bit 4*q + e.
+// Phase 2 (the warp): the tasks of the 32 items are spread over the lanes.
+// A task's cell Z is counted unless an earlier quad containing Z (in
+// (by, bx) order: qmask[Z][p] for p below this quad's index in Z's frame)
+// is full; a counted cell adds its runs of the members (located by rank in
+// Z's feature mask) to the item's shared-memory accumulator.
+// Phase 3: one atomicAdd per member per item.
 // stats[c*2] = full quads, stats[c*2+1] = cells in U_c.
 template <int WT>
-__global__ void __launch_bounds__(256, 5) k_filter_level(
-    uint64_t nitems, uint32_t ngrp, const uint64_t* __restrict__ grp_item_off, const uint32_t* __restrict__ grp_fd,
-    const uint32_t* __restrict__ grp_lfd, const uint32_t* __restrict__ grp_cand_off,
-    const uint32_t* __restrict__ grp_cands, uint32_t k, const uint32_t* __restrict__ cand,
-    const uint32_t* __restrict__ need_all, const uint32_t* __restrict__ frun_off,
-    const uint32_t* __restrict__ frun_cell, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
-    const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ crun,
-    const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub,
-    unsigned long long* __restrict__ stats) {
+__global__ void __launch_bounds__(256) k_filter_level(
+    uint64_t Rn, const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcell,
+    const uint32_t* __restrict__ drv_count, const uint32_t* __restrict__ drv_start,
+    const uint32_t* __restrict__ flocal, const uint32_t* __restrict__ order, uint32_t k,
+    const uint32_t* __restrict__ cand, const uint32_t* __restrict__ need_all, const int32_t* __restrict__ nb9,
+    const uint32_t* __restrict__ cmask, const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ crun,
+    const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub, unsigned long long* __restrict__ stats) {
     constexpr uint32_t W = WT;
+    constexpr int kM = kMaxMembersFiltered;
+    __shared__ uint32_t s_need[kFilterWarps][32][WT];
+    __shared__ uint32_t s_lf[kFilterWarps][32][kM];
+    __shared__ uint32_t s_acc[kFilterWarps][32][kM];
+    __shared__ uint32_t s_cells[kFilterWarps][32];
     const uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered;
-    for (uint64_t item = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; item < nitems;
-         item += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = ngrp;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (grp_item_off[mid] <= item) lo = mid;
-            else hi = mid;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint64_t nwarps = (uint64_t)gridDim.x * kFilterWarps;
+    for (uint64_t rbase = ((uint64_t)blockIdx.x * kFilterWarps + wid) * 32; rbase < Rn; rbase += nwarps * 32) {
+        // this warp's 32 runs and the candidates their features drive
+        const uint64_t myr = rbase + lane;
+        uint32_t G = 0, f = 0;
+        if (myr < Rn) {
+            f = rfeat[myr];
+            G = drv_count[f];
         }
-        const uint32_t G = grp_cand_off[lo + 1] - grp_cand_off[lo];
-        const uint64_t r = item - grp_item_off[lo];
-        const uint64_t ci = r / G;
-        const uint32_t c = grp_cands[grp_cand_off[lo] + (uint32_t)(r - ci * G)];
-        const uint32_t fd = grp_fd[lo], lfd = grp_lfd[lo], f0 = fd - lfd;
-        const uint32_t C = frun_cell[frun_off[fd] + ci];
-        uint32_t need[WT];
+        uint32_t rin = G;
 #pragma unroll
-        for (int w = 0; w < WT; ++w) need[w] = need_all[(uint64_t)c * W + w];
-        const uint32_t* q4 = qmask + (uint64_t)C * 4 * W;
-        uint32_t full = 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, rin, o);
+            if (lane >= o) rin += t;
+        }
+        const uint32_t rex = rin - G;
+        const uint32_t ritems = __shfl_sync(0xffffffffu, rin, 31);
+        for (uint32_t i0 = 0; i0 < ritems; i0 += 32) {
+            const uint32_t it = i0 + lane;
+            int j = 0;   // run lane owning item it
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (covers<WT>(q4 + q * W, need)) full |= 1u << q;
-        if (!full) continue;
-        const uint32_t* mem = cand + (uint64_t)c * k;
-        const int32_t* nbc = nb9 + (uint64_t)C * 9;
-        uint32_t acc[kMaxMembersFiltered];
-#pragma unroll
-        for (int j = 0; j < kMaxMembersFiltered; ++j) acc[j] = 0;
-        uint32_t nquads = 0, ncells = 0;
-        for (int q = 0; q < 4; ++q) {
-            if (!(full >> q & 1u)) continue;
-            const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
-            // visit the quad from its first cell (in (ey, ex) order) holding the driver
-            bool first = true;
-            for (int e = 0; e < 4 && first; ++e) {
-                const int ox = qx + (e & 1), oy = qy + (e >> 1);
-                if (ox == 0 && oy == 0) break;
-                const int32_t v = nbc[(oy + 1) * 3 + (ox + 1)];
-                if (v >= 0 && (cmask[(uint64_t)v * W + (lfd >> 5)] >> (lfd & 31) & 1u)) first = false;
+            for (int bstep = 16; bstep > 0; bstep >>= 1) {
+                uint32_t ev = __shfl_sync(0xffffffffu, rex, j + bstep);
+                if (ev <= it) j += bstep;
             }
-            if (!first) continue;
-            ++nquads;
-            for (int e = 0; e < 4; ++e) {
-                const int ex = e & 1, ey = e >> 1;
-                const int32_t Z = nbc[(qy + ey + 1) * 3 + (qx + ex + 1)];
-                if (Z < 0) continue;
+            const uint32_t rex_j = __shfl_sync(0xffffffffu, rex, j);
+            const uint32_t fd = __shfl_sync(0xffffffffu, f, j);
+            const bool valid = it < ritems;
+            uint32_t C = 0, c = 0, tmask = 0, nquads = 0;
+            if (valid) {
+                C = rcell[rbase + j];
+                c = order[drv_start[fd] + (it - rex_j)];
+                const uint32_t lfd = flocal[fd], f0 = fd - lfd;
+                uint32_t need[WT];
+#pragma unroll
+                for (int w = 0; w < WT; ++w) {
+                    need[w] = need_all[(uint64_t)c * W + w];
+                    s_need[wid][lane][w] = need[w];
+                }
+                const uint32_t* q4 = qmask + (uint64_t)C * 4 * W;
+                uint32_t full = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (covers<WT>(q4 + q * W, need)) full |= 1u << q;
+                if (full) {
+                    const int32_t* nbc = nb9 + (uint64_t)C * 9;
+                    int32_t nbv[9];
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) nbv[t] = nbc[t];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (!(full >> q & 1u)) continue;
+                        const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
+                        bool first = true;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int ox = qx + (e & 1), oy = qy + (e >> 1);
+                            if (ox == 0 && oy == 0) break;
+                            const int32_t v = nbv[(oy + 1) * 3 + (ox + 1)];
+                            if (first && v >= 0 && (cmask[(uint64_t)v * W + (lfd >> 5)] >> (lfd & 31) & 1u))
+                                first = false;
+                        }
+                        if (!first) continue;
+                        ++nquads;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (nbv[(qy + (e >> 1) + 1) * 3 + (qx + (e & 1) + 1)] >= 0) tmask |= 1u << (q * 4 + e);
+                    }
+                }
+                const uint32_t* mem = cand + (uint64_t)c * k;
+#pragma unroll
+                for (int jj = 0; jj < kM; ++jj) {
+                    s_lf[wid][lane][jj] = (uint32_t)jj < m ? mem[jj] - f0 : 0u;
+                    s_acc[wid][lane][jj] = 0;
+                }
+            }
+            s_cells[wid][lane] = 0;
+            // warp-wide task list
+            const uint32_t cnt = __popc(tmask);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const uint32_t excl = incl - cnt;
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                const uint32_t t = t0 + lane;
+                int o = 0;   // owner lane: last lane whose range starts at or before t
+#pragma unroll
+                for (int bstep = 16; bstep > 0; bstep >>= 1) {
+                    uint32_t ev = __shfl_sync(0xffffffffu, excl, o + bstep);
+                    if (ev <= t) o += bstep;
+                }
+                const uint32_t ex_o = __shfl_sync(0xffffffffu, excl, o);
+                const uint32_t tm_o = __shfl_sync(0xffffffffu, tmask, o);
+                const uint32_t C_o = __shfl_sync(0xffffffffu, C, o);
+                if (t >= total) continue;
+                // the (t - ex_o)-th set bit of the owner's task mask
+                uint32_t bits = tm_o;
+                for (uint32_t i = t - ex_o; i > 0; --i) bits &= bits - 1;
+                const int tb = __ffs(bits) - 1, q = tb >> 2, e = tb & 3;
+                const int qx = (q & 1) - 1, qy = (q >> 1) - 1, ex = e & 1, ey = e >> 1;
+                const int32_t Z = nb9[(uint64_t)C_o * 9 + (qy + ey + 1) * 3 + (qx + ex + 1)];
+                uint32_t need[WT];
+#pragma unroll
+                for (int w = 0; w < WT; ++w) need[w] = s_need[wid][o][w];
                 // this quad is quad pq of Z; earlier quads of Z are p < pq
                 const int pq = (1 - ey) * 2 + (1 - ex);
-                bool claimed = true;
                 const uint32_t* z4 = qmask + (uint64_t)Z * 4 * W;
+                bool claimed = true;
                 for (int p = 0; p < pq && claimed; ++p)
                     if (covers<WT>(z4 + p * W, need)) claimed = false;
                 if (!claimed) continue;
-                ++ncells;
-                // member j's run in Z: crun[Z] + rank of its bit in Z's feature mask
+                atomicAdd(&s_cells[wid][o], 1u);
                 uint32_t zm[WT];
 #pragma unroll
                 for (int w = 0; w < WT; ++w) zm[w] = cmask[(uint64_t)Z * W + w];
                 const uint32_t q0 = crun[Z];
 #pragma unroll
-                for (int j = 0; j < kMaxMembersFiltered; ++j) {
-                    if ((uint32_t)j < m) {
-                        const uint32_t lf = mem[j] - f0, wq = lf >> 5;
+                for (int jj = 0; jj < kM; ++jj) {
+                    if ((uint32_t)jj < m) {
+                        const uint32_t lf = s_lf[wid][o][jj], wq = lf >> 5;
                         uint32_t rk = 0, word = 0;
 #pragma unroll
                         for (int w = 0; w < WT; ++w) {
                             if ((uint32_t)w < wq) rk += __popc(zm[w]);
                             if ((uint32_t)w == wq) word = zm[w];
                         }
-                        if (word >> (lf & 31) & 1u) acc[j] += rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))];
+                        if (word >> (lf & 31) & 1u)
+                            atomicAdd(&s_acc[wid][o][jj], rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))]);
                     }
                 }
             }
-        }
+            __syncwarp();
+            if (valid && tmask) {
 #pragma unroll
-        for (int j = 0; j < kMaxMembersFiltered; ++j)
-            if ((uint32_t)j < m && acc[j]) atomicAdd(&ub[(uint64_t)c * k + j], acc[j]);
-        if (stats && nquads) {
-            atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nquads);
-            atomicAdd(&stats[(uint64_t)c * 2 + 1], (unsigned long long)ncells);
+                for (int jj = 0; jj < kM; ++jj)
+                    if ((uint32_t)jj < m && s_acc[wid][lane][jj])
+                        atomicAdd(&ub[(uint64_t)c * k + jj], s_acc[wid][lane][jj]);
+                if (stats) {
+                    atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nquads);
+                    atomicAdd(&stats[(uint64_t)c * 2 + 1], (unsigned long long)s_cells[wid][lane]);
+                }
+            }
+            __syncwarp();
         }
     }
 }
@@ -263,52 +343,43 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
         }
         drv[c] = best;
     }
+    // candidates grouped by driver feature: drv_count[f] of them from drv_start[f] in `order`
     std::vector<uint32_t> order(ncand);
     for (uint64_t c = 0; c < ncand; ++c) order[c] = (uint32_t)c;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return drv[a] < drv[c]; });
-    std::vector<uint32_t> gfd, glfd, gcoff;
+    std::vector<uint32_t> dcount(b.F, 0), dstart(b.F, 0), flocal(b.F, 0);
     for (uint64_t i = 0; i < ncand; ++i) {
-        const uint32_t c = order[i], fd = drv[c];
-        if (gfd.empty() || gfd.back() != fd) {
-            gfd.push_back(fd);
-            glfd.push_back(fd - b.jobs[h_job[c]].grid.f0);
-            gcoff.push_back((uint32_t)i);
-        }
+        const uint32_t fd = drv[order[i]];
+        if (dcount[fd]++ == 0) dstart[fd] = (uint32_t)i;
     }
-    gcoff.push_back((uint32_t)ncand);
-    std::vector<uint64_t> goff(1, 0);
-    for (size_t g = 0; g < gfd.size(); ++g)
-        goff.push_back(goff.back() + (uint64_t)(b.h_frun_off[gfd[g] + 1] - b.h_frun_off[gfd[g]]) *
-                                         (gcoff[g + 1] - gcoff[g]));
-    const uint32_t ngrp = (uint32_t)gfd.size();
-    const uint64_t nitems = goff.back();
+    uint64_t nitems = 0;
+    for (uint32_t f = 0; f < b.F; ++f) {
+        flocal[f] = f - b.jobs[b.h_fjob[f]].grid.f0;
+        nitems += (uint64_t)dcount[f] * (b.h_frun_off[f + 1] - b.h_frun_off[f]);
+    }
     b.filter_items += nitems;
     if (nitems == 0) return;
-    DevBuf<uint32_t> dcand, dneed, dgfd, dglfd, dgcoff, dgc;
-    DevBuf<uint64_t> dgoff;
+    DevBuf<uint32_t> dcand, dneed, dcnt, dst, dfl, dord;
     dcand.alloc(ncand * k, s);
     dneed.alloc(need.size(), s);
-    dgfd.alloc(ngrp, s);
-    dglfd.alloc(ngrp, s);
-    dgcoff.alloc(ngrp + 1, s);
-    dgc.alloc(ncand, s);
-    dgoff.alloc(ngrp + 1, s);
+    dcnt.alloc(b.F, s);
+    dst.alloc(b.F, s);
+    dfl.alloc(b.F, s);
+    dord.alloc(ncand, s);
     COLO_CUDA(cudaMemcpyAsync(dcand.get(), h_cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
     COLO_CUDA(cudaMemcpyAsync(dneed.get(), need.data(), need.size() * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dgfd.get(), gfd.data(), ngrp * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dglfd.get(), glfd.data(), ngrp * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dgcoff.get(), gcoff.data(), (ngrp + 1) * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dgc.get(), order.data(), ncand * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dgoff.get(), goff.data(), (ngrp + 1) * 8, cudaMemcpyHostToDevice, s));
-    uint64_t blocks = (nitems + 255) / 256;
+    COLO_CUDA(cudaMemcpyAsync(dcnt.get(), dcount.data(), b.F * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dst.get(), dstart.data(), b.F * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dfl.get(), flocal.data(), b.F * 4, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(dord.get(), order.data(), ncand * 4, cudaMemcpyHostToDevice, s));
+    uint64_t blocks = (b.Rn + 255) / 256;
     uint64_t cap = (uint64_t)b.sms * 16;
     if (blocks > cap) blocks = cap;
     KScope ks("filter_level");
-#define COLO_FL(WW)                                                                                              \
-    k_filter_level<WW><<<(unsigned)blocks, 256, 0, s>>>(                                                         \
-        nitems, ngrp, dgoff.get(), dgfd.get(), dglfd.get(), dgcoff.get(), dgc.get(), k, dcand.get(), dneed.get(), \
-        b.frun_off.get(), b.frun_cell.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(),            \
-        b.rfeat.get(), b.rcnt.get(), d_ub, d_stats)
+#define COLO_FL(WW)                                                                                          \
+    k_filter_level<WW><<<(unsigned)blocks, 256, 0, s>>>(                                                     \
+        b.Rn, b.rfeat.get(), b.rcell.get(), dcnt.get(), dst.get(), dfl.get(), dord.get(), k, dcand.get(),    \
+        dneed.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(), b.rcnt.get(), d_ub, d_stats)
     switch (b.W) {
         case 1: COLO_FL(1); break;
         case 2: COLO_FL(2); break;

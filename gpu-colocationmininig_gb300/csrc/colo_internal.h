@@ -139,6 +139,7 @@ struct KTimer {
     std::vector<KernelStat> stats;
     std::vector<cudaEvent_t> pool;
     int open_slot = -1;
+    int depth = 0;                  // nested scopes: the outermost one is timed
     cudaEvent_t open_a = nullptr;
     cudaEvent_t get() {
         if (!pool.empty()) {
@@ -157,13 +158,13 @@ struct KTimer {
         return (int)stats.size() - 1;
     }
     void begin(const char* name) {
-        if (!on) return;
+        if (!on || depth++ > 0) return;
         open_slot = slot(name);
         open_a = get();
         COLO_CUDA(cudaEventRecord(open_a, s));
     }
     void end() {
-        if (!on || open_slot < 0) return;
+        if (!on || --depth > 0 || open_slot < 0) return;
         cudaEvent_t b = get();
         COLO_CUDA(cudaEventRecord(b, s));
         pend.push_back({open_slot, open_a, b});
@@ -204,6 +205,8 @@ struct KScope {
 // Primitives (colo_prims.cu)
 // ---------------------------------------------------------------------------
 
+// Sum of n values (synchronises to read it back).
+uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s);
 // out[i] = sum(in[0..i)) ; returns total (synchronises to read it back if total_host != nullptr).
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host);

@@ -51,7 +51,7 @@ template <int T, int MODE>
 __global__ void __launch_bounds__(256) k_join(
     uint64_t A, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
     const uint32_t* __restrict__ sid, const uint32_t* __restrict__ scell, const uint32_t* __restrict__ sfeat,
-    const float* __restrict__ sx, const float* __restrict__ sy, const uint32_t* __restrict__ rstart,
+    const float2* __restrict__ sxy, const uint32_t* __restrict__ rstart,
     const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_L,
     const uint64_t* __restrict__ cap_off, const uint64_t* __restrict__ nrl_off,
     const uint32_t* __restrict__ nrl_run, const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids,
@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) k_join(
     const uint32_t p = act_pos[i];
     const uint32_t r = act_run[i];
     const uint32_t a = sid[p];
-    const float xa = sx[p], ya = sy[p];
+    const float2 pa = sxy[p];
+    const float xa = pa.x, ya = pa.y;
     const JobGrid& g = grids[fjob[sfeat[p]]];
     const float R2 = g.R2, hu = g.R2hu;
     const uint64_t qend = nrl_off[scell[p] + 1];
@@ -79,7 +80,10 @@ __global__ void __launch_bounds__(256) k_join(
         for (uint32_t b0 = 0; b0 < tc; b0 += T) {
             const uint32_t t = b0 + gl;
             bool ok = false;
-            if (t < tc) ok = ref_within(xa, ya, sx[ts + t], sy[ts + t], R2, hu);
+            if (t < tc) {
+                const float2 pb = sxy[ts + t];
+                ok = ref_within(xa, ya, pb.x, pb.y, R2, hu);
+            }
             const uint32_t bal = (__ballot_sync(gmask, ok) >> gbase) & ((T == 32) ? 0xffffffffu : ((1u << T) - 1u));
             if (MODE != J_COUNT && ok) nb[base + k + __popc(bal & ((1u << gl) - 1u))] = sid[ts + t];
             k += __popc(bal);
@@ -100,7 +104,7 @@ void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uin
     KScope ks(mode == J_SINGLE ? "join" : mode == J_COUNT ? "join_count" : "join_fill");
 #define COLO_JOIN(MD)                                                                                        \
     k_join<T, MD><<<grid, 256, 0, b.s>>>(A, act_pos, act_run, b.sid.get(), b.scell.get(), b.sfeat.get(),     \
-                                         b.sx.get(), b.sy.get(), b.rstart.get(), b.rcnt.get(), b.run_sfx.get(), \
+                                         b.sxy.get(), b.rstart.get(), b.rcnt.get(), b.run_sfx.get(),            \
                                          b.run_L.get(), cap_off, b.nrl_off.get(), b.nrl_run.get(),          \
                                          b.fjob.get(), b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get())
     if (mode == J_SINGLE) COLO_JOIN(J_SINGLE);
@@ -150,9 +154,12 @@ void join_neighbors(Batch& b) {
     cap.alloc(Rn, s);
     act_off.alloc(Rn, s);
     cap_off.alloc(Rn, s);
-    k_run_caps<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rcnt.get(), b.run_L.get(), act.get(), cap.get());
-    COLO_LAUNCH_CHECK();
-    count_launch();
+    {
+        KScope ks("join_setup");
+        k_run_caps<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rcnt.get(), b.run_L.get(), act.get(), cap.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
     uint32_t A = 0;
     scan_u32_to_u32(act.get(), act_off.get(), Rn, s, &A);
     // upper bound of the single-pass layout = pair evaluations
@@ -164,6 +171,7 @@ void join_neighbors(Batch& b) {
     act_pos.alloc(A, s);
     act_run.alloc(A, s);
     if (A) {
+        KScope ks("join_setup");
         k_expand_active<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rstart.get(), b.rcnt.get(), b.run_L.get(),
                                                           act_off.get(), act_pos.get(), act_run.get());
         COLO_LAUNCH_CHECK();
@@ -186,12 +194,8 @@ void join_neighbors(Batch& b) {
         b.nb.alloc(E ? E : 1, s);
         dispatch_join(b, J_FILL, A, act_pos.get(), act_run.get(), nullptr);
     }
-    // total entries (statistics)
-    DevBuf<uint64_t> tmp;
-    tmp.alloc(b.N ? b.N : 1, s);
-    uint64_t E = 0;
-    if (b.N) scan_u32_to_u64(b.nb_cnt.get(), tmp.get(), b.N, s, &E);
-    b.E = E;
+    // total entries
+    b.E = b.join_single ? sum_u32(b.nb_cnt.get(), b.N, s) : b.nb_cap;
 }
 
 void eval_sqdist(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) k_level(
     const CandDesc* __restrict__ cands, const uint64_t* __restrict__ chunk_off, uint64_t ncand,
     uint64_t nchunks, const uint64_t* __restrict__ nb_beg, const uint32_t* __restrict__ nb_cnt,
     const uint32_t* __restrict__ nb,
-    const float* __restrict__ x, const float* __restrict__ y, const uint32_t* __restrict__ fstart,
+    const float2* __restrict__ xy, const uint32_t* __restrict__ fstart,
     const uint32_t* __restrict__ fcount, const JobGrid* __restrict__ grids,
     uint32_t* __restrict__ overflow, unsigned long long* __restrict__ items) {
     constexpr int KR = (K == 0) ? 1 : K;   // register members kept for K > 0
@@ -83,8 +83,9 @@ __global__ void __launch_bounds__(256) k_level(
 #pragma unroll
             for (int i = 1; i < KR - 1; ++i) {
                 rid[i] = d.parent[(uint64_t)i * d.pstride + row];
-                rx[i] = x[rid[i]];
-                ry[i] = y[rid[i]];
+                const float2 pi = xy[rid[i]];
+                rx[i] = pi.x;
+                ry[i] = pi.y;
             }
         }
         uint64_t o0 = nb_beg[a0], o1 = o0 + nb_cnt[a0];
@@ -126,18 +127,21 @@ __global__ void __launch_bounds__(256) k_level(
         if (active) b = nb[lo_j + (item - ex_j)];
         if (K == 0) {
             if (active && k > 2) {
-                const float xb = x[b], yb = y[b];
+                const float2 pb = xy[b];
+                const float xb = pb.x, yb = pb.y;
                 const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
                 for (uint32_t i = 1; i + 1 < k && ok; ++i) {
                     uint32_t ri = d.parent[(uint64_t)i * d.pstride + prow_j];
-                    ok = ref_within(x[ri], y[ri], xb, yb, R2, hu);
+                    const float2 pr = xy[ri];
+                    ok = ref_within(pr.x, pr.y, xb, yb, R2, hu);
                 }
             }
         } else if (K > 2) {
             float xb = 0.f, yb = 0.f;
             if (active) {
-                xb = x[b];
-                yb = y[b];
+                const float2 pb = xy[b];
+                xb = pb.x;
+                yb = pb.y;
             }
 #pragma unroll
             for (int i = 1; i < KR - 1; ++i) {
@@ -292,7 +296,7 @@ void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
     unsigned grid = (unsigned)((threads + 255) / 256);
 #define COLO_LVL(KK)                                                                              \
     k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_beg.get(), b.nb_cnt.get(), \
-                                            b.nb.get(), b.x, b.y, b.fstart.get(), b.fcount.get(),  \
+                                            b.nb.get(), b.xy.get(), b.fstart.get(), b.fcount.get(),  \
                                             b.grids.get(), ovf, w.items)
     switch (k) {
         case 2: COLO_LVL(2); break;

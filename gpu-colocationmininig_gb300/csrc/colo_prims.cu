@@ -105,8 +105,25 @@ __global__ void k_scan_tiles(const Tin* __restrict__ in, Tout* __restrict__ out,
     }
 }
 
+__global__ void k_sum_u32(const uint32_t* __restrict__ in, uint64_t n, unsigned long long* __restrict__ out) {
+    unsigned long long v = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        v += in[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __shared__ unsigned long long ws[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) ws[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v) atomicAdd(out, v);
+    }
+}
+
 template <class Tin, class Tout>
 void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total_host) {
+    KScope ks("scan");
     uint64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles == 0) tiles = 1;
     DevBuf<Tout> partial;
@@ -214,6 +231,24 @@ __global__ void k_radix_scatter(const KT* __restrict__ kin, const uint32_t* __re
 }
 
 }  // namespace
+
+uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
+    KScope ks("sum");
+    DevBuf<unsigned long long> acc;
+    acc.alloc(1, s);
+    acc.zero(s);
+    if (n) {
+        uint64_t blocks = (n + 255) / 256;
+        if (blocks > 2048) blocks = 2048;
+        k_sum_u32<<<(unsigned)blocks, 256, 0, s>>>(in, n, acc.get());
+        COLO_LAUNCH_CHECK();
+        count_launch();
+    }
+    unsigned long long h = 0;
+    COLO_CUDA(cudaMemcpyAsync(&h, acc.get(), 8, cudaMemcpyDeviceToHost, s));
+    COLO_CUDA(cudaStreamSynchronize(s));
+    return h;
+}
 
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host) {

@@ -85,8 +85,9 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
 // Level-k upper bounds for host candidates cand[c*k + j] (global features) of
 // jobs job[c]: d_ub[c*k + j] (zeroed by the caller).  d_stats (optional,
 // zeroed, 2 per candidate): full quads and cells of U_c.
+// d_cand (optional): the same candidates already on the device.
 void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint64_t ncand, uint32_t k,
-                  uint32_t* d_ub, unsigned long long* d_stats);
+                  uint32_t* d_ub, unsigned long long* d_stats, const uint32_t* d_cand = nullptr);
 
 // colo_level.cu --------------------------------------------------------------
 // One candidate's view for the level kernels.

@@ -321,7 +321,7 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
 }
 
 void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint64_t ncand, uint32_t k,
-                  uint32_t* d_ub, unsigned long long* d_stats) {
+                  uint32_t* d_ub, unsigned long long* d_stats, const uint32_t* d_cand_in) {
     if (ncand == 0) return;
     if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 256 features per job"};
     cudaStream_t s = b.s;
@@ -360,13 +360,14 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     b.filter_items += nitems;
     if (nitems == 0) return;
     DevBuf<uint32_t> dcand, dneed, dcnt, dst, dfl, dord;
-    dcand.alloc(ncand * k, s);
+    if (!d_cand_in) dcand.alloc(ncand * k, s);
+    const uint32_t* d_cand = d_cand_in ? d_cand_in : dcand.get();
     dneed.alloc(need.size(), s);
     dcnt.alloc(b.F, s);
     dst.alloc(b.F, s);
     dfl.alloc(b.F, s);
     dord.alloc(ncand, s);
-    COLO_CUDA(cudaMemcpyAsync(dcand.get(), h_cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
+    if (!d_cand_in) COLO_CUDA(cudaMemcpyAsync(dcand.get(), h_cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
     COLO_CUDA(cudaMemcpyAsync(dneed.get(), need.data(), need.size() * 4, cudaMemcpyHostToDevice, s));
     COLO_CUDA(cudaMemcpyAsync(dcnt.get(), dcount.data(), b.F * 4, cudaMemcpyHostToDevice, s));
     COLO_CUDA(cudaMemcpyAsync(dst.get(), dstart.data(), b.F * 4, cudaMemcpyHostToDevice, s));
@@ -378,7 +379,7 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     KScope ks("filter_level");
 #define COLO_FL(WW)                                                                                          \
     k_filter_level<WW><<<(unsigned)blocks, 256, 0, s>>>(                                                     \
-        b.Rn, b.rfeat.get(), b.rcell.get(), dcnt.get(), dst.get(), dfl.get(), dord.get(), k, dcand.get(),    \
+        b.Rn, b.rfeat.get(), b.rcell.get(), dcnt.get(), dst.get(), dfl.get(), dord.get(), k, d_cand,          \
         dneed.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(), b.rcnt.get(), d_ub, d_stats)
     switch (b.W) {
         case 1: COLO_FL(1); break;

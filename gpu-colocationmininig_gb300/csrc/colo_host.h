@@ -37,6 +37,7 @@ struct LevelTrace {
     std::vector<uint32_t> argmin;
     std::vector<uint64_t> fquads, fcells;       // filter: full quads, cells of U_c (k >= 3)
     std::vector<float> feat;                    // cost-model features, 24 per candidate
+    std::vector<float> pred;                    // LEARNED: predicted log1p(rows) per candidate
     std::vector<std::vector<uint32_t>> tables;   // row-major, kept on request
     std::vector<uint8_t> has_table;
 };

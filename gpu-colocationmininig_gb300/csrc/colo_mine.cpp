@@ -422,6 +422,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             L.has_table.assign(C, 0);
             tr[j] = &L;
         }
+        const bool learned_mode = mode == COLO_MODE_LEARNED && !ctx->model.empty();
         if (k == 2) {
             DevBuf<uint32_t> ub2;
             std::vector<uint64_t> job_off;
@@ -453,18 +454,57 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
             }
             uint64_t ncand = owner.size();
-            DevBuf<uint32_t> dub;
+            DevBuf<uint32_t> dub, dcand;
             DevBuf<unsigned long long> dfs;
             dub.alloc(ncand * k, s);
             dub.zero(s);
             dfs.alloc(ncand * 2, s);
             dfs.zero(s);
-            filter_level(b, hc.data(), hjob.data(), ncand, k, dub.get(), dfs.get());
+            dcand.alloc(ncand * k, s);
+            COLO_CUDA(cudaMemcpyAsync(dcand.get(), hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
+            filter_level(b, hc.data(), hjob.data(), ncand, k, dub.get(), dfs.get(), dcand.get());
+            // cost-model features and predictions on the device, read back with the bounds
+            bool rec_all = false;
+            for (uint32_t j = 0; j < J; ++j) rec_all |= tr[j] && (pv[j].reserved[0] & 2) != 0;
+            const bool infer = learned_mode && ncand > 0;
+            std::vector<float> hX, hY;
+            DevBuf<float> dX, dY, dparams;
+            DevBuf<uint64_t> dprow;
+            if ((rec_all || infer) && ncand) {
+                std::vector<uint64_t> hprow(ncand, 0);
+                for (uint64_t q = 0; q < ncand; ++q) {
+                    auto it = js[owner[q].first].tables.find(std::vector<uint32_t>(&hc[q * k], &hc[q * k] + k - 1));
+                    hprow[q] = it == js[owner[q].first].tables.end() ? 0 : it->second.rows;
+                }
+                dprow.alloc(ncand, s);
+                dX.alloc(ncand * kMlpIn, s);
+                COLO_CUDA(cudaMemcpyAsync(dprow.get(), hprow.data(), ncand * 8, cudaMemcpyHostToDevice, s));
+                mlp_features(ncand, k, dcand.get(), dub.get(), dfs.get(), b.fcount.get(), dprow.get(), dX.get(), s);
+                if (rec_all) {
+                    hX.resize(ncand * kMlpIn);
+                    COLO_CUDA(cudaMemcpyAsync(hX.data(), dX.get(), hX.size() * 4, cudaMemcpyDeviceToHost, s));
+                }
+                if (infer) {
+                    dparams.alloc(kMlpParams, s);
+                    dY.alloc(ncand, s);
+                    hY.resize(ncand);
+                    COLO_CUDA(cudaMemcpyAsync(dparams.get(), ctx->model.data(), kMlpParams * 4,
+                                              cudaMemcpyHostToDevice, s));
+                    mlp_forward(dparams.get(), dX.get(), ncand, dY.get(), s);
+                    COLO_CUDA(cudaMemcpyAsync(hY.data(), dY.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
+                }
+            }
             std::vector<uint32_t> hub(ncand * k);
             std::vector<uint64_t> hfs(ncand * 2);
             COLO_CUDA(cudaMemcpyAsync(hub.data(), dub.get(), hub.size() * 4, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaMemcpyAsync(hfs.data(), dfs.get(), hfs.size() * 8, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaStreamSynchronize(s));
+            for (uint32_t j = 0; j < J; ++j) {
+                if (!tr[j]) continue;
+                const size_t C = tr[j]->cand.size() / k;
+                if ((pv[j].reserved[0] & 2) != 0) tr[j]->feat.assign(C * kMlpIn, 0.f);
+                if (infer) tr[j]->pred.assign(C, 0.f);
+            }
             for (uint64_t q = 0; q < ncand; ++q) {
                 LevelTrace& L = *tr[owner[q].first];
                 size_t c = owner[q].second;
@@ -473,6 +513,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 cnt_fcm += hfs[2 * q + 1] * std::min<uint32_t>(k, kMaxMembersFiltered);
                 cnt_fquads += hfs[2 * q];
                 cnt_fcells += hfs[2 * q + 1];
+                if (!L.feat.empty()) std::memcpy(&L.feat[c * kMlpIn], &hX[q * kMlpIn], kMlpIn * sizeof(float));
+                if (infer) L.pred[c] = hY[q];
             }
             for (uint64_t q = 0; q < ncand; ++q) {
                 LevelTrace& L = *tr[owner[q].first];
@@ -481,27 +523,45 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 L.pass[c] = filter_pass(&L.ub[c * k], &L.cand[c * k], k, b.h_fcount, js[owner[q].first].thr);
             }
         }
-        // cost-model features: of every candidate when the caller records them
-        // (reserved[0] bit 1, training data), else of the candidates a LEARNED
-        // mine refines
-        const bool learned_mode = mode == COLO_MODE_LEARNED && !ctx->model.empty();
-        for (uint32_t j = 0; j < J; ++j) {
-            if (!tr[j]) continue;
-            const bool all = (pv[j].reserved[0] & 2) != 0;
-            if (!all && !learned_mode) continue;
-            LevelTrace& L = *tr[j];
-            const size_t C = L.cand.size() / k;
-            L.feat.assign(C * kMlpIn, 0.f);
-            for (size_t c = 0; c < C; ++c) {
-                if (!all && !L.pass[c]) continue;
-                const uint32_t* mem = &L.cand[c * k];
-                uint64_t prow = b.h_fcount[mem[0]];
-                if (k > 2) {
-                    auto it = js[j].tables.find(std::vector<uint32_t>(mem, mem + k - 1));
-                    prow = it == js[j].tables.end() ? 0 : it->second.rows;
+        // pairs: cost-model features on the host (every candidate when the caller
+        // records them, reserved[0] bit 1; else the ones a LEARNED mine refines)
+        // and, for LEARNED, one inference launch
+        if (k == 2) {
+            std::vector<float> X;
+            std::vector<std::pair<uint32_t, size_t>> who;
+            for (uint32_t j = 0; j < J; ++j) {
+                if (!tr[j]) continue;
+                const bool all = (pv[j].reserved[0] & 2) != 0;
+                if (!all && !learned_mode) continue;
+                LevelTrace& L = *tr[j];
+                const size_t C = L.cand.size() / k;
+                L.feat.assign(C * kMlpIn, 0.f);
+                for (size_t c = 0; c < C; ++c) {
+                    if (!all && !L.pass[c]) continue;
+                    const uint32_t* mem = &L.cand[c * k];
+                    candidate_features(k, mem, b.h_fcount.data(), &L.ub[c * k], b.h_fcount[mem[0]], 0, 0,
+                                       &L.feat[c * kMlpIn]);
+                    if (learned_mode && L.pass[c]) {
+                        X.insert(X.end(), &L.feat[c * kMlpIn], &L.feat[c * kMlpIn] + kMlpIn);
+                        who.push_back({j, c});
+                    }
                 }
-                candidate_features(k, mem, b.h_fcount.data(), &L.ub[c * k], prow, L.fquads[c], L.fcells[c],
-                                   &L.feat[c * kMlpIn]);
+                if (!all) L.feat.clear();   // kept only when the caller records them
+            }
+            if (!who.empty()) {
+                DevBuf<float> dparams, dx, dy;
+                std::vector<float> y(who.size());
+                dparams.alloc(kMlpParams, s);
+                dx.alloc(X.size(), s);
+                dy.alloc(who.size(), s);
+                COLO_CUDA(cudaMemcpyAsync(dparams.get(), ctx->model.data(), kMlpParams * 4, cudaMemcpyHostToDevice, s));
+                COLO_CUDA(cudaMemcpyAsync(dx.get(), X.data(), X.size() * 4, cudaMemcpyHostToDevice, s));
+                mlp_forward(dparams.get(), dx.get(), who.size(), dy.get(), s);
+                COLO_CUDA(cudaMemcpyAsync(y.data(), dy.get(), y.size() * 4, cudaMemcpyDeviceToHost, s));
+                COLO_CUDA(cudaStreamSynchronize(s));
+                for (uint32_t j = 0; j < J; ++j)
+                    if (tr[j]) tr[j]->pred.assign(tr[j]->cand.size() / k, 0.f);
+                for (size_t i = 0; i < who.size(); ++i) tr[who[i].first]->pred[who[i].second] = y[i];
             }
         }
         t_filter += ms_since(t0);
@@ -551,20 +611,11 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         bool learned = mode == COLO_MODE_LEARNED && !ctx->model.empty() && ncand > 0;
         std::vector<uint64_t> cap, pc;
         if (learned) {
-            std::vector<float> X(ncand * kMlpIn), y(ncand);
+            std::vector<float> y(ncand);
             for (uint64_t q = 0; q < ncand; ++q) {
                 const LevelTrace& L = *tr[owner[q].first];
-                std::memcpy(&X[q * kMlpIn], &L.feat[owner[q].second * kMlpIn], kMlpIn * sizeof(float));
+                y[q] = L.pred.empty() ? 0.f : L.pred[owner[q].second];
             }
-            DevBuf<float> dparams, dx, dy;
-            dparams.alloc(kMlpParams, s);
-            dx.alloc(X.size(), s);
-            dy.alloc(ncand, s);
-            COLO_CUDA(cudaMemcpyAsync(dparams.get(), ctx->model.data(), kMlpParams * 4, cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(dx.get(), X.data(), X.size() * 4, cudaMemcpyHostToDevice, s));
-            mlp_forward(dparams.get(), dx.get(), ncand, dy.get(), s);
-            COLO_CUDA(cudaMemcpyAsync(y.data(), dy.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
-            COLO_CUDA(cudaStreamSynchronize(s));
             // a row extends a parent row by one last-member instance: rows <= prow * n_last
             pc.resize(ncand);
             uint64_t words = 0;
@@ -654,20 +705,22 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                                               cudaMemcpyDeviceToHost, s));
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
-            } else if (learned) {
-                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr, d_items.get()};
-                level_single(b, w, k, ar.overflow.get());
-                level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
-                COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
-                COLO_CUDA(cudaStreamSynchronize(s));
             } else {
                 LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr, d_items.get()};
-                level_count(b, w, k, true);
+                if (learned) level_single(b, w, k, ar.overflow.get());
+                else level_count(b, w, k, true);
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
                 COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
-                COLO_CUDA(cudaStreamSynchronize(s));
             }
         }
+        // row counts, overflow flags and the work counter, with the statistics: one wait
+        std::vector<uint64_t> hrows(ncand);
+        std::vector<uint32_t> hovf(ncand, 0);
+        unsigned long long h_items = 0;
+        if (ncand) COLO_CUDA(cudaMemcpyAsync(hrows.data(), ar.rows.get(), ncand * 8, cudaMemcpyDeviceToHost, s));
+        if (learned) COLO_CUDA(cudaMemcpyAsync(hovf.data(), ar.overflow.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaMemcpyAsync(&h_items, d_items.get(), 8, cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaStreamSynchronize(s));
         // participation index (getParticipationIndex, Codes/DeviceProcess.cu:108-132)
         std::vector<uint8_t> prev_flag(ncand, 0);
         for (uint64_t q = 0; q < ncand; ++q) {
@@ -698,20 +751,11 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             prev_flag[q] = L.prevalent[c];
         }
         // row counts (per-candidate counters of the count pass) and fill offsets
-        std::vector<uint64_t> hrows(ncand);
-        std::vector<uint32_t> hovf(ncand, 0);
-        if (ncand)
-            COLO_CUDA(cudaMemcpy(hrows.data(), ar.rows.get(), ncand * 8, cudaMemcpyDeviceToHost));
         if (learned) {
-            COLO_CUDA(cudaMemcpy(hovf.data(), ar.overflow.get(), ncand * 4, cudaMemcpyDeviceToHost));
             cnt_single += ncand;
             for (uint64_t q = 0; q < ncand; ++q) cnt_single_ovf += hovf[q] ? 1 : 0;
         }
-        {
-            unsigned long long it = 0;
-            COLO_CUDA(cudaMemcpy(&it, d_items.get(), 8, cudaMemcpyDeviceToHost));
-            cnt_items += it;
-        }
+        cnt_items += h_items;
         cnt_d2h += ncand * 8 + hstats.size() * 8;
         std::vector<uint64_t> gb(ncand + 1, 0);
         for (uint64_t q = 0; q < ncand; ++q) gb[q + 1] = gb[q] + hrows[q];

@@ -359,7 +359,50 @@ __global__ void k_zero_pad_rows(float* P) {
         if (i < H) P[OFF_W1 + r * H + i] = 0.f;
 }
 
+// Cost-model features of level-k candidates (the layout colo_result_features
+// documents), from the filter's bounds and quad statistics on the device.
+__global__ void k_features(uint64_t ncand, uint32_t k, const uint32_t* __restrict__ cand,
+                           const uint32_t* __restrict__ ub, const unsigned long long* __restrict__ fstats,
+                           const uint32_t* __restrict__ fcount, const uint64_t* __restrict__ prow,
+                           float* __restrict__ X) {
+    const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncand) return;
+    const uint32_t* mem = cand + c * k;
+    const uint32_t m = k < 8 ? k : 8;
+    float x[IN];
+    for (int i = 0; i < IN; ++i) x[i] = 0.f;
+    x[0] = (float)k / 8.0f;
+    float minn = INFINITY, minub = INFINITY;
+    for (uint32_t j = 0; j < k; ++j) minn = fminf(minn, (float)fcount[mem[j]]);
+    for (uint32_t j = 0; j < m; ++j) {
+        const float u = (float)ub[c * k + j];
+        x[1 + j] = log1pf((float)fcount[mem[j]]);
+        x[9 + j] = log1pf(u);
+        minub = fminf(minub, u);
+    }
+    const float lnl = log1pf((float)fcount[mem[k - 1]]), lpr = log1pf((float)prow[c]);
+    x[17] = lpr;
+    x[18] = log1pf(fstats ? (float)fstats[c * 2 + 1] : 0.f);
+    x[19] = log1pf(fstats ? (float)fstats[c * 2] : 0.f);
+    x[20] = log1pf(minn);
+    x[21] = log1pf(minub);
+    x[22] = lpr - lnl;
+    x[23] = k <= 8 ? log1pf((float)ub[c * k + k - 1]) - lnl : 0.f;
+    for (int i = 0; i < IN; ++i) X[c * IN + i] = x[i];
+}
+
 }  // namespace
+
+void mlp_features(uint64_t ncand, uint32_t k, const uint32_t* d_cand, const uint32_t* d_ub,
+                  const unsigned long long* d_fstats, const uint32_t* d_fcount, const uint64_t* d_prow, float* d_x,
+                  cudaStream_t s) {
+    if (ncand == 0) return;
+    KScope ks("mlp_features");
+    k_features<<<(unsigned)((ncand + 127) / 128), 128, 0, s>>>(ncand, k, d_cand, d_ub, d_fstats, d_fcount, d_prow,
+                                                               d_x);
+    COLO_LAUNCH_CHECK();
+    count_launch();
+}
 
 void mlp_forward(const float* d_params, const float* d_x, uint64_t n, float* d_y, cudaStream_t s) {
     if (n == 0) return;

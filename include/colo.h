@@ -221,8 +221,10 @@ colo_status colo_ctx_set_model(colo_ctx* ctx, const float* params);
  * log1p(full quads), [20] log1p(min n_j), [21] log1p(min ub_j), [22]
  * log1p(parent rows) - log1p(n_last), [23] log1p(ub_last) - log1p(n_last).
  * Quad statistics are 0 for pairs.  Recorded for every candidate when the
- * mine's colo_params.reserved[0] has bit 1 set (training data), else only
- * for the candidates a COLO_MODE_LEARNED mine refines (zeros elsewhere). */
+ * mine's colo_params.reserved[0] has bit 1 set (training data); zeros
+ * otherwise.  (A COLO_MODE_LEARNED mine computes them for its predictions
+ * without keeping them: on the device right after the level filter for
+ * k >= 3, on the host for pairs.) */
 colo_status colo_result_features(const colo_result* r, uint32_t li, float* x);
 
 /* ---- allocation-free entry point -------------------------------------- */

@@ -106,18 +106,24 @@ def evaluate(ctx: Context, params: np.ndarray, x: np.ndarray, t: np.ndarray) -> 
     return {"model": errors(y, t), "heuristic": errors(heuristic_log_rows(x), t), "samples": int(len(t))}
 
 
-def train(ctx: Context, x: np.ndarray, t: np.ndarray, epochs: int = 40, batch: int = 2048, lr: float = 2e-3,
-          seed: int = 0):
-    p0 = init_model(seed)
-    p0[-1] = float(np.mean(t))        # start the output bias at the mean target
-    return ctx.model_train(p0, x, t, epochs, batch, lr, seed)
+SCHEDULE = ((40, 2e-3), (30, 5e-4), (30, 1e-4))   # (epochs, learning rate) phases, Adam restarted per phase
+
+
+def train(ctx: Context, x: np.ndarray, t: np.ndarray, schedule=SCHEDULE, batch: int = 2048, seed: int = 0):
+    """GPU training in phases of decreasing learning rate; returns (parameters, per-epoch loss)."""
+    p = init_model(seed)
+    p[-1] = float(np.mean(t))        # start the output bias at the mean target
+    hist = []
+    for i, (epochs, lr) in enumerate(schedule):
+        p, h = ctx.model_train(p, x, t, epochs, batch, lr, seed + i)
+        hist.extend(h.tolist())
+    return p, np.array(hist, np.float32)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["train"])
     ap.add_argument("--out", required=True)
-    ap.add_argument("--epochs", type=int, default=40)
     args = ap.parse_args()
     ctx = Context(0)
     t0 = time.time()
@@ -125,7 +131,7 @@ def main():
     t_collect = time.time() - t0
     xh, th, kh = collect(ctx, HELDOUT_SEEDS)
     t0 = time.time()
-    params, hist = train(ctx, x, t, args.epochs)
+    params, hist = train(ctx, x, t)
     t_train = time.time() - t0
     ev = evaluate(ctx, params, xh, th)
     ev_train = evaluate(ctx, params, x, t)

@@ -51,43 +51,69 @@ __global__ void k_gather_sorted(uint64_t n, uint32_t F, const uint32_t* __restri
     sfeat[p] = lo;
 }
 
+// Cell and run heads in the sorted order, counted and compacted in two
+// passes over the keys (no flag arrays): per 2048-point tile the number of
+// cell heads (high 32 bits) and run heads (low 32 bits), then the same
+// flags exclusive-scanned within the tile plus the tile's base.
+constexpr int kHeadThreads = 256, kHeadItems = 8, kHeadTile = kHeadThreads * kHeadItems;
+
 template <class KT>
-__global__ void k_heads(uint64_t n, const KT* __restrict__ keys,
-                        const uint32_t* __restrict__ sfeat, uint32_t* __restrict__ cell_head,
-                        uint32_t* __restrict__ run_head) {
-    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    bool ch = (p == 0) || keys[p] != keys[p - 1];
-    bool rh = ch || sfeat[p] != sfeat[p - 1];
-    cell_head[p] = ch;
-    run_head[p] = rh;
+__device__ __forceinline__ uint64_t head_flags(uint64_t p, uint64_t n, const KT* __restrict__ keys,
+                                               const uint32_t* __restrict__ sfeat) {
+    if (p >= n) return 0;
+    const bool ch = p == 0 || keys[p - 1] != keys[p];
+    const bool rh = ch || sfeat[p - 1] != sfeat[p];
+    return ((uint64_t)ch << 32) | (uint64_t)rh;
 }
 
 template <class KT>
-__global__ void k_compact(uint64_t n, const KT* __restrict__ keys,
-                          const uint32_t* __restrict__ sfeat, const uint32_t* __restrict__ fjob,
-                          const uint32_t* __restrict__ cell_head, const uint32_t* __restrict__ run_head,
-                          const uint32_t* __restrict__ cell_ex, const uint32_t* __restrict__ run_ex,
-                          uint64_t* __restrict__ ckey, uint32_t* __restrict__ cstart,
-                          uint32_t* __restrict__ crun, uint32_t* __restrict__ cjob,
-                          uint32_t* __restrict__ rfeat, uint32_t* __restrict__ rstart,
-                          uint32_t* __restrict__ rcell, uint32_t* __restrict__ scell) {
-    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    uint32_t ch = cell_head[p], rh = run_head[p];
-    uint32_t c = cell_ex[p] + ch - 1;
-    scell[p] = c;
-    if (ch) {
-        ckey[c] = keys[p];
-        cstart[c] = (uint32_t)p;
-        crun[c] = run_ex[p];
-        cjob[c] = fjob[sfeat[p]];
+__global__ void __launch_bounds__(kHeadThreads) k_head_tiles(uint64_t n, const KT* __restrict__ keys,
+                                                            const uint32_t* __restrict__ sfeat,
+                                                            uint64_t* __restrict__ partial) {
+    const uint64_t base = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)threadIdx.x * kHeadItems;
+    uint64_t v = 0;
+#pragma unroll
+    for (int i = 0; i < kHeadItems; ++i) v += head_flags(base + i, n, keys, sfeat);
+    uint64_t tot;
+    block_excl_scan<uint64_t>(v, &tot);
+    if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+template <class KT>
+__global__ void __launch_bounds__(kHeadThreads) k_head_compact(
+    uint64_t n, const KT* __restrict__ keys, const uint32_t* __restrict__ sfeat, const uint32_t* __restrict__ fjob,
+    const uint64_t* __restrict__ partial, uint64_t* __restrict__ ckey, uint32_t* __restrict__ cstart,
+    uint32_t* __restrict__ crun, uint32_t* __restrict__ cjob, uint32_t* __restrict__ rfeat,
+    uint32_t* __restrict__ rstart, uint32_t* __restrict__ rcell, uint32_t* __restrict__ scell) {
+    const uint64_t base = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)threadIdx.x * kHeadItems;
+    uint64_t fl[kHeadItems];
+    uint64_t v = 0;
+#pragma unroll
+    for (int i = 0; i < kHeadItems; ++i) {
+        fl[i] = head_flags(base + i, n, keys, sfeat);
+        v += fl[i];
     }
-    if (rh) {
-        uint32_t r = run_ex[p];
-        rfeat[r] = sfeat[p];
-        rstart[r] = (uint32_t)p;
-        rcell[r] = c;
+    uint64_t tot;
+    uint64_t ex = block_excl_scan<uint64_t>(v, &tot) + partial[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < kHeadItems; ++i) {
+        const uint64_t p = base + i;
+        if (p >= n) break;
+        const uint32_t ch = (uint32_t)(fl[i] >> 32), rh = (uint32_t)fl[i];
+        const uint32_t c = (uint32_t)(ex >> 32) + ch - 1, r = (uint32_t)ex;
+        scell[p] = c;
+        if (ch) {
+            ckey[c] = keys[p];
+            cstart[c] = (uint32_t)p;
+            crun[c] = r;
+            cjob[c] = fjob[sfeat[p]];
+        }
+        if (rh) {
+            rfeat[r] = sfeat[p];
+            rstart[r] = (uint32_t)p;
+            rcell[r] = c;
+        }
+        ex += fl[i];
     }
 }
 
@@ -450,20 +476,18 @@ void sort_and_compact(Batch& b) {
         count_launch();
     }
 
-    DevBuf<uint32_t> ch, rh, cex, rex;
-    ch.alloc(n, s);
-    rh.alloc(n, s);
-    cex.alloc(n, s);
-    rex.alloc(n, s);
+    const uint64_t tiles = (n + kHeadTile - 1) / kHeadTile;
+    DevBuf<uint64_t> part;
+    part.alloc(tiles + 1, s);
+    uint64_t totals = 0;
     {
         KScope ks("cell_compact");
-        k_heads<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), ch.get(), rh.get());
+        k_head_tiles<KT><<<(unsigned)tiles, kHeadThreads, 0, s>>>(n, keys.get(), b.sfeat.get(), part.get());
         COLO_LAUNCH_CHECK();
         count_launch();
+        scan_partials_u64(part.get(), tiles, s, &totals);
     }
-    uint32_t M = 0, Rn = 0;
-    scan_u32_to_u32(ch.get(), cex.get(), n, s, &M);
-    scan_u32_to_u32(rh.get(), rex.get(), n, s, &Rn);
+    const uint32_t M = (uint32_t)(totals >> 32), Rn = (uint32_t)totals;
     b.M = M;
     b.Rn = Rn;
     b.ckey.alloc(M, s);
@@ -477,11 +501,9 @@ void sort_and_compact(Batch& b) {
     b.scell.alloc(n, s);
     {
         KScope ks("cell_compact");
-        k_compact<KT><<<grid_for(n, 256), 256, 0, s>>>(n, keys.get(), b.sfeat.get(), b.fjob.get(), ch.get(),
-                                                    rh.get(), cex.get(), rex.get(), b.ckey.get(),
-                                                    b.cstart.get(), b.crun.get(), b.cjob.get(),
-                                                    b.rfeat.get(), b.rstart.get(), b.rcell.get(),
-                                                    b.scell.get());
+        k_head_compact<KT><<<(unsigned)tiles, kHeadThreads, 0, s>>>(
+            n, keys.get(), b.sfeat.get(), b.fjob.get(), part.get(), b.ckey.get(), b.cstart.get(), b.crun.get(),
+            b.cjob.get(), b.rfeat.get(), b.rstart.get(), b.rcell.get(), b.scell.get());
         COLO_LAUNCH_CHECK();
         count_launch();
     }

@@ -85,4 +85,39 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return (1u << (threadIdx.x & 31)) - 1u;
 }
 
+// Warp and block scans (one value per thread).
+template <class T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Exclusive block scan of one value per thread; returns the exclusive prefix
+// and writes the block total to *total.
+template <class T>
+__device__ __forceinline__ T block_excl_scan(T v, T* total) {
+    __shared__ T warp_tot[33];   // [32] holds the block total
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    T inc = warp_incl_scan(v);
+    if (lane == 31) warp_tot[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        T w = lane < nw ? warp_tot[lane] : T(0);
+        T wi = warp_incl_scan(w);
+        if (lane < nw) warp_tot[lane] = wi - w;
+        if (lane == nw - 1) warp_tot[32] = wi;
+    }
+    __syncthreads();
+    T res = inc - v + warp_tot[wid];
+    *total = warp_tot[32];
+    __syncthreads();
+    return res;
+}
+
 }  // namespace colo

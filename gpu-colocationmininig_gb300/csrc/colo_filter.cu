@@ -173,15 +173,16 @@ __global__ void __launch_bounds__(256) k_filter_level(
                     s_need[wid][lane][w] = need[w];
                 }
                 const uint32_t* q4 = qmask + (uint64_t)C * 4 * W;
+                // the neighbour table is loaded with the quad masks (independent loads in flight together)
+                const int32_t* nbc = nb9 + (uint64_t)C * 9;
+                int32_t nbv[9];
+#pragma unroll
+                for (int t = 0; t < 9; ++t) nbv[t] = nbc[t];
                 uint32_t full = 0;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (covers<WT>(q4 + q * W, need)) full |= 1u << q;
                 if (full) {
-                    const int32_t* nbc = nb9 + (uint64_t)C * 9;
-                    int32_t nbv[9];
-#pragma unroll
-                    for (int t = 0; t < 9; ++t) nbv[t] = nbc[t];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         if (!(full >> q & 1u)) continue;
@@ -245,15 +246,17 @@ __global__ void __launch_bounds__(256) k_filter_level(
                 // this quad is quad pq of Z; earlier quads of Z are p < pq
                 const int pq = (1 - ey) * 2 + (1 - ex);
                 const uint32_t* z4 = qmask + (uint64_t)Z * 4 * W;
-                bool claimed = true;
-                for (int p = 0; p < pq && claimed; ++p)
-                    if (covers<WT>(z4 + p * W, need)) claimed = false;
-                if (!claimed) continue;
-                atomicAdd(&s_cells[wid][o], 1u);
+                // Z's feature mask and first run are loaded with its quad masks
                 uint32_t zm[WT];
 #pragma unroll
                 for (int w = 0; w < WT; ++w) zm[w] = cmask[(uint64_t)Z * W + w];
                 const uint32_t q0 = crun[Z];
+                bool claimed = true;
+#pragma unroll
+                for (int p = 0; p < 3; ++p)
+                    if (p < pq && covers<WT>(z4 + p * W, need)) claimed = false;
+                if (!claimed) continue;
+                atomicAdd(&s_cells[wid][o], 1u);
 #pragma unroll
                 for (int jj = 0; jj < kM; ++jj) {
                     if ((uint32_t)jj < m) {

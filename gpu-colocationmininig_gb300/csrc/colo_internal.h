@@ -205,6 +205,9 @@ struct KScope {
 // Primitives (colo_prims.cu)
 // ---------------------------------------------------------------------------
 
+// In place: exclusive scan of partial[0..m), partial[m] = total (read back
+// when total_host != nullptr).
+void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* total_host);
 // Sum of n values (synchronises to read it back).
 uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s);
 // out[i] = sum(in[0..i)) ; returns total (synchronises to read it back if total_host != nullptr).

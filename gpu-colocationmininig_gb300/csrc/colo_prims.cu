@@ -1,6 +1,7 @@
 // colo_prims.cu -- device-wide scan and a stable LSD radix sort (hand-written,
 // no library).  The reference uses thrust::exclusive_scan / sort_by_key
 // (Codes/DeviceProcess.cu:342-344); these are their replacements.
+#include "colo_device.cuh"
 #include "colo_internal.h"
 
 namespace colo {
@@ -13,40 +14,6 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
-
-template <class T>
-__device__ __forceinline__ T warp_incl_scan(T v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        T t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += t;
-    }
-    return v;
-}
-
-// Exclusive block scan of one value per thread; returns the exclusive prefix
-// and writes the block total to *total.
-template <class T>
-__device__ __forceinline__ T block_excl_scan(T v, T* total) {
-    __shared__ T warp_tot[33];   // [32] holds the block total
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nw = blockDim.x >> 5;
-    T inc = warp_incl_scan(v);
-    if (lane == 31) warp_tot[wid] = inc;
-    __syncthreads();
-    if (wid == 0) {
-        T w = lane < nw ? warp_tot[lane] : T(0);
-        T wi = warp_incl_scan(w);
-        if (lane < nw) warp_tot[lane] = wi - w;
-        if (lane == nw - 1) warp_tot[32] = wi;
-    }
-    __syncthreads();
-    T res = inc - v + warp_tot[wid];
-    *total = warp_tot[32];
-    __syncthreads();
-    return res;
-}
 
 template <class Tin, class Tout>
 __global__ void k_tile_sums(const Tin* __restrict__ in, uint64_t n, Tout* __restrict__ partial) {
@@ -231,6 +198,16 @@ __global__ void k_radix_scatter(const KT* __restrict__ kin, const uint32_t* __re
 }
 
 }  // namespace
+
+void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* total_host) {
+    k_scan_partials<uint64_t><<<1, 1024, 0, s>>>(partial, m);
+    COLO_LAUNCH_CHECK();
+    count_launch();
+    if (total_host) {
+        COLO_CUDA(cudaMemcpyAsync(total_host, partial + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaStreamSynchronize(s));
+    }
+}
 
 uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
     KScope ks("sum");

@@ -183,7 +183,7 @@ def bench_jobs(args, rank, world, local, dist):
     (colo_mine_batch) against the plain form mining the jobs one at a time."""
     import torch
     import colo
-    from colo import gen
+    from colo import gen, replicas
 
     dev = torch.device("cuda", local)
     jobs = gen.config2_jobs(512, scale=args.scale)
@@ -222,17 +222,14 @@ def bench_jobs(args, rank, world, local, dist):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        out[form] = (ms, res)
+        total, ms = replicas.aggregate(dist, sum(r.num_candidates() for r in res) * args.steps, ms, dev)
+        out[form] = (ms, res, total)
     cands = sum(r.num_candidates() for r in out["batched"][1])
     same = all(a.patterns() == b.patterns() for a, b in zip(out["batched"][1], out["plain"][1]))
     if rank == 0:
         ms_b, ms_p = out["batched"][0], out["plain"][0]
         print(json.dumps({
-            "metric": METRIC, "value": cands * args.steps * world / (ms_b / 1e3), "unit": "candidates/s",
+            "metric": METRIC, "value": out["batched"][2] / (ms_b / 1e3), "unit": "candidates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator)",
@@ -240,7 +237,7 @@ def bench_jobs(args, rank, world, local, dist):
                                    "R = 3 x mean spacing x U[0.5, 2], PI in {0.1, 0.2, 0.3}",
                        "points": int(sum(w.n for w in jobs)), "jobs": len(jobs), "candidates_per_step": cands,
                        "form": "batched+learned" if mode == colo.MODE_LEARNED else "batched"},
-            "plain": {"value": cands * args.steps * world / (ms_p / 1e3), "unit": "candidates/s",
+            "plain": {"value": out["plain"][2] / (ms_p / 1e3), "unit": "candidates/s",
                       "ms_per_step": ms_p / args.steps},
             "headline_vs_plain": ms_p / ms_b, "identical_patterns_all_forms": same,
         }), flush=True)
@@ -281,6 +278,7 @@ def main():
 
     import torch
     import colo
+    from colo import replicas
 
     dist = None
     if world > 1:
@@ -321,11 +319,9 @@ def main():
             e1.record(stream)
             barrier_sync()
         ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms, results, clk.summary()
+        units = sum(r.num_candidates() for r in results)
+        total, ms = replicas.aggregate(dist, units, ms, dev)   # all ranks' candidates, slowest rank's time
+        return ms, results, clk.summary(), total
 
     forms = set(args.forms.split(","))
     # headline form: batched + learned presizing (the committed trained cost model)
@@ -338,24 +334,24 @@ def main():
     ctx.set_model(model)
     # pick the join's lanes per anchor for this dataset (untimed; kept by the context)
     tuned = ctx.autotune(ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size))
-    ms_b, res_b, clocks = timed(head_mode, True)
+    ms_b, res_b, clocks, tot_b = timed(head_mode, True)
     cands = res_b[0].num_candidates()
-    value = cands * args.steps * world / (ms_b / 1e3)
-    ms_e, res_e, ms_p, res_p = ms_b, res_b, ms_b, res_b
+    value = tot_b / (ms_b / 1e3)
+    ms_e, res_e, ms_p, res_p, tot_e, tot_p = ms_b, res_b, ms_b, res_b, tot_b, tot_b
     if "e2e" in forms:
-        ms_e, res_e, _ = timed(head_mode, False)
-    e2e = cands * args.steps * world / (ms_e / 1e3)
-    ms_bt, res_bt = ms_b, res_b
+        ms_e, res_e, _, tot_e = timed(head_mode, False)
+    e2e = tot_e / (ms_e / 1e3)
+    ms_bt, res_bt, tot_bt = ms_b, res_b, tot_b
     if "batched" in forms and head_mode != colo.MODE_BATCHED:
-        ms_bt, res_bt, _ = timed(colo.MODE_BATCHED, True)
+        ms_bt, res_bt, _, tot_bt = timed(colo.MODE_BATCHED, True)
     if "plain" in forms:
-        ms_p, res_p, _ = timed(colo.MODE_PLAIN, True)
-    plain = cands * args.steps * world / (ms_p / 1e3)
+        ms_p, res_p, _, tot_p = timed(colo.MODE_PLAIN, True)
+    plain = tot_p / (ms_p / 1e3)
     # every form mined the same patterns
     same = all(r.patterns() == res_b[0].patterns() for r in res_b + res_e + res_p + res_bt)
 
     # per-kernel CUDA-event times (a separate profiled pass, so `value` carries no event overhead)
-    ms_k, res_k, _ = timed(head_mode, True, profile=True)
+    ms_k, res_k, _, _ = timed(head_mode, True, profile=True)
     kern = {}
     for r in res_k:
         for name, (nl, kms) in r.kernels.items():
@@ -409,8 +405,13 @@ def main():
                 "h2d_bytes_per_step": int(res_e[0].counters["h2d_bytes"]),
                 "d2h_bytes_per_step": int(res_e[0].counters["d2h_bytes"])},
         "plain": {"value": plain, "unit": "candidates/s", "ms_per_step": ms_p / args.steps},
-        "batched": {"value": cands * args.steps * world / (ms_bt / 1e3), "unit": "candidates/s",
-                    "ms_per_step": ms_bt / args.steps},
+        "batched": {"value": tot_bt / (ms_bt / 1e3), "unit": "candidates/s",
+                    "ms_per_step": ms_bt / args.steps,
+                    "host_phase_ms": {k: round(statistics.mean(r.times[k] for r in res_bt), 3)
+                                      for k in ("bucket", "join", "filter", "refine", "fill", "apriori", "total")},
+                    "level_filter_wait_us": int(res_bt[0].counters["level_filter_wait_us"])},
+        "pairs_model_us": int(res_b[0].counters["pairs_model_us"]),
+        "level_filter_wait_us": int(res_b[0].counters["level_filter_wait_us"]),
         "headline_vs_plain": (ms_p / ms_b),
         "learned_presize": ({"single_pass": int(res_b[0].counters["single_pass"]),
                              "overflow_fallback": int(res_b[0].counters["single_pass_overflow"])}

@@ -28,7 +28,7 @@ MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
 COUNTERS = ["launches", "active_anchors", "neighbors", "rows_written", "join_pairs", "points", "cells", "runs",
             "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
             "nrl_entries", "refined", "filter_items", "single_pass", "single_pass_overflow", "filter_cell_members",
-            "filter_full_quads", "filter_cells", "reserved22", "reserved23"]
+            "filter_full_quads", "filter_cells", "pairs_model_us", "level_filter_wait_us"]
 
 # Every symbol declared in include/colo.h (checked by the CPU tests).
 EXPORTS = [

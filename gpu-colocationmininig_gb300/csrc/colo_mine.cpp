@@ -161,7 +161,8 @@ struct JobState {
     uint32_t max_size = 0;
     bool active = true;
     std::vector<uint32_t> cands;     // this level's candidates (global features)
-    std::unordered_map<std::vector<uint32_t>, TableRef, PatternHash> tables;   // prefixes
+    std::vector<uint32_t> parent;    // per candidate: index of its (k-1)-prefix among the previous level's candidates
+    std::vector<TableRef> prev_tables;   // per previous-level candidate: its instance table (rows 0 if none)
     MineResult* out = nullptr;
 };
 
@@ -170,8 +171,9 @@ struct JobState {
 // (k-1)-subsets must all be prevalent (generateandCheckSubsets, 669-679);
 // a failing subset check ends the inner loop ("break", 541-542) and so does
 // a prefix mismatch (551-552).
-std::vector<uint32_t> apriori_next(const std::vector<uint32_t>& prev, uint32_t km1) {
+std::vector<uint32_t> apriori_next(const std::vector<uint32_t>& prev, uint32_t km1, std::vector<uint32_t>& parent) {
     std::vector<uint32_t> out;
+    parent.clear();
     size_t P = prev.size() / km1;
     if (P < 2) return out;
     std::unordered_set<std::vector<uint32_t>, PatternHash> have;
@@ -202,6 +204,7 @@ std::vector<uint32_t> apriori_next(const std::vector<uint32_t>& prev, uint32_t k
             }
             if (!ok) break;
             out.insert(out.end(), cand.begin(), cand.end());
+            parent.push_back((uint32_t)i);   // its (k-1)-prefix is prev pattern i
         }
     }
     return out;
@@ -347,6 +350,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     } unset;
     uint64_t cnt_items = 0, cnt_parent = 0, cnt_fillw = 0, cnt_bmw = 0, cnt_d2h = 0, cnt_refined = 0, cnt_fcm = 0;
     uint64_t cnt_single = 0, cnt_single_ovf = 0, cnt_fquads = 0, cnt_fcells = 0;
+    uint64_t us_pairs_model = 0, us_level_wait = 0;
     DevBuf<unsigned long long> d_items;
     d_items.alloc(1, s);
     Batch b;
@@ -463,6 +467,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             dcand.alloc(ncand * k, s);
             COLO_CUDA(cudaMemcpyAsync(dcand.get(), hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
             filter_level(b, hc.data(), hjob.data(), ncand, k, dub.get(), dfs.get(), dcand.get());
+            const auto tl0 = Clock::now();
             // cost-model features and predictions on the device, read back with the bounds
             bool rec_all = false;
             for (uint32_t j = 0; j < J; ++j) rec_all |= tr[j] && (pv[j].reserved[0] & 2) != 0;
@@ -473,8 +478,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             if ((rec_all || infer) && ncand) {
                 std::vector<uint64_t> hprow(ncand, 0);
                 for (uint64_t q = 0; q < ncand; ++q) {
-                    auto it = js[owner[q].first].tables.find(std::vector<uint32_t>(&hc[q * k], &hc[q * k] + k - 1));
-                    hprow[q] = it == js[owner[q].first].tables.end() ? 0 : it->second.rows;
+                    const JobState& st = js[owner[q].first];
+                    hprow[q] = st.prev_tables[st.parent[owner[q].second]].rows;
                 }
                 dprow.alloc(ncand, s);
                 dX.alloc(ncand * kMlpIn, s);
@@ -499,6 +504,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             COLO_CUDA(cudaMemcpyAsync(hub.data(), dub.get(), hub.size() * 4, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaMemcpyAsync(hfs.data(), dfs.get(), hfs.size() * 8, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaStreamSynchronize(s));
+            us_level_wait += (uint64_t)(ms_since(tl0) * 1000.0);
             for (uint32_t j = 0; j < J; ++j) {
                 if (!tr[j]) continue;
                 const size_t C = tr[j]->cand.size() / k;
@@ -527,6 +533,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         // records them, reserved[0] bit 1; else the ones a LEARNED mine refines)
         // and, for LEARNED, one inference launch
         if (k == 2) {
+            const auto tm0 = Clock::now();
+            struct AddUs {
+                uint64_t& acc;
+                Clock::time_point t;
+                ~AddUs() { acc += (uint64_t)(ms_since(t) * 1000.0); }
+            } add_us{us_pairs_model, tm0};
             std::vector<float> X;
             std::vector<std::pair<uint32_t, size_t>> who;
             for (uint32_t j = 0; j < J; ++j) {
@@ -584,13 +596,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     d.prow = b.h_fcount[mem[0]];
                     d.pstride = d.prow;
                 } else {
-                    std::vector<uint32_t> pre(mem, mem + k - 1);
-                    auto it = js[j].tables.find(pre);
-                    if (it == js[j].tables.end())
+                    const TableRef& pt = js[j].prev_tables[js[j].parent[c]];
+                    if (!pt.cols && pt.rows)
                         throw StatusError{COLO_ERR_INTERNAL, "missing parent instance table"};
-                    d.parent = it->second.cols;
-                    d.prow = it->second.rows;
-                    d.pstride = it->second.stride;
+                    d.parent = pt.cols;
+                    d.prow = pt.rows;
+                    d.pstride = pt.stride;
                 }
                 for (uint32_t t = 0; t < k; ++t) d.m[t] = mem[t];
                 d.job = j;
@@ -764,19 +775,27 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
 
         // ---- next candidates (Apriori) and the tables they need ----
         t0 = Clock::now();
-        std::vector<std::unordered_set<std::vector<uint32_t>, PatternHash>> needed(J);
+        // needed[j][c]: candidate c of this level is the prefix of a next-level candidate
+        std::vector<std::vector<uint8_t>> needed(J);
         for (uint32_t j = 0; j < J; ++j) {
             if (!tr[j]) continue;
             LevelTrace& L = *tr[j];
-            std::vector<uint32_t> prev;
+            std::vector<uint32_t> prev, prev_c;
             for (size_t c = 0; c < L.cand.size() / k; ++c)
-                if (L.prevalent[c]) prev.insert(prev.end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
-            std::vector<uint32_t> next;
+                if (L.prevalent[c]) {
+                    prev.insert(prev.end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+                    prev_c.push_back((uint32_t)c);
+                }
+            std::vector<uint32_t> next, par;
             bool cap_ok = (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf;
-            if (cap_ok) next = apriori_next(prev, k);
+            if (cap_ok) next = apriori_next(prev, k, par);
             js[j].cands = next;
-            for (size_t c = 0; c < next.size() / (k + 1); ++c)
-                needed[j].emplace(next.begin() + c * (k + 1), next.begin() + c * (k + 1) + k);
+            needed[j].assign(L.cand.size() / k, 0);
+            for (auto& pp : par) {
+                pp = prev_c[pp];        // now an index among this level's candidates
+                needed[j][pp] = 1;
+            }
+            js[j].parent = std::move(par);
         }
         t_apriori += ms_since(t0);
 
@@ -786,10 +805,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         uint64_t total_rows = 0;
         for (uint64_t q = 0; q < ncand; ++q) {
             if (!prev_flag[q]) continue;
-            LevelTrace& L = *tr[owner[q].first];
-            size_t c = owner[q].second;
-            std::vector<uint32_t> pat(L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
-            if (!needed[owner[q].first].count(pat)) continue;
+            if (!needed[owner[q].first][owner[q].second]) continue;
             if (learned && !hovf[q]) {
                 keepq.push_back(q);
                 continue;
@@ -860,7 +876,10 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         COLO_CUDA(cudaStreamSynchronize(s));
         // register the new tables (prefixes of the next level)
-        for (auto& st : js) st.tables.clear();
+        for (uint32_t j = 0; j < J; ++j) {
+            js[j].prev_tables.clear();
+            if (tr[j]) js[j].prev_tables.assign(tr[j]->cand.size() / k, TableRef{});
+        }
         std::vector<std::pair<uint64_t, TableRef>> made;
         for (size_t i = 0; i < fillq.size(); ++i) made.push_back({fillq[i], TableRef{fd[i].out, fd[i].out_rows, fd[i].out_rows}});
         for (uint64_t q : keepq) {
@@ -872,8 +891,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             const TableRef& t = mt.second;
             LevelTrace& L = *tr[owner[q].first];
             size_t c = owner[q].second;
-            std::vector<uint32_t> pat(L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
-            js[owner[q].first].tables[pat] = t;
+            js[owner[q].first].prev_tables[c] = t;
             if (pv[owner[q].first].keep_tables) {
                 uint64_t rows = t.rows;
                 std::vector<uint32_t> colm(rows * k);
@@ -916,6 +934,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->counters[19] = cnt_fcm;
         r->counters[20] = cnt_fquads;
         r->counters[21] = cnt_fcells;
+        r->counters[22] = us_pairs_model;
+        r->counters[23] = us_level_wait;
         r->times[0] = ms_since(t_all);
         r->times[1] = t_upload;
         r->times[2] = t_bucket;

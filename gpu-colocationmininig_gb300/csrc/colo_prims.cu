@@ -197,6 +197,157 @@ __global__ void k_radix_scatter(const KT* __restrict__ kin, const uint32_t* __re
     }
 }
 
+// ---------------------------------------------------------------------------
+// One-sweep LSD radix sort: the digit histograms of every pass from one read
+// of the keys, then one kernel per pass.  A block takes the next tile number
+// from a counter, ranks its keys stably as above, publishes its per-digit
+// counts, and looks back over the preceding tiles' published counts (a tile
+// that has finished its own look-back publishes its inclusive prefix, which
+// ends the walk) to place its keys.  Tiles are numbered in the order blocks
+// start, so a block only waits on tiles of blocks already running.  Every
+// wait is bounded: past the limit the block sets *err, uses what it has and
+// finishes (the host reports COLO_ERR_TIMEOUT).
+// ---------------------------------------------------------------------------
+
+constexpr unsigned long long kFlagA = 1ull << 62;   // tile count published
+constexpr unsigned long long kFlagP = 2ull << 62;   // inclusive prefix published
+constexpr unsigned long long kValMask = (1ull << 62) - 1;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+template <class KT>
+__global__ void k_digit_hist(const KT* __restrict__ keys, uint64_t n, int passes,
+                             unsigned long long* __restrict__ ghist) {
+    __shared__ uint32_t h[8][kRadix];
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const KT k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(uint32_t)(k >> (p * kRadixBits)) & (kRadix - 1)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
+        const uint32_t v = (&h[0][0])[i];
+        if (v) atomicAdd(&ghist[i], (unsigned long long)v);
+    }
+}
+
+// Exclusive scan of each pass's 256 counters in place (one block of 256).
+__global__ void k_digit_scan(unsigned long long* __restrict__ ghist, int passes) {
+    __shared__ unsigned long long sh[kRadix];
+    for (int p = 0; p < passes; ++p) {
+        const unsigned long long v = ghist[p * kRadix + threadIdx.x];
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < kRadix; o <<= 1) {
+            unsigned long long t = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0ull;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        ghist[p * kRadix + threadIdx.x] = sh[threadIdx.x] - v;
+        __syncthreads();
+    }
+}
+
+template <class KT>
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(
+    const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
+    uint64_t n, int shift, const unsigned long long* __restrict__ gofs, unsigned long long* __restrict__ status,
+    uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
+    __shared__ uint32_t wh[kSortWarps][kRadix];
+    __shared__ unsigned long long s_base[kRadix];   // global position of the tile's first key of digit d
+    __shared__ uint32_t s_off[kRadix];              // tile-local position of the first key of digit d
+    __shared__ KT s_key[kSortTile];
+    __shared__ uint32_t s_val[kSortTile];
+    __shared__ uint32_t s_tile;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&wh[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t tile0 = (uint64_t)tile * kSortTile;
+    const uint64_t base = tile0 + (uint64_t)w * (32 * kSortRounds);
+    KT key[kSortRounds];
+    uint32_t val[kSortRounds];
+    uint32_t rank[kSortRounds];
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const uint64_t i = base + (uint64_t)r * 32 + lane;
+        const bool ok = i < n;
+        key[r] = ok ? kin[i] : 0;
+        val[r] = ok ? vin[i] : 0;
+        const uint32_t d = ok ? ((uint32_t)(key[r] >> shift) & (kRadix - 1)) : 0xFFFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if (ok && lane == leader) {
+            old = wh[w][d];
+            wh[w][d] = old + __popc(peers);
+        }
+        old = __shfl_sync(0xffffffffu, old, leader);
+        rank[r] = ok ? old + __popc(peers & lt) : 0xFFFFFFFFu;
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;   // kSortThreads == kRadix: one thread per digit
+        uint32_t cnt = 0;
+        for (int ww = 0; ww < kSortWarps; ++ww) {
+            const uint32_t t = wh[ww][d];
+            wh[ww][d] = cnt;
+            cnt += t;
+        }
+        uint32_t tot;
+        s_off[d] = block_excl_scan<uint32_t>(cnt, &tot);
+        volatile unsigned long long* st = status + (uint64_t)tile * kRadix + d;
+        unsigned long long prefix = 0;
+        if (tile == 0) {
+            *st = kFlagP | cnt;
+        } else {
+            *st = kFlagA | cnt;
+            uint32_t spins = 0;
+            for (int64_t t = (int64_t)tile - 1; t >= 0;) {
+                const unsigned long long v = *(volatile const unsigned long long*)(status + (uint64_t)t * kRadix + d);
+                const unsigned long long flag = v & ~kValMask;
+                if (flag == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(err, 1u);
+                        break;
+                    }
+                    __nanosleep(64);
+                    continue;
+                }
+                prefix += v & kValMask;
+                if (flag == kFlagP) break;
+                --t;
+            }
+            *st = kFlagP | (prefix + cnt);
+        }
+        s_base[d] = gofs[d] + prefix;
+    }
+    __syncthreads();
+    // stage the tile in digit order, then write it out: consecutive threads
+    // write consecutive positions of one digit's range
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        if (rank[r] == 0xFFFFFFFFu) continue;
+        const uint32_t d = (uint32_t)(key[r] >> shift) & (kRadix - 1);
+        const uint32_t lp = s_off[d] + wh[w][d] + rank[r];
+        s_key[lp] = key[r];
+        s_val[lp] = val[r];
+    }
+    __syncthreads();
+    const uint32_t valid = (uint32_t)(n - tile0 < (uint64_t)kSortTile ? n - tile0 : (uint64_t)kSortTile);
+    for (uint32_t i = threadIdx.x; i < valid; i += kSortThreads) {
+        const KT k = s_key[i];
+        const uint32_t d = (uint32_t)(k >> shift) & (kRadix - 1);
+        const uint64_t pos = s_base[d] + (i - s_off[d]);
+        kout[pos] = k;
+        vout[pos] = s_val[i];
+    }
+}
+
 }  // namespace
 
 void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* total_host) {
@@ -248,26 +399,38 @@ template <class KT>
 void radix_sort_impl(KT* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
-    uint32_t nblocks = (uint32_t)((n + kSortTile - 1) / kSortTile);
+    const int passes = (bits + kRadixBits - 1) / kRadixBits;
+    const uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     DevBuf<KT> k2;
-    DevBuf<uint32_t> v2, hist, offs;
+    DevBuf<uint32_t> v2, tickets, err;
+    DevBuf<unsigned long long> ghist, status;
     k2.alloc(n, s);
     v2.alloc(n, s);
-    hist.alloc((uint64_t)kRadix * nblocks, s);
-    offs.alloc((uint64_t)kRadix * nblocks, s);
+    ghist.alloc((uint64_t)passes * kRadix, s);
+    status.alloc((uint64_t)ntiles * kRadix, s);
+    tickets.alloc(passes, s);
+    err.alloc(1, s);
+    ghist.zero(s);
+    tickets.zero(s);
+    err.zero(s);
+    KScope ks(name);
+    {
+        uint64_t blocks = (n + 255) / 256;
+        if (blocks > 1024) blocks = 1024;
+        k_digit_hist<KT><<<(unsigned)blocks, 256, 0, s>>>(keys, n, passes, ghist.get());
+        COLO_LAUNCH_CHECK();
+        k_digit_scan<<<1, kRadix, 0, s>>>(ghist.get(), passes);
+        COLO_LAUNCH_CHECK();
+        count_launch(2);
+    }
     KT* ka = keys;
     uint32_t* va = vals;
     KT* kb = k2.get();
     uint32_t* vb = v2.get();
-    int passes = (bits + kRadixBits - 1) / kRadixBits;
     for (int p = 0; p < passes; ++p) {
-        int shift = p * kRadixBits;
-        KScope ks(name);
-        k_radix_hist<KT><<<nblocks, kSortThreads, 0, s>>>(ka, n, shift, hist.get(), nblocks);
-        COLO_LAUNCH_CHECK();
-        count_launch();
-        scan_u32_to_u32(hist.get(), offs.get(), (uint64_t)kRadix * nblocks, s, nullptr);
-        k_radix_scatter<KT><<<nblocks, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, offs.get(), nblocks);
+        status.zero(s);
+        k_onesweep<KT><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, p * kRadixBits, ghist.get() + p * kRadix,
+                                                       status.get(), tickets.get() + p, err.get());
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);
@@ -277,6 +440,10 @@ void radix_sort_impl(KT* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_
         COLO_CUDA(cudaMemcpyAsync(keys, ka, n * sizeof(KT), cudaMemcpyDeviceToDevice, s));
         COLO_CUDA(cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     }
+    uint32_t herr = 0;
+    COLO_CUDA(cudaMemcpyAsync(&herr, err.get(), 4, cudaMemcpyDeviceToHost, s));
+    COLO_CUDA(cudaStreamSynchronize(s));
+    if (herr) throw StatusError{COLO_ERR_TIMEOUT, "radix sort: a tile waited too long for its predecessors"};
 }
 
 }  // namespace

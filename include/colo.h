@@ -143,7 +143,9 @@ colo_status colo_result_times(const colo_result* r, double* ms8);
  * [17] candidates filled in one presized pass, [18] of those, overflowed and
  * refilled by the two-pass fallback, [19] (cell of U_c, member) run lookups
  * of the level filters, [20] full quads found by the level filters, [21]
- * cells of U_c summed over candidates, [22..23] reserved. */
+ * cells of U_c summed over candidates, [22] microseconds of the pairs'
+ * cost-model step on the host, [23] microseconds from the level filters'
+ * launches to their readback. */
 colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n);
 /* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set). */
 uint32_t colo_result_num_kernels(const colo_result* r);

@@ -132,7 +132,8 @@ int colo_gen_points(const colo_gen_spec* sp, float* x, float* y, int32_t* fid, f
     }
     // ---- hotspots (each belongs to one feature, chosen by size) ----
     struct Hot { double cx, cy, sig; };
-    std::vector<std::vector<Hot>> hot(F), dense(F);
+    std::vector<std::vector<Hot>> hot(F);
+    std::vector<Hot> dense;   // shared by all features: every feature sends dense_frac of its points there
     auto pick_feature = [&]() {
         uint64_t r = rng.below(N);
         for (uint32_t f = 0; f < F; ++f) {
@@ -147,10 +148,7 @@ int colo_gen_points(const colo_gen_spec* sp, float* x, float* y, int32_t* fid, f
         double lo = std::log(sp->hot_sig_lo), hi = std::log(sp->hot_sig_hi);
         hot[f].push_back({rng.u01() * W, rng.u01() * W, std::exp(lo + rng.u01() * (hi - lo))});
     }
-    for (uint32_t h = 0; h < sp->ndense; ++h) {
-        uint32_t f = pick_feature();
-        dense[f].push_back({rng.u01() * W, rng.u01() * W, sp->dense_sigma});
-    }
+    for (uint32_t h = 0; h < sp->ndense; ++h) dense.push_back({rng.u01() * W, rng.u01() * W, sp->dense_sigma});
     auto clampw = [&](double v) {
         if (v < 0) v = 0;
         if (v >= W) v = std::nextafter(W, 0.0);
@@ -183,10 +181,10 @@ int colo_gen_points(const colo_gen_spec* sp, float* x, float* y, int32_t* fid, f
         }
     for (uint32_t f = 0; f < F; ++f) {
         uint64_t left = start[f + 1] - cur[f];
-        uint64_t nd = dense[f].empty() ? 0 : (uint64_t)std::floor(sp->dense_frac * (double)cnt[f]);
+        uint64_t nd = dense.empty() ? 0 : (uint64_t)std::floor(sp->dense_frac * (double)cnt[f]);
         if (nd > left) nd = left;
         for (uint64_t t = 0; t < nd; ++t) {
-            const Hot& h = dense[f][rng.below(dense[f].size())];
+            const Hot& h = dense[rng.below(dense.size())];
             uint64_t i = cur[f]++;
             place(h.cx, h.cy, h.sig, &x[i], &y[i]);
         }

@@ -35,7 +35,7 @@ EXPORTS = [
     "colo_status_string", "colo_create", "colo_destroy", "colo_last_error", "colo_params_default",
     "colo_read_params", "colo_read_config", "colo_dataset_from_csv", "colo_dataset_from_host",
     "colo_dataset_write_csv", "colo_dataset_upload", "colo_dataset_evict", "colo_dataset_num_points",
-    "colo_dataset_num_features", "colo_dataset_feature_name", "colo_dataset_free", "colo_mine",
+    "colo_dataset_num_features", "colo_dataset_feature_name", "colo_dataset_feature_count", "colo_dataset_free", "colo_mine",
     "colo_mine_batch", "colo_result_num_levels", "colo_result_level_size", "colo_result_level_candidates",
     "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
@@ -101,6 +101,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_dataset_num_points": (C.c_uint64, [_P]),
         "colo_dataset_num_features": (C.c_uint32, [_P]),
         "colo_dataset_feature_name": (C.c_char_p, [_P, C.c_uint32]),
+        "colo_dataset_feature_count": (C.c_uint64, [_P, C.c_uint32]),
         "colo_dataset_free": (None, [_P]),
         "colo_mine": (C.c_int, [_P, _P, C.POINTER(Params), C.POINTER(_P)]),
         "colo_mine_batch": (C.c_int, [_P, C.POINTER(_P), C.POINTER(Params), C.c_uint32, C.POINTER(_P)]),

@@ -29,7 +29,8 @@ struct Batch {
     uint64_t key_bits = 1;
     // host copies of small arrays
     std::vector<JobHost> jobs;
-    std::vector<uint32_t> h_fstart, h_fcount, h_fjob, h_frun_off;
+    std::vector<uint32_t> h_fstart, h_fcount, h_fjob;
+    std::vector<uint32_t> h_frun_off;   // prefix of the number of runs (occupied cells) per feature
     // points (by id)
     const float* x = nullptr;    // borrowed (dataset device copy)
     const float* y = nullptr;
@@ -50,7 +51,6 @@ struct Batch {
     DevBuf<uint32_t> qmask;      // per cell: masks of the 4 quads containing it ([M][4][W])
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
-    DevBuf<uint32_t> frun_off, frun, frun_cell;   // runs in feature order and their cells
     // neighbourhood run lists: for cell c, the runs of its adjacent cells
     // ordered by (feature, cell): nrl_feat/nrl_run[nrl_off[c] .. nrl_off[c+1])
     DevBuf<uint64_t> nrl_off;
@@ -74,7 +74,7 @@ struct Batch {
 };
 
 // colo_bucket.cu
-void bucket_points(Batch& b);            // cells, runs, masks, nb9, frun
+void bucket_points(Batch& b);            // cells, runs, masks, nb9, runs per feature
 void build_neighborhoods(Batch& b);      // NRL / NPL
 // colo_join.cu
 void join_neighbors(Batch& b);           // neighbour CSR

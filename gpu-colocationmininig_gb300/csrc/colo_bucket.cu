@@ -208,27 +208,23 @@ __global__ void k_quad_masks(uint64_t M, uint32_t W, const uint64_t* __restrict_
     }
 }
 
-__global__ void k_frun_keys(uint64_t Rn, const uint32_t* __restrict__ rfeat, uint64_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals) {
-    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= Rn) return;
-    keys[r] = rfeat[r];
-    vals[r] = (uint32_t)r;
-}
+// Runs per feature: a block-local histogram (F <= kHistMax), else global atomics.
+constexpr uint32_t kHistMax = 12288;
 
-// frun_cell[i] = cell of the i-th run in feature order
-__global__ void k_frun_cell(uint64_t Rn, const uint32_t* __restrict__ frun, const uint32_t* __restrict__ rcell,
-                            uint32_t* __restrict__ frun_cell) {
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < Rn) frun_cell[i] = rcell[frun[i]];
-}
-
-// frun_off[f] = first position of feature f in the feature-sorted run list
-__global__ void k_frun_off(uint32_t F, uint64_t Rn, const uint64_t* __restrict__ keys,
-                           uint32_t* __restrict__ frun_off) {
-    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f > F) return;
-    frun_off[f] = (uint32_t)lower_bound_dev(keys, (uint64_t)0, Rn, (uint64_t)f);
+__global__ void k_feature_runs(uint64_t Rn, uint32_t F, const uint32_t* __restrict__ rfeat, uint32_t* __restrict__ cnt) {
+    extern __shared__ uint32_t h[];
+    const bool local = F <= kHistMax;
+    if (local)
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < Rn; r += (uint64_t)gridDim.x * blockDim.x) {
+        if (local) atomicAdd(&h[rfeat[r]], 1u);
+        else atomicAdd(&cnt[rfeat[r]], 1u);
+    }
+    __syncthreads();
+    if (local)
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
+            if (h[i]) atomicAdd(&cnt[i], h[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -549,39 +545,27 @@ void bucket_points(Batch& b) {
         count_launch();
     }
 
-    // feature-major run index: runs sorted by feature (stable, cell order kept)
+    // runs per feature (the level filters drive each candidate from its member with the fewest cells)
     {
-        DevBuf<uint64_t> fk;
-        fk.alloc(Rn, s);
-        b.frun.alloc(Rn, s);
-        b.frun_off.alloc(b.F + 1, s);
-        {
-            KScope ks("run_index");
-            k_frun_keys<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), fk.get(), b.frun.get());
+        KScope ks("run_index");
+        DevBuf<uint32_t> cnt;
+        cnt.alloc(b.F ? b.F : 1, s);
+        cnt.zero(s);
+        const uint64_t blocks = std::min<uint64_t>((Rn + 255) / 256, (uint64_t)b.sms * 4);
+        const size_t smem = b.F <= kHistMax ? (size_t)b.F * 4 : 0;
+        if (smem > 48 * 1024)
+            COLO_CUDA(cudaFuncSetAttribute(k_feature_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (Rn) {
+            k_feature_runs<<<(unsigned)(blocks ? blocks : 1), 256, smem, s>>>(Rn, b.F, b.rfeat.get(), cnt.get());
             COLO_LAUNCH_CHECK();
             count_launch();
         }
-        int fbits = 1;
-        while (fbits < 32 && (1ull << fbits) < b.F) fbits++;
-        radix_sort_u64_u32(fk.get(), b.frun.get(), Rn, fbits, s, "run_sort");
-        {
-            KScope ks("run_index");
-            k_frun_off<<<grid_for(b.F + 1, 128), 128, 0, s>>>(b.F, Rn, fk.get(), b.frun_off.get());
-            COLO_LAUNCH_CHECK();
-            count_launch();
-        }
-        b.frun_cell.alloc(Rn, s);
-        {
-            KScope ks("run_index");
-            k_frun_cell<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.frun.get(), b.rcell.get(), b.frun_cell.get());
-            COLO_LAUNCH_CHECK();
-            count_launch();
-        }
+        std::vector<uint32_t> hc(b.F);
+        if (b.F) COLO_CUDA(cudaMemcpyAsync(hc.data(), cnt.get(), b.F * 4, cudaMemcpyDeviceToHost, s));
         COLO_CUDA(cudaStreamSynchronize(s));
+        b.h_frun_off.assign(b.F + 1, 0);
+        for (uint32_t f = 0; f < b.F; ++f) b.h_frun_off[f + 1] = b.h_frun_off[f] + hc[f];
     }
-    b.h_frun_off.resize(b.F + 1);
-    COLO_CUDA(cudaMemcpyAsync(b.h_frun_off.data(), b.frun_off.get(), (b.F + 1) * 4,
-                              cudaMemcpyDeviceToHost, s));
     DevFlags hf;
     COLO_CUDA(cudaMemcpyAsync(&hf, b.flags.get(), sizeof(hf), cudaMemcpyDeviceToHost, s));
     COLO_CUDA(cudaStreamSynchronize(s));

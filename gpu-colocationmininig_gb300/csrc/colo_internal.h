@@ -2,15 +2,17 @@
 //
 // Device layout of one mining batch (one or more independent jobs):
 //   points      x[N], y[N] f32, feat[N] u32 (global feature index; features of
-//               a job are contiguous and a job's points are contiguous)
+//               a job are contiguous and a job's points are contiguous); xy[N]
+//               packed coordinates by id
 //   features    fstart[F], fcount[F], fjob[F]
 //   jobs        JobGrid[J] (the reference grid of each job, R^2, threshold)
-//   bucketed    points sorted by (job cell key, point id): sid/sx/sy/sfeat/scell
+//   bucketed    points sorted by (job cell key, point id): sid/sxy/sfeat/scell
 //   cells       occupied cells ckey[M], cstart[M+1] (sorted positions),
 //               crun[M+1] (run ranges), nb9[M*9] (geometric 3x3 neighbours),
-//               cmask[M*W] (feature bit masks, local feature index)
-//   runs        (cell, feature) runs rfeat/rstart/rcnt/rcell[Rn], feature-major
-//               index frun_off[F+1]/frun[Rn]
+//               cmask[M*W] (feature bit masks, local feature index),
+//               qmask[M*4*W] (masks of the 4 quads containing the cell)
+//   runs        (cell, feature) runs rfeat/rstart/rcnt/rcell[Rn], cell-major;
+//               runs per feature on the host (h_frun_off prefix)
 //   NRL         per cell, the runs of its adjacent cells ordered by
 //               (feature, cell): nrl_off[M+1], nrl_feat, nrl_run; per run the
 //               start of its higher-feature suffix run_sfx and its size run_L

@@ -813,10 +813,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             fillq.push_back(q);
             total_rows += gb[q + 1] - gb[q];
         }
-        if (learned) {
-            rows_written += gb[ncand];
-            cnt_fillw += single_words;
-        }
+        if (learned)   // rows the single pass wrote (tables that fit their presize)
+            for (uint64_t q = 0; q < ncand; ++q)
+                if (!hovf[q]) {
+                    rows_written += gb[q + 1] - gb[q];
+                    cnt_fillw += (gb[q + 1] - gb[q]) * k;
+                }
         tables_cur.reset(new DevBuf<uint32_t>());
         tables_cur->alloc(total_rows * k ? total_rows * k : 1, s);
         // output offsets of every parent row: exclusive scan of the slots
@@ -1094,6 +1096,11 @@ colo_status colo_dataset_evict(colo_dataset* ds) {
 
 uint64_t colo_dataset_num_points(const colo_dataset* ds) { return ds ? ds->hp.x.size() : 0; }
 uint32_t colo_dataset_num_features(const colo_dataset* ds) { return ds ? (uint32_t)ds->names.size() : 0; }
+uint64_t colo_dataset_feature_count(const colo_dataset* ds, uint32_t f) {
+    if (!ds || f >= ds->fcount.size()) return 0;
+    return ds->fcount[f];
+}
+
 const char* colo_dataset_feature_name(const colo_dataset* ds, uint32_t f) {
     return (ds && f < ds->names.size()) ? ds->names[f].c_str() : nullptr;
 }

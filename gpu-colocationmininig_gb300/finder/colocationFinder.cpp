@@ -150,7 +150,7 @@ int colocationFinder::Begin(Integer argc, char** argv) {
                 out << "\t" << rows[c] << "\t";
                 for (uint32_t j = 0; j < k; ++j) out << (j ? "," : "") << num[c * k + j];
                 out << "\t";
-                for (uint32_t j = 0; j < k; ++j) out << (j ? "," : "") << "n" << j;
+                for (uint32_t j = 0; j < k; ++j) out << (j ? "," : "") << colo_dataset_feature_count(ds_, cand[c * k + j]);
                 char buf[64];
                 std::snprintf(buf, sizeof buf, "\t%.9g\n", (double)pi[c]);
                 out << buf;

@@ -95,6 +95,8 @@ colo_status colo_dataset_upload(colo_dataset* ds);
 colo_status colo_dataset_evict(colo_dataset* ds);
 uint64_t colo_dataset_num_points(const colo_dataset* ds);
 uint32_t colo_dataset_num_features(const colo_dataset* ds);
+/* Number of instances of feature f (0 if f is out of range). */
+uint64_t colo_dataset_feature_count(const colo_dataset* ds, uint32_t f);
 /* Name (as written in the CSV) of feature f. */
 const char* colo_dataset_feature_name(const colo_dataset* ds, uint32_t f);
 void colo_dataset_free(colo_dataset* ds);

@@ -24,6 +24,7 @@ OK = 0
 STATUS = {0: "COLO_OK", 1: "COLO_ERR_ARG", 2: "COLO_ERR_IO", 3: "COLO_ERR_PARSE", 4: "COLO_ERR_INPUT",
           5: "COLO_ERR_CUDA", 6: "COLO_ERR_NOMEM", 7: "COLO_ERR_TIMEOUT", 8: "COLO_ERR_CAPACITY",
           9: "COLO_ERR_NO_DEVICE", 10: "COLO_ERR_INTERNAL"}
+ERR_ARG, ERR_IO, ERR_PARSE, ERR_INPUT, ERR_CAPACITY = 1, 2, 3, 4, 8
 MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
 COUNTERS = ["launches", "active_anchors", "neighbors", "rows_written", "join_pairs", "points", "cells", "runs",
             "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
@@ -41,7 +42,8 @@ EXPORTS = [
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
     "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
-    "colo_ctx_set_model", "colo_result_features", "colo_autotune",
+    "colo_ctx_set_model", "colo_result_features", "colo_autotune", "colo_dataset_from_csv_threads",
+    "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary",
 ]
 MODEL_FEATURES = 24
 MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -96,6 +98,10 @@ def load(build: bool = True) -> C.CDLL:
         "colo_dataset_from_csv": (C.c_int, [_P, C.c_char_p, C.POINTER(_P)]),
         "colo_dataset_from_host": (C.c_int, [_P, _f32p, _f32p, _i32p, C.c_uint64, _f32p, C.POINTER(_P)]),
         "colo_dataset_write_csv": (C.c_int, [_P, C.c_char_p]),
+        "colo_dataset_from_csv_threads": (C.c_int, [_P, C.c_char_p, C.c_uint32, C.POINTER(_P)]),
+        "colo_dataset_write_binary": (C.c_int, [_P, C.c_char_p]),
+        "colo_dataset_from_binary": (C.c_int, [_P, C.c_char_p, C.POINTER(_P)]),
+        "colo_csv_to_binary": (C.c_int, [C.c_char_p, C.c_char_p, C.c_uint32, C.c_char_p, C.c_size_t]),
         "colo_dataset_upload": (C.c_int, [_P]),
         "colo_dataset_evict": (C.c_int, [_P]),
         "colo_dataset_num_points": (C.c_uint64, [_P]),
@@ -172,6 +178,38 @@ def read_config(path: str) -> List[str]:
     if st != OK:
         raise ColoError(st, str(path))
     return [b.value.decode() for b in bufs]
+
+
+def csv_to_binary(csv_path: str, bin_path: str, threads: int = 0) -> None:
+    """Parse a CSV dataset on the host (`threads` parser threads, 0: automatic) and write it as a
+    binary point file.  Needs no GPU."""
+    err = C.create_string_buffer(512)
+    st = load().colo_csv_to_binary(str(csv_path).encode(), str(bin_path).encode(), threads, err, len(err))
+    if st:
+        raise ColoError(st, err.value.decode(errors="replace"))
+
+
+BINARY_MAGIC = b"COLOPTS1"
+
+
+def read_binary(path: str):
+    """(x, y, raw_id, names, bounds) of a binary point file, read with numpy (no library call)."""
+    buf = np.fromfile(path, np.uint8)
+    if len(buf) < 64 or bytes(buf[:8]) != BINARY_MAGIC:
+        raise ValueError(f"{path}: not a binary point file")
+    ver, hb = np.frombuffer(buf[8:16], np.uint32)
+    n, nf, nb = (int(v) for v in np.frombuffer(buf[16:40], np.uint64))
+    bounds = np.frombuffer(buf[40:56], np.float32).copy()
+    if ver != 1 or hb != 64 or len(buf) != 64 + 12 * n + 4 * nf + nb:
+        raise ValueError(f"{path}: bad header")
+    x = np.frombuffer(buf[64:64 + 4 * n], np.float32).copy()
+    y = np.frombuffer(buf[64 + 4 * n:64 + 8 * n], np.float32).copy()
+    raw = np.frombuffer(buf[64 + 8 * n:64 + 12 * n], np.int32).copy()
+    lens = np.frombuffer(buf[64 + 12 * n:64 + 12 * n + 4 * nf], np.uint32)
+    text = bytes(buf[64 + 12 * n + 4 * nf:])
+    ends = np.cumsum(lens)
+    names = [text[e - ln:e].decode(errors="surrogateescape") for e, ln in zip(ends.tolist(), lens.tolist())]
+    return x, y, raw, names, bounds
 
 
 @dataclass
@@ -431,10 +469,22 @@ class Dataset:
         self.nfeat = int(ctx.lib.colo_dataset_num_features(handle))
 
     @classmethod
-    def from_csv(cls, ctx: Context, path: str) -> "Dataset":
+    def from_csv(cls, ctx: Context, path: str, threads: int = 0) -> "Dataset":
+        """populateData's CSV, parsed by `threads` threads (0: automatic)."""
         h = _P()
-        ctx.check(ctx.lib.colo_dataset_from_csv(ctx.h, str(path).encode(), C.byref(h)), "dataset_from_csv")
+        ctx.check(ctx.lib.colo_dataset_from_csv_threads(ctx.h, str(path).encode(), threads, C.byref(h)),
+                  "dataset_from_csv")
         return cls(ctx, h)
+
+    @classmethod
+    def from_binary(cls, ctx: Context, path: str) -> "Dataset":
+        """A binary point file written by write_binary or csv_to_binary."""
+        h = _P()
+        ctx.check(ctx.lib.colo_dataset_from_binary(ctx.h, str(path).encode(), C.byref(h)), "dataset_from_binary")
+        return cls(ctx, h)
+
+    def write_binary(self, path: str):
+        self.ctx.check(self.ctx.lib.colo_dataset_write_binary(self.h, str(path).encode()), "dataset_write_binary")
 
     @classmethod
     def from_arrays(cls, ctx: Context, x, y, fid, bounds) -> "Dataset":

@@ -81,7 +81,8 @@ void join_neighbors(Batch& b);           // neighbour CSR
 // colo_filter.cu
 // Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
 // bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.
-void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_off);
+// Runs on stream s (no wait at the end).
+void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_off, cudaStream_t s);
 // Level-k upper bounds for host candidates cand[c*k + j] (global features) of
 // jobs job[c]: d_ub[c*k + j] (zeroed by the caller).  d_stats (optional,
 // zeroed, 2 per candidate): full quads and cells of U_c.

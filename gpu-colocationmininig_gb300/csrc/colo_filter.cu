@@ -290,8 +290,7 @@ __global__ void __launch_bounds__(256) k_filter_level(
 
 }  // namespace
 
-void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_off) {
-    cudaStream_t s = b.s;
+void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_off, cudaStream_t s) {
     job_off.assign(b.J + 1, 0);
     for (uint32_t j = 0; j < b.J; ++j)
         job_off[j + 1] = job_off[j] + (uint64_t)b.jobs[j].grid.nf * b.jobs[j].grid.nf;
@@ -310,7 +309,11 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     }
     if (smem > 48 * 1024)
         COLO_CUDA(cudaFuncSetAttribute(k_filter_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    uint64_t blocks = (uint64_t)b.sms * (smem > 100 * 1024 ? 1 : 2);
+    // as many resident blocks per SM as the accumulator allows (at most 8)
+    uint64_t per_sm = smem ? (200 * 1024) / smem : 8;
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 8) per_sm = 8;
+    uint64_t blocks = (uint64_t)b.sms * per_sm;
     uint64_t per = (b.Rn + blocks - 1) / blocks;
     per = (per + kFilterThreads - 1) / kFilterThreads * kFilterThreads;
     blocks = (b.Rn + per - 1) / per;
@@ -320,7 +323,6 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
         b.rcnt.get(), d_job_off.get(), ub2.get(), acc_dim, per);
     COLO_LAUNCH_CHECK();
     count_launch();
-    COLO_CUDA(cudaStreamSynchronize(s));
 }
 
 void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint64_t ncand, uint32_t k,

@@ -15,13 +15,15 @@ namespace colo {
 struct HostPoints {
     std::vector<float> x, y;
     std::vector<int32_t> raw;
-    std::vector<std::string> first_token;   // the id token as written (names)
+    // the id token as written, at every point whose id differs from the
+    // previous point's (the feature names, colocationFinder.cpp:168-184)
+    std::vector<std::pair<uint64_t, std::string>> tokens;
     float bounds[4] = {0, 0, 0, 0};
     void clear() {
         x.clear();
         y.clear();
         raw.clear();
-        first_token.clear();
+        tokens.clear();
     }
 };
 
@@ -55,7 +57,11 @@ struct BatchStorage;   // owned device copies for multi-job batches
 
 colo_status read_params_file(const char* path, colo_params* p, std::string& err);
 colo_status read_config_file(const char* path, std::string out[5], std::string& err);
-colo_status parse_points_csv(const char* path, HostPoints& hp, std::string& err);
+// threads = 0: one per hardware thread, fewer for small files
+colo_status parse_points_csv(const char* path, HostPoints& hp, std::string& err, unsigned threads = 0);
+colo_status write_points_binary(const HostPoints& hp, const std::vector<std::string>& names, const char* path,
+                                std::string& err);
+colo_status read_points_binary(const char* path, HostPoints& hp, std::string& err);
 colo_status write_points_csv(const HostPoints& hp, const std::vector<std::string>& names,
                              const std::vector<uint32_t>& feat, const char* path, std::string& err);
 colo_status write_patterns(const MineResult& r, const std::vector<std::string>& names,

@@ -46,9 +46,12 @@ void group_features(colo_dataset* ds) {
     ds->names.clear();
     ds->fstart.clear();
     ds->fcount.clear();
+    size_t tk = 0;
     for (size_t i = 0; i < n; ++i) {
         if (i == 0 || hp.raw[i] != hp.raw[i - 1]) {
-            ds->names.push_back(hp.first_token.empty() ? std::to_string(hp.raw[i]) : hp.first_token[i]);
+            while (tk < hp.tokens.size() && hp.tokens[tk].first < i) ++tk;
+            const bool named = tk < hp.tokens.size() && hp.tokens[tk].first == i;
+            ds->names.push_back(named ? hp.tokens[tk].second : std::to_string(hp.raw[i]));
             ds->fstart.push_back((uint32_t)i);
             ds->fcount.push_back(0);
         }
@@ -430,10 +433,10 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         if (k == 2) {
             DevBuf<uint32_t> ub2;
             std::vector<uint64_t> job_off;
-            filter_pairs(b, ub2, job_off);
+            filter_pairs(b, ub2, job_off, s);
             std::vector<uint32_t> h(job_off[J]);
-            if (!h.empty())
-                COLO_CUDA(cudaMemcpy(h.data(), ub2.get(), h.size() * 4, cudaMemcpyDeviceToHost));
+            if (!h.empty()) COLO_CUDA(cudaMemcpyAsync(h.data(), ub2.get(), h.size() * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaStreamSynchronize(s));
             for (uint32_t j = 0; j < J; ++j) {
                 if (!tr[j]) continue;
                 LevelTrace& L = *tr[j];
@@ -1037,19 +1040,69 @@ colo_status colo_read_config(const char* path, char* location, char* param_file,
     return COLO_OK;
 }
 
-colo_status colo_dataset_from_csv(colo_ctx* ctx, const char* path, colo_dataset** out) {
+colo_status colo_dataset_from_csv_threads(colo_ctx* ctx, const char* path, uint32_t threads, colo_dataset** out) {
     if (!ctx || !path || !out) return COLO_ERR_ARG;
     return guarded(ctx, [&]() {
         std::unique_ptr<colo_dataset> ds(new colo_dataset());
         ds->ctx = ctx;
         std::string err;
-        colo_status st = parse_points_csv(path, ds->hp, err);
+        colo_status st = parse_points_csv(path, ds->hp, err, threads);
         if (st != COLO_OK) return set_err(ctx, st, err);
         group_features(ds.get());
         ctx->refs++;
         *out = ds.release();
         return COLO_OK;
     });
+}
+
+colo_status colo_dataset_from_csv(colo_ctx* ctx, const char* path, colo_dataset** out) {
+    return colo_dataset_from_csv_threads(ctx, path, 0, out);
+}
+
+colo_status colo_dataset_from_binary(colo_ctx* ctx, const char* path, colo_dataset** out) {
+    if (!ctx || !path || !out) return COLO_ERR_ARG;
+    return guarded(ctx, [&]() {
+        std::unique_ptr<colo_dataset> ds(new colo_dataset());
+        ds->ctx = ctx;
+        std::string err;
+        colo_status st = read_points_binary(path, ds->hp, err);
+        if (st != COLO_OK) return set_err(ctx, st, err);
+        group_features(ds.get());
+        ctx->refs++;
+        *out = ds.release();
+        return COLO_OK;
+    });
+}
+
+colo_status colo_dataset_write_binary(const colo_dataset* ds, const char* path) {
+    if (!ds || !path) return COLO_ERR_ARG;
+    std::string err;
+    colo_status st = write_points_binary(ds->hp, ds->names, path, err);
+    return st != COLO_OK ? set_err(ds->ctx, st, err) : st;
+}
+
+colo_status colo_csv_to_binary(const char* csv_path, const char* bin_path, uint32_t threads, char* err,
+                               size_t err_cap) {
+    if (!csv_path || !bin_path) return COLO_ERR_ARG;
+    std::string msg;
+    colo_status st;
+    try {
+        colo_dataset ds;
+        st = parse_points_csv(csv_path, ds.hp, msg, threads);
+        if (st == COLO_OK) {
+            group_features(&ds);
+            st = write_points_binary(ds.hp, ds.names, bin_path, msg);
+        }
+    } catch (const std::bad_alloc&) {
+        st = COLO_ERR_NOMEM;
+        msg = "host allocation failed";
+    }
+    if (err && err_cap) {
+        const size_t m = std::min(msg.size(), err_cap - 1);
+        std::memcpy(err, msg.data(), m);
+        err[m] = 0;
+    }
+    return st;
 }
 
 colo_status colo_dataset_from_host(colo_ctx* ctx, const float* x, const float* y, const int32_t* fid,

@@ -128,7 +128,8 @@ colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float th
             if (k == 2) {
                 DevBuf<uint32_t> ub2;
                 std::vector<uint64_t> job_off;
-                filter_pairs(b, ub2, job_off);
+                filter_pairs(b, ub2, job_off, s);
+                COLO_CUDA(cudaStreamSynchronize(s));
                 std::vector<uint32_t> h(job_off[1]);
                 COLO_CUDA(cudaMemcpy(h.data(), ub2.get(), h.size() * 4, cudaMemcpyDeviceToHost));
                 uint32_t nf = b.F;

@@ -44,7 +44,12 @@ void colocationFinder::populateData(std::string datasetFilename) {
     dataset_ = datasetFilename;
     if (ds_) colo_dataset_free(ds_);
     ds_ = nullptr;
-    status = colo_dataset_from_csv(ctx_, datasetFilename.c_str(), &ds_);
+    // A dataset named *.colo is a binary point file (colo_csv_to_binary); any
+    // other name is the reference's CSV.
+    const bool binary = datasetFilename.size() > 5 &&
+                        datasetFilename.compare(datasetFilename.size() - 5, 5, ".colo") == 0;
+    status = binary ? colo_dataset_from_binary(ctx_, datasetFilename.c_str(), &ds_)
+                    : colo_dataset_from_csv(ctx_, datasetFilename.c_str(), &ds_);
     if (status != COLO_OK) {
         error = colo_last_error(ctx_);
         return;

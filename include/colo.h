@@ -88,6 +88,25 @@ colo_status colo_dataset_from_host(colo_ctx* ctx, const float* x, const float* y
                                    colo_dataset** out);
 /* Write a dataset in the reference's CSV format (for the CLI and tests). */
 colo_status colo_dataset_write_csv(const colo_dataset* ds, const char* path);
+/* colo_dataset_from_csv with a chosen number of parser threads (0: one per
+ * hardware thread, fewer for small files).  The text is cut into runs of
+ * whole lines parsed in parallel; points, features, names and the line named
+ * by an error are those of the serial reading.  No counterpart in the
+ * reference (its populateData reads serially). */
+colo_status colo_dataset_from_csv_threads(colo_ctx* ctx, const char* path, uint32_t threads,
+                                          colo_dataset** out);
+/* Binary point file: the points (x, y f32), raw ids (i32), feature names and
+ * bounds of a dataset, loaded without parsing.  Little-endian; a 64-byte
+ * header ("COLOPTS1", version 1, header bytes, n, features, name bytes,
+ * bounds[4]), then x[n], y[n], id[n], name_len[features] u32, the names.
+ * No counterpart in the reference. */
+colo_status colo_dataset_write_binary(const colo_dataset* ds, const char* path);
+colo_status colo_dataset_from_binary(colo_ctx* ctx, const char* path, colo_dataset** out);
+/* Host only (needs no device): parse a CSV dataset (threads as above) and
+ * write it as a binary point file.  err receives a failure's message
+ * (err_cap bytes, NUL-terminated; may be NULL). */
+colo_status colo_csv_to_binary(const char* csv_path, const char* bin_path, uint32_t threads, char* err,
+                               size_t err_cap);
 /* Copy the points to the device now (initializeDeviceMemory,
  * colocationFinder.cpp:443-464); otherwise colo_mine copies them. */
 colo_status colo_dataset_upload(colo_dataset* ds);

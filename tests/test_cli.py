@@ -72,3 +72,25 @@ def test_cli_writes_the_oracles_patterns(tmp_path, case):
             assert rows == int(lev.rows[c]) and nums == [int(v) for v in lev.num[c]]
             assert cnts == [int(counts[m]) for m in lev.cand[c]]
             assert np.float32(pi) == np.float32(lev.pi[c])
+
+
+@pytest.mark.gpu
+def test_cli_reads_a_binary_point_file(tmp_path):
+    """A config whose dataset line names a .colo file gives the same pattern files as the CSV."""
+    outs = {}
+    for form in ("csv", "colo"):
+        d = tmp_path / form
+        d.mkdir()
+        data = GOLDEN / "levels.csv"
+        if form == "colo":
+            data = d / "levels.colo"
+            colo.csv_to_binary(GOLDEN / "levels.csv", data)
+        out = d / "out"
+        out.mkdir()
+        cfg = d / "config.txt"
+        cfg.write_text(f"{out}/\n{GOLDEN / 'levels.param.txt'}\n{data}\n{out}/\nreport.txt\n")
+        r = subprocess.run([str(_cli()), str(cfg)], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        outs[form] = {f.name: f.read_text() for f in sorted(out.glob("ColocationDegree_*.txt"))}
+        outs[form]["report"] = (out / "report.txt").read_text()
+    assert outs["csv"] and outs["csv"] == outs["colo"]

@@ -112,8 +112,11 @@ def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
     `launches` = launches per step, `words` = 32-bit mask words per cell.
     """
     N, E, M, Rn = c["points"], c["neighbors"], c["cells"], c["runs"]
-    if name == "radix_sort":       # per digit pass over the points: read and write (8 B key + 4 B id)
-        return 24.0 * N * launches
+    kb = 4.0 if c.get("key_bits", 64) <= 32 else 8.0   # cell keys are 32-bit when every key fits
+    if name == "radix_sort":       # per digit pass over the points: read and write the key and the 4 B id
+        return 2.0 * (kb + 4.0) * N * launches
+    if name == "radix_hist":       # one read of the keys for every pass's digit histogram
+        return kb * N
     if name == "run_sort":         # per digit pass over the runs
         return 24.0 * Rn * launches
     if name == "cell_keys":        # read x, y, feature; write key, id
@@ -141,6 +144,22 @@ def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
     if name == "filter_level":     # per item the driver cell's 4 quad masks; per (cell of U_c, member) one run
         return 16.0 * words * c["filter_items"] + 8.0 * c["filter_cell_members"]
     return 0.0
+
+
+def cell_key_bits(grids) -> int:
+    """Bits of the batch's cell keys: the sum of the jobs' grid sizes, each grid set as setGrid
+    does (colocationFinder.cpp:102-126) in float."""
+    total = 0
+    for bounds, R in grids:
+        b = np.asarray(bounds, np.float32)
+        R = np.float32(R)
+        gx = int(np.ceil((b[2] - b[0]) / R))
+        gy = int(np.ceil(((b[3] + R) - b[1]) / R))
+        total += gx * gy
+    bits = 1
+    while bits < 64 and (1 << bits) < total:
+        bits += 1
+    return bits
 
 
 def load_traffic(kernel: str):
@@ -358,7 +377,8 @@ def main():
             a = kern.setdefault(name, [0, 0.0])
             a[0] += nl
             a[1] += kms
-    counters = res_b[0].counters
+    counters = dict(res_b[0].counters)
+    counters["key_bits"] = cell_key_bits([(wl.bounds, wl.R)])
     words = (wl.nfeat + 31) // 32
     peak, peak_kind = measured_peak_gbs()
     roof = None

@@ -143,8 +143,14 @@ __global__ void k_cell_masks(uint64_t Rn, const uint32_t* __restrict__ rfeat,
 // (cx+dx, cy+dy) inside the job's grid, or -1.  Keys ascend along a grid row,
 // so the row of the cell itself is read from the adjacent entries and each
 // other row needs one lower_bound (above: after c, below: before c).
+//
+// qfirst[c] bit q: c is the first occupied cell of its quad q in (ey, ex)
+// order (the level filter counts each full quad once, at that cell).  Quad q
+// has lower-left cell (cx+qx, cy+qy), qx = (q & 1) - 1, qy = (q >> 1) - 1, and
+// holds c at corner (ex, ey) = (-qx, -qy); quads outside 0 <= bx <= gx-2,
+// 0 <= by <= gy-2 are never full and get no bit.
 __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                      const JobGrid* __restrict__ grids, int32_t* __restrict__ nb9) {
+                      const JobGrid* __restrict__ grids, int32_t* __restrict__ nb9, uint8_t* __restrict__ qfirst) {
     uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M) return;
     const JobGrid g = grids[cjob[c]];
@@ -153,23 +159,47 @@ __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint3
     const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
     const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < (int64_t)g.gx ? cx + 1 : cx;
     int32_t* out = nb9 + c * 9;
+    uint32_t occ = 0;   // bit (dy+1)*3 + (dx+1): that neighbour is occupied
     for (int dy = -1; dy <= 1; ++dy) {
-        int32_t v[3] = {-1, -1, -1};
+        int32_t v0 = -1, v1 = -1, v2 = -1;
         const int64_t ny = cy + dy;
         if (dy == 0) {
-            v[1] = (int32_t)c;
-            if (cx > 0 && c > 0 && ckey[c - 1] == key - 1) v[0] = (int32_t)(c - 1);
-            if (cx + 1 < (int64_t)g.gx && c + 1 < M && ckey[c + 1] == key + 1) v[2] = (int32_t)(c + 1);
+            v1 = (int32_t)c;
+            if (cx > 0 && c > 0 && ckey[c - 1] == key - 1) v0 = (int32_t)(c - 1);
+            if (cx + 1 < (int64_t)g.gx && c + 1 < M && ckey[c + 1] == key + 1) v2 = (int32_t)(c + 1);
         } else if (ny >= 0 && ny < (int64_t)g.gy) {
             const uint64_t k0 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x0;
             const uint64_t k1 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x1;
             uint64_t pos = dy < 0 ? lower_bound_dev(ckey, (uint64_t)0, c, k0) : lower_bound_dev(ckey, c + 1, M, k0);
-            for (; pos < M && ckey[pos] <= k1; ++pos) v[(int64_t)(ckey[pos] - g.key_base - (uint64_t)ny * g.gx) - cx + 1] = (int32_t)pos;
+            for (; pos < M && ckey[pos] <= k1; ++pos) {
+                const int64_t dx = (int64_t)(ckey[pos] - g.key_base - (uint64_t)ny * g.gx) - cx;
+                if (dx < 0) v0 = (int32_t)pos;
+                else if (dx == 0) v1 = (int32_t)pos;
+                else v2 = (int32_t)pos;
+            }
         }
-        out[(dy + 1) * 3 + 0] = v[0];
-        out[(dy + 1) * 3 + 1] = v[1];
-        out[(dy + 1) * 3 + 2] = v[2];
+        out[(dy + 1) * 3 + 0] = v0;
+        out[(dy + 1) * 3 + 1] = v1;
+        out[(dy + 1) * 3 + 2] = v2;
+        occ |= ((v0 >= 0 ? 1u : 0u) | (v1 >= 0 ? 2u : 0u) | (v2 >= 0 ? 4u : 0u)) << ((dy + 1) * 3);
     }
+    uint32_t qf = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
+        const int64_t bx = cx + qx, by = cy + qy;
+        if (!(bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy)) continue;
+        const int ex = -qx, ey = -qy;
+        bool first = true;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            if (e >= ey * 2 + ex) break;
+            const int ox = (e & 1) - ex, oy = (e >> 1) - ey;
+            if (occ >> ((oy + 1) * 3 + (ox + 1)) & 1u) first = false;
+        }
+        if (first) qf |= 1u << q;
+    }
+    qfirst[c] = (uint8_t)qf;
 }
 
 // Per cell and mask word: the feature masks of the four quads (2x2 cell
@@ -457,10 +487,7 @@ void sort_and_compact(Batch& b) {
     COLO_LAUNCH_CHECK();
     count_launch();
     }
-    if (sizeof(KT) == 4)
-        radix_sort_u32_u32(reinterpret_cast<uint32_t*>(keys.get()), b.sid.get(), n, (int)b.key_bits, s);
-    else
-        radix_sort_u64_u32(reinterpret_cast<uint64_t*>(keys.get()), b.sid.get(), n, (int)b.key_bits, s);
+    radix_sort(keys, b.sid, n, (int)b.key_bits, s);
 
     b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);
@@ -528,9 +555,11 @@ void bucket_points(Batch& b) {
         count_launch();
     }
     b.nb9.alloc((uint64_t)M * 9, s);
+    b.qfirst.alloc(M, s);
     {
         KScope ks("cell_neighbours");
-        k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get());
+        k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
+                                               b.qfirst.get());
         COLO_LAUNCH_CHECK();
         count_launch();
     }

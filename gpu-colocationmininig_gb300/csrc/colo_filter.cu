@@ -15,9 +15,9 @@
 // each feature g of the 3x3 block, add count(C, f) to bound(f side of {f,g}).
 // The accumulator is an F x F matrix in shared memory.
 //
-// Level k >= 3: quads are enumerated from the cells of a driver member (the
-// one with the fewest cells); each quad is visited once (by its first driver
-// cell) and each cell is counted by its first full quad in (by, bx) order.
+// Level k >= 3: a cell is in U_c when one of its four quads is full; the
+// cells tested for c are those with c's driver member (the one with the
+// fewest cells) in their 3x3 block, which holds every cell of U_c.
 #include <algorithm>
 
 #include "colo_batch.h"
@@ -29,6 +29,7 @@ namespace {
 constexpr int kFilterThreads = 256;
 constexpr int kFilterWarps = kFilterThreads / 32;
 constexpr int kMaxW = 8;   // mask words handled in registers (256 features per job)
+constexpr uint64_t kAccMax = 16384;   // block-private level sums (64 KB of shared memory)
 
 // One thread per run (C, f); a block owns a contiguous range of runs, so the
 // job changes rarely and the F x F accumulator lives in shared memory.
@@ -99,191 +100,184 @@ __device__ __forceinline__ bool covers(const uint32_t* __restrict__ qm, const ui
     return ok;
 }
 
-// Level k >= 3.  Items are (driver cell, candidate) pairs taken in run
-// order: a warp owns 32 consecutive (cell, feature) runs -- cell-major, so
-// all warps in flight work on a narrow band of cells whose data stays in L2
-// -- and expands each run whose feature drives G candidates into G items
-// (warp prefix sum; candidates of one driver are adjacent lanes).
+// Position of the r-th set bit (r < popc(v)) of v.
+__device__ __forceinline__ uint32_t select_bit(uint32_t v, uint32_t r) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (int half = 16; half > 0; half >>= 1) {
+        const uint32_t lo = __popc(v & ((1u << half) - 1u));
+        if (r >= lo) {
+            r -= lo;
+            v >>= half;
+            pos += half;
+        }
+    }
+    return pos;
+}
+
+// Last lane whose exclusive offset is <= t (the lane owning entry t).
+__device__ __forceinline__ int owner_lane(uint32_t excl, uint32_t t) {
+    int o = 0;
+#pragma unroll
+    for (int bstep = 16; bstep > 0; bstep >>= 1) {
+        const uint32_t ev = __shfl_sync(0xffffffffu, excl, o + bstep);
+        if (ev <= t) o += bstep;
+    }
+    return o;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Level k >= 3, one (cell Z, candidate c) pair per lane.
 //
-// Phase 1 (a lane per item): the quads containing the driver cell C (masks
-// qmask[C]) that are full for the candidate and are visited from C -- a
-// quad is visited only from its first cell in (ey, ex) order holding the
-// driver feature, so each full quad is seen once per candidate.  Each cell
-// of a visited quad is a task: a 16-bit mask, bit 4*q + e.
-// Phase 2 (the warp): the tasks of the 32 items are spread over the lanes.
-// A task's cell Z is counted unless an earlier quad containing Z (in
-// (by, bx) order: qmask[Z][p] for p below this quad's index in Z's frame)
-// is full; a counted cell adds its runs of the members (located by rank in
-// Z's feature mask) to the item's shared-memory accumulator.
-// Phase 3: one atomicAdd per member per item.
+// A cell Z lies in U_c exactly when one of its four quads (qmask[Z]) is full
+// for c.  A full quad holds a cell of every member, in particular of c's
+// driver member d (the member with the fewest cells), so every cell of U_c
+// has d in its 3x3 feature mask nbmask[Z].  The pairs tested are therefore
+// (Z, c) for every occupied cell Z and every candidate whose driver is in
+// nbmask[Z]; each pair is tested once, so each cell of U_c is counted once
+// with no ownership rule.  A full quad is counted at its first occupied cell
+// in (ey, ex) order (bit q of qfirst[Z]), so each is counted once.
+//
+// A warp takes 32 consecutive cells, expands them into (Z, driver) pairs and
+// those into (Z, candidate) pairs (warp prefix sums; candidates of one driver
+// in adjacent lanes, so lanes share Z's masks in L1).
 // stats[c*2] = full quads, stats[c*2+1] = cells in U_c.
+//
+// Sums go to a block-private accumulator in shared memory when the level's
+// candidates fit (acc_n = ncand * (m + 2) counters: m bounds, quads, cells),
+// and are added to ub / stats once per block at the end: a level has few
+// candidates and millions of hits, and global atomics on the same few
+// addresses serialise in their L2 slice.
 template <int WT>
-__global__ void __launch_bounds__(256) k_filter_level(
-    uint64_t Rn, const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcell,
+__global__ void __launch_bounds__(256) k_filter_cells(
+    uint64_t M, const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
+    const uint32_t* __restrict__ nbmask, const uint32_t* __restrict__ dmask,
     const uint32_t* __restrict__ drv_count, const uint32_t* __restrict__ drv_start,
-    const uint32_t* __restrict__ flocal, const uint32_t* __restrict__ order, uint32_t k,
-    const uint32_t* __restrict__ cand, const uint32_t* __restrict__ need_all, const int32_t* __restrict__ nb9,
-    const uint32_t* __restrict__ cmask, const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ crun,
-    const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub, unsigned long long* __restrict__ stats) {
+    const uint32_t* __restrict__ order, const uint32_t* __restrict__ need_all, const uint32_t* __restrict__ lmem,
+    uint32_t k, const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ cmask,
+    const uint32_t* __restrict__ crun, const uint8_t* __restrict__ qfirst, const uint32_t* __restrict__ rcnt,
+    uint32_t* __restrict__ ub, unsigned long long* __restrict__ stats, uint32_t acc_n) {
     constexpr uint32_t W = WT;
-    constexpr int kM = kMaxMembersFiltered;
-    __shared__ uint32_t s_need[kFilterWarps][32][WT];
-    __shared__ uint32_t s_lf[kFilterWarps][32][kM];
-    __shared__ uint32_t s_acc[kFilterWarps][32][kM];
-    __shared__ uint32_t s_cells[kFilterWarps][32];
+    extern __shared__ uint32_t acc[];
     const uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint64_t nwarps = (uint64_t)gridDim.x * kFilterWarps;
-    for (uint64_t rbase = ((uint64_t)blockIdx.x * kFilterWarps + wid) * 32; rbase < Rn; rbase += nwarps * 32) {
-        // this warp's 32 runs and the candidates their features drive
-        const uint64_t myr = rbase + lane;
-        uint32_t G = 0, f = 0;
-        if (myr < Rn) {
-            f = rfeat[myr];
-            G = drv_count[f];
-        }
-        uint32_t rin = G;
+    const uint32_t stride = m + 2;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i = threadIdx.x; i < acc_n; i += blockDim.x) acc[i] = 0;
+    __syncthreads();
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t zbase = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; zbase < M;
+         zbase += nwarps * 32) {
+        // this lane's cell and the drivers of its 3x3 block
+        const uint64_t Z = zbase + lane;
+        uint32_t dz[WT], f0 = 0, nd = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t t = __shfl_up_sync(0xffffffffu, rin, o);
-            if (lane >= o) rin += t;
-        }
-        const uint32_t rex = rin - G;
-        const uint32_t ritems = __shfl_sync(0xffffffffu, rin, 31);
-        for (uint32_t i0 = 0; i0 < ritems; i0 += 32) {
-            const uint32_t it = i0 + lane;
-            int j = 0;   // run lane owning item it
+        for (int w = 0; w < WT; ++w) dz[w] = 0;
+        if (Z < M) {
+            const uint32_t job = cjob[Z];
+            f0 = grids[job].f0;
 #pragma unroll
-            for (int bstep = 16; bstep > 0; bstep >>= 1) {
-                uint32_t ev = __shfl_sync(0xffffffffu, rex, j + bstep);
-                if (ev <= it) j += bstep;
+            for (int w = 0; w < WT; ++w) {
+                dz[w] = nbmask[Z * W + w] & dmask[(uint64_t)job * W + w];
+                nd += __popc(dz[w]);
             }
-            const uint32_t rex_j = __shfl_sync(0xffffffffu, rex, j);
-            const uint32_t fd = __shfl_sync(0xffffffffu, f, j);
-            const bool valid = it < ritems;
-            uint32_t C = 0, c = 0, tmask = 0, nquads = 0;
-            if (valid) {
-                C = rcell[rbase + j];
-                c = order[drv_start[fd] + (it - rex_j)];
-                const uint32_t lfd = flocal[fd], f0 = fd - lfd;
+        }
+        const uint32_t pincl = warp_incl_sum(nd, lane);
+        const uint32_t pex = pincl - nd;
+        const uint32_t npairs = __shfl_sync(0xffffffffu, pincl, 31);
+        for (uint32_t p0 = 0; p0 < npairs; p0 += 32) {
+            // (cell, driver) pair p0 + lane
+            const uint32_t t = p0 + lane;
+            const int o = owner_lane(pex, t);
+            const uint32_t ex_o = __shfl_sync(0xffffffffu, pex, o);
+            const uint32_t f0_o = __shfl_sync(0xffffffffu, f0, o);
+            uint32_t r = t - ex_o, d = 0;
+            bool found = false;
+#pragma unroll
+            for (int w = 0; w < WT; ++w) {
+                const uint32_t v = __shfl_sync(0xffffffffu, dz[w], o);
+                const uint32_t pc = __popc(v);
+                if (!found && r < pc) {
+                    d = (uint32_t)w * 32 + select_bit(v, r);
+                    found = true;
+                } else if (!found) {
+                    r -= pc;
+                }
+            }
+            uint32_t G = 0, start = 0;
+            if (t < npairs) {
+                G = drv_count[f0_o + d];
+                start = drv_start[f0_o + d];
+            }
+            const uint64_t Zp = zbase + (uint64_t)o;
+            const uint32_t iincl = warp_incl_sum(G, lane);
+            const uint32_t iex = iincl - G;
+            const uint32_t nitems = __shfl_sync(0xffffffffu, iincl, 31);
+            for (uint32_t i0 = 0; i0 < nitems; i0 += 32) {
+                // (cell, candidate) pair i0 + lane
+                const uint32_t it = i0 + lane;
+                const int o2 = owner_lane(iex, it);
+                const uint32_t ex2 = __shfl_sync(0xffffffffu, iex, o2);
+                const uint32_t st2 = __shfl_sync(0xffffffffu, start, o2);
+                const uint64_t Zi = __shfl_sync(0xffffffffu, Zp, o2);
+                if (it >= nitems) continue;
+                const uint32_t c = order[st2 + (it - ex2)];
                 uint32_t need[WT];
 #pragma unroll
-                for (int w = 0; w < WT; ++w) {
-                    need[w] = need_all[(uint64_t)c * W + w];
-                    s_need[wid][lane][w] = need[w];
-                }
-                const uint32_t* q4 = qmask + (uint64_t)C * 4 * W;
-                // the neighbour table is loaded with the quad masks (independent loads in flight together)
-                const int32_t* nbc = nb9 + (uint64_t)C * 9;
-                int32_t nbv[9];
-#pragma unroll
-                for (int t = 0; t < 9; ++t) nbv[t] = nbc[t];
+                for (int w = 0; w < WT; ++w) need[w] = need_all[(uint64_t)c * W + w];
+                const uint32_t* q4 = qmask + Zi * 4 * W;
                 uint32_t full = 0;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (covers<WT>(q4 + q * W, need)) full |= 1u << q;
-                if (full) {
+                if (!full) continue;
+                uint32_t cm[WT];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (!(full >> q & 1u)) continue;
-                        const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
-                        bool first = true;
+                for (int w = 0; w < WT; ++w) cm[w] = cmask[Zi * W + w];
+                const uint32_t q0 = crun[Zi];
+                const uint32_t lm[2] = {lmem[(uint64_t)c * 2], lmem[(uint64_t)c * 2 + 1]};
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int ox = qx + (e & 1), oy = qy + (e >> 1);
-                            if (ox == 0 && oy == 0) break;
-                            const int32_t v = nbv[(oy + 1) * 3 + (ox + 1)];
-                            if (first && v >= 0 && (cmask[(uint64_t)v * W + (lfd >> 5)] >> (lfd & 31) & 1u))
-                                first = false;
-                        }
-                        if (!first) continue;
-                        ++nquads;
+                for (int jj = 0; jj < kMaxMembersFiltered; ++jj) {
+                    if ((uint32_t)jj >= m) break;
+                    const uint32_t lf = (lm[jj >> 2] >> ((jj & 3) * 8)) & 0xFFu, wq = lf >> 5;
+                    uint32_t rk = 0, word = 0;
 #pragma unroll
-                        for (int e = 0; e < 4; ++e)
-                            if (nbv[(qy + (e >> 1) + 1) * 3 + (qx + (e & 1) + 1)] >= 0) tmask |= 1u << (q * 4 + e);
+                    for (int w = 0; w < WT; ++w) {
+                        if ((uint32_t)w < wq) rk += __popc(cm[w]);
+                        if ((uint32_t)w == wq) word = cm[w];
+                    }
+                    if (word >> (lf & 31) & 1u) {
+                        const uint32_t v = rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))];
+                        if (acc_n) atomicAdd(&acc[c * stride + jj], v);
+                        else atomicAdd(&ub[(uint64_t)c * k + jj], v);
                     }
                 }
-                const uint32_t* mem = cand + (uint64_t)c * k;
-#pragma unroll
-                for (int jj = 0; jj < kM; ++jj) {
-                    s_lf[wid][lane][jj] = (uint32_t)jj < m ? mem[jj] - f0 : 0u;
-                    s_acc[wid][lane][jj] = 0;
+                const uint32_t nq = __popc(full & qfirst[Zi]);
+                if (acc_n) {
+                    if (nq) atomicAdd(&acc[c * stride + m], nq);
+                    atomicAdd(&acc[c * stride + m + 1], 1u);
+                } else if (stats) {
+                    if (nq) atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nq);
+                    atomicAdd(&stats[(uint64_t)c * 2 + 1], 1ull);
                 }
             }
-            s_cells[wid][lane] = 0;
-            // warp-wide task list
-            const uint32_t cnt = __popc(tmask);
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const uint32_t excl = incl - cnt;
-            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-            __syncwarp();
-            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                const uint32_t t = t0 + lane;
-                int o = 0;   // owner lane: last lane whose range starts at or before t
-#pragma unroll
-                for (int bstep = 16; bstep > 0; bstep >>= 1) {
-                    uint32_t ev = __shfl_sync(0xffffffffu, excl, o + bstep);
-                    if (ev <= t) o += bstep;
-                }
-                const uint32_t ex_o = __shfl_sync(0xffffffffu, excl, o);
-                const uint32_t tm_o = __shfl_sync(0xffffffffu, tmask, o);
-                const uint32_t C_o = __shfl_sync(0xffffffffu, C, o);
-                if (t >= total) continue;
-                // the (t - ex_o)-th set bit of the owner's task mask
-                uint32_t bits = tm_o;
-                for (uint32_t i = t - ex_o; i > 0; --i) bits &= bits - 1;
-                const int tb = __ffs(bits) - 1, q = tb >> 2, e = tb & 3;
-                const int qx = (q & 1) - 1, qy = (q >> 1) - 1, ex = e & 1, ey = e >> 1;
-                const int32_t Z = nb9[(uint64_t)C_o * 9 + (qy + ey + 1) * 3 + (qx + ex + 1)];
-                uint32_t need[WT];
-#pragma unroll
-                for (int w = 0; w < WT; ++w) need[w] = s_need[wid][o][w];
-                // this quad is quad pq of Z; earlier quads of Z are p < pq
-                const int pq = (1 - ey) * 2 + (1 - ex);
-                const uint32_t* z4 = qmask + (uint64_t)Z * 4 * W;
-                // Z's feature mask and first run are loaded with its quad masks
-                uint32_t zm[WT];
-#pragma unroll
-                for (int w = 0; w < WT; ++w) zm[w] = cmask[(uint64_t)Z * W + w];
-                const uint32_t q0 = crun[Z];
-                bool claimed = true;
-#pragma unroll
-                for (int p = 0; p < 3; ++p)
-                    if (p < pq && covers<WT>(z4 + p * W, need)) claimed = false;
-                if (!claimed) continue;
-                atomicAdd(&s_cells[wid][o], 1u);
-#pragma unroll
-                for (int jj = 0; jj < kM; ++jj) {
-                    if ((uint32_t)jj < m) {
-                        const uint32_t lf = s_lf[wid][o][jj], wq = lf >> 5;
-                        uint32_t rk = 0, word = 0;
-#pragma unroll
-                        for (int w = 0; w < WT; ++w) {
-                            if ((uint32_t)w < wq) rk += __popc(zm[w]);
-                            if ((uint32_t)w == wq) word = zm[w];
-                        }
-                        if (word >> (lf & 31) & 1u)
-                            atomicAdd(&s_acc[wid][o][jj], rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))]);
-                    }
-                }
-            }
-            __syncwarp();
-            if (valid && tmask) {
-#pragma unroll
-                for (int jj = 0; jj < kM; ++jj)
-                    if ((uint32_t)jj < m && s_acc[wid][lane][jj])
-                        atomicAdd(&ub[(uint64_t)c * k + jj], s_acc[wid][lane][jj]);
-                if (stats) {
-                    atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nquads);
-                    atomicAdd(&stats[(uint64_t)c * 2 + 1], (unsigned long long)s_cells[wid][lane]);
-                }
-            }
-            __syncwarp();
+        }
+    }
+    if (acc_n) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < acc_n; i += blockDim.x) {
+            const uint32_t v = acc[i];
+            if (!v) continue;
+            const uint32_t c = i / stride, r = i - c * stride;
+            if (r < m) atomicAdd(&ub[(uint64_t)c * k + r], v);
+            else if (stats) atomicAdd(&stats[(uint64_t)c * 2 + (r - m)], (unsigned long long)v);
         }
     }
 }
@@ -327,12 +321,16 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
 
 void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint64_t ncand, uint32_t k,
                   uint32_t* d_ub, unsigned long long* d_stats, const uint32_t* d_cand_in) {
+    (void)d_cand_in;
     if (ncand == 0) return;
     if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 256 features per job"};
     cudaStream_t s = b.s;
     const uint32_t m = k < kMaxMembersFiltered ? k : (uint32_t)kMaxMembersFiltered;
-    // driver = member with the fewest cells; candidates grouped by driver
-    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0);
+    // driver = member with the fewest cells; candidates grouped by driver;
+    // per candidate its need mask and local member ids (bytes), per job the
+    // mask of its drivers
+    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0), lmem((size_t)ncand * 2, 0),
+        dmask((size_t)b.J * b.W, 0);
     for (uint64_t c = 0; c < ncand; ++c) {
         const uint32_t* mem = h_cand + c * k;
         const uint32_t f0 = b.jobs[h_job[c]].grid.f0;
@@ -345,47 +343,62 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
             }
             uint32_t lf = mem[j] - f0;
             need[(size_t)c * b.W + (lf >> 5)] |= 1u << (lf & 31);
+            lmem[(size_t)c * 2 + (j >> 2)] |= lf << ((j & 3) * 8);
         }
         drv[c] = best;
+        const uint32_t ld = best - f0;
+        dmask[(size_t)h_job[c] * b.W + (ld >> 5)] |= 1u << (ld & 31);
     }
-    // candidates grouped by driver feature: drv_count[f] of them from drv_start[f] in `order`
     std::vector<uint32_t> order(ncand);
     for (uint64_t c = 0; c < ncand; ++c) order[c] = (uint32_t)c;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return drv[a] < drv[c]; });
-    std::vector<uint32_t> dcount(b.F, 0), dstart(b.F, 0), flocal(b.F, 0);
+    std::vector<uint32_t> dcount(b.F, 0), dstart(b.F, 0);
     for (uint64_t i = 0; i < ncand; ++i) {
         const uint32_t fd = drv[order[i]];
         if (dcount[fd]++ == 0) dstart[fd] = (uint32_t)i;
     }
-    uint64_t nitems = 0;
-    for (uint32_t f = 0; f < b.F; ++f) {
-        flocal[f] = f - b.jobs[b.h_fjob[f]].grid.f0;
-        nitems += (uint64_t)dcount[f] * (b.h_frun_off[f + 1] - b.h_frun_off[f]);
-    }
+    uint64_t nitems = 0;   // (driver cell, candidate) pairs: the work the driver choice bounds
+    for (uint32_t f = 0; f < b.F; ++f) nitems += (uint64_t)dcount[f] * (b.h_frun_off[f + 1] - b.h_frun_off[f]);
     b.filter_items += nitems;
     if (nitems == 0) return;
-    DevBuf<uint32_t> dcand, dneed, dcnt, dst, dfl, dord;
-    if (!d_cand_in) dcand.alloc(ncand * k, s);
-    const uint32_t* d_cand = d_cand_in ? d_cand_in : dcand.get();
-    dneed.alloc(need.size(), s);
-    dcnt.alloc(b.F, s);
-    dst.alloc(b.F, s);
-    dfl.alloc(b.F, s);
-    dord.alloc(ncand, s);
-    if (!d_cand_in) COLO_CUDA(cudaMemcpyAsync(dcand.get(), h_cand, ncand * k * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dneed.get(), need.data(), need.size() * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dcnt.get(), dcount.data(), b.F * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dst.get(), dstart.data(), b.F * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dfl.get(), flocal.data(), b.F * 4, cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaMemcpyAsync(dord.get(), order.data(), ncand * 4, cudaMemcpyHostToDevice, s));
-    uint64_t blocks = (b.Rn + 255) / 256;
-    uint64_t cap = (uint64_t)b.sms * 16;
-    if (blocks > cap) blocks = cap;
+    // one upload: need | lmem | dmask | dcount | dstart | order
+    const size_t n_need = need.size(), n_lmem = lmem.size(), n_dm = dmask.size();
+    std::vector<uint32_t> pack;
+    pack.reserve(n_need + n_lmem + n_dm + 2 * (size_t)b.F + ncand);
+    pack.insert(pack.end(), need.begin(), need.end());
+    pack.insert(pack.end(), lmem.begin(), lmem.end());
+    pack.insert(pack.end(), dmask.begin(), dmask.end());
+    pack.insert(pack.end(), dcount.begin(), dcount.end());
+    pack.insert(pack.end(), dstart.begin(), dstart.end());
+    pack.insert(pack.end(), order.begin(), order.end());
+    DevBuf<uint32_t> dpack;
+    dpack.alloc(pack.size(), s);
+    COLO_CUDA(cudaMemcpyAsync(dpack.get(), pack.data(), pack.size() * 4, cudaMemcpyHostToDevice, s));
+    const uint32_t* d_need = dpack.get();
+    const uint32_t* d_lmem = d_need + n_need;
+    const uint32_t* d_dmask = d_lmem + n_lmem;
+    const uint32_t* d_dcount = d_dmask + n_dm;
+    const uint32_t* d_dstart = d_dcount + b.F;
+    const uint32_t* d_order = d_dstart + b.F;
+    // block-private sums when the level's counters fit in 64 KB of shared memory
+    const uint64_t acc64 = ncand * (uint64_t)(m + 2);
+    const uint32_t acc_n = acc64 <= kAccMax ? (uint32_t)acc64 : 0u;
+    const size_t smem = (size_t)acc_n * 4;
+    // a grid-stride loop over 32-cell chunks: as many blocks as fit at once
+    auto grid = [&](const void* fn) {
+        if (smem > 48 * 1024)
+            COLO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        COLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem));
+        const uint64_t cap = (uint64_t)b.sms * (uint64_t)(per_sm > 0 ? per_sm : 1);
+        const uint64_t want = (b.M + 255) / 256;
+        return (unsigned)(want < cap ? want : cap);
+    };
     KScope ks("filter_level");
 #define COLO_FL(WW)                                                                                          \
-    k_filter_level<WW><<<(unsigned)blocks, 256, 0, s>>>(                                                     \
-        b.Rn, b.rfeat.get(), b.rcell.get(), dcnt.get(), dst.get(), dfl.get(), dord.get(), k, d_cand,          \
-        dneed.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(), b.crun.get(), b.rcnt.get(), d_ub, d_stats)
+    k_filter_cells<WW><<<grid((const void*)k_filter_cells<WW>), 256, smem, s>>>(                            \
+        b.M, b.cjob.get(), b.grids.get(), b.nbmask.get(), d_dmask, d_dcount, d_dstart, d_order, d_need, d_lmem, \
+        k, b.qmask.get(), b.cmask.get(), b.crun.get(), b.qfirst.get(), b.rcnt.get(), d_ub, d_stats, acc_n)
     switch (b.W) {
         case 1: COLO_FL(1); break;
         case 2: COLO_FL(2); break;

@@ -220,10 +220,11 @@ void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host);
 // Stable LSD radix sort of (key, val) pairs by the low `bits` bits of key.
-// Results land back in keys/vals.
-void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s,
-                        const char* name = "radix_sort");
-void radix_sort_u32_u32(uint32_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s,
-                        const char* name = "radix_sort");
+// The sorted pairs are in keys/vals on return (the buffers may have been
+// exchanged for the sort's second buffers, which avoids a copy back).
+void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
+                const char* name = "radix_sort");
+void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
+                const char* name = "radix_sort");
 
 }  // namespace colo

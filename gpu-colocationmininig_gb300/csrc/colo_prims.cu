@@ -121,92 +121,34 @@ void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total
 // Radix sort
 // ---------------------------------------------------------------------------
 
-constexpr int kRadixBits = 8;
-constexpr int kRadix = 1 << kRadixBits;
+constexpr int kMaxRadixBits = 8;                        // digits of at most 8 bits
+constexpr int kMaxRadix = 1 << kMaxRadixBits;
+constexpr int kMaxPasses = 8;
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortRounds = 8;                          // items per lane
 constexpr int kSortTile = kSortThreads * kSortRounds;   // 2048
 
-template <class KT>
-__global__ void k_radix_hist(const KT* __restrict__ keys, uint64_t n, int shift,
-                             uint32_t* __restrict__ hist, uint32_t nblocks) {
-    __shared__ uint32_t h[kRadix];
-    for (int i = threadIdx.x; i < kRadix; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    uint64_t base = (uint64_t)blockIdx.x * kSortTile;
-    for (int r = 0; r < kSortRounds; ++r) {
-        uint64_t i = base + (uint64_t)r * kSortThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & (kRadix - 1)], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[(uint64_t)d * nblocks + blockIdx.x] = h[d];
-}
-
-// Stable scatter: items of a tile are ranked in (warp, round, lane) order,
-// which is their input order.
-template <class KT>
-__global__ void k_radix_scatter(const KT* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                KT* __restrict__ kout, uint32_t* __restrict__ vout,
-                                uint64_t n, int shift, const uint32_t* __restrict__ offs,
-                                uint32_t nblocks) {
-    __shared__ uint32_t wh[kSortWarps][kRadix];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&wh[0][0])[i] = 0;
-    __syncthreads();
-    uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)w * (32 * kSortRounds);
-    KT key[kSortRounds];
-    uint32_t val[kSortRounds];
-    uint32_t rank[kSortRounds];
-    const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
-        uint64_t i = base + (uint64_t)r * 32 + lane;
-        bool ok = i < n;
-        key[r] = ok ? kin[i] : 0;
-        val[r] = ok ? vin[i] : 0;
-        uint32_t d = ok ? ((uint32_t)(key[r] >> shift) & (kRadix - 1)) : 0xFFFFu;
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        int leader = __ffs(peers) - 1;
-        uint32_t old = 0;
-        if (ok && lane == leader) {
-            old = wh[w][d];
-            wh[w][d] = old + __popc(peers);
-        }
-        old = __shfl_sync(0xffffffffu, old, leader);
-        rank[r] = ok ? old + __popc(peers & lt) : 0xFFFFFFFFu;
-        __syncwarp();
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
-        uint32_t run = 0;
-        for (int ww = 0; ww < kSortWarps; ++ww) {
-            uint32_t t = wh[ww][d];
-            wh[ww][d] = run;
-            run += t;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
-        if (rank[r] == 0xFFFFFFFFu) continue;
-        uint32_t d = (uint32_t)(key[r] >> shift) & (kRadix - 1);
-        uint64_t pos = (uint64_t)offs[(uint64_t)d * nblocks + blockIdx.x] + wh[w][d] + rank[r];
-        kout[pos] = key[r];
-        vout[pos] = val[r];
-    }
-}
+// Digit split of the key: pass p sorts `width[p]` bits from `shift[p]`.
+struct PassPlan {
+    int n;
+    int shift[kMaxPasses];
+    int width[kMaxPasses];
+};
 
 // ---------------------------------------------------------------------------
 // One-sweep LSD radix sort: the digit histograms of every pass from one read
 // of the keys, then one kernel per pass.  A block takes the next tile number
-// from a counter, ranks its keys stably as above, publishes its per-digit
-// counts, and looks back over the preceding tiles' published counts (a tile
-// that has finished its own look-back publishes its inclusive prefix, which
-// ends the walk) to place its keys.  Tiles are numbered in the order blocks
-// start, so a block only waits on tiles of blocks already running.  Every
-// wait is bounded: past the limit the block sets *err, uses what it has and
-// finishes (the host reports COLO_ERR_TIMEOUT).
+// from a counter, ranks its keys stably, publishes its per-digit counts, and
+// looks back over the preceding tiles' published counts (a tile that has
+// finished its own look-back publishes its inclusive prefix, which ends the
+// walk) to place its keys.  Tiles are numbered in the order blocks start, so
+// a block only waits on tiles of blocks already running.  Every wait is
+// bounded: past the limit the block sets *err, uses what it has and finishes
+// (the host reports COLO_ERR_TIMEOUT).  The key's bits are split evenly over
+// the fewest passes of at most 8 bits (25 bits: 7 + 6 + 6 + 6): narrower
+// digits leave more keys per digit in a tile, so the scatter writes longer
+// runs.
 // ---------------------------------------------------------------------------
 
 constexpr unsigned long long kFlagA = 1ull << 62;   // tile count published
@@ -215,54 +157,58 @@ constexpr unsigned long long kValMask = (1ull << 62) - 1;
 constexpr uint32_t kSpinLimit = 1u << 22;
 
 template <class KT>
-__global__ void k_digit_hist(const KT* __restrict__ keys, uint64_t n, int passes,
+__global__ void k_digit_hist(const KT* __restrict__ keys, uint64_t n, PassPlan plan,
                              unsigned long long* __restrict__ ghist) {
-    __shared__ uint32_t h[8][kRadix];
-    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+    __shared__ uint32_t h[kMaxPasses * kMaxRadix];
+    for (int i = threadIdx.x; i < plan.n * kMaxRadix; i += blockDim.x) h[i] = 0;
     __syncthreads();
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const KT k = keys[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(uint32_t)(k >> (p * kRadixBits)) & (kRadix - 1)], 1u);
+        for (int p = 0; p < plan.n; ++p)
+            atomicAdd(&h[p * kMaxRadix + ((uint32_t)(k >> plan.shift[p]) & ((1u << plan.width[p]) - 1u))], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
-        const uint32_t v = (&h[0][0])[i];
+    for (int i = threadIdx.x; i < plan.n * kMaxRadix; i += blockDim.x) {
+        const uint32_t v = h[i];
         if (v) atomicAdd(&ghist[i], (unsigned long long)v);
     }
 }
 
-// Exclusive scan of each pass's 256 counters in place (one block of 256).
+// Exclusive scan of each pass's counters in place (one block of kMaxRadix).
 __global__ void k_digit_scan(unsigned long long* __restrict__ ghist, int passes) {
-    __shared__ unsigned long long sh[kRadix];
+    __shared__ unsigned long long sh[kMaxRadix];
     for (int p = 0; p < passes; ++p) {
-        const unsigned long long v = ghist[p * kRadix + threadIdx.x];
+        const unsigned long long v = ghist[p * kMaxRadix + threadIdx.x];
         sh[threadIdx.x] = v;
         __syncthreads();
-        for (int o = 1; o < kRadix; o <<= 1) {
+        for (int o = 1; o < kMaxRadix; o <<= 1) {
             unsigned long long t = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0ull;
             __syncthreads();
             sh[threadIdx.x] += t;
             __syncthreads();
         }
-        ghist[p * kRadix + threadIdx.x] = sh[threadIdx.x] - v;
+        ghist[p * kMaxRadix + threadIdx.x] = sh[threadIdx.x] - v;
         __syncthreads();
     }
 }
 
-template <class KT>
+template <class KT, int RB>
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
-    uint64_t n, int shift, const unsigned long long* __restrict__ gofs, unsigned long long* __restrict__ status,
-    uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
-    __shared__ uint32_t wh[kSortWarps][kRadix];
-    __shared__ unsigned long long s_base[kRadix];   // global position of the tile's first key of digit d
-    __shared__ uint32_t s_off[kRadix];              // tile-local position of the first key of digit d
+    uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
+    unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
+    constexpr int R = 1 << RB;
+    constexpr int D = R / kSortThreads;             // digits per thread in the look-back (1 or 2)
+    static_assert(D >= 1 && D * kSortThreads == R, "digit count");
+    __shared__ uint32_t wh[kSortWarps][R];
+    __shared__ unsigned long long s_base[R];   // global position of the tile's first key of digit d
+    __shared__ uint32_t s_off[R];              // tile-local position of the first key of digit d
     __shared__ KT s_key[kSortTile];
     __shared__ uint32_t s_val[kSortTile];
     __shared__ uint32_t s_tile;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
-    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&wh[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < kSortWarps * R; i += blockDim.x) (&wh[0][0])[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint64_t tile0 = (uint64_t)tile * kSortTile;
@@ -277,7 +223,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
         const bool ok = i < n;
         key[r] = ok ? kin[i] : 0;
         val[r] = ok ? vin[i] : 0;
-        const uint32_t d = ok ? ((uint32_t)(key[r] >> shift) & (kRadix - 1)) : 0xFFFFu;
+        const uint32_t d = ok ? ((uint32_t)(key[r] >> shift) & dmask) : 0xFFFFu;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const int leader = __ffs(peers) - 1;
         uint32_t old = 0;
@@ -291,40 +237,53 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
     }
     __syncthreads();
     {
-        const int d = threadIdx.x;   // kSortThreads == kRadix: one thread per digit
-        uint32_t cnt = 0;
-        for (int ww = 0; ww < kSortWarps; ++ww) {
-            const uint32_t t = wh[ww][d];
-            wh[ww][d] = cnt;
-            cnt += t;
+        // thread t owns digits t*D .. t*D + D-1
+        uint32_t cnt[D], sum = 0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            const int d = threadIdx.x * D + i;
+            uint32_t c = 0;
+            for (int ww = 0; ww < kSortWarps; ++ww) {
+                const uint32_t t = wh[ww][d];
+                wh[ww][d] = c;
+                c += t;
+            }
+            cnt[i] = c;
+            sum += c;
         }
         uint32_t tot;
-        s_off[d] = block_excl_scan<uint32_t>(cnt, &tot);
-        volatile unsigned long long* st = status + (uint64_t)tile * kRadix + d;
-        unsigned long long prefix = 0;
-        if (tile == 0) {
-            *st = kFlagP | cnt;
-        } else {
-            *st = kFlagA | cnt;
-            uint32_t spins = 0;
-            for (int64_t t = (int64_t)tile - 1; t >= 0;) {
-                const unsigned long long v = *(volatile const unsigned long long*)(status + (uint64_t)t * kRadix + d);
-                const unsigned long long flag = v & ~kValMask;
-                if (flag == 0) {
-                    if (++spins > kSpinLimit) {
-                        atomicOr(err, 1u);
-                        break;
+        uint32_t ex = block_excl_scan<uint32_t>(sum, &tot);
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            const int d = threadIdx.x * D + i;
+            s_off[d] = ex;
+            ex += cnt[i];
+            volatile unsigned long long* st = status + (uint64_t)tile * R + d;
+            unsigned long long prefix = 0;
+            if (tile == 0) {
+                *st = kFlagP | cnt[i];
+            } else {
+                *st = kFlagA | cnt[i];
+                uint32_t spins = 0;
+                for (int64_t t = (int64_t)tile - 1; t >= 0;) {
+                    const unsigned long long v = *(volatile const unsigned long long*)(status + (uint64_t)t * R + d);
+                    const unsigned long long flag = v & ~kValMask;
+                    if (flag == 0) {
+                        if (++spins > kSpinLimit) {
+                            atomicOr(err, 1u);
+                            break;
+                        }
+                        __nanosleep(64);
+                        continue;
                     }
-                    __nanosleep(64);
-                    continue;
+                    prefix += v & kValMask;
+                    if (flag == kFlagP) break;
+                    --t;
                 }
-                prefix += v & kValMask;
-                if (flag == kFlagP) break;
-                --t;
+                *st = kFlagP | (prefix + cnt[i]);
             }
-            *st = kFlagP | (prefix + cnt);
+            s_base[d] = gofs[d] + prefix;
         }
-        s_base[d] = gofs[d] + prefix;
     }
     __syncthreads();
     // stage the tile in digit order, then write it out: consecutive threads
@@ -332,7 +291,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
         if (rank[r] == 0xFFFFFFFFu) continue;
-        const uint32_t d = (uint32_t)(key[r] >> shift) & (kRadix - 1);
+        const uint32_t d = (uint32_t)(key[r] >> shift) & dmask;
         const uint32_t lp = s_off[d] + wh[w][d] + rank[r];
         s_key[lp] = key[r];
         s_val[lp] = val[r];
@@ -341,7 +300,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
     const uint32_t valid = (uint32_t)(n - tile0 < (uint64_t)kSortTile ? n - tile0 : (uint64_t)kSortTile);
     for (uint32_t i = threadIdx.x; i < valid; i += kSortThreads) {
         const KT k = s_key[i];
-        const uint32_t d = (uint32_t)(k >> shift) & (kRadix - 1);
+        const uint32_t d = (uint32_t)(k >> shift) & dmask;
         const uint64_t pos = s_base[d] + (i - s_off[d]);
         kout[pos] = k;
         vout[pos] = s_val[i];
@@ -396,49 +355,60 @@ void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t
 namespace {
 
 template <class KT>
-void radix_sort_impl(KT* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
+void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
+                     const char* name) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
-    const int passes = (bits + kRadixBits - 1) / kRadixBits;
+    // fewest passes of at most 8 bits, widths as even as possible (25 bits: 7 + 6 + 6 + 6)
+    PassPlan plan{};
+    plan.n = (bits + kMaxRadixBits - 1) / kMaxRadixBits;
+    for (int p = 0, sh = 0; p < plan.n; ++p) {
+        plan.width[p] = bits / plan.n + (p < bits % plan.n ? 1 : 0);
+        plan.shift[p] = sh;
+        sh += plan.width[p];
+    }
     const uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     DevBuf<KT> k2;
     DevBuf<uint32_t> v2, tickets, err;
     DevBuf<unsigned long long> ghist, status;
     k2.alloc(n, s);
     v2.alloc(n, s);
-    ghist.alloc((uint64_t)passes * kRadix, s);
-    status.alloc((uint64_t)ntiles * kRadix, s);
-    tickets.alloc(passes, s);
+    ghist.alloc((uint64_t)plan.n * kMaxRadix, s);
+    status.alloc((uint64_t)ntiles * kMaxRadix, s);
+    tickets.alloc(plan.n, s);
     err.alloc(1, s);
     ghist.zero(s);
     tickets.zero(s);
     err.zero(s);
-    KScope ks(name);
     {
+        KScope ks("radix_hist");
         uint64_t blocks = (n + 255) / 256;
         if (blocks > 1024) blocks = 1024;
-        k_digit_hist<KT><<<(unsigned)blocks, 256, 0, s>>>(keys, n, passes, ghist.get());
+        k_digit_hist<KT><<<(unsigned)blocks, 256, 0, s>>>(keys.get(), n, plan, ghist.get());
         COLO_LAUNCH_CHECK();
-        k_digit_scan<<<1, kRadix, 0, s>>>(ghist.get(), passes);
+        k_digit_scan<<<1, kMaxRadix, 0, s>>>(ghist.get(), plan.n);
         COLO_LAUNCH_CHECK();
         count_launch(2);
     }
-    KT* ka = keys;
-    uint32_t* va = vals;
+    KT* ka = keys.get();
+    uint32_t* va = vals.get();
     KT* kb = k2.get();
     uint32_t* vb = v2.get();
-    for (int p = 0; p < passes; ++p) {
-        status.zero(s);
-        k_onesweep<KT><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, p * kRadixBits, ghist.get() + p * kRadix,
-                                                       status.get(), tickets.get() + p, err.get());
+    for (int p = 0; p < plan.n; ++p) {
+        KScope ks(name);   // one timed launch per digit pass
+        const uint32_t dm = (1u << plan.width[p]) - 1u;
+        COLO_CUDA(cudaMemsetAsync(status.get(), 0, (uint64_t)ntiles * kMaxRadix * 8, s));
+        k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
+                                                                     ghist.get() + p * kMaxRadix, status.get(),
+                                                                     tickets.get() + p, err.get());
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);
         std::swap(va, vb);
     }
-    if (ka != keys) {
-        COLO_CUDA(cudaMemcpyAsync(keys, ka, n * sizeof(KT), cudaMemcpyDeviceToDevice, s));
-        COLO_CUDA(cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    if (ka != keys.get()) {   // an odd number of passes: the result is in the second buffers
+        keys.swap(k2);
+        vals.swap(v2);
     }
     uint32_t herr = 0;
     COLO_CUDA(cudaMemcpyAsync(&herr, err.get(), 4, cudaMemcpyDeviceToHost, s));
@@ -448,11 +418,13 @@ void radix_sort_impl(KT* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_
 
 }  // namespace
 
-void radix_sort_u64_u32(uint64_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
+void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
+                const char* name) {
     radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name);
 }
 
-void radix_sort_u32_u32(uint32_t* keys, uint32_t* vals, uint64_t n, int bits, cudaStream_t s, const char* name) {
+void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
+                const char* name) {
     radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name);
 }
 

@@ -52,31 +52,56 @@ __global__ void k_gather_sorted(uint64_t n, uint32_t F, const uint32_t* __restri
 }
 
 // Cell and run heads in the sorted order, counted and compacted in two
-// passes over the keys (no flag arrays): per 2048-point tile the number of
-// cell heads (high 32 bits) and run heads (low 32 bits), then the same
-// flags exclusive-scanned within the tile plus the tile's base.
-constexpr int kHeadThreads = 256, kHeadItems = 8, kHeadTile = kHeadThreads * kHeadItems;
+// passes over the keys (no flag arrays).  A 2048-point tile is eight warp
+// segments of 256 points; a warp reads its segment 32 consecutive points at a
+// time (coalesced) and ranks heads with ballots.  Pass 1 stores per tile the
+// number of cell heads (high 32 bits) and run heads (low 32 bits); pass 2
+// writes each point's cell and the head arrays at the tile's scanned base.
+constexpr int kHeadThreads = 256, kHeadRounds = 8, kHeadTile = kHeadThreads * kHeadRounds;
+constexpr int kHeadWarps = kHeadThreads / 32;
 
 template <class KT>
-__device__ __forceinline__ uint64_t head_flags(uint64_t p, uint64_t n, const KT* __restrict__ keys,
-                                               const uint32_t* __restrict__ sfeat) {
-    if (p >= n) return 0;
-    const bool ch = p == 0 || keys[p - 1] != keys[p];
-    const bool rh = ch || sfeat[p - 1] != sfeat[p];
-    return ((uint64_t)ch << 32) | (uint64_t)rh;
+__device__ __forceinline__ void head_flags(uint64_t p, uint64_t n, const KT* __restrict__ keys,
+                                           const uint32_t* __restrict__ sfeat, bool& ch, bool& rh) {
+    ch = rh = false;
+    if (p >= n) return;
+    ch = p == 0 || keys[p - 1] != keys[p];
+    rh = ch || sfeat[p - 1] != sfeat[p];
+}
+
+// Ballots of the cell and run heads of the calling warp's segment.
+template <class KT>
+__device__ __forceinline__ void head_ballots(uint64_t seg, uint64_t n, const KT* __restrict__ keys,
+                                             const uint32_t* __restrict__ sfeat, int lane,
+                                             uint32_t (&chb)[kHeadRounds], uint32_t (&rhb)[kHeadRounds]) {
+#pragma unroll
+    for (int r = 0; r < kHeadRounds; ++r) {
+        bool ch, rh;
+        head_flags(seg + (uint64_t)r * 32 + lane, n, keys, sfeat, ch, rh);
+        chb[r] = __ballot_sync(0xffffffffu, ch);
+        rhb[r] = __ballot_sync(0xffffffffu, rh);
+    }
 }
 
 template <class KT>
 __global__ void __launch_bounds__(kHeadThreads) k_head_tiles(uint64_t n, const KT* __restrict__ keys,
                                                             const uint32_t* __restrict__ sfeat,
                                                             uint64_t* __restrict__ partial) {
-    const uint64_t base = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)threadIdx.x * kHeadItems;
+    __shared__ uint64_t s_tot[kHeadWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t seg = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)w * (32 * kHeadRounds);
+    uint32_t chb[kHeadRounds], rhb[kHeadRounds];
+    head_ballots(seg, n, keys, sfeat, lane, chb, rhb);
     uint64_t v = 0;
 #pragma unroll
-    for (int i = 0; i < kHeadItems; ++i) v += head_flags(base + i, n, keys, sfeat);
-    uint64_t tot;
-    block_excl_scan<uint64_t>(v, &tot);
-    if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+    for (int r = 0; r < kHeadRounds; ++r) v += ((uint64_t)__popc(chb[r]) << 32) + (uint64_t)__popc(rhb[r]);
+    if (lane == 0) s_tot[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t t = 0;
+        for (int i = 0; i < kHeadWarps; ++i) t += s_tot[i];
+        partial[blockIdx.x] = t;
+    }
 }
 
 template <class KT>
@@ -85,35 +110,42 @@ __global__ void __launch_bounds__(kHeadThreads) k_head_compact(
     const uint64_t* __restrict__ partial, uint64_t* __restrict__ ckey, uint32_t* __restrict__ cstart,
     uint32_t* __restrict__ crun, uint32_t* __restrict__ cjob, uint32_t* __restrict__ rfeat,
     uint32_t* __restrict__ rstart, uint32_t* __restrict__ rcell, uint32_t* __restrict__ scell) {
-    const uint64_t base = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)threadIdx.x * kHeadItems;
-    uint64_t fl[kHeadItems];
+    __shared__ uint64_t s_tot[kHeadWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t seg = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)w * (32 * kHeadRounds);
+    uint32_t chb[kHeadRounds], rhb[kHeadRounds];
+    head_ballots(seg, n, keys, sfeat, lane, chb, rhb);
     uint64_t v = 0;
 #pragma unroll
-    for (int i = 0; i < kHeadItems; ++i) {
-        fl[i] = head_flags(base + i, n, keys, sfeat);
-        v += fl[i];
-    }
-    uint64_t tot;
-    uint64_t ex = block_excl_scan<uint64_t>(v, &tot) + partial[blockIdx.x];
+    for (int r = 0; r < kHeadRounds; ++r) v += ((uint64_t)__popc(chb[r]) << 32) + (uint64_t)__popc(rhb[r]);
+    if (lane == 0) s_tot[w] = v;
+    __syncthreads();
+    uint64_t ex = partial[blockIdx.x];
+    for (int i = 0; i < w; ++i) ex += s_tot[i];
+    uint32_t cb = (uint32_t)(ex >> 32), rb = (uint32_t)ex;   // heads before this round
+    const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
-    for (int i = 0; i < kHeadItems; ++i) {
-        const uint64_t p = base + i;
-        if (p >= n) break;
-        const uint32_t ch = (uint32_t)(fl[i] >> 32), rh = (uint32_t)fl[i];
-        const uint32_t c = (uint32_t)(ex >> 32) + ch - 1, r = (uint32_t)ex;
-        scell[p] = c;
-        if (ch) {
-            ckey[c] = keys[p];
-            cstart[c] = (uint32_t)p;
-            crun[c] = r;
-            cjob[c] = fjob[sfeat[p]];
+    for (int r = 0; r < kHeadRounds; ++r) {
+        const uint64_t p = seg + (uint64_t)r * 32 + lane;
+        const bool ch = chb[r] >> lane & 1u, rh = rhb[r] >> lane & 1u;
+        const uint32_t c = cb + __popc(chb[r] & lt) + (ch ? 1u : 0u) - 1u;   // the cell of p
+        const uint32_t ri = rb + __popc(rhb[r] & lt);
+        if (p < n) {
+            scell[p] = c;
+            if (ch) {
+                ckey[c] = keys[p];
+                cstart[c] = (uint32_t)p;
+                crun[c] = ri;
+                cjob[c] = fjob[sfeat[p]];
+            }
+            if (rh) {
+                rfeat[ri] = sfeat[p];
+                rstart[ri] = (uint32_t)p;
+                rcell[ri] = c;
+            }
         }
-        if (rh) {
-            rfeat[r] = sfeat[p];
-            rstart[r] = (uint32_t)p;
-            rcell[r] = c;
-        }
-        ex += fl[i];
+        cb += __popc(chb[r]);
+        rb += __popc(rhb[r]);
     }
 }
 
@@ -202,39 +234,84 @@ __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint3
     qfirst[c] = (uint8_t)qf;
 }
 
-// Per cell and mask word: the feature masks of the four quads (2x2 cell
-// blocks) containing the cell, qmask[(c*4 + q)*W + w] with q = (qy+1)*2 +
-// (qx+1) for the quad whose lower-left cell is (cx+qx, cy+qy), qx, qy in
-// {-1, 0} -- q ascends in the quads' (by, bx) order.  A quad outside
-// 0 <= bx <= gx-2, 0 <= by <= gy-2 gets an empty mask, so it is never full.
+// Per cell: the feature masks of the four quads (2x2 cell blocks) containing
+// the cell, qmask[(c*4 + q)*W + w] with q = (qy+1)*2 + (qx+1) for the quad
+// whose lower-left cell is (cx+qx, cy+qy), qx, qy in {-1, 0} -- q ascends in
+// the quads' (by, bx) order.  A quad outside 0 <= bx <= gx-2,
+// 0 <= by <= gy-2 gets an empty mask, so it is never full.
 // nbmask[c*W + w] = union of the masks of the occupied cells of c's 3x3 block.
-__global__ void k_quad_masks(uint64_t M, uint32_t W, const uint64_t* __restrict__ ckey,
-                             const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
-                             const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
-                             uint32_t* __restrict__ qmask, uint32_t* __restrict__ nbmask) {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= M * W) return;
-    const uint64_t c = t / W;
-    const uint32_t w = (uint32_t)(t % W);
+// One thread per cell and WT mask words (WT = W); rows are read and written
+// as 16-byte vectors when W is a multiple of 4.
+template <int WT>
+__device__ __forceinline__ void ld_row(const uint32_t* __restrict__ p, uint32_t (&o)[WT]) {
+    if constexpr (WT % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT / 4; ++i) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(p) + i);
+            o[4 * i] = v.x;
+            o[4 * i + 1] = v.y;
+            o[4 * i + 2] = v.z;
+            o[4 * i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < WT; ++i) o[i] = __ldg(p + i);
+    }
+}
+
+template <int WT>
+__device__ __forceinline__ void st_row(uint32_t* __restrict__ p, const uint32_t (&v)[WT]) {
+    if constexpr (WT % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT / 4; ++i)
+            reinterpret_cast<uint4*>(p)[i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < WT; ++i) p[i] = v[i];
+    }
+}
+
+template <int WT>
+__global__ void k_quad_masks(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+                             const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
+                             const uint32_t* __restrict__ cmask, uint32_t* __restrict__ qmask,
+                             uint32_t* __restrict__ nbmask) {
+    const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M) return;
     const JobGrid g = grids[cjob[c]];
     const uint64_t local = ckey[c] - g.key_base;
     const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
-    uint32_t m[9];
-    uint32_t all = 0;
+    int32_t nb[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) nb[q] = nb9[c * 9 + q];
+    uint32_t m[9][WT];
+    uint32_t all[WT];
+#pragma unroll
+    for (int w = 0; w < WT; ++w) all[w] = 0;
+#pragma unroll
     for (int q = 0; q < 9; ++q) {
-        int32_t v = nb9[c * 9 + q];
-        m[q] = v >= 0 ? cmask[(uint64_t)v * W + w] : 0u;
-        all |= m[q];
+        if (nb[q] >= 0) {
+            ld_row<WT>(cmask + (uint64_t)nb[q] * WT, m[q]);
+        } else {
+#pragma unroll
+            for (int w = 0; w < WT; ++w) m[q][w] = 0;
+        }
+#pragma unroll
+        for (int w = 0; w < WT; ++w) all[w] |= m[q][w];
     }
-    nbmask[t] = all;
+    st_row<WT>(nbmask + c * WT, all);
+#pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
         const int64_t bx = cx + qx, by = cy + qy;
-        uint32_t qm = 0;
-        if (bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy)
-            qm = m[(qy + 1) * 3 + qx + 1] | m[(qy + 1) * 3 + qx + 2] | m[(qy + 2) * 3 + qx + 1] |
-                 m[(qy + 2) * 3 + qx + 2];
-        qmask[(c * 4 + q) * W + w] = qm;
+        const bool valid = bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy;
+        uint32_t qm[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w)
+            qm[w] = valid ? (m[(qy + 1) * 3 + qx + 1][w] | m[(qy + 1) * 3 + qx + 2][w] | m[(qy + 2) * 3 + qx + 1][w] |
+                             m[(qy + 2) * 3 + qx + 2][w])
+                          : 0u;
+        st_row<WT>(qmask + (c * 4 + q) * WT, qm);
     }
 }
 
@@ -567,9 +644,25 @@ void bucket_points(Batch& b) {
     b.qmask.alloc((uint64_t)M * 4 * b.W, s);
     {
         KScope ks("quad_masks");
-        k_quad_masks<<<grid_for((uint64_t)M * b.W, 256), 256, 0, s>>>(M, b.W, b.ckey.get(), b.cjob.get(),
-                                                                     b.grids.get(), b.nb9.get(), b.cmask.get(),
-                                                                     b.qmask.get(), b.nbmask.get());
+#define COLO_QM(WW)                                                                                    \
+    k_quad_masks<WW><<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), \
+                                                      b.cmask.get(), b.qmask.get(), b.nbmask.get())
+        switch (b.W) {
+            case 1: COLO_QM(1); break;
+            case 2: COLO_QM(2); break;
+            case 3: COLO_QM(3); break;
+            case 4: COLO_QM(4); break;
+            case 5: COLO_QM(5); break;
+            case 6: COLO_QM(6); break;
+            case 7: COLO_QM(7); break;
+            case 8: COLO_QM(8); break;
+            case 12: COLO_QM(12); break;
+            case 16: COLO_QM(16); break;
+            case 24: COLO_QM(24); break;
+            case 32: COLO_QM(32); break;
+            default: throw StatusError{COLO_ERR_CAPACITY, "the quad filter handles at most 1024 features per job"};
+        }
+#undef COLO_QM
         COLO_LAUNCH_CHECK();
         count_launch();
     }

@@ -28,7 +28,8 @@ namespace {
 
 constexpr int kFilterThreads = 256;
 constexpr int kFilterWarps = kFilterThreads / 32;
-constexpr int kMaxW = 8;   // mask words handled in registers (256 features per job)
+constexpr int kMaxW = 32;  // mask words per cell (1024 features per job); rows of 9+ words are padded
+                           // to 12, 16, 24 or 32 words when the batch is set up
 constexpr uint64_t kAccMax = 16384;   // block-private level sums (64 KB of shared memory)
 
 // One thread per run (C, f); a block owns a contiguous range of runs, so the
@@ -100,6 +101,40 @@ __device__ __forceinline__ bool covers(const uint32_t* __restrict__ qm, const ui
     return ok;
 }
 
+template <int WT>
+__device__ __forceinline__ bool covers(const uint32_t (&qm)[WT], const uint32_t (&need)[WT]) {
+    bool ok = true;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) ok &= (qm[w] & need[w]) == need[w];
+    return ok;
+}
+
+// One mask row of WT words; rows start on a multiple of WT words from a
+// 256-byte-aligned base, so 4-word rows load as one 16-byte vector.
+template <int WT>
+__device__ __forceinline__ void load_row(const uint32_t* __restrict__ p, uint32_t (&out)[WT]) {
+    if constexpr (WT % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT / 4; ++i) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(p) + i);
+            out[4 * i] = v.x;
+            out[4 * i + 1] = v.y;
+            out[4 * i + 2] = v.z;
+            out[4 * i + 3] = v.w;
+        }
+    } else if constexpr (WT % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT / 2; ++i) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(p) + i);
+            out[2 * i] = v.x;
+            out[2 * i + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < WT; ++i) out[i] = __ldg(p + i);
+    }
+}
+
 // Position of the r-th set bit (r < popc(v)) of v.
 __device__ __forceinline__ uint32_t select_bit(uint32_t v, uint32_t r) {
     uint32_t pos = 0;
@@ -157,7 +192,7 @@ __device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, int lane) {
 // candidates and millions of hits, and global atomics on the same few
 // addresses serialise in their L2 slice.
 template <int WT>
-__global__ void __launch_bounds__(256) k_filter_cells(
+__global__ void __launch_bounds__(256, (WT <= 8 ? 5 : 1)) k_filter_cells(
     uint64_t M, const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
     const uint32_t* __restrict__ nbmask, const uint32_t* __restrict__ dmask,
     const uint32_t* __restrict__ drv_count, const uint32_t* __restrict__ drv_start,
@@ -173,22 +208,44 @@ __global__ void __launch_bounds__(256) k_filter_cells(
     for (uint32_t i = threadIdx.x; i < acc_n; i += blockDim.x) acc[i] = 0;
     __syncthreads();
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    for (uint64_t zbase = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; zbase < M;
-         zbase += nwarps * 32) {
+    // the next chunk's job and 3x3 mask are loaded before this chunk is
+    // processed, so their latency overlaps this chunk's work
+    const uint64_t zstride = nwarps * 32;
+    uint64_t zbase = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+    uint32_t job_c = 0, nb_c[WT];
+#pragma unroll
+    for (int w = 0; w < WT; ++w) nb_c[w] = 0;
+    if (zbase + lane < M) {
+        job_c = cjob[zbase + lane];
+        load_row<WT>(nbmask + (zbase + lane) * W, nb_c);
+    }
+    for (; zbase < M; zbase += zstride) {
+        const uint64_t Zn = zbase + zstride + lane;
+        uint32_t job_n = 0, nb_n[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w) nb_n[w] = 0;
+        if (Zn < M) {
+            job_n = cjob[Zn];
+            load_row<WT>(nbmask + Zn * W, nb_n);
+        }
         // this lane's cell and the drivers of its 3x3 block
         const uint64_t Z = zbase + lane;
         uint32_t dz[WT], f0 = 0, nd = 0;
 #pragma unroll
         for (int w = 0; w < WT; ++w) dz[w] = 0;
         if (Z < M) {
-            const uint32_t job = cjob[Z];
-            f0 = grids[job].f0;
+            f0 = grids[job_c].f0;
+            uint32_t dm[WT];
+            load_row<WT>(dmask + (uint64_t)job_c * W, dm);
 #pragma unroll
             for (int w = 0; w < WT; ++w) {
-                dz[w] = nbmask[Z * W + w] & dmask[(uint64_t)job * W + w];
+                dz[w] = nb_c[w] & dm[w];
                 nd += __popc(dz[w]);
             }
         }
+        job_c = job_n;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) nb_c[w] = nb_n[w];
         const uint32_t pincl = warp_incl_sum(nd, lane);
         const uint32_t pex = pincl - nd;
         const uint32_t npairs = __shfl_sync(0xffffffffu, pincl, 31);
@@ -230,23 +287,25 @@ __global__ void __launch_bounds__(256) k_filter_cells(
                 if (it >= nitems) continue;
                 const uint32_t c = order[st2 + (it - ex2)];
                 uint32_t need[WT];
-#pragma unroll
-                for (int w = 0; w < WT; ++w) need[w] = need_all[(uint64_t)c * W + w];
+                load_row<WT>(need_all + (uint64_t)c * W, need);
                 const uint32_t* q4 = qmask + Zi * 4 * W;
                 uint32_t full = 0;
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (covers<WT>(q4 + q * W, need)) full |= 1u << q;
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t qm[WT];
+                    load_row<WT>(q4 + q * W, qm);
+                    if (covers<WT>(qm, need)) full |= 1u << q;
+                }
                 if (!full) continue;
                 uint32_t cm[WT];
-#pragma unroll
-                for (int w = 0; w < WT; ++w) cm[w] = cmask[Zi * W + w];
+                load_row<WT>(cmask + Zi * W, cm);
                 const uint32_t q0 = crun[Zi];
-                const uint32_t lm[2] = {lmem[(uint64_t)c * 2], lmem[(uint64_t)c * 2 + 1]};
+                uint32_t lm[4];
+                load_row<4>(lmem + (uint64_t)c * 4, lm);
 #pragma unroll
                 for (int jj = 0; jj < kMaxMembersFiltered; ++jj) {
                     if ((uint32_t)jj >= m) break;
-                    const uint32_t lf = (lm[jj >> 2] >> ((jj & 3) * 8)) & 0xFFu, wq = lf >> 5;
+                    const uint32_t lf = (lm[jj >> 1] >> ((jj & 1) * 16)) & 0xFFFFu, wq = lf >> 5;
                     uint32_t rk = 0, word = 0;
 #pragma unroll
                     for (int w = 0; w < WT; ++w) {
@@ -291,7 +350,7 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     ub2.alloc(job_off[b.J] ? job_off[b.J] : 1, s);
     ub2.zero(s);
     if (b.M == 0) return;
-    if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 256 features per job"};
+    if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 1024 features per job"};
     DevBuf<uint64_t> d_job_off;
     d_job_off.alloc(b.J + 1, s);
     COLO_CUDA(cudaMemcpyAsync(d_job_off.get(), job_off.data(), (b.J + 1) * 8, cudaMemcpyHostToDevice, s));
@@ -323,13 +382,13 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
                   uint32_t* d_ub, unsigned long long* d_stats, const uint32_t* d_cand_in) {
     (void)d_cand_in;
     if (ncand == 0) return;
-    if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 256 features per job"};
+    if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 1024 features per job"};
     cudaStream_t s = b.s;
     const uint32_t m = k < kMaxMembersFiltered ? k : (uint32_t)kMaxMembersFiltered;
     // driver = member with the fewest cells; candidates grouped by driver;
     // per candidate its need mask and local member ids (bytes), per job the
     // mask of its drivers
-    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0), lmem((size_t)ncand * 2, 0),
+    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0), lmem((size_t)ncand * 4, 0),
         dmask((size_t)b.J * b.W, 0);
     for (uint64_t c = 0; c < ncand; ++c) {
         const uint32_t* mem = h_cand + c * k;
@@ -343,7 +402,7 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
             }
             uint32_t lf = mem[j] - f0;
             need[(size_t)c * b.W + (lf >> 5)] |= 1u << (lf & 31);
-            lmem[(size_t)c * 2 + (j >> 2)] |= lf << ((j & 3) * 8);
+            lmem[(size_t)c * 4 + (j >> 1)] |= lf << ((j & 1) * 16);
         }
         drv[c] = best;
         const uint32_t ld = best - f0;
@@ -361,13 +420,18 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     for (uint32_t f = 0; f < b.F; ++f) nitems += (uint64_t)dcount[f] * (b.h_frun_off[f + 1] - b.h_frun_off[f]);
     b.filter_items += nitems;
     if (nitems == 0) return;
-    // one upload: need | lmem | dmask | dcount | dstart | order
-    const size_t n_need = need.size(), n_lmem = lmem.size(), n_dm = dmask.size();
+    // one upload: need | lmem | dmask | dcount | dstart | order, each part on a
+    // 16-byte boundary (mask rows are read as vectors)
+    auto up4 = [](size_t v) { return (v + 3) & ~(size_t)3; };
+    const size_t n_need = up4(need.size()), n_lmem = up4(lmem.size()), n_dm = up4(dmask.size());
     std::vector<uint32_t> pack;
     pack.reserve(n_need + n_lmem + n_dm + 2 * (size_t)b.F + ncand);
     pack.insert(pack.end(), need.begin(), need.end());
+    pack.resize(n_need, 0);
     pack.insert(pack.end(), lmem.begin(), lmem.end());
+    pack.resize(n_need + n_lmem, 0);
     pack.insert(pack.end(), dmask.begin(), dmask.end());
+    pack.resize(n_need + n_lmem + n_dm, 0);
     pack.insert(pack.end(), dcount.begin(), dcount.end());
     pack.insert(pack.end(), dstart.begin(), dstart.end());
     pack.insert(pack.end(), order.begin(), order.end());
@@ -407,7 +471,12 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
         case 5: COLO_FL(5); break;
         case 6: COLO_FL(6); break;
         case 7: COLO_FL(7); break;
-        default: COLO_FL(8); break;
+        case 8: COLO_FL(8); break;
+        case 12: COLO_FL(12); break;
+        case 16: COLO_FL(16); break;
+        case 24: COLO_FL(24); break;
+        case 32: COLO_FL(32); break;
+        default: throw StatusError{COLO_ERR_INTERNAL, "mask words not padded to a supported width"};
     }
 #undef COLO_FL
     COLO_LAUNCH_CHECK();

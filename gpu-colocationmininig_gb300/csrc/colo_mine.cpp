@@ -319,7 +319,10 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
         p0 += ds->hp.x.size();
         b.Fmax_local = std::max(b.Fmax_local, g.nf);
     }
+    // mask words per cell: 1..8, else padded to 12, 16, 24 or 32 (the widths
+    // the mask kernels are built for; up to 1024 features per job)
     b.W = (b.Fmax_local + 31) / 32;
+    if (b.W > 8) b.W = b.W <= 12 ? 12 : b.W <= 16 ? 16 : b.W <= 24 ? 24 : b.W <= 32 ? 32 : b.W;
     b.key_bits = 1;
     while (b.key_bits < 64 && (1ull << b.key_bits) < key_base) b.key_bits++;
     b.fstart.alloc(b.F ? b.F : 1, s);

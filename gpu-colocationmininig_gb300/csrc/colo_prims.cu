@@ -15,13 +15,18 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
+// A tile of kScanTile items is eight warp segments of 256; a warp reads its
+// segment 32 consecutive items per round (coalesced loads and stores).
 template <class Tin, class Tout>
 __global__ void k_tile_sums(const Tin* __restrict__ in, uint64_t n, Tout* __restrict__ partial) {
-    uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t seg = (uint64_t)blockIdx.x * kScanTile + (uint64_t)w * (32 * kScanItems);
     Tout s = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i)
-        if (base + i < n) s += (Tout)in[base + i];
+    for (int i = 0; i < kScanItems; ++i) {
+        const uint64_t p = seg + (uint64_t)i * 32 + lane;
+        if (p < n) s += (Tout)in[p];
+    }
     Tout tot;
     block_excl_scan<Tout>(s, &tot);
     if (threadIdx.x == 0) partial[blockIdx.x] = tot;
@@ -55,20 +60,27 @@ __global__ void k_scan_partials(T* partial, uint64_t m) {
 template <class Tin, class Tout>
 __global__ void k_scan_tiles(const Tin* __restrict__ in, Tout* __restrict__ out, uint64_t n,
                              const Tout* __restrict__ partial) {
-    uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t seg = (uint64_t)blockIdx.x * kScanTile + (uint64_t)w * (32 * kScanItems);
     Tout v[kScanItems];
     Tout s = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        v[i] = (base + i < n) ? (Tout)in[base + i] : Tout(0);
+        const uint64_t p = seg + (uint64_t)i * 32 + lane;
+        v[i] = p < n ? (Tout)in[p] : Tout(0);
         s += v[i];
     }
+    // the block's exclusive prefix at this warp's segment: the scan of the
+    // threads' sums, taken at the warp's first lane
     Tout tot;
-    Tout ex = block_excl_scan<Tout>(s, &tot) + partial[blockIdx.x];
+    const Tout ex_thread = block_excl_scan<Tout>(s, &tot);
+    Tout carry = __shfl_sync(0xffffffffu, ex_thread, 0) + partial[blockIdx.x];
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        if (base + i < n) out[base + i] = ex;
-        ex += v[i];
+        const Tout inc = warp_incl_scan(v[i]);
+        const uint64_t p = seg + (uint64_t)i * 32 + lane;
+        if (p < n) out[p] = carry + inc - v[i];
+        carry += __shfl_sync(0xffffffffu, inc, 31);
     }
 }
 
@@ -192,8 +204,10 @@ __global__ void k_digit_scan(unsigned long long* __restrict__ ghist, int passes)
     }
 }
 
+// Six resident blocks per SM (40 registers for 32-bit keys): the look-back
+// and the tile's dependent loads are latency, so more tiles in flight help.
 template <class KT, int RB>
-__global__ void __launch_bounds__(kSortThreads) k_onesweep(
+__global__ void __launch_bounds__(kSortThreads, 6) k_onesweep(
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
     uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
     unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
@@ -394,6 +408,9 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
     uint32_t* va = vals.get();
     KT* kb = k2.get();
     uint32_t* vb = v2.get();
+    // six blocks of ~28 KB per SM: ask for the largest shared-memory carveout
+    COLO_CUDA(cudaFuncSetAttribute((const void*)k_onesweep<KT, kMaxRadixBits>,
+                                   cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
     for (int p = 0; p < plan.n; ++p) {
         KScope ks(name);   // one timed launch per digit pass
         const uint32_t dm = (1u << plan.width[p]) - 1u;

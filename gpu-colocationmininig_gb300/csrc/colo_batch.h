@@ -45,6 +45,8 @@ struct Batch {
     // cells
     DevBuf<uint64_t> ckey;
     DevBuf<uint32_t> cstart, crun, cjob;
+    uint64_t rows = 0;           // grid rows of all jobs (row table size - 1)
+    DevBuf<uint32_t> rowstart;   // per grid row: first occupied cell at or after the row (empty when too large)
     DevBuf<int32_t> nb9;
     DevBuf<uint32_t> cmask;
     DevBuf<uint32_t> nbmask;     // per cell: feature mask of its geometric 3x3 block

@@ -171,6 +171,28 @@ __global__ void k_cell_masks(uint64_t Rn, const uint32_t* __restrict__ rfeat,
     atomicOr(&cmask[(uint64_t)c * W + (lf >> 5)], 1u << (lf & 31));
 }
 
+// rowstart[Y] = first occupied cell whose key is at or after the first key of
+// grid row Y (rows of all jobs, job j's row y at Y = row_base_j + y);
+// rowstart[rows] = M.
+__global__ void k_row_starts(uint64_t rows, uint32_t J, uint64_t M, const uint64_t* __restrict__ ckey,
+                             const JobGrid* __restrict__ grids, uint32_t* __restrict__ rowstart) {
+    const uint64_t Y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (Y > rows) return;
+    if (Y == rows) {
+        rowstart[Y] = (uint32_t)M;
+        return;
+    }
+    uint32_t lo = 0, hi = J;   // last job whose first row is <= Y
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (grids[mid].row_base <= Y) lo = mid;
+        else hi = mid;
+    }
+    const JobGrid g = grids[lo];
+    const uint64_t key = g.key_base + (Y - g.row_base) * g.gx;
+    rowstart[Y] = (uint32_t)lower_bound_dev(ckey, (uint64_t)0, M, key);
+}
+
 // nb9[c*9 + (dy+1)*3 + (dx+1)] = occupied index of the geometric neighbour
 // (cx+dx, cy+dy) inside the job's grid, or -1.  Keys ascend along a grid row,
 // so the row of the cell itself is read from the adjacent entries and each
@@ -181,8 +203,11 @@ __global__ void k_cell_masks(uint64_t Rn, const uint32_t* __restrict__ rfeat,
 // has lower-left cell (cx+qx, cy+qy), qx = (q & 1) - 1, qy = (q >> 1) - 1, and
 // holds c at corner (ex, ey) = (-qx, -qy); quads outside 0 <= bx <= gx-2,
 // 0 <= by <= gy-2 are never full and get no bit.
+// rowstart (optional, rows + 1 entries) bounds the search of a row to the
+// cells of that row.
 __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                      const JobGrid* __restrict__ grids, int32_t* __restrict__ nb9, uint8_t* __restrict__ qfirst) {
+                      const JobGrid* __restrict__ grids, const uint32_t* __restrict__ rowstart,
+                      int32_t* __restrict__ nb9, uint8_t* __restrict__ qfirst) {
     uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M) return;
     const JobGrid g = grids[cjob[c]];
@@ -202,7 +227,13 @@ __global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint3
         } else if (ny >= 0 && ny < (int64_t)g.gy) {
             const uint64_t k0 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x0;
             const uint64_t k1 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x1;
-            uint64_t pos = dy < 0 ? lower_bound_dev(ckey, (uint64_t)0, c, k0) : lower_bound_dev(ckey, c + 1, M, k0);
+            uint64_t lo = dy < 0 ? 0 : c + 1, hi = dy < 0 ? c : M;
+            if (rowstart) {
+                const uint64_t Y = g.row_base + (uint64_t)ny;
+                lo = rowstart[Y];
+                hi = rowstart[Y + 1];
+            }
+            uint64_t pos = lower_bound_dev(ckey, lo, hi, k0);
             for (; pos < M && ckey[pos] <= k1; ++pos) {
                 const int64_t dx = (int64_t)(ckey[pos] - g.key_base - (uint64_t)ny * g.gx) - cx;
                 if (dx < 0) v0 = (int32_t)pos;
@@ -635,8 +666,18 @@ void bucket_points(Batch& b) {
     b.qfirst.alloc(M, s);
     {
         KScope ks("cell_neighbours");
-        k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
-                                               b.qfirst.get());
+        // the row table when it is not much larger than the cell list
+        const bool table = b.rows < (1ull << 31) && b.rows <= 4 * (uint64_t)M + (1u << 20);
+        b.rowstart.release();
+        if (table) {
+            b.rowstart.alloc(b.rows + 1, s);
+            k_row_starts<<<grid_for(b.rows + 1, 256), 256, 0, s>>>(b.rows, b.J, M, b.ckey.get(), b.grids.get(),
+                                                                  b.rowstart.get());
+            COLO_LAUNCH_CHECK();
+            count_launch();
+        }
+        k_nb9<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(),
+                                               table ? b.rowstart.get() : nullptr, b.nb9.get(), b.qfirst.get());
         COLO_LAUNCH_CHECK();
         count_launch();
     }

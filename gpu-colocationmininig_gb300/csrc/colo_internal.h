@@ -38,6 +38,7 @@ struct JobGrid {
     uint32_t gx, gy;
     uint64_t total;              // gx*gy
     uint64_t key_base;           // first cell key of this job in the batch
+    uint64_t row_base;           // first grid row of this job in the batch's row table
     int32_t compat32;            // 32-bit reference cell arithmetic is exact
     uint32_t f0, nf;             // global feature range of the job
 };

@@ -299,7 +299,7 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     b.h_fcount.resize(b.F);
     b.h_fjob.resize(b.F);
     b.jobs.resize(J);
-    uint64_t key_base = 0, p0 = 0;
+    uint64_t key_base = 0, p0 = 0, row_base = 0;
     b.Fmax_local = 1;
     for (uint32_t j = 0; j < J; ++j) {
         colo_dataset* ds = dsv[j];
@@ -310,9 +310,11 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
         }
         JobGrid g = make_grid(ds->hp.bounds, pv[j].distance, pv[j].pi_threshold);
         g.key_base = key_base;
+        g.row_base = row_base;
         g.f0 = job_f0[j];
         g.nf = (uint32_t)ds->names.size();
         key_base += g.total;
+        row_base += g.gy;
         b.jobs[j].grid = g;
         b.jobs[j].p0 = p0;
         b.jobs[j].np = ds->hp.x.size();
@@ -325,6 +327,7 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     if (b.W > 8) b.W = b.W <= 12 ? 12 : b.W <= 16 ? 16 : b.W <= 24 ? 24 : b.W <= 32 ? 32 : b.W;
     b.key_bits = 1;
     while (b.key_bits < 64 && (1ull << b.key_bits) < key_base) b.key_bits++;
+    b.rows = row_base;
     b.fstart.alloc(b.F ? b.F : 1, s);
     b.fcount.alloc(b.F ? b.F : 1, s);
     b.fjob.alloc(b.F ? b.F : 1, s);

@@ -34,7 +34,6 @@ struct Batch {
     // points (by id)
     const float* x = nullptr;    // borrowed (dataset device copy)
     const float* y = nullptr;
-    const uint32_t* feat = nullptr;
     DevBuf<uint32_t> fstart, fcount, fjob;
     DevBuf<JobGrid> grids;
     DevBuf<DevFlags> flags;
@@ -45,6 +44,7 @@ struct Batch {
     // cells
     DevBuf<uint64_t> ckey;
     DevBuf<uint32_t> cstart, crun, cjob;
+    uint64_t h2d_points = 0;     // bytes of point data copied to the device for this batch
     uint64_t rows = 0;           // grid rows of all jobs (row table size - 1)
     DevBuf<uint32_t> rowstart;   // per grid row: first occupied cell at or after the row (empty when too large)
     DevBuf<int32_t> nb9;

@@ -13,23 +13,61 @@
 namespace colo {
 namespace {
 
-template <class KT>
-__global__ void k_cell_keys(uint64_t n, const float* __restrict__ x, const float* __restrict__ y,
-                            const uint32_t* __restrict__ feat, const uint32_t* __restrict__ fjob,
-                            const JobGrid* __restrict__ grids, KT* __restrict__ keys,
-                            uint32_t* __restrict__ vals, float2* __restrict__ xy, DevFlags* flags) {
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const JobGrid g = grids[fjob[feat[i]]];
-    const float xi = x[i], yi = y[i];
-    xy[i] = make_float2(xi, yi);
-    uint64_t c = ref_cell(g, xi, yi);
-    if (c >= g.total) {
-        atomicAdd(&flags->out_of_grid, 1u);
-        c = g.total - 1;
+// Cell keys, point ids and packed coordinates, and the digit histograms of
+// every radix pass over the keys (block-private counts added to hist once
+// per block), so the sort does not read the keys again to count them.
+// A point's feature is the last feature whose first point is at or before it
+// (points are grouped by feature); the start table stays in L1.
+__device__ __forceinline__ uint32_t feature_of(uint32_t id, uint32_t F, const uint32_t* __restrict__ fstart) {
+    uint32_t lo = 0, hi = F;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (fstart[mid] <= id) lo = mid;
+        else hi = mid;
     }
-    keys[i] = (KT)(g.key_base + c);
-    vals[i] = (uint32_t)i;
+    return lo;
+}
+
+template <class KT>
+__global__ void __launch_bounds__(256) k_cell_keys(
+    uint64_t n, const float* __restrict__ x, const float* __restrict__ y, uint32_t F,
+    const uint32_t* __restrict__ fstart, const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids,
+    KT* __restrict__ keys, uint32_t* __restrict__ vals, float2* __restrict__ xy, DevFlags* flags, RadixPlan plan,
+    unsigned long long* __restrict__ hist) {
+    __shared__ uint32_t h[kRadixMaxPasses * kRadixDigits];
+    for (int i = threadIdx.x; i < plan.n * kRadixDigits; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    // each block takes one contiguous range of points (coalesced, and a
+    // thread's successive points are blockDim apart, so the feature found for
+    // one point usually covers the next)
+    const uint64_t per = ((n + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
+    const uint64_t i0 = (uint64_t)blockIdx.x * per, i1 = i0 + per < n ? i0 + per : n;
+    uint32_t f = 0, flo = 1, fhi = 0;   // cached feature and its point range [flo, fhi)
+    for (uint64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        if (!(i >= flo && i < fhi)) {
+            f = feature_of((uint32_t)i, F, fstart);
+            flo = fstart[f];
+            fhi = f + 1 < F ? fstart[f + 1] : (uint32_t)n;
+        }
+        const JobGrid g = grids[fjob[f]];
+        const float xi = x[i], yi = y[i];
+        xy[i] = make_float2(xi, yi);
+        uint64_t c = ref_cell(g, xi, yi);
+        if (c >= g.total) {
+            atomicAdd(&flags->out_of_grid, 1u);
+            c = g.total - 1;
+        }
+        const KT key = (KT)(g.key_base + c);
+        keys[i] = key;
+        vals[i] = (uint32_t)i;
+        for (int p = 0; p < plan.n; ++p)
+            atomicAdd(&h[p * kRadixDigits + ((uint32_t)(key >> plan.shift[p]) & ((1u << plan.width[p]) - 1u))], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < plan.n * kRadixDigits; i += blockDim.x) {
+        const uint32_t v = h[i];
+        if (v) atomicAdd(&hist[i], (unsigned long long)v);
+    }
 }
 
 // Sorted copies: coordinates gathered as one 8-byte load; the feature of a
@@ -42,13 +80,7 @@ __global__ void k_gather_sorted(uint64_t n, uint32_t F, const uint32_t* __restri
     if (p >= n) return;
     const uint32_t id = sid[p];
     sxy[p] = xy[id];
-    uint32_t lo = 0, hi = F;   // last feature whose start is <= id
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (fstart[mid] <= id) lo = mid;
-        else hi = mid;
-    }
-    sfeat[p] = lo;
+    sfeat[p] = feature_of(id, F, fstart);
 }
 
 // Cell and run heads in the sorted order, counted and compacted in two
@@ -587,15 +619,22 @@ void sort_and_compact(Batch& b) {
     DevBuf<KT> keys;
     keys.alloc(n, s);
     b.sid.alloc(n, s);
+    const int bits = sizeof(KT) == 4 && b.key_bits > 32 ? 32 : (int)b.key_bits;
+    const RadixPlan plan = radix_plan(bits);
+    DevBuf<unsigned long long> hist;
+    hist.alloc((uint64_t)(plan.n > 0 ? plan.n : 1) * kRadixDigits, s);
+    hist.zero(s);
     {
     KScope ks("cell_keys");
     b.xy.alloc(n, s);
-    k_cell_keys<KT><<<grid_for(n, 256), 256, 0, s>>>(n, b.x, b.y, b.feat, b.fjob.get(), b.grids.get(),
-                                                      keys.get(), b.sid.get(), b.xy.get(), b.flags.get());
+    const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)b.sms * 8);
+    k_cell_keys<KT><<<(unsigned)(blocks ? blocks : 1), 256, 0, s>>>(n, b.x, b.y, b.F, b.fstart.get(), b.fjob.get(), b.grids.get(),
+                                                                    keys.get(), b.sid.get(), b.xy.get(), b.flags.get(),
+                                                                    plan, hist.get());
     COLO_LAUNCH_CHECK();
     count_launch();
     }
-    radix_sort(keys, b.sid, n, (int)b.key_bits, s);
+    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get());
 
     b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);

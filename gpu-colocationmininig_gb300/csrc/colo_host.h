@@ -89,7 +89,6 @@ struct colo_dataset {
     std::vector<std::string> names;
     std::vector<uint32_t> fstart, fcount;
     colo::DevBuf<float> dx, dy;
-    colo::DevBuf<uint32_t> dfeat;
     bool resident = false;
     bool pinned = false;                     // host arrays page-locked for uploads
 };
@@ -105,7 +104,7 @@ void candidate_features(uint32_t k, const uint32_t* mem, const uint32_t* fcount,
 colo_status set_err(colo_ctx* ctx, colo_status st, const std::string& msg);
 void ctx_release(colo_ctx* ctx);
 colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn);
-void upload_dataset(colo_dataset* ds, cudaStream_t s);
+uint64_t upload_dataset(colo_dataset* ds, cudaStream_t s);   // bytes copied (0 when resident)
 // Points, features, job grids and the bucketed/joined device state of a batch.
 // `own` keeps the concatenated device copies of multi-job batches alive.
 void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J, Batch& b,

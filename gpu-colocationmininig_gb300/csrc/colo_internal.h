@@ -220,12 +220,24 @@ void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t
                      uint32_t* total_host);
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host);
+// Digit split of a radix sort: pass p sorts width[p] (<= 8) bits from shift[p].
+constexpr int kRadixDigits = 256;
+constexpr int kRadixMaxPasses = 8;
+struct RadixPlan {
+    int n;
+    int shift[kRadixMaxPasses];
+    int width[kRadixMaxPasses];
+};
+RadixPlan radix_plan(int bits);
 // Stable LSD radix sort of (key, val) pairs by the low `bits` bits of key.
 // The sorted pairs are in keys/vals on return (the buffers may have been
 // exchanged for the sort's second buffers, which avoids a copy back).
+// hist, when given, holds every pass's digit counts of the keys
+// (hist[p * kRadixDigits + d], radix_plan(bits) passes), counted by the
+// caller while it wrote the keys; the sort then skips its own count.
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name = "radix_sort");
+                const char* name = "radix_sort", unsigned long long* hist = nullptr);
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name = "radix_sort");
+                const char* name = "radix_sort", unsigned long long* hist = nullptr);
 
 }  // namespace colo

@@ -119,27 +119,27 @@ colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn) {
     }
 }
 
-void upload_dataset(colo_dataset* ds, cudaStream_t s) {
-    if (ds->resident) return;
+uint64_t upload_dataset(colo_dataset* ds, cudaStream_t s) {
+    if (ds->resident) return 0;
     uint64_t n = ds->hp.x.size();
     if (!ds->pinned && n) {
         // page-lock the host arrays once so every upload is a direct DMA
         bool ok = cudaHostRegister(ds->hp.x.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
         ok = ok && cudaHostRegister(ds->hp.y.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
-        ok = ok && cudaHostRegister(ds->feat.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
         if (!ok) cudaGetLastError();
         ds->pinned = true;
     }
+    // coordinates only: a point's feature follows from the feature start table
+    // (points are grouped by feature), so no per-point feature array is copied
     ds->dx.alloc(n, s);
     ds->dy.alloc(n, s);
-    ds->dfeat.alloc(n, s);
     if (n) {
         COLO_CUDA(cudaMemcpyAsync(ds->dx.get(), ds->hp.x.data(), n * 4, cudaMemcpyHostToDevice, s));
         COLO_CUDA(cudaMemcpyAsync(ds->dy.get(), ds->hp.y.data(), n * 4, cudaMemcpyHostToDevice, s));
-        COLO_CUDA(cudaMemcpyAsync(ds->dfeat.get(), ds->feat.data(), n * 4, cudaMemcpyHostToDevice, s));
     }
     COLO_CUDA(cudaStreamSynchronize(s));
     ds->resident = true;
+    return 8 * n;   // bytes copied
 }
 
 namespace {
@@ -266,33 +266,26 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     b.N = N;
     b.F = job_f0[J];
     if (J == 1) {
-        upload_dataset(dsv[0], s);
+        b.h2d_points = upload_dataset(dsv[0], s);
         b.x = dsv[0]->dx.get();
         b.y = dsv[0]->dy.get();
-        b.feat = dsv[0]->dfeat.get();
     } else {
         ownf.resize(2);
-        ownu.resize(1);
         ownf[0].alloc(N, s);
         ownf[1].alloc(N, s);
-        ownu[0].alloc(N, s);
-        std::vector<uint32_t> tmp;
         uint64_t off = 0;
         for (uint32_t j = 0; j < J; ++j) {
             colo_dataset* ds = dsv[j];
             uint64_t n = ds->hp.x.size();
             if (!n) continue;
-            tmp.resize(n);
-            for (uint64_t i = 0; i < n; ++i) tmp[i] = ds->feat[i] + job_f0[j];
             COLO_CUDA(cudaMemcpyAsync(ownf[0].get() + off, ds->hp.x.data(), n * 4, cudaMemcpyHostToDevice, s));
             COLO_CUDA(cudaMemcpyAsync(ownf[1].get() + off, ds->hp.y.data(), n * 4, cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(ownu[0].get() + off, tmp.data(), n * 4, cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaStreamSynchronize(s));
             off += n;
         }
+        COLO_CUDA(cudaStreamSynchronize(s));
+        b.h2d_points = 8 * N;
         b.x = ownf[0].get();
         b.y = ownf[1].get();
-        b.feat = ownu[0].get();
     }
     if (t_upload) *t_upload = ms_since(t0);
     b.h_fstart.resize(b.F);
@@ -934,7 +927,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->counters[9] = cnt_parent;
         r->counters[10] = cnt_fillw;
         r->counters[11] = cnt_bmw;
-        r->counters[12] = (b.jobs.size() == 1 && t_upload > 0.01) ? 12 * b.N : 0;
+        r->counters[12] = b.h2d_points;
         r->counters[13] = cnt_d2h;
         r->counters[14] = b.nrl_total;
         r->counters[4] = b.join_pairs;
@@ -1148,7 +1141,6 @@ colo_status colo_dataset_evict(colo_dataset* ds) {
     if (!ds) return COLO_ERR_ARG;
     ds->dx.release();
     ds->dy.release();
-    ds->dfeat.release();
     ds->resident = false;
     return COLO_OK;
 }
@@ -1170,7 +1162,6 @@ void colo_dataset_free(colo_dataset* ds) {
     if (ds->pinned && !ds->hp.x.empty()) {
         cudaHostUnregister(ds->hp.x.data());
         cudaHostUnregister(ds->hp.y.data());
-        cudaHostUnregister(ds->feat.data());
         cudaGetLastError();
     }
     delete ds;

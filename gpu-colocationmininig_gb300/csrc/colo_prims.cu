@@ -134,19 +134,14 @@ void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total
 // ---------------------------------------------------------------------------
 
 constexpr int kMaxRadixBits = 8;                        // digits of at most 8 bits
-constexpr int kMaxRadix = 1 << kMaxRadixBits;
-constexpr int kMaxPasses = 8;
+static_assert((1 << kMaxRadixBits) == kRadixDigits, "digit count");
+constexpr int kMaxRadix = kRadixDigits;
+constexpr int kMaxPasses = kRadixMaxPasses;
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortRounds = 8;                          // items per lane
 constexpr int kSortTile = kSortThreads * kSortRounds;   // 2048
 
-// Digit split of the key: pass p sorts `width[p]` bits from `shift[p]`.
-struct PassPlan {
-    int n;
-    int shift[kMaxPasses];
-    int width[kMaxPasses];
-};
 
 // ---------------------------------------------------------------------------
 // One-sweep LSD radix sort: the digit histograms of every pass from one read
@@ -169,7 +164,7 @@ constexpr unsigned long long kValMask = (1ull << 62) - 1;
 constexpr uint32_t kSpinLimit = 1u << 22;
 
 template <class KT>
-__global__ void k_digit_hist(const KT* __restrict__ keys, uint64_t n, PassPlan plan,
+__global__ void k_digit_hist(const KT* __restrict__ keys, uint64_t n, RadixPlan plan,
                              unsigned long long* __restrict__ ghist) {
     __shared__ uint32_t h[kMaxPasses * kMaxRadix];
     for (int i = threadIdx.x; i < plan.n * kMaxRadix; i += blockDim.x) h[i] = 0;
@@ -370,39 +365,36 @@ namespace {
 
 template <class KT>
 void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                     const char* name) {
+                     const char* name, unsigned long long* hist_in) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
-    // fewest passes of at most 8 bits, widths as even as possible (25 bits: 7 + 6 + 6 + 6)
-    PassPlan plan{};
-    plan.n = (bits + kMaxRadixBits - 1) / kMaxRadixBits;
-    for (int p = 0, sh = 0; p < plan.n; ++p) {
-        plan.width[p] = bits / plan.n + (p < bits % plan.n ? 1 : 0);
-        plan.shift[p] = sh;
-        sh += plan.width[p];
-    }
+    const RadixPlan plan = radix_plan(bits);
     const uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     DevBuf<KT> k2;
     DevBuf<uint32_t> v2, tickets, err;
     DevBuf<unsigned long long> ghist, status;
     k2.alloc(n, s);
     v2.alloc(n, s);
-    ghist.alloc((uint64_t)plan.n * kMaxRadix, s);
+    if (!hist_in) ghist.alloc((uint64_t)plan.n * kMaxRadix, s);
+    unsigned long long* hist = hist_in ? hist_in : ghist.get();
     status.alloc((uint64_t)ntiles * kMaxRadix, s);
     tickets.alloc(plan.n, s);
     err.alloc(1, s);
-    ghist.zero(s);
     tickets.zero(s);
     err.zero(s);
     {
         KScope ks("radix_hist");
-        uint64_t blocks = (n + 255) / 256;
-        if (blocks > 1024) blocks = 1024;
-        k_digit_hist<KT><<<(unsigned)blocks, 256, 0, s>>>(keys.get(), n, plan, ghist.get());
+        if (!hist_in) {
+            ghist.zero(s);
+            uint64_t blocks = (n + 255) / 256;
+            if (blocks > 1024) blocks = 1024;
+            k_digit_hist<KT><<<(unsigned)blocks, 256, 0, s>>>(keys.get(), n, plan, hist);
+            COLO_LAUNCH_CHECK();
+            count_launch();
+        }
+        k_digit_scan<<<1, kMaxRadix, 0, s>>>(hist, plan.n);
         COLO_LAUNCH_CHECK();
-        k_digit_scan<<<1, kMaxRadix, 0, s>>>(ghist.get(), plan.n);
-        COLO_LAUNCH_CHECK();
-        count_launch(2);
+        count_launch();
     }
     KT* ka = keys.get();
     uint32_t* va = vals.get();
@@ -416,7 +408,7 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         const uint32_t dm = (1u << plan.width[p]) - 1u;
         COLO_CUDA(cudaMemsetAsync(status.get(), 0, (uint64_t)ntiles * kMaxRadix * 8, s));
         k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
-                                                                     ghist.get() + p * kMaxRadix, status.get(),
+                                                                     hist + p * kMaxRadix, status.get(),
                                                                      tickets.get() + p, err.get());
         COLO_LAUNCH_CHECK();
         count_launch();
@@ -435,14 +427,27 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
 
 }  // namespace
 
+RadixPlan radix_plan(int bits) {
+    // fewest passes of at most 8 bits, widths as even as possible (25 bits: 7 + 6 + 6 + 6)
+    RadixPlan plan{};
+    if (bits <= 0) return plan;
+    plan.n = (bits + kMaxRadixBits - 1) / kMaxRadixBits;
+    for (int p = 0, sh = 0; p < plan.n; ++p) {
+        plan.width[p] = bits / plan.n + (p < bits % plan.n ? 1 : 0);
+        plan.shift[p] = sh;
+        sh += plan.width[p];
+    }
+    return plan;
+}
+
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name) {
-    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name);
+                const char* name, unsigned long long* hist) {
+    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist);
 }
 
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name) {
-    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name);
+                const char* name, unsigned long long* hist) {
+    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist);
 }
 
 }  // namespace colo

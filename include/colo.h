@@ -158,7 +158,8 @@ colo_status colo_result_times(const colo_result* r, double* ms8);
  * higher-feature neighbour cells, [2] neighbour entries E, [3] table rows
  * written, [4] pair distance evaluations in the join, [5] points, [6] occupied cells, [7] runs, [8] slice entries
  * examined by count passes, [9] parent words read by count passes,
- * [10] table words written, [11] bitmap words, [12] host-to-device bytes,
+ * [10] table words written, [11] bitmap words, [12] host-to-device bytes
+ * of point coordinates (0 when the points were resident),
  * [13] device-to-host bytes, [14] neighbourhood-run entries, [15] refined
  * candidates, [16] (driver cell, candidate) items of the level filters,
  * [17] candidates filled in one presized pass, [18] of those, overflowed and

@@ -162,6 +162,36 @@ def cell_key_bits(grids) -> int:
     return bits
 
 
+def measure_io(ctx, wl, ds, params, patterns):
+    """End to end including input I/O: the workload written once (untimed) as the reference's CSV and
+    as a binary point file, then each loaded through the public API and mined (one cold mine: page
+    locking and upload included).  Times in ms from the load call to the result."""
+    import shutil
+    import tempfile
+
+    import colo
+    d = tempfile.mkdtemp(prefix="colo_io_")
+    try:
+        csv, binp = os.path.join(d, "points.csv"), os.path.join(d, "points.colo")
+        ds.write_csv(csv)
+        ds.write_binary(binp)
+        out = {"csv_bytes": os.path.getsize(csv), "binary_bytes": os.path.getsize(binp)}
+        for name, load in (("csv", lambda: colo.Dataset.from_csv(ctx, csv)),
+                           ("binary", lambda: colo.Dataset.from_binary(ctx, binp))):
+            t0 = time.perf_counter()
+            dl = load()
+            t1 = time.perf_counter()
+            r = ctx.mine(dl, params)
+            t2 = time.perf_counter()
+            out[f"{name}_load_ms"] = round((t1 - t0) * 1e3, 2)
+            out[f"e2e_with_{name}_ms"] = round((t2 - t0) * 1e3, 2)
+            out[f"{name}_identical"] = r.patterns() == patterns
+            del dl, r
+        return out
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def load_traffic(kernel: str):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary (or None)."""
     f = ROOT / "profiles" / "traffic.json"
@@ -405,9 +435,12 @@ def main():
             dist.destroy_process_group()
         return
     cpu = None
+    io = None
     if not args.no_cpu and world == 1:
         v, cores, sample, _ = run_cpu(wl, args.cpu_frac, 1, 0)
         cpu = {"value": v, "unit": "candidates/s", "cores": cores, "kind": "port", "sample": sample}
+        io = measure_io(ctx, wl, ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size),
+                        res_b[0].patterns())
     line = {
         "metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_b / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -419,7 +452,7 @@ def main():
                    "filter_items": int(counters["filter_items"]), "filter_full_quads": int(counters["filter_full_quads"]),
                    "filter_cells": int(counters["filter_cells"]),
                    "form": "batched+learned" if head_mode == colo.MODE_LEARNED else "batched",
-                   "l2": "inputs (240 MB) larger than L2 (129 MB); no flush",
+                   "l2": "inputs (x, y f32: 160 MB) larger than L2 (129 MB); no flush",
                    "parallelism": f"replicas x{world}", "autotuned": tuned},
         "e2e": {"value": e2e, "unit": "candidates/s", "ms_per_step": ms_e / args.steps,
                 "h2d_bytes_per_step": int(res_e[0].counters["h2d_bytes"]),
@@ -440,6 +473,7 @@ def main():
         "gpu_launches": int(sum(r.counters["launches"] for r in res_b)),
         "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,
         "host_phase_ms": phases,
+        "io": io,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -29,7 +29,7 @@ MODE_PLAIN, MODE_BATCHED, MODE_LEARNED = 0, 1, 2
 COUNTERS = ["launches", "active_anchors", "neighbors", "rows_written", "join_pairs", "points", "cells", "runs",
             "count_items", "count_parent_words", "fill_words", "bitmap_words", "h2d_bytes", "d2h_bytes",
             "nrl_entries", "refined", "filter_items", "single_pass", "single_pass_overflow", "filter_cell_members",
-            "filter_full_quads", "filter_cells", "pairs_model_us", "level_filter_wait_us"]
+            "filter_full_quads", "filter_cells", "pairs_model_us", "level_filter_wait_us", "host_table_bytes"]
 
 # Every symbol declared in include/colo.h (checked by the CPU tests).
 EXPORTS = [
@@ -43,7 +43,7 @@ EXPORTS = [
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
     "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
     "colo_ctx_set_model", "colo_result_features", "colo_autotune", "colo_dataset_from_csv_threads",
-    "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary",
+    "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary", "colo_stage_apriori",
 ]
 MODEL_FEATURES = 24
 MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -129,6 +129,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_stage_sqdist": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, _f32p]),
         "colo_stage_within": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _f32p, _u8p]),
         "colo_table_pi_static": (C.c_int, [_P, C.c_uint64, C.c_uint32, _u32p, _u32p, _P, _P, _P]),
+        "colo_stage_apriori": (C.c_int, [_P, _u32p, C.c_uint64, C.c_uint32, _u32p, _u32p, C.c_uint64, _u64p]),
         "colo_model_forward": (C.c_int, [_P, _f32p, _f32p, C.c_uint64, _f32p]),
         "colo_model_grad": (C.c_int, [_P, _f32p, _f32p, _f32p, C.c_uint64, _f32p, _f32p]),
         "colo_model_train": (C.c_int, [_P, _f32p, _f32p, _f32p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float,
@@ -146,9 +147,13 @@ def load(build: bool = True) -> C.CDLL:
 
 
 def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHED, max_size: int = 0,
-                   keep_tables: bool = False, profile: bool = False, features: bool = False) -> Params:
+                   keep_tables: bool = False, profile: bool = False, features: bool = False,
+                   device_apriori: bool = False, host_tables: bool = False) -> Params:
     """Mining parameters; `profile` times every kernel, `features` records the cost-model
-    features of every candidate (training data)."""
+    features of every candidate (training data), `device_apriori` generates every level's
+    candidates on the device (by default only levels with many prevalent patterns), `host_tables`
+    keeps the instance tables in pinned host memory (by default only tables too large for the
+    device)."""
     p = Params()
     load().colo_params_default(C.byref(p))
     p.distance = distance
@@ -156,7 +161,8 @@ def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHE
     p.mode = mode
     p.max_size = max_size
     p.keep_tables = 1 if keep_tables else 0
-    p.reserved[0] = (1 if profile else 0) | (2 if features else 0)
+    p.reserved[0] = ((1 if profile else 0) | (2 if features else 0) | (4 if device_apriori else 0) |
+                     (8 if host_tables else 0))
     return p
 
 
@@ -367,6 +373,18 @@ class Context:
         self.check(self.lib.colo_stage_filter(self.h, ds.h, R, thr, _ptr(cand, _u32p), n, k, _ptr(ub, _u64p),
                                               _ptr(pas, _u8p)), "stage_filter")
         return ub, pas
+
+    def stage_apriori(self, prev: np.ndarray, k: int):
+        """Level-k candidates of the prevalent (k-1)-patterns `prev` on the device: (candidates, parent)."""
+        prev = np.ascontiguousarray(prev, np.uint32).reshape(-1, k - 1)
+        n = C.c_uint64(0)
+        self.check(self.lib.colo_stage_apriori(self.h, _ptr(prev, _u32p), len(prev), k, None, None, 0, C.byref(n)),
+                   "stage_apriori")
+        out = np.zeros((max(n.value, 1), k), np.uint32)
+        par = np.zeros(max(n.value, 1), np.uint32)
+        self.check(self.lib.colo_stage_apriori(self.h, _ptr(prev, _u32p), len(prev), k, _ptr(out, _u32p),
+                                               _ptr(par, _u32p), n.value, C.byref(n)), "stage_apriori")
+        return out[: n.value], par[: n.value]
 
     def stage_sqdist(self, x1, y1, x2, y2) -> np.ndarray:
         a = [np.ascontiguousarray(v, np.float32) for v in (x1, y1, x2, y2)]

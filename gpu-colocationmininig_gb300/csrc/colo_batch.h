@@ -81,6 +81,11 @@ void bucket_points(Batch& b);            // cells, runs, masks, nb9, runs per fe
 void build_neighborhoods(Batch& b);      // NRL / NPL
 // colo_join.cu
 void join_neighbors(Batch& b);           // neighbour CSR
+// Level-k candidates of every job from its prevalent (k-1)-patterns (km1
+// features each, lexicographic), with each candidate's prefix pattern index;
+// a null entry is a job with no next level.  colo_apriori.cu.
+void apriori_device(cudaStream_t s, const std::vector<const std::vector<uint32_t>*>& prev, uint32_t km1,
+                    std::vector<std::vector<uint32_t>>& out, std::vector<std::vector<uint32_t>>& parent);
 // colo_filter.cu
 // Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
 // bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.

@@ -18,12 +18,14 @@ struct HostPoints {
     // the id token as written, at every point whose id differs from the
     // previous point's (the feature names, colocationFinder.cpp:168-184)
     std::vector<std::pair<uint64_t, std::string>> tokens;
+    bool tokens_complete = false;   // tokens hold every group start (file readers)
     float bounds[4] = {0, 0, 0, 0};
     void clear() {
         x.clear();
         y.clear();
         raw.clear();
         tokens.clear();
+        tokens_complete = false;
     }
 };
 
@@ -45,7 +47,7 @@ struct LevelTrace {
 };
 
 // counters[]: the list in include/colo.h (colo_result_counters).
-constexpr int kNumCounters = 24;
+constexpr int kNumCounters = 25;
 struct MineResult {
     std::vector<LevelTrace> levels;
     double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -63,7 +65,11 @@ colo_status write_points_binary(const HostPoints& hp, const std::vector<std::str
                                 std::string& err);
 colo_status read_points_binary(const char* path, HostPoints& hp, std::string& err);
 colo_status write_points_csv(const HostPoints& hp, const std::vector<std::string>& names,
-                             const std::vector<uint32_t>& feat, const char* path, std::string& err);
+                             const std::vector<uint32_t>& fstart, const std::vector<uint32_t>& fcount, const char* path,
+                             std::string& err);
+// Positions where the raw id changes (0 first), found in parallel; *minus_one
+// is set when some id is -1.
+std::vector<uint64_t> group_starts(const int32_t* raw, uint64_t n, bool* minus_one);
 colo_status write_patterns(const MineResult& r, const std::vector<std::string>& names,
                            const char* location, std::string& err);
 
@@ -85,7 +91,6 @@ struct colo_ctx {
 struct colo_dataset {
     colo_ctx* ctx = nullptr;
     colo::HostPoints hp;
-    std::vector<uint32_t> feat;              // feature index per point
     std::vector<std::string> names;
     std::vector<uint32_t> fstart, fcount;
     colo::DevBuf<float> dx, dy;

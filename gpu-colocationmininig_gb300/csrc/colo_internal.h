@@ -119,6 +119,52 @@ struct DevBuf {
     size_t bytes() const { return n * sizeof(T); }
 };
 
+// Instance-table storage: device memory, or pinned host memory mapped into
+// the device's address space when the tables would not fit in device memory
+// (on Grace the kernels then read and write them over NVLink-C2C).
+struct TableBuf {
+    DevBuf<uint32_t> dev;
+    void* host = nullptr;
+    uint32_t* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = 0;
+    TableBuf() = default;
+    TableBuf(const TableBuf&) = delete;
+    TableBuf& operator=(const TableBuf&) = delete;
+    void alloc(size_t count, cudaStream_t st, bool on_host) {
+        release();
+        s = st;
+        n = count;
+        if (!on_host) {
+            dev.alloc(count, st);
+            p = dev.get();
+            return;
+        }
+        if (cudaHostAlloc(&host, (count ? count : 1) * sizeof(uint32_t), cudaHostAllocMapped) != cudaSuccess) {
+            host = nullptr;
+            cudaGetLastError();
+            throw StatusError{COLO_ERR_NOMEM, "pinned host allocation of " + std::to_string(count * 4) +
+                                                  " bytes for instance tables failed"};
+        }
+        void* d = nullptr;
+        COLO_CUDA(cudaHostGetDevicePointer(&d, host, 0));
+        p = static_cast<uint32_t*>(d);
+    }
+    void release() {
+        if (host) {
+            cudaStreamSynchronize(s);   // kernels of this stream may still use the tables
+            cudaFreeHost(host);
+            host = nullptr;
+        }
+        dev.release();
+        p = nullptr;
+        n = 0;
+    }
+    ~TableBuf() { release(); }
+    uint32_t* get() const { return p; }
+    bool on_host() const { return host != nullptr; }
+};
+
 // Launch counter (kernels of this library launched by the current mine).
 extern thread_local uint64_t g_launches;
 inline void count_launch(uint64_t n = 1) { g_launches += n; }

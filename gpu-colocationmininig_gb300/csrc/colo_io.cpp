@@ -165,7 +165,7 @@ struct FileView {
         }
         n = (size_t)st.st_size;
         if (n > 0) {
-            map = ::mmap(nullptr, n, PROT_READ, MAP_PRIVATE, fd, 0);
+            map = ::mmap(nullptr, n, PROT_READ, MAP_PRIVATE | MAP_POPULATE, fd, 0);
             if (map == MAP_FAILED) {
                 map = nullptr;
                 buf.resize(n);
@@ -381,6 +381,7 @@ colo_status parse_points_csv(const char* path, HostPoints& hp, std::string& err,
         std::memcpy(hp.y.data() + off[t], c.y.data(), c.y.size() * sizeof(float));
         std::memcpy(hp.raw.data() + off[t], c.raw.data(), c.raw.size() * sizeof(int32_t));
     });
+    hp.tokens_complete = true;
     const char* b = last < T ? ch[last].after : end;
     if (b >= end) {
         err = "dataset: bounds line missing";
@@ -403,19 +404,44 @@ colo_status parse_points_csv(const char* path, HostPoints& hp, std::string& err,
 }
 
 colo_status write_points_csv(const HostPoints& hp, const std::vector<std::string>& names,
-                             const std::vector<uint32_t>& feat, const char* path, std::string& err) {
+                             const std::vector<uint32_t>& fstart, const std::vector<uint32_t>& fcount, const char* path,
+                             std::string& err) {
     FILE* fo = std::fopen(path, "wb");
     if (!fo) {
         err = std::string("cannot write ") + path;
         return COLO_ERR_IO;
     }
     std::fprintf(fo, "%zu\n", hp.x.size());
-    for (size_t i = 0; i < hp.x.size(); ++i)
-        std::fprintf(fo, "%s,%.9g,%.9g\n", names[feat[i]].c_str(), (double)hp.x[i], (double)hp.y[i]);
+    for (size_t f = 0; f < names.size(); ++f)
+        for (uint64_t i = fstart[f]; i < (uint64_t)fstart[f] + fcount[f]; ++i)
+            std::fprintf(fo, "%s,%.9g,%.9g\n", names[f].c_str(), (double)hp.x[i], (double)hp.y[i]);
     std::fprintf(fo, "\n%.9g,%.9g,%.9g,%.9g", (double)hp.bounds[0], (double)hp.bounds[1],
                  (double)hp.bounds[2], (double)hp.bounds[3]);
     std::fclose(fo);
     return COLO_OK;
+}
+
+std::vector<uint64_t> group_starts(const int32_t* raw, uint64_t n, bool* minus_one) {
+    *minus_one = false;
+    std::vector<uint64_t> out;
+    if (n == 0) return out;
+    unsigned T = std::thread::hardware_concurrency();
+    if (T == 0) T = 1;
+    T = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(std::min<unsigned>(T, 64), n >> 20));
+    std::vector<std::vector<uint64_t>> part(T);
+    std::vector<char> bad(T, 0);
+    run_threads(T, [&](unsigned t) {
+        const uint64_t a = n * t / T, b = n * (t + 1) / T;
+        for (uint64_t i = a; i < b; ++i) {
+            if (raw[i] == -1) bad[t] = 1;
+            if (i == 0 || raw[i] != raw[i - 1]) part[t].push_back(i);
+        }
+    });
+    for (unsigned t = 0; t < T; ++t) {
+        *minus_one |= bad[t] != 0;
+        out.insert(out.end(), part[t].begin(), part[t].end());
+    }
+    return out;
 }
 
 // ---------------------------------------------------------------------------
@@ -478,60 +504,93 @@ colo_status write_points_binary(const HostPoints& hp, const std::vector<std::str
 }
 
 colo_status read_points_binary(const char* path, HostPoints& hp, std::string& err) {
-    FileView fv(path);
-    if (!fv.ok) {
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) {
         err = std::string("cannot read dataset: ") + path;
         return COLO_ERR_IO;
     }
+    struct Closer {
+        int fd;
+        ~Closer() { ::close(fd); }
+    } closer{fd};
+    struct stat st;
+    if (::fstat(fd, &st) != 0) {
+        err = std::string("cannot read dataset: ") + path;
+        return COLO_ERR_IO;
+    }
+    const uint64_t fsize = (uint64_t)st.st_size;
+    // whole read of [off, off + bytes) into dst
+    auto pread_all = [fd](void* dst, uint64_t bytes, uint64_t off) {
+        char* p = static_cast<char*>(dst);
+        while (bytes) {
+            const ssize_t r = ::pread(fd, p, bytes, (off_t)off);
+            if (r <= 0) return false;
+            p += r;
+            off += (uint64_t)r;
+            bytes -= (uint64_t)r;
+        }
+        return true;
+    };
     BinHeader h;
-    if (fv.n < sizeof(h)) {
+    if (fsize < sizeof(h) || !pread_all(&h, sizeof(h), 0)) {
         err = "binary points: file shorter than its header";
         return COLO_ERR_PARSE;
     }
-    std::memcpy(&h, fv.p, sizeof(h));
     if (std::memcmp(h.magic, kBinMagic, 8) != 0 || h.version != 1 || h.header_bytes != sizeof(h)) {
         err = "binary points: not a version-1 point file";
         return COLO_ERR_PARSE;
     }
-    const uint64_t body = fv.n - sizeof(h);
+    const uint64_t body = fsize - sizeof(h);
     if (h.n > body / 12 || h.nfeat > (body - 12 * h.n) / 4 || h.name_bytes != body - 12 * h.n - 4 * h.nfeat) {
         err = "binary points: sizes in the header do not match the file (truncated or corrupt)";
         return COLO_ERR_PARSE;
     }
     const uint64_t n = h.n;
-    const char* q = fv.p + sizeof(h);
     hp.clear();
     hp.x.resize(n);
     hp.y.resize(n);
     hp.raw.resize(n);
+    // the three columns read in parallel, each straight into its array
     void* dst[3] = {hp.x.data(), hp.y.data(), hp.raw.data()};
-    const unsigned T = n >= (1u << 20) ? 3u : 1u;
-    run_threads(T, [&](unsigned t) {
-        for (unsigned i = t; i < 3; i += T)
-            if (n) std::memcpy(dst[i], q + 4 * n * i, n * 4);
+    bool ok3[3] = {true, true, true};
+    run_threads(n >= (1u << 20) ? 3u : 1u, [&](unsigned t) {
+        for (unsigned i = t; i < 3; i += (n >= (1u << 20) ? 3u : 1u))
+            if (n) ok3[i] = pread_all(dst[i], n * 4, sizeof(h) + 4 * n * i);
     });
-    std::memcpy(hp.bounds, h.bounds, sizeof(hp.bounds));
     std::vector<uint32_t> len(h.nfeat);
-    if (h.nfeat) std::memcpy(len.data(), q + 12 * n, h.nfeat * 4);
-    const char* names = q + 12 * n + 4 * h.nfeat;
-    uint64_t used = 0, g = 0;
-    for (uint64_t i = 0; i < n; ++i) {
-        if (hp.raw[i] == -1) {
-            err = "binary points: feature id -1 is the reference's 'no feature yet' marker";
-            return COLO_ERR_PARSE;
-        }
-        if (i > 0 && hp.raw[i] == hp.raw[i - 1]) continue;
-        if (g >= h.nfeat || len[g] > h.name_bytes - used) {
-            err = "binary points: the ids form more features than the file names";
-            return COLO_ERR_PARSE;
-        }
-        hp.tokens.emplace_back(i, std::string(names + used, len[g]));
-        used += len[g++];
+    std::string names(h.name_bytes, '\0');
+    if (!ok3[0] || !ok3[1] || !ok3[2] || (h.nfeat && !pread_all(len.data(), h.nfeat * 4, sizeof(h) + 12 * n)) ||
+        (h.name_bytes && !pread_all(&names[0], h.name_bytes, sizeof(h) + 12 * n + 4 * h.nfeat))) {
+        err = std::string("cannot read dataset: ") + path;
+        return COLO_ERR_IO;
     }
-    if (g != h.nfeat || used != h.name_bytes) {
-        err = "binary points: the ids form fewer features than the file names";
+    std::memcpy(hp.bounds, h.bounds, sizeof(hp.bounds));
+    bool minus_one = false;
+    const std::vector<uint64_t> starts = group_starts(hp.raw.data(), n, &minus_one);
+    if (minus_one) {
+        err = "binary points: feature id -1 is the reference's 'no feature yet' marker";
         return COLO_ERR_PARSE;
     }
+    if (starts.size() != h.nfeat) {
+        err = "binary points: the ids form " + std::to_string(starts.size()) + " features, the file names " +
+              std::to_string(h.nfeat);
+        return COLO_ERR_PARSE;
+    }
+    uint64_t used = 0;
+    hp.tokens.reserve(starts.size());
+    for (uint64_t g = 0; g < starts.size(); ++g) {
+        if (len[g] > h.name_bytes - used) {
+            err = "binary points: name lengths exceed the name table";
+            return COLO_ERR_PARSE;
+        }
+        hp.tokens.emplace_back(starts[g], names.substr(used, len[g]));
+        used += len[g];
+    }
+    if (used != h.name_bytes) {
+        err = "binary points: name lengths do not cover the name table";
+        return COLO_ERR_PARSE;
+    }
+    hp.tokens_complete = true;
     return COLO_OK;
 }
 

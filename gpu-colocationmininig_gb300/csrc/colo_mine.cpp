@@ -38,26 +38,30 @@ colo_status guarded(colo_ctx* ctx, Fn&& fn) {
 }
 
 // Feature grouping of populateData (colocationFinder.cpp:168-229): a change of
-// raw id starts a new feature, named by the id token as written.
+// raw id starts a new feature, named by the id token as written.  The file
+// readers record the token of every group start; host arrays have none, and
+// their features are named by the id's decimal form.
 void group_features(colo_dataset* ds) {
     const HostPoints& hp = ds->hp;
-    size_t n = hp.x.size();
-    ds->feat.resize(n);
+    const uint64_t n = hp.x.size();
     ds->names.clear();
     ds->fstart.clear();
     ds->fcount.clear();
-    size_t tk = 0;
-    for (size_t i = 0; i < n; ++i) {
-        if (i == 0 || hp.raw[i] != hp.raw[i - 1]) {
-            while (tk < hp.tokens.size() && hp.tokens[tk].first < i) ++tk;
-            const bool named = tk < hp.tokens.size() && hp.tokens[tk].first == i;
-            ds->names.push_back(named ? hp.tokens[tk].second : std::to_string(hp.raw[i]));
-            ds->fstart.push_back((uint32_t)i);
-            ds->fcount.push_back(0);
+    if (hp.tokens_complete) {
+        for (const auto& t : hp.tokens) {
+            ds->names.push_back(t.second);
+            ds->fstart.push_back((uint32_t)t.first);
         }
-        ds->feat[i] = (uint32_t)(ds->names.size() - 1);
-        ds->fcount.back()++;
+    } else {
+        bool minus_one = false;
+        for (uint64_t i : group_starts(hp.raw.data(), n, &minus_one)) {
+            ds->names.push_back(std::to_string(hp.raw[i]));
+            ds->fstart.push_back((uint32_t)i);
+        }
     }
+    ds->fcount.resize(ds->fstart.size());
+    for (size_t f = 0; f < ds->fstart.size(); ++f)
+        ds->fcount[f] = (f + 1 < ds->fstart.size() ? ds->fstart[f + 1] : (uint32_t)n) - ds->fstart[f];
 }
 
 // setGrid (colocationFinder.cpp:102-126).
@@ -174,6 +178,11 @@ struct JobState {
 // (k-1)-subsets must all be prevalent (generateandCheckSubsets, 669-679);
 // a failing subset check ends the inner loop ("break", 541-542) and so does
 // a prefix mismatch (551-552).
+// Prevalent patterns of a level (all jobs) above which the next level's
+// candidates are generated on the device (apriori_device); below it the host
+// loop is faster than the launches and copies.
+constexpr uint64_t kDeviceAprioriMin = 4096;
+
 std::vector<uint32_t> apriori_next(const std::vector<uint32_t>& prev, uint32_t km1, std::vector<uint32_t>& parent) {
     std::vector<uint32_t> out;
     parent.clear();
@@ -398,7 +407,21 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 js[j].cands.push_back(js[j].f0 + c);
             }
     }
-    std::unique_ptr<DevBuf<uint32_t>> tables_prev, tables_cur, single_prev;
+    std::unique_ptr<TableBuf> tables_prev, tables_cur, single_prev;
+    // level tables go to pinned host memory when forced (reserved[0] bit 3)
+    // or when they would leave less than 1/8 of the device's memory free
+    bool host_tables = false;
+    for (uint32_t j = 0; j < J; ++j) host_tables |= (pv[j].reserved[0] & 8) != 0;
+    uint64_t cnt_host_table_bytes = 0;
+    auto tables_go_to_host = [&](uint64_t bytes) {
+        if (host_tables) return true;
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return bytes + tot / 8 > fr;
+    };
     for (uint32_t k = 2;; ++k) {
         bool any = false;
         for (auto& st : js) any |= (st.active && !st.cands.empty());
@@ -667,12 +690,14 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         ar.rows.alloc(ncand ? ncand : 1, s);
         ar.rows.zero(s);
         ar.stats.alloc(ncand * k * 4 + 1, s);
-        std::unique_ptr<DevBuf<uint32_t>> single_cur;
+        std::unique_ptr<TableBuf> single_cur;
         uint64_t single_words = 0;
         if (learned) {
             for (uint64_t q = 0; q < ncand; ++q) single_words += cap[q] * k;
-            single_cur.reset(new DevBuf<uint32_t>());
-            single_cur->alloc(single_words ? single_words : 1, s);
+            single_cur.reset(new TableBuf());
+            const bool on_host = tables_go_to_host(single_words * 4);
+            single_cur->alloc(single_words ? single_words : 1, s, on_host);
+            if (on_host) cnt_host_table_bytes += single_words * 4;
             ar.cursor.alloc(ncand, s);
             ar.cursor.zero(s);
             ar.overflow.alloc(ncand, s);
@@ -779,18 +804,42 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         t0 = Clock::now();
         // needed[j][c]: candidate c of this level is the prefix of a next-level candidate
         std::vector<std::vector<uint8_t>> needed(J);
+        std::vector<std::vector<uint32_t>> prevs(J), prevcs(J), dnext, dpar;
+        std::vector<const std::vector<uint32_t>*> gen(J, nullptr);
+        uint64_t prev_total = 0;
         for (uint32_t j = 0; j < J; ++j) {
             if (!tr[j]) continue;
             LevelTrace& L = *tr[j];
-            std::vector<uint32_t> prev, prev_c;
             for (size_t c = 0; c < L.cand.size() / k; ++c)
                 if (L.prevalent[c]) {
-                    prev.insert(prev.end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
-                    prev_c.push_back((uint32_t)c);
+                    prevs[j].insert(prevs[j].end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+                    prevcs[j].push_back((uint32_t)c);
                 }
+            const bool cap_ok = (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf;
+            if (cap_ok) {
+                gen[j] = &prevs[j];
+                prev_total += prevcs[j].size();
+            }
+        }
+        // many prevalent patterns: all jobs' candidates in two device passes
+        bool force_dev = false;
+        for (uint32_t j = 0; j < J; ++j) force_dev |= (pv[j].reserved[0] & 4) != 0;
+        const bool on_device = (prev_total >= kDeviceAprioriMin || (force_dev && prev_total > 0)) &&
+                               k + 1 <= (uint32_t)kMaxK;
+        if (on_device) apriori_device(s, gen, k, dnext, dpar);
+        for (uint32_t j = 0; j < J; ++j) {
+            if (!tr[j]) continue;
+            LevelTrace& L = *tr[j];
+            const std::vector<uint32_t>& prev_c = prevcs[j];
             std::vector<uint32_t> next, par;
-            bool cap_ok = (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf;
-            if (cap_ok) next = apriori_next(prev, k, par);
+            if (gen[j]) {
+                if (on_device) {
+                    next = std::move(dnext[j]);
+                    par = std::move(dpar[j]);
+                } else {
+                    next = apriori_next(prevs[j], k, par);
+                }
+            }
             js[j].cands = next;
             needed[j].assign(L.cand.size() / k, 0);
             for (auto& pp : par) {
@@ -821,8 +870,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     rows_written += gb[q + 1] - gb[q];
                     cnt_fillw += (gb[q + 1] - gb[q]) * k;
                 }
-        tables_cur.reset(new DevBuf<uint32_t>());
-        tables_cur->alloc(total_rows * k ? total_rows * k : 1, s);
+        tables_cur.reset(new TableBuf());
+        {
+            const bool on_host = tables_go_to_host(total_rows * k * 4);
+            tables_cur->alloc(total_rows * k ? total_rows * k : 1, s, on_host);
+            if (on_host) cnt_host_table_bytes += total_rows * k * 4;
+        }
         // output offsets of every parent row: exclusive scan of the slots
         DevBuf<uint64_t> G;
         if (!fillq.empty()) {
@@ -901,7 +954,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 std::vector<uint32_t> colm(rows * k);
                 if (rows)
                     COLO_CUDA(cudaMemcpy2D(colm.data(), rows * 4, t.cols, t.stride * 4, rows * 4, k,
-                                           cudaMemcpyDeviceToHost));
+                                           cudaMemcpyDefault));   // the tables may be in host memory
                 if (L.tables.size() < L.cand.size() / k) L.tables.resize(L.cand.size() / k);
                 std::vector<uint32_t>& rm = L.tables[c];
                 rm.resize(rows * k);
@@ -940,6 +993,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->counters[21] = cnt_fcells;
         r->counters[22] = us_pairs_model;
         r->counters[23] = us_level_wait;
+        r->counters[24] = cnt_host_table_bytes;
         r->times[0] = ms_since(t_all);
         r->times[1] = t_upload;
         r->times[2] = t_bucket;
@@ -1126,7 +1180,7 @@ colo_status colo_dataset_from_host(colo_ctx* ctx, const float* x, const float* y
 colo_status colo_dataset_write_csv(const colo_dataset* ds, const char* path) {
     if (!ds || !path) return COLO_ERR_ARG;
     std::string err;
-    return write_points_csv(ds->hp, ds->names, ds->feat, path, err);
+    return write_points_csv(ds->hp, ds->names, ds->fstart, ds->fcount, path, err);
 }
 
 colo_status colo_dataset_upload(colo_dataset* ds) {

@@ -2,6 +2,7 @@
 // counterparts of the reference's inner extern "C" API
 // (Codes/DeviceProcess.h:4-36).  They run one stage on a dataset and copy
 // its result to host arrays, so each kernel can be checked in isolation.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -162,6 +163,26 @@ colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float th
                 pass[c] = pi0 >= thr;
             }
         }
+        return COLO_OK;
+    });
+}
+
+colo_status colo_stage_apriori(colo_ctx* ctx, const uint32_t* prev, uint64_t nprev, uint32_t k, uint32_t* out,
+                               uint32_t* parent, uint64_t cap, uint64_t* n_out) {
+    if (!ctx || !n_out || k < 2 || (nprev && !prev) || (cap && (!out || !parent))) return COLO_ERR_ARG;
+    if (k > (uint32_t)kMaxK) return set_err(ctx, COLO_ERR_CAPACITY, "patterns larger than 32 features are not supported");
+    return run_guarded(ctx, [&]() -> colo_status {
+        std::vector<uint32_t> rows(prev, prev + nprev * (k - 1));
+        std::vector<const std::vector<uint32_t>*> gen{&rows};
+        std::vector<std::vector<uint32_t>> next, par;
+        apriori_device(ctx->s, gen, k - 1, next, par);
+        const uint64_t n = par[0].size();
+        const uint64_t m = std::min<uint64_t>(n, cap);
+        if (m) {
+            std::memcpy(out, next[0].data(), m * k * 4);
+            std::memcpy(parent, par[0].data(), m * 4);
+        }
+        *n_out = n;
         return COLO_OK;
     });
 }

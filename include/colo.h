@@ -56,7 +56,12 @@ typedef struct {
     int32_t mode;            /* colo_mode */
     int32_t keep_tables;     /* 1: keep every instance table in the result (tests) */
     int32_t reserved[6];     /* reserved[0] bit 0: time every kernel with CUDA events;
-                                bit 1: record cost-model features of every candidate */
+                                bit 1: record cost-model features of every candidate;
+                                bit 2: generate candidates on the device at every level
+                                (otherwise only for levels with 4096+ prevalent patterns);
+                                bit 3: keep instance tables in pinned host memory mapped
+                                into the device (otherwise only tables that would leave
+                                less than 1/8 of device memory free go there) */
 } colo_params;
 
 const char* colo_status_string(colo_status s);
@@ -167,7 +172,8 @@ colo_status colo_result_times(const colo_result* r, double* ms8);
  * of the level filters, [20] full quads found by the level filters, [21]
  * cells of U_c summed over candidates, [22] microseconds of the pairs'
  * cost-model step on the host, [23] microseconds from the level filters'
- * launches to their readback. */
+ * launches to their readback, [24] bytes of instance tables placed in pinned
+ * host memory. */
 colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n);
 /* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set). */
 uint32_t colo_result_num_kernels(const colo_result* r);
@@ -205,6 +211,15 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
  * fallback near the boundary); either output may be NULL. */
 colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
                               const float* y2, uint64_t n, float R2, float* out, uint8_t* within);
+
+/* candidateColocationGeneral (colocationFinder.cpp:517-557) on the device:
+ * the level-k candidates of the nprev prevalent (k-1)-patterns in prev
+ * (row-major, lexicographic order), with the reference's breaks.  Writes up
+ * to cap candidates (k features each) to out and each one's prefix pattern
+ * index to parent; *n_out receives the number of candidates.  The mining
+ * loop takes this path when a level has many prevalent patterns. */
+colo_status colo_stage_apriori(colo_ctx* ctx, const uint32_t* prev, uint64_t nprev, uint32_t k, uint32_t* out,
+                               uint32_t* parent, uint64_t cap, uint64_t* n_out);
 
 /* ---- autotuning ------------------------------------------------------- */
 /* Times the cell-pair join of this dataset at 4, 8, 16 and 32 lanes per

@@ -67,7 +67,8 @@ struct Batch {
     // (feature, neighbour cell, id) order
     DevBuf<uint64_t> nb_beg;
     DevBuf<uint32_t> nb_cnt, nb;
-    uint64_t E = 0;              // neighbour entries
+    uint64_t E = 0;              // neighbour entries (UINT64_MAX: still on the device in dE)
+    DevBuf<unsigned long long> dE;
     uint64_t nb_cap = 0;         // allocated entries (upper bound in single-pass mode)
     uint64_t join_pairs = 0;     // pair distance evaluations
     uint64_t active_anchors = 0; // anchors whose cell has higher-feature neighbours
@@ -81,6 +82,7 @@ void bucket_points(Batch& b);            // cells, runs, masks, nb9, runs per fe
 void build_neighborhoods(Batch& b);      // NRL / NPL
 // colo_join.cu
 void join_neighbors(Batch& b);           // neighbour CSR
+uint64_t neighbor_entries(Batch& b);     // E (waits for the device sum once)
 // Level-k candidates of every job from its prevalent (k-1)-patterns (km1
 // features each, lexicographic), with each candidate's prefix pattern index;
 // a null entry is a job with no next level.  colo_apriori.cu.

@@ -634,7 +634,8 @@ void sort_and_compact(Batch& b) {
     COLO_LAUNCH_CHECK();
     count_launch();
     }
-    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get());
+    // a look-back timeout lands in the batch's flags, read with the compaction totals
+    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get(), &b.flags.get()->timeout);
 
     b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);
@@ -762,18 +763,19 @@ void bucket_points(Batch& b) {
             COLO_LAUNCH_CHECK();
             count_launch();
         }
+        // the run counts and the error flags come back with one wait
         std::vector<uint32_t> hc(b.F);
+        DevFlags hf;
         if (b.F) COLO_CUDA(cudaMemcpyAsync(hc.data(), cnt.get(), b.F * 4, cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaMemcpyAsync(&hf, b.flags.get(), sizeof(hf), cudaMemcpyDeviceToHost, s));
         COLO_CUDA(cudaStreamSynchronize(s));
         b.h_frun_off.assign(b.F + 1, 0);
         for (uint32_t f = 0; f < b.F; ++f) b.h_frun_off[f + 1] = b.h_frun_off[f] + hc[f];
+        if (hf.timeout) throw StatusError{COLO_ERR_TIMEOUT, "radix sort: a tile waited too long for its predecessors"};
+        if (hf.out_of_grid)
+            throw StatusError{COLO_ERR_INPUT, std::to_string(hf.out_of_grid) +
+                                                  " point(s) fall outside the grid derived from the bounds line"};
     }
-    DevFlags hf;
-    COLO_CUDA(cudaMemcpyAsync(&hf, b.flags.get(), sizeof(hf), cudaMemcpyDeviceToHost, s));
-    COLO_CUDA(cudaStreamSynchronize(s));
-    if (hf.out_of_grid)
-        throw StatusError{COLO_ERR_INPUT, std::to_string(hf.out_of_grid) +
-                                              " point(s) fall outside the grid derived from the bounds line"};
 }
 
 void build_neighborhoods(Batch& b) {
@@ -817,7 +819,6 @@ void build_neighborhoods(Batch& b) {
         COLO_LAUNCH_CHECK();
         count_launch(2);
     }
-    COLO_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace colo

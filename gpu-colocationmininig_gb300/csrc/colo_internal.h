@@ -259,13 +259,16 @@ struct KScope {
 void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* total_host);
 // Sum of n values (synchronises to read it back).
 uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s);
-// out[i] = sum(in[0..i)) ; returns total (synchronises to read it back if total_host != nullptr).
+// Sum of n values into *out (device), without waiting.
+void sum_u32_dev(const uint32_t* in, uint64_t n, cudaStream_t s, unsigned long long* out);
+// out[i] = sum(in[0..i)).  The total is read back (with a wait) when
+// total_host is given, and copied to device memory (no wait) when total_dev is.
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
-                     uint64_t* total_host);
+                     uint64_t* total_host, uint64_t* total_dev = nullptr);
 void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t s,
-                     uint32_t* total_host);
+                     uint32_t* total_host, uint32_t* total_dev = nullptr);
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
-                     uint64_t* total_host);
+                     uint64_t* total_host, uint64_t* total_dev = nullptr);
 // Digit split of a radix sort: pass p sorts width[p] (<= 8) bits from shift[p].
 constexpr int kRadixDigits = 256;
 constexpr int kRadixMaxPasses = 8;
@@ -281,9 +284,11 @@ RadixPlan radix_plan(int bits);
 // hist, when given, holds every pass's digit counts of the keys
 // (hist[p * kRadixDigits + d], radix_plan(bits) passes), counted by the
 // caller while it wrote the keys; the sort then skips its own count.
+// err_dev, when given, receives the timeout flag of a look-back wait (the
+// caller checks it at its next wait); otherwise the sort waits and throws.
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name = "radix_sort", unsigned long long* hist = nullptr);
+                const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr);
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name = "radix_sort", unsigned long long* hist = nullptr);
+                const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr);
 
 }  // namespace colo

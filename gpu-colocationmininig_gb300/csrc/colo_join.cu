@@ -160,11 +160,18 @@ void join_neighbors(Batch& b) {
         COLO_LAUNCH_CHECK();
         count_launch();
     }
-    uint32_t A = 0;
-    scan_u32_to_u32(act.get(), act_off.get(), Rn, s, &A);
-    // upper bound of the single-pass layout = pair evaluations
-    uint64_t U = 0;
-    scan_u64_to_u64(cap.get(), cap_off.get(), Rn, s, &U);
+    // active anchors A and the single-pass layout's size U (= pair
+    // evaluations), read back together with one wait
+    DevBuf<uint64_t> totals;
+    totals.alloc(2, s);
+    totals.zero(s);
+    scan_u32_to_u32(act.get(), act_off.get(), Rn, s, nullptr, reinterpret_cast<uint32_t*>(totals.get()));
+    scan_u64_to_u64(cap.get(), cap_off.get(), Rn, s, nullptr, totals.get() + 1);
+    uint64_t ht[2] = {0, 0};
+    COLO_CUDA(cudaMemcpyAsync(ht, totals.get(), 16, cudaMemcpyDeviceToHost, s));
+    COLO_CUDA(cudaStreamSynchronize(s));
+    const uint32_t A = (uint32_t)ht[0];
+    const uint64_t U = ht[1];
     b.active_anchors = A;
     b.join_pairs = U;
     DevBuf<uint32_t> act_pos, act_run;
@@ -194,8 +201,25 @@ void join_neighbors(Batch& b) {
         b.nb.alloc(E ? E : 1, s);
         dispatch_join(b, J_FILL, A, act_pos.get(), act_run.get(), nullptr);
     }
-    // total entries
-    b.E = b.join_single ? sum_u32(b.nb_cnt.get(), b.N, s) : b.nb_cap;
+    // total entries: known for the two-pass layout; for the single-pass one
+    // summed on the device and read at the mine's next wait (b.dE)
+    b.dE.alloc(1, s);
+    if (b.join_single) {
+        sum_u32_dev(b.nb_cnt.get(), b.N, s, b.dE.get());
+        b.E = UINT64_MAX;
+    } else {
+        b.E = b.nb_cap;
+    }
+}
+
+uint64_t neighbor_entries(Batch& b) {
+    if (b.E == UINT64_MAX) {
+        unsigned long long e = 0;
+        COLO_CUDA(cudaMemcpyAsync(&e, b.dE.get(), 8, cudaMemcpyDeviceToHost, b.s));
+        COLO_CUDA(cudaStreamSynchronize(b.s));
+        b.E = e;
+    }
+    return b.E;
 }
 
 void eval_sqdist(const float* x1, const float* y1, const float* x2, const float* y2, uint64_t n,

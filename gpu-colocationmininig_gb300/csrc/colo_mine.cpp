@@ -1004,7 +1004,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         r->times[7] = t_apriori;
         r->counters[0] = g_launches;
         r->counters[1] = b.active_anchors;
-        r->counters[2] = b.E;
+        r->counters[2] = neighbor_entries(b);
         r->counters[3] = rows_written;
     }
 }

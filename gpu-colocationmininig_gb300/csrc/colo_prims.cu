@@ -101,7 +101,7 @@ __global__ void k_sum_u32(const uint32_t* __restrict__ in, uint64_t n, unsigned 
 }
 
 template <class Tin, class Tout>
-void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total_host) {
+void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total_host, Tout* total_dev) {
     KScope ks("scan");
     uint64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles == 0) tiles = 1;
@@ -122,6 +122,9 @@ void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total
         COLO_LAUNCH_CHECK();
         count_launch();
     }
+    if (total_dev)
+        COLO_CUDA(cudaMemcpyAsync(total_dev, partial.get() + (n > 0 ? tiles : 0), sizeof(Tout),
+                                  cudaMemcpyDeviceToDevice, s));
     if (total_host) {
         COLO_CUDA(cudaMemcpyAsync(total_host, partial.get() + (n > 0 ? tiles : 0), sizeof(Tout),
                                   cudaMemcpyDeviceToHost, s));
@@ -328,18 +331,22 @@ void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* 
     }
 }
 
-uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
+void sum_u32_dev(const uint32_t* in, uint64_t n, cudaStream_t s, unsigned long long* out) {
     KScope ks("sum");
-    DevBuf<unsigned long long> acc;
-    acc.alloc(1, s);
-    acc.zero(s);
+    COLO_CUDA(cudaMemsetAsync(out, 0, 8, s));
     if (n) {
         uint64_t blocks = (n + 255) / 256;
         if (blocks > 2048) blocks = 2048;
-        k_sum_u32<<<(unsigned)blocks, 256, 0, s>>>(in, n, acc.get());
+        k_sum_u32<<<(unsigned)blocks, 256, 0, s>>>(in, n, out);
         COLO_LAUNCH_CHECK();
         count_launch();
     }
+}
+
+uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
+    DevBuf<unsigned long long> acc;
+    acc.alloc(1, s);
+    sum_u32_dev(in, n, s, acc.get());
     unsigned long long h = 0;
     COLO_CUDA(cudaMemcpyAsync(&h, acc.get(), 8, cudaMemcpyDeviceToHost, s));
     COLO_CUDA(cudaStreamSynchronize(s));
@@ -347,25 +354,25 @@ uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
 }
 
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
-                     uint64_t* total_host) {
-    scan_impl<uint32_t, uint64_t>(in, out, n, s, total_host);
+                     uint64_t* total_host, uint64_t* total_dev) {
+    scan_impl<uint32_t, uint64_t>(in, out, n, s, total_host, total_dev);
 }
 
 void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t s,
-                     uint32_t* total_host) {
-    scan_impl<uint32_t, uint32_t>(in, out, n, s, total_host);
+                     uint32_t* total_host, uint32_t* total_dev) {
+    scan_impl<uint32_t, uint32_t>(in, out, n, s, total_host, total_dev);
 }
 
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
-                     uint64_t* total_host) {
-    scan_impl<uint64_t, uint64_t>(in, out, n, s, total_host);
+                     uint64_t* total_host, uint64_t* total_dev) {
+    scan_impl<uint64_t, uint64_t>(in, out, n, s, total_host, total_dev);
 }
 
 namespace {
 
 template <class KT>
 void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                     const char* name, unsigned long long* hist_in) {
+                     const char* name, unsigned long long* hist_in, uint32_t* err_dev) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
     const RadixPlan plan = radix_plan(bits);
@@ -379,9 +386,12 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
     unsigned long long* hist = hist_in ? hist_in : ghist.get();
     status.alloc((uint64_t)ntiles * kMaxRadix, s);
     tickets.alloc(plan.n, s);
-    err.alloc(1, s);
     tickets.zero(s);
-    err.zero(s);
+    if (!err_dev) {
+        err.alloc(1, s);
+        err.zero(s);
+    }
+    uint32_t* errp = err_dev ? err_dev : err.get();
     {
         KScope ks("radix_hist");
         if (!hist_in) {
@@ -409,7 +419,7 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         COLO_CUDA(cudaMemsetAsync(status.get(), 0, (uint64_t)ntiles * kMaxRadix * 8, s));
         k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
                                                                      hist + p * kMaxRadix, status.get(),
-                                                                     tickets.get() + p, err.get());
+                                                                     tickets.get() + p, errp);
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);
@@ -419,6 +429,7 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         keys.swap(k2);
         vals.swap(v2);
     }
+    if (err_dev) return;   // the caller reads the error word at its next wait
     uint32_t herr = 0;
     COLO_CUDA(cudaMemcpyAsync(&herr, err.get(), 4, cudaMemcpyDeviceToHost, s));
     COLO_CUDA(cudaStreamSynchronize(s));
@@ -441,13 +452,13 @@ RadixPlan radix_plan(int bits) {
 }
 
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name, unsigned long long* hist) {
-    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist);
+                const char* name, unsigned long long* hist, uint32_t* err_dev) {
+    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist, err_dev);
 }
 
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name, unsigned long long* hist) {
-    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist);
+                const char* name, unsigned long long* hist, uint32_t* err_dev) {
+    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist, err_dev);
 }
 
 }  // namespace colo

@@ -84,7 +84,7 @@ colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint6
             build_neighborhoods(b);
             join_neighbors(b);
         }
-        *total = b.E;
+        *total = neighbor_entries(b);
         cudaStream_t s = ctx->s;
         if (offs) offs[0] = 0;
         if ((offs || nbr) && b.N) {
@@ -96,7 +96,7 @@ colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint6
             if (b.nb_cap)
                 COLO_CUDA(cudaMemcpyAsync(all.data(), b.nb.get(), b.nb_cap * 4, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaStreamSynchronize(s));
-            if (nbr && cap < b.E) return COLO_ERR_CAPACITY;
+            if (nbr && cap < neighbor_entries(b)) return COLO_ERR_CAPACITY;
             uint64_t o = 0;
             for (uint64_t a = 0; a < b.N; ++a) {
                 if (nbr) std::memcpy(nbr + o, all.data() + beg[a], cnt[a] * 4);

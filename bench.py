@@ -164,8 +164,9 @@ def cell_key_bits(grids) -> int:
 
 def measure_io(ctx, wl, ds, params, patterns):
     """End to end including input I/O: the workload written once (untimed) as the reference's CSV and
-    as a binary point file, then each loaded through the public API and mined (one cold mine: page
-    locking and upload included).  Times in ms from the load call to the result."""
+    as a binary point file, then each loaded through the public API -- the CSV by the host reader and
+    by the device reader -- and mined (one cold mine: page locking and upload included).  Times in
+    ms from the load call to the result."""
     import shutil
     import tempfile
 
@@ -177,6 +178,7 @@ def measure_io(ctx, wl, ds, params, patterns):
         ds.write_binary(binp)
         out = {"csv_bytes": os.path.getsize(csv), "binary_bytes": os.path.getsize(binp)}
         for name, load in (("csv", lambda: colo.Dataset.from_csv(ctx, csv)),
+                           ("csv_device", lambda: colo.Dataset.from_csv(ctx, csv, device=True)),
                            ("binary", lambda: colo.Dataset.from_binary(ctx, binp))):
             t0 = time.perf_counter()
             dl = load()

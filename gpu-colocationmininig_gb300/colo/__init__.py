@@ -44,6 +44,7 @@ EXPORTS = [
     "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
     "colo_ctx_set_model", "colo_result_features", "colo_autotune", "colo_dataset_from_csv_threads",
     "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary", "colo_stage_apriori",
+    "colo_dataset_from_csv_device",
 ]
 MODEL_FEATURES = 24
 MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -101,6 +102,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_dataset_from_csv_threads": (C.c_int, [_P, C.c_char_p, C.c_uint32, C.POINTER(_P)]),
         "colo_dataset_write_binary": (C.c_int, [_P, C.c_char_p]),
         "colo_dataset_from_binary": (C.c_int, [_P, C.c_char_p, C.POINTER(_P)]),
+        "colo_dataset_from_csv_device": (C.c_int, [_P, C.c_char_p, C.POINTER(_P)]),
         "colo_csv_to_binary": (C.c_int, [C.c_char_p, C.c_char_p, C.c_uint32, C.c_char_p, C.c_size_t]),
         "colo_dataset_upload": (C.c_int, [_P]),
         "colo_dataset_evict": (C.c_int, [_P]),
@@ -487,11 +489,15 @@ class Dataset:
         self.nfeat = int(ctx.lib.colo_dataset_num_features(handle))
 
     @classmethod
-    def from_csv(cls, ctx: Context, path: str, threads: int = 0) -> "Dataset":
-        """populateData's CSV, parsed by `threads` threads (0: automatic)."""
+    def from_csv(cls, ctx: Context, path: str, threads: int = 0, device: bool = False) -> "Dataset":
+        """populateData's CSV, parsed by `threads` host threads (0: automatic), or on the device."""
         h = _P()
-        ctx.check(ctx.lib.colo_dataset_from_csv_threads(ctx.h, str(path).encode(), threads, C.byref(h)),
-                  "dataset_from_csv")
+        if device:
+            ctx.check(ctx.lib.colo_dataset_from_csv_device(ctx.h, str(path).encode(), C.byref(h)),
+                      "dataset_from_csv_device")
+        else:
+            ctx.check(ctx.lib.colo_dataset_from_csv_threads(ctx.h, str(path).encode(), threads, C.byref(h)),
+                      "dataset_from_csv")
         return cls(ctx, h)
 
     @classmethod

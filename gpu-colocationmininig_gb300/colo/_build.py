@@ -22,7 +22,7 @@ OBJDIR = LIBDIR / "obj"
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["colo_prims.cu", "colo_bucket.cu", "colo_join.cu", "colo_filter.cu", "colo_level.cu",
-                "colo_static.cu", "colo_mlp.cu", "colo_apriori.cu"]
+                "colo_static.cu", "colo_mlp.cu", "colo_apriori.cu", "colo_ingest.cu"]
 HOST_SOURCES = ["colo_mine.cpp", "colo_stage.cpp", "colo_io.cpp", "colo_model.cpp"]
 HEADERS = ["colo_internal.h", "colo_batch.h", "colo_device.cuh", "colo_host.h", "colo_mlp.h"]
 

@@ -64,6 +64,10 @@ colo_status parse_points_csv(const char* path, HostPoints& hp, std::string& err,
 colo_status write_points_binary(const HostPoints& hp, const std::vector<std::string>& names, const char* path,
                                 std::string& err);
 colo_status read_points_binary(const char* path, HostPoints& hp, std::string& err);
+// The CSV parsed on the device (colo_ingest.cu): hp as parse_points_csv fills
+// it, and the coordinates' device copies in dx, dy.
+colo_status parse_points_csv_device(cudaStream_t s, const char* path, HostPoints& hp, DevBuf<float>& dx,
+                                    DevBuf<float>& dy, std::string& err);
 colo_status write_points_csv(const HostPoints& hp, const std::vector<std::string>& names,
                              const std::vector<uint32_t>& fstart, const std::vector<uint32_t>& fcount, const char* path,
                              std::string& err);

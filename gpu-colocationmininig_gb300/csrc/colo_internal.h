@@ -120,8 +120,8 @@ struct DevBuf {
 };
 
 // Instance-table storage: device memory, or pinned host memory mapped into
-// the device's address space when the tables would not fit in device memory
-// (on Grace the kernels then read and write them over NVLink-C2C).
+// the device's address space when asked for or when the device allocation
+// fails (on Grace the kernels then read and write them over NVLink-C2C).
 struct TableBuf {
     DevBuf<uint32_t> dev;
     void* host = nullptr;
@@ -136,9 +136,13 @@ struct TableBuf {
         s = st;
         n = count;
         if (!on_host) {
-            dev.alloc(count, st);
-            p = dev.get();
-            return;
+            try {
+                dev.alloc(count, st);
+                p = dev.get();
+                return;
+            } catch (const StatusError& e) {
+                if (e.st != COLO_ERR_NOMEM) throw;
+            }
         }
         if (cudaHostAlloc(&host, (count ? count : 1) * sizeof(uint32_t), cudaHostAllocMapped) != cudaSuccess) {
             host = nullptr;

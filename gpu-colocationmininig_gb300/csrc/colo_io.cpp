@@ -290,6 +290,35 @@ void run_threads(unsigned T, Fn&& fn) {
 
 }  // namespace
 
+// One point line, one count line and the bounds line with the reader's rules
+// (for the device reader's host-side lines).
+bool csv_parse_line(const char* b, const char* e, int32_t* id, float* x, float* y, bool* minus_one,
+                    std::string* token) {
+    *minus_one = false;
+    std::vector<std::string> f;
+    split_fields(b, e, f);
+    long v;
+    if (f.size() < 3 || !parse_int(f[0], &v) || !parse_float(f[1], x) || !parse_float(f[2], y)) return false;
+    if (v == -1) {
+        *minus_one = true;
+        return false;
+    }
+    *id = (int32_t)v;
+    if (token) *token = f[0];
+    return true;
+}
+
+bool csv_parse_count(const char* b, const char* e, long* n) { return parse_int(b, e, n) && *n >= 0; }
+
+bool csv_parse_bounds(const char* b, const char* e, float bounds[4]) {
+    std::vector<std::string> f;
+    split_fields(b, e, f);
+    if (f.size() < 4) return false;
+    for (int i = 0; i < 4; ++i)
+        if (!parse_float(f[i], &bounds[i])) return false;
+    return true;
+}
+
 // populateData (colocationFinder.cpp:139-254), parsed in parallel: the point
 // lines are cut into runs of whole lines, one per thread; each run is parsed
 // until its end or an empty line, and the runs are joined in order up to the

@@ -409,19 +409,10 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     }
     std::unique_ptr<TableBuf> tables_prev, tables_cur, single_prev;
     // level tables go to pinned host memory when forced (reserved[0] bit 3)
-    // or when they would leave less than 1/8 of the device's memory free
+    // or when their device allocation fails
     bool host_tables = false;
     for (uint32_t j = 0; j < J; ++j) host_tables |= (pv[j].reserved[0] & 8) != 0;
     uint64_t cnt_host_table_bytes = 0;
-    auto tables_go_to_host = [&](uint64_t bytes) {
-        if (host_tables) return true;
-        size_t fr = 0, tot = 0;
-        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        return bytes + tot / 8 > fr;
-    };
     for (uint32_t k = 2;; ++k) {
         bool any = false;
         for (auto& st : js) any |= (st.active && !st.cands.empty());
@@ -695,9 +686,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         if (learned) {
             for (uint64_t q = 0; q < ncand; ++q) single_words += cap[q] * k;
             single_cur.reset(new TableBuf());
-            const bool on_host = tables_go_to_host(single_words * 4);
-            single_cur->alloc(single_words ? single_words : 1, s, on_host);
-            if (on_host) cnt_host_table_bytes += single_words * 4;
+            single_cur->alloc(single_words ? single_words : 1, s, host_tables);
+            if (single_cur->on_host()) cnt_host_table_bytes += single_words * 4;
             ar.cursor.alloc(ncand, s);
             ar.cursor.zero(s);
             ar.overflow.alloc(ncand, s);
@@ -871,11 +861,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     cnt_fillw += (gb[q + 1] - gb[q]) * k;
                 }
         tables_cur.reset(new TableBuf());
-        {
-            const bool on_host = tables_go_to_host(total_rows * k * 4);
-            tables_cur->alloc(total_rows * k ? total_rows * k : 1, s, on_host);
-            if (on_host) cnt_host_table_bytes += total_rows * k * 4;
-        }
+        tables_cur->alloc(total_rows * k ? total_rows * k : 1, s, host_tables);
+        if (tables_cur->on_host()) cnt_host_table_bytes += total_rows * k * 4;
         // output offsets of every parent row: exclusive scan of the slots
         DevBuf<uint64_t> G;
         if (!fillq.empty()) {
@@ -1110,6 +1097,22 @@ colo_status colo_dataset_from_csv_threads(colo_ctx* ctx, const char* path, uint3
 
 colo_status colo_dataset_from_csv(colo_ctx* ctx, const char* path, colo_dataset** out) {
     return colo_dataset_from_csv_threads(ctx, path, 0, out);
+}
+
+colo_status colo_dataset_from_csv_device(colo_ctx* ctx, const char* path, colo_dataset** out) {
+    if (!ctx || !path || !out) return COLO_ERR_ARG;
+    return guarded(ctx, [&]() {
+        std::unique_ptr<colo_dataset> ds(new colo_dataset());
+        ds->ctx = ctx;
+        std::string err;
+        colo_status st = parse_points_csv_device(ctx->s, path, ds->hp, ds->dx, ds->dy, err);
+        if (st != COLO_OK) return set_err(ctx, st, err);
+        group_features(ds.get());
+        ds->resident = true;   // the parsed coordinates are already on the device
+        ctx->refs++;
+        *out = ds.release();
+        return COLO_OK;
+    });
 }
 
 colo_status colo_dataset_from_binary(colo_ctx* ctx, const char* path, colo_dataset** out) {

@@ -60,8 +60,8 @@ typedef struct {
                                 bit 2: generate candidates on the device at every level
                                 (otherwise only for levels with 4096+ prevalent patterns);
                                 bit 3: keep instance tables in pinned host memory mapped
-                                into the device (otherwise only tables that would leave
-                                less than 1/8 of device memory free go there) */
+                                into the device (otherwise only tables whose device
+                                allocation fails go there) */
 } colo_params;
 
 const char* colo_status_string(colo_status s);
@@ -100,6 +100,14 @@ colo_status colo_dataset_write_csv(const colo_dataset* ds, const char* path);
  * reference (its populateData reads serially). */
 colo_status colo_dataset_from_csv_threads(colo_ctx* ctx, const char* path, uint32_t threads,
                                           colo_dataset** out);
+/* populateData's CSV parsed on the device: the text is copied to the device
+ * once, line ends are found and every line is parsed by its own thread with
+ * the host reader's rules; coordinates whose exact conversion cannot be
+ * proved on the device (and lines with quotes or escapes) are parsed on the
+ * host.  Same result and errors as colo_dataset_from_csv; the dataset's
+ * coordinates are resident on the device afterwards.  No counterpart in the
+ * reference. */
+colo_status colo_dataset_from_csv_device(colo_ctx* ctx, const char* path, colo_dataset** out);
 /* Binary point file: the points (x, y f32), raw ids (i32), feature names and
  * bounds of a dataset, loaded without parsing.  Little-endian; a 64-byte
  * header ("COLOPTS1", version 1, header bytes, n, features, name bytes,

@@ -181,12 +181,27 @@ __device__ int parse_float_dev(const uint8_t* b, const uint8_t* e, float* v) {
     return 0;
 }
 
+__device__ __forceinline__ void to_host(uint64_t i, uint8_t* st, unsigned long long* marks, uint64_t* host_list,
+                                        uint64_t host_cap) {
+    st[i] = L_HOST;
+    const unsigned long long q = atomicAdd(&marks[2], 1ull);
+    if (q < host_cap) host_list[q] = i;
+}
+
+__device__ __forceinline__ void failed(uint64_t i, uint8_t code, uint8_t* st, unsigned long long* marks) {
+    st[i] = code;
+    atomicMin(&marks[1], (unsigned long long)i);
+}
+
 // One thread per line of the body: lines 0 .. L-1 end at nl[i]; line L (if
 // the text does not end with a newline) ends at n.
 __global__ void k_parse_lines(const uint8_t* __restrict__ buf, uint64_t n, const uint64_t* __restrict__ nl,
                               uint64_t L, uint64_t lines, float* __restrict__ x, float* __restrict__ y,
                               int32_t* __restrict__ raw, uint8_t* __restrict__ st,
-                              unsigned long long* __restrict__ first_empty) {
+                              unsigned long long* __restrict__ marks, uint64_t* __restrict__ host_list,
+                              uint64_t host_cap) {
+    // marks[0]: first empty line, marks[1]: first malformed / id -1 line,
+    // marks[2]: lines left to the host (their indices in host_list, unordered)
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= lines) return;
     const uint64_t b = i == 0 ? 0 : nl[i - 1] + 1;
@@ -194,7 +209,7 @@ __global__ void k_parse_lines(const uint8_t* __restrict__ buf, uint64_t n, const
     if (e > b && buf[e - 1] == '\r') --e;
     if (e == b) {
         st[i] = L_EMPTY;
-        atomicMin(first_empty, (unsigned long long)i);
+        atomicMin(&marks[0], (unsigned long long)i);
         return;
     }
     const uint8_t* p = buf + b;
@@ -203,7 +218,7 @@ __global__ void k_parse_lines(const uint8_t* __restrict__ buf, uint64_t n, const
     for (const uint8_t* q = p; q < pe; ++q) {
         const uint8_t ch = *q;
         if (ch == '"' || ch == '\\') {   // the tokenizer's quotes and escapes: the host
-            st[i] = L_HOST;
+            to_host(i, st, marks, host_list, host_cap);
             return;
         }
         if (ch == ',') {
@@ -215,21 +230,21 @@ __global__ void k_parse_lines(const uint8_t* __restrict__ buf, uint64_t n, const
     int32_t id = 0;
     float xv = 0.f, yv = 0.f;
     if (!c2 || parse_int_dev(p, c1, &id) != 0) {
-        st[i] = L_BAD;
+        failed(i, L_BAD, st, marks);
         return;
     }
     const int fx = parse_float_dev(c1 + 1, c2, &xv);
     const int fy = parse_float_dev(c2 + 1, c3 ? c3 : pe, &yv);
     if (fx == 2 || fy == 2) {
-        st[i] = L_BAD;
+        failed(i, L_BAD, st, marks);
         return;
     }
     if (fx == 1 || fy == 1) {   // the host decides (a float it rejects makes the line malformed)
-        st[i] = L_HOST;
+        to_host(i, st, marks, host_list, host_cap);
         return;
     }
     if (id == -1) {
-        st[i] = L_MINUS1;
+        failed(i, L_MINUS1, st, marks);
         return;
     }
     x[i] = xv;
@@ -361,35 +376,49 @@ colo_status parse_points_csv_device(cudaStream_t s, const char* path, HostPoints
     DevBuf<float> px, py;
     DevBuf<int32_t> praw;
     DevBuf<uint8_t> pst;
-    DevBuf<unsigned long long> pfe;
+    DevBuf<unsigned long long> marks;
+    DevBuf<uint64_t> hlist;
+    const uint64_t host_cap = std::max<uint64_t>(1024, lines / 64);
+    marks.alloc(3, s);
+    hlist.alloc(host_cap, s);
+    {
+        const unsigned long long init[3] = {~0ull, ~0ull, 0ull};
+        COLO_CUDA(cudaMemcpyAsync(marks.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+    }
     px.alloc(lines ? lines : 1, s);
     py.alloc(lines ? lines : 1, s);
     praw.alloc(lines ? lines : 1, s);
     pst.alloc(lines ? lines : 1, s);
-    pfe.alloc(1, s);
-    COLO_CUDA(cudaMemsetAsync(pfe.get(), 0xFF, 8, s));
     if (lines) {
         KScope ks("csv_parse");
         k_parse_lines<<<(unsigned)((lines + 255) / 256), 256, 0, s>>>(dbuf.get(), nb, dnl.get(), L, lines, px.get(),
-                                                                     py.get(), praw.get(), pst.get(), pfe.get());
+                                                                     py.get(), praw.get(), pst.get(), marks.get(),
+                                                                     hlist.get(), host_cap);
         COLO_LAUNCH_CHECK();
         count_launch();
     }
-    unsigned long long first_empty = ~0ull;
-    std::vector<uint8_t> hst(lines);
-    COLO_CUDA(cudaMemcpyAsync(&first_empty, pfe.get(), 8, cudaMemcpyDeviceToHost, s));
-    if (lines) COLO_CUDA(cudaMemcpyAsync(hst.data(), pst.get(), lines, cudaMemcpyDeviceToHost, s));
+    unsigned long long hm[3] = {~0ull, ~0ull, 0ull};
+    COLO_CUDA(cudaMemcpyAsync(hm, marks.get(), sizeof(hm), cudaMemcpyDeviceToHost, s));
     COLO_CUDA(cudaStreamSynchronize(s));
+    const unsigned long long first_empty = hm[0];
     const uint64_t np = first_empty < lines ? first_empty : lines;   // point lines before the empty line
-    // lines the host reads: flagged point lines up to the first device failure, and the bounds line
-    uint64_t first_bad = np;
+    // the first failing device line before the empty line, and its kind
+    const uint64_t first_bad = hm[1] < np ? hm[1] : np;
+    uint8_t bad_kind = L_BAD;
+    if (first_bad < np) COLO_CUDA(cudaMemcpy(&bad_kind, pst.get() + first_bad, 1, cudaMemcpyDeviceToHost));
+    // lines the host reads: the listed ones before the first device failure, and the bounds line
     std::vector<uint64_t> want;
-    for (uint64_t i = 0; i < np; ++i) {
-        if (hst[i] == L_BAD || hst[i] == L_MINUS1) {
-            first_bad = i;
-            break;
-        }
-        if (hst[i] == L_HOST) want.push_back(i);
+    if (hm[2] > host_cap) {   // more than the list holds: find them from the statuses
+        std::vector<uint8_t> hst(np);
+        if (np) COLO_CUDA(cudaMemcpy(hst.data(), pst.get(), np, cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < first_bad; ++i)
+            if (hst[i] == L_HOST) want.push_back(i);
+    } else if (hm[2]) {
+        std::vector<uint64_t> hl(hm[2]);
+        COLO_CUDA(cudaMemcpy(hl.data(), hlist.get(), hm[2] * 8, cudaMemcpyDeviceToHost));
+        for (uint64_t i : hl)
+            if (i < first_bad) want.push_back(i);
+        std::sort(want.begin(), want.end());
     }
     const bool has_bounds = first_empty < lines && first_empty + 1 < lines;
     if (has_bounds) want.push_back(first_empty + 1);
@@ -438,7 +467,7 @@ colo_status parse_points_csv_device(cudaStream_t s, const char* path, HostPoints
         host_tokens.emplace_back(i, std::move(tok));
     }
     if (first_bad < np) {
-        err = hst[first_bad] == L_MINUS1 ? "dataset: feature id -1 is the reference's 'no feature yet' marker (line " +
+        err = bad_kind == L_MINUS1 ? "dataset: feature id -1 is the reference's 'no feature yet' marker (line " +
                                                std::to_string(first_bad + 2) + ")"
                                          : "dataset: malformed point line " + std::to_string(first_bad + 2);
         return COLO_ERR_PARSE;

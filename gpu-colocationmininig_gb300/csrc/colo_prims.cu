@@ -142,8 +142,13 @@ constexpr int kMaxRadix = kRadixDigits;
 constexpr int kMaxPasses = kRadixMaxPasses;
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortRounds = 8;                          // items per lane
-constexpr int kSortTile = kSortThreads * kSortRounds;   // 2048
+// Tile shape: 8 items per lane (2048-key tiles) and six resident blocks per
+// SM (40 registers for 32-bit keys).  The pass is latency-bound, so more tiles
+// in flight help; 4096-key tiles at three blocks per SM measured 4% slower.
+template <class KT>
+struct SortShape {
+    static constexpr int rounds = 8, min_blocks = 6;
+};
 
 
 // ---------------------------------------------------------------------------
@@ -202,14 +207,13 @@ __global__ void k_digit_scan(unsigned long long* __restrict__ ghist, int passes)
     }
 }
 
-// Six resident blocks per SM (40 registers for 32-bit keys): the look-back
-// and the tile's dependent loads are latency, so more tiles in flight help.
-template <class KT, int RB>
-__global__ void __launch_bounds__(kSortThreads, 6) k_onesweep(
+template <class KT, int RB, int kSortRounds = SortShape<KT>::rounds>
+__global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_onesweep(
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
     uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
     unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
     constexpr int R = 1 << RB;
+    constexpr int kSortTile = kSortThreads * kSortRounds;
     constexpr int D = R / kSortThreads;             // digits per thread in the look-back (1 or 2)
     static_assert(D >= 1 && D * kSortThreads == R, "digit count");
     __shared__ uint32_t wh[kSortWarps][R];
@@ -376,6 +380,7 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
     const RadixPlan plan = radix_plan(bits);
+    constexpr int kSortTile = kSortThreads * SortShape<KT>::rounds;
     const uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     DevBuf<KT> k2;
     DevBuf<uint32_t> v2, tickets, err;

@@ -184,7 +184,8 @@ __device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, int lane) {
 // A warp takes 32 consecutive cells, expands them into (Z, driver) pairs and
 // those into (Z, candidate) pairs (warp prefix sums; candidates of one driver
 // in adjacent lanes, so lanes share Z's masks in L1).
-// stats[c*2] = full quads, stats[c*2+1] = cells in U_c.
+// stats[c*2] = full quads, stats[c*2+1] = cells in U_c.  cjob is null for a
+// one-job batch (every cell in job 0), which saves the scan a load per cell.
 //
 // Sums go to a block-private accumulator in shared memory when the level's
 // candidates fit (acc_n = ncand * (m + 2) counters: m bounds, quads, cells),
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(256, (WT <= 8 ? 5 : 1)) k_filter_cells(
 #pragma unroll
     for (int w = 0; w < WT; ++w) nb_c[w] = 0;
     if (zbase + lane < M) {
-        job_c = cjob[zbase + lane];
+        job_c = cjob ? cjob[zbase + lane] : 0u;
         load_row<WT>(nbmask + (zbase + lane) * W, nb_c);
     }
     for (; zbase < M; zbase += zstride) {
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(256, (WT <= 8 ? 5 : 1)) k_filter_cells(
 #pragma unroll
         for (int w = 0; w < WT; ++w) nb_n[w] = 0;
         if (Zn < M) {
-            job_n = cjob[Zn];
+            job_n = cjob ? cjob[Zn] : 0u;
             load_row<WT>(nbmask + Zn * W, nb_n);
         }
         // this lane's cell and the drivers of its 3x3 block
@@ -461,7 +462,8 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     KScope ks("filter_level");
 #define COLO_FL(WW)                                                                                          \
     k_filter_cells<WW><<<grid((const void*)k_filter_cells<WW>), 256, smem, s>>>(                            \
-        b.M, b.cjob.get(), b.grids.get(), b.nbmask.get(), d_dmask, d_dcount, d_dstart, d_order, d_need, d_lmem, \
+        b.M, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), b.nbmask.get(), d_dmask, d_dcount, d_dstart, d_order,   \
+        d_need, d_lmem,                                                                                              \
         k, b.qmask.get(), b.cmask.get(), b.crun.get(), b.qfirst.get(), b.rcnt.get(), d_ub, d_stats, acc_n)
     switch (b.W) {
         case 1: COLO_FL(1); break;

@@ -125,14 +125,13 @@ struct LevelWork {
     const uint64_t* chunk_off;   // device: prefix of 32-row chunks per candidate (ncand+1)
     uint64_t ncand;
     uint64_t nchunks;
-    unsigned long long* next;    // device work counter (persistent kernels)
     unsigned long long* items;   // optional: sum of candidate-slice lengths examined
 };
 
 // count pass: slots + bitmaps; fill pass: rows; single pass: rows at
 // reserved positions + slots + bitmaps (overflow recorded per candidate).
-void level_count(Batch& b, const LevelWork& w, uint32_t k, bool persistent);
-void level_fill(Batch& b, const LevelWork& w, uint32_t k, bool persistent);
+void level_count(Batch& b, const LevelWork& w, uint32_t k);
+void level_fill(Batch& b, const LevelWork& w, uint32_t k);
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow);
 // Participation statistics per candidate and member: [A, last, first, full]
 // (A = set bits in [0, n-2]).

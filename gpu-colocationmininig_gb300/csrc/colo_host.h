@@ -117,5 +117,5 @@ uint64_t upload_dataset(colo_dataset* ds, cudaStream_t s);   // bytes copied (0 
 // Points, features, job grids and the bucketed/joined device state of a batch.
 // `own` keeps the concatenated device copies of multi-job batches alive.
 void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J, Batch& b,
-                 std::vector<DevBuf<float>>& ownf, std::vector<DevBuf<uint32_t>>& ownu, double* t_upload);
+                 std::vector<DevBuf<float>>& ownf, double* t_upload);
 }  // namespace colo

@@ -315,8 +315,8 @@ void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
 
 }  // namespace
 
-void level_count(Batch& b, const LevelWork& w, uint32_t k, bool) { launch_level<MODE_COUNT>(b, w, k, nullptr); }
-void level_fill(Batch& b, const LevelWork& w, uint32_t k, bool) { launch_level<MODE_FILL>(b, w, k, nullptr); }
+void level_count(Batch& b, const LevelWork& w, uint32_t k) { launch_level<MODE_COUNT>(b, w, k, nullptr); }
+void level_fill(Batch& b, const LevelWork& w, uint32_t k) { launch_level<MODE_FILL>(b, w, k, nullptr); }
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow) {
     launch_level<MODE_SINGLE>(b, w, k, d_overflow);
 }

@@ -258,7 +258,7 @@ uint64_t presize_rows(float pred) {
 // The mining driver for a batch of jobs.
 // ---------------------------------------------------------------------------
 void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J, Batch& b,
-                 std::vector<DevBuf<float>>& ownf, std::vector<DevBuf<uint32_t>>& ownu, double* t_upload) {
+                 std::vector<DevBuf<float>>& ownf, double* t_upload) {
     cudaStream_t s = ctx->s;
     b.s = s;
     b.sms = ctx->sms;
@@ -368,9 +368,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     const int mode = pv[0].mode;
     const bool plain = (mode == COLO_MODE_PLAIN);
     std::vector<DevBuf<float>> ownf;
-    std::vector<DevBuf<uint32_t>> ownu;
     double t_upload = 0;
-    setup_batch(ctx, dsv, pv, J, b, ownf, ownu, &t_upload);
+    setup_batch(ctx, dsv, pv, J, b, ownf, &t_upload);
     const uint64_t N = b.N;
     std::vector<JobState> js(J);
     for (uint32_t j = 0; j < J; ++j) {
@@ -726,17 +725,17 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), 2 * ncand * 8, cudaMemcpyHostToDevice, s));
                 for (uint64_t q = 0; q < ncand; ++q) {
-                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr, d_items.get()};
-                    level_count(b, w, k, false);
+                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], d_items.get()};
+                    level_count(b, w, k);
                     level_pi(b, ar.descs.get() + q, 1, k, ar.stats.get() + q * k * 4);
                     COLO_CUDA(cudaMemcpyAsync(hstats.data() + q * k * 4, ar.stats.get() + q * k * 4, k * 4 * 8,
                                               cudaMemcpyDeviceToHost, s));
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
             } else {
-                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), nullptr, d_items.get()};
+                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), d_items.get()};
                 if (learned) level_single(b, w, k, ar.overflow.get());
-                else level_count(b, w, k, true);
+                else level_count(b, w, k);
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
                 COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
             }
@@ -909,13 +908,13 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), hoff.size() * 8, cudaMemcpyHostToDevice, s));
                 for (size_t q = 0; q < fd.size(); ++q) {
-                    LevelWork w{dfd.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr, nullptr};
-                    level_fill(b, w, k, false);
+                    LevelWork w{dfd.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
+                    level_fill(b, w, k);
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
             } else {
-                LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr, nullptr};
-                level_fill(b, w, k, true);
+                LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr};
+                level_fill(b, w, k);
             }
         }
         COLO_CUDA(cudaStreamSynchronize(s));

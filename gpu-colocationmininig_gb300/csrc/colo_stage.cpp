@@ -32,9 +32,8 @@ colo_status colo_stage_cells(colo_ctx* ctx, colo_dataset* ds, float R, uint64_t*
         colo_params p = params_for(R, 0.f);
         Batch b;
         std::vector<DevBuf<float>> of;
-        std::vector<DevBuf<uint32_t>> ou;
         colo_dataset* dsv[1] = {ds};
-        setup_batch(ctx, dsv, &p, 1, b, of, ou, nullptr);
+        setup_batch(ctx, dsv, &p, 1, b, of, nullptr);
         if (b.N) bucket_points(b);
         cudaStream_t s = ctx->s;
         uint64_t cap = *nruns;
@@ -75,9 +74,8 @@ colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint6
         colo_params p = params_for(R, 0.f);
         Batch b;
         std::vector<DevBuf<float>> of;
-        std::vector<DevBuf<uint32_t>> ou;
         colo_dataset* dsv[1] = {ds};
-        setup_batch(ctx, dsv, &p, 1, b, of, ou, nullptr);
+        setup_batch(ctx, dsv, &p, 1, b, of, nullptr);
         uint64_t cap = *total;
         if (b.N) {
             bucket_points(b);
@@ -117,9 +115,8 @@ colo_status colo_stage_filter(colo_ctx* ctx, colo_dataset* ds, float R, float th
         colo_params p = params_for(R, thr);
         Batch b;
         std::vector<DevBuf<float>> of;
-        std::vector<DevBuf<uint32_t>> ou;
         colo_dataset* dsv[1] = {ds};
-        setup_batch(ctx, dsv, &p, 1, b, of, ou, nullptr);
+        setup_batch(ctx, dsv, &p, 1, b, of, nullptr);
         if (b.N) bucket_points(b);
         for (uint64_t c = 0; c < ncand * k; ++c)
             if (cand[c] >= b.F) return COLO_ERR_ARG;
@@ -226,9 +223,8 @@ colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p,
         static const int widths[4] = {4, 8, 16, 32};
         Batch b;
         std::vector<DevBuf<float>> of;
-        std::vector<DevBuf<uint32_t>> ou;
         colo_dataset* dsv[1] = {ds};
-        setup_batch(ctx, dsv, p, 1, b, of, ou, nullptr);
+        setup_batch(ctx, dsv, p, 1, b, of, nullptr);
         int best = 8;
         double best_ms = 1e300, t[4] = {0, 0, 0, 0};
         if (b.N) {

@@ -207,11 +207,49 @@ __global__ void k_digit_scan(unsigned long long* __restrict__ ghist, int passes)
     }
 }
 
+// Bulk (TMA engine) copy of a full tile from global to shared memory,
+// completing on an mbarrier: one thread issues it, every thread waits.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// dst and src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+// Waits for phase `parity` of the barrier at most `limit` polls; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// A full tile's keys and ids come into shared memory by one bulk copy each
+// (bulk != 0: the host checked that both arrays are 16-byte aligned); the
+// ranking reads them from there, and the same buffers then stage the tile
+// in digit order.
 template <class KT, int RB, int kSortRounds = SortShape<KT>::rounds>
 __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_onesweep(
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
     uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
-    unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
+    unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err, int bulk) {
     constexpr int R = 1 << RB;
     constexpr int kSortTile = kSortThreads * kSortRounds;
     constexpr int D = R / kSortThreads;             // digits per thread in the look-back (1 or 2)
@@ -219,16 +257,37 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
     __shared__ uint32_t wh[kSortWarps][R];
     __shared__ unsigned long long s_base[R];   // global position of the tile's first key of digit d
     __shared__ uint32_t s_off[R];              // tile-local position of the first key of digit d
-    __shared__ KT s_key[kSortTile];
-    __shared__ uint32_t s_val[kSortTile];
+    __shared__ alignas(16) KT s_key[kSortTile];
+    __shared__ alignas(16) uint32_t s_val[kSortTile];
+    __shared__ alignas(8) uint64_t s_bar;
     __shared__ uint32_t s_tile;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    if (threadIdx.x == 0) {
+        s_tile = atomicAdd(ticket, 1u);
+        if (bulk) mbar_init(&s_bar, 1);
+    }
     for (int i = threadIdx.x; i < kSortWarps * R; i += blockDim.x) (&wh[0][0])[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint64_t tile0 = (uint64_t)tile * kSortTile;
     const uint64_t base = tile0 + (uint64_t)w * (32 * kSortRounds);
+    const bool staged = bulk && n - tile0 >= (uint64_t)kSortTile;   // full tiles only (uniform in the block)
+    if (staged) {
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&s_bar, kSortTile * (uint32_t)(sizeof(KT) + sizeof(uint32_t)));
+            bulk_g2s(s_key, kin + tile0, kSortTile * (uint32_t)sizeof(KT), &s_bar);
+            bulk_g2s(s_val, vin + tile0, kSortTile * (uint32_t)sizeof(uint32_t), &s_bar);
+        }
+        const bool done = mbar_wait(&s_bar, 0, kSpinLimit);
+        if (!__syncthreads_and(done ? 1 : 0)) {
+            // the copy did not complete for every thread in time: report it, give it one
+            // more bounded wait (it writes into this block's shared memory) and leave, the
+            // whole block together; the host turns err into a timeout
+            if (threadIdx.x == 0) atomicOr(err, 1u);
+            mbar_wait(&s_bar, 0, kSpinLimit);
+            return;
+        }
+    }
     KT key[kSortRounds];
     uint32_t val[kSortRounds];
     uint32_t rank[kSortRounds];
@@ -237,8 +296,9 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
     for (int r = 0; r < kSortRounds; ++r) {
         const uint64_t i = base + (uint64_t)r * 32 + lane;
         const bool ok = i < n;
-        key[r] = ok ? kin[i] : 0;
-        val[r] = ok ? vin[i] : 0;
+        const uint32_t li = (uint32_t)(i - tile0);
+        key[r] = ok ? (staged ? s_key[li] : kin[i]) : 0;
+        val[r] = ok ? (staged ? s_val[li] : vin[i]) : 0;
         const uint32_t d = ok ? ((uint32_t)(key[r] >> shift) & dmask) : 0xFFFFu;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const int leader = __ffs(peers) - 1;
@@ -422,9 +482,10 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         KScope ks(name);   // one timed launch per digit pass
         const uint32_t dm = (1u << plan.width[p]) - 1u;
         COLO_CUDA(cudaMemsetAsync(status.get(), 0, (uint64_t)ntiles * kMaxRadix * 8, s));
+        const int bulk = ((uintptr_t)ka % 16 == 0 && (uintptr_t)va % 16 == 0) ? 1 : 0;
         k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
                                                                      hist + p * kMaxRadix, status.get(),
-                                                                     tickets.get() + p, errp);
+                                                                     tickets.get() + p, errp, bulk);
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);

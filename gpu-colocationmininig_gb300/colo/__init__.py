@@ -44,7 +44,7 @@ EXPORTS = [
     "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
     "colo_ctx_set_model", "colo_result_features", "colo_autotune", "colo_dataset_from_csv_threads",
     "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary", "colo_stage_apriori",
-    "colo_dataset_from_csv_device",
+    "colo_dataset_from_csv_device", "colo_set_join_group",
 ]
 MODEL_FEATURES = 24
 MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -138,6 +138,7 @@ def load(build: bool = True) -> C.CDLL:
                                        C.c_uint64, _f32p]),
         "colo_ctx_set_model": (C.c_int, [_P, _f32p]),
         "colo_autotune": (C.c_int, [_P, _P, C.POINTER(Params), _i32p, C.POINTER(C.c_double)]),
+        "colo_set_join_group": (C.c_int, [_P, C.c_int32]),
         "colo_result_features": (C.c_int, [_P, C.c_uint32, _f32p]),
     }
     for name, (res, args) in sig.items():
@@ -198,6 +199,8 @@ def csv_to_binary(csv_path: str, bin_path: str, threads: int = 0) -> None:
 
 
 BINARY_MAGIC = b"COLOPTS1"
+# lanes per anchor that the join autotuner times (colo_autotune, in this order)
+JOIN_WIDTHS = (1, 2, 4, 8, 16, 32)
 
 
 def read_binary(path: str):
@@ -410,9 +413,13 @@ class Context:
     def autotune(self, ds: "Dataset", params: Params) -> dict:
         """Pick the join's lanes per anchor for this dataset (kept for later mines)."""
         jg = C.c_int32(0)
-        ms = (C.c_double * 4)()
+        ms = (C.c_double * len(JOIN_WIDTHS))()
         self.check(self.lib.colo_autotune(self.h, ds.h, C.byref(params), C.byref(jg), ms), "autotune")
-        return {"join_group": int(jg.value), "join_ms": dict(zip((4, 8, 16, 32), list(ms)))}
+        return {"join_group": int(jg.value), "join_ms": dict(zip(JOIN_WIDTHS, list(ms)))}
+
+    def set_join_group(self, width: int) -> None:
+        """Pin the join's lanes per anchor (one of JOIN_WIDTHS; 0 for the default)."""
+        self.check(self.lib.colo_set_join_group(self.h, int(width)), "set_join_group")
 
     # ---- learned cost model -------------------------------------------------
     def model_forward(self, params: np.ndarray, x: np.ndarray) -> np.ndarray:

@@ -77,16 +77,27 @@ __global__ void __launch_bounds__(256) k_join(
     for (uint64_t q = run_sfx[r]; q < qend; ++q) {
         const uint32_t tr = nrl_run[q];
         const uint32_t ts = rstart[tr], tc = rcnt[tr];
-        for (uint32_t b0 = 0; b0 < tc; b0 += T) {
-            const uint32_t t = b0 + gl;
-            bool ok = false;
-            if (t < tc) {
+        if constexpr (T == 1) {
+            // one lane per anchor: no group vote
+            for (uint32_t t = 0; t < tc; ++t) {
                 const float2 pb = sxy[ts + t];
-                ok = ref_within(xa, ya, pb.x, pb.y, R2, hu);
+                if (ref_within(xa, ya, pb.x, pb.y, R2, hu)) {
+                    if (MODE != J_COUNT) nb[base + k] = sid[ts + t];
+                    ++k;
+                }
             }
-            const uint32_t bal = (__ballot_sync(gmask, ok) >> gbase) & ((T == 32) ? 0xffffffffu : ((1u << T) - 1u));
-            if (MODE != J_COUNT && ok) nb[base + k + __popc(bal & ((1u << gl) - 1u))] = sid[ts + t];
-            k += __popc(bal);
+        } else {
+            for (uint32_t b0 = 0; b0 < tc; b0 += T) {
+                const uint32_t t = b0 + gl;
+                bool ok = false;
+                if (t < tc) {
+                    const float2 pb = sxy[ts + t];
+                    ok = ref_within(xa, ya, pb.x, pb.y, R2, hu);
+                }
+                const uint32_t bal = (__ballot_sync(gmask, ok) >> gbase) & ((T == 32) ? 0xffffffffu : ((1u << T) - 1u));
+                if (MODE != J_COUNT && ok) nb[base + k + __popc(bal & ((1u << gl) - 1u))] = sid[ts + t];
+                k += __popc(bal);
+            }
         }
     }
     if (gl == 0) {
@@ -118,6 +129,8 @@ void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uin
 void dispatch_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uint32_t* act_run,
                    const uint64_t* cap_off) {
     switch (b.join_group) {
+        case 1: run_join<1>(b, mode, A, act_pos, act_run, cap_off); break;
+        case 2: run_join<2>(b, mode, A, act_pos, act_run, cap_off); break;
         case 4: run_join<4>(b, mode, A, act_pos, act_run, cap_off); break;
         case 16: run_join<16>(b, mode, A, act_pos, act_run, cap_off); break;
         case 32: run_join<32>(b, mode, A, act_pos, act_run, cap_off); break;

@@ -329,11 +329,15 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
         }
         uint32_t tot;
         uint32_t ex = block_excl_scan<uint32_t>(sum, &tot);
+        // status words and look-back for the dmask + 1 digits in use only (a tile's words
+        // are kMaxRadix apart: packing them closer measured slower)
+        const uint32_t nd = dmask + 1;
 #pragma unroll
         for (int i = 0; i < D; ++i) {
             const int d = threadIdx.x * D + i;
             s_off[d] = ex;
             ex += cnt[i];
+            if ((uint32_t)d >= nd) continue;
             volatile unsigned long long* st = status + (uint64_t)tile * R + d;
             unsigned long long prefix = 0;
             if (tile == 0) {
@@ -481,7 +485,9 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
     for (int p = 0; p < plan.n; ++p) {
         KScope ks(name);   // one timed launch per digit pass
         const uint32_t dm = (1u << plan.width[p]) - 1u;
-        COLO_CUDA(cudaMemsetAsync(status.get(), 0, (uint64_t)ntiles * kMaxRadix * 8, s));
+        // the words of the digits in use are cleared for every pass (a pitched clear:
+        // a tile's words stay kMaxRadix apart, which spreads the polled lines over L2)
+        COLO_CUDA(cudaMemset2DAsync(status.get(), kMaxRadix * 8, 0, ((size_t)1 << plan.width[p]) * 8, ntiles, s));
         const int bulk = ((uintptr_t)ka % 16 == 0 && (uintptr_t)va % 16 == 0) ? 1 : 0;
         k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
                                                                      hist + p * kMaxRadix, status.get(),

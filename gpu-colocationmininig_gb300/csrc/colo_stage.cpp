@@ -216,24 +216,26 @@ colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, c
     });
 }
 
+static constexpr int kJoinWidths = COLO_JOIN_WIDTHS;
+
 colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, int32_t* join_group,
                           double* ms) {
     if (!ctx || !ds || !p) return COLO_ERR_ARG;
     return run_guarded(ctx, [&]() -> colo_status {
-        static const int widths[4] = {4, 8, 16, 32};
+        static const int widths[kJoinWidths] = {1, 2, 4, 8, 16, 32};
         Batch b;
         std::vector<DevBuf<float>> of;
         colo_dataset* dsv[1] = {ds};
         setup_batch(ctx, dsv, p, 1, b, of, nullptr);
         int best = 8;
-        double best_ms = 1e300, t[4] = {0, 0, 0, 0};
+        double best_ms = 1e300, t[kJoinWidths] = {0, 0, 0, 0, 0, 0};
         if (b.N) {
             bucket_points(b);
             build_neighborhoods(b);
             cudaEvent_t e0, e1;
             COLO_CUDA(cudaEventCreate(&e0));
             COLO_CUDA(cudaEventCreate(&e1));
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < kJoinWidths; ++i) {
                 b.join_group = widths[i];
                 join_neighbors(b);   // warm-up
                 float tot = 0.f;
@@ -260,6 +262,15 @@ colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p,
         if (ms) std::memcpy(ms, t, sizeof(t));
         return COLO_OK;
     });
+}
+
+colo_status colo_set_join_group(colo_ctx* ctx, int32_t join_group) {
+    if (!ctx) return COLO_ERR_ARG;
+    if (join_group != 0 && join_group != 1 && join_group != 2 && join_group != 4 && join_group != 8 &&
+        join_group != 16 && join_group != 32)
+        return COLO_ERR_ARG;
+    ctx->join_group = join_group;
+    return COLO_OK;
 }
 
 }  // extern "C"

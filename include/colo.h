@@ -230,14 +230,19 @@ colo_status colo_stage_apriori(colo_ctx* ctx, const uint32_t* prev, uint64_t npr
                                uint32_t* parent, uint64_t cap, uint64_t* n_out);
 
 /* ---- autotuning ------------------------------------------------------- */
-/* Times the cell-pair join of this dataset at 4, 8, 16 and 32 lanes per
- * anchor (CUDA events, after a warm-up) and keeps the fastest for later
+/* Times the cell-pair join of this dataset at 1, 2, 4, 8, 16 and 32 lanes
+ * per anchor (CUDA events, after a warm-up) and keeps the fastest for later
  * mines on this context.  The join writes the same lists at every width.
- * join_group (optional) receives the choice, ms (optional, 4 doubles) the
- * times.  The cell size is not tuned: it is R, as the reference's neighbour
+ * join_group (optional) receives the choice, ms (optional,
+ * COLO_JOIN_WIDTHS doubles, in that order) the times.  The cell size is not tuned: it is R, as the reference's neighbour
  * rule is defined on that grid.  No counterpart in the reference. */
+#define COLO_JOIN_WIDTHS 6
 colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, int32_t* join_group,
                           double* ms);
+/* Sets the join's lanes per anchor for later mines on this context without
+ * timing (1, 2, 4, 8, 16 or 32; 0 restores the default).  COLO_ERR_ARG for any
+ * other width. */
+colo_status colo_set_join_group(colo_ctx* ctx, int32_t join_group);
 
 /* ---- learned cost model ----------------------------------------------- */
 /* A 24 -> 64 -> 64 -> 1 ReLU MLP (BF16 weights and activations, FP32

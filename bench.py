@@ -127,8 +127,8 @@ def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
         return 44.0 * M
     if name == "quad_masks":       # read 9 indices + masks, write 4 quad masks + the 3x3 union
         return 36.0 * M + 4.0 * words * M * 6
-    if name == "nrl_fill":         # write (feature, run) per list entry + per-run suffix and count
-        return 8.0 * c["nrl_entries"] + 12.0 * Rn
+    if name == "nrl_fill":         # write the run per list entry + per-run suffix and count
+        return 4.0 * c["nrl_entries"] + 12.0 * Rn
     if name == "join":             # B_b = 12 N + 4 E + 8 (N + 1): points once, lists and offsets written
         return 12.0 * N + 4.0 * E + 8.0 * (N + 1)
     if name in ("join_count", "join_fill"):   # the same split over the two-pass layout

@@ -55,9 +55,10 @@ struct Batch {
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
     // neighbourhood run lists: for cell c, the runs of its adjacent cells
-    // ordered by (feature, cell): nrl_feat/nrl_run[nrl_off[c] .. nrl_off[c+1])
+    // ordered by (feature, cell), entries above the cell's lowest own feature:
+    // nrl_run[nrl_off[c] .. nrl_off[c+1])
     DevBuf<uint64_t> nrl_off;
-    DevBuf<uint32_t> nrl_feat, nrl_run;
+    DevBuf<uint32_t> nrl_run;
     uint64_t nrl_total = 0;
     // per run: first entry of its cell's list with a higher feature (absolute
     // index) and the number of target points from there to the list's end

@@ -423,24 +423,55 @@ __device__ __forceinline__ int adjacent_cells(uint64_t c, const uint64_t* ckey, 
     return cnt;
 }
 
+// A cell's list keeps only the adjacent runs with a feature above the cell's
+// lowest own feature: the join reads a list from an own run's suffix on, and
+// the lowest own run's suffix starts past every entry of feature <= its own.
+// Most lists are then empty: the 3x3 mask (the union over all nine
+// neighbour slots, a superset of the adjacent cells) shows it without the
+// stencil.
 __global__ void k_nrl_count(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                             const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                            const uint32_t* __restrict__ crun, uint32_t* __restrict__ nrl_len) {
-    uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= M) return;
-    int32_t adj[9];
-    int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+                            const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
+                            const uint32_t* __restrict__ nbmask, uint32_t W, uint32_t* __restrict__ nrl_len,
+                            uint32_t* __restrict__ work, uint32_t* __restrict__ nwork) {
+    const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nr = 0;
-    for (int s = 0; s < na; ++s) nr += crun[adj[s] + 1] - crun[adj[s]];
-    nrl_len[c] = nr;
+    if (c < M) {
+        const uint32_t fmin = rfeat[crun[c]];
+        const uint32_t lf = fmin - grids[cjob[c]].f0;   // local feature index of the mask bits
+        const uint32_t* nm = nbmask + c * W;
+        const uint32_t w0 = lf >> 5, b0 = lf & 31;
+        uint32_t above = b0 == 31 ? 0u : (nm[w0] & (0xffffffffu << (b0 + 1)));
+        for (uint32_t w = w0 + 1; w < W && !above; ++w) above = nm[w];
+        if (above) {
+            int32_t adj[9];
+            const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+            for (int t = 0; t < na; ++t) {
+                const uint64_t q0 = crun[adj[t]], q1 = crun[adj[t] + 1];
+                nr += (uint32_t)(q1 - lower_bound_dev(rfeat, q0, q1, fmin + 1));
+            }
+        }
+        nrl_len[c] = nr;
+    }
+    // the cells with a list go to the fill's queue (one atomic per warp)
+    const uint32_t has = __ballot_sync(0xffffffffu, nr > 0);
+    if (has) {
+        const int lane = threadIdx.x & 31, leader = __ffs(has) - 1;
+        uint32_t at = 0;
+        if (lane == leader) at = atomicAdd(nwork, (uint32_t)__popc(has));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (nr > 0) work[at + __popc(has & ((1u << lane) - 1u))] = (uint32_t)c;
+    }
 }
 
-// The list of cell c (lanes l = 0..G-1 of a group share it).  A run of
-// feature f in adjacent slot s lands at sum over slots of (#runs with feature
-// < f) plus the number of earlier slots that also hold f.  Per own run of
-// the cell: the first entry with a higher feature and the number of target
-// points from there on (the points of each adjacent cell past its runs of
-// features <= f), both from one binary search per slot.
+// The list of cell c (lanes l = 0..G-1 of a group share it).  In the full
+// (feature, slot) order a run of feature f in adjacent slot s is at the sum
+// over slots of (#runs with feature < f) plus the number of earlier slots
+// that also hold f; the kept list drops the off0 entries of feature <= the
+// cell's lowest own feature.  Per own run of the cell: the first entry with a
+// higher feature and the number of target points from there on (the points
+// of each adjacent cell past its runs of features <= f), both from one binary
+// search per slot.
 template <int G>
 __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __restrict__ ckey,
                                          const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
@@ -448,23 +479,26 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
                                          const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
                                          const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ cmask,
                                          uint32_t W, const uint64_t* __restrict__ nrl_off,
-                                         uint32_t* __restrict__ nrl_feat, uint32_t* __restrict__ nrl_run,
-                                         uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
+                                         uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
+                                         uint32_t* __restrict__ run_L) {
     int32_t adj[9];
     const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+    const uint32_t fmin = rfeat[crun[c]];
     uint32_t q0[9], q1[9], pre[10];
+    uint64_t off0 = 0;
     pre[0] = 0;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
         if (t < na) {
             q0[t] = crun[adj[t]];
             q1[t] = crun[adj[t] + 1];
+            off0 += lower_bound_dev(rfeat, (uint64_t)q0[t], (uint64_t)q1[t], fmin + 1) - q0[t];
         } else {
             q0[t] = q1[t] = 0;
         }
         pre[t + 1] = pre[t] + (q1[t] - q0[t]);
     }
-    const uint64_t base = nrl_off[c];
+    const uint64_t base = nrl_off[c] - off0;   // where entry 0 of the full order would be
     for (uint32_t e = l; e < pre[9]; e += G) {
         int sl = 0;
         uint32_t r = 0;
@@ -475,6 +509,7 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
                 r = q0[t] + (e - pre[t]);
             }
         const uint32_t f = rfeat[r];
+        if (f <= fmin) continue;
         uint64_t pos = 0;
 #pragma unroll
         for (int t = 0; t < 9; ++t) {
@@ -484,7 +519,6 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
                 if (t < sl && lb < q1[t] && rfeat[lb] == f) pos += 1;
             }
         }
-        nrl_feat[base + pos] = f;
         nrl_run[base + pos] = r;
     }
     for (uint32_t r = crun[c] + l; r < crun[c + 1]; r += G) {
@@ -506,36 +540,36 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
 
 constexpr uint32_t kBigList = 512;   // cells with longer lists get a warp each
 
-// One thread per cell: the list is the 9-way merge of the adjacent cells'
-// run lists (each ascending by feature) by (feature, slot).  The running
-// point count P gives the suffix counts: the cell's own run of feature f
-// gets sfx = the first position after every entry of feature <= f and
-// L = (total points) - P(sfx).  Cells with lists longer than kBigList are
-// queued for k_nrl_fill_big.
-__global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                           const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                           const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
-                           const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
-                           const uint32_t* __restrict__ rcnt,
-                           const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_feat,
-                           uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
-                           uint32_t* __restrict__ run_L, uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
-    uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= M) return;
-    const uint64_t base = nrl_off[c];
-    if (nrl_off[c + 1] - base > kBigList) {
+// One thread per cell: the list is the 9-way merge, by (feature, slot), of
+// the adjacent cells' runs above the lowest own feature (each slot ascending
+// by feature).  The running point count P gives the suffix counts: the
+// cell's own run of feature f gets sfx = the first position after every
+// entry of feature <= f and L = (points in the list) - P(sfx).  Cells with
+// lists longer than kBigList are queued for k_nrl_fill_big.
+__device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __restrict__ ckey,
+                                              const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
+                                              const int32_t* __restrict__ nb9, const uint32_t* __restrict__ crun,
+                                              const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt,
+                                              const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_run,
+                                              uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L,
+                                              uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
+    const uint64_t base = nrl_off[c], kept = nrl_off[c + 1] - base;
+    const uint32_t r0 = crun[c], r1 = crun[c + 1];
+    if (kept > kBigList) {   // the merge below is serial in the list
         big[atomicAdd(nbig, 1u)] = (uint32_t)c;
         return;
     }
     int32_t adj[9];
     const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+    const uint32_t fmin = rfeat[r0];
+    // each slot's cursor starts at its first run above the lowest own feature
     uint32_t h[9], e[9], f[9];
     int own = 0;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
         if (t < na) {
-            h[t] = crun[adj[t]];
             e[t] = crun[adj[t] + 1];
+            h[t] = (uint32_t)lower_bound_dev(rfeat, (uint64_t)crun[adj[t]], (uint64_t)e[t], fmin + 1);
             f[t] = h[t] < e[t] ? rfeat[h[t]] : 0xffffffffu;
             if ((uint64_t)adj[t] == c) own = t;
         } else {
@@ -543,6 +577,9 @@ __global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const 
             f[t] = 0xffffffffu;
         }
     }
+    // the lowest own run's suffix is the whole list
+    run_sfx[r0] = base;
+    run_L[r0] = 0;
     uint64_t pos = base;
     uint32_t P = 0, pend_r = 0, pend_f = 0;
     bool pend = false;
@@ -568,9 +605,7 @@ __global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const 
                 r = h[t]++;
                 f[t] = h[t] < e[t] ? rfeat[h[t]] : 0xffffffffu;
             }
-        nrl_feat[pos] = fm;
-        nrl_run[pos] = r;
-        ++pos;
+        nrl_run[pos++] = r;
         P += rcnt[r];
         if (ts == own) {
             pend = true;
@@ -582,7 +617,22 @@ __global__ void k_nrl_fill(uint64_t M, const uint64_t* __restrict__ ckey, const 
         run_sfx[pend_r] = pos;
         run_L[pend_r] = P;
     }
-    for (uint32_t r = crun[c]; r < crun[c + 1]; ++r) run_L[r] = P - run_L[r];
+    for (uint32_t r = r0; r < r1; ++r) run_L[r] = P - run_L[r];
+}
+
+// Grid-stride over the queue of cells with a list (the count pass's queue);
+// run_L is zero for every other run, run_sfx is read only where run_L > 0.
+__global__ void k_nrl_fill(const uint32_t* __restrict__ work, const uint32_t* __restrict__ nwork,
+                           const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+                           const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
+                           const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
+                           const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ nrl_off,
+                           uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
+                           uint32_t* __restrict__ run_L, uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
+    const uint32_t n = *nwork;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        nrl_fill_cell(work[i], ckey, cjob, grids, nb9, crun, rfeat, rcnt, nrl_off, nrl_run, run_sfx, run_L, big,
+                      nbig);
 }
 
 // A warp per queued cell (grid-stride over the queue).
@@ -592,14 +642,13 @@ __global__ void k_nrl_fill_big(const uint32_t* __restrict__ big, const uint32_t*
                                const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
                                const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
                                const uint32_t* __restrict__ cmask, uint32_t W,
-                               const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_feat,
-                               uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
-                               uint32_t* __restrict__ run_L) {
+                               const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_run,
+                               uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
     const uint32_t n = *nbig;
     const int lane = threadIdx.x & 31;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5)
-        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, cmask, W, nrl_off, nrl_feat,
-                     nrl_run, run_sfx, run_L);
+        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, cmask, W, nrl_off, nrl_run,
+                     run_sfx, run_L);
 }
 
 inline unsigned grid_for(uint64_t n, int threads) {
@@ -781,12 +830,16 @@ void bucket_points(Batch& b) {
 void build_neighborhoods(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t M = b.M;
-    DevBuf<uint32_t> nrl_len;
+    DevBuf<uint32_t> nrl_len, work, nwork;
     nrl_len.alloc(M, s);
+    work.alloc(M ? M : 1, s);
+    nwork.alloc(1, s);
+    nwork.zero(s);
     {
         KScope ks("nrl_count");
         k_nrl_count<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
-                                                      b.crun.get(), nrl_len.get());
+                                                      b.crun.get(), b.rfeat.get(), b.nbmask.get(), b.W,
+                                                      nrl_len.get(), work.get(), nwork.get());
         COLO_LAUNCH_CHECK();
         count_launch();
     }
@@ -795,8 +848,7 @@ void build_neighborhoods(Batch& b) {
     scan_u32_to_u64(nrl_len.get(), b.nrl_off.get(), M, s, &tr);
     COLO_CUDA(cudaMemcpyAsync(b.nrl_off.get() + M, &tr, 8, cudaMemcpyHostToDevice, s));
     b.nrl_total = tr;
-    b.nrl_feat.alloc(tr, s);
-    b.nrl_run.alloc(tr, s);
+    b.nrl_run.alloc(tr ? tr : 1, s);
     b.run_sfx.alloc(b.Rn, s);
     b.run_L.alloc(b.Rn, s);
     {
@@ -805,17 +857,18 @@ void build_neighborhoods(Batch& b) {
         big.alloc(M ? M : 1, s);
         nbig.alloc(1, s);
         nbig.zero(s);
-        k_nrl_fill<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
-                                                     b.cstart.get(), b.crun.get(), b.rfeat.get(), b.rstart.get(),
-                                                     b.rcnt.get(), b.nrl_off.get(), b.nrl_feat.get(),
-                                                     b.nrl_run.get(), b.run_sfx.get(), b.run_L.get(), big.get(),
-                                                     nbig.get());
+        COLO_CUDA(cudaMemsetAsync(b.run_L.get(), 0, b.Rn * 4, s));
+        const uint64_t cap = grid_for(M, 128);
+        k_nrl_fill<<<(unsigned)std::min<uint64_t>(cap, (uint64_t)b.sms * 16), 128, 0, s>>>(
+            work.get(), nwork.get(), b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.crun.get(),
+            b.rfeat.get(), b.rcnt.get(), b.nrl_off.get(), b.nrl_run.get(), b.run_sfx.get(), b.run_L.get(), big.get(),
+            nbig.get());
         COLO_LAUNCH_CHECK();
         k_nrl_fill_big<<<(unsigned)(b.sms * 8), 256, 0, s>>>(big.get(), nbig.get(), b.ckey.get(), b.cjob.get(),
                                                              b.grids.get(), b.nb9.get(), b.cstart.get(), b.crun.get(),
                                                              b.rfeat.get(), b.rstart.get(), b.cmask.get(), b.W,
-                                                             b.nrl_off.get(), b.nrl_feat.get(), b.nrl_run.get(),
-                                                             b.run_sfx.get(), b.run_L.get());
+                                                             b.nrl_off.get(), b.nrl_run.get(), b.run_sfx.get(),
+                                                             b.run_L.get());
         COLO_LAUNCH_CHECK();
         count_launch(2);
     }

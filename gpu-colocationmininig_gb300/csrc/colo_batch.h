@@ -50,6 +50,7 @@ struct Batch {
     DevBuf<int32_t> nb9;
     DevBuf<uint32_t> cmask;
     DevBuf<uint32_t> nbmask;     // per cell: feature mask of its geometric 3x3 block
+    DevBuf<uint32_t> listq, nlistq;   // cells whose 3x3 block has a feature above their lowest own one
     DevBuf<uint32_t> qmask;      // per cell: masks of the 4 quads containing it ([M][4][W])
     DevBuf<uint8_t> qfirst;      // per cell: bit q set when it is the first occupied cell of its quad q
     // runs

@@ -334,48 +334,86 @@ __device__ __forceinline__ void st_row(uint32_t* __restrict__ p, const uint32_t 
     }
 }
 
+constexpr int kQuadThreads = 128;
+
 template <int WT>
-__global__ void k_quad_masks(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
-                             const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
-                             const uint32_t* __restrict__ cmask, uint32_t* __restrict__ qmask,
-                             uint32_t* __restrict__ nbmask) {
+__global__ void __launch_bounds__(kQuadThreads) k_quad_masks(
+    uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+    const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
+    uint32_t* __restrict__ qmask, uint32_t* __restrict__ nbmask, uint32_t* __restrict__ listq,
+    uint32_t* __restrict__ nlistq) {
     const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= M) return;
-    const JobGrid g = grids[cjob[c]];
-    const uint64_t local = ckey[c] - g.key_base;
-    const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
-    int32_t nb[9];
+    bool above = false;
+    if (c < M) {
+        const JobGrid g = grids[cjob[c]];
+        const uint64_t local = ckey[c] - g.key_base;
+        const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+        int32_t nb[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) nb[q] = nb9[c * 9 + q];
-    uint32_t m[9][WT];
-    uint32_t all[WT];
+        for (int q = 0; q < 9; ++q) nb[q] = nb9[c * 9 + q];
+        uint32_t m[9][WT];
+        uint32_t all[WT];
 #pragma unroll
-    for (int w = 0; w < WT; ++w) all[w] = 0;
+        for (int w = 0; w < WT; ++w) all[w] = 0;
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        if (nb[q] >= 0) {
-            ld_row<WT>(cmask + (uint64_t)nb[q] * WT, m[q]);
-        } else {
+        for (int q = 0; q < 9; ++q) {
+            if (nb[q] >= 0) {
+                ld_row<WT>(cmask + (uint64_t)nb[q] * WT, m[q]);
+            } else {
 #pragma unroll
-            for (int w = 0; w < WT; ++w) m[q][w] = 0;
+                for (int w = 0; w < WT; ++w) m[q][w] = 0;
+            }
+#pragma unroll
+            for (int w = 0; w < WT; ++w) all[w] |= m[q][w];
+        }
+        st_row<WT>(nbmask + c * WT, all);
+        // the cell needs a neighbourhood run list when its 3x3 block holds a
+        // feature above its own lowest one (m[4] is the cell's own mask; the block
+        // is the union over all nine slots, a superset of the adjacent cells):
+        // such cells are queued for the list kernels
+        bool seen = false;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) {
+            const uint32_t own = m[4][w];
+            if (seen) {
+                above |= all[w] != 0;
+            } else if (own) {
+                seen = true;
+                const uint32_t low = own & (0u - own);
+                above |= (all[w] & ~((low << 1) - 1u)) != 0;
+            }
         }
 #pragma unroll
-        for (int w = 0; w < WT; ++w) all[w] |= m[q][w];
-    }
-    st_row<WT>(nbmask + c * WT, all);
+        for (int q = 0; q < 4; ++q) {
+            const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
+            const int64_t bx = cx + qx, by = cy + qy;
+            const bool valid = bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy;
+            uint32_t qm[WT];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
-        const int64_t bx = cx + qx, by = cy + qy;
-        const bool valid = bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy;
-        uint32_t qm[WT];
-#pragma unroll
-        for (int w = 0; w < WT; ++w)
-            qm[w] = valid ? (m[(qy + 1) * 3 + qx + 1][w] | m[(qy + 1) * 3 + qx + 2][w] | m[(qy + 2) * 3 + qx + 1][w] |
-                             m[(qy + 2) * 3 + qx + 2][w])
-                          : 0u;
-        st_row<WT>(qmask + (c * 4 + q) * WT, qm);
+            for (int w = 0; w < WT; ++w)
+                qm[w] = valid ? (m[(qy + 1) * 3 + qx + 1][w] | m[(qy + 1) * 3 + qx + 2][w] | m[(qy + 2) * 3 + qx + 1][w] |
+                                 m[(qy + 2) * 3 + qx + 2][w])
+                              : 0u;
+            st_row<WT>(qmask + (c * 4 + q) * WT, qm);
+        }
     }
+    // one atomic per block for the queue
+    __shared__ uint32_t s_cnt[kQuadThreads / 32], s_base;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t has = __ballot_sync(0xffffffffu, above);
+    if (lane == 0) s_cnt[wid] = (uint32_t)__popc(has);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kQuadThreads / 32; ++w) {
+            const uint32_t v = s_cnt[w];
+            s_cnt[w] = t;
+            t += v;
+        }
+        s_base = t ? atomicAdd(nlistq, t) : 0u;
+    }
+    __syncthreads();
+    if (above) listq[s_base + s_cnt[wid] + __popc(has & ((1u << lane) - 1u))] = (uint32_t)c;
 }
 
 // Runs per feature: a block-local histogram (F <= kHistMax), else global atomics.
@@ -426,41 +464,25 @@ __device__ __forceinline__ int adjacent_cells(uint64_t c, const uint64_t* ckey, 
 // A cell's list keeps only the adjacent runs with a feature above the cell's
 // lowest own feature: the join reads a list from an own run's suffix on, and
 // the lowest own run's suffix starts past every entry of feature <= its own.
-// Most lists are then empty: the 3x3 mask (the union over all nine
-// neighbour slots, a superset of the adjacent cells) shows it without the
-// stencil.
-__global__ void k_nrl_count(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+// Most lists are then empty; the cells whose 3x3 mask allows one were queued
+// by k_quad_masks (nrl_len is zero for the others).  Grid-stride over the queue.
+__global__ void k_nrl_count(const uint32_t* __restrict__ listq, const uint32_t* __restrict__ nlistq,
+                            const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                             const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
                             const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
-                            const uint32_t* __restrict__ nbmask, uint32_t W, uint32_t* __restrict__ nrl_len,
-                            uint32_t* __restrict__ work, uint32_t* __restrict__ nwork) {
-    const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t nr = 0;
-    if (c < M) {
+                            uint32_t* __restrict__ nrl_len) {
+    const uint32_t n = *nlistq;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t c = listq[i];
         const uint32_t fmin = rfeat[crun[c]];
-        const uint32_t lf = fmin - grids[cjob[c]].f0;   // local feature index of the mask bits
-        const uint32_t* nm = nbmask + c * W;
-        const uint32_t w0 = lf >> 5, b0 = lf & 31;
-        uint32_t above = b0 == 31 ? 0u : (nm[w0] & (0xffffffffu << (b0 + 1)));
-        for (uint32_t w = w0 + 1; w < W && !above; ++w) above = nm[w];
-        if (above) {
-            int32_t adj[9];
-            const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
-            for (int t = 0; t < na; ++t) {
-                const uint64_t q0 = crun[adj[t]], q1 = crun[adj[t] + 1];
-                nr += (uint32_t)(q1 - lower_bound_dev(rfeat, q0, q1, fmin + 1));
-            }
+        int32_t adj[9];
+        const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
+        uint32_t nr = 0;
+        for (int t = 0; t < na; ++t) {
+            const uint64_t q0 = crun[adj[t]], q1 = crun[adj[t] + 1];
+            nr += (uint32_t)(q1 - lower_bound_dev(rfeat, q0, q1, fmin + 1));
         }
         nrl_len[c] = nr;
-    }
-    // the cells with a list go to the fill's queue (one atomic per warp)
-    const uint32_t has = __ballot_sync(0xffffffffu, nr > 0);
-    if (has) {
-        const int lane = threadIdx.x & 31, leader = __ffs(has) - 1;
-        uint32_t at = 0;
-        if (lane == leader) at = atomicAdd(nwork, (uint32_t)__popc(has));
-        at = __shfl_sync(0xffffffffu, at, leader);
-        if (nr > 0) work[at + __popc(has & ((1u << lane) - 1u))] = (uint32_t)c;
     }
 }
 
@@ -554,6 +576,7 @@ __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __rest
                                               uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L,
                                               uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
     const uint64_t base = nrl_off[c], kept = nrl_off[c + 1] - base;
+    if (kept == 0) return;   // no own run has targets (run_L is zero)
     const uint32_t r0 = crun[c], r1 = crun[c + 1];
     if (kept > kBigList) {   // the merge below is serial in the list
         big[atomicAdd(nbig, 1u)] = (uint32_t)c;
@@ -620,8 +643,8 @@ __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __rest
     for (uint32_t r = r0; r < r1; ++r) run_L[r] = P - run_L[r];
 }
 
-// Grid-stride over the queue of cells with a list (the count pass's queue);
-// run_L is zero for every other run, run_sfx is read only where run_L > 0.
+// Grid-stride over the queued cells; run_L is zero for every run of the
+// others, and run_sfx is read only where run_L > 0.
 __global__ void k_nrl_fill(const uint32_t* __restrict__ work, const uint32_t* __restrict__ nwork,
                            const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                            const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
@@ -772,11 +795,15 @@ void bucket_points(Batch& b) {
     }
     b.nbmask.alloc((uint64_t)M * b.W, s);
     b.qmask.alloc((uint64_t)M * 4 * b.W, s);
+    b.listq.alloc(M ? M : 1, s);
+    b.nlistq.alloc(1, s);
+    b.nlistq.zero(s);
     {
         KScope ks("quad_masks");
 #define COLO_QM(WW)                                                                                    \
-    k_quad_masks<WW><<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), \
-                                                      b.cmask.get(), b.qmask.get(), b.nbmask.get())
+    k_quad_masks<WW><<<grid_for(M, kQuadThreads), kQuadThreads, 0, s>>>(                              \
+        M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(),       \
+        b.nbmask.get(), b.listq.get(), b.nlistq.get())
         switch (b.W) {
             case 1: COLO_QM(1); break;
             case 2: COLO_QM(2); break;
@@ -830,16 +857,14 @@ void bucket_points(Batch& b) {
 void build_neighborhoods(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t M = b.M;
-    DevBuf<uint32_t> nrl_len, work, nwork;
-    nrl_len.alloc(M, s);
-    work.alloc(M ? M : 1, s);
-    nwork.alloc(1, s);
-    nwork.zero(s);
+    DevBuf<uint32_t> nrl_len;
+    nrl_len.alloc(M ? M : 1, s);
+    nrl_len.zero(s);
+    const unsigned qgrid = (unsigned)std::min<uint64_t>(grid_for(M, 128), (uint64_t)b.sms * 16);
     {
         KScope ks("nrl_count");
-        k_nrl_count<<<grid_for(M, 128), 128, 0, s>>>(M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(),
-                                                      b.crun.get(), b.rfeat.get(), b.nbmask.get(), b.W,
-                                                      nrl_len.get(), work.get(), nwork.get());
+        k_nrl_count<<<qgrid, 128, 0, s>>>(b.listq.get(), b.nlistq.get(), b.ckey.get(), b.cjob.get(), b.grids.get(),
+                                          b.nb9.get(), b.crun.get(), b.rfeat.get(), nrl_len.get());
         COLO_LAUNCH_CHECK();
         count_launch();
     }
@@ -858,9 +883,8 @@ void build_neighborhoods(Batch& b) {
         nbig.alloc(1, s);
         nbig.zero(s);
         COLO_CUDA(cudaMemsetAsync(b.run_L.get(), 0, b.Rn * 4, s));
-        const uint64_t cap = grid_for(M, 128);
-        k_nrl_fill<<<(unsigned)std::min<uint64_t>(cap, (uint64_t)b.sms * 16), 128, 0, s>>>(
-            work.get(), nwork.get(), b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.crun.get(),
+        k_nrl_fill<<<qgrid, 128, 0, s>>>(
+            b.listq.get(), b.nlistq.get(), b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.crun.get(),
             b.rfeat.get(), b.rcnt.get(), b.nrl_off.get(), b.nrl_run.get(), b.run_sfx.get(), b.run_L.get(), big.get(),
             nbig.get());
         COLO_LAUNCH_CHECK();

@@ -57,13 +57,16 @@ struct Batch {
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
     // neighbourhood run lists: for cell c, the runs of its adjacent cells
     // ordered by (feature, cell), entries above the cell's lowest own feature:
-    // nrl_run[nrl_off[c] .. nrl_off[c+1])
+    // nrl_ent[nrl_off[c] .. nrl_off[c+1]), each the run's (first sorted
+    // position, point count)
     DevBuf<uint64_t> nrl_off;
-    DevBuf<uint32_t> nrl_run;
+    DevBuf<uint2> nrl_ent;
     uint64_t nrl_total = 0;
     // per run: first entry of its cell's list with a higher feature (absolute
-    // index) and the number of target points from there to the list's end
+    // index), the entries from there to the list's end (run_qn), and the
+    // number of target points in them; run_sfx and run_qn are set where run_L > 0
     DevBuf<uint64_t> run_sfx;
+    DevBuf<uint32_t> run_qn;
     DevBuf<uint32_t> run_L;
     // neighbour lists N+(a) = nb[nb_beg[a] .. nb_beg[a] + nb_cnt[a]), each in
     // (feature, neighbour cell, id) order

@@ -500,8 +500,9 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
                                          const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cstart,
                                          const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
                                          const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ cmask,
-                                         uint32_t W, const uint64_t* __restrict__ nrl_off,
-                                         uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
+                                         const uint32_t* __restrict__ rcnt, uint32_t W,
+                                         const uint64_t* __restrict__ nrl_off, uint2* __restrict__ nrl_ent,
+                                         uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_qn,
                                          uint32_t* __restrict__ run_L) {
     int32_t adj[9];
     const int na = adjacent_cells(c, ckey, cjob, grids, nb9, adj);
@@ -541,7 +542,7 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
                 if (t < sl && lb < q1[t] && rfeat[lb] == f) pos += 1;
             }
         }
-        nrl_run[base + pos] = r;
+        nrl_ent[base + pos] = make_uint2(rstart[r], rcnt[r]);
     }
     for (uint32_t r = crun[c] + l; r < crun[c + 1]; r += G) {
         const uint32_t f = rfeat[r];
@@ -556,6 +557,7 @@ __device__ __forceinline__ void nrl_cell(uint64_t c, int l, const uint64_t* __re
             }
         }
         run_sfx[r] = sfx;
+        run_qn[r] = (uint32_t)(nrl_off[c + 1] - sfx);
         run_L[r] = L;
     }
 }
@@ -571,9 +573,10 @@ constexpr uint32_t kBigList = 512;   // cells with longer lists get a warp each
 __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __restrict__ ckey,
                                               const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
                                               const int32_t* __restrict__ nb9, const uint32_t* __restrict__ crun,
-                                              const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rcnt,
-                                              const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_run,
-                                              uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L,
+                                              const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
+                                              const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ nrl_off,
+                                              uint2* __restrict__ nrl_ent, uint64_t* __restrict__ run_sfx,
+                                              uint32_t* __restrict__ run_qn, uint32_t* __restrict__ run_L,
                                               uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
     const uint64_t base = nrl_off[c], kept = nrl_off[c + 1] - base;
     if (kept == 0) return;   // no own run has targets (run_L is zero)
@@ -601,7 +604,9 @@ __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __rest
         }
     }
     // the lowest own run's suffix is the whole list
+    const uint64_t end = base + kept;
     run_sfx[r0] = base;
+    run_qn[r0] = (uint32_t)kept;
     run_L[r0] = 0;
     uint64_t pos = base;
     uint32_t P = 0, pend_r = 0, pend_f = 0;
@@ -618,6 +623,7 @@ __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __rest
         if (fm == 0xffffffffu) break;
         if (pend && pend_f < fm) {
             run_sfx[pend_r] = pos;
+            run_qn[pend_r] = (uint32_t)(end - pos);
             run_L[pend_r] = P;
             pend = false;
         }
@@ -628,8 +634,9 @@ __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __rest
                 r = h[t]++;
                 f[t] = h[t] < e[t] ? rfeat[h[t]] : 0xffffffffu;
             }
-        nrl_run[pos++] = r;
-        P += rcnt[r];
+        const uint32_t rc = rcnt[r];
+        nrl_ent[pos++] = make_uint2(rstart[r], rc);
+        P += rc;
         if (ts == own) {
             pend = true;
             pend_r = r;
@@ -638,6 +645,7 @@ __device__ __forceinline__ void nrl_fill_cell(uint64_t c, const uint64_t* __rest
     }
     if (pend) {
         run_sfx[pend_r] = pos;
+        run_qn[pend_r] = 0;
         run_L[pend_r] = P;
     }
     for (uint32_t r = r0; r < r1; ++r) run_L[r] = P - run_L[r];
@@ -649,13 +657,14 @@ __global__ void k_nrl_fill(const uint32_t* __restrict__ work, const uint32_t* __
                            const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                            const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9,
                            const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
-                           const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ nrl_off,
-                           uint32_t* __restrict__ nrl_run, uint64_t* __restrict__ run_sfx,
+                           const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ rcnt,
+                           const uint64_t* __restrict__ nrl_off, uint2* __restrict__ nrl_ent,
+                           uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_qn,
                            uint32_t* __restrict__ run_L, uint32_t* __restrict__ big, uint32_t* __restrict__ nbig) {
     const uint32_t n = *nwork;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        nrl_fill_cell(work[i], ckey, cjob, grids, nb9, crun, rfeat, rcnt, nrl_off, nrl_run, run_sfx, run_L, big,
-                      nbig);
+        nrl_fill_cell(work[i], ckey, cjob, grids, nb9, crun, rfeat, rstart, rcnt, nrl_off, nrl_ent, run_sfx, run_qn,
+                      run_L, big, nbig);
 }
 
 // A warp per queued cell (grid-stride over the queue).
@@ -665,13 +674,14 @@ __global__ void k_nrl_fill_big(const uint32_t* __restrict__ big, const uint32_t*
                                const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ crun,
                                const uint32_t* __restrict__ rfeat, const uint32_t* __restrict__ rstart,
                                const uint32_t* __restrict__ cmask, uint32_t W,
-                               const uint64_t* __restrict__ nrl_off, uint32_t* __restrict__ nrl_run,
-                               uint64_t* __restrict__ run_sfx, uint32_t* __restrict__ run_L) {
+                               const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ nrl_off,
+                               uint2* __restrict__ nrl_ent, uint64_t* __restrict__ run_sfx,
+                               uint32_t* __restrict__ run_qn, uint32_t* __restrict__ run_L) {
     const uint32_t n = *nbig;
     const int lane = threadIdx.x & 31;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5)
-        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, cmask, W, nrl_off, nrl_run,
-                     run_sfx, run_L);
+        nrl_cell<32>(big[i], lane, ckey, cjob, grids, nb9, cstart, crun, rfeat, rstart, cmask, rcnt, W, nrl_off,
+                     nrl_ent, run_sfx, run_qn, run_L);
 }
 
 inline unsigned grid_for(uint64_t n, int threads) {
@@ -873,8 +883,9 @@ void build_neighborhoods(Batch& b) {
     scan_u32_to_u64(nrl_len.get(), b.nrl_off.get(), M, s, &tr);
     COLO_CUDA(cudaMemcpyAsync(b.nrl_off.get() + M, &tr, 8, cudaMemcpyHostToDevice, s));
     b.nrl_total = tr;
-    b.nrl_run.alloc(tr ? tr : 1, s);
+    b.nrl_ent.alloc(tr ? tr : 1, s);
     b.run_sfx.alloc(b.Rn, s);
+    b.run_qn.alloc(b.Rn, s);
     b.run_L.alloc(b.Rn, s);
     {
         KScope ks("nrl_fill");
@@ -885,14 +896,14 @@ void build_neighborhoods(Batch& b) {
         COLO_CUDA(cudaMemsetAsync(b.run_L.get(), 0, b.Rn * 4, s));
         k_nrl_fill<<<qgrid, 128, 0, s>>>(
             b.listq.get(), b.nlistq.get(), b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.crun.get(),
-            b.rfeat.get(), b.rcnt.get(), b.nrl_off.get(), b.nrl_run.get(), b.run_sfx.get(), b.run_L.get(), big.get(),
-            nbig.get());
+            b.rfeat.get(), b.rstart.get(), b.rcnt.get(), b.nrl_off.get(), b.nrl_ent.get(), b.run_sfx.get(),
+            b.run_qn.get(), b.run_L.get(), big.get(), nbig.get());
         COLO_LAUNCH_CHECK();
         k_nrl_fill_big<<<(unsigned)(b.sms * 8), 256, 0, s>>>(big.get(), nbig.get(), b.ckey.get(), b.cjob.get(),
                                                              b.grids.get(), b.nb9.get(), b.cstart.get(), b.crun.get(),
                                                              b.rfeat.get(), b.rstart.get(), b.cmask.get(), b.W,
-                                                             b.nrl_off.get(), b.nrl_run.get(), b.run_sfx.get(),
-                                                             b.run_L.get());
+                                                             b.rcnt.get(), b.nrl_off.get(), b.nrl_ent.get(),
+                                                             b.run_sfx.get(), b.run_qn.get(), b.run_L.get());
         COLO_LAUNCH_CHECK();
         count_launch(2);
     }

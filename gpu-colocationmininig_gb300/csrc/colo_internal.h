@@ -15,7 +15,7 @@
 //               runs per feature on the host (h_frun_off prefix)
 //   NRL         per cell, the runs of its adjacent cells with a feature above
 //               the cell's lowest own feature, ordered by (feature, cell):
-//               nrl_off[M+1], nrl_run; per run the start of its
+//               nrl_off[M+1], nrl_ent (start, count); per run the start of its
 //               higher-feature suffix run_sfx and its size run_L
 //   neighbours  N+(a) = nb[nb_beg[a] .. nb_beg[a] + nb_cnt[a]) by point id
 #pragma once

@@ -50,12 +50,11 @@ __global__ void k_expand_active(uint64_t Rn, const uint32_t* __restrict__ rstart
 template <int T, int MODE>
 __global__ void __launch_bounds__(256) k_join(
     uint64_t A, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
-    const uint32_t* __restrict__ sid, const uint32_t* __restrict__ scell, const uint32_t* __restrict__ sfeat,
-    const float2* __restrict__ sxy, const uint32_t* __restrict__ rstart,
-    const uint32_t* __restrict__ rcnt, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_L,
-    const uint64_t* __restrict__ cap_off, const uint64_t* __restrict__ nrl_off,
-    const uint32_t* __restrict__ nrl_run, const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids,
-    uint64_t* __restrict__ nb_beg, uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb) {
+    const uint32_t* __restrict__ sid, const uint32_t* __restrict__ sfeat, const float2* __restrict__ sxy,
+    const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn,
+    const uint32_t* __restrict__ run_L, const uint64_t* __restrict__ cap_off, const uint2* __restrict__ nrl_ent,
+    const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids, uint64_t* __restrict__ nb_beg,
+    uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb) {
     const int lane = threadIdx.x & 31;
     const int gl = lane % T;
     const int gbase = lane - gl;
@@ -67,16 +66,16 @@ __global__ void __launch_bounds__(256) k_join(
     const uint32_t a = sid[p];
     const float2 pa = sxy[p];
     const float xa = pa.x, ya = pa.y;
-    const JobGrid& g = grids[fjob[sfeat[p]]];
+    const JobGrid& g = grids[fjob ? fjob[sfeat[p]] : 0u];   // fjob is null for one-job batches
     const float R2 = g.R2, hu = g.R2hu;
-    const uint64_t qend = nrl_off[scell[p] + 1];
+    const uint64_t q0 = run_sfx[r], qend = q0 + run_qn[r];
     uint64_t base = 0;
     if (MODE == J_SINGLE) base = cap_off[r] + (uint64_t)(p - rstart[r]) * run_L[r];
     if (MODE == J_FILL) base = nb_beg[a];
     uint32_t k = 0;
-    for (uint64_t q = run_sfx[r]; q < qend; ++q) {
-        const uint32_t tr = nrl_run[q];
-        const uint32_t ts = rstart[tr], tc = rcnt[tr];
+    for (uint64_t q = q0; q < qend; ++q) {
+        const uint2 te = nrl_ent[q];   // the target run's first sorted position and point count
+        const uint32_t ts = te.x, tc = te.y;
         if constexpr (T == 1) {
             // one lane per anchor: no group vote
             for (uint32_t t = 0; t < tc; ++t) {
@@ -114,10 +113,10 @@ void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uin
     unsigned grid = (unsigned)((threads + 255) / 256);
     KScope ks(mode == J_SINGLE ? "join" : mode == J_COUNT ? "join_count" : "join_fill");
 #define COLO_JOIN(MD)                                                                                        \
-    k_join<T, MD><<<grid, 256, 0, b.s>>>(A, act_pos, act_run, b.sid.get(), b.scell.get(), b.sfeat.get(),     \
-                                         b.sxy.get(), b.rstart.get(), b.rcnt.get(), b.run_sfx.get(),            \
-                                         b.run_L.get(), cap_off, b.nrl_off.get(), b.nrl_run.get(),          \
-                                         b.fjob.get(), b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get())
+    k_join<T, MD><<<grid, 256, 0, b.s>>>(A, act_pos, act_run, b.sid.get(), b.sfeat.get(), b.sxy.get(),       \
+                                         b.rstart.get(), b.run_sfx.get(), b.run_qn.get(), b.run_L.get(),        \
+                                         cap_off, b.nrl_ent.get(), b.J > 1 ? b.fjob.get() : nullptr,           \
+                                         b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get())
     if (mode == J_SINGLE) COLO_JOIN(J_SINGLE);
     else if (mode == J_COUNT) COLO_JOIN(J_COUNT);
     else COLO_JOIN(J_FILL);

@@ -304,6 +304,9 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cpu-frac", type=float, default=0.02)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--join-group", type=int, default=0,
+                    help="pin the join's lanes per anchor instead of autotuning (profiling runs: "
+                         "ncu serialises launches and distorts the autotuner's timings)")
     ap.add_argument("--forms", default="batched,e2e,plain",
                     help="comma list of batched (resident), e2e (host buffers), plain; the headline form "
                          "(batched+learned) always runs")
@@ -384,7 +387,11 @@ def main():
     head_mode = colo.MODE_LEARNED if model is not None else colo.MODE_BATCHED
     ctx.set_model(model)
     # pick the join's lanes per anchor for this dataset (untimed; kept by the context)
-    tuned = ctx.autotune(ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size))
+    if args.join_group:
+        ctx.set_join_group(args.join_group)
+        tuned = {"join_group": args.join_group, "join_ms": None}
+    else:
+        tuned = ctx.autotune(ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size))
     ms_b, res_b, clocks, tot_b = timed(head_mode, True)
     cands = res_b[0].num_candidates()
     value = tot_b / (ms_b / 1e3)

@@ -514,51 +514,61 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
             }
             uint64_t ncand = owner.size();
-            DevBuf<uint32_t> dub, dcand;
-            DevBuf<unsigned long long> dfs;
-            dub.alloc(ncand * k, s);
-            dub.zero(s);
-            dfs.alloc(ncand * 2, s);
-            dfs.zero(s);
-            dcand.alloc(ncand * k, s);
-            COLO_CUDA(cudaMemcpyAsync(dcand.get(), hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
-            filter_level(b, hc.data(), hjob.data(), ncand, k, dub.get(), dfs.get(), dcand.get());
-            const auto tl0 = Clock::now();
-            // cost-model features and predictions on the device, read back with the bounds
             bool rec_all = false;
             for (uint32_t j = 0; j < J; ++j) rec_all |= tr[j] && (pv[j].reserved[0] & 2) != 0;
             const bool infer = learned_mode && ncand > 0;
+            const bool want_x = (rec_all || infer) && ncand;
+            // the level's filter buffers from one allocation: bounds and cell
+            // statistics (zeroed, adjacent), candidates, cost-model inputs and outputs
+            size_t off = 0;
+            auto take = [&](uint64_t bytes) {
+                const size_t o = off;
+                off += (size_t)((bytes + 255) & ~(uint64_t)255);
+                return o;
+            };
+            const size_t o_ub = take(ncand * k * 4), o_fs = take(ncand * 2 * 8), zeroed = off;
+            const size_t o_cand = take(ncand * k * 4);
+            const size_t o_prow = want_x ? take(ncand * 8) : 0, o_x = want_x ? take(ncand * kMlpIn * 4) : 0;
+            const size_t o_par = infer ? take(kMlpParams * 4) : 0, o_y = infer ? take(ncand * 4) : 0;
+            DevBuf<unsigned char> fmem;
+            fmem.alloc(off ? off : 256, s);
+            unsigned char* fb = fmem.get();
+            uint32_t* d_ub = reinterpret_cast<uint32_t*>(fb + o_ub);
+            unsigned long long* d_fs = reinterpret_cast<unsigned long long*>(fb + o_fs);
+            uint32_t* d_cand = reinterpret_cast<uint32_t*>(fb + o_cand);
+            if (zeroed) COLO_CUDA(cudaMemsetAsync(fb, 0, zeroed, s));
+            COLO_CUDA(cudaMemcpyAsync(d_cand, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
+            filter_level(b, hc.data(), hjob.data(), ncand, k, d_ub, d_fs, d_cand);
+            const auto tl0 = Clock::now();
+            // cost-model features and predictions on the device, read back with the bounds
             std::vector<float> hX, hY;
-            DevBuf<float> dX, dY, dparams;
-            DevBuf<uint64_t> dprow;
-            if ((rec_all || infer) && ncand) {
+            if (want_x) {
+                uint64_t* d_prow = reinterpret_cast<uint64_t*>(fb + o_prow);
+                float* d_x = reinterpret_cast<float*>(fb + o_x);
                 std::vector<uint64_t> hprow(ncand, 0);
                 for (uint64_t q = 0; q < ncand; ++q) {
                     const JobState& st = js[owner[q].first];
                     hprow[q] = st.prev_tables[st.parent[owner[q].second]].rows;
                 }
-                dprow.alloc(ncand, s);
-                dX.alloc(ncand * kMlpIn, s);
-                COLO_CUDA(cudaMemcpyAsync(dprow.get(), hprow.data(), ncand * 8, cudaMemcpyHostToDevice, s));
-                mlp_features(ncand, k, dcand.get(), dub.get(), dfs.get(), b.fcount.get(), dprow.get(), dX.get(), s);
+                COLO_CUDA(cudaMemcpyAsync(d_prow, hprow.data(), ncand * 8, cudaMemcpyHostToDevice, s));
+                mlp_features(ncand, k, d_cand, d_ub, d_fs, b.fcount.get(), d_prow, d_x, s);
                 if (rec_all) {
                     hX.resize(ncand * kMlpIn);
-                    COLO_CUDA(cudaMemcpyAsync(hX.data(), dX.get(), hX.size() * 4, cudaMemcpyDeviceToHost, s));
+                    COLO_CUDA(cudaMemcpyAsync(hX.data(), d_x, hX.size() * 4, cudaMemcpyDeviceToHost, s));
                 }
                 if (infer) {
-                    dparams.alloc(kMlpParams, s);
-                    dY.alloc(ncand, s);
+                    float* d_par = reinterpret_cast<float*>(fb + o_par);
+                    float* d_y = reinterpret_cast<float*>(fb + o_y);
                     hY.resize(ncand);
-                    COLO_CUDA(cudaMemcpyAsync(dparams.get(), ctx->model.data(), kMlpParams * 4,
-                                              cudaMemcpyHostToDevice, s));
-                    mlp_forward(dparams.get(), dX.get(), ncand, dY.get(), s);
-                    COLO_CUDA(cudaMemcpyAsync(hY.data(), dY.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
+                    COLO_CUDA(cudaMemcpyAsync(d_par, ctx->model.data(), kMlpParams * 4, cudaMemcpyHostToDevice, s));
+                    mlp_forward(d_par, d_x, ncand, d_y, s);
+                    COLO_CUDA(cudaMemcpyAsync(hY.data(), d_y, ncand * 4, cudaMemcpyDeviceToHost, s));
                 }
             }
             std::vector<uint32_t> hub(ncand * k);
             std::vector<uint64_t> hfs(ncand * 2);
-            COLO_CUDA(cudaMemcpyAsync(hub.data(), dub.get(), hub.size() * 4, cudaMemcpyDeviceToHost, s));
-            COLO_CUDA(cudaMemcpyAsync(hfs.data(), dfs.get(), hfs.size() * 8, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(hub.data(), d_ub, hub.size() * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(hfs.data(), d_fs, hfs.size() * 8, cudaMemcpyDeviceToHost, s));
             COLO_CUDA(cudaStreamSynchronize(s));
             us_level_wait += (uint64_t)(ms_since(tl0) * 1000.0);
             for (uint32_t j = 0; j < J; ++j) {

@@ -90,6 +90,8 @@ struct colo_ctx {
     int refs = 1;          // the owner plus one per live dataset (freed at zero)
     std::vector<float> model;   // cost-model parameters for LEARNED mines (empty: none)
     int join_group = 0;         // lanes per anchor in the join (0: default; set by colo_autotune)
+    void* stage = nullptr;      // page-locked staging for the level loop's readbacks
+    size_t stage_bytes = 0;
 };
 
 struct colo_dataset {

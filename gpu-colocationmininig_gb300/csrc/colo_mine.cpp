@@ -105,6 +105,7 @@ void ctx_release(colo_ctx* ctx) {
         cudaStreamSynchronize(ctx->s);
         cudaStreamDestroy(ctx->s);
     }
+    if (ctx->stage) cudaFreeHost(ctx->stage);
     delete ctx;
 }
 
@@ -233,6 +234,48 @@ bool filter_pass(const uint64_t* ub, const uint32_t* mem, uint32_t k, const std:
     }
     return pi0 >= thr;
 }
+
+// Readbacks staged in page-locked memory: a device-to-host copy into pageable
+// memory blocks the host until the stream reaches it, one into the context's
+// pinned buffer is only queued, so one wait covers all of a phase's copies and
+// finish() then moves the bytes to their destinations.  The buffer grows only
+// here, after the stream has drained.
+struct Readback {
+    colo_ctx* ctx;
+    cudaStream_t s;
+    struct Item {
+        void* dst;
+        size_t off, bytes;
+    };
+    std::vector<Item> items;
+    size_t off = 0;
+    Readback(colo_ctx* c, cudaStream_t st, size_t need) : ctx(c), s(st) {
+        need += 64 * 16;   // 16-byte alignment of each copy
+        if (need > ctx->stage_bytes) {
+            COLO_CUDA(cudaStreamSynchronize(s));
+            if (ctx->stage) cudaFreeHost(ctx->stage);
+            ctx->stage = nullptr;
+            ctx->stage_bytes = 0;
+            const size_t nb = std::max<size_t>(need, (size_t)1 << 20);
+            COLO_CUDA(cudaHostAlloc(&ctx->stage, nb, cudaHostAllocDefault));
+            ctx->stage_bytes = nb;
+        }
+    }
+    void copy(void* dst, const void* src, size_t bytes) {
+        if (!bytes) return;
+        off = (off + 15) & ~(size_t)15;
+        if (off + bytes > ctx->stage_bytes) throw StatusError{COLO_ERR_INTERNAL, "readback staging too small"};
+        COLO_CUDA(cudaMemcpyAsync(static_cast<char*>(ctx->stage) + off, src, bytes, cudaMemcpyDeviceToHost, s));
+        items.push_back({dst, off, bytes});
+        off += bytes;
+    }
+    void finish() {
+        COLO_CUDA(cudaStreamSynchronize(s));
+        for (const Item& it : items) std::memcpy(it.dst, static_cast<char*>(ctx->stage) + it.off, it.bytes);
+        items.clear();
+        off = 0;
+    }
+};
 
 // A typed view into the level arena's one allocation.
 template <class T>
@@ -541,6 +584,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             filter_level(b, hc.data(), hjob.data(), ncand, k, d_ub, d_fs, d_cand);
             const auto tl0 = Clock::now();
             // cost-model features and predictions on the device, read back with the bounds
+            Readback rb(ctx, s, (rec_all ? ncand * kMlpIn * 4 : 0) + (infer ? ncand * 4 : 0) + ncand * k * 4 +
+                                    ncand * 2 * 8);
             std::vector<float> hX, hY;
             if (want_x) {
                 uint64_t* d_prow = reinterpret_cast<uint64_t*>(fb + o_prow);
@@ -554,7 +599,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 mlp_features(ncand, k, d_cand, d_ub, d_fs, b.fcount.get(), d_prow, d_x, s);
                 if (rec_all) {
                     hX.resize(ncand * kMlpIn);
-                    COLO_CUDA(cudaMemcpyAsync(hX.data(), d_x, hX.size() * 4, cudaMemcpyDeviceToHost, s));
+                    rb.copy(hX.data(), d_x, hX.size() * 4);
                 }
                 if (infer) {
                     float* d_par = reinterpret_cast<float*>(fb + o_par);
@@ -562,14 +607,14 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     hY.resize(ncand);
                     COLO_CUDA(cudaMemcpyAsync(d_par, ctx->model.data(), kMlpParams * 4, cudaMemcpyHostToDevice, s));
                     mlp_forward(d_par, d_x, ncand, d_y, s);
-                    COLO_CUDA(cudaMemcpyAsync(hY.data(), d_y, ncand * 4, cudaMemcpyDeviceToHost, s));
+                    rb.copy(hY.data(), d_y, ncand * 4);
                 }
             }
             std::vector<uint32_t> hub(ncand * k);
             std::vector<uint64_t> hfs(ncand * 2);
-            COLO_CUDA(cudaMemcpyAsync(hub.data(), d_ub, hub.size() * 4, cudaMemcpyDeviceToHost, s));
-            COLO_CUDA(cudaMemcpyAsync(hfs.data(), d_fs, hfs.size() * 8, cudaMemcpyDeviceToHost, s));
-            COLO_CUDA(cudaStreamSynchronize(s));
+            rb.copy(hub.data(), d_ub, hub.size() * 4);
+            rb.copy(hfs.data(), d_fs, hfs.size() * 8);
+            rb.finish();
             us_level_wait += (uint64_t)(ms_since(tl0) * 1000.0);
             for (uint32_t j = 0; j < J; ++j) {
                 if (!tr[j]) continue;
@@ -747,6 +792,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
         }
         std::vector<uint64_t> hstats(ncand * k * 4);
+        Readback rb(ctx, s, hstats.size() * 8 + ncand * 8 + ncand * 4 + 8);
         d_items.zero(s);
         cnt_refined += ncand;
         cnt_bmw += nwords;
@@ -777,17 +823,17 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 if (learned) level_single(b, w, k, ar.overflow.get());
                 else level_count(b, w, k);
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
-                COLO_CUDA(cudaMemcpyAsync(hstats.data(), ar.stats.get(), hstats.size() * 8, cudaMemcpyDeviceToHost, s));
+                rb.copy(hstats.data(), ar.stats.get(), hstats.size() * 8);
             }
         }
         // row counts, overflow flags and the work counter, with the statistics: one wait
         std::vector<uint64_t> hrows(ncand);
         std::vector<uint32_t> hovf(ncand, 0);
         unsigned long long h_items = 0;
-        if (ncand) COLO_CUDA(cudaMemcpyAsync(hrows.data(), ar.rows.get(), ncand * 8, cudaMemcpyDeviceToHost, s));
-        if (learned) COLO_CUDA(cudaMemcpyAsync(hovf.data(), ar.overflow.get(), ncand * 4, cudaMemcpyDeviceToHost, s));
-        COLO_CUDA(cudaMemcpyAsync(&h_items, d_items.get(), 8, cudaMemcpyDeviceToHost, s));
-        COLO_CUDA(cudaStreamSynchronize(s));
+        if (ncand) rb.copy(hrows.data(), ar.rows.get(), ncand * 8);
+        if (learned) rb.copy(hovf.data(), ar.overflow.get(), ncand * 4);
+        rb.copy(&h_items, d_items.get(), 8);
+        rb.finish();
         // participation index (getParticipationIndex, Codes/DeviceProcess.cu:108-132)
         std::vector<uint8_t> prev_flag(ncand, 0);
         for (uint64_t q = 0; q < ncand; ++q) {

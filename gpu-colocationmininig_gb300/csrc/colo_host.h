@@ -101,7 +101,9 @@ struct colo_dataset {
     std::vector<uint32_t> fstart, fcount;
     colo::DevBuf<float> dx, dy;
     bool resident = false;
-    bool pinned = false;                     // host arrays page-locked for uploads
+    bool pinned = false;                     // page-locking of the host arrays was attempted
+    const float* mx = nullptr;               // device addresses of the page-locked, mapped host
+    const float* my = nullptr;               //   arrays (null when locking or mapping failed)
 };
 
 struct colo_result {

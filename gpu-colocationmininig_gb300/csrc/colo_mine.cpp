@@ -124,16 +124,30 @@ colo_status run_guarded(colo_ctx* ctx, const std::function<colo_status()>& fn) {
     }
 }
 
+// Page-locks the host coordinate arrays once (uploads are then direct DMA)
+// and maps them, so that kernels can also read them over the host link.
+void pin_dataset(colo_dataset* ds) {
+    const uint64_t n = ds->hp.x.size();
+    if (ds->pinned || !n) return;
+    ds->pinned = true;
+    bool ok = cudaHostRegister(ds->hp.x.data(), n * 4, cudaHostRegisterMapped) == cudaSuccess;
+    ok = ok && cudaHostRegister(ds->hp.y.data(), n * 4, cudaHostRegisterMapped) == cudaSuccess;
+    void* px = nullptr;
+    void* py = nullptr;
+    ok = ok && cudaHostGetDevicePointer(&px, ds->hp.x.data(), 0) == cudaSuccess;
+    ok = ok && cudaHostGetDevicePointer(&py, ds->hp.y.data(), 0) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        return;
+    }
+    ds->mx = static_cast<const float*>(px);
+    ds->my = static_cast<const float*>(py);
+}
+
 uint64_t upload_dataset(colo_dataset* ds, cudaStream_t s) {
     if (ds->resident) return 0;
     uint64_t n = ds->hp.x.size();
-    if (!ds->pinned && n) {
-        // page-lock the host arrays once so every upload is a direct DMA
-        bool ok = cudaHostRegister(ds->hp.x.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
-        ok = ok && cudaHostRegister(ds->hp.y.data(), n * 4, cudaHostRegisterDefault) == cudaSuccess;
-        if (!ok) cudaGetLastError();
-        ds->pinned = true;
-    }
+    pin_dataset(ds);
     // coordinates only: a point's feature follows from the feature start table
     // (points are grouped by feature), so no per-point feature array is copied
     ds->dx.alloc(n, s);
@@ -359,9 +373,20 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     b.N = N;
     b.F = job_f0[J];
     if (J == 1) {
-        b.h2d_points = upload_dataset(dsv[0], s);
-        b.x = dsv[0]->dx.get();
-        b.y = dsv[0]->dy.get();
+        colo_dataset* ds = dsv[0];
+        if (!ds->resident) pin_dataset(ds);
+        if (!ds->resident && ds->mx && ds->my) {
+            // streamed: the cell-key pass reads the page-locked host arrays over
+            // the host link (the only pass that reads them: it writes the packed
+            // device copy every later pass uses), so no separate upload runs
+            b.x = ds->mx;
+            b.y = ds->my;
+            b.h2d_points = 8 * N;
+        } else {
+            b.h2d_points = upload_dataset(ds, s);
+            b.x = ds->dx.get();
+            b.y = ds->dy.get();
+        }
     } else {
         ownf.resize(2);
         ownf[0].alloc(N, s);

@@ -120,10 +120,13 @@ colo_status colo_dataset_from_binary(colo_ctx* ctx, const char* path, colo_datas
  * (err_cap bytes, NUL-terminated; may be NULL). */
 colo_status colo_csv_to_binary(const char* csv_path, const char* bin_path, uint32_t threads, char* err,
                                size_t err_cap);
-/* Copy the points to the device now (initializeDeviceMemory,
- * colocationFinder.cpp:443-464); otherwise colo_mine copies them. */
+/* Copy the points to the device now and keep them there for later mines
+ * (initializeDeviceMemory, colocationFinder.cpp:443-464).  Otherwise a mine of
+ * one dataset page-locks and maps the host arrays and its cell-key pass reads
+ * them over the host link (no device copy is kept); a batch of several
+ * datasets copies them. */
 colo_status colo_dataset_upload(colo_dataset* ds);
-/* Drop the device copy (the next mine copies again). */
+/* Drop the device copy (the next mine reads the host arrays again). */
 colo_status colo_dataset_evict(colo_dataset* ds);
 uint64_t colo_dataset_num_points(const colo_dataset* ds);
 uint32_t colo_dataset_num_features(const colo_dataset* ds);

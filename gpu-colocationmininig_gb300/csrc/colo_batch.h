@@ -39,7 +39,8 @@ struct Batch {
     DevBuf<DevFlags> flags;
     // bucketed (sorted by cell key, then id)
     DevBuf<float2> xy;           // coordinates by id, packed (built by the cell-key pass)
-    DevBuf<uint32_t> sid, sfeat, scell;
+    DevBuf<uint32_t> sid, sfeat, scell;   // scell (cell of each sorted point) only when keep_scell
+    bool keep_scell = false;              // colo_stage_cells reports each point's cell
     DevBuf<float2> sxy;          // coordinates in cell-sorted order
     // cells
     DevBuf<uint64_t> ckey;

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kHeadThreads) k_head_compact(
         const uint32_t c = cb + __popc(chb[r] & lt) + (ch ? 1u : 0u) - 1u;   // the cell of p
         const uint32_t ri = rb + __popc(rhb[r] & lt);
         if (p < n) {
-            scell[p] = c;
+            if (scell) scell[p] = c;
             if (ch) {
                 ckey[c] = keys[p];
                 cstart[c] = (uint32_t)p;
@@ -751,12 +751,12 @@ void sort_and_compact(Batch& b) {
     b.rstart.alloc(Rn, s);
     b.rcnt.alloc(Rn, s);
     b.rcell.alloc(Rn, s);
-    b.scell.alloc(n, s);
+    if (b.keep_scell) b.scell.alloc(n, s);
     {
         KScope ks("cell_compact");
         k_head_compact<KT><<<(unsigned)tiles, kHeadThreads, 0, s>>>(
             n, keys.get(), b.sfeat.get(), b.fjob.get(), part.get(), b.ckey.get(), b.cstart.get(), b.crun.get(),
-            b.cjob.get(), b.rfeat.get(), b.rstart.get(), b.rcell.get(), b.scell.get());
+            b.cjob.get(), b.rfeat.get(), b.rstart.get(), b.rcell.get(), b.keep_scell ? b.scell.get() : nullptr);
         COLO_LAUNCH_CHECK();
         count_launch();
     }

@@ -34,6 +34,7 @@ colo_status colo_stage_cells(colo_ctx* ctx, colo_dataset* ds, float R, uint64_t*
         std::vector<DevBuf<float>> of;
         colo_dataset* dsv[1] = {ds};
         setup_batch(ctx, dsv, &p, 1, b, of, nullptr);
+        b.keep_scell = cell_of != nullptr;
         if (b.N) bucket_points(b);
         cudaStream_t s = ctx->s;
         uint64_t cap = *nruns;

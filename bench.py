@@ -8,8 +8,9 @@ over that dataset.
 
   value   candidates/s of the headline form (batched; learned when enabled)
           with the points resident in HBM when the timed region starts
-  e2e     the same through the C ABI from host buffers: every step copies the
-          points host->device and the per-level results device->host
+  e2e     the same through the C ABI from host buffers: every step moves the
+          points host->device (the cell-key pass reads the page-locked host
+          arrays over the host link) and the per-level results device->host
   plain   the project's plain two-pass form (per-candidate launches) on the
           same resident data, for the batched-vs-plain ratio
 

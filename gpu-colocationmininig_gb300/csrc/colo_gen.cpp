@@ -49,6 +49,42 @@ struct Rng {
     }
 };
 
+// Logarithm and exponential from IEEE-754 basic operations only (this file is
+// compiled with -ffp-contract=off), so the generated points are the same bits
+// on every platform; libm's log/exp/pow may differ in the last place between
+// architectures.  log: x = m * 2^e with m in [sqrt(1/2), sqrt(2)), then
+// log m = 2 atanh(t), t = (m - 1) / (m + 1), by its odd power series
+// (|t| <= 0.172, 24 terms).  exp: x = k ln2 + r with |r| <= ln2 / 2, then
+// the Taylor series of e^r (28 terms) scaled by 2^k.
+constexpr double kLn2 = 0.69314718055994530942;
+
+double det_log(double x) {
+    int e = 0;
+    double m = std::frexp(x, &e);
+    if (m < 0.70710678118654752440) {
+        m *= 2.0;
+        e -= 1;
+    }
+    const double t = (m - 1.0) / (m + 1.0), t2 = t * t;
+    double s = 0.0, p = t;
+    for (int i = 0; i < 24; ++i) {
+        s += p / (double)(2 * i + 1);
+        p *= t2;
+    }
+    return 2.0 * s + (double)e * kLn2;
+}
+
+double det_exp(double x) {
+    const double k = std::floor(x / kLn2 + 0.5);
+    const double r = x - k * kLn2;
+    double s = 1.0, term = 1.0;
+    for (int i = 1; i < 28; ++i) {
+        term *= r / (double)i;
+        s += term;
+    }
+    return std::ldexp(s, (int)k);
+}
+
 }  // namespace
 
 extern "C" {
@@ -89,7 +125,7 @@ int colo_gen_points(const colo_gen_spec* sp, float* x, float* y, int32_t* fid, f
     } else {
         std::vector<double> w(F);
         double H = 0;
-        for (uint32_t f = 0; f < F; ++f) H += (w[f] = std::pow((double)(f + 1), -sp->zipf_s));
+        for (uint32_t f = 0; f < F; ++f) H += (w[f] = det_exp(-sp->zipf_s * det_log((double)(f + 1))));
         uint64_t tot = 0;
         for (uint32_t f = 0; f < F; ++f) {
             cnt[f] = std::max<uint64_t>(1, (uint64_t)std::floor((double)N * w[f] / H));
@@ -145,8 +181,8 @@ int colo_gen_points(const colo_gen_spec* sp, float* x, float* y, int32_t* fid, f
     const double W = sp->width;
     for (uint32_t h = 0; h < sp->nhot; ++h) {
         uint32_t f = pick_feature();
-        double lo = std::log(sp->hot_sig_lo), hi = std::log(sp->hot_sig_hi);
-        hot[f].push_back({rng.u01() * W, rng.u01() * W, std::exp(lo + rng.u01() * (hi - lo))});
+        double lo = det_log(sp->hot_sig_lo), hi = det_log(sp->hot_sig_hi);
+        hot[f].push_back({rng.u01() * W, rng.u01() * W, det_exp(lo + rng.u01() * (hi - lo))});
     }
     for (uint32_t h = 0; h < sp->ndense; ++h) dense.push_back({rng.u01() * W, rng.u01() * W, sp->dense_sigma});
     auto clampw = [&](double v) {

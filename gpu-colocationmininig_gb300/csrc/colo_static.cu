@@ -53,7 +53,8 @@ __global__ void k_static_clear(uint32_t* __restrict__ w, uint64_t nwords) {
 }
 
 // One entry of the row-major table per thread step: set the member's bit.
-// Ids outside the member's instance range are counted, not written.
+// An id outside the member's instance range is not written; it raises the
+// invalid flag (a flag, not a count, so no number of bad ids can wrap it).
 __global__ void k_static_mark(const uint32_t* __restrict__ table, uint64_t entries, Members m,
                               uint32_t* __restrict__ scratch) {
     uint32_t* bits = scratch + kCtrlWords;
@@ -68,7 +69,7 @@ __global__ void k_static_mark(const uint32_t* __restrict__ table, uint64_t entri
         }
         atomicOr(&bits[m.bm_off[j] + (local >> 5)], 1u << (local & 31));
     }
-    if (bad) atomicAdd(&scratch[0], bad);
+    if (bad) atomicOr(&scratch[0], 1u);
 }
 
 // Block j counts member j's bitmap: A = bits in [0, n-2], last = bit n-1,
@@ -134,7 +135,9 @@ uint32_t* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device, looked up once
 // per device (cudaGetSymbolAddress; the symbol's host-side name is only a
-// handle, never a device address).
+// handle, never a device address).  The address is cached for the life of
+// the process: a cudaDeviceReset of that device after its first call would
+// leave it dangling, which is why the header rules out calls after a reset.
 colo_status scratch_for_current_device(uint32_t** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return COLO_ERR_NO_DEVICE;

@@ -303,7 +303,9 @@ colo_status colo_result_features(const colo_result* r, uint32_t li, float* x);
  * words), held by every GPU where the library is loaded until exit.
  * COLO_ERR_CAPACITY when the sum over members of ceil(fcount/32) exceeds it.
  * The first call on a device looks up the array's device address (once per
- * device); make that first call before any stream capture.  All calls share
+ * device) and caches it; make that first call before any stream capture.  A
+ * cudaDeviceReset of a device after its first call is not supported: the
+ * cached address would no longer be valid.  All calls share
  * the array and each clears what it uses: calls that overlap on the GPU race
  * and give wrong results. */
 #define COLO_TABLE_PI_STATIC_WORDS (1u << 20)

@@ -1,7 +1,8 @@
 """Build the reference's own sources for the CPU (golden-vector harness).
 
 TEST INFRASTRUCTURE.  Compiles, from where they lie under the reference tree
-(default /root/reference/Codes), colocationFinder.cpp and DeviceProcess.cu
+(the project's Codes/ directory, given as an argument or as
+$COLO_REFERENCE_ROOT/Codes), colocationFinder.cpp and DeviceProcess.cu
 with g++ against the project-written stand-ins in shim/ (CUDA runtime and
 kernel execution model, the Thrust calls used, Boost's tokenizer) and links
 them with ref_harness.cpp into oracle/_ref/ref_harness.
@@ -84,8 +85,18 @@ def transform(cu: str, barrier_kernels) -> str:
     return out
 
 
-def build(ref_codes: str = "/root/reference/Codes") -> Path:
-    codes = Path(ref_codes)
+def reference_codes(arg: str = None) -> Path:
+    """The reference's Codes/ directory: the argument, else $COLO_REFERENCE_ROOT/Codes; None when neither is set."""
+    if arg:
+        return Path(arg)
+    root = os.environ.get("COLO_REFERENCE_ROOT")
+    return Path(root) / "Codes" if root else None
+
+
+def build(ref_codes: str = None) -> Path:
+    codes = reference_codes(ref_codes)
+    if codes is None:
+        raise FileNotFoundError("no reference tree: pass its Codes/ directory or set COLO_REFERENCE_ROOT")
     if not (codes / "DeviceProcess.cu").exists():
         raise FileNotFoundError(f"reference sources not found under {codes}")
     OUT.mkdir(exist_ok=True)
@@ -115,4 +126,4 @@ def build(ref_codes: str = "/root/reference/Codes") -> Path:
 
 
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/Codes"))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -1,7 +1,8 @@
 """Generate the golden vectors in tests/golden/ from the reference itself.
 
-Run here (where the reference tree is mounted):
-    python tests/golden/make_golden.py [/path/to/reference/Codes]
+Run where the reference tree is available:
+    python tests/golden/make_golden.py /path/to/reference/Codes
+or with COLO_REFERENCE_ROOT set to the reference project's root.
 
 Each case is a small seeded point set written in the reference's CSV format
 (<name>.csv) with its parameter file; oracle/ref_emu/build_ref.py compiles
@@ -154,4 +155,4 @@ def main(codes: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/Codes")
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -95,6 +95,50 @@ def test_static_entry_matches_mining_numerators(cfg, scale):
 
 
 @pytest.mark.gpu
+def test_static_entry_takes_no_device_memory():
+    """The device's free memory does not drop across calls of the entry point.
+
+    Everything the calls touch is in place first: the torch buffers, and the
+    library's module with its scratch array (loaded by a warm-up call).  A
+    cudaMalloc on the call path would show as less free memory afterwards;
+    other tests' contexts freed meanwhile can only raise it.
+    """
+    import gc
+
+    torch = pytest.importorskip("torch")
+    ctx = colo.Context(0)
+    cases, starts, counts = _mined(ctx, gen.config(0))
+    call = _Caller(torch)
+    dev_tables = [(torch.from_numpy(np.ascontiguousarray(t, np.uint32).view(np.int32)).cuda(), t.shape[0],
+                   np.ascontiguousarray(starts[c], np.uint32), np.ascontiguousarray(counts[c], np.uint32), num)
+                  for t, c, num, _ in cases]
+    lib = call.lib
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def run_all():
+        for t, rows, fs, fc, _ in dev_tables:
+            st = lib.colo_table_pi_static(t.data_ptr(), rows, len(fs), fs.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                          fc.ctypes.data_as(C.POINTER(C.c_uint32)), call.num.data_ptr(),
+                                          call.pi.data_ptr(), stream)
+            assert st == 0, colo.STATUS.get(st, st)
+        torch.cuda.synchronize()
+
+    run_all()                      # warm-up: module load, scratch address lookup
+    gc.collect()
+    gc.disable()
+    try:
+        free0, _ = torch.cuda.mem_get_info()
+        for _ in range(3):
+            run_all()
+        free1, _ = torch.cuda.mem_get_info()
+    finally:
+        gc.enable()
+    assert free1 >= free0, (free0, free1)
+    t, rows, fs, fc, num = dev_tables[-1]
+    assert np.array_equal(call.num[:len(fs)].cpu().numpy().view(np.uint64), num)
+
+
+@pytest.mark.gpu
 def test_static_entry_flags_ids_outside_members():
     torch = pytest.importorskip("torch")
     call = _Caller(torch)

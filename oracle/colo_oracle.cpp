@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -24,8 +25,12 @@
 #include <fstream>
 #include <limits>
 #include <string>
+#include <unordered_map>
 #include <unordered_set>
 #include <vector>
+#ifdef _OPENMP
+#include <parallel/algorithm>
+#endif
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -699,6 +704,7 @@ struct oracle_result {
     int status = 0;
     uint64_t unresolved = 0;    /* ambiguous comparisons without a device outcome */
     std::vector<OLevel> levels;
+    double phase_ms[6] = {0, 0, 0, 0, 0, 0};   /* oracle_mine_fast: bucketing, join, filter, refine, fill, Apriori */
 };
 
 extern "C" {
@@ -847,6 +853,7 @@ int oracle_mine(const float* x, const float* y, const uint32_t* feat, uint64_t n
 }
 
 void oracle_free(oracle_result* r) { delete r; }
+void oracle_phase_ms(const oracle_result* r, double* ms6) { std::memcpy(ms6, r->phase_ms, sizeof(r->phase_ms)); }
 int oracle_status(const oracle_result* r) { return r->status; }
 uint64_t oracle_unresolved(const oracle_result* r) { return r->unresolved; }
 uint32_t oracle_num_levels(const oracle_result* r) { return (uint32_t)r->levels.size(); }
@@ -933,35 +940,83 @@ int oracle_sq_decide(float x1, float y1, float x2, float y2, float R2, int* ambi
 /* Every pair of points of different features whose comparison with R^2 an
  * exact tie could flip.  Candidate pairs come from a uniform grid of cell
  * size R over the true coordinates (a 5x5 stencil covers every pair at
- * distance <= 2R), so the set does not depend on the reference grid. */
+ * distance <= 2R), so the set does not depend on the reference grid.  Each
+ * unordered pair of grid cells is visited once, in parallel; within a pair
+ * of cells only points of different features are compared, and only sums
+ * within 2^-20 of R^2 go through the exact test. */
 uint64_t oracle_ambiguous_pairs(const float* x, const float* y, const uint32_t* feat, uint64_t n,
                                 float R, uint64_t* keys, uint64_t cap) {
-    float R2 = R * R;
-    double w = (double)R;
-    std::vector<std::pair<uint64_t, uint32_t>> cells(n);
-    auto key_of = [&](int64_t cx, int64_t cy) {
-        return ((uint64_t)(cx + (1ll << 31)) << 32) ^ (uint64_t)(cy + (1ll << 31));
+    const float R2 = R * R;
+    const double w = (double)R, R2d = (double)R2, win = std::ldexp(R2d, -20);
+    struct P {
+        int64_t cy, cx;
+        uint32_t f, id;
     };
-    std::vector<int64_t> cx(n), cy(n);
-    for (uint64_t i = 0; i < n; ++i) {
-        cx[i] = (int64_t)std::floor((double)x[i] / w);
-        cy[i] = (int64_t)std::floor((double)y[i] / w);
-        cells[i] = {key_of(cx[i], cy[i]), (uint32_t)i};
-    }
-    std::sort(cells.begin(), cells.end());
-    std::vector<uint64_t> found;
-    for (uint64_t i = 0; i < n; ++i) {
-        for (int dy = -2; dy <= 2; ++dy)
-            for (int dx = -2; dx <= 2; ++dx) {
-                uint64_t k = key_of(cx[i] + dx, cy[i] + dy);
-                auto it = std::lower_bound(cells.begin(), cells.end(), std::make_pair(k, 0u));
-                for (; it != cells.end() && it->first == k; ++it) {
-                    uint32_t j = it->second;
-                    if (j <= i || feat[j] == feat[i]) continue;
-                    SqDecision dc = sq_decide(x[i], y[i], x[j], y[j], R2);
-                    if (dc.ambiguous) found.push_back(((uint64_t)i << 32) | j);
-                }
+    std::vector<P> pts(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i)
+        pts[i] = {(int64_t)std::floor((double)y[i] / w), (int64_t)std::floor((double)x[i] / w), feat[i], (uint32_t)i};
+    auto less = [](const P& a, const P& b) {
+        if (a.cy != b.cy) return a.cy < b.cy;
+        if (a.cx != b.cx) return a.cx < b.cx;
+        if (a.f != b.f) return a.f < b.f;
+        return a.id < b.id;
+    };
+#ifdef _OPENMP
+    __gnu_parallel::sort(pts.begin(), pts.end(), less);
+#else
+    std::sort(pts.begin(), pts.end(), less);
+#endif
+    std::vector<uint64_t> cb;            /* first point of each grid cell */
+    std::vector<uint64_t> rb;            /* first cell of each grid row */
+    for (uint64_t p = 0; p < n; ++p)
+        if (p == 0 || pts[p].cx != pts[p - 1].cx || pts[p].cy != pts[p - 1].cy) {
+            if (cb.empty() || pts[p].cy != pts[cb.back()].cy) rb.push_back(cb.size());
+            cb.push_back(p);
+        }
+    const uint64_t NC = cb.size(), NR = rb.size();
+    cb.push_back(n);
+    rb.push_back(NC);
+    std::vector<uint64_t> crow(NC);
+    for (uint64_t r = 0; r < NR; ++r)
+        for (uint64_t c = rb[r]; c < rb[r + 1]; ++c) crow[c] = r;
+    auto pair_cells = [&](uint64_t A, uint64_t B, std::vector<uint64_t>& out) {
+        for (uint64_t i = cb[A]; i < cb[A + 1]; ++i) {
+            const P& a = pts[i];
+            for (uint64_t j = (A == B ? i + 1 : cb[B]); j < cb[B + 1]; ++j) {
+                const P& b = pts[j];
+                if (a.f == b.f) continue;
+                const float dx = x[b.id] - x[a.id], dy = y[b.id] - y[a.id];
+                const double S = (double)dx * (double)dx + (double)dy * (double)dy;
+                if (std::fabs(S - R2d) > win) continue;
+                if (!sq_decide(x[a.id], y[a.id], x[b.id], y[b.id], R2).ambiguous) continue;
+                const uint32_t lo = a.id < b.id ? a.id : b.id, hi = a.id < b.id ? b.id : a.id;
+                out.push_back(((uint64_t)lo << 32) | hi);
             }
+        }
+    };
+    std::vector<uint64_t> found;
+#pragma omp parallel
+    {
+        std::vector<uint64_t> loc;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t A = 0; A < (int64_t)NC; ++A) {
+            const int64_t ay = pts[cb[A]].cy, ax = pts[cb[A]].cx;
+            for (uint64_t r = crow[A]; r < NR && r <= crow[A] + 2; ++r) {
+                const int64_t ry = pts[cb[rb[r]]].cy;
+                if (ry > ay + 2) break;
+                const int64_t x0 = ry == ay ? ax : ax - 2;   /* same row: this cell and the ones after it */
+                uint64_t lo = rb[r], hi = rb[r + 1];
+                while (lo < hi) {                          /* first cell of the row with cx >= x0 */
+                    const uint64_t mid = (lo + hi) / 2;
+                    if (pts[cb[mid]].cx < x0) lo = mid + 1;
+                    else hi = mid;
+                }
+                for (uint64_t B = lo; B < rb[r + 1] && pts[cb[B]].cx <= ax + 2; ++B) pair_cells((uint64_t)A, B, loc);
+            }
+        }
+#pragma omp critical
+        found.insert(found.end(), loc.begin(), loc.end());
     }
     std::sort(found.begin(), found.end());
     if (keys) std::memcpy(keys, found.data(), std::min<uint64_t>(found.size(), cap) * 8);
@@ -1198,6 +1253,759 @@ void oracle_mlp_grad(const float* P, const float* X, const float* T, uint64_t n,
             for (int o = 0; o < MH; ++o) G[M_W1 + i * MH + o] += r.xb[i] * dz1b[o];
     }
     if (loss) *loss = L;
+}
+
+}  // extern "C"
+
+/* ======================================================================== */
+/* Scaled mining: oracle_mine_fast                                          */
+/*                                                                          */
+/* The same results as oracle_mine -- every level's candidates, filter      */
+/* bounds and verdicts, row counts, participation numerators, PI bits and   */
+/* instance tables in the reference's row order -- organised so that        */
+/* 10^7-10^8 points finish in seconds on a multicore host.  It is the timed */
+/* CPU baseline at full workload sizes and the source of the full-size      */
+/* parity fixtures; tests/test_cpu_oracle.py checks it against oracle_mine  */
+/* (the literal restatement) and against the reference's golden vectors.    */
+/*                                                                          */
+/* What changes is the order of work, not the rules:                        */
+/*  - bucketing sorts (cell, id) pairs in parallel and keeps occupied cells  */
+/*    only, with each cell's reference-neighbour cells (the visit order of   */
+/*    DeviceProcess_Kernel.h:24-32) and its geometric 3x3 cells precomputed; */
+/*  - the neighbour relation N+(a) = {b : feat(b) > feat(a), refadj(a->b),  */
+/*    sq(a,b) <= R^2} is evaluated once, each list ordered by (feature,     */
+/*    visit order, id): the slice of one feature is exactly the sequence    */
+/*    degree2TableSlotCounter_Kernel (Kernel.h:12-55) and the level-k       */
+/*    kernels (Kernel.h:255-385) walk for an anchor;                        */
+/*  - the quad filter (Kernel.h:469-509) tests 2x2 quads with per-cell      */
+/*    feature bitsets; pairs are bounded cell by cell (a cell Z is in U_c   */
+/*    when one of its quads holds both members; the member in Z is in all   */
+/*    of them), larger candidates from the quads of their rarest member's   */
+/*    cells, each cell of U_c counted once;                                 */
+/*  - participation numerators are counted from per-member bitsets with the  */
+/*    window rule of getParticipationIndex (DeviceProcess.cu:108-132):       */
+/*    k = 2: num0 = |P0 & [0, L0-1]|, num1 = |P1 \ {0}| + [0 in P1 or L0 in  */
+/*    P0]; k >= 3: num0 = |P0 & [0, L0-1]|, num_j = [L_{j-1} in P_{j-1}] +   */
+/*    |P_j & [0, L_j-1]| (L_j = n_j - 1);                                   */
+/*  - Apriori checks subsets in a hash set instead of a linear scan          */
+/*    (colocationFinder.cpp:618-634), with the same breaks.                 */
+/* ======================================================================== */
+
+namespace {
+
+struct FastData {
+    uint64_t n = 0;
+    uint32_t F = 0;
+    const float* x = nullptr;
+    const float* y = nullptr;
+    const uint32_t* feat = nullptr;
+    std::vector<uint32_t> fstart, fcount;
+    oracle_grid g{};
+    float R2 = 0.0f, thr = 0.0f;
+    std::vector<uint64_t> cellOf;     /* per point */
+    std::vector<uint32_t> order;      /* point ids sorted by (cell, id) */
+    std::vector<uint64_t> ckey;       /* occupied cells, ascending */
+    std::vector<uint64_t> crun;       /* M + 1: first run of each cell */
+    std::vector<uint32_t> rfeat, rcnt;
+    std::vector<uint64_t> rstart;     /* first position in `order` */
+    std::vector<int32_t> nb9;         /* 9 per cell: reference neighbour cells in visit order, -1 none */
+    std::vector<int32_t> g9;          /* 9 per cell: geometric 3x3 (dy major), -1 none */
+    uint32_t W = 0;                   /* 64-bit words per feature bitset */
+    std::vector<uint64_t> cbits;      /* M * W */
+    std::vector<uint64_t> fcell_off;  /* F + 1 */
+    std::vector<uint32_t> fcell;      /* occupied cells holding each feature */
+    std::vector<uint64_t> nboff;      /* n + 1: N+(a) */
+    std::vector<uint32_t> nbv;
+    std::vector<uint64_t> act_off;    /* F + 1: anchors with a non-empty N+, by feature */
+    std::vector<uint32_t> act;
+    const uint64_t* res_keys = nullptr;
+    const uint8_t* res_le = nullptr;
+    uint64_t nres = 0;
+    mutable std::atomic<uint64_t> unresolved{0};
+
+    bool near(uint32_t a, uint32_t b) const {   /* Data::near */
+        SqDecision dc = sq_decide(x[a], y[a], x[b], y[b], R2);
+        if (!dc.ambiguous) return dc.le;
+        uint64_t key = a < b ? ((uint64_t)a << 32 | b) : ((uint64_t)b << 32 | a);
+        const uint64_t* it = std::lower_bound(res_keys, res_keys + nres, key);
+        if (it != res_keys + nres && *it == key) return res_le[it - res_keys] != 0;
+        unresolved.fetch_add(1, std::memory_order_relaxed);
+        return dc.le;
+    }
+    int64_t cell_index(uint64_t cell) const {
+        auto it = std::lower_bound(ckey.begin(), ckey.end(), cell);
+        return (it != ckey.end() && *it == cell) ? (int64_t)(it - ckey.begin()) : -1;
+    }
+    uint32_t count(uint32_t ci, uint32_t f) const {
+        const uint32_t* b = rfeat.data() + crun[ci];
+        const uint32_t* e = rfeat.data() + crun[ci + 1];
+        const uint32_t* it = std::lower_bound(b, e, f);
+        return (it != e && *it == f) ? rcnt[it - rfeat.data()] : 0u;
+    }
+    /* [lo, hi) of the entries of feature f in N+(a) */
+    void slice(uint32_t a, uint32_t f, uint64_t* lo, uint64_t* hi) const {
+        const uint32_t* b = nbv.data() + nboff[a];
+        const uint32_t* e = nbv.data() + nboff[a + 1];
+        const uint32_t* l = std::lower_bound(b, e, f, [&](uint32_t id, uint32_t v) { return feat[id] < v; });
+        const uint32_t* h = std::upper_bound(l, e, f, [&](uint32_t v, uint32_t id) { return v < feat[id]; });
+        *lo = (uint64_t)(l - nbv.data());
+        *hi = (uint64_t)(h - nbv.data());
+    }
+};
+
+int build_fast(FastData& d, const float* x, const float* y, const uint32_t* feat, uint64_t n, uint32_t F,
+               const float bounds[4], float R, float thr) {
+    d.n = n;
+    d.F = F;
+    d.x = x;
+    d.y = y;
+    d.feat = feat;
+    d.thr = thr;
+    d.R2 = R * R;                        /* colocationFinder.cpp:73 */
+    if (make_grid(bounds[0], bounds[1], bounds[2], bounds[3], R, &d.g)) return 2;
+    d.fstart.assign(F, 0);
+    d.fcount.assign(F, 0);
+    for (uint64_t i = 0; i < n; ++i) {   /* colocationFinder.cpp:168-229 */
+        if (feat[i] >= F) return 3;
+        if (i > 0 && feat[i] < feat[i - 1]) return 3;
+        if (d.fcount[feat[i]] == 0) d.fstart[feat[i]] = (uint32_t)i;
+        d.fcount[feat[i]]++;
+    }
+    for (uint32_t f = 0; f < F; ++f)
+        if (d.fcount[f] == 0) return 3;
+    const oracle_grid& g = d.g;
+    d.cellOf.resize(n);
+    std::atomic<int> bad{0};
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        if (!std::isfinite(x[i]) || !std::isfinite(y[i])) {
+            bad.store(4);
+            continue;
+        }
+        d.cellOf[i] = cell_of(g, x[i], y[i]);
+        if (d.cellOf[i] >= g.total_cells) bad.store(4);
+    }
+    if (bad.load()) return bad.load();
+    /* the stable sort by cell of DeviceProcess.cu:342 = sort by (cell, id) */
+    struct Key {
+        uint64_t cell;
+        uint32_t id, f;
+    };
+    std::vector<Key> keys(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) keys[i] = {d.cellOf[i], (uint32_t)i, feat[i]};
+    auto by_cell = [](const Key& a, const Key& b) { return a.cell < b.cell || (a.cell == b.cell && a.id < b.id); };
+#ifdef _OPENMP
+    __gnu_parallel::sort(keys.begin(), keys.end(), by_cell);
+#else
+    std::sort(keys.begin(), keys.end(), by_cell);
+#endif
+    d.order.resize(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < (int64_t)n; ++p) d.order[p] = keys[p].id;
+    /* occupied cells and (cell, feature) runs: ids ascend within a cell, so
+     * features do too and each run is contiguous */
+    for (uint64_t p = 0; p < n; ++p) {
+        const uint64_t cell = keys[p].cell;
+        const bool new_cell = p == 0 || keys[p - 1].cell != cell;
+        if (new_cell) {
+            d.ckey.push_back(cell);
+            d.crun.push_back(d.rfeat.size());
+        }
+        if (new_cell || keys[p - 1].f != keys[p].f) {
+            d.rfeat.push_back(keys[p].f);
+            d.rstart.push_back(p);
+            d.rcnt.push_back(0);
+        }
+        d.rcnt.back()++;
+    }
+    d.crun.push_back(d.rfeat.size());
+    std::vector<Key>().swap(keys);
+    const uint64_t M = d.ckey.size();
+    if (M >= (1ull << 31)) return 6;
+    d.nb9.assign(M * 9, -1);
+    d.g9.assign(M * 9, -1);
+    /* geometric 3x3 by walking the grid rows: cells of one row ascend in x,
+     * so each neighbouring row is scanned once per row */
+    std::vector<uint64_t> rowy, rowb;   /* occupied rows: y and first cell */
+    {
+        std::vector<uint64_t> cy(M);
+#pragma omp parallel for schedule(static)
+        for (int64_t ci = 0; ci < (int64_t)M; ++ci) cy[ci] = d.ckey[ci] / g.gx;
+        for (uint64_t ci = 0; ci < M; ++ci)
+            if (ci == 0 || cy[ci] != cy[ci - 1]) {
+                rowy.push_back(cy[ci]);
+                rowb.push_back(ci);
+            }
+        rowb.push_back(M);
+    }
+    const int64_t NR = (int64_t)rowy.size();
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t ri = 0; ri < NR; ++ri) {
+        const uint64_t y = rowy[ri];
+        int64_t nbr[2] = {ri > 0 && rowy[ri - 1] + 1 == y ? ri - 1 : -1, ri + 1 < NR && rowy[ri + 1] == y + 1 ? ri + 1 : -1};
+        uint64_t ptr[2] = {nbr[0] >= 0 ? rowb[nbr[0]] : 0, nbr[1] >= 0 ? rowb[nbr[1]] : 0};
+        for (uint64_t ci = rowb[ri]; ci < rowb[ri + 1]; ++ci) {
+            const uint64_t x = d.ckey[ci] % g.gx;
+            int32_t* o = &d.g9[ci * 9];
+            if (ci > rowb[ri] && d.ckey[ci - 1] + 1 == d.ckey[ci]) o[3] = (int32_t)(ci - 1);
+            if (ci + 1 < rowb[ri + 1] && d.ckey[ci + 1] == d.ckey[ci] + 1) o[5] = (int32_t)(ci + 1);
+            o[4] = (int32_t)ci;
+            for (int side = 0; side < 2; ++side) {
+                if (nbr[side] < 0) continue;
+                const uint64_t e = rowb[nbr[side] + 1];
+                uint64_t& p = ptr[side];
+                while (p < e && d.ckey[p] % g.gx + 1 < x) ++p;     /* first cell with x' >= x - 1 */
+                for (uint64_t q = p; q < e && d.ckey[q] % g.gx <= x + 1; ++q)
+                    o[(side ? 6 : 0) + (int)(d.ckey[q] % g.gx + 1 - x)] = (int32_t)q;
+            }
+        }
+    }
+    /* the reference's neighbour cells in visit order: the geometric entry
+     * when the visited id is one, a search otherwise (the column-wrap cases) */
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t ci = 0; ci < (int64_t)M; ++ci) {
+        int s = 0;
+        const int64_t cx = (int64_t)(d.ckey[ci] % g.gx), cy = (int64_t)(d.ckey[ci] / g.gx);
+        for_neighbor_cells(g, d.ckey[ci], [&](uint64_t nc) {
+            const int64_t dx = (int64_t)(nc % g.gx) - cx, dy = (int64_t)(nc / g.gx) - cy;
+            d.nb9[ci * 9 + s++] = (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) ? d.g9[ci * 9 + (dy + 1) * 3 + (dx + 1)]
+                                                                              : (int32_t)d.cell_index(nc);
+        });
+    }
+    d.W = (F + 63) / 64;
+    d.cbits.assign(M * d.W, 0);
+    d.fcell_off.assign(F + 1, 0);
+    for (uint64_t ci = 0; ci < M; ++ci)
+        for (uint64_t r = d.crun[ci]; r < d.crun[ci + 1]; ++r) {
+            d.cbits[ci * d.W + d.rfeat[r] / 64] |= 1ull << (d.rfeat[r] % 64);
+            d.fcell_off[d.rfeat[r] + 1]++;
+        }
+    for (uint32_t f = 0; f < F; ++f) d.fcell_off[f + 1] += d.fcell_off[f];
+    d.fcell.resize(d.fcell_off[F]);
+    {
+        std::vector<uint64_t> cur(d.fcell_off.begin(), d.fcell_off.end() - 1);
+        for (uint64_t ci = 0; ci < M; ++ci)
+            for (uint64_t r = d.crun[ci]; r < d.crun[ci + 1]; ++r) d.fcell[cur[d.rfeat[r]]++] = (uint32_t)ci;
+    }
+    return 0;
+}
+
+/* N+(a) for every point (the neighbour tests of Kernel.h:12-55 / 255-316,
+ * evaluated once).  Count pass, offsets, fill pass; each list is then ordered
+ * by feature, keeping the visit order within a feature. */
+void join_fast(FastData& d) {
+    const uint64_t n = d.n, M = d.ckey.size();
+    std::vector<uint32_t> cnt(n, 0);
+    auto walk = [&](uint64_t ci, uint32_t a, uint32_t fa, auto&& emit) {
+        for (int s = 0; s < 9; ++s) {
+            const int32_t nc = d.nb9[ci * 9 + s];
+            if (nc < 0) continue;
+            const uint32_t* fb = d.rfeat.data() + d.crun[nc];
+            const uint32_t* fe = d.rfeat.data() + d.crun[nc + 1];
+            for (const uint32_t* it = std::upper_bound(fb, fe, fa); it != fe; ++it) {
+                const uint64_t r = (uint64_t)(it - d.rfeat.data());
+                for (uint64_t p = d.rstart[r]; p < d.rstart[r] + d.rcnt[r]; ++p) {
+                    const uint32_t b = d.order[p];
+                    if (d.near(a, b)) emit(b);
+                }
+            }
+        }
+    };
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t ci = 0; ci < (int64_t)M; ++ci)
+        for (uint64_t r = d.crun[ci]; r < d.crun[ci + 1]; ++r)
+            for (uint64_t p = d.rstart[r]; p < d.rstart[r] + d.rcnt[r]; ++p) {
+                const uint32_t a = d.order[p];
+                uint32_t c = 0;
+                walk((uint64_t)ci, a, d.rfeat[r], [&](uint32_t) { ++c; });
+                cnt[a] = c;
+            }
+    d.nboff.assign(n + 1, 0);
+    for (uint64_t a = 0; a < n; ++a) d.nboff[a + 1] = d.nboff[a] + cnt[a];
+    d.nbv.resize(d.nboff[n]);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t ci = 0; ci < (int64_t)M; ++ci)
+        for (uint64_t r = d.crun[ci]; r < d.crun[ci + 1]; ++r)
+            for (uint64_t p = d.rstart[r]; p < d.rstart[r] + d.rcnt[r]; ++p) {
+                const uint32_t a = d.order[p];
+                if (!cnt[a]) continue;
+                uint32_t* out = d.nbv.data() + d.nboff[a];
+                uint32_t w = 0;
+                walk((uint64_t)ci, a, d.rfeat[r], [&](uint32_t b) { out[w++] = b; });
+                std::stable_sort(out, out + w, [&](uint32_t u, uint32_t v) { return d.feat[u] < d.feat[v]; });
+            }
+    d.act_off.assign(d.F + 1, 0);
+    for (uint64_t a = 0; a < n; ++a)
+        if (cnt[a]) {
+            d.act.push_back((uint32_t)a);
+            d.act_off[d.feat[a] + 1]++;
+        }
+    for (uint32_t f = 0; f < d.F; ++f) d.act_off[f + 1] += d.act_off[f];
+}
+
+inline uint64_t popc_prefix(const std::vector<uint64_t>& bits, uint64_t nbits) {   /* bits [0, nbits) */
+    uint64_t s = 0, w = nbits / 64;
+    for (uint64_t i = 0; i < w; ++i) s += (uint64_t)__builtin_popcountll(bits[i]);
+    if (nbits % 64) s += (uint64_t)__builtin_popcountll(bits[w] & ((1ull << (nbits % 64)) - 1));
+    return s;
+}
+inline bool bit_of(const std::vector<uint64_t>& bits, uint64_t i) { return (bits[i / 64] >> (i % 64)) & 1u; }
+inline void set_bit_atomic(std::vector<uint64_t>& bits, uint64_t i) {
+    __atomic_fetch_or(&bits[i / 64], 1ull << (i % 64), __ATOMIC_RELAXED);
+}
+
+/* The window sums of getParticipationIndex (DeviceProcess.cu:108-132) from
+ * per-member participation bitsets (see the section comment), then the
+ * float ratio and strict-< minimum starting at 1.0f. */
+void numerators_fast(const FastData& d, const uint32_t* c, uint32_t k, const std::vector<std::vector<uint64_t>>& P,
+                     uint64_t* num, float* pi_out, uint32_t* argmin_out) {
+    for (uint32_t j = 0; j < k; ++j) {
+        const uint64_t nj = d.fcount[c[j]];
+        const uint64_t within = popc_prefix(P[j], nj - 1);   /* P_j & [0, L_j - 1] */
+        if (j == 0) {
+            num[j] = within;
+        } else if (k == 2) {
+            const uint64_t all = popc_prefix(P[1], nj);
+            const bool zero = bit_of(P[1], 0);
+            num[j] = (all - (zero ? 1 : 0)) + ((zero || bit_of(P[0], d.fcount[c[0]] - 1)) ? 1 : 0);
+        } else {
+            num[j] = (bit_of(P[j - 1], d.fcount[c[j - 1]] - 1) ? 1 : 0) + within;
+        }
+    }
+    float PI = 1.0f;
+    uint32_t am = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+        float pr = (float)num[j] / (float)d.fcount[c[j]];
+        if (pr < PI) {
+            PI = pr;
+            am = j;
+        }
+    }
+    *pi_out = PI;
+    *argmin_out = am;
+}
+
+/* threshold_Kernel (Kernel.h:545-573), as threshold_pass */
+bool threshold_fast(const FastData& d, const uint32_t* c, uint32_t k, const uint64_t* ub) {
+    float pi0 = 1.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        float pr = (float)((double)ub[j] / (double)(float)d.fcount[c[j]]);
+        if (j == 0) pi0 = pr;
+        else if (pi0 > pr) pi0 = pr;
+    }
+    return pi0 >= d.thr;
+}
+
+/* Valid quads of cell ci (bx in [0, gx-2], by in [0, gy-2]) as the four
+ * positions of its geometric 3x3 they cover; fn(cells[4]) per quad. */
+template <class Fn>
+inline void for_quads(const FastData& d, uint64_t ci, Fn&& fn) {
+    const oracle_grid& g = d.g;
+    const int64_t cx = (int64_t)(d.ckey[ci] % g.gx), cy = (int64_t)(d.ckey[ci] / g.gx);
+    for (int oy = -1; oy <= 0; ++oy)
+        for (int ox = -1; ox <= 0; ++ox) {
+            const int64_t bx = cx + ox, by = cy + oy;
+            if (bx < 0 || by < 0 || bx > (int64_t)g.gx - 2 || by > (int64_t)g.gy - 2) continue;
+            int32_t q[4];
+            for (int yy = 0; yy < 2; ++yy)
+                for (int xx = 0; xx < 2; ++xx) q[yy * 2 + xx] = d.g9[ci * 9 + (oy + yy + 1) * 3 + (ox + xx + 1)];
+            fn(q);
+        }
+}
+
+/* Degree-2 bounds for all pairs i < j (generation order of
+ * colocationFinder.cpp:75-82), cell by cell. */
+void filter_pairs_fast(const FastData& d, std::vector<uint64_t>& ub) {
+    const uint32_t F = d.F, W = d.W;
+    const uint64_t C = (uint64_t)F * (F - 1) / 2;
+    auto idx = [F](uint64_t i, uint64_t j) { return i * (2ull * F - i - 1) / 2 + (j - i - 1); };
+    ub.assign(C * 2, 0);
+    const uint64_t M = d.ckey.size();
+#pragma omp parallel
+    {
+        std::vector<uint64_t> loc(C * 2, 0);
+        std::vector<uint64_t> Q(W);
+#pragma omp for schedule(dynamic, 4096)
+        for (int64_t ci = 0; ci < (int64_t)M; ++ci) {
+            std::fill(Q.begin(), Q.end(), 0);
+            bool any = false;
+            for_quads(d, (uint64_t)ci, [&](const int32_t* q) {
+                any = true;
+                for (int t = 0; t < 4; ++t)
+                    if (q[t] >= 0)
+                        for (uint32_t w = 0; w < W; ++w) Q[w] |= d.cbits[(uint64_t)q[t] * W + w];
+            });
+            if (!any) continue;
+            for (uint64_t r = d.crun[ci]; r < d.crun[ci + 1]; ++r) {
+                const uint32_t i = d.rfeat[r];
+                const uint64_t c = d.rcnt[r];
+                for (uint32_t w = 0; w < W; ++w)
+                    for (uint64_t m = Q[w]; m; m &= m - 1) {
+                        const uint32_t j = w * 64 + (uint32_t)__builtin_ctzll(m);
+                        if (j == i) continue;
+                        if (i < j) loc[idx(i, j) * 2 + 0] += c;
+                        else loc[idx(j, i) * 2 + 1] += c;
+                    }
+            }
+        }
+#pragma omp critical
+        for (uint64_t t = 0; t < C * 2; ++t) ub[t] += loc[t];
+    }
+}
+
+/* Degree >= 3 bound of one candidate (filter_sparse's rule), from the quads
+ * of the cells of its member with the fewest cells.  stamp: per-thread cell
+ * marks, gen: a value not yet used in it. */
+void filter_cand_fast(const FastData& d, const uint32_t* c, uint32_t k, uint64_t* ub, std::vector<uint32_t>& stamp,
+                      uint32_t gen) {
+    const uint32_t m = k < 8 ? k : 8, W = d.W;
+    for (uint32_t j = 0; j < k; ++j) ub[j] = 0;
+    std::vector<uint64_t> mb(W, 0);
+    uint32_t drv = c[0];
+    for (uint32_t j = 0; j < m; ++j) {
+        mb[c[j] / 64] |= 1ull << (c[j] % 64);
+        if (d.fcell_off[c[j] + 1] - d.fcell_off[c[j]] < d.fcell_off[drv + 1] - d.fcell_off[drv]) drv = c[j];
+    }
+    for (uint64_t t = d.fcell_off[drv]; t < d.fcell_off[drv + 1]; ++t)
+        for_quads(d, d.fcell[t], [&](const int32_t* q) {
+            for (uint32_t w = 0; w < W; ++w) {
+                uint64_t v = 0;
+                for (int s = 0; s < 4; ++s)
+                    if (q[s] >= 0) v |= d.cbits[(uint64_t)q[s] * W + w];
+                if ((v & mb[w]) != mb[w]) return;
+            }
+            for (int s = 0; s < 4; ++s) {
+                if (q[s] < 0 || stamp[q[s]] == gen) continue;
+                stamp[q[s]] = gen;
+                for (uint32_t j = 0; j < m; ++j) ub[j] += d.count((uint32_t)q[s], c[j]);
+            }
+        });
+}
+
+struct FastRef {
+    uint64_t rows = 0;
+    std::vector<uint32_t> slots;   /* per anchor (k = 2, active anchors of c[0]) or parent row */
+};
+
+/* Degree-2 count (degree2TableSlotCounter_Kernel, Kernel.h:12-55) and PI. */
+FastRef refine2_fast(const FastData& d, const uint32_t* c, uint64_t* num, float* pi, uint32_t* am) {
+    FastRef out;
+    const uint32_t f0 = c[0], f1 = c[1];
+    std::vector<std::vector<uint64_t>> P(2);
+    P[0].assign(d.fcount[f0] / 64 + 1, 0);
+    P[1].assign(d.fcount[f1] / 64 + 1, 0);
+    const uint64_t a0 = d.act_off[f0], a1 = d.act_off[f0 + 1];
+    out.slots.assign(a1 - a0, 0);
+    for (uint64_t t = a0; t < a1; ++t) {
+        const uint32_t a = d.act[t];
+        uint64_t lo, hi;
+        d.slice(a, f1, &lo, &hi);
+        if (lo == hi) continue;
+        out.slots[t - a0] = (uint32_t)(hi - lo);
+        out.rows += hi - lo;
+        P[0][(a - d.fstart[f0]) / 64] |= 1ull << ((a - d.fstart[f0]) % 64);
+        for (uint64_t e = lo; e < hi; ++e) {
+            const uint32_t b = d.nbv[e] - d.fstart[f1];
+            P[1][b / 64] |= 1ull << (b % 64);
+        }
+    }
+    numerators_fast(d, c, 2, P, num, pi, am);
+    return out;
+}
+
+/* degree2TableGenerator_Kernel (Kernel.h:56-100): rows (a, b) by anchor, then slice order. */
+std::vector<uint32_t> fill2_fast(const FastData& d, const uint32_t* c, const FastRef& ref) {
+    std::vector<uint32_t> tab;
+    tab.reserve(ref.rows * 2);
+    const uint64_t a0 = d.act_off[c[0]];
+    for (uint64_t t = 0; t < ref.slots.size(); ++t) {
+        if (!ref.slots[t]) continue;
+        const uint32_t a = d.act[a0 + t];
+        uint64_t lo, hi;
+        d.slice(a, c[1], &lo, &hi);
+        for (uint64_t e = lo; e < hi; ++e) {
+            tab.push_back(a);
+            tab.push_back(d.nbv[e]);
+        }
+    }
+    return tab;
+}
+
+/* Level k >= 3 count (generalInstanceTableSlotCounter_Kernel, Kernel.h:255-316)
+ * over the prefix table, and PI.  par: split the parent rows over threads. */
+FastRef refinek_fast(const FastData& d, const uint32_t* c, uint32_t k, const std::vector<uint32_t>& parent, bool par,
+                     uint64_t* num, float* pi, uint32_t* am) {
+    FastRef out;
+    const uint32_t km1 = k - 1, last = c[k - 1];
+    const uint64_t prow = parent.size() / km1;
+    std::vector<std::vector<uint64_t>> P(k);
+    for (uint32_t j = 0; j < k; ++j) P[j].assign(d.fcount[c[j]] / 64 + 1, 0);
+    out.slots.assign(prow, 0);
+    uint64_t rows = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : rows) if (par)
+    for (int64_t t = 0; t < (int64_t)prow; ++t) {
+        const uint32_t* r = &parent[(size_t)t * km1];
+        uint64_t lo, hi;
+        d.slice(r[0], last, &lo, &hi);
+        uint32_t cnt = 0;
+        for (uint64_t e = lo; e < hi; ++e) {
+            const uint32_t b = d.nbv[e];
+            bool ok = true;
+            for (uint32_t i = 1; i < km1 && ok; ++i)
+                if (!d.near(r[i], b)) ok = false;
+            if (!ok) continue;
+            ++cnt;
+            set_bit_atomic(P[km1], b - d.fstart[last]);
+        }
+        if (cnt)
+            for (uint32_t i = 0; i < km1; ++i) set_bit_atomic(P[i], r[i] - d.fstart[c[i]]);
+        out.slots[t] = cnt;
+        rows += cnt;
+    }
+    out.rows = rows;
+    numerators_fast(d, c, k, P, num, pi, am);
+    return out;
+}
+
+/* generateInstanceTableGeneral_Kernel (Kernel.h:318-385): parent row order, then slice order. */
+std::vector<uint32_t> fillk_fast(const FastData& d, const uint32_t* c, uint32_t k, const std::vector<uint32_t>& parent,
+                                 const FastRef& ref, bool par) {
+    const uint32_t km1 = k - 1, last = c[k - 1];
+    const uint64_t prow = parent.size() / km1;
+    std::vector<uint64_t> off(prow + 1, 0);
+    for (uint64_t t = 0; t < prow; ++t) off[t + 1] = off[t] + ref.slots[t];
+    std::vector<uint32_t> tab(off[prow] * k);
+#pragma omp parallel for schedule(dynamic, 1024) if (par)
+    for (int64_t t = 0; t < (int64_t)prow; ++t) {
+        if (!ref.slots[t]) continue;
+        const uint32_t* r = &parent[(size_t)t * km1];
+        uint64_t lo, hi, o = off[t] * k;
+        d.slice(r[0], last, &lo, &hi);
+        for (uint64_t e = lo; e < hi; ++e) {
+            const uint32_t b = d.nbv[e];
+            bool ok = true;
+            for (uint32_t i = 1; i < km1 && ok; ++i)
+                if (!d.near(r[i], b)) ok = false;
+            if (!ok) continue;
+            for (uint32_t i = 0; i < km1; ++i) tab[o++] = r[i];
+            tab[o++] = b;
+        }
+    }
+    return tab;
+}
+
+struct PatHash {
+    size_t operator()(const std::vector<uint32_t>& v) const {
+        uint64_t h = 1469598103934665603ull;
+        for (uint32_t x : v) h = (h ^ x) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+using PatMap = std::unordered_map<std::vector<uint32_t>, int64_t, PatHash>;
+
+PatMap pattern_index(const std::vector<uint32_t>& list, size_t cnt, uint32_t deg) {
+    PatMap m;
+    m.reserve(cnt * 2);
+    for (size_t i = 0; i < cnt; ++i) {
+        std::vector<uint32_t> p(list.begin() + i * deg, list.begin() + (i + 1) * deg);
+        m.emplace(std::move(p), (int64_t)i);   /* first occurrence, as getIndex's linear search */
+    }
+    return m;
+}
+
+/* candidateColocationGeneral (colocationFinder.cpp:517-557) with the same
+ * breaks as apriori(); subsets are looked up in a hash set. */
+std::vector<uint32_t> apriori_fast(const std::vector<uint32_t>& prev, size_t nprev, uint32_t degree) {
+    std::vector<uint32_t> cand;
+    const uint32_t lastIndex = degree - 2, w = degree - 1;
+    PatMap have = pattern_index(prev, nprev, w);
+    std::vector<std::vector<uint32_t>> subs;
+    for (size_t i = 0; i < nprev; ++i) {
+        bool flag = true;
+        for (size_t j = i + 1; j < nprev; ++j) {
+            for (size_t t = 0; t < lastIndex; ++t)
+                if (prev[i * w + t] != prev[j * w + t]) {
+                    flag = false;
+                    break;
+                }
+            if (flag && prev[i * w + lastIndex] < prev[j * w + lastIndex]) {
+                std::vector<uint32_t> inter(prev.begin() + i * w, prev.begin() + (i + 1) * w);
+                inter.push_back(prev[j * w + lastIndex]);
+                subsets_lex(inter, subs);
+                flag = true;
+                for (size_t s = 2; s < degree; ++s) {
+                    flag = have.count(subs[s]) > 0;
+                    if (!flag) break;
+                }
+                if (!flag) break;
+                cand.insert(cand.end(), inter.begin(), inter.end());
+            } else {
+                break;
+            }
+        }
+    }
+    return cand;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_mine_fast(const float* x, const float* y, const uint32_t* feat, uint64_t n, uint32_t nfeat,
+                     const float bounds[4], float R, float thr, uint32_t max_k, int threads, int keep_tables,
+                     const uint64_t* res_keys, const uint8_t* res_le, uint64_t nres, oracle_result** out) {
+    oracle_result* res = new oracle_result();
+    *out = res;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    if (n == 0 || nfeat < 2) return res->status = 0;
+    using clk = std::chrono::steady_clock;
+    auto t0 = clk::now();
+    auto lap = [&](int ph) {
+        auto t1 = clk::now();
+        res->phase_ms[ph] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        t0 = t1;
+    };
+    FastData d;
+    int st = build_fast(d, x, y, feat, n, nfeat, bounds, R, thr);
+    if (st) return res->status = st;
+    lap(0);
+    d.res_keys = res_keys;
+    d.res_le = res_le;
+    d.nres = res_keys ? nres : 0;
+    struct Tally {
+        oracle_result* r;
+        const FastData& d;
+        ~Tally() { r->unresolved = d.unresolved.load(); }
+    } tally{res, d};
+    join_fast(d);
+    lap(1);
+    const uint64_t M = d.ckey.size();
+    const uint64_t kParRows = 1u << 16;   /* tables at least this long split their rows over threads */
+
+    std::vector<uint32_t> cands;
+    for (uint32_t i = 0; i + 1 < nfeat; ++i)       /* colocationFinder.cpp:75-82 */
+        for (uint32_t j = i + 1; j < nfeat; ++j) {
+            cands.push_back(i);
+            cands.push_back(j);
+        }
+    uint32_t k = 2;
+    std::vector<uint32_t> prev, parentList;
+    std::vector<size_t> prevIdx;
+    std::vector<std::vector<uint32_t>> parentTables;
+    while (true) {
+        const size_t C = cands.size() / k;
+        OLevel L;
+        L.k = k;
+        L.cand = cands;
+        L.ub.assign(C * k, 0);
+        L.num.assign(C * k, 0);
+        L.rows.assign(C, 0);
+        L.pass.assign(C, 0);
+        L.prevalent.assign(C, 0);
+        L.pi.assign(C, -1.0f);
+        L.argmin.assign(C, 0);
+        /* filter */
+        if (k == 2) {
+            filter_pairs_fast(d, L.ub);
+        } else {
+#pragma omp parallel
+            {
+                std::vector<uint32_t> stamp(M, 0);
+                uint32_t gen = 0;
+#pragma omp for schedule(dynamic, 1)
+                for (int64_t c = 0; c < (int64_t)C; ++c) filter_cand_fast(d, &cands[c * k], k, &L.ub[c * k], stamp, ++gen);
+            }
+        }
+        for (size_t c = 0; c < C; ++c) L.pass[c] = threshold_fast(d, &cands[c * k], k, &L.ub[c * k]) ? 1 : 0;
+        lap(2);
+        /* refinement of the candidates that pass */
+        std::vector<FastRef> refs(C);
+        std::vector<int64_t> parent_of(C, -1);
+        PatMap parentIdx;
+        if (k > 2) parentIdx = pattern_index(parentList, parentList.size() / (k - 1), k - 1);
+        std::vector<size_t> todo;
+        for (size_t c = 0; c < C; ++c) {
+            if (!L.pass[c]) continue;
+            if (k > 2) {
+                std::vector<uint32_t> p(cands.begin() + c * k, cands.begin() + c * k + (k - 1));
+                auto it = parentIdx.find(p);
+                if (it == parentIdx.end()) return res->status = 5;
+                parent_of[c] = it->second;
+            }
+            todo.push_back(c);
+        }
+        auto refine_one = [&](size_t c, bool par) {
+            const uint32_t* cc = &cands[c * k];
+            if (k == 2)
+                refs[c] = refine2_fast(d, cc, &L.num[c * k], &L.pi[c], &L.argmin[c]);
+            else
+                refs[c] = refinek_fast(d, cc, k, parentTables[parent_of[c]], par, &L.num[c * k], &L.pi[c],
+                                       &L.argmin[c]);
+            L.rows[c] = refs[c].rows;
+        };
+        auto big = [&](size_t c) { return k > 2 && parentTables[parent_of[c]].size() / (k - 1) >= kParRows; };
+        for (size_t c : todo)
+            if (big(c)) refine_one(c, true);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int64_t t = 0; t < (int64_t)todo.size(); ++t)
+            if (!big(todo[t])) refine_one(todo[t], false);
+        lap(3);
+        prev.clear();
+        prevIdx.clear();
+        for (size_t c : todo)
+            if (!(L.pi[c] < thr)) {                      /* cpp:335, cpp:827 */
+                L.prevalent[c] = 1;
+                prev.insert(prev.end(), &cands[c * k], &cands[c * k] + k);
+                prevIdx.push_back(c);
+            }
+        const size_t P = prevIdx.size();
+        std::vector<uint32_t> next;
+        if (P > 0 && (max_k == 0 || k + 1 <= max_k) && k + 1 <= nfeat) next = apriori_fast(prev, P, k + 1);
+        const size_t Cn = next.size() / (k + 1);
+        lap(5);
+        /* tables of the prevalent patterns that prefix a next candidate */
+        std::vector<uint8_t> need(P, 0);
+        {
+            PatMap pidx = pattern_index(prev, P, k);
+            for (size_t i = 0; i < Cn; ++i) {
+                std::vector<uint32_t> p(next.begin() + i * (k + 1), next.begin() + i * (k + 1) + k);
+                auto it = pidx.find(p);
+                if (it != pidx.end()) need[it->second] = 1;
+            }
+        }
+        std::vector<std::vector<uint32_t>> newTables(P);
+        L.tables.assign(keep_tables ? C : 0, {});
+        L.has_table.assign(C, 0);
+        auto fill_one = [&](size_t p, bool par) {
+            const size_t c = prevIdx[p];
+            const uint32_t* cc = &cands[c * k];
+            newTables[p] = k == 2 ? fill2_fast(d, cc, refs[c]) : fillk_fast(d, cc, k, parentTables[parent_of[c]], refs[c], par);
+        };
+        for (size_t p = 0; p < P; ++p)
+            if (need[p] && big(prevIdx[p])) fill_one(p, true);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int64_t p = 0; p < (int64_t)P; ++p)
+            if (need[p] && !big(prevIdx[p])) fill_one((size_t)p, false);
+        for (size_t p = 0; p < P; ++p) {
+            if (!need[p]) continue;
+            const size_t c = prevIdx[p];
+            L.has_table[c] = 1;
+            if (keep_tables) L.tables[c] = newTables[p];
+        }
+        lap(4);
+        res->levels.push_back(std::move(L));
+        if (Cn == 0) break;
+        parentTables.swap(newTables);
+        parentList = prev;
+        cands = next;
+        k++;
+    }
+    return res->status = 0;
 }
 
 }  // extern "C"

@@ -72,7 +72,20 @@ int oracle_mine(const float* x, const float* y, const uint32_t* feat, uint64_t n
                 const uint64_t* res_keys, const uint8_t* res_le, uint64_t nres,
                 oracle_result** out);
 
+/* The same results as oracle_mine (every level's candidates, bounds,
+ * verdicts, rows, numerators, PI bits and tables in the same order),
+ * organised for 10^7-10^8 points: parallel bucketing, the neighbour lists
+ * evaluated once, bitset quad tests and hashed Apriori subset checks. */
+int oracle_mine_fast(const float* x, const float* y, const uint32_t* feat, uint64_t n,
+                     uint32_t nfeat, const float bounds[4], float R, float thr,
+                     uint32_t max_k, int threads, int keep_tables,
+                     const uint64_t* res_keys, const uint8_t* res_le, uint64_t nres,
+                     oracle_result** out);
+
 void     oracle_free(oracle_result* r);
+/* Wall-clock milliseconds of oracle_mine_fast's phases: bucketing, join,
+ * filter, refine, fill, Apriori (zeros for oracle_mine). */
+void     oracle_phase_ms(const oracle_result* r, double* ms6);
 int      oracle_status(const oracle_result* r);
 /* Ambiguous comparisons met without a device outcome in res_keys/res_le
  * (sorted keys as from oracle_ambiguous_pairs; res_le = device sq <= R2). */

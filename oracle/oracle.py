@@ -53,7 +53,10 @@ def load():
     sig = {
         "oracle_mine": (C.c_int, [_f32p, _f32p, _u32p, C.c_uint64, C.c_uint32, _f32p, C.c_float, C.c_float,
                                   C.c_uint32, C.c_int, C.c_int, _u64p, _u8p, C.c_uint64, C.POINTER(V)]),
+        "oracle_mine_fast": (C.c_int, [_f32p, _f32p, _u32p, C.c_uint64, C.c_uint32, _f32p, C.c_float, C.c_float,
+                                       C.c_uint32, C.c_int, C.c_int, _u64p, _u8p, C.c_uint64, C.POINTER(V)]),
         "oracle_free": (None, [V]),
+        "oracle_phase_ms": (None, [V, _f64p]),
         "oracle_status": (C.c_int, [V]),
         "oracle_unresolved": (C.c_uint64, [V]),
         "oracle_num_levels": (C.c_uint32, [V]),
@@ -116,6 +119,7 @@ class OResult:
     status: int
     unresolved: int
     levels: List[OLevel]
+    phase_ms: Optional[dict] = None
 
     def patterns(self):
         out = []
@@ -144,7 +148,10 @@ def resolutions(res) -> tuple:
     return keys, le, len(keys)
 
 
-def mine(x, y, fid, bounds, R, thr, max_k=0, threads=0, keep_tables=False, res=None) -> OResult:
+def mine(x, y, fid, bounds, R, thr, max_k=0, threads=0, keep_tables=False, res=None, fast=False) -> OResult:
+    """Full mining run.  fast=False: the literal restatement (oracle_mine);
+    fast=True: oracle_mine_fast, the same results organised for 10^7-10^8
+    points (neighbour lists once, bitset quad tests, parallel sort)."""
     lib = load()
     x = np.ascontiguousarray(x, np.float32)
     y = np.ascontiguousarray(y, np.float32)
@@ -153,8 +160,9 @@ def mine(x, y, fid, bounds, R, thr, max_k=0, threads=0, keep_tables=False, res=N
     b = np.ascontiguousarray(bounds, np.float32)
     keys, le, nres = resolutions(res)
     h = C.c_void_p()
-    lib.oracle_mine(_p(x, _f32p), _p(y, _f32p), _p(feat, _u32p), len(x), nf, _p(b, _f32p), R, thr, max_k, threads,
-                    1 if keep_tables else 0, _p(keys, _u64p), _p(le, _u8p), nres, C.byref(h))
+    fn = lib.oracle_mine_fast if fast else lib.oracle_mine
+    fn(_p(x, _f32p), _p(y, _f32p), _p(feat, _u32p), len(x), nf, _p(b, _f32p), R, thr, max_k, threads,
+       1 if keep_tables else 0, _p(keys, _u64p), _p(le, _u8p), nres, C.byref(h))
     try:
         st = lib.oracle_status(h)
         unres = lib.oracle_unresolved(h)
@@ -181,7 +189,10 @@ def mine(x, y, fid, bounds, R, thr, max_k=0, threads=0, keep_tables=False, res=N
                         lib.oracle_table(h, li, c, _p(t, _u32p))
                         lev.tables[c] = t
             levels.append(lev)
-        return OResult(st, unres, levels)
+        ph = np.zeros(6, np.float64)
+        lib.oracle_phase_ms(h, _p(ph, _f64p))
+        names = ("bucket", "join", "filter", "refine", "fill", "apriori")
+        return OResult(st, unres, levels, {k: round(float(v), 2) for k, v in zip(names, ph)})
     finally:
         lib.oracle_free(h)
 

@@ -102,3 +102,75 @@ def test_generator_is_deterministic_and_grouped():
     assert np.array_equal(a.x, b.x) and np.array_equal(a.fid, b.fid)
     assert np.all(np.diff(a.fid) >= 0)
     assert a.x.min() >= 0 and a.x.max() < a.bounds[2]
+
+
+# ---- the scaled oracle (oracle_mine_fast) against the literal restatement ----
+
+@pytest.mark.parametrize("cfg,scale", [(0, 1.0), (1, 0.02), (3, 0.002), (4, 0.0002)])
+def test_fast_oracle_equals_literal_oracle(cfg, scale):
+    from helpers import assert_same_trace
+
+    wl = gen.config(cfg, scale=scale)
+    lit = oracle.mine(wl.x, wl.y, wl.fid, wl.bounds, wl.R, wl.thr, max_k=wl.max_size, keep_tables=True)
+    fast = oracle.mine(wl.x, wl.y, wl.fid, wl.bounds, wl.R, wl.thr, max_k=wl.max_size, keep_tables=True, fast=True)
+    assert lit.status == 0 and fast.status == 0
+    assert_same_trace(fast, lit, tables=True)
+
+
+def test_fast_oracle_reproduces_reference_golden():
+    from golden_check import CASES, assert_matches_golden, load, paths
+
+    for case in CASES:
+        g = load(case)
+        csv, par = paths(case)
+        x, y, feat, b, names = oracle.parse_csv(str(csv))
+        R, thr, _ = oracle.parse_params(str(par))
+        res = oracle.mine(x, y, feat.astype(np.int32), b, R, thr, keep_tables=True, fast=True)
+        assert res.status == 0 and res.unresolved == 0, case
+        assert_matches_golden(res, g)
+
+
+def _planted_midpoints(n_pairs=600, noise=2400, seed=3):
+    """Pairs whose exact squared distance is the midpoint 1 + 2^-24 between
+    R^2 = 1 and the next float (dx = 1, dy = 2^-12), among uniform noise."""
+    rng = np.random.default_rng(seed)
+    bx = rng.integers(1, 500, n_pairs).astype(np.float32)
+    by = rng.integers(1, 500, n_pairs).astype(np.float32)
+    x = np.concatenate([bx, bx + 1, rng.uniform(0, 500, noise).astype(np.float32)])
+    y = np.concatenate([by, by + np.float32(2.0 ** -12), rng.uniform(0, 500, noise).astype(np.float32)])
+    f = np.concatenate([np.zeros(n_pairs), np.ones(n_pairs), rng.integers(0, 3, noise)]).astype(np.int32)
+    order = np.argsort(f, kind="stable")
+    return x[order], y[order], f[order]
+
+
+def test_ambiguous_pairs_equal_brute_force():
+    x, y, f = _planted_midpoints()
+    got = oracle.ambiguous_pairs(x, y, f, 1.0)
+    n = len(x)
+    i, j = np.triu_indices(n, 1)
+    keep = f[i] != f[j]
+    i, j = i[keep], j[keep]
+    _, amb, _, _ = oracle.sq_decide_batch(x[i], y[i], x[j], y[j], np.float32(1.0))
+    want = np.sort((i[amb].astype(np.uint64) << np.uint64(32)) | j[amb].astype(np.uint64))
+    assert len(want) >= 600
+    assert np.array_equal(got, want)
+
+
+def test_fast_oracle_applies_device_outcomes_of_ambiguous_pairs():
+    """Both oracles take the outcome of every ambiguous pair from the caller;
+    flipping outcomes changes the trace the same way in both."""
+    from helpers import assert_same_trace
+
+    x, y, f = _planted_midpoints(n_pairs=400, noise=600, seed=9)
+    keys = oracle.ambiguous_pairs(x, y, f, 1.0)
+    bounds = np.array([0, 0, 502, 502], np.float32)
+    rng = np.random.default_rng(1)
+    for le in (np.ones(len(keys), np.uint8), np.zeros(len(keys), np.uint8),
+               rng.integers(0, 2, len(keys)).astype(np.uint8)):
+        a = oracle.mine(x, y, f, bounds, 1.0, 0.1, keep_tables=True, res=(keys, le))
+        b = oracle.mine(x, y, f, bounds, 1.0, 0.1, keep_tables=True, res=(keys, le), fast=True)
+        assert a.unresolved == 0 and b.unresolved == 0
+        assert_same_trace(b, a, tables=True)
+    rows = [oracle.mine(x, y, f, bounds, 1.0, 0.1, res=(keys, np.full(len(keys), v, np.uint8)), fast=True)
+            .levels[0].rows[0] for v in (0, 1)]
+    assert rows[1] - rows[0] >= 400   # every planted pair counts only when its outcome says <=

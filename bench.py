@@ -15,8 +15,8 @@ over that dataset.
           same resident data, for the batched-vs-plain ratio
 
 With --impl reference the CPU oracle (the reference's semantics restated in
-C++/OpenMP; the reference itself has no CPU path) mines a bounded sample of
-the same workload on all host cores.  Under torchrun every rank runs an
+C++/OpenMP, scaled form; the reference itself has no CPU path) mines the same
+workload in full, every step, on all host cores.  Under torchrun every rank runs an
 independent replica (the path does not exchange data between GPUs).
 """
 from __future__ import annotations
@@ -40,6 +40,8 @@ import numpy as np  # noqa: E402
 METRIC = "end-to-end mining s & candidates/s, batched+learned vs plain on 1 GB300, bit-exact PI"
 WORKLOAD = ("config3: 20,000,000 points, 100 features (Zipf s=1.2), 75% in 5,000 hotspots "
             "(sigma log-U[5,500]), 30 planted colocations of size 2-7, R=20, PI 0.15")
+JOBS_WORKLOAD = ("512 independent jobs, 2k-400k points each (log-uniform), 8-32 features, "
+                 "R = 3 x mean spacing x U[0.5, 2], PI in {0.1, 0.2, 0.3}")
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 
 
@@ -205,29 +207,50 @@ def load_traffic(kernel: str):
         return None
 
 
-def cpu_sample(wl, frac: float):
-    """Spatial window x < frac * width of the same dataset (same density)."""
-    keep = wl.x < np.float32(frac * float(wl.bounds[2]))
-    return wl.x[keep], wl.y[keep], wl.fid[keep], int(keep.sum())
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
-def run_cpu(wl, frac: float, steps: int, warmup: int):
+def run_cpu(workloads, steps: int, warmup: int):
+    """The CPU oracle (the reference's semantics restated in C++/OpenMP, scaled form) mining every
+    workload in full, every step, on all host cores.  Returns (candidates/s, cores, sample, s/step,
+    phase ms of the last step)."""
     import oracle
 
-    x, y, fid, n = cpu_sample(wl, frac)
-    times, cands = [], 0
+    times, cands, phases = [], 0, None
     for i in range(warmup + steps):
         t = time.perf_counter()
-        r = oracle.mine(x, y, fid, wl.bounds, wl.R, wl.thr, max_k=wl.max_size)
+        c = 0
+        for wl in workloads:
+            r = oracle.mine(wl.x, wl.y, wl.fid, wl.bounds, wl.R, wl.thr, max_k=wl.max_size, fast=True)
+            if r.status != 0:
+                raise RuntimeError(f"oracle status {r.status}")
+            c += r.num_candidates()
+            phases = r.phase_ms
         el = time.perf_counter() - t
         if i >= warmup:
             times.append(el)
-            cands = r.num_candidates()
+            cands = c
     cores = os.cpu_count()
     value = cands * len(times) / sum(times) if times else 0.0
-    sample = (f"spatial window x < {frac:g} * width of the same dataset ({n} of {wl.n} points, same density), "
-              f"full mining per step")
-    return value, cores, sample, sum(times) / max(len(times), 1)
+    npts = sum(wl.n for wl in workloads)
+    sample = (f"the full workload every step: all {npts} points, every level (oracle_mine_fast, "
+              f"OpenMP on {cores} threads of a {cpu_model()})")
+    return value, cores, sample, sum(times) / max(len(times), 1), phases
 
 
 def bench_jobs(args, rank, world, local, dist):
@@ -285,8 +308,7 @@ def bench_jobs(args, rank, world, local, dist):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator)",
-            "config": {"workload": "512 independent jobs, 2k-400k points each (log-uniform), 8-32 features, "
-                                   "R = 3 x mean spacing x U[0.5, 2], PI in {0.1, 0.2, 0.3}",
+            "config": {"workload": JOBS_WORKLOAD,
                        "points": int(sum(w.n for w in jobs)), "jobs": len(jobs), "candidates_per_step": cands,
                        "form": "batched+learned" if mode == colo.MODE_LEARNED else "batched"},
             "plain": {"value": out["plain"][2] / (ms_p / 1e3), "unit": "candidates/s",
@@ -303,7 +325,6 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", type=int, default=3)
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--cpu-frac", type=float, default=0.02)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--join-group", type=int, default=0,
                     help="pin the join's lanes per anchor instead of autotuning (profiling runs: "
@@ -318,15 +339,18 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        wl = gen.config(args.config, scale=args.scale)
-        value, cores, sample, sec = run_cpu(wl, args.cpu_frac, args.steps, args.warmup)
+        if args.config == 2:
+            wls, workload = gen.config2_jobs(512, scale=args.scale), JOBS_WORKLOAD
+        else:
+            wls, workload = [gen.config(args.config, scale=args.scale)], WORKLOAD
+        value, cores, sample, sec, phases = run_cpu(wls, args.steps, args.warmup)
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "sample": sample},
+            "config": {"workload": workload, "points": int(sum(w.n for w in wls)), "sample": sample},
             "cpu_baseline": {"value": value, "unit": "candidates/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "phase_ms_last_step": phases},
             "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }), flush=True)
         return
@@ -447,8 +471,9 @@ def main():
     cpu = None
     io = None
     if not args.no_cpu and world == 1:
-        v, cores, sample, _ = run_cpu(wl, args.cpu_frac, 1, 0)
-        cpu = {"value": v, "unit": "candidates/s", "cores": cores, "kind": "port", "sample": sample}
+        v, cores, sample, sec, phases = run_cpu([wl], 1, 0)
+        cpu = {"value": v, "unit": "candidates/s", "cores": cores, "kind": "port", "sample": sample,
+               "s_per_step": round(sec, 3), "phase_ms": phases}
         io = measure_io(ctx, wl, ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size),
                         res_b[0].patterns())
     line = {

@@ -53,6 +53,13 @@ struct Batch {
     DevBuf<uint32_t> nbmask;     // per cell: feature mask of its geometric 3x3 block
     DevBuf<uint32_t> listq, nlistq;   // cells whose 3x3 block has a feature above their lowest own one
     DevBuf<uint32_t> qmask;      // per cell: masks of the 4 quads containing it ([M][4][W])
+    // driver lists: for global feature f, the cells whose 3x3 block holds f
+    // (nbmask bit), dlist[doff[f] .. doff[f+1]), in no particular order; the
+    // level filters test exactly these cells for the candidates f drives
+    DevBuf<uint32_t> dlist;
+    DevBuf<uint64_t> doff;
+    std::vector<uint64_t> h_doff;
+    bool dlist_ready = false;    // lists filled (on the first level filter of the mine)
     DevBuf<uint8_t> qfirst;      // per cell: bit q set when it is the first occupied cell of its quad q
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
@@ -80,6 +87,7 @@ struct Batch {
     uint64_t active_anchors = 0; // anchors whose cell has higher-feature neighbours
     bool join_single = true;     // single pass into per-run upper-bound regions
     int join_group = 8;          // lanes per anchor in the join (autotuned)
+    uint32_t test_spin = 0;      // tests only: the sort's look-back gives up after this many polls
     uint64_t filter_items = 0;   // (driver cell, candidate) items of the level filters
 };
 
@@ -95,6 +103,10 @@ uint64_t neighbor_entries(Batch& b);     // E (waits for the device sum once)
 void apriori_device(cudaStream_t s, const std::vector<const std::vector<uint32_t>*>& prev, uint32_t km1,
                     std::vector<std::vector<uint32_t>>& out, std::vector<std::vector<uint32_t>>& parent);
 // colo_filter.cu
+// Driver lists: per-feature cell counts into d_cnt (F entries, zeroed by the
+// caller); the lists themselves are filled from b.h_doff by the first level
+// filter of the mine.
+void driver_lists_count(Batch& b, uint32_t* d_cnt);
 // Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
 // bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.
 // Runs on stream s (no wait at the end).
@@ -117,8 +129,7 @@ struct CandDesc {
     const uint64_t* offs;        // per parent row output offsets (fill pass input)
     uint32_t* out;               // column-major output table (k columns, rows = total)
     uint64_t out_rows;           // rows of the output table (column stride)
-    uint64_t out_cap;            // capacity (single-pass mode)
-    unsigned long long* cursor;  // single-pass mode: rows reserved so far
+    uint64_t out_cap;            // capacity (single-pass mode; also its column stride)
     unsigned long long* rows;    // count pass: rows of this candidate (atomic sum)
     uint32_t* bitmap;            // member bitmaps: member j's words start at bm_base plus
     uint64_t bm_base;            // the sum over i < j of ceil(fcount[m[i]] / 32)
@@ -132,10 +143,13 @@ struct LevelWork {
     uint64_t ncand;
     uint64_t nchunks;
     unsigned long long* items;   // optional: sum of candidate-slice lengths examined
+    unsigned long long* chunk_status = nullptr;   // single pass: nchunks words, zeroed
+    unsigned long long* ticket = nullptr;         // single pass: chunk ticket counter, zeroed
 };
 
-// count pass: slots + bitmaps; fill pass: rows; single pass: rows at
-// reserved positions + slots + bitmaps (overflow recorded per candidate).
+// count pass: slots + bitmaps; fill pass: rows; single pass: slots +
+// bitmaps + rows at their count-and-fill positions (overflow recorded per
+// candidate; a look-back that waits too long sets the batch's timeout flag).
 void level_count(Batch& b, const LevelWork& w, uint32_t k);
 void level_fill(Batch& b, const LevelWork& w, uint32_t k);
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow);

@@ -717,7 +717,7 @@ void sort_and_compact(Batch& b) {
     count_launch();
     }
     // a look-back timeout lands in the batch's flags, read with the compaction totals
-    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get(), &b.flags.get()->timeout);
+    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get(), &b.flags.get()->timeout, b.test_spin);
 
     b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);
@@ -849,14 +849,24 @@ void bucket_points(Batch& b) {
             COLO_LAUNCH_CHECK();
             count_launch();
         }
-        // the run counts and the error flags come back with one wait
-        std::vector<uint32_t> hc(b.F);
+        // cells per driver list (3x3 blocks holding each feature)
+        DevBuf<uint32_t> dcnt;
+        dcnt.alloc(b.F ? b.F : 1, s);
+        dcnt.zero(s);
+        driver_lists_count(b, dcnt.get());
+        // the run counts, list sizes and error flags come back with one wait
+        std::vector<uint32_t> hc(b.F), hd(b.F);
         DevFlags hf;
-        if (b.F) COLO_CUDA(cudaMemcpyAsync(hc.data(), cnt.get(), b.F * 4, cudaMemcpyDeviceToHost, s));
+        if (b.F) {
+            COLO_CUDA(cudaMemcpyAsync(hc.data(), cnt.get(), b.F * 4, cudaMemcpyDeviceToHost, s));
+            COLO_CUDA(cudaMemcpyAsync(hd.data(), dcnt.get(), b.F * 4, cudaMemcpyDeviceToHost, s));
+        }
         COLO_CUDA(cudaMemcpyAsync(&hf, b.flags.get(), sizeof(hf), cudaMemcpyDeviceToHost, s));
         COLO_CUDA(cudaStreamSynchronize(s));
         b.h_frun_off.assign(b.F + 1, 0);
         for (uint32_t f = 0; f < b.F; ++f) b.h_frun_off[f + 1] = b.h_frun_off[f] + hc[f];
+        b.h_doff.assign(b.F + 1, 0);
+        for (uint32_t f = 0; f < b.F; ++f) b.h_doff[f + 1] = b.h_doff[f] + hd[f];
         if (hf.timeout) throw StatusError{COLO_ERR_TIMEOUT, "radix sort: a tile waited too long for its predecessors"};
         if (hf.out_of_grid)
             throw StatusError{COLO_ERR_INPUT, std::to_string(hf.out_of_grid) +

@@ -17,8 +17,11 @@
 //
 // Level k >= 3: a cell is in U_c when one of its four quads is full; the
 // cells tested for c are those with c's driver member (the one with the
-// fewest cells) in their 3x3 block, which holds every cell of U_c.
+// fewest cells) in their 3x3 block, which holds every cell of U_c.  Those
+// cells are listed once per mine, per feature (driver lists), so a level
+// touches only the lists of its drivers.
 #include <algorithm>
+#include <cstring>
 
 #include "colo_batch.h"
 #include "colo_device.cuh"
@@ -135,73 +138,100 @@ __device__ __forceinline__ void load_row(const uint32_t* __restrict__ p, uint32_
     }
 }
 
-// Position of the r-th set bit (r < popc(v)) of v.
-__device__ __forceinline__ uint32_t select_bit(uint32_t v, uint32_t r) {
-    uint32_t pos = 0;
-#pragma unroll
-    for (int half = 16; half > 0; half >>= 1) {
-        const uint32_t lo = __popc(v & ((1u << half) - 1u));
-        if (r >= lo) {
-            r -= lo;
-            v >>= half;
-            pos += half;
-        }
-    }
-    return pos;
-}
+// ---- driver lists -----------------------------------------------------------
+// Cells per feature f whose 3x3 block holds f (bit f of nbmask): a block-local
+// histogram when the batch has at most kDilHist features, else global atomics.
+constexpr uint32_t kDilHist = 4096;
 
-// Last lane whose exclusive offset is <= t (the lane owning entry t).
-__device__ __forceinline__ int owner_lane(uint32_t excl, uint32_t t) {
-    int o = 0;
-#pragma unroll
-    for (int bstep = 16; bstep > 0; bstep >>= 1) {
-        const uint32_t ev = __shfl_sync(0xffffffffu, excl, o + bstep);
-        if (ev <= t) o += bstep;
-    }
-    return o;
-}
-
-__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, int lane) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += t;
-    }
-    return v;
-}
-
-// Level k >= 3, one (cell Z, candidate c) pair per lane.
-//
-// A cell Z lies in U_c exactly when one of its four quads (qmask[Z]) is full
-// for c.  A full quad holds a cell of every member, in particular of c's
-// driver member d (the member with the fewest cells), so every cell of U_c
-// has d in its 3x3 feature mask nbmask[Z].  The pairs tested are therefore
-// (Z, c) for every occupied cell Z and every candidate whose driver is in
-// nbmask[Z]; each pair is tested once, so each cell of U_c is counted once
-// with no ownership rule.  A full quad is counted at its first occupied cell
-// in (ey, ex) order (bit q of qfirst[Z]), so each is counted once.
-//
-// A warp takes 32 consecutive cells, expands them into (Z, driver) pairs and
-// those into (Z, candidate) pairs (warp prefix sums; candidates of one driver
-// in adjacent lanes, so lanes share Z's masks in L1).
-// stats[c*2] = full quads, stats[c*2+1] = cells in U_c.  cjob is null for a
-// one-job batch (every cell in job 0), which saves the scan a load per cell.
-//
-// Sums go to a block-private accumulator in shared memory when the level's
-// candidates fit (acc_n = ncand * (m + 2) counters: m bounds, quads, cells),
-// and are added to ub / stats once per block at the end: a level has few
-// candidates and millions of hits, and global atomics on the same few
-// addresses serialise in their L2 slice.
 template <int WT>
-__global__ void __launch_bounds__(256, (WT <= 8 ? 5 : 1)) k_filter_cells(
-    uint64_t M, const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids,
-    const uint32_t* __restrict__ nbmask, const uint32_t* __restrict__ dmask,
-    const uint32_t* __restrict__ drv_count, const uint32_t* __restrict__ drv_start,
-    const uint32_t* __restrict__ order, const uint32_t* __restrict__ need_all, const uint32_t* __restrict__ lmem,
-    uint32_t k, const uint32_t* __restrict__ qmask, const uint32_t* __restrict__ cmask,
-    const uint32_t* __restrict__ crun, const uint8_t* __restrict__ qfirst, const uint32_t* __restrict__ rcnt,
-    uint32_t* __restrict__ ub, unsigned long long* __restrict__ stats, uint32_t acc_n) {
+__global__ void __launch_bounds__(256) k_dil_count(uint64_t M, const uint32_t* __restrict__ cjob,
+                                                   const JobGrid* __restrict__ grids,
+                                                   const uint32_t* __restrict__ nbmask, uint32_t F,
+                                                   uint32_t* __restrict__ cnt) {
+    extern __shared__ uint32_t h[];
+    const bool local = F <= kDilHist;
+    if (local)
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint64_t z = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; z < M; z += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t row[WT];
+        load_row<WT>(nbmask + z * WT, row);
+        const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w)
+            for (uint32_t bits = row[w]; bits; bits &= bits - 1) {
+                const uint32_t f = f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1);
+                if (local) atomicAdd(&h[f], 1u);
+                else atomicAdd(&cnt[f], 1u);
+            }
+    }
+    __syncthreads();
+    if (local)
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
+            if (h[i]) atomicAdd(&cnt[i], h[i]);
+}
+
+// Each block owns `per` consecutive cells: it counts its entries per feature,
+// reserves one range per feature in the lists, and writes its cells there.
+template <int WT>
+__global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, const uint32_t* __restrict__ cjob,
+                                                  const JobGrid* __restrict__ grids,
+                                                  const uint32_t* __restrict__ nbmask, uint32_t F,
+                                                  const uint64_t* __restrict__ doff, uint32_t* __restrict__ cursor,
+                                                  uint32_t* __restrict__ dlist) {
+    extern __shared__ unsigned long long hb[];   // F bases, then F counters (32-bit)
+    uint32_t* hc = reinterpret_cast<uint32_t*>(hb + F);
+    const bool local = F <= kDilHist;
+    const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
+    auto each = [&](auto&& fn) {
+        for (uint64_t z = z0 + threadIdx.x; z < z1; z += blockDim.x) {
+            uint32_t row[WT];
+            load_row<WT>(nbmask + z * WT, row);
+            const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
+#pragma unroll
+            for (int w = 0; w < WT; ++w)
+                for (uint32_t bits = row[w]; bits; bits &= bits - 1)
+                    fn(z, f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1));
+        }
+    };
+    if (!local) {
+        each([&](uint64_t z, uint32_t f) { dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z; });
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) hc[i] = 0;
+    __syncthreads();
+    each([&](uint64_t, uint32_t f) { atomicAdd(&hc[f], 1u); });
+    __syncthreads();
+    for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
+        const uint32_t c = hc[f];
+        if (c) hb[f] = doff[f] + atomicAdd(&cursor[f], c);
+        hc[f] = 0;
+    }
+    __syncthreads();
+    each([&](uint64_t z, uint32_t f) { dlist[hb[f] + atomicAdd(&hc[f], 1u)] = (uint32_t)z; });
+}
+
+// Level k >= 3 over the driver lists.  Candidates are grouped by driver
+// (group g: driver feature gfeat[g], candidates order[gstart[g] ..
+// gstart[g] + gcount[g])); a unit is 32 cells of the driver's list times up
+// to 32 of its candidates, units of one cell chunk adjacent (they read the
+// same quad masks).  A warp takes a unit: lane = cell, loop over the
+// candidates; a (cell Z, candidate c) pair is tested exactly as in a scan
+// of every cell with the driver in its 3x3 block: Z is in U_c when one of
+// its four quads covers c's members, each cell of U_c is met once, and a
+// full quad is counted at its first occupied cell (qfirst).  Sums go to a
+// block-private accumulator when the level's counters fit (acc_n).
+template <int WT>
+__global__ void __launch_bounds__(256, (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1))) k_filter_drv(
+    uint64_t nunits, uint32_t ngroups, const uint64_t* __restrict__ uoff, const uint32_t* __restrict__ gfeat,
+    const uint32_t* __restrict__ gstart, const uint32_t* __restrict__ gcount, const uint64_t* __restrict__ doff,
+    const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ order, const uint32_t* __restrict__ need_all,
+    const uint32_t* __restrict__ lmem, uint32_t k, const uint32_t* __restrict__ qmask,
+    const uint32_t* __restrict__ cmask, const uint32_t* __restrict__ crun, const uint8_t* __restrict__ qfirst,
+    const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub, unsigned long long* __restrict__ stats,
+    uint32_t acc_n) {
     constexpr uint32_t W = WT;
+    constexpr bool kCacheQuads = WT <= 8;
     extern __shared__ uint32_t acc[];
     const uint32_t m = k < kMaxMembersFiltered ? k : kMaxMembersFiltered;
     const uint32_t stride = m + 2;
@@ -209,124 +239,78 @@ __global__ void __launch_bounds__(256, (WT <= 8 ? 5 : 1)) k_filter_cells(
     for (uint32_t i = threadIdx.x; i < acc_n; i += blockDim.x) acc[i] = 0;
     __syncthreads();
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    // the next chunk's job and 3x3 mask are loaded before this chunk is
-    // processed, so their latency overlaps this chunk's work
-    const uint64_t zstride = nwarps * 32;
-    uint64_t zbase = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
-    uint32_t job_c = 0, nb_c[WT];
-#pragma unroll
-    for (int w = 0; w < WT; ++w) nb_c[w] = 0;
-    if (zbase + lane < M) {
-        job_c = cjob ? cjob[zbase + lane] : 0u;
-        load_row<WT>(nbmask + (zbase + lane) * W, nb_c);
-    }
-    for (; zbase < M; zbase += zstride) {
-        const uint64_t Zn = zbase + zstride + lane;
-        uint32_t job_n = 0, nb_n[WT];
-#pragma unroll
-        for (int w = 0; w < WT; ++w) nb_n[w] = 0;
-        if (Zn < M) {
-            job_n = cjob ? cjob[Zn] : 0u;
-            load_row<WT>(nbmask + Zn * W, nb_n);
+    for (uint64_t u = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < nunits; u += nwarps) {
+        uint32_t lo = 0, hi = ngroups;   // the group of unit u: last g with uoff[g] <= u
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(uoff + mid) <= u) lo = mid;
+            else hi = mid;
         }
-        // this lane's cell and the drivers of its 3x3 block
-        const uint64_t Z = zbase + lane;
-        uint32_t dz[WT], f0 = 0, nd = 0;
+        const uint32_t f = __ldg(gfeat + lo), G = __ldg(gcount + lo), gs = __ldg(gstart + lo);
+        const uint32_t gch = (G + 31) / 32;
+        const uint64_t local = u - __ldg(uoff + lo);
+        const uint64_t cc = local / gch;
+        const uint32_t gc = (uint32_t)(local - cc * gch);
+        const uint64_t l0 = __ldg(doff + f), L = __ldg(doff + f + 1) - l0;
+        const uint64_t zi = cc * 32 + (uint64_t)lane;
+        const bool valid = zi < L;
+        const uint64_t Z = valid ? __ldg(dlist + l0 + zi) : 0u;
+        const uint32_t* q4 = qmask + Z * 4 * W;
+        uint32_t qr[kCacheQuads ? 4 : 1][kCacheQuads ? WT : 1];
+        if constexpr (kCacheQuads) {
+            if (valid) {
 #pragma unroll
-        for (int w = 0; w < WT; ++w) dz[w] = 0;
-        if (Z < M) {
-            f0 = grids[job_c].f0;
-            uint32_t dm[WT];
-            load_row<WT>(dmask + (uint64_t)job_c * W, dm);
-#pragma unroll
-            for (int w = 0; w < WT; ++w) {
-                dz[w] = nb_c[w] & dm[w];
-                nd += __popc(dz[w]);
+                for (int q = 0; q < 4; ++q) load_row<WT>(q4 + q * W, qr[q]);
             }
         }
-        job_c = job_n;
+        const uint32_t t1 = gc * 32 + 32 < G ? gc * 32 + 32 : G;
+        for (uint32_t t = gc * 32; t < t1; ++t) {
+            const uint32_t c = __ldg(order + gs + t);
+            uint32_t need[WT];
+            load_row<WT>(need_all + (uint64_t)c * W, need);
+            if (!valid) continue;
+            uint32_t full = 0;
 #pragma unroll
-        for (int w = 0; w < WT; ++w) nb_c[w] = nb_n[w];
-        const uint32_t pincl = warp_incl_sum(nd, lane);
-        const uint32_t pex = pincl - nd;
-        const uint32_t npairs = __shfl_sync(0xffffffffu, pincl, 31);
-        for (uint32_t p0 = 0; p0 < npairs; p0 += 32) {
-            // (cell, driver) pair p0 + lane
-            const uint32_t t = p0 + lane;
-            const int o = owner_lane(pex, t);
-            const uint32_t ex_o = __shfl_sync(0xffffffffu, pex, o);
-            const uint32_t f0_o = __shfl_sync(0xffffffffu, f0, o);
-            uint32_t r = t - ex_o, d = 0;
-            bool found = false;
-#pragma unroll
-            for (int w = 0; w < WT; ++w) {
-                const uint32_t v = __shfl_sync(0xffffffffu, dz[w], o);
-                const uint32_t pc = __popc(v);
-                if (!found && r < pc) {
-                    d = (uint32_t)w * 32 + select_bit(v, r);
-                    found = true;
-                } else if (!found) {
-                    r -= pc;
-                }
-            }
-            uint32_t G = 0, start = 0;
-            if (t < npairs) {
-                G = drv_count[f0_o + d];
-                start = drv_start[f0_o + d];
-            }
-            const uint64_t Zp = zbase + (uint64_t)o;
-            const uint32_t iincl = warp_incl_sum(G, lane);
-            const uint32_t iex = iincl - G;
-            const uint32_t nitems = __shfl_sync(0xffffffffu, iincl, 31);
-            for (uint32_t i0 = 0; i0 < nitems; i0 += 32) {
-                // (cell, candidate) pair i0 + lane
-                const uint32_t it = i0 + lane;
-                const int o2 = owner_lane(iex, it);
-                const uint32_t ex2 = __shfl_sync(0xffffffffu, iex, o2);
-                const uint32_t st2 = __shfl_sync(0xffffffffu, start, o2);
-                const uint64_t Zi = __shfl_sync(0xffffffffu, Zp, o2);
-                if (it >= nitems) continue;
-                const uint32_t c = order[st2 + (it - ex2)];
-                uint32_t need[WT];
-                load_row<WT>(need_all + (uint64_t)c * W, need);
-                const uint32_t* q4 = qmask + Zi * 4 * W;
-                uint32_t full = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < 4; ++q) {
+                bool ok;
+                if constexpr (kCacheQuads) {
+                    ok = covers<WT>(qr[q], need);
+                } else {
                     uint32_t qm[WT];
                     load_row<WT>(q4 + q * W, qm);
-                    if (covers<WT>(qm, need)) full |= 1u << q;
+                    ok = covers<WT>(qm, need);
                 }
-                if (!full) continue;
-                uint32_t cm[WT];
-                load_row<WT>(cmask + Zi * W, cm);
-                const uint32_t q0 = crun[Zi];
-                uint32_t lm[4];
-                load_row<4>(lmem + (uint64_t)c * 4, lm);
+                if (ok) full |= 1u << q;
+            }
+            if (!full) continue;
+            uint32_t cm[WT];
+            load_row<WT>(cmask + Z * W, cm);
+            const uint32_t q0 = crun[Z];
+            uint32_t lm[4];
+            load_row<4>(lmem + (uint64_t)c * 4, lm);
 #pragma unroll
-                for (int jj = 0; jj < kMaxMembersFiltered; ++jj) {
-                    if ((uint32_t)jj >= m) break;
-                    const uint32_t lf = (lm[jj >> 1] >> ((jj & 1) * 16)) & 0xFFFFu, wq = lf >> 5;
-                    uint32_t rk = 0, word = 0;
+            for (int jj = 0; jj < kMaxMembersFiltered; ++jj) {
+                if ((uint32_t)jj >= m) break;
+                const uint32_t lf = (lm[jj >> 1] >> ((jj & 1) * 16)) & 0xFFFFu, wq = lf >> 5;
+                uint32_t rk = 0, word = 0;
 #pragma unroll
-                    for (int w = 0; w < WT; ++w) {
-                        if ((uint32_t)w < wq) rk += __popc(cm[w]);
-                        if ((uint32_t)w == wq) word = cm[w];
-                    }
-                    if (word >> (lf & 31) & 1u) {
-                        const uint32_t v = rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))];
-                        if (acc_n) atomicAdd(&acc[c * stride + jj], v);
-                        else atomicAdd(&ub[(uint64_t)c * k + jj], v);
-                    }
+                for (int w = 0; w < WT; ++w) {
+                    if ((uint32_t)w < wq) rk += __popc(cm[w]);
+                    if ((uint32_t)w == wq) word = cm[w];
                 }
-                const uint32_t nq = __popc(full & qfirst[Zi]);
-                if (acc_n) {
-                    if (nq) atomicAdd(&acc[c * stride + m], nq);
-                    atomicAdd(&acc[c * stride + m + 1], 1u);
-                } else if (stats) {
-                    if (nq) atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nq);
-                    atomicAdd(&stats[(uint64_t)c * 2 + 1], 1ull);
+                if (word >> (lf & 31) & 1u) {
+                    const uint32_t v = rcnt[q0 + rk + __popc(word & ((1u << (lf & 31)) - 1u))];
+                    if (acc_n) atomicAdd(&acc[c * stride + jj], v);
+                    else atomicAdd(&ub[(uint64_t)c * k + jj], v);
                 }
+            }
+            const uint32_t nq = __popc(full & qfirst[Z]);
+            if (acc_n) {
+                if (nq) atomicAdd(&acc[c * stride + m], nq);
+                atomicAdd(&acc[c * stride + m + 1], 1u);
+            } else if (stats) {
+                if (nq) atomicAdd(&stats[(uint64_t)c * 2], (unsigned long long)nq);
+                atomicAdd(&stats[(uint64_t)c * 2 + 1], 1ull);
             }
         }
     }
@@ -340,6 +324,68 @@ __global__ void __launch_bounds__(256, (WT <= 8 ? 5 : 1)) k_filter_cells(
             else if (stats) atomicAdd(&stats[(uint64_t)c * 2 + (r - m)], (unsigned long long)v);
         }
     }
+}
+
+}  // namespace
+
+#define COLO_W_SWITCH(W, MACRO)                                                                   \
+    switch (W) {                                                                                  \
+        case 1: MACRO(1); break;                                                                  \
+        case 2: MACRO(2); break;                                                                  \
+        case 3: MACRO(3); break;                                                                  \
+        case 4: MACRO(4); break;                                                                  \
+        case 5: MACRO(5); break;                                                                  \
+        case 6: MACRO(6); break;                                                                  \
+        case 7: MACRO(7); break;                                                                  \
+        case 8: MACRO(8); break;                                                                  \
+        case 12: MACRO(12); break;                                                                \
+        case 16: MACRO(16); break;                                                                \
+        case 24: MACRO(24); break;                                                                \
+        case 32: MACRO(32); break;                                                                \
+        default: throw StatusError{COLO_ERR_INTERNAL, "mask words not padded to a supported width"}; \
+    }
+
+void driver_lists_count(Batch& b, uint32_t* d_cnt) {
+    if (b.M == 0 || b.F == 0) return;
+    cudaStream_t s = b.s;
+    const size_t smem = b.F <= kDilHist ? (size_t)b.F * 4 : 0;
+    const uint64_t blocks = std::min<uint64_t>((b.M + 255) / 256, (uint64_t)b.sms * 4);
+    KScope ks("driver_lists");
+#define COLO_DC(WW)                                                                                        \
+    k_dil_count<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
+                                                        b.nbmask.get(), b.F, d_cnt)
+    COLO_W_SWITCH(b.W, COLO_DC)
+#undef COLO_DC
+    COLO_LAUNCH_CHECK();
+    count_launch();
+}
+
+namespace {
+
+void driver_lists_fill(Batch& b) {
+    cudaStream_t s = b.s;
+    b.dlist_ready = true;
+    const uint64_t total = b.h_doff.empty() ? 0 : b.h_doff[b.F];
+    b.dlist.alloc(total ? total : 1, s);
+    b.doff.alloc(b.F + 1, s);
+    COLO_CUDA(cudaMemcpyAsync(b.doff.get(), b.h_doff.data(), (b.F + 1) * 8, cudaMemcpyHostToDevice, s));
+    if (total == 0) return;
+    DevBuf<uint32_t> cursor;
+    cursor.alloc(b.F, s);
+    cursor.zero(s);
+    const size_t smem = b.F <= kDilHist ? (size_t)b.F * 12 : 0;
+    if (smem > 48 * 1024) throw StatusError{COLO_ERR_INTERNAL, "driver-list histogram exceeds 48 KB"};
+    uint64_t blocks = std::min<uint64_t>((b.M + 255) / 256, (uint64_t)b.sms * 4);
+    const uint64_t per = (b.M + blocks - 1) / blocks;
+    blocks = (b.M + per - 1) / per;
+    KScope ks("driver_lists");
+#define COLO_DF(WW)                                                                                           \
+    k_dil_fill<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
+                                                       b.nbmask.get(), b.F, b.doff.get(), cursor.get(), b.dlist.get())
+    COLO_W_SWITCH(b.W, COLO_DF)
+#undef COLO_DF
+    COLO_LAUNCH_CHECK();
+    count_launch();
 }
 
 }  // namespace
@@ -386,17 +432,18 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     if (b.W > kMaxW) throw StatusError{COLO_ERR_CAPACITY, "the filter handles at most 1024 features per job"};
     cudaStream_t s = b.s;
     const uint32_t m = k < kMaxMembersFiltered ? k : (uint32_t)kMaxMembersFiltered;
-    // driver = member with the fewest cells; candidates grouped by driver;
-    // per candidate its need mask and local member ids (bytes), per job the
-    // mask of its drivers
-    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0), lmem((size_t)ncand * 4, 0),
-        dmask((size_t)b.J * b.W, 0);
+    // driver = member with the shortest driver list (the fewest cells with it in
+    // their 3x3 block: the cells its candidates are tested on); candidates
+    // grouped by driver; per candidate its need mask and local member ids
+    // (16 bits each)
+    std::vector<uint32_t> drv(ncand), need((size_t)ncand * b.W, 0), lmem((size_t)ncand * 4, 0);
     for (uint64_t c = 0; c < ncand; ++c) {
         const uint32_t* mem = h_cand + c * k;
         const uint32_t f0 = b.jobs[h_job[c]].grid.f0;
-        uint32_t best = mem[0], bn = UINT32_MAX;
+        uint32_t best = mem[0];
+        uint64_t bn = UINT64_MAX;
         for (uint32_t j = 0; j < m; ++j) {
-            uint32_t nr = b.h_frun_off[mem[j] + 1] - b.h_frun_off[mem[j]];
+            const uint64_t nr = b.h_doff[mem[j] + 1] - b.h_doff[mem[j]];
             if (nr < bn) {
                 bn = nr;
                 best = mem[j];
@@ -406,8 +453,6 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
             lmem[(size_t)c * 4 + (j >> 1)] |= lf << ((j & 1) * 16);
         }
         drv[c] = best;
-        const uint32_t ld = best - f0;
-        dmask[(size_t)h_job[c] * b.W + (ld >> 5)] |= 1u << (ld & 31);
     }
     std::vector<uint32_t> order(ncand);
     for (uint64_t c = 0; c < ncand; ++c) order[c] = (uint32_t)c;
@@ -421,65 +466,69 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     for (uint32_t f = 0; f < b.F; ++f) nitems += (uint64_t)dcount[f] * (b.h_frun_off[f + 1] - b.h_frun_off[f]);
     b.filter_items += nitems;
     if (nitems == 0) return;
-    // one upload: need | lmem | dmask | dcount | dstart | order, each part on a
-    // 16-byte boundary (mask rows are read as vectors)
+    if (!b.dlist_ready) driver_lists_fill(b);
+    // groups (one per driver) and their units: 32 list cells x up to 32 candidates
+    std::vector<uint32_t> gfeat, gstart, gcount;
+    std::vector<uint64_t> uoff(1, 0);
+    for (uint32_t f = 0; f < b.F; ++f) {
+        if (!dcount[f]) continue;
+        const uint64_t L = b.h_doff[f + 1] - b.h_doff[f];
+        gfeat.push_back(f);
+        gstart.push_back(dstart[f]);
+        gcount.push_back(dcount[f]);
+        uoff.push_back(uoff.back() + (L + 31) / 32 * ((dcount[f] + 31) / 32));
+    }
+    const uint32_t ngroups = (uint32_t)gfeat.size();
+    const uint64_t nunits = uoff.back();
+    if (nunits == 0) return;
+    // one upload: need | lmem | order | gfeat | gstart | gcount | uoff (u64), mask rows and the
+    // u64 part on 16-byte boundaries
     auto up4 = [](size_t v) { return (v + 3) & ~(size_t)3; };
-    const size_t n_need = up4(need.size()), n_lmem = up4(lmem.size()), n_dm = up4(dmask.size());
-    std::vector<uint32_t> pack;
-    pack.reserve(n_need + n_lmem + n_dm + 2 * (size_t)b.F + ncand);
-    pack.insert(pack.end(), need.begin(), need.end());
-    pack.resize(n_need, 0);
-    pack.insert(pack.end(), lmem.begin(), lmem.end());
-    pack.resize(n_need + n_lmem, 0);
-    pack.insert(pack.end(), dmask.begin(), dmask.end());
-    pack.resize(n_need + n_lmem + n_dm, 0);
-    pack.insert(pack.end(), dcount.begin(), dcount.end());
-    pack.insert(pack.end(), dstart.begin(), dstart.end());
-    pack.insert(pack.end(), order.begin(), order.end());
+    const size_t n_need = up4(need.size()), n_lmem = up4(lmem.size()), n_ord = up4(order.size());
+    const size_t n_g = up4(ngroups);
+    std::vector<uint32_t> pack(n_need + n_lmem + n_ord + 3 * n_g + 2 * uoff.size(), 0);
+    size_t o = 0;
+    std::copy(need.begin(), need.end(), pack.begin() + o);
+    o += n_need;
+    std::copy(lmem.begin(), lmem.end(), pack.begin() + o);
+    o += n_lmem;
+    std::copy(order.begin(), order.end(), pack.begin() + o);
+    o += n_ord;
+    std::copy(gfeat.begin(), gfeat.end(), pack.begin() + o);
+    std::copy(gstart.begin(), gstart.end(), pack.begin() + o + n_g);
+    std::copy(gcount.begin(), gcount.end(), pack.begin() + o + 2 * n_g);
+    o += 3 * n_g;
+    std::memcpy(pack.data() + o, uoff.data(), uoff.size() * 8);
     DevBuf<uint32_t> dpack;
     dpack.alloc(pack.size(), s);
     COLO_CUDA(cudaMemcpyAsync(dpack.get(), pack.data(), pack.size() * 4, cudaMemcpyHostToDevice, s));
     const uint32_t* d_need = dpack.get();
     const uint32_t* d_lmem = d_need + n_need;
-    const uint32_t* d_dmask = d_lmem + n_lmem;
-    const uint32_t* d_dcount = d_dmask + n_dm;
-    const uint32_t* d_dstart = d_dcount + b.F;
-    const uint32_t* d_order = d_dstart + b.F;
+    const uint32_t* d_order = d_lmem + n_lmem;
+    const uint32_t* d_gfeat = d_order + n_ord;
+    const uint32_t* d_gstart = d_gfeat + n_g;
+    const uint32_t* d_gcount = d_gstart + n_g;
+    const uint64_t* d_uoff = reinterpret_cast<const uint64_t*>(d_gcount + n_g);
     // block-private sums when the level's counters fit in 64 KB of shared memory
     const uint64_t acc64 = ncand * (uint64_t)(m + 2);
     const uint32_t acc_n = acc64 <= kAccMax ? (uint32_t)acc64 : 0u;
     const size_t smem = (size_t)acc_n * 4;
-    // a grid-stride loop over 32-cell chunks: as many blocks as fit at once
+    // a grid-stride loop over units (one warp each): as many blocks as fit at once
     auto grid = [&](const void* fn) {
         if (smem > 48 * 1024)
             COLO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
         COLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem));
         const uint64_t cap = (uint64_t)b.sms * (uint64_t)(per_sm > 0 ? per_sm : 1);
-        const uint64_t want = (b.M + 255) / 256;
+        const uint64_t want = (nunits + 7) / 8;
         return (unsigned)(want < cap ? want : cap);
     };
     KScope ks("filter_level");
-#define COLO_FL(WW)                                                                                          \
-    k_filter_cells<WW><<<grid((const void*)k_filter_cells<WW>), 256, smem, s>>>(                            \
-        b.M, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), b.nbmask.get(), d_dmask, d_dcount, d_dstart, d_order,   \
-        d_need, d_lmem,                                                                                              \
-        k, b.qmask.get(), b.cmask.get(), b.crun.get(), b.qfirst.get(), b.rcnt.get(), d_ub, d_stats, acc_n)
-    switch (b.W) {
-        case 1: COLO_FL(1); break;
-        case 2: COLO_FL(2); break;
-        case 3: COLO_FL(3); break;
-        case 4: COLO_FL(4); break;
-        case 5: COLO_FL(5); break;
-        case 6: COLO_FL(6); break;
-        case 7: COLO_FL(7); break;
-        case 8: COLO_FL(8); break;
-        case 12: COLO_FL(12); break;
-        case 16: COLO_FL(16); break;
-        case 24: COLO_FL(24); break;
-        case 32: COLO_FL(32); break;
-        default: throw StatusError{COLO_ERR_INTERNAL, "mask words not padded to a supported width"};
-    }
+#define COLO_FL(WW)                                                                                             \
+    k_filter_drv<WW><<<grid((const void*)k_filter_drv<WW>), 256, smem, s>>>(                                    \
+        nunits, ngroups, d_uoff, d_gfeat, d_gstart, d_gcount, b.doff.get(), b.dlist.get(), d_order, d_need,       \
+        d_lmem, k, b.qmask.get(), b.cmask.get(), b.crun.get(), b.qfirst.get(), b.rcnt.get(), d_ub, d_stats, acc_n)
+    COLO_W_SWITCH(b.W, COLO_FL)
 #undef COLO_FL
     COLO_LAUNCH_CHECK();
     count_launch();

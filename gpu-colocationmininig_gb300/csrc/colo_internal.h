@@ -291,9 +291,15 @@ RadixPlan radix_plan(int bits);
 // caller while it wrote the keys; the sort then skips its own count.
 // err_dev, when given, receives the timeout flag of a look-back wait (the
 // caller checks it at its next wait); otherwise the sort waits and throws.
+// test_spin != 0 (tests of the timeout path only): the look-back gives up
+// after test_spin polls, and in the first pass tile 0 withholds its counts,
+// so tile 1's wait runs out; every wait stays bounded and the sort ends with
+// the timeout flag set (its output is discarded by the caller).
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr);
+                const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr,
+                uint32_t test_spin = 0);
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr);
+                const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr,
+                uint32_t test_spin = 0);
 
 }  // namespace colo

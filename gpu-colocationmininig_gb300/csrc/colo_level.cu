@@ -15,6 +15,14 @@
 // per item (load-balanced expand).  Hits are compacted with one ballot per
 // step; output rows are written column-major (one coalesced stream per
 // column).  Participation bits are set with atomicOr on 32-bit words.
+//
+// The single pass (presized tables, COLO_MODE_LEARNED) writes rows in the
+// same order as count + fill: a warp takes its chunk by ticket (chunks of
+// warps already running come first), counts its hits, publishes the count,
+// and looks back over the candidate's earlier chunks (decoupled look-back,
+// every wait bounded) for the rows before it; it then writes its rows at
+// their exact offsets, replaying the ballots it kept (steps beyond the kept
+// ones are evaluated again).
 #include "colo_batch.h"
 #include "colo_device.cuh"
 
@@ -26,6 +34,11 @@ enum { MODE_COUNT = 0, MODE_FILL = 1, MODE_SINGLE = 2 };
 __device__ __forceinline__ void set_bit(uint32_t* words, uint32_t bit) {
     atomicOr(&words[bit >> 5], 1u << (bit & 31));
 }
+
+constexpr unsigned long long kChunkA = 1ull << 62;   // chunk count published
+constexpr unsigned long long kChunkP = 2ull << 62;   // inclusive prefix published
+constexpr unsigned long long kChunkVal = (1ull << 62) - 1;
+constexpr uint32_t kChunkSpin = 1u << 22;
 
 // Word offset of member j's participation bitmap in the level's bitmap arena.
 __device__ __forceinline__ uint64_t bm_offset(const CandDesc& d, uint32_t j, const uint32_t* __restrict__ fcount) {
@@ -43,10 +56,17 @@ __global__ void __launch_bounds__(256) k_level(
     const uint32_t* __restrict__ nb,
     const float2* __restrict__ xy, const uint32_t* __restrict__ fstart,
     const uint32_t* __restrict__ fcount, const JobGrid* __restrict__ grids,
-    uint32_t* __restrict__ overflow, unsigned long long* __restrict__ items) {
+    uint32_t* __restrict__ overflow, unsigned long long* __restrict__ items,
+    unsigned long long* __restrict__ chunk_status, unsigned long long* __restrict__ ticket,
+    uint32_t* __restrict__ timeout) {
     constexpr int KR = (K == 0) ? 1 : K;   // register members kept for K > 0
     const int lane = threadIdx.x & 31;
-    const uint64_t ch = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t ch = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (MODE == MODE_SINGLE) {   // chunks in the order warps start
+        unsigned long long tk = 0;
+        if (lane == 0) tk = atomicAdd(ticket, 1ull);
+        ch = __shfl_sync(0xffffffffu, tk, 0);
+    }
     if (ch >= nchunks) return;
     // candidate of this chunk
     uint64_t lo = 0, hi = ncand;
@@ -108,105 +128,166 @@ __global__ void __launch_bounds__(256) k_level(
     if (MODE == MODE_FILL && valid) out0 = d.offs[row] - d.offs[0];   // offsets may be a slice of a longer scan
     const uint32_t lt = (1u << lane) - 1u;
     bool ovf = false;
+    const uint64_t chunk_row0 = (ch - chunk_off[lo]) * 32;
 
-    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+    // item t0 + lane: its owner row (lane j), the row's first item and slice, and whether b
+    // extends the row (the other k-2 members within R)
+    struct Item {
+        int j;
+        uint32_t ex_j, in_j, b;
+        bool active;
+    };
+    auto locate = [&](uint32_t t0) {
+        Item it;
         const uint32_t item = t0 + lane;
-        const bool active = item < total;
-        // owner lane: last lane whose slice starts at or before item
+        it.active = item < total;
         int j = 0;
 #pragma unroll
         for (int bstep = 16; bstep > 0; bstep >>= 1) {
             uint32_t ev = __shfl_sync(0xffffffffu, excl, j + bstep);
             if (ev <= item) j += bstep;
         }
-        const uint32_t ex_j = __shfl_sync(0xffffffffu, excl, j);
-        const uint32_t in_j = __shfl_sync(0xffffffffu, incl, j);
+        it.j = j;
+        it.ex_j = __shfl_sync(0xffffffffu, excl, j);
+        it.in_j = __shfl_sync(0xffffffffu, incl, j);
         const uint64_t lo_j = __shfl_sync(0xffffffffu, slo, j);
-        uint32_t b = 0;
-        bool ok = active;
-        if (active) b = nb[lo_j + (item - ex_j)];
+        it.b = it.active ? nb[lo_j + (item - it.ex_j)] : 0u;
+        return it;
+    };
+    auto extends = [&](const Item& it) {
+        bool ok = it.active;
         if (K == 0) {
-            if (active && k > 2) {
-                const float2 pb = xy[b];
-                const float xb = pb.x, yb = pb.y;
-                const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
+            if (it.active && k > 2) {
+                const float2 pb = xy[it.b];
+                const uint64_t prow_j = chunk_row0 + (uint64_t)it.j;
                 for (uint32_t i = 1; i + 1 < k && ok; ++i) {
                     uint32_t ri = d.parent[(uint64_t)i * d.pstride + prow_j];
                     const float2 pr = xy[ri];
-                    ok = ref_within(pr.x, pr.y, xb, yb, R2, hu);
+                    ok = ref_within(pr.x, pr.y, pb.x, pb.y, R2, hu);
                 }
             }
         } else if (K > 2) {
             float xb = 0.f, yb = 0.f;
-            if (active) {
-                const float2 pb = xy[b];
+            if (it.active) {
+                const float2 pb = xy[it.b];
                 xb = pb.x;
                 yb = pb.y;
             }
 #pragma unroll
             for (int i = 1; i < KR - 1; ++i) {
-                float xi = __shfl_sync(0xffffffffu, rx[i], j);
-                float yi = __shfl_sync(0xffffffffu, ry[i], j);
+                float xi = __shfl_sync(0xffffffffu, rx[i], it.j);
+                float yi = __shfl_sync(0xffffffffu, ry[i], it.j);
                 ok = ok && ref_within(xi, yi, xb, yb, R2, hu);
             }
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, ok);
-        // lanes of this step that belong to my own row
+        return ok;
+    };
+    // lanes of step t0 that belong to my own row
+    auto own_mask = [&](uint32_t t0) {
         int r0 = (int)excl - (int)t0, r1 = (int)incl - (int)t0;
         r0 = r0 < 0 ? 0 : r0;
         r1 = r1 > 32 ? 32 : r1;
-        uint32_t mymask = 0;
-        if (r1 > r0) mymask = (r1 - r0 == 32) ? 0xffffffffu : (((1u << (r1 - r0)) - 1u) << r0);
-        const uint32_t my_hits = __popc(bal & mymask);
-
-        if (MODE == MODE_COUNT || MODE == MODE_SINGLE) {
-            if (ok) set_bit(d.bitmap + bm_last, b - last_start);
-        }
-        if (MODE == MODE_FILL) {
-            const uint32_t before_j = __shfl_sync(0xffffffffu, mine, j);
-            const uint64_t out_j = __shfl_sync(0xffffffffu, out0, j);
-            int q0 = (int)ex_j - (int)t0, q1 = (int)in_j - (int)t0;
-            q0 = q0 < 0 ? 0 : q0;
-            q1 = q1 > 32 ? 32 : q1;
-            uint32_t jmask = (q1 > q0) ? ((q1 - q0 == 32) ? 0xffffffffu : (((1u << (q1 - q0)) - 1u) << q0)) : 0u;
-            const uint64_t pos = out_j + before_j + __popc(bal & jmask & lt);
-            if (K > 0) {
+        return (r1 > r0) ? ((r1 - r0 == 32) ? 0xffffffffu : (((1u << (r1 - r0)) - 1u) << r0)) : 0u;
+    };
+    // writes the hits of one step: rows of owner j go to out_j + (j's rows written so far)
+    auto write_step = [&](const Item& it, bool ok, uint32_t bal, uint32_t t0, uint64_t col_stride, bool capped) {
+        const uint32_t before_j = __shfl_sync(0xffffffffu, mine, it.j);
+        const uint64_t out_j = __shfl_sync(0xffffffffu, out0, it.j);
+        int q0 = (int)it.ex_j - (int)t0, q1 = (int)it.in_j - (int)t0;
+        q0 = q0 < 0 ? 0 : q0;
+        q1 = q1 > 32 ? 32 : q1;
+        const uint32_t jmask = (q1 > q0) ? ((q1 - q0 == 32) ? 0xffffffffu : (((1u << (q1 - q0)) - 1u) << q0)) : 0u;
+        const uint64_t pos = out_j + before_j + __popc(bal & jmask & lt);
+        const bool room = !capped || pos < d.out_cap;
+        if (ok && !room) ovf = true;
+        const bool wr = ok && room;
+        if (K > 0) {
 #pragma unroll
-                for (int i = 0; i < KR - 1; ++i) {
-                    uint32_t v = __shfl_sync(0xffffffffu, rid[i], j);
-                    if (ok) d.out[(uint64_t)i * d.out_rows + pos] = v;
-                }
-            } else if (ok) {
-                const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
-                d.out[pos] = d.parent ? d.parent[prow_j] : fstart[d.m[0]] + (uint32_t)prow_j;
-                for (uint32_t i = 1; i + 1 < k; ++i)
-                    d.out[(uint64_t)i * d.out_rows + pos] = d.parent[(uint64_t)i * d.pstride + prow_j];
+            for (int i = 0; i < KR - 1; ++i) {
+                uint32_t v = __shfl_sync(0xffffffffu, rid[i], it.j);
+                if (wr) d.out[(uint64_t)i * col_stride + pos] = v;
             }
-            if (ok) d.out[(uint64_t)(k - 1) * d.out_rows + pos] = b;
+        } else if (wr) {
+            const uint64_t prow_j = chunk_row0 + (uint64_t)it.j;
+            d.out[pos] = d.parent ? d.parent[prow_j] : fstart[d.m[0]] + (uint32_t)prow_j;
+            for (uint32_t i = 1; i + 1 < k; ++i)
+                d.out[(uint64_t)i * col_stride + pos] = d.parent[(uint64_t)i * d.pstride + prow_j];
+        }
+        if (wr) d.out[(uint64_t)(k - 1) * col_stride + pos] = it.b;
+    };
+
+    uint32_t bal_lo = 0, bal_hi = 0;   // single pass: ballot of step s kept in lane s % 32 (s < 64)
+    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        const Item it = locate(t0);
+        const bool ok = extends(it);
+        const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+        const uint32_t my_hits = __popc(bal & own_mask(t0));
+        if (MODE == MODE_COUNT || MODE == MODE_SINGLE) {
+            if (ok) set_bit(d.bitmap + bm_last, it.b - last_start);
         }
         if (MODE == MODE_SINGLE) {
-            const uint32_t n_ok = __popc(bal);
-            unsigned long long base = 0;
-            if (lane == 0 && n_ok) base = atomicAdd(d.cursor, (unsigned long long)n_ok);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            const uint64_t pos = base + __popc(bal & lt);
-            const bool room = pos < d.out_cap;
-            if (ok && !room) ovf = true;
-            if (K > 0) {
-#pragma unroll
-                for (int i = 0; i < KR - 1; ++i) {
-                    uint32_t v = __shfl_sync(0xffffffffu, rid[i], j);
-                    if (ok && room) d.out[(uint64_t)i * d.out_cap + pos] = v;
-                }
-            } else if (ok && room) {
-                const uint64_t prow_j = ((ch - chunk_off[lo]) * 32 + j);
-                d.out[pos] = d.parent ? d.parent[prow_j] : fstart[d.m[0]] + (uint32_t)prow_j;
-                for (uint32_t i = 1; i + 1 < k; ++i)
-                    d.out[(uint64_t)i * d.out_cap + pos] = d.parent[(uint64_t)i * d.pstride + prow_j];
-            }
-            if (ok && room) d.out[(uint64_t)(k - 1) * d.out_cap + pos] = b;
+            const uint32_t step = t0 >> 5;
+            if (step < 32 && lane == (int)step) bal_lo = bal;
+            else if (step >= 32 && step < 64 && lane == (int)(step - 32)) bal_hi = bal;
         }
+        if (MODE == MODE_FILL) write_step(it, ok, bal, t0, d.out_rows, false);
         mine += my_hits;
+    }
+    if (MODE == MODE_SINGLE) {
+        // the chunk's rows, then the rows of the candidate's earlier chunks
+        const uint32_t wsum = __reduce_add_sync(0xffffffffu, mine);
+        unsigned long long prefix = 0;
+        if (lane == 0) {
+            volatile unsigned long long* st = chunk_status + ch;
+            if (chunk_off[lo] == ch) {
+                *st = kChunkP | wsum;
+            } else {
+                *st = kChunkA | wsum;
+                uint32_t spins = 0;
+                for (uint64_t t = ch - 1;;) {
+                    const unsigned long long v = *(volatile const unsigned long long*)(chunk_status + t);
+                    const unsigned long long flag = v & ~kChunkVal;
+                    if (flag == 0) {
+                        if (++spins > kChunkSpin) {   // give up: report it and write with what we have
+                            atomicOr(timeout, 1u);
+                            break;
+                        }
+                        __nanosleep(64);
+                        continue;
+                    }
+                    prefix += v & kChunkVal;
+                    if (flag == kChunkP) break;
+                    --t;
+                }
+                *st = kChunkP | (prefix + wsum);
+            }
+        }
+        prefix = __shfl_sync(0xffffffffu, prefix, 0);
+        // my row's first output row: the chunk's prefix plus the rows of the chunk's earlier rows
+        uint32_t rincl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, rincl, o);
+            if (lane >= o) rincl += t;
+        }
+        const uint32_t slots = mine;
+        out0 = prefix + (rincl - mine);
+        mine = 0;
+        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+            const Item it = locate(t0);
+            const uint32_t step = t0 >> 5;
+            bool ok;
+            if (step < 64) {
+                const uint32_t kept = __shfl_sync(0xffffffffu, step < 32 ? bal_lo : bal_hi, (int)(step & 31));
+                ok = it.active && ((kept >> lane) & 1u);
+            } else {
+                ok = extends(it);
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+            write_step(it, ok, bal, t0, d.out_cap, true);
+            mine += __popc(bal & own_mask(t0));
+        }
+        mine = slots;
     }
     if (MODE == MODE_SINGLE) {
         if (__any_sync(0xffffffffu, ovf) && lane == 0) atomicOr(&overflow[lo], 1u);
@@ -297,7 +378,8 @@ void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
 #define COLO_LVL(KK)                                                                              \
     k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_beg.get(), b.nb_cnt.get(), \
                                             b.nb.get(), b.xy.get(), b.fstart.get(), b.fcount.get(),  \
-                                            b.grids.get(), ovf, w.items)
+                                            b.grids.get(), ovf, w.items, w.chunk_status, w.ticket,    \
+                                            &b.flags.get()->timeout)
     switch (k) {
         case 2: COLO_LVL(2); break;
         case 3: COLO_LVL(3); break;

@@ -299,21 +299,22 @@ struct ArenaSpan {
 };
 
 // The refinement's per-level device buffers, carved from one stream-ordered
-// allocation with the zero-initialised ones (bitmap, rows, cursor, overflow)
+// allocation with the zero-initialised ones (bitmap, rows, chunk status, overflow)
 // adjacent, so that a level costs one allocation, one clear and one free
 // instead of nine, four and nine.  Parts start on 256-byte boundaries.
 struct LevelArena {
     DevBuf<unsigned char> mem;
     ArenaSpan<uint32_t> bitmap;
     ArenaSpan<unsigned long long> rows;
-    ArenaSpan<unsigned long long> cursor;   // single pass: rows reserved per candidate
+    ArenaSpan<unsigned long long> status;   // single pass: per chunk look-back word, then the chunk ticket
     ArenaSpan<uint32_t> overflow;           // single pass: 1 when the table outgrew its capacity
     ArenaSpan<uint32_t> slots;
     ArenaSpan<CandDesc> descs;
     ArenaSpan<uint64_t> chunk_off;
     ArenaSpan<uint64_t> stats;
 
-    void init(uint64_t nslots, uint64_t nwords, uint64_t ncand, uint32_t k, bool single, cudaStream_t s) {
+    void init(uint64_t nslots, uint64_t nwords, uint64_t ncand, uint64_t nchunks, uint32_t k, bool single,
+              cudaStream_t s) {
         size_t off = 0;
         auto take = [&](uint64_t bytes) {
             const size_t o = off;
@@ -322,7 +323,7 @@ struct LevelArena {
         };
         const size_t o_bitmap = take(std::max<uint64_t>(nwords, 1) * 4);
         const size_t o_rows = take(std::max<uint64_t>(ncand, 1) * 8);
-        const size_t o_cursor = single ? take(ncand * 8) : 0;
+        const size_t o_status = single ? take((nchunks + 1) * 8) : 0;
         const size_t o_overflow = single ? take(ncand * 4) : 0;
         const size_t zeroed = off;
         const size_t o_slots = take(std::max<uint64_t>(nslots, 1) * 4);
@@ -333,7 +334,7 @@ struct LevelArena {
         unsigned char* b = mem.get();
         bitmap.p = reinterpret_cast<uint32_t*>(b + o_bitmap);
         rows.p = reinterpret_cast<unsigned long long*>(b + o_rows);
-        cursor.p = single ? reinterpret_cast<unsigned long long*>(b + o_cursor) : nullptr;
+        status.p = single ? reinterpret_cast<unsigned long long*>(b + o_status) : nullptr;
         overflow.p = single ? reinterpret_cast<uint32_t*>(b + o_overflow) : nullptr;
         slots.p = reinterpret_cast<uint32_t*>(b + o_slots);
         descs.p = reinterpret_cast<CandDesc*>(b + o_descs);
@@ -362,6 +363,7 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     b.sms = ctx->sms;
     b.J = J;
     if (ctx->join_group) b.join_group = ctx->join_group;
+    b.test_spin = pv[0].reserved[1] > 0 ? (uint32_t)pv[0].reserved[1] : 0u;
     auto t0 = Clock::now();
     std::vector<uint32_t> job_f0(J + 1, 0);
     uint64_t N = 0;
@@ -795,7 +797,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             slot_base.swap(sb2);
         }
         LevelArena ar;
-        ar.init(nslots, nwords, ncand, k, learned, s);
+        ar.init(nslots, nwords, ncand, chunk_off.back(), k, learned, s);
         std::unique_ptr<TableBuf> single_cur;
         uint64_t single_words = 0;
         if (learned) {
@@ -812,12 +814,11 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 hd[q].out = single_cur->get() + o;
                 hd[q].out_cap = cap[q];
                 hd[q].out_rows = cap[q];
-                hd[q].cursor = ar.cursor.get() + q;
                 o += cap[q] * k;
             }
         }
         std::vector<uint64_t> hstats(ncand * k * 4);
-        Readback rb(ctx, s, hstats.size() * 8 + ncand * 8 + ncand * 4 + 8);
+        Readback rb(ctx, s, hstats.size() * 8 + ncand * 8 + ncand * 4 + 8 + sizeof(DevFlags));
         d_items.zero(s);
         cnt_refined += ncand;
         cnt_bmw += nwords;
@@ -845,6 +846,10 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
             } else {
                 LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), d_items.get()};
+                if (learned) {
+                    w.chunk_status = ar.status.get();
+                    w.ticket = ar.status.get() + chunk_off.back();
+                }
                 if (learned) level_single(b, w, k, ar.overflow.get());
                 else level_count(b, w, k);
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
@@ -856,9 +861,15 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         std::vector<uint32_t> hovf(ncand, 0);
         unsigned long long h_items = 0;
         if (ncand) rb.copy(hrows.data(), ar.rows.get(), ncand * 8);
-        if (learned) rb.copy(hovf.data(), ar.overflow.get(), ncand * 4);
+        DevFlags hflags{};
+        if (learned) {
+            rb.copy(hovf.data(), ar.overflow.get(), ncand * 4);
+            rb.copy(&hflags, b.flags.get(), sizeof(hflags));
+        }
         rb.copy(&h_items, d_items.get(), 8);
         rb.finish();
+        if (hflags.timeout)
+            throw StatusError{COLO_ERR_TIMEOUT, "single-pass tables: a chunk waited too long for its predecessors"};
         // participation index (getParticipationIndex, Codes/DeviceProcess.cu:108-132)
         std::vector<uint8_t> prev_flag(ncand, 0);
         for (uint64_t q = 0; q < ncand; ++q) {

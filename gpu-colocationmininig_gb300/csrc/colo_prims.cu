@@ -249,7 +249,8 @@ template <class KT, int RB, int kSortRounds = SortShape<KT>::rounds>
 __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_onesweep(
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
     uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
-    unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err, int bulk) {
+    unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err, int bulk,
+    uint32_t spin_limit, int withhold) {
     constexpr int R = 1 << RB;
     constexpr int kSortTile = kSortThreads * kSortRounds;
     constexpr int D = R / kSortThreads;             // digits per thread in the look-back (1 or 2)
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
             volatile unsigned long long* st = status + (uint64_t)tile * R + d;
             unsigned long long prefix = 0;
             if (tile == 0) {
-                *st = kFlagP | cnt[i];
+                if (!withhold) *st = kFlagP | cnt[i];   // withhold: a test of the bounded wait below
             } else {
                 *st = kFlagA | cnt[i];
                 uint32_t spins = 0;
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
                     const unsigned long long v = *(volatile const unsigned long long*)(status + (uint64_t)t * R + d);
                     const unsigned long long flag = v & ~kValMask;
                     if (flag == 0) {
-                        if (++spins > kSpinLimit) {
+                        if (++spins > spin_limit) {
                             atomicOr(err, 1u);
                             break;
                         }
@@ -440,7 +441,7 @@ namespace {
 
 template <class KT>
 void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                     const char* name, unsigned long long* hist_in, uint32_t* err_dev) {
+                     const char* name, unsigned long long* hist_in, uint32_t* err_dev, uint32_t test_spin) {
     if (n <= 1 || bits <= 0) return;
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
     const RadixPlan plan = radix_plan(bits);
@@ -491,7 +492,9 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         const int bulk = ((uintptr_t)ka % 16 == 0 && (uintptr_t)va % 16 == 0) ? 1 : 0;
         k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
                                                                      hist + p * kMaxRadix, status.get(),
-                                                                     tickets.get() + p, errp, bulk);
+                                                                     tickets.get() + p, errp, bulk,
+                                                                     test_spin ? test_spin : kSpinLimit,
+                                                                     test_spin && p == 0 ? 1 : 0);
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);
@@ -524,13 +527,13 @@ RadixPlan radix_plan(int bits) {
 }
 
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name, unsigned long long* hist, uint32_t* err_dev) {
-    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist, err_dev);
+                const char* name, unsigned long long* hist, uint32_t* err_dev, uint32_t test_spin) {
+    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist, err_dev, test_spin);
 }
 
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name, unsigned long long* hist, uint32_t* err_dev) {
-    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist, err_dev);
+                const char* name, unsigned long long* hist, uint32_t* err_dev, uint32_t test_spin) {
+    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist, err_dev, test_spin);
 }
 
 }  // namespace colo

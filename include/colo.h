@@ -61,7 +61,12 @@ typedef struct {
                                 (otherwise only for levels with 4096+ prevalent patterns);
                                 bit 3: keep instance tables in pinned host memory mapped
                                 into the device (otherwise only tables whose device
-                                allocation fails go there) */
+                                allocation fails go there);
+                                reserved[1] > 0, tests of the timeout path only: the
+                                bucketing sort's look-back gives up after that many
+                                polls and its first tile withholds its counts, so the
+                                mine fails with COLO_ERR_TIMEOUT (no wait is unbounded;
+                                the context stays usable) */
 } colo_params;
 
 const char* colo_status_string(colo_status s);

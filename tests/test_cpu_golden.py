@@ -34,17 +34,28 @@ def test_golden_cases_cover_the_quirks():
     assert [l["k"] for l in g["levels"]] == [2]
 
 
-SEATTLE = Path("/root/reference/TestCase/Data/Seattle2012.csv")
+SEATTLE = Path(__file__).resolve().parent / "golden" / "seattle2012.csv.gz"
 
 
-@pytest.mark.skipif(not SEATTLE.exists(), reason="the reference's test case is not mounted")
-def test_seattle_experiment_log_counts():
+def _seattle(tmp_path):
+    """The reference's real-data fixture (TestCase/Data/Seattle2012.csv, committed gzipped)."""
+    import gzip
+    import shutil
+
+    p = tmp_path / "Seattle2012.csv"
+    with gzip.open(SEATTLE, "rb") as src, open(p, "wb") as dst:
+        shutil.copyfileobj(src, dst)
+    return oracle.parse_csv(str(p))
+
+
+@pytest.mark.parametrize("fast", [False, True], ids=["literal", "scaled"])
+def test_seattle_experiment_log_counts(tmp_path, fast):
     # TestCase/ExperimentLog/ExperimentLog1.csv:1-2 of the reference logs, for
     # Seattle2012 with PI 0.55 and R 10: "70,83,0.843373" -- 83 candidates in
     # all levels, 70 of them pruned by the filter.
-    x, y, feat, b, names = oracle.parse_csv(str(SEATTLE))
+    x, y, feat, b, names = _seattle(tmp_path)
     assert len(x) == 165458 and len(names) == 13
-    r = oracle.mine(x, y, feat.astype(np.int32), b, 10.0, 0.55)
+    r = oracle.mine(x, y, feat.astype(np.int32), b, 10.0, 0.55, fast=fast)
     total = sum(len(l.cand) for l in r.levels)
     pruned = sum(int((l.passed == 0).sum()) for l in r.levels)
     assert (pruned, total) == (70, 83)

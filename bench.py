@@ -40,6 +40,21 @@ import numpy as np  # noqa: E402
 METRIC = "end-to-end mining s & candidates/s, batched+learned vs plain on 1 GB300, bit-exact PI"
 WORKLOAD = ("config3: 20,000,000 points, 100 features (Zipf s=1.2), 75% in 5,000 hotspots "
             "(sigma log-U[5,500]), 30 planted colocations of size 2-7, R=20, PI 0.15")
+WORKLOADS = {
+    0: "config0: 20,000 points, 10 features x 2,000, planted {0,1},{2,3,4},{5..8}, R=50, PI 0.3, sizes <= 4",
+    1: ("config1: 1,000,000 points, 40 features (Zipf s=1.0), 70% in 500 hotspots (sigma log-U[50,2000]), "
+        "12 planted colocations of size 2-6, R=100, PI 0.2, sizes <= 6"),
+    3: WORKLOAD,
+    4: ("config4: 200 features (Zipf s=1.3), 2% of every feature in sigma=5 dense hotspots, the rest as config3, "
+        "60 planted colocations of size 2-8, R=10, PI 0.1, no size cap"),
+}
+
+
+def workload_name(cfg: int, scale: float, n: int) -> str:
+    w = WORKLOADS.get(cfg, f"config{cfg}")
+    return w if scale == 1.0 else f"{w}; at scale {scale:g} ({n:,} points, same density)"
+
+
 JOBS_WORKLOAD = ("512 independent jobs, 2k-400k points each (log-uniform), 8-32 features, "
                  "R = 3 x mean spacing x U[0.5, 2], PI in {0.1, 0.2, 0.3}")
 PEAKS = ROOT / "MEASURED_PEAKS.json"
@@ -317,6 +332,74 @@ def bench_jobs(args, rank, world, local, dist):
         }), flush=True)
 
 
+def side_configs(ctx, dev, stream, head_mode, steps: int = 3, warmup: int = 1, cpu: bool = True):
+    """The other configurations, each timed in the plain two-pass form and in the headline form on
+    resident points (CUDA events on the library's stream), with the CPU oracle's time beside them:
+    config0 (20,000 points), config1 (1,000,000 points) and config2 (512 independent jobs; batched:
+    one colo_mine_batch call, plain: the jobs mined one at a time).  Fewer steps than the headline
+    line: these are the reported numbers for the configurations the headline does not cover."""
+    import torch
+    import colo
+    import oracle
+    from colo import gen
+
+    def timed(run):
+        for _ in range(warmup):
+            run()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = None
+        for _ in range(steps):
+            res = run()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / steps, res
+
+    out = {}
+    for cfg in (0, 1):
+        wl = gen.config(cfg)
+        ds = colo.Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
+        ds.upload()
+        r = {"workload": f"config{cfg}", "points": wl.n}
+        pats = None
+        same = True
+        for name, mode in (("headline", head_mode), ("plain", colo.MODE_PLAIN)):
+            prm = colo.default_params(wl.R, wl.thr, mode, max_size=wl.max_size)
+            ms, res = timed(lambda: ctx.mine(ds, prm))
+            c = res.num_candidates()
+            r[name] = {"ms_per_step": round(ms, 4), "candidates_per_s": c / (ms / 1e3), "candidates": c}
+            same &= pats is None or res.patterns() == pats
+            pats = res.patterns()
+        r["headline_vs_plain"] = r["plain"]["ms_per_step"] / r["headline"]["ms_per_step"]
+        r["identical_patterns"] = same
+        if cpu:
+            t = time.perf_counter()
+            o = oracle.mine(wl.x, wl.y, wl.fid, wl.bounds, wl.R, wl.thr, max_k=wl.max_size, fast=True)
+            sec = time.perf_counter() - t
+            r["cpu_oracle"] = {"ms_per_step": round(sec * 1e3, 2), "candidates_per_s": o.num_candidates() / sec,
+                               "identical_patterns": o.patterns() == pats}
+        out[f"config{cfg}"] = r
+        del ds
+    jobs = gen.config2_jobs(512)
+    dss = [colo.Dataset.from_arrays(ctx, w.x, w.y, w.fid, w.bounds) for w in jobs]
+    for d in dss:
+        d.upload()
+    hp = [colo.default_params(w.R, w.thr, head_mode, max_size=w.max_size) for w in jobs]
+    pp = [colo.default_params(w.R, w.thr, colo.MODE_PLAIN, max_size=w.max_size) for w in jobs]
+    ms_b, rb = timed(lambda: ctx.mine_batch(dss, hp))
+    ms_p, rp = timed(lambda: [ctx.mine(d, p) for d, p in zip(dss, pp)])
+    cands = sum(x.num_candidates() for x in rb)
+    out["config2"] = {"workload": JOBS_WORKLOAD, "points": int(sum(w.n for w in jobs)), "jobs": len(jobs),
+                      "headline": {"ms_per_step": round(ms_b, 3), "candidates_per_s": cands / (ms_b / 1e3),
+                                   "candidates": cands},
+                      "plain": {"ms_per_step": round(ms_p, 3), "candidates_per_s": cands / (ms_p / 1e3)},
+                      "headline_vs_plain": ms_p / ms_b,
+                      "identical_patterns": all(a.patterns() == b.patterns() for a, b in zip(rb, rp)),
+                      "steps": steps, "warmup": warmup}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -326,6 +409,8 @@ def main():
     ap.add_argument("--config", type=int, default=3)
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the other configurations (config0, config1, config2) reported beside the headline")
     ap.add_argument("--join-group", type=int, default=0,
                     help="pin the join's lanes per anchor instead of autotuning (profiling runs: "
                          "ncu serialises launches and distorts the autotuner's timings)")
@@ -342,7 +427,8 @@ def main():
         if args.config == 2:
             wls, workload = gen.config2_jobs(512, scale=args.scale), JOBS_WORKLOAD
         else:
-            wls, workload = [gen.config(args.config, scale=args.scale)], WORKLOAD
+            wls = [gen.config(args.config, scale=args.scale)]
+            workload = workload_name(args.config, args.scale, wls[0].n)
         value, cores, sample, sec, phases = run_cpu(wls, args.steps, args.warmup)
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": args.gpus,
@@ -470,6 +556,9 @@ def main():
         return
     cpu = None
     io = None
+    side = None
+    if not args.no_side and world == 1 and args.config == 3 and args.scale == 1.0:
+        side = side_configs(ctx, dev, stream, head_mode, cpu=not args.no_cpu)
     if not args.no_cpu and world == 1:
         v, cores, sample, sec, phases = run_cpu([wl], 1, 0)
         cpu = {"value": v, "unit": "candidates/s", "cores": cores, "kind": "port", "sample": sample,
@@ -480,7 +569,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_b / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator; no public dataset exists)",
-        "config": {"workload": WORKLOAD, "points": wl.n, "features": wl.nfeat, "candidates_per_step": cands,
+        "config": {"workload": workload_name(args.config, args.scale, wl.n), "points": wl.n, "features": wl.nfeat,
+                   "candidates_per_step": cands,
                    "join_active_anchors": int(counters["active_anchors"]), "join_pairs": int(counters["join_pairs"]),
                    "neighbor_entries": int(counters["neighbors"]), "cells": int(counters["cells"]),
                    "runs": int(counters["runs"]), "nrl_entries": int(counters["nrl_entries"]),
@@ -509,6 +599,7 @@ def main():
         "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,
         "host_phase_ms": phases,
         "io": io,
+        "side_configs": side,
     }
     print(json.dumps(line), flush=True)
     if dist:

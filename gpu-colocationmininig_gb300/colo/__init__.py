@@ -151,12 +151,13 @@ def load(build: bool = True) -> C.CDLL:
 
 def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHED, max_size: int = 0,
                    keep_tables: bool = False, profile: bool = False, features: bool = False,
-                   device_apriori: bool = False, host_tables: bool = False) -> Params:
+                   device_apriori: bool = False, host_tables: bool = False, single_pass: bool = False) -> Params:
     """Mining parameters; `profile` times every kernel, `features` records the cost-model
     features of every candidate (training data), `device_apriori` generates every level's
     candidates on the device (by default only levels with many prevalent patterns), `host_tables`
     keeps the instance tables in pinned host memory (by default only tables too large for the
-    device)."""
+    device), `single_pass` (COLO_MODE_LEARNED) writes every refined candidate's table while counting
+    it (by default only tables presized at 2^20 rows or more)."""
     p = Params()
     load().colo_params_default(C.byref(p))
     p.distance = distance
@@ -165,7 +166,7 @@ def default_params(distance: float, pi_threshold: float, mode: int = MODE_BATCHE
     p.max_size = max_size
     p.keep_tables = 1 if keep_tables else 0
     p.reserved[0] = ((1 if profile else 0) | (2 if features else 0) | (4 if device_apriori else 0) |
-                     (8 if host_tables else 0))
+                     (8 if host_tables else 0) | (16 if single_pass else 0))
     return p
 
 

@@ -834,7 +834,12 @@ void bucket_points(Batch& b) {
         count_launch();
     }
 
-    // runs per feature (the level filters drive each candidate from its member with the fewest cells)
+    // cells per driver list (3x3 blocks holding each feature)
+    DevBuf<uint32_t> dcnt;
+    dcnt.alloc(b.F ? b.F : 1, s);
+    dcnt.zero(s);
+    driver_lists_count(b, dcnt.get());
+    // runs per feature
     {
         KScope ks("run_index");
         DevBuf<uint32_t> cnt;
@@ -849,11 +854,6 @@ void bucket_points(Batch& b) {
             COLO_LAUNCH_CHECK();
             count_launch();
         }
-        // cells per driver list (3x3 blocks holding each feature)
-        DevBuf<uint32_t> dcnt;
-        dcnt.alloc(b.F ? b.F : 1, s);
-        dcnt.zero(s);
-        driver_lists_count(b, dcnt.get());
         // the run counts, list sizes and error flags come back with one wait
         std::vector<uint32_t> hc(b.F), hd(b.F);
         DevFlags hf;

@@ -30,7 +30,6 @@ namespace colo {
 namespace {
 
 constexpr int kFilterThreads = 256;
-constexpr int kFilterWarps = kFilterThreads / 32;
 constexpr int kMaxW = 32;  // mask words per cell (1024 features per job); rows of 9+ words are padded
                            // to 12, 16, 24 or 32 words when the batch is set up
 constexpr uint64_t kAccMax = 16384;   // block-private level sums (64 KB of shared memory)
@@ -141,10 +140,33 @@ __device__ __forceinline__ void load_row(const uint32_t* __restrict__ p, uint32_
 // ---- driver lists -----------------------------------------------------------
 // Cells per feature f whose 3x3 block holds f (bit f of nbmask): a block-local
 // histogram when the batch has at most kDilHist features, else global atomics.
+// A block owns `per` consecutive cells and its lanes take them from 32
+// far-apart stretches: neighbouring cells share their features, and lanes of
+// one warp adding to the same counter would serialise.
 constexpr uint32_t kDilHist = 4096;
 
+template <int WT, class Fn>
+__device__ __forceinline__ void dil_cells(uint64_t z0, uint64_t z1, const uint32_t* __restrict__ cjob,
+                                          const JobGrid* __restrict__ grids, const uint32_t* __restrict__ nbmask,
+                                          Fn&& fn) {
+    const uint64_t n = z1 > z0 ? z1 - z0 : 0;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint64_t stretch = (n + 31) / 32;   // lane l walks cells z0 + l*stretch + i
+    for (uint64_t i = warp; i < stretch; i += nw) {
+        const uint64_t z = z0 + (uint64_t)lane * stretch + i;
+        if (z >= z1) continue;
+        uint32_t row[WT];
+        load_row<WT>(nbmask + z * WT, row);
+        const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w)
+            for (uint32_t bits = row[w]; bits; bits &= bits - 1)
+                fn(z, f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1));
+    }
+}
+
 template <int WT>
-__global__ void __launch_bounds__(256) k_dil_count(uint64_t M, const uint32_t* __restrict__ cjob,
+__global__ void __launch_bounds__(256) k_dil_count(uint64_t M, uint64_t per, const uint32_t* __restrict__ cjob,
                                                    const JobGrid* __restrict__ grids,
                                                    const uint32_t* __restrict__ nbmask, uint32_t F,
                                                    uint32_t* __restrict__ cnt) {
@@ -153,26 +175,19 @@ __global__ void __launch_bounds__(256) k_dil_count(uint64_t M, const uint32_t* _
     if (local)
         for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    for (uint64_t z = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; z < M; z += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t row[WT];
-        load_row<WT>(nbmask + z * WT, row);
-        const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
-#pragma unroll
-        for (int w = 0; w < WT; ++w)
-            for (uint32_t bits = row[w]; bits; bits &= bits - 1) {
-                const uint32_t f = f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1);
-                if (local) atomicAdd(&h[f], 1u);
-                else atomicAdd(&cnt[f], 1u);
-            }
-    }
+    const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
+    dil_cells<WT>(z0, z1, cjob, grids, nbmask, [&](uint64_t, uint32_t f) {
+        if (local) atomicAdd(&h[f], 1u);
+        else atomicAdd(&cnt[f], 1u);
+    });
     __syncthreads();
     if (local)
         for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
             if (h[i]) atomicAdd(&cnt[i], h[i]);
 }
 
-// Each block owns `per` consecutive cells: it counts its entries per feature,
-// reserves one range per feature in the lists, and writes its cells there.
+// The same cells per block: count per feature, reserve one range per feature
+// in the lists, write the cells there.
 template <int WT>
 __global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, const uint32_t* __restrict__ cjob,
                                                   const JobGrid* __restrict__ grids,
@@ -183,24 +198,14 @@ __global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, cons
     uint32_t* hc = reinterpret_cast<uint32_t*>(hb + F);
     const bool local = F <= kDilHist;
     const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
-    auto each = [&](auto&& fn) {
-        for (uint64_t z = z0 + threadIdx.x; z < z1; z += blockDim.x) {
-            uint32_t row[WT];
-            load_row<WT>(nbmask + z * WT, row);
-            const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
-#pragma unroll
-            for (int w = 0; w < WT; ++w)
-                for (uint32_t bits = row[w]; bits; bits &= bits - 1)
-                    fn(z, f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1));
-        }
-    };
     if (!local) {
-        each([&](uint64_t z, uint32_t f) { dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z; });
+        dil_cells<WT>(z0, z1, cjob, grids, nbmask,
+                      [&](uint64_t z, uint32_t f) { dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z; });
         return;
     }
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) hc[i] = 0;
     __syncthreads();
-    each([&](uint64_t, uint32_t f) { atomicAdd(&hc[f], 1u); });
+    dil_cells<WT>(z0, z1, cjob, grids, nbmask, [&](uint64_t, uint32_t f) { atomicAdd(&hc[f], 1u); });
     __syncthreads();
     for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
         const uint32_t c = hc[f];
@@ -208,7 +213,8 @@ __global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, cons
         hc[f] = 0;
     }
     __syncthreads();
-    each([&](uint64_t z, uint32_t f) { dlist[hb[f] + atomicAdd(&hc[f], 1u)] = (uint32_t)z; });
+    dil_cells<WT>(z0, z1, cjob, grids, nbmask,
+                  [&](uint64_t z, uint32_t f) { dlist[hb[f] + atomicAdd(&hc[f], 1u)] = (uint32_t)z; });
 }
 
 // Level k >= 3 over the driver lists.  Candidates are grouped by driver
@@ -349,10 +355,12 @@ void driver_lists_count(Batch& b, uint32_t* d_cnt) {
     if (b.M == 0 || b.F == 0) return;
     cudaStream_t s = b.s;
     const size_t smem = b.F <= kDilHist ? (size_t)b.F * 4 : 0;
-    const uint64_t blocks = std::min<uint64_t>((b.M + 255) / 256, (uint64_t)b.sms * 4);
+    uint64_t blocks = std::min<uint64_t>((b.M + 255) / 256, (uint64_t)b.sms * 4);
+    const uint64_t per = (b.M + blocks - 1) / blocks;
+    blocks = (b.M + per - 1) / per;
     KScope ks("driver_lists");
-#define COLO_DC(WW)                                                                                        \
-    k_dil_count<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
+#define COLO_DC(WW)                                                                                             \
+    k_dil_count<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
                                                         b.nbmask.get(), b.F, d_cnt)
     COLO_W_SWITCH(b.W, COLO_DC)
 #undef COLO_DC

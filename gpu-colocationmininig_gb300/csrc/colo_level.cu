@@ -40,6 +40,12 @@ constexpr unsigned long long kChunkP = 2ull << 62;   // inclusive prefix publish
 constexpr unsigned long long kChunkVal = (1ull << 62) - 1;
 constexpr uint32_t kChunkSpin = 1u << 22;
 
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // Word offset of member j's participation bitmap in the level's bitmap arena.
 __device__ __forceinline__ uint64_t bm_offset(const CandDesc& d, uint32_t j, const uint32_t* __restrict__ fcount) {
     uint64_t o = d.bm_base;
@@ -234,35 +240,39 @@ __global__ void __launch_bounds__(256) k_level(
         mine += my_hits;
     }
     if (MODE == MODE_SINGLE) {
-        // the chunk's rows, then the rows of the candidate's earlier chunks
+        // the chunk's rows, then the rows of the candidate's earlier chunks: the warp reads 32
+        // predecessors' words at once, back to the nearest published prefix
         const uint32_t wsum = __reduce_add_sync(0xffffffffu, mine);
+        const uint64_t first = chunk_off[lo];
         unsigned long long prefix = 0;
-        if (lane == 0) {
-            volatile unsigned long long* st = chunk_status + ch;
-            if (chunk_off[lo] == ch) {
-                *st = kChunkP | wsum;
-            } else {
-                *st = kChunkA | wsum;
-                uint32_t spins = 0;
-                for (uint64_t t = ch - 1;;) {
-                    const unsigned long long v = *(volatile const unsigned long long*)(chunk_status + t);
-                    const unsigned long long flag = v & ~kChunkVal;
-                    if (flag == 0) {
-                        if (++spins > kChunkSpin) {   // give up: report it and write with what we have
-                            atomicOr(timeout, 1u);
-                            break;
-                        }
-                        __nanosleep(64);
-                        continue;
+        if (lane == 0) *(volatile unsigned long long*)(chunk_status + ch) = (first == ch ? kChunkP : kChunkA) | wsum;
+        if (first != ch) {
+            uint32_t spins = 0;
+            int64_t base = (int64_t)ch - 1;
+            while (true) {
+                const int64_t t = base - lane;
+                // words before the candidate's first chunk read as an empty published prefix
+                const unsigned long long v =
+                    t >= (int64_t)first ? *(volatile const unsigned long long*)(chunk_status + t) : kChunkP;
+                const unsigned long long flag = v & ~kChunkVal;
+                const uint32_t pm = __ballot_sync(0xffffffffu, flag == kChunkP);
+                const uint32_t zm = __ballot_sync(0xffffffffu, flag == 0);
+                const int fp = pm ? __ffs(pm) - 1 : 32;                 // nearest published prefix
+                const uint32_t upto = fp == 32 ? 0xffffffffu : ((2u << fp) - 1u);
+                if (zm & upto) {                                         // a chunk before it not counted yet
+                    if (++spins > kChunkSpin) {                          // give up: report it, write with what we have
+                        if (lane == 0) atomicOr(timeout, 1u);
+                        break;
                     }
-                    prefix += v & kChunkVal;
-                    if (flag == kChunkP) break;
-                    --t;
+                    __nanosleep(64);
+                    continue;
                 }
-                *st = kChunkP | (prefix + wsum);
+                prefix += warp_sum_u64(((upto >> lane) & 1u) ? (v & kChunkVal) : 0ull);
+                if (fp < 32) break;
+                base -= 32;
             }
+            if (lane == 0) *(volatile unsigned long long*)(chunk_status + ch) = kChunkP | (prefix + wsum);
         }
-        prefix = __shfl_sync(0xffffffffu, prefix, 0);
         // my row's first output row: the chunk's prefix plus the rows of the chunk's earlier rows
         uint32_t rincl = mine;
 #pragma unroll

@@ -328,7 +328,7 @@ struct LevelArena {
         const size_t zeroed = off;
         const size_t o_slots = take(std::max<uint64_t>(nslots, 1) * 4);
         const size_t o_descs = take(std::max<uint64_t>(ncand, 1) * sizeof(CandDesc));
-        const size_t o_chunk = take((ncand + 1) * 8);
+        const size_t o_chunk = take((ncand + 2) * 8);
         const size_t o_stats = take((ncand * k * 4 + 1) * 8);
         mem.alloc(off, s);
         unsigned char* b = mem.get();
@@ -343,6 +343,10 @@ struct LevelArena {
         COLO_CUDA(cudaMemsetAsync(b, 0, zeroed, s));
     }
 };
+
+// Tables presized at fewer rows than this are counted and, when needed, filled
+// after the next level's candidates are known instead of written while counted.
+constexpr uint64_t kSinglePassMinRows = 1u << 20;
 
 // Capacity of a presized single-pass table from the predicted log1p(rows).
 uint64_t presize_rows(float pred) {
@@ -796,12 +800,29 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             owner.swap(own2);
             slot_base.swap(sb2);
         }
+        // the single pass writes a table while counting it; it pays for tables predicted large
+        // (a fill pass would walk them again), small ones are counted and the needed ones filled
+        // after the next level's candidates are known.  Candidates [0, ns) take the single pass.
+        uint64_t ns = 0;
+        if (learned) {
+            bool force = false;
+            for (uint32_t j = 0; j < J; ++j) force |= (pv[j].reserved[0] & 16) != 0;
+            while (ns < ncand && (force || cap[ns] >= kSinglePassMinRows)) ++ns;
+        }
+        // chunk prefixes of the two groups, each from 0: [0, ns] then [ns, ncand]
+        std::vector<uint64_t> chunk_all(1, 0);
+        for (uint64_t q = 0; q < ncand; ++q) {
+            if (q == ns) chunk_all.push_back(0);
+            chunk_all.push_back(chunk_all.back() + (hd[q].prow + 31) / 32);
+        }
+        if (ns == ncand) chunk_all.push_back(0);
+        const uint64_t nch_single = chunk_all[ns], nch_count = chunk_all.back();
         LevelArena ar;
-        ar.init(nslots, nwords, ncand, chunk_off.back(), k, learned, s);
+        ar.init(nslots, nwords, ncand, nch_single, k, ns > 0, s);
         std::unique_ptr<TableBuf> single_cur;
         uint64_t single_words = 0;
-        if (learned) {
-            for (uint64_t q = 0; q < ncand; ++q) single_words += cap[q] * k;
+        if (ns) {
+            for (uint64_t q = 0; q < ns; ++q) single_words += cap[q] * k;
             single_cur.reset(new TableBuf());
             single_cur->alloc(single_words ? single_words : 1, s, host_tables);
             if (single_cur->on_host()) cnt_host_table_bytes += single_words * 4;
@@ -810,7 +831,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             hd[q].slots = ar.slots.get() + slot_base[q];
             hd[q].bitmap = ar.bitmap.get();
             hd[q].rows = ar.rows.get() + q;
-            if (learned) {
+            if (q < ns) {
                 hd[q].out = single_cur->get() + o;
                 hd[q].out_cap = cap[q];
                 hd[q].out_rows = cap[q];
@@ -825,7 +846,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         for (uint64_t q = 0; q < ncand; ++q) cnt_parent += (uint64_t)(k - 1) * hd[q].prow;
         if (ncand) {
             COLO_CUDA(cudaMemcpyAsync(ar.descs.get(), hd.data(), ncand * sizeof(CandDesc), cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(ar.chunk_off.get(), chunk_off.data(), (ncand + 1) * 8, cudaMemcpyHostToDevice, s));
+            COLO_CUDA(cudaMemcpyAsync(ar.chunk_off.get(), chunk_all.data(), (ncand + 2) * 8, cudaMemcpyHostToDevice, s));
             if (plain) {
                 // per candidate, as the reference refines (one candidate at a time)
                 DevBuf<uint64_t> one_off;
@@ -845,13 +866,16 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
             } else {
-                LevelWork w{ar.descs.get(), ar.chunk_off.get(), ncand, chunk_off.back(), d_items.get()};
-                if (learned) {
+                if (ns) {
+                    LevelWork w{ar.descs.get(), ar.chunk_off.get(), ns, nch_single, d_items.get()};
                     w.chunk_status = ar.status.get();
-                    w.ticket = ar.status.get() + chunk_off.back();
+                    w.ticket = ar.status.get() + nch_single;
+                    level_single(b, w, k, ar.overflow.get());
                 }
-                if (learned) level_single(b, w, k, ar.overflow.get());
-                else level_count(b, w, k);
+                if (ns < ncand) {
+                    LevelWork w{ar.descs.get() + ns, ar.chunk_off.get() + ns + 1, ncand - ns, nch_count, d_items.get()};
+                    level_count(b, w, k);
+                }
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
                 rb.copy(hstats.data(), ar.stats.get(), hstats.size() * 8);
             }
@@ -862,8 +886,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         unsigned long long h_items = 0;
         if (ncand) rb.copy(hrows.data(), ar.rows.get(), ncand * 8);
         DevFlags hflags{};
-        if (learned) {
-            rb.copy(hovf.data(), ar.overflow.get(), ncand * 4);
+        if (ns) {
+            rb.copy(hovf.data(), ar.overflow.get(), ns * 4);
             rb.copy(&hflags, b.flags.get(), sizeof(hflags));
         }
         rb.copy(&h_items, d_items.get(), 8);
@@ -900,10 +924,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             prev_flag[q] = L.prevalent[c];
         }
         // row counts (per-candidate counters of the count pass) and fill offsets
-        if (learned) {
-            cnt_single += ncand;
-            for (uint64_t q = 0; q < ncand; ++q) cnt_single_ovf += hovf[q] ? 1 : 0;
-        }
+        cnt_single += ns;
+        for (uint64_t q = 0; q < ns; ++q) cnt_single_ovf += hovf[q] ? 1 : 0;
         cnt_items += h_items;
         cnt_d2h += ncand * 8 + hstats.size() * 8;
         std::vector<uint64_t> gb(ncand + 1, 0);
@@ -968,15 +990,14 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         for (uint64_t q = 0; q < ncand; ++q) {
             if (!prev_flag[q]) continue;
             if (!needed[owner[q].first][owner[q].second]) continue;
-            if (learned && !hovf[q]) {
+            if (q < ns && !hovf[q]) {
                 keepq.push_back(q);
                 continue;
             }
             fillq.push_back(q);
             total_rows += gb[q + 1] - gb[q];
         }
-        if (learned)   // rows the single pass wrote (tables that fit their presize)
-            for (uint64_t q = 0; q < ncand; ++q)
+        for (uint64_t q = 0; q < ns; ++q)   // rows the single pass wrote (tables that fit their presize)
                 if (!hovf[q]) {
                     rows_written += gb[q + 1] - gb[q];
                     cnt_fillw += (gb[q + 1] - gb[q]) * k;

@@ -62,6 +62,9 @@ typedef struct {
                                 bit 3: keep instance tables in pinned host memory mapped
                                 into the device (otherwise only tables whose device
                                 allocation fails go there);
+                                bit 4 (COLO_MODE_LEARNED): write every refined
+                                candidate's table in the counting pass (otherwise only
+                                tables presized at 2^20 rows or more);
                                 reserved[1] > 0, tests of the timeout path only: the
                                 bucketing sort's look-back gives up after that many
                                 polls and its first tile withholds its counts, so the

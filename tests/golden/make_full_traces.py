@@ -4,7 +4,9 @@ own workloads, for the GPU test tests/test_gpu_fulltrace.py.
     python tests/golden/make_full_traces.py [case ...]
 
 Cases: config3 (20,000,000 points, the workload bench.py times), config1
-(1,000,000 points) and the reference's real-data fixture Seattle2012
+(1,000,000 points), config4 at scale 0.005 (500,000 points with the dense
+sigma = 5 hotspot at full density: levels up to 8, 2.8e9 rows in all) and the
+reference's real-data fixture Seattle2012
 (seattle2012.csv.gz beside this script, copied from the reference's
 TestCase/Data/) at R = 10 with PI 0.3 (its parameter.txt) and 0.55 (its
 experiment log).  The trace is the scaled oracle's (oracle_mine_fast, equal
@@ -39,8 +41,9 @@ import oracle  # noqa: E402
 
 SEATTLE = HERE / "seattle2012.csv.gz"
 CASES = {
-    "config3": ("gen", 3, None),
-    "config1": ("gen", 1, None),
+    "config3": ("gen", 3, 1.0),
+    "config1": ("gen", 1, 1.0),
+    "config4_0.005": ("gen", 4, 0.005),
     "seattle_pi0.3": ("csv", SEATTLE, 0.3),
     "seattle_pi0.55": ("csv", SEATTLE, 0.55),
 }
@@ -68,14 +71,14 @@ def read_seattle():
 
 
 def load_case(name):
-    kind, src, thr = CASES[name]
+    kind, src, arg = CASES[name]
     if kind == "gen":
         from colo import gen
 
-        wl = gen.config(src)
+        wl = gen.config(src, scale=arg)
         return wl.x, wl.y, wl.fid, wl.bounds, wl.R, wl.thr, wl.max_size
     x, y, fid, b, _ = read_seattle()
-    return x, y, fid, b, 10.0, thr, 0
+    return x, y, fid, b, 10.0, arg, 0
 
 
 def trace(name):
@@ -91,8 +94,10 @@ def trace(name):
     res = oracle.mine(x, y, fid, b, R, thr, max_k=max_k, keep_tables=True,
                       res=(amb, le) if len(amb) else None, fast=True)
     assert res.status == 0 and res.unresolved == 0, (res.status, res.unresolved)
+    kind, src, arg = CASES[name]
     out = {"meta": np.frombuffer(json.dumps({
-        "case": name, "points": int(len(x)), "digest": dataset_digest(x, y, fid, b), "R": float(R),
+        "case": name, "config": src if kind == "gen" else None, "scale": arg if kind == "gen" else None,
+        "points": int(len(x)), "digest": dataset_digest(x, y, fid, b), "R": float(R),
         "thr": float(thr), "max_size": int(max_k), "levels": [int(l.k) for l in res.levels],
         "candidates": res.num_candidates(), "prevalent": len(res.patterns())}).encode(), np.uint8),
         "amb_keys": amb.astype(np.uint64), "amb_le": le}

@@ -8,6 +8,8 @@ prevalence, argmin and the SHA-256 of every instance table, row order
 included) of
   config3         20,000,000 points, 100 features, R 20, PI 0.15 (bench.py's workload)
   config1         1,000,000 points, 40 features, R 100, PI 0.2
+  config4_0.005   500,000 points, 200 features, R 10, PI 0.1, no size cap: the dense
+                  sigma = 5 hotspot at full density, levels up to 8, 2.8e9 rows
   seattle_pi0.3   the reference's real-data fixture Seattle2012, R 10, PI 0.3
   seattle_pi0.55  the same at PI 0.55 (the reference's experiment log)
 Each synthetic dataset is regenerated here and checked against the digest
@@ -30,7 +32,7 @@ from colo import gen
 pytestmark = pytest.mark.gpu
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES = ["config3", "config1", "seattle_pi0.3", "seattle_pi0.55"]
+CASES = ["config3", "config1", "config4_0.005", "seattle_pi0.3", "seattle_pi0.55"]
 MODES = {"plain": colo.MODE_PLAIN, "batched": colo.MODE_BATCHED, "learned": colo.MODE_LEARNED}
 FIELDS = ("cand", "ub", "pass", "rows", "num", "pi", "prevalent", "argmin")
 
@@ -72,7 +74,7 @@ def case_dataset(ctx, name, meta, seattle_csv):
     """(Dataset, x, y, R, thr, max_size) of a case, built once per module."""
     if name not in _data:
         if name.startswith("config"):
-            wl = gen.config(int(name[len("config"):]))
+            wl = gen.config(meta.get("config") or int(name[len("config"):]), scale=meta.get("scale") or 1.0)
             assert digest(wl.x, wl.y, wl.fid, wl.bounds) == meta["digest"], "generator output changed"
             ds = colo.Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
             _data[name] = (ds, wl.x, wl.y, wl.R, wl.thr, wl.max_size)

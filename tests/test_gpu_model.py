@@ -106,13 +106,18 @@ def test_learned_mining_is_identical(ctx, cfg, scale, model):
     p = colo.load_model() if model == "trained" else np.zeros(colo.MODEL_PARAMS, np.float32)
     ctx.set_model(p)
     try:
+        # the default policy (single pass for tables presized large) and a single pass for every table
         got = ctx.mine(ds, colo.default_params(wl.R, wl.thr, colo.MODE_LEARNED, max_size=wl.max_size,
                                                keep_tables=True))
+        every = ctx.mine(ds, colo.default_params(wl.R, wl.thr, colo.MODE_LEARNED, max_size=wl.max_size,
+                                                 keep_tables=True, single_pass=True))
     finally:
         ctx.set_model(None)
     _same(got, ref)
-    c = got.counters
+    _same(every, ref)
+    c = every.counters
     assert c["single_pass"] == c["refined"]
+    assert got.counters["single_pass"] <= c["refined"]
     if model == "zeros" and any(int(r) > 32 for lev in ref.levels for r in lev.rows):
         assert c["single_pass_overflow"] > 0    # the fallback ran
 
@@ -148,7 +153,7 @@ def test_trained_model_beats_the_model_free_presize(ctx):
     for name, p in (("trained", params), ("heuristic", hp)):
         ctx.set_model(p)
         try:
-            out[name] = ctx.mine(ds, colo.default_params(wl.R, 0.07, colo.MODE_LEARNED))
+            out[name] = ctx.mine(ds, colo.default_params(wl.R, 0.07, colo.MODE_LEARNED, single_pass=True))
         finally:
             ctx.set_model(None)
     print({k: (v.counters["single_pass"], v.counters["single_pass_overflow"]) for k, v in out.items()})

@@ -497,12 +497,13 @@ def main():
         pass
     head_mode = colo.MODE_LEARNED if model is not None else colo.MODE_BATCHED
     ctx.set_model(model)
-    # pick the join's lanes per anchor for this dataset (untimed; kept by the context)
+    # launch shapes for this dataset (untimed; kept by the context): the join's lanes per anchor, the
+    # level filter's candidates per unit, the level kernels' threads per block
     if args.join_group:
         ctx.set_join_group(args.join_group)
-        tuned = {"join_group": args.join_group, "join_ms": None}
+        tuned = {"join_group": args.join_group, "filter_unit": None, "level_block": None}
     else:
-        tuned = ctx.autotune(ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size))
+        tuned = ctx.autotune_all(ds, colo.default_params(wl.R, wl.thr, head_mode, max_size=wl.max_size))
     ms_b, res_b, clocks, tot_b = timed(head_mode, True)
     cands = res_b[0].num_candidates()
     value = tot_b / (ms_b / 1e3)

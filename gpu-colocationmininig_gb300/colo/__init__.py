@@ -44,7 +44,8 @@ EXPORTS = [
     "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
     "colo_ctx_set_model", "colo_result_features", "colo_autotune", "colo_dataset_from_csv_threads",
     "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary", "colo_stage_apriori",
-    "colo_dataset_from_csv_device", "colo_set_join_group",
+    "colo_dataset_from_csv_device", "colo_set_join_group", "colo_autotune_all", "colo_set_tuning",
+    "colo_get_tuning",
 ]
 MODEL_FEATURES = 24
 MODEL_PARAMS = 32 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -139,6 +140,9 @@ def load(build: bool = True) -> C.CDLL:
         "colo_ctx_set_model": (C.c_int, [_P, _f32p]),
         "colo_autotune": (C.c_int, [_P, _P, C.POINTER(Params), _i32p, C.POINTER(C.c_double)]),
         "colo_set_join_group": (C.c_int, [_P, C.c_int32]),
+        "colo_autotune_all": (C.c_int, [_P, _P, C.POINTER(Params), C.c_char_p, C.POINTER(Tuning)]),
+        "colo_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+        "colo_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
         "colo_result_features": (C.c_int, [_P, C.c_uint32, _f32p]),
     }
     for name, (res, args) in sig.items():
@@ -202,6 +206,18 @@ def csv_to_binary(csv_path: str, bin_path: str, threads: int = 0) -> None:
 BINARY_MAGIC = b"COLOPTS1"
 # lanes per anchor that the join autotuner times (colo_autotune, in this order)
 JOIN_WIDTHS = (1, 2, 4, 8, 16, 32)
+# the other tuned launch shapes (colo_autotune_all)
+FILTER_UNITS = (8, 16, 32)
+LEVEL_BLOCKS = (64, 128, 256)
+
+
+class Tuning(C.Structure):
+    _fields_ = [("join_group", C.c_int32), ("filter_unit", C.c_int32), ("level_block", C.c_int32),
+                ("from_cache", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"join_group": self.join_group, "filter_unit": self.filter_unit, "level_block": self.level_block,
+                "from_cache": bool(self.from_cache)}
 
 
 def read_binary(path: str):
@@ -421,6 +437,23 @@ class Context:
     def set_join_group(self, width: int) -> None:
         """Pin the join's lanes per anchor (one of JOIN_WIDTHS; 0 for the default)."""
         self.check(self.lib.colo_set_join_group(self.h, int(width)), "set_join_group")
+
+    def autotune_all(self, ds: "Dataset", params: Params, cache: Optional[str] = None) -> dict:
+        """Tune the join width, the filter unit and the level block size for this dataset (kept for
+        later mines); `cache` is a text file of tuned shapes read before and appended after tuning."""
+        t = Tuning()
+        self.check(self.lib.colo_autotune_all(self.h, ds.h, C.byref(params), None if cache is None else
+                                              str(cache).encode(), C.byref(t)), "autotune_all")
+        return t.as_dict()
+
+    def set_tuning(self, join_group: int = 0, filter_unit: int = 0, level_block: int = 0) -> None:
+        t = Tuning(join_group, filter_unit, level_block, 0)
+        self.check(self.lib.colo_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        self.check(self.lib.colo_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return t.as_dict()
 
     # ---- learned cost model -------------------------------------------------
     def model_forward(self, params: np.ndarray, x: np.ndarray) -> np.ndarray:

@@ -87,6 +87,8 @@ struct Batch {
     uint64_t active_anchors = 0; // anchors whose cell has higher-feature neighbours
     bool join_single = true;     // single pass into per-run upper-bound regions
     int join_group = 8;          // lanes per anchor in the join (autotuned)
+    int filter_unit = 32;        // candidates per warp unit in the level filter (autotuned: 8, 16, 32)
+    int level_block = 256;       // threads per block of the level kernels (autotuned: 64, 128, 256)
     uint32_t test_spin = 0;      // tests only: the sort's look-back gives up after this many polls
     uint64_t filter_items = 0;   // (driver cell, candidate) items of the level filters
 };

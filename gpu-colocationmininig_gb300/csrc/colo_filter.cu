@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, cons
 // Level k >= 3 over the driver lists.  Candidates are grouped by driver
 // (group g: driver feature gfeat[g], candidates order[gstart[g] ..
 // gstart[g] + gcount[g])); a unit is 32 cells of the driver's list times up
-// to 32 of its candidates, units of one cell chunk adjacent (they read the
-// same quad masks).  A warp takes a unit: lane = cell, loop over the
+// to cu (8, 16 or 32, autotuned) of its candidates, units of one cell chunk
+// adjacent (they read the same quad masks).  A warp takes a unit: lane = cell, loop over the
 // candidates; a (cell Z, candidate c) pair is tested exactly as in a scan
 // of every cell with the driver in its 3x3 block: Z is in U_c when one of
 // its four quads covers c's members, each cell of U_c is met once, and a
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(256, (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1))) k_filt
     const uint32_t* __restrict__ lmem, uint32_t k, const uint32_t* __restrict__ qmask,
     const uint32_t* __restrict__ cmask, const uint32_t* __restrict__ crun, const uint8_t* __restrict__ qfirst,
     const uint32_t* __restrict__ rcnt, uint32_t* __restrict__ ub, unsigned long long* __restrict__ stats,
-    uint32_t acc_n) {
+    uint32_t acc_n, uint32_t cu) {
     constexpr uint32_t W = WT;
     constexpr bool kCacheQuads = WT <= 8;
     extern __shared__ uint32_t acc[];
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256, (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1))) k_filt
             else hi = mid;
         }
         const uint32_t f = __ldg(gfeat + lo), G = __ldg(gcount + lo), gs = __ldg(gstart + lo);
-        const uint32_t gch = (G + 31) / 32;
+        const uint32_t gch = (G + cu - 1) / cu;
         const uint64_t local = u - __ldg(uoff + lo);
         const uint64_t cc = local / gch;
         const uint32_t gc = (uint32_t)(local - cc * gch);
@@ -269,8 +269,8 @@ __global__ void __launch_bounds__(256, (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1))) k_filt
                 for (int q = 0; q < 4; ++q) load_row<WT>(q4 + q * W, qr[q]);
             }
         }
-        const uint32_t t1 = gc * 32 + 32 < G ? gc * 32 + 32 : G;
-        for (uint32_t t = gc * 32; t < t1; ++t) {
+        const uint32_t t1 = gc * cu + cu < G ? gc * cu + cu : G;
+        for (uint32_t t = gc * cu; t < t1; ++t) {
             const uint32_t c = __ldg(order + gs + t);
             uint32_t need[WT];
             load_row<WT>(need_all + (uint64_t)c * W, need);
@@ -475,7 +475,8 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     b.filter_items += nitems;
     if (nitems == 0) return;
     if (!b.dlist_ready) driver_lists_fill(b);
-    // groups (one per driver) and their units: 32 list cells x up to 32 candidates
+    // groups (one per driver) and their units: 32 list cells x up to cu candidates
+    const uint32_t cu = (b.filter_unit == 8 || b.filter_unit == 16) ? (uint32_t)b.filter_unit : 32u;
     std::vector<uint32_t> gfeat, gstart, gcount;
     std::vector<uint64_t> uoff(1, 0);
     for (uint32_t f = 0; f < b.F; ++f) {
@@ -484,7 +485,7 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
         gfeat.push_back(f);
         gstart.push_back(dstart[f]);
         gcount.push_back(dcount[f]);
-        uoff.push_back(uoff.back() + (L + 31) / 32 * ((dcount[f] + 31) / 32));
+        uoff.push_back(uoff.back() + (L + 31) / 32 * ((dcount[f] + cu - 1) / cu));
     }
     const uint32_t ngroups = (uint32_t)gfeat.size();
     const uint64_t nunits = uoff.back();
@@ -535,7 +536,7 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
 #define COLO_FL(WW)                                                                                             \
     k_filter_drv<WW><<<grid((const void*)k_filter_drv<WW>), 256, smem, s>>>(                                    \
         nunits, ngroups, d_uoff, d_gfeat, d_gstart, d_gcount, b.doff.get(), b.dlist.get(), d_order, d_need,       \
-        d_lmem, k, b.qmask.get(), b.cmask.get(), b.crun.get(), b.qfirst.get(), b.rcnt.get(), d_ub, d_stats, acc_n)
+        d_lmem, k, b.qmask.get(), b.cmask.get(), b.crun.get(), b.qfirst.get(), b.rcnt.get(), d_ub, d_stats, acc_n, cu)
     COLO_W_SWITCH(b.W, COLO_FL)
 #undef COLO_FL
     COLO_LAUNCH_CHECK();

@@ -383,10 +383,11 @@ template <int MODE>
 void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
     if (w.nchunks == 0) return;
     KScope ks(MODE == MODE_COUNT ? "level_count" : MODE == MODE_FILL ? "level_fill" : "level_single");
+    const unsigned block = (b.level_block == 64 || b.level_block == 128) ? (unsigned)b.level_block : 256u;
     uint64_t threads = w.nchunks * 32;
-    unsigned grid = (unsigned)((threads + 255) / 256);
+    unsigned grid = (unsigned)((threads + block - 1) / block);
 #define COLO_LVL(KK)                                                                              \
-    k_level<KK, MODE><<<grid, 256, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_beg.get(), b.nb_cnt.get(), \
+    k_level<KK, MODE><<<grid, block, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_beg.get(), b.nb_cnt.get(), \
                                             b.nb.get(), b.xy.get(), b.fstart.get(), b.fcount.get(),  \
                                             b.grids.get(), ovf, w.items, w.chunk_status, w.ticket,    \
                                             &b.flags.get()->timeout)

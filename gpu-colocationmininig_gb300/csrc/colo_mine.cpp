@@ -367,6 +367,8 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     b.sms = ctx->sms;
     b.J = J;
     if (ctx->join_group) b.join_group = ctx->join_group;
+    if (ctx->filter_unit) b.filter_unit = ctx->filter_unit;
+    if (ctx->level_block) b.level_block = ctx->level_block;
     b.test_spin = pv[0].reserved[1] > 0 ? (uint32_t)pv[0].reserved[1] : 0u;
     auto t0 = Clock::now();
     std::vector<uint32_t> job_f0(J + 1, 0);

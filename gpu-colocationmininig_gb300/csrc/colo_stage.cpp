@@ -3,7 +3,9 @@
 // (Codes/DeviceProcess.h:4-36).  They run one stage on a dataset and copy
 // its result to host arrays, so each kernel can be checked in isolation.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "colo_batch.h"
@@ -263,6 +265,184 @@ colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p,
         if (ms) std::memcpy(ms, t, sizeof(t));
         return COLO_OK;
     });
+}
+
+}  // extern "C"
+
+namespace {
+
+// ---- tuning cache ----------------------------------------------------------
+// One text line per tuned dataset shape:
+//   colo-tune 1 n=<points> f=<features> m=<occupied cells> r=<R float bits, hex> sms=<SMs> join=<lanes>
+//   funit=<candidates per filter unit> lblock=<level threads per block>
+// Lines that do not parse are skipped; a shape tuned twice keeps its first line.
+struct TuneKey {
+    uint64_t n = 0, f = 0, m = 0;
+    uint32_t rbits = 0;
+    int sms = 0;
+    bool operator==(const TuneKey& o) const {
+        return n == o.n && f == o.f && m == o.m && rbits == o.rbits && sms == o.sms;
+    }
+};
+
+bool cache_lookup(const char* path, const TuneKey& key, colo_tuning* t) {
+    FILE* fp = std::fopen(path, "r");
+    if (!fp) return false;
+    char line[512];
+    bool hit = false;
+    while (!hit && std::fgets(line, sizeof(line), fp)) {
+        unsigned long long n, f, m;
+        unsigned rb;
+        int sms, j, u, lb, ver;
+        if (std::sscanf(line, "colo-tune %d n=%llu f=%llu m=%llu r=%x sms=%d join=%d funit=%d lblock=%d", &ver, &n,
+                        &f, &m, &rb, &sms, &j, &u, &lb) != 9 || ver != 1)
+            continue;
+        TuneKey k;
+        k.n = n;
+        k.f = f;
+        k.m = m;
+        k.rbits = rb;
+        k.sms = sms;
+        if (!(k == key)) continue;
+        t->join_group = j;
+        t->filter_unit = u;
+        t->level_block = lb;
+        hit = true;
+    }
+    std::fclose(fp);
+    return hit;
+}
+
+bool cache_store(const char* path, const TuneKey& key, const colo_tuning& t) {
+    FILE* fp = std::fopen(path, "a");
+    if (!fp) return false;
+    std::fprintf(fp, "colo-tune 1 n=%llu f=%llu m=%llu r=%08x sms=%d join=%d funit=%d lblock=%d\n",
+                 (unsigned long long)key.n, (unsigned long long)key.f, (unsigned long long)key.m, key.rbits, key.sms,
+                 t.join_group, t.filter_unit, t.level_block);
+    return std::fclose(fp) == 0;
+}
+
+bool valid_tuning(const colo_tuning& t) {
+    const int j = t.join_group, u = t.filter_unit, lb = t.level_block;
+    const bool jok = j == 0 || j == 1 || j == 2 || j == 4 || j == 8 || j == 16 || j == 32;
+    const bool uok = u == 0 || u == 8 || u == 16 || u == 32;
+    const bool lok = lb == 0 || lb == 64 || lb == 128 || lb == 256;
+    return jok && uok && lok;
+}
+
+// CUDA-event milliseconds of the kernel families whose names start with one of the prefixes,
+// from one profiled mine (after one unprofiled warm-up mine).
+colo_status time_families(colo_ctx* ctx, colo_dataset* ds, const colo_params* p,
+                          std::initializer_list<const char*> prefixes, double* ms) {
+    colo_params q = *p;
+    q.reserved[0] |= 1;   // time every kernel
+    q.keep_tables = 0;
+    colo_result* r = nullptr;
+    colo_status st = colo_mine(ctx, ds, p, &r);
+    colo_result_free(r);
+    if (st != COLO_OK) return st;
+    r = nullptr;
+    st = colo_mine(ctx, ds, &q, &r);
+    if (st != COLO_OK) return st;
+    double t = 0;
+    for (const auto& k : r->r.kernels)
+        for (const char* pre : prefixes)
+            if (k.name.rfind(pre, 0) == 0) t += k.ms;
+    colo_result_free(r);
+    *ms = t;
+    return COLO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+colo_status colo_autotune_all(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, const char* cache_path,
+                              colo_tuning* out) {
+    if (!ctx || !ds || !p) return COLO_ERR_ARG;
+    TuneKey key;
+    key.n = ds->hp.x.size();
+    key.f = ds->names.size();
+    std::memcpy(&key.rbits, &p->distance, 4);
+    key.sms = ctx->sms;
+    // the occupied cells of the dataset at this R (one bucketing pass)
+    colo_status st = run_guarded(ctx, [&]() -> colo_status {
+        Batch b;
+        std::vector<DevBuf<float>> of;
+        colo_dataset* dsv[1] = {ds};
+        setup_batch(ctx, dsv, p, 1, b, of, nullptr);
+        if (b.N) bucket_points(b);
+        key.m = b.M;
+        return COLO_OK;
+    });
+    if (st != COLO_OK) return st;
+    colo_tuning t{};
+    if (cache_path && cache_lookup(cache_path, key, &t) && valid_tuning(t)) {
+        ctx->join_group = t.join_group;
+        ctx->filter_unit = t.filter_unit;
+        ctx->level_block = t.level_block;
+        t.from_cache = 1;
+        if (out) *out = t;
+        return COLO_OK;
+    }
+    // lanes per anchor in the join
+    int32_t jg = 8;
+    st = colo_autotune(ctx, ds, p, &jg, nullptr);
+    if (st != COLO_OK) return st;
+    t.join_group = jg;
+    // candidates per unit of the level filter, then threads per block of the level kernels,
+    // each from the time of its own kernels in a whole mine
+    const int units[3] = {8, 16, 32}, blocks[3] = {64, 128, 256};
+    double best = 1e300;
+    t.filter_unit = 32;
+    for (int u : units) {
+        ctx->filter_unit = u;
+        double ms = 0;
+        st = time_families(ctx, ds, p, {"filter_level"}, &ms);
+        if (st != COLO_OK) return st;
+        if (ms < best) {
+            best = ms;
+            t.filter_unit = u;
+        }
+    }
+    ctx->filter_unit = t.filter_unit;
+    best = 1e300;
+    t.level_block = 256;
+    for (int lb : blocks) {
+        ctx->level_block = lb;
+        double ms = 0;
+        st = time_families(ctx, ds, p, {"level_"}, &ms);
+        if (st != COLO_OK) return st;
+        if (ms < best) {
+            best = ms;
+            t.level_block = lb;
+        }
+    }
+    ctx->level_block = t.level_block;
+    t.from_cache = 0;
+    if (cache_path && !cache_store(cache_path, key, t)) {
+        ctx->err = std::string("cannot write the tuning cache ") + cache_path;
+        return COLO_ERR_IO;
+    }
+    if (out) *out = t;
+    return COLO_OK;
+}
+
+colo_status colo_set_tuning(colo_ctx* ctx, const colo_tuning* t) {
+    if (!ctx || !t || !valid_tuning(*t)) return COLO_ERR_ARG;
+    ctx->join_group = t->join_group;
+    ctx->filter_unit = t->filter_unit;
+    ctx->level_block = t->level_block;
+    return COLO_OK;
+}
+
+colo_status colo_get_tuning(const colo_ctx* ctx, colo_tuning* t) {
+    if (!ctx || !t) return COLO_ERR_ARG;
+    t->join_group = ctx->join_group;
+    t->filter_unit = ctx->filter_unit;
+    t->level_block = ctx->level_block;
+    t->from_cache = 0;
+    return COLO_OK;
 }
 
 colo_status colo_set_join_group(colo_ctx* ctx, int32_t join_group) {

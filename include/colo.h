@@ -255,6 +255,30 @@ colo_status colo_autotune(colo_ctx* ctx, colo_dataset* ds, const colo_params* p,
  * other width. */
 colo_status colo_set_join_group(colo_ctx* ctx, int32_t join_group);
 
+/* Launch shapes tuned per dataset (no counterpart in the reference): lanes
+ * per anchor in the cell-pair join (1, 2, 4, 8, 16, 32), candidates per warp
+ * unit in the level filter (8, 16, 32) and threads per block of the level
+ * kernels (64, 128, 256); 0 keeps the default (8, 32, 256).  Every setting
+ * gives the same results. */
+typedef struct {
+    int32_t join_group;
+    int32_t filter_unit;
+    int32_t level_block;
+    int32_t from_cache;      /* colo_autotune_all: 1 when the shapes came from the cache file */
+} colo_tuning;
+/* Tunes all three for this dataset and parameters and keeps them for later
+ * mines on this context: the join as colo_autotune does, then the filter unit
+ * and the level block size from the CUDA-event time of their own kernels in
+ * whole mines.  cache_path (optional) is a text file of tuned shapes keyed by
+ * (points, features, occupied cells, R, SM count): a key found there is
+ * applied without timing; a new key is appended.  out (optional) receives
+ * the shapes. */
+colo_status colo_autotune_all(colo_ctx* ctx, colo_dataset* ds, const colo_params* p, const char* cache_path,
+                              colo_tuning* out);
+/* Sets / reads the context's launch shapes (COLO_ERR_ARG for other values). */
+colo_status colo_set_tuning(colo_ctx* ctx, const colo_tuning* t);
+colo_status colo_get_tuning(const colo_ctx* ctx, colo_tuning* t);
+
 /* ---- learned cost model ----------------------------------------------- */
 /* A 24 -> 64 -> 64 -> 1 ReLU MLP (BF16 weights and activations, FP32
  * accumulation, hand-written tensor-core kernels) that predicts

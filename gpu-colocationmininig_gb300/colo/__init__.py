@@ -213,11 +213,11 @@ LEVEL_BLOCKS = (64, 128, 256)
 
 class Tuning(C.Structure):
     _fields_ = [("join_group", C.c_int32), ("filter_unit", C.c_int32), ("level_block", C.c_int32),
-                ("from_cache", C.c_int32)]
+                ("level_queue", C.c_int32), ("from_cache", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {"join_group": self.join_group, "filter_unit": self.filter_unit, "level_block": self.level_block,
-                "from_cache": bool(self.from_cache)}
+                "level_queue": self.level_queue, "from_cache": bool(self.from_cache)}
 
 
 def read_binary(path: str):
@@ -446,8 +446,9 @@ class Context:
                                               str(cache).encode(), C.byref(t)), "autotune_all")
         return t.as_dict()
 
-    def set_tuning(self, join_group: int = 0, filter_unit: int = 0, level_block: int = 0) -> None:
-        t = Tuning(join_group, filter_unit, level_block, 0)
+    def set_tuning(self, join_group: int = 0, filter_unit: int = 0, level_block: int = 0,
+                   level_queue: int = 0) -> None:
+        t = Tuning(join_group, filter_unit, level_block, level_queue, 0)
         self.check(self.lib.colo_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def tuning(self) -> dict:

@@ -58,8 +58,9 @@ struct Batch {
     // level filters test exactly these cells for the candidates f drives
     DevBuf<uint32_t> dlist;
     DevBuf<uint64_t> doff;
-    std::vector<uint64_t> h_doff;
-    bool dlist_ready = false;    // lists filled (on the first level filter of the mine)
+    std::vector<uint64_t> h_dcnt;    // cells per feature's list (every feature)
+    std::vector<uint64_t> h_doff;    // offsets of the lists filled (features in dlist_have; others empty)
+    std::vector<uint8_t> dlist_have; // features whose lists are filled (by the level filters, on demand)
     DevBuf<uint8_t> qfirst;      // per cell: bit q set when it is the first occupied cell of its quad q
     // runs
     DevBuf<uint32_t> rfeat, rstart, rcnt, rcell;
@@ -89,6 +90,7 @@ struct Batch {
     int join_group = 8;          // lanes per anchor in the join (autotuned)
     int filter_unit = 32;        // candidates per warp unit in the level filter (autotuned: 8, 16, 32)
     int level_block = 256;       // threads per block of the level kernels (autotuned: 64, 128, 256)
+    int level_queue = 0;         // 1: level count/fill kernels as a persistent work queue (autotuned)
     uint32_t test_spin = 0;      // tests only: the sort's look-back gives up after this many polls
     uint64_t filter_items = 0;   // (driver cell, candidate) items of the level filters
 };
@@ -106,8 +108,9 @@ void apriori_device(cudaStream_t s, const std::vector<const std::vector<uint32_t
                     std::vector<std::vector<uint32_t>>& out, std::vector<std::vector<uint32_t>>& parent);
 // colo_filter.cu
 // Driver lists: per-feature cell counts into d_cnt (F entries, zeroed by the
-// caller); the lists themselves are filled from b.h_doff by the first level
-// filter of the mine.
+// caller); the lists themselves are filled by the level filters for the
+// features their candidates have (a level's candidates only have members of
+// the previous level's, so the first level filter fills them all).
 void driver_lists_count(Batch& b, uint32_t* d_cnt);
 // Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
 // bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.

@@ -865,8 +865,9 @@ void bucket_points(Batch& b) {
         COLO_CUDA(cudaStreamSynchronize(s));
         b.h_frun_off.assign(b.F + 1, 0);
         for (uint32_t f = 0; f < b.F; ++f) b.h_frun_off[f + 1] = b.h_frun_off[f] + hc[f];
+        b.h_dcnt.assign(hd.begin(), hd.end());
         b.h_doff.assign(b.F + 1, 0);
-        for (uint32_t f = 0; f < b.F; ++f) b.h_doff[f + 1] = b.h_doff[f] + hd[f];
+        b.dlist_have.assign(b.F, 0);
         if (hf.timeout) throw StatusError{COLO_ERR_TIMEOUT, "radix sort: a tile waited too long for its predecessors"};
         if (hf.out_of_grid)
             throw StatusError{COLO_ERR_INPUT, std::to_string(hf.out_of_grid) +

@@ -145,10 +145,11 @@ __device__ __forceinline__ void load_row(const uint32_t* __restrict__ p, uint32_
 // one warp adding to the same counter would serialise.
 constexpr uint32_t kDilHist = 4096;
 
+// fn(z, f) for every feature f of cell z's 3x3 block that is in the want bitset.
 template <int WT, class Fn>
 __device__ __forceinline__ void dil_cells(uint64_t z0, uint64_t z1, const uint32_t* __restrict__ cjob,
                                           const JobGrid* __restrict__ grids, const uint32_t* __restrict__ nbmask,
-                                          Fn&& fn) {
+                                          const uint32_t* __restrict__ want, Fn&& fn) {
     const uint64_t n = z1 > z0 ? z1 - z0 : 0;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint64_t stretch = (n + 31) / 32;   // lane l walks cells z0 + l*stretch + i
@@ -160,8 +161,10 @@ __device__ __forceinline__ void dil_cells(uint64_t z0, uint64_t z1, const uint32
         const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
 #pragma unroll
         for (int w = 0; w < WT; ++w)
-            for (uint32_t bits = row[w]; bits; bits &= bits - 1)
-                fn(z, f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1));
+            for (uint32_t bits = row[w]; bits; bits &= bits - 1) {
+                const uint32_t f = f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1);
+                if (!want || (__ldg(want + (f >> 5)) >> (f & 31) & 1u)) fn(z, f);
+            }
     }
 }
 
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(256) k_dil_count(uint64_t M, uint64_t per, con
         for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) h[i] = 0;
     __syncthreads();
     const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
-    dil_cells<WT>(z0, z1, cjob, grids, nbmask, [&](uint64_t, uint32_t f) {
+    dil_cells<WT>(z0, z1, cjob, grids, nbmask, nullptr, [&](uint64_t, uint32_t f) {
         if (local) atomicAdd(&h[f], 1u);
         else atomicAdd(&cnt[f], 1u);
     });
@@ -193,19 +196,19 @@ __global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, cons
                                                   const JobGrid* __restrict__ grids,
                                                   const uint32_t* __restrict__ nbmask, uint32_t F,
                                                   const uint64_t* __restrict__ doff, uint32_t* __restrict__ cursor,
-                                                  uint32_t* __restrict__ dlist) {
+                                                  uint32_t* __restrict__ dlist, const uint32_t* __restrict__ want) {
     extern __shared__ unsigned long long hb[];   // F bases, then F counters (32-bit)
     uint32_t* hc = reinterpret_cast<uint32_t*>(hb + F);
     const bool local = F <= kDilHist;
     const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
     if (!local) {
-        dil_cells<WT>(z0, z1, cjob, grids, nbmask,
+        dil_cells<WT>(z0, z1, cjob, grids, nbmask, want,
                       [&](uint64_t z, uint32_t f) { dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z; });
         return;
     }
     for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) hc[i] = 0;
     __syncthreads();
-    dil_cells<WT>(z0, z1, cjob, grids, nbmask, [&](uint64_t, uint32_t f) { atomicAdd(&hc[f], 1u); });
+    dil_cells<WT>(z0, z1, cjob, grids, nbmask, want, [&](uint64_t, uint32_t f) { atomicAdd(&hc[f], 1u); });
     __syncthreads();
     for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
         const uint32_t c = hc[f];
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, cons
         hc[f] = 0;
     }
     __syncthreads();
-    dil_cells<WT>(z0, z1, cjob, grids, nbmask,
+    dil_cells<WT>(z0, z1, cjob, grids, nbmask, want,
                   [&](uint64_t z, uint32_t f) { dlist[hb[f] + atomicAdd(&hc[f], 1u)] = (uint32_t)z; });
 }
 
@@ -370,13 +373,26 @@ void driver_lists_count(Batch& b, uint32_t* d_cnt) {
 
 namespace {
 
-void driver_lists_fill(Batch& b) {
+// The lists of every feature in `need` (and of those already filled): the lists are filled
+// again for the union when a feature is missing.
+void driver_lists_fill(Batch& b, const std::vector<uint8_t>& need) {
+    bool missing = false;
+    for (uint32_t f = 0; f < b.F; ++f) missing |= need[f] && !b.dlist_have[f];
+    if (!missing) return;
     cudaStream_t s = b.s;
-    b.dlist_ready = true;
-    const uint64_t total = b.h_doff.empty() ? 0 : b.h_doff[b.F];
+    std::vector<uint32_t> want((b.F + 31) / 32, 0);
+    b.h_doff.assign(b.F + 1, 0);
+    for (uint32_t f = 0; f < b.F; ++f) {
+        b.dlist_have[f] |= need[f];
+        if (b.dlist_have[f]) want[f >> 5] |= 1u << (f & 31);
+        b.h_doff[f + 1] = b.h_doff[f] + (b.dlist_have[f] ? b.h_dcnt[f] : 0);
+    }
+    const uint64_t total = b.h_doff[b.F];
     b.dlist.alloc(total ? total : 1, s);
-    b.doff.alloc(b.F + 1, s);
+    b.doff.alloc(b.F + 1 + want.size() / 2 + 1, s);   // offsets, then the want bitset
+    uint32_t* d_want = reinterpret_cast<uint32_t*>(b.doff.get() + b.F + 1);
     COLO_CUDA(cudaMemcpyAsync(b.doff.get(), b.h_doff.data(), (b.F + 1) * 8, cudaMemcpyHostToDevice, s));
+    COLO_CUDA(cudaMemcpyAsync(d_want, want.data(), want.size() * 4, cudaMemcpyHostToDevice, s));
     if (total == 0) return;
     DevBuf<uint32_t> cursor;
     cursor.alloc(b.F, s);
@@ -389,7 +405,8 @@ void driver_lists_fill(Batch& b) {
     KScope ks("driver_lists");
 #define COLO_DF(WW)                                                                                           \
     k_dil_fill<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
-                                                       b.nbmask.get(), b.F, b.doff.get(), cursor.get(), b.dlist.get())
+                                                       b.nbmask.get(), b.F, b.doff.get(), cursor.get(), b.dlist.get(), \
+                                                       d_want)
     COLO_W_SWITCH(b.W, COLO_DF)
 #undef COLO_DF
     COLO_LAUNCH_CHECK();
@@ -451,7 +468,7 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
         uint32_t best = mem[0];
         uint64_t bn = UINT64_MAX;
         for (uint32_t j = 0; j < m; ++j) {
-            const uint64_t nr = b.h_doff[mem[j] + 1] - b.h_doff[mem[j]];
+            const uint64_t nr = b.h_dcnt[mem[j]];
             if (nr < bn) {
                 bn = nr;
                 best = mem[j];
@@ -474,7 +491,11 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     for (uint32_t f = 0; f < b.F; ++f) nitems += (uint64_t)dcount[f] * (b.h_frun_off[f + 1] - b.h_frun_off[f]);
     b.filter_items += nitems;
     if (nitems == 0) return;
-    if (!b.dlist_ready) driver_lists_fill(b);
+    {
+        std::vector<uint8_t> need(b.F, 0);   // every member's list (drivers of this and later levels)
+        for (uint64_t c = 0; c < ncand * k; ++c) need[h_cand[c]] = 1;
+        driver_lists_fill(b, need);
+    }
     // groups (one per driver) and their units: 32 list cells x up to cu candidates
     const uint32_t cu = (b.filter_unit == 8 || b.filter_unit == 16) ? (uint32_t)b.filter_unit : 32u;
     std::vector<uint32_t> gfeat, gstart, gcount;

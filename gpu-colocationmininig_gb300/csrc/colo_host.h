@@ -92,6 +92,7 @@ struct colo_ctx {
     int join_group = 0;         // lanes per anchor in the join (0: default; set by colo_autotune)
     int filter_unit = 0;        // candidates per warp unit in the level filter (0: default 32)
     int level_block = 0;        // threads per block of the level kernels (0: default 256)
+    int level_queue = 0;        // 1: level count/fill kernels as a persistent work queue
     void* stage = nullptr;      // page-locked staging for the level loop's readbacks
     size_t stage_bytes = 0;
 };

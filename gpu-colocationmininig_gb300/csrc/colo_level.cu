@@ -31,8 +31,14 @@ namespace {
 
 enum { MODE_COUNT = 0, MODE_FILL = 1, MODE_SINGLE = 2 };
 
+// Participation bits: a word is read (from L2) before the atomic, so a bit
+// already set costs a load, not another atomic on the same address -- in
+// dense data thousands of rows hit the same few words.  A stale read only
+// costs an extra (idempotent) atomic.
 __device__ __forceinline__ void set_bit(uint32_t* words, uint32_t bit) {
-    atomicOr(&words[bit >> 5], 1u << (bit & 31));
+    uint32_t* w = &words[bit >> 5];
+    const uint32_t m = 1u << (bit & 31);
+    if (!(__ldcg(w) & m)) atomicOr(w, m);
 }
 
 constexpr unsigned long long kChunkA = 1ull << 62;   // chunk count published
@@ -64,22 +70,36 @@ __global__ void __launch_bounds__(256) k_level(
     const uint32_t* __restrict__ fcount, const JobGrid* __restrict__ grids,
     uint32_t* __restrict__ overflow, unsigned long long* __restrict__ items,
     unsigned long long* __restrict__ chunk_status, unsigned long long* __restrict__ ticket,
-    uint32_t* __restrict__ timeout) {
+    uint32_t* __restrict__ timeout, int persistent) {
     constexpr int KR = (K == 0) ? 1 : K;   // register members kept for K > 0
     const int lane = threadIdx.x & 31;
+    // one chunk per warp, or (persistent) warps that take chunk tickets until none is left; the
+    // single pass always takes tickets, so its chunks run in the order warps start them
+    const bool by_ticket = MODE == MODE_SINGLE || persistent;
+    for (bool first = true;; first = false) {
     uint64_t ch = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (MODE == MODE_SINGLE) {   // chunks in the order warps start
+    if (by_ticket) {
         unsigned long long tk = 0;
         if (lane == 0) tk = atomicAdd(ticket, 1ull);
         ch = __shfl_sync(0xffffffffu, tk, 0);
+    } else if (!first) {
+        break;
     }
-    if (ch >= nchunks) return;
-    // candidate of this chunk
-    uint64_t lo = 0, hi = ncand;
+    if (ch >= nchunks) break;
+    // candidate of this chunk: the last c with chunk_off[c] <= ch, by a 32-way search (the
+    // lanes probe 32 evenly spaced prefixes per round, so a few dependent loads instead of
+    // one per halving)
+    uint64_t lo = 0, hi = ncand;   // answer in [lo, hi)
     while (hi - lo > 1) {
-        uint64_t mid = (lo + hi) >> 1;
-        if (chunk_off[mid] <= ch) lo = mid;
-        else hi = mid;
+        const uint64_t span = hi - lo;
+        const uint64_t step = span <= 32 ? 1 : (span + 31) / 32;
+        const uint64_t probe = lo + (uint64_t)lane * step;
+        const bool le = probe < hi && chunk_off[probe] <= ch;
+        const uint32_t bal = __ballot_sync(0xffffffffu, le);   // lane 0 (probe lo) is always set
+        const int last = 31 - __clz(bal);
+        const uint64_t nlo = lo + (uint64_t)last * step;
+        hi = nlo + step < hi ? nlo + step : hi;
+        lo = nlo;
     }
     const CandDesc& d = cands[lo];
     const uint32_t k = (K == 0) ? d.k : (uint32_t)K;
@@ -311,7 +331,6 @@ __global__ void __launch_bounds__(256) k_level(
         if (mine) {
             set_bit(d.bitmap + d.bm_base, a0 - fstart[d.m[0]]);
             if (K > 0) {
-#pragma unroll
                 uint64_t o = d.bm_base + (fcount[d.m[0]] + 31u) / 32u;
 #pragma unroll
                 for (int q = 1; q < KR - 1; ++q) {
@@ -326,6 +345,7 @@ __global__ void __launch_bounds__(256) k_level(
             }
         }
     }
+    }   // chunks of this warp
 }
 
 // Participation statistics: per (candidate, member) [A, last, first, full]
@@ -386,11 +406,18 @@ void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
     const unsigned block = (b.level_block == 64 || b.level_block == 128) ? (unsigned)b.level_block : 256u;
     uint64_t threads = w.nchunks * 32;
     unsigned grid = (unsigned)((threads + block - 1) / block);
+    // persistent queue: as many blocks as are resident at once (64 registers a thread: 32 warps
+    // an SM), their warps taking chunk tickets (the ticket word follows the chunk words)
+    const int persistent = (b.level_queue && MODE != MODE_SINGLE && w.ticket) ? 1 : 0;
+    if (persistent) {
+        const uint64_t cap = (uint64_t)b.sms * (32u * 32u / block);
+        if (grid > cap) grid = (unsigned)cap;
+    }
 #define COLO_LVL(KK)                                                                              \
     k_level<KK, MODE><<<grid, block, 0, b.s>>>(w.cands, w.chunk_off, w.ncand, w.nchunks, b.nb_beg.get(), b.nb_cnt.get(), \
                                             b.nb.get(), b.xy.get(), b.fstart.get(), b.fcount.get(),  \
                                             b.grids.get(), ovf, w.items, w.chunk_status, w.ticket,    \
-                                            &b.flags.get()->timeout)
+                                            &b.flags.get()->timeout, persistent)
     switch (k) {
         case 2: COLO_LVL(2); break;
         case 3: COLO_LVL(3); break;

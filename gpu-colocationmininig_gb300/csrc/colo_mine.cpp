@@ -307,6 +307,7 @@ struct LevelArena {
     ArenaSpan<uint32_t> bitmap;
     ArenaSpan<unsigned long long> rows;
     ArenaSpan<unsigned long long> status;   // single pass: per chunk look-back word, then the chunk ticket
+    ArenaSpan<unsigned long long> tickets;  // chunk tickets of the count and fill launches (persistent queue)
     ArenaSpan<uint32_t> overflow;           // single pass: 1 when the table outgrew its capacity
     ArenaSpan<uint32_t> slots;
     ArenaSpan<CandDesc> descs;
@@ -324,6 +325,7 @@ struct LevelArena {
         const size_t o_bitmap = take(std::max<uint64_t>(nwords, 1) * 4);
         const size_t o_rows = take(std::max<uint64_t>(ncand, 1) * 8);
         const size_t o_status = single ? take((nchunks + 1) * 8) : 0;
+        const size_t o_tickets = take(2 * 8);
         const size_t o_overflow = single ? take(ncand * 4) : 0;
         const size_t zeroed = off;
         const size_t o_slots = take(std::max<uint64_t>(nslots, 1) * 4);
@@ -335,6 +337,7 @@ struct LevelArena {
         bitmap.p = reinterpret_cast<uint32_t*>(b + o_bitmap);
         rows.p = reinterpret_cast<unsigned long long*>(b + o_rows);
         status.p = single ? reinterpret_cast<unsigned long long*>(b + o_status) : nullptr;
+        tickets.p = reinterpret_cast<unsigned long long*>(b + o_tickets);
         overflow.p = single ? reinterpret_cast<uint32_t*>(b + o_overflow) : nullptr;
         slots.p = reinterpret_cast<uint32_t*>(b + o_slots);
         descs.p = reinterpret_cast<CandDesc*>(b + o_descs);
@@ -369,6 +372,7 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     if (ctx->join_group) b.join_group = ctx->join_group;
     if (ctx->filter_unit) b.filter_unit = ctx->filter_unit;
     if (ctx->level_block) b.level_block = ctx->level_block;
+    b.level_queue = ctx->level_queue > 0 ? 1 : 0;
     b.test_spin = pv[0].reserved[1] > 0 ? (uint32_t)pv[0].reserved[1] : 0u;
     auto t0 = Clock::now();
     std::vector<uint32_t> job_f0(J + 1, 0);
@@ -876,6 +880,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 if (ns < ncand) {
                     LevelWork w{ar.descs.get() + ns, ar.chunk_off.get() + ns + 1, ncand - ns, nch_count, d_items.get()};
+                    w.ticket = ar.tickets.get();
                     level_count(b, w, k);
                 }
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
@@ -1059,6 +1064,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
             } else {
                 LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr};
+                w.ticket = ar.tickets.get() + 1;
                 level_fill(b, w, k);
             }
         }

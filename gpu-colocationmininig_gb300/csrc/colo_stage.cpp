@@ -273,8 +273,8 @@ namespace {
 
 // ---- tuning cache ----------------------------------------------------------
 // One text line per tuned dataset shape:
-//   colo-tune 1 n=<points> f=<features> m=<occupied cells> r=<R float bits, hex> sms=<SMs> join=<lanes>
-//   funit=<candidates per filter unit> lblock=<level threads per block>
+//   colo-tune 2 n=<points> f=<features> m=<occupied cells> r=<R float bits, hex> sms=<SMs> join=<lanes>
+//   funit=<candidates per filter unit> lblock=<level threads per block> lqueue=<0|1>
 // Lines that do not parse are skipped; a shape tuned twice keeps its first line.
 struct TuneKey {
     uint64_t n = 0, f = 0, m = 0;
@@ -293,9 +293,9 @@ bool cache_lookup(const char* path, const TuneKey& key, colo_tuning* t) {
     while (!hit && std::fgets(line, sizeof(line), fp)) {
         unsigned long long n, f, m;
         unsigned rb;
-        int sms, j, u, lb, ver;
-        if (std::sscanf(line, "colo-tune %d n=%llu f=%llu m=%llu r=%x sms=%d join=%d funit=%d lblock=%d", &ver, &n,
-                        &f, &m, &rb, &sms, &j, &u, &lb) != 9 || ver != 1)
+        int sms, j, u, lb, lq, ver;
+        if (std::sscanf(line, "colo-tune %d n=%llu f=%llu m=%llu r=%x sms=%d join=%d funit=%d lblock=%d lqueue=%d",
+                        &ver, &n, &f, &m, &rb, &sms, &j, &u, &lb, &lq) != 10 || ver != 2)
             continue;
         TuneKey k;
         k.n = n;
@@ -307,6 +307,7 @@ bool cache_lookup(const char* path, const TuneKey& key, colo_tuning* t) {
         t->join_group = j;
         t->filter_unit = u;
         t->level_block = lb;
+        t->level_queue = lq;
         hit = true;
     }
     std::fclose(fp);
@@ -316,9 +317,9 @@ bool cache_lookup(const char* path, const TuneKey& key, colo_tuning* t) {
 bool cache_store(const char* path, const TuneKey& key, const colo_tuning& t) {
     FILE* fp = std::fopen(path, "a");
     if (!fp) return false;
-    std::fprintf(fp, "colo-tune 1 n=%llu f=%llu m=%llu r=%08x sms=%d join=%d funit=%d lblock=%d\n",
+    std::fprintf(fp, "colo-tune 2 n=%llu f=%llu m=%llu r=%08x sms=%d join=%d funit=%d lblock=%d lqueue=%d\n",
                  (unsigned long long)key.n, (unsigned long long)key.f, (unsigned long long)key.m, key.rbits, key.sms,
-                 t.join_group, t.filter_unit, t.level_block);
+                 t.join_group, t.filter_unit, t.level_block, t.level_queue);
     return std::fclose(fp) == 0;
 }
 
@@ -327,7 +328,7 @@ bool valid_tuning(const colo_tuning& t) {
     const bool jok = j == 0 || j == 1 || j == 2 || j == 4 || j == 8 || j == 16 || j == 32;
     const bool uok = u == 0 || u == 8 || u == 16 || u == 32;
     const bool lok = lb == 0 || lb == 64 || lb == 128 || lb == 256;
-    return jok && uok && lok;
+    return jok && uok && lok && (t.level_queue == 0 || t.level_queue == 1);
 }
 
 // CUDA-event milliseconds of the kernel families whose names start with one of the prefixes,
@@ -381,6 +382,7 @@ colo_status colo_autotune_all(colo_ctx* ctx, colo_dataset* ds, const colo_params
         ctx->join_group = t.join_group;
         ctx->filter_unit = t.filter_unit;
         ctx->level_block = t.level_block;
+        ctx->level_queue = t.level_queue;
         t.from_cache = 1;
         if (out) *out = t;
         return COLO_OK;
@@ -419,6 +421,19 @@ colo_status colo_autotune_all(colo_ctx* ctx, colo_dataset* ds, const colo_params
         }
     }
     ctx->level_block = t.level_block;
+    best = 1e300;
+    t.level_queue = 0;
+    for (int lq : {0, 1}) {
+        ctx->level_queue = lq;
+        double ms = 0;
+        st = time_families(ctx, ds, p, {"level_"}, &ms);
+        if (st != COLO_OK) return st;
+        if (ms < best) {
+            best = ms;
+            t.level_queue = lq;
+        }
+    }
+    ctx->level_queue = t.level_queue;
     t.from_cache = 0;
     if (cache_path && !cache_store(cache_path, key, t)) {
         ctx->err = std::string("cannot write the tuning cache ") + cache_path;
@@ -433,6 +448,7 @@ colo_status colo_set_tuning(colo_ctx* ctx, const colo_tuning* t) {
     ctx->join_group = t->join_group;
     ctx->filter_unit = t->filter_unit;
     ctx->level_block = t->level_block;
+    ctx->level_queue = t->level_queue;
     return COLO_OK;
 }
 
@@ -441,6 +457,7 @@ colo_status colo_get_tuning(const colo_ctx* ctx, colo_tuning* t) {
     t->join_group = ctx->join_group;
     t->filter_unit = ctx->filter_unit;
     t->level_block = ctx->level_block;
+    t->level_queue = ctx->level_queue;
     t->from_cache = 0;
     return COLO_OK;
 }

@@ -257,19 +257,22 @@ colo_status colo_set_join_group(colo_ctx* ctx, int32_t join_group);
 
 /* Launch shapes tuned per dataset (no counterpart in the reference): lanes
  * per anchor in the cell-pair join (1, 2, 4, 8, 16, 32), candidates per warp
- * unit in the level filter (8, 16, 32) and threads per block of the level
- * kernels (64, 128, 256); 0 keeps the default (8, 32, 256).  Every setting
- * gives the same results. */
+ * unit in the level filter (8, 16, 32), threads per block of the level
+ * kernels (64, 128, 256; 0 keeps the defaults 8, 32, 256) and the level
+ * queue (0: one warp per 32-row chunk; 1: a persistent grid whose warps take
+ * chunks by ticket, largest candidates first in COLO_MODE_LEARNED).  Every
+ * setting gives the same results. */
 typedef struct {
     int32_t join_group;
     int32_t filter_unit;
     int32_t level_block;
+    int32_t level_queue;
     int32_t from_cache;      /* colo_autotune_all: 1 when the shapes came from the cache file */
 } colo_tuning;
-/* Tunes all three for this dataset and parameters and keeps them for later
- * mines on this context: the join as colo_autotune does, then the filter unit
- * and the level block size from the CUDA-event time of their own kernels in
- * whole mines.  cache_path (optional) is a text file of tuned shapes keyed by
+/* Tunes all four for this dataset and parameters and keeps them for later
+ * mines on this context: the join as colo_autotune does, then the filter unit,
+ * the level block size and the level queue from the CUDA-event time of their
+ * own kernels in whole mines.  cache_path (optional) is a text file of tuned shapes keyed by
  * (points, features, occupied cells, R, SM count): a key found there is
  * applied without timing; a new key is appended.  out (optional) receives
  * the shapes. */

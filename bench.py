@@ -58,6 +58,44 @@ def workload_name(cfg: int, scale: float, n: int) -> str:
 JOBS_WORKLOAD = ("512 independent jobs, 2k-400k points each (log-uniform), 8-32 features, "
                  "R = 3 x mean spacing x U[0.5, 2], PI in {0.1, 0.2, 0.3}")
 PEAKS = ROOT / "MEASURED_PEAKS.json"
+L2_BYTES = 129 * 1000 * 1000   # GB300 L2
+
+
+def l2_note(input_bytes: int) -> str:
+    """How the timed steps treat L2 (StepTimer's rule), for the JSON line's config."""
+    if input_bytes < L2_BYTES:
+        return f"inputs (x, y f32: {input_bytes / 1e6:.1f} MB) fit in L2 (129 MB): 256 MB written between timed steps"
+    return f"inputs (x, y f32: {input_bytes / 1e6:.0f} MB) larger than L2 (129 MB); no flush"
+
+
+class StepTimer:
+    """Per-step CUDA events on the library's stream, summed over the timed steps.  When a step's
+    inputs fit in L2 (`input_bytes` < 129 MB) a 256 MB device write between steps, outside the
+    events, flushes L2 so no step starts on inputs the previous one left cached."""
+
+    def __init__(self, torch, dev, stream, input_bytes: int):
+        self.torch, self.stream = torch, stream
+        self.flush = input_bytes < L2_BYTES
+        self.buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if self.flush else None
+        self.pairs = []
+
+
+    def step(self, fn):
+        """Runs fn() as one timed step; returns its result."""
+        torch = self.torch
+        if self.flush:
+            with torch.cuda.stream(self.stream):
+                self.buf.fill_(len(self.pairs) & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(self.stream)
+        out = fn()
+        e1.record(self.stream)
+        self.pairs.append((e0, e1))
+        return out
+
+    def ms(self) -> float:
+        """Total of the steps' times (after a synchronize)."""
+        return sum(a.elapsed_time(b) for a, b in self.pairs)
 
 
 def dist_env():
@@ -139,8 +177,8 @@ def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
         return 24.0 * Rn * launches
     if name == "cell_keys":        # read x, y, feature; write key, id
         return 24.0 * N
-    if name == "gather_sorted":    # read the sorted ids, gather x, y, feature, write them in cell order
-        return 28.0 * N
+    if name == "gather_sorted":    # read the sorted ids and keys, gather x, y, write x, y, feature in cell order
+        return (28.0 + kb) * N
     if name == "cell_neighbours":  # read the key, write 9 neighbour indices
         return 44.0 * M
     if name == "quad_masks":       # read 9 indices + masks, write 4 quad masks + the 3x3 union
@@ -159,8 +197,8 @@ def algorithmic_bytes(name: str, c: dict, launches: float, words: int) -> float:
         return 4.0 * c["bitmap_words"]
     if name == "filter_pairs":
         return 8.0 * Rn + 4.0 * words * M
-    if name == "filter_level":     # per item the driver cell's 4 quad masks; per (cell of U_c, member) one run
-        return 16.0 * words * c["filter_items"] + 8.0 * c["filter_cell_members"]
+    if name == "filter_level":     # B_c: a 4-byte count per (cell of U_c, member) run read
+        return 4.0 * c["filter_cell_members"]
     return 0.0
 
 
@@ -298,20 +336,19 @@ def bench_jobs(args, rank, world, local, dist):
         return ctx.mine_batch(dss, ps)
 
     out = {}
+    in_bytes = 8 * int(sum(w.n for w in jobs))
     for form in ("batched", "plain"):
         for _ in range(args.warmup):
             run(form)
         if dist:
             dist.barrier()
         torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        tm = StepTimer(torch, dev, stream, in_bytes)
         res = None
         for _ in range(args.steps):
-            res = run(form)
-        e1.record(stream)
+            res = tm.step(lambda: run(form))
         torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1)
+        ms = tm.ms()
         total, ms = replicas.aggregate(dist, sum(r.num_candidates() for r in res) * args.steps, ms, dev)
         out[form] = (ms, res, total)
     cands = sum(r.num_candidates() for r in out["batched"][1])
@@ -325,7 +362,8 @@ def bench_jobs(args, rank, world, local, dist):
             "data": "synthetic (seeded generator)",
             "config": {"workload": JOBS_WORKLOAD,
                        "points": int(sum(w.n for w in jobs)), "jobs": len(jobs), "candidates_per_step": cands,
-                       "form": "batched+learned" if mode == colo.MODE_LEARNED else "batched"},
+                       "form": "batched+learned" if mode == colo.MODE_LEARNED else "batched",
+                       "l2": l2_note(in_bytes)},
             "plain": {"value": out["plain"][2] / (ms_p / 1e3), "unit": "candidates/s",
                       "ms_per_step": ms_p / args.steps},
             "headline_vs_plain": ms_p / ms_b, "identical_patterns_all_forms": same,
@@ -343,30 +381,28 @@ def side_configs(ctx, dev, stream, head_mode, steps: int = 3, warmup: int = 1, c
     import oracle
     from colo import gen
 
-    def timed(run):
+    def timed(run, in_bytes):
         for _ in range(warmup):
             run()
         torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        tm = StepTimer(torch, dev, stream, in_bytes)
         res = None
         for _ in range(steps):
-            res = run()
-        e1.record(stream)
+            res = tm.step(run)
         torch.cuda.synchronize(dev)
-        return e0.elapsed_time(e1) / steps, res
+        return tm.ms() / steps, res
 
     out = {}
     for cfg in (0, 1):
         wl = gen.config(cfg)
         ds = colo.Dataset.from_arrays(ctx, wl.x, wl.y, wl.fid, wl.bounds)
         ds.upload()
-        r = {"workload": f"config{cfg}", "points": wl.n}
+        r = {"workload": f"config{cfg}", "points": wl.n, "l2": l2_note(8 * wl.n)}
         pats = None
         same = True
         for name, mode in (("headline", head_mode), ("plain", colo.MODE_PLAIN)):
             prm = colo.default_params(wl.R, wl.thr, mode, max_size=wl.max_size)
-            ms, res = timed(lambda: ctx.mine(ds, prm))
+            ms, res = timed(lambda: ctx.mine(ds, prm), 8 * wl.n)
             c = res.num_candidates()
             r[name] = {"ms_per_step": round(ms, 4), "candidates_per_s": c / (ms / 1e3), "candidates": c}
             same &= pats is None or res.patterns() == pats
@@ -387,10 +423,12 @@ def side_configs(ctx, dev, stream, head_mode, steps: int = 3, warmup: int = 1, c
         d.upload()
     hp = [colo.default_params(w.R, w.thr, head_mode, max_size=w.max_size) for w in jobs]
     pp = [colo.default_params(w.R, w.thr, colo.MODE_PLAIN, max_size=w.max_size) for w in jobs]
-    ms_b, rb = timed(lambda: ctx.mine_batch(dss, hp))
-    ms_p, rp = timed(lambda: [ctx.mine(d, p) for d, p in zip(dss, pp)])
+    jb = 8 * int(sum(w.n for w in jobs))
+    ms_b, rb = timed(lambda: ctx.mine_batch(dss, hp), jb)
+    ms_p, rp = timed(lambda: [ctx.mine(d, p) for d, p in zip(dss, pp)], jb)
     cands = sum(x.num_candidates() for x in rb)
     out["config2"] = {"workload": JOBS_WORKLOAD, "points": int(sum(w.n for w in jobs)), "jobs": len(jobs),
+                      "l2": l2_note(jb),
                       "headline": {"ms_per_step": round(ms_b, 3), "candidates_per_s": cands / (ms_b / 1e3),
                                    "candidates": cands},
                       "plain": {"ms_per_step": round(ms_p, 3), "candidates_per_s": cands / (ms_p / 1e3)},
@@ -473,17 +511,14 @@ def main():
             ctx.mine(ds, params)
         results = []
         barrier_sync()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+        tm = StepTimer(torch, dev, stream, 8 * wl.n)
         with ClockSampler(local) as clk:
-            e0.record(stream)
             for _ in range(args.steps):
                 if not resident:
                     ds.evict()
-                results.append(ctx.mine(ds, params))
-            e1.record(stream)
+                results.append(tm.step(lambda: ctx.mine(ds, params)))
             barrier_sync()
-        ms = e0.elapsed_time(e1)
+        ms = tm.ms()
         units = sum(r.num_candidates() for r in results)
         total, ms = replicas.aggregate(dist, units, ms, dev)   # all ranks' candidates, slowest rank's time
         return ms, results, clk.summary(), total
@@ -578,7 +613,7 @@ def main():
                    "filter_items": int(counters["filter_items"]), "filter_full_quads": int(counters["filter_full_quads"]),
                    "filter_cells": int(counters["filter_cells"]),
                    "form": "batched+learned" if head_mode == colo.MODE_LEARNED else "batched",
-                   "l2": "inputs (x, y f32: 160 MB) larger than L2 (129 MB); no flush",
+                   "l2": l2_note(8 * wl.n),
                    "parallelism": f"replicas x{world}", "autotuned": tuned},
         "e2e": {"value": e2e, "unit": "candidates/s", "ms_per_step": ms_e / args.steps,
                 "h2d_bytes_per_step": int(res_e[0].counters["h2d_bytes"]),

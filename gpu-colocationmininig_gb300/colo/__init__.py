@@ -41,7 +41,7 @@ EXPORTS = [
     "colo_result_level", "colo_result_table", "colo_result_write_patterns", "colo_result_times",
     "colo_result_counters", "colo_result_free", "colo_stage_cells", "colo_stage_neighbors",
     "colo_stage_filter", "colo_stage_sqdist", "colo_result_num_kernels", "colo_result_kernel", "colo_ctx_stream",
-    "colo_stage_within", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
+    "colo_stage_within", "colo_stage_scan", "colo_table_pi_static", "colo_model_forward", "colo_model_grad", "colo_model_train",
     "colo_ctx_set_model", "colo_result_features", "colo_autotune", "colo_dataset_from_csv_threads",
     "colo_dataset_write_binary", "colo_dataset_from_binary", "colo_csv_to_binary", "colo_stage_apriori",
     "colo_dataset_from_csv_device", "colo_set_join_group", "colo_autotune_all", "colo_set_tuning",
@@ -131,6 +131,7 @@ def load(build: bool = True) -> C.CDLL:
         "colo_stage_filter": (C.c_int, [_P, _P, C.c_float, C.c_float, _u32p, C.c_uint64, C.c_uint32, _u64p, _u8p]),
         "colo_stage_sqdist": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, _f32p]),
         "colo_stage_within": (C.c_int, [_P, _f32p, _f32p, _f32p, _f32p, C.c_uint64, C.c_float, _f32p, _u8p]),
+        "colo_stage_scan": (C.c_int, [_P, _P, C.c_uint64, C.c_int, _u64p, _u64p]),
         "colo_table_pi_static": (C.c_int, [_P, C.c_uint64, C.c_uint32, _u32p, _u32p, _P, _P, _P]),
         "colo_stage_apriori": (C.c_int, [_P, _u32p, C.c_uint64, C.c_uint32, _u32p, _u32p, C.c_uint64, _u64p]),
         "colo_model_forward": (C.c_int, [_P, _f32p, _f32p, C.c_uint64, _f32p]),
@@ -414,6 +415,18 @@ class Context:
         self.check(self.lib.colo_stage_sqdist(self.h, *[_ptr(v, _f32p) for v in a], len(out), _ptr(out, _f32p)),
                    "stage_sqdist")
         return out
+
+    def stage_scan(self, values) -> tuple[np.ndarray, int]:
+        """Exclusive scan of uint32 or uint64 values on the device: (offsets as uint64, total)."""
+        v = np.ascontiguousarray(values)
+        if v.dtype not in (np.uint32, np.uint64):
+            raise TypeError("stage_scan takes uint32 or uint64 values")
+        out = np.zeros(max(len(v), 1), np.uint64)
+        tot = C.c_uint64(0)
+        self.check(self.lib.colo_stage_scan(self.h, v.ctypes.data_as(_P) if len(v) else None, len(v),
+                                            1 if v.dtype == np.uint64 else 0, _ptr(out, _u64p), C.byref(tot)),
+                   "stage_scan")
+        return out[: len(v)], int(tot.value)
 
     def stream(self) -> int:
         return int(self.lib.colo_ctx_stream(self.h) or 0)

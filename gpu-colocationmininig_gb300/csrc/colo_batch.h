@@ -81,6 +81,7 @@ struct Batch {
     // (feature, neighbour cell, id) order
     DevBuf<uint64_t> nb_beg;
     DevBuf<uint32_t> nb_cnt, nb;
+    DevBuf<uint32_t> act_pos;        // sorted positions of the join's active anchors (cell order)
     uint64_t E = 0;              // neighbour entries (UINT64_MAX: still on the device in dE)
     DevBuf<unsigned long long> dE;
     uint64_t nb_cap = 0;         // allocated entries (upper bound in single-pass mode)
@@ -107,11 +108,10 @@ uint64_t neighbor_entries(Batch& b);     // E (waits for the device sum once)
 void apriori_device(cudaStream_t s, const std::vector<const std::vector<uint32_t>*>& prev, uint32_t km1,
                     std::vector<std::vector<uint32_t>>& out, std::vector<std::vector<uint32_t>>& parent);
 // colo_filter.cu
-// Driver lists: per-feature cell counts into d_cnt (F entries, zeroed by the
-// caller); the lists themselves are filled by the level filters for the
-// features their candidates have (a level's candidates only have members of
-// the previous level's, so the first level filter fills them all).
-void driver_lists_count(Batch& b, uint32_t* d_cnt);
+// Driver lists: their sizes are counted by the quad masks' kernel; the lists
+// themselves are filled by the level filters for the drivers of their
+// candidates (a level whose drivers are not all filled yet fills the union of
+// the old and new ones).
 // Level-2 upper bounds of every pair of every job: ub2[job_off[j] + lf*Fj + lg] is the
 // bound of feature lf's side of pair {lf, lg}.  job_off has J+1 entries.
 // Runs on stream s (no wait at the end).
@@ -156,6 +156,11 @@ struct LevelWork {
 // bitmaps + rows at their count-and-fill positions (overflow recorded per
 // candidate; a look-back that waits too long sets the batch's timeout flag).
 void level_count(Batch& b, const LevelWork& w, uint32_t k);
+// Level 2's count pass per anchor: d_cid[d_cid_off[j] + lf * nf_j + lg] is the index
+// in d_cands of pair (lf, lg) of job j (0xFFFFFFFF: not refined); the candidates'
+// slots must be zero.
+void level_pairs_count(Batch& b, const CandDesc* d_cands, uint64_t ncand, const uint64_t* d_cid_off,
+                       const uint32_t* d_cid, unsigned long long* d_items);
 void level_fill(Batch& b, const LevelWork& w, uint32_t k);
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow);
 // Participation statistics per candidate and member: [A, last, first, full]

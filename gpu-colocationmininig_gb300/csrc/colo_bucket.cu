@@ -16,17 +16,6 @@ namespace {
 // Cell keys, point ids and packed coordinates, and the digit histograms of
 // every radix pass over the keys (block-private counts added to hist once
 // per block), so the sort does not read the keys again to count them.
-// A point's feature is the last feature whose first point is at or before it
-// (points are grouped by feature); the start table stays in L1.
-__device__ __forceinline__ uint32_t feature_of(uint32_t id, uint32_t F, const uint32_t* __restrict__ fstart) {
-    uint32_t lo = 0, hi = F;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (fstart[mid] <= id) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
 
 template <class KT>
 __global__ void __launch_bounds__(256) k_cell_keys(
@@ -70,19 +59,6 @@ __global__ void __launch_bounds__(256) k_cell_keys(
     }
 }
 
-// Sorted copies: coordinates gathered as one 8-byte load; the feature of a
-// point id is found in the feature start table (points are grouped by
-// feature), which stays in L1.
-__global__ void k_gather_sorted(uint64_t n, uint32_t F, const uint32_t* __restrict__ sid,
-                                const float2* __restrict__ xy, const uint32_t* __restrict__ fstart,
-                                float2* __restrict__ sxy, uint32_t* __restrict__ sfeat) {
-    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    const uint32_t id = sid[p];
-    sxy[p] = xy[id];
-    sfeat[p] = feature_of(id, F, fstart);
-}
-
 // Cell and run heads in the sorted order, counted and compacted in two
 // passes over the keys (no flag arrays).  A 2048-point tile is eight warp
 // segments of 256 points; a warp reads its segment 32 consecutive points at a
@@ -115,18 +91,49 @@ __device__ __forceinline__ void head_ballots(uint64_t seg, uint64_t n, const KT*
     }
 }
 
+// Sorted copies and pass 1 of the heads in one pass: per point its
+// coordinates (one 8-byte gather) and feature (from the feature start table,
+// points being grouped by feature; it stays in L1), and per tile the cell
+// and run head counts.  A point's predecessor comes from the lane before it
+// (lane 0 reads it).  An id outside the points (only after a sort that timed
+// out; the host then stops the mine) reads point 0.
 template <class KT>
-__global__ void __launch_bounds__(kHeadThreads) k_head_tiles(uint64_t n, const KT* __restrict__ keys,
-                                                            const uint32_t* __restrict__ sfeat,
-                                                            uint64_t* __restrict__ partial) {
+__global__ void __launch_bounds__(kHeadThreads) k_gather_heads(uint64_t n, uint32_t F, const KT* __restrict__ keys,
+                                                              const uint32_t* __restrict__ sid,
+                                                              const float2* __restrict__ xy,
+                                                              const uint32_t* __restrict__ fstart,
+                                                              float2* __restrict__ sxy, uint32_t* __restrict__ sfeat,
+                                                              uint64_t* __restrict__ partial) {
     __shared__ uint64_t s_tot[kHeadWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t seg = (uint64_t)blockIdx.x * kHeadTile + (uint64_t)w * (32 * kHeadRounds);
-    uint32_t chb[kHeadRounds], rhb[kHeadRounds];
-    head_ballots(seg, n, keys, sfeat, lane, chb, rhb);
     uint64_t v = 0;
 #pragma unroll
-    for (int r = 0; r < kHeadRounds; ++r) v += ((uint64_t)__popc(chb[r]) << 32) + (uint64_t)__popc(rhb[r]);
+    for (int r = 0; r < kHeadRounds; ++r) {
+        const uint64_t p = seg + (uint64_t)r * 32 + lane;
+        const bool in = p < n;
+        KT key = 0;
+        uint32_t f = 0;
+        if (in) {
+            uint32_t id = sid[p];
+            if (id >= n) id = 0;
+            sxy[p] = xy[id];
+            f = feature_of(id, F, fstart);
+            sfeat[p] = f;
+            key = keys[p];
+        }
+        KT pkey = __shfl_up_sync(0xffffffffu, key, 1);
+        uint32_t pf = __shfl_up_sync(0xffffffffu, f, 1);
+        if (lane == 0 && in && p > 0) {
+            uint32_t pid = sid[p - 1];
+            if (pid >= n) pid = 0;
+            pkey = keys[p - 1];
+            pf = feature_of(pid, F, fstart);
+        }
+        const bool ch = in && (p == 0 || pkey != key);
+        const bool rh = ch || (in && pf != f);
+        v += ((uint64_t)__popc(__ballot_sync(0xffffffffu, ch)) << 32) + (uint64_t)__popc(__ballot_sync(0xffffffffu, rh));
+    }
     if (lane == 0) s_tot[w] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -336,84 +343,132 @@ __device__ __forceinline__ void st_row(uint32_t* __restrict__ p, const uint32_t 
 
 constexpr int kQuadThreads = 128;
 
+// Features a block of cells counts in shared memory for the driver-list sizes
+// (larger batches count with global atomics).
+constexpr uint32_t kQuadHist = 1024;
+
+// Per cell: the four quad masks and the 3x3 mask (nbmask), the queue of cells
+// that need a neighbourhood run list, and the driver-list sizes: dcnt[f] =
+// cells whose 3x3 mask holds f.  A block walks 128 cells at a time over a
+// strided range and keeps one histogram for all of them (one global atomic per
+// feature per block at the end); a warp's 32 cells are counted by a bit
+// transpose (lane b holds feature b's column of the warp's cell x feature
+// matrix and adds its popcount).
 template <int WT>
 __global__ void __launch_bounds__(kQuadThreads) k_quad_masks(
     uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
     const JobGrid* __restrict__ grids, const int32_t* __restrict__ nb9, const uint32_t* __restrict__ cmask,
     uint32_t* __restrict__ qmask, uint32_t* __restrict__ nbmask, uint32_t* __restrict__ listq,
-    uint32_t* __restrict__ nlistq) {
-    const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool above = false;
-    if (c < M) {
-        const JobGrid g = grids[cjob[c]];
-        const uint64_t local = ckey[c] - g.key_base;
-        const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
-        int32_t nb[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) nb[q] = nb9[c * 9 + q];
-        uint32_t m[9][WT];
+    uint32_t* __restrict__ nlistq, uint32_t F, uint32_t* __restrict__ dcnt) {
+    __shared__ uint32_t s_hist[kQuadHist];
+    __shared__ uint32_t s_cnt[kQuadThreads / 32], s_base;
+    const bool local_hist = F <= kQuadHist;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (local_hist)
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) s_hist[i] = 0;
+    __syncthreads();
+    for (uint64_t c0 = (uint64_t)blockIdx.x * kQuadThreads; c0 < M; c0 += (uint64_t)gridDim.x * kQuadThreads) {
+        const uint64_t c = c0 + threadIdx.x;
+        bool above = false;
         uint32_t all[WT];
 #pragma unroll
         for (int w = 0; w < WT; ++w) all[w] = 0;
+        uint32_t f0 = 0;
+        if (c < M) {
+            const JobGrid g = grids[cjob[c]];
+            f0 = g.f0;
+            const uint64_t local = ckey[c] - g.key_base;
+            const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+            int32_t nb[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            if (nb[q] >= 0) {
-                ld_row<WT>(cmask + (uint64_t)nb[q] * WT, m[q]);
+            for (int q = 0; q < 9; ++q) nb[q] = nb9[c * 9 + q];
+            uint32_t m[9][WT];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                if (nb[q] >= 0) {
+                    ld_row<WT>(cmask + (uint64_t)nb[q] * WT, m[q]);
+                } else {
+#pragma unroll
+                    for (int w = 0; w < WT; ++w) m[q][w] = 0;
+                }
+#pragma unroll
+                for (int w = 0; w < WT; ++w) all[w] |= m[q][w];
+            }
+            st_row<WT>(nbmask + c * WT, all);
+            // the cell needs a neighbourhood run list when its 3x3 block holds a
+            // feature above its own lowest one (m[4] is the cell's own mask; the block
+            // is the union over all nine slots, a superset of the adjacent cells):
+            // such cells are queued for the list kernels
+            bool seen = false;
+#pragma unroll
+            for (int w = 0; w < WT; ++w) {
+                const uint32_t own = m[4][w];
+                if (seen) {
+                    above |= all[w] != 0;
+                } else if (own) {
+                    seen = true;
+                    const uint32_t low = own & (0u - own);
+                    above |= (all[w] & ~((low << 1) - 1u)) != 0;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
+                const int64_t bx = cx + qx, by = cy + qy;
+                const bool valid = bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy;
+                uint32_t qm[WT];
+#pragma unroll
+                for (int w = 0; w < WT; ++w)
+                    qm[w] = valid ? (m[(qy + 1) * 3 + qx + 1][w] | m[(qy + 1) * 3 + qx + 2][w] |
+                                     m[(qy + 2) * 3 + qx + 1][w] | m[(qy + 2) * 3 + qx + 2][w])
+                                  : 0u;
+                st_row<WT>(qmask + (c * 4 + q) * WT, qm);
+            }
+        }
+        // driver-list sizes (lanes of another job than lane 0's, at job boundaries of a
+        // batch, count one bit at a time)
+        {
+            const uint32_t fl = __shfl_sync(0xffffffffu, f0, 0);
+            if (__all_sync(0xffffffffu, c >= M || f0 == fl)) {
+#pragma unroll
+                for (int w = 0; w < WT; ++w) {
+                    if (!__any_sync(0xffffffffu, all[w])) continue;
+                    const uint32_t n = __popc(warp_transpose32(all[w]));
+                    if (n) {
+                        const uint32_t f = fl + (uint32_t)w * 32 + (uint32_t)lane;
+                        if (local_hist) atomicAdd(&s_hist[f], n);
+                        else atomicAdd(&dcnt[f], n);
+                    }
+                }
             } else {
 #pragma unroll
-                for (int w = 0; w < WT; ++w) m[q][w] = 0;
-            }
-#pragma unroll
-            for (int w = 0; w < WT; ++w) all[w] |= m[q][w];
-        }
-        st_row<WT>(nbmask + c * WT, all);
-        // the cell needs a neighbourhood run list when its 3x3 block holds a
-        // feature above its own lowest one (m[4] is the cell's own mask; the block
-        // is the union over all nine slots, a superset of the adjacent cells):
-        // such cells are queued for the list kernels
-        bool seen = false;
-#pragma unroll
-        for (int w = 0; w < WT; ++w) {
-            const uint32_t own = m[4][w];
-            if (seen) {
-                above |= all[w] != 0;
-            } else if (own) {
-                seen = true;
-                const uint32_t low = own & (0u - own);
-                above |= (all[w] & ~((low << 1) - 1u)) != 0;
+                for (int w = 0; w < WT; ++w)
+                    for (uint32_t bits = all[w]; bits; bits &= bits - 1)
+                        atomicAdd(&dcnt[f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1)], 1u);
             }
         }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int qx = (q & 1) - 1, qy = (q >> 1) - 1;
-            const int64_t bx = cx + qx, by = cy + qy;
-            const bool valid = bx >= 0 && by >= 0 && bx + 2 <= (int64_t)g.gx && by + 2 <= (int64_t)g.gy;
-            uint32_t qm[WT];
-#pragma unroll
-            for (int w = 0; w < WT; ++w)
-                qm[w] = valid ? (m[(qy + 1) * 3 + qx + 1][w] | m[(qy + 1) * 3 + qx + 2][w] | m[(qy + 2) * 3 + qx + 1][w] |
-                                 m[(qy + 2) * 3 + qx + 2][w])
-                              : 0u;
-            st_row<WT>(qmask + (c * 4 + q) * WT, qm);
+        // one atomic per block and round for the queue
+        const uint32_t has = __ballot_sync(0xffffffffu, above);
+        if (lane == 0) s_cnt[wid] = (uint32_t)__popc(has);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < kQuadThreads / 32; ++w) {
+                const uint32_t v = s_cnt[w];
+                s_cnt[w] = t;
+                t += v;
+            }
+            s_base = t ? atomicAdd(nlistq, t) : 0u;
         }
+        __syncthreads();
+        if (above) listq[s_base + s_cnt[wid] + __popc(has & ((1u << lane) - 1u))] = (uint32_t)c;
+        __syncthreads();   // s_cnt and s_base are rewritten by the next round
     }
-    // one atomic per block for the queue
-    __shared__ uint32_t s_cnt[kQuadThreads / 32], s_base;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t has = __ballot_sync(0xffffffffu, above);
-    if (lane == 0) s_cnt[wid] = (uint32_t)__popc(has);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (int w = 0; w < kQuadThreads / 32; ++w) {
-            const uint32_t v = s_cnt[w];
-            s_cnt[w] = t;
-            t += v;
-        }
-        s_base = t ? atomicAdd(nlistq, t) : 0u;
+    if (local_hist) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
+            if (s_hist[i]) atomicAdd(&dcnt[i], s_hist[i]);
     }
-    __syncthreads();
-    if (above) listq[s_base + s_cnt[wid] + __popc(has & ((1u << lane) - 1u))] = (uint32_t)c;
 }
 
 // Runs per feature: a block-local histogram (F <= kHistMax), else global atomics.
@@ -721,24 +776,26 @@ void sort_and_compact(Batch& b) {
 
     b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);
-    {
-        KScope ks("gather_sorted");
-        k_gather_sorted<<<grid_for(n, 256), 256, 0, s>>>(n, b.F, b.sid.get(), b.xy.get(), b.fstart.get(),
-                                                         b.sxy.get(), b.sfeat.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
-    }
-
     const uint64_t tiles = (n + kHeadTile - 1) / kHeadTile;
     DevBuf<uint64_t> part;
     part.alloc(tiles + 1, s);
     uint64_t totals = 0;
     {
-        KScope ks("cell_compact");
-        k_head_tiles<KT><<<(unsigned)tiles, kHeadThreads, 0, s>>>(n, keys.get(), b.sfeat.get(), part.get());
+        KScope ks("gather_sorted");
+        k_gather_heads<KT><<<(unsigned)tiles, kHeadThreads, 0, s>>>(n, b.F, keys.get(), b.sid.get(), b.xy.get(),
+                                                                   b.fstart.get(), b.sxy.get(), b.sfeat.get(),
+                                                                   part.get());
         COLO_LAUNCH_CHECK();
         count_launch();
+    }
+    {
+        KScope ks("cell_compact");
+        // the sort's timeout word comes back with the totals: after a timeout the keys are not
+        // a sorted permutation, and nothing past this point may read them
+        uint32_t sort_err = 0;
+        COLO_CUDA(cudaMemcpyAsync(&sort_err, &b.flags.get()->timeout, 4, cudaMemcpyDeviceToHost, s));
         scan_partials_u64(part.get(), tiles, s, &totals);
+        if (sort_err) throw StatusError{COLO_ERR_TIMEOUT, "radix sort: a tile waited too long for its predecessors"};
     }
     const uint32_t M = (uint32_t)(totals >> 32), Rn = (uint32_t)totals;
     b.M = M;
@@ -808,12 +865,23 @@ void bucket_points(Batch& b) {
     b.listq.alloc(M ? M : 1, s);
     b.nlistq.alloc(1, s);
     b.nlistq.zero(s);
+    // cells per driver list (3x3 blocks holding each feature), counted with the masks
+    DevBuf<uint32_t> dcnt;
+    dcnt.alloc(b.F ? b.F : 1, s);
+    dcnt.zero(s);
     {
         KScope ks("quad_masks");
-#define COLO_QM(WW)                                                                                    \
-    k_quad_masks<WW><<<grid_for(M, kQuadThreads), kQuadThreads, 0, s>>>(                              \
-        M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(),       \
-        b.nbmask.get(), b.listq.get(), b.nlistq.get())
+        // one wave of resident blocks (each keeps one histogram for all its cells)
+#define COLO_QM(WW)                                                                                          \
+    do {                                                                                                     \
+        int per_sm = 1;                                                                                      \
+        COLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_quad_masks<WW>, kQuadThreads, 0)); \
+        const unsigned qblocks = (unsigned)std::max<uint64_t>(                                               \
+            1, std::min<uint64_t>(grid_for(M, kQuadThreads), (uint64_t)b.sms * (uint64_t)std::max(per_sm, 1))); \
+        k_quad_masks<WW><<<qblocks, kQuadThreads, 0, s>>>(                                                   \
+            M, b.ckey.get(), b.cjob.get(), b.grids.get(), b.nb9.get(), b.cmask.get(), b.qmask.get(),         \
+            b.nbmask.get(), b.listq.get(), b.nlistq.get(), b.F, dcnt.get());                                 \
+    } while (0)
         switch (b.W) {
             case 1: COLO_QM(1); break;
             case 2: COLO_QM(2); break;
@@ -834,11 +902,6 @@ void bucket_points(Batch& b) {
         count_launch();
     }
 
-    // cells per driver list (3x3 blocks holding each feature)
-    DevBuf<uint32_t> dcnt;
-    dcnt.alloc(b.F ? b.F : 1, s);
-    dcnt.zero(s);
-    driver_lists_count(b, dcnt.get());
     // runs per feature
     {
         KScope ks("run_index");

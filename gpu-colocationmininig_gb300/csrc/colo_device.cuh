@@ -81,8 +81,38 @@ __device__ __forceinline__ uint32_t mask_rank(const uint32_t* __restrict__ m, ui
     return r + __popc(m[wq] & ((1u << (b & 31)) - 1u));
 }
 
+// A point's feature is the last feature whose first point is at or before it
+// (points are grouped by feature); the start table stays in L1.
+__device__ __forceinline__ uint32_t feature_of(uint32_t id, uint32_t F, const uint32_t* __restrict__ fstart) {
+    uint32_t lo = 0, hi = F;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (fstart[mid] <= id) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+// 32 x 32 bit transpose across a full warp: lane i holds row i (bit j =
+// column j); afterwards lane j holds column j (bit i = row i's bit j).  Five
+// block swaps of halving size: at size s, lanes without bit s take their
+// partner's low s-bit groups into their high ones, lanes with bit s the
+// partner's high groups into their low ones.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+    const uint32_t lane = threadIdx.x & 31;
+    constexpr uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const int s = 16 >> i;
+        const uint32_t m = masks[i];
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
+        x = (lane & (uint32_t)s) ? ((x & ~m) | ((y >> s) & m)) : ((x & m) | ((y & m) << s));
+    }
+    return x;
 }
 
 // Warp and block scans (one value per thread).

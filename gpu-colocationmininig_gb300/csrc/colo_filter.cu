@@ -138,86 +138,107 @@ __device__ __forceinline__ void load_row(const uint32_t* __restrict__ p, uint32_
 }
 
 // ---- driver lists -----------------------------------------------------------
-// Cells per feature f whose 3x3 block holds f (bit f of nbmask): a block-local
-// histogram when the batch has at most kDilHist features, else global atomics.
-// A block owns `per` consecutive cells and its lanes take them from 32
-// far-apart stretches: neighbouring cells share their features, and lanes of
-// one warp adding to the same counter would serialise.
-constexpr uint32_t kDilHist = 4096;
+// The list of feature f holds the cells whose 3x3 block holds f (bit f of
+// nbmask); the lists of the wanted features (the level drivers) are filled
+// here, their sizes come from the quad masks' kernel.  A block owns a range of
+// consecutive cells and walks it twice, 256 cells (one per thread) at a time.
+// A warp's 32 cells are a bit matrix (cell x feature) per mask word;
+// transposed, lane b holds feature b's column.  Pass 0 adds the columns'
+// popcounts to a block histogram; one global atomic per (block, feature) then
+// reserves the block's range of each list; pass 1 adds them again, the
+// atomic's old value placing the warp's cells in that range, and lane b
+// writes its column's cells.  Order within a list is not fixed (the level
+// filter sums over it).  Batches with more than kDilHist features skip the
+// histogram: one global atomic per (warp, feature).
+constexpr uint32_t kDilHist = 2048;
+constexpr int kDilThreads = 256;
 
-// fn(z, f) for every feature f of cell z's 3x3 block that is in the want bitset.
-template <int WT, class Fn>
-__device__ __forceinline__ void dil_cells(uint64_t z0, uint64_t z1, const uint32_t* __restrict__ cjob,
-                                          const JobGrid* __restrict__ grids, const uint32_t* __restrict__ nbmask,
-                                          const uint32_t* __restrict__ want, Fn&& fn) {
-    const uint64_t n = z1 > z0 ? z1 - z0 : 0;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint64_t stretch = (n + 31) / 32;   // lane l walks cells z0 + l*stretch + i
-    for (uint64_t i = warp; i < stretch; i += nw) {
-        const uint64_t z = z0 + (uint64_t)lane * stretch + i;
-        if (z >= z1) continue;
-        uint32_t row[WT];
-        load_row<WT>(nbmask + z * WT, row);
-        const uint32_t f0 = grids[cjob ? cjob[z] : 0u].f0;
+// Bits of cell z's mask word w that are wanted: the want bitset (global
+// features) taken from bit f0 + 32 w on.  The bitset holds one spare word.
+__device__ __forceinline__ uint32_t dil_wanted(const uint32_t* __restrict__ want, uint32_t f0, int w, uint32_t row) {
+    const uint32_t p = f0 + (uint32_t)w * 32;
+    const uint32_t lo = __ldg(want + (p >> 5)), hi = __ldg(want + (p >> 5) + 1);
+    return row & __funnelshift_r(lo, hi, p & 31);
+}
+
+template <int WT>
+__global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t per, const uint32_t* __restrict__ cjob,
+                                                          const JobGrid* __restrict__ grids,
+                                                          const uint32_t* __restrict__ nbmask, uint32_t F,
+                                                          const uint64_t* __restrict__ doff,
+                                                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ dlist,
+                                                          const uint32_t* __restrict__ want) {
+    __shared__ unsigned long long s_base[kDilHist];
+    __shared__ uint32_t s_cnt[kDilHist], s_touch[kDilHist], s_nt;
+    const bool local = F <= kDilHist;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
+    if (local)
+        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) s_cnt[i] = 0;
+    if (threadIdx.x == 0) s_nt = 0;
+    __syncthreads();
+    for (int pass = local ? 0 : 1; pass < 2; ++pass) {
+        for (uint64_t t0 = z0; t0 < z1; t0 += kDilThreads) {
+            const uint64_t z = t0 + threadIdx.x;
+            const uint64_t zw = t0 + (threadIdx.x & ~31u);   // the warp's first cell
+            uint32_t row[WT];
+            uint32_t f0 = 0;
+            if (z < z1) {
+                f0 = grids[cjob ? cjob[z] : 0u].f0;
+                load_row<WT>(nbmask + z * WT, row);
 #pragma unroll
-        for (int w = 0; w < WT; ++w)
-            for (uint32_t bits = row[w]; bits; bits &= bits - 1) {
-                const uint32_t f = f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1);
-                if (!want || (__ldg(want + (f >> 5)) >> (f & 31) & 1u)) fn(z, f);
+                for (int w = 0; w < WT; ++w)   // a nonzero word lies below F, so its bitset words exist
+                    if (row[w]) row[w] = dil_wanted(want, f0, w, row[w]);
+            } else {
+#pragma unroll
+                for (int w = 0; w < WT; ++w) row[w] = 0;
             }
+            const uint32_t fl = __shfl_sync(0xffffffffu, f0, 0);
+            if (!__all_sync(0xffffffffu, z >= z1 || f0 == fl)) {
+                // the warp straddles a job boundary (batches of several jobs): in pass 1 every
+                // lane writes its own entries, one global atomic each
+#pragma unroll
+                for (int w = 0; w < WT; ++w) {
+                    if (pass == 1)
+                        for (uint32_t bits = row[w]; bits; bits &= bits - 1) {
+                            const uint32_t f = f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1);
+                            dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z;
+                        }
+                    row[w] = 0;
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < WT; ++w) {
+                if (!__any_sync(0xffffffffu, row[w])) continue;
+                const uint32_t col = warp_transpose32(row[w]);
+                const uint32_t n = __popc(col);
+                if (!n) continue;
+                const uint32_t f = fl + (uint32_t)w * 32 + lane;
+                uint64_t o;
+                if (local) {
+                    const uint32_t old = atomicAdd(&s_cnt[f], n);
+                    if (pass == 0) {
+                        if (old == 0) s_touch[atomicAdd(&s_nt, 1u)] = f;
+                        continue;
+                    }
+                    o = s_base[f] + old;
+                } else {
+                    o = doff[f] + atomicAdd(&cursor[f], n);
+                }
+                for (uint32_t bits = col; bits; bits &= bits - 1) dlist[o++] = (uint32_t)(zw + (uint32_t)(__ffs(bits) - 1));
+            }
+        }
+        if (pass == 0) {   // reserve the block's ranges; pass 1 counts again from zero
+            __syncthreads();
+            const uint32_t nt = s_nt;
+            for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
+                const uint32_t f = s_touch[i];
+                s_base[f] = doff[f] + atomicAdd(&cursor[f], s_cnt[f]);
+                s_cnt[f] = 0;
+            }
+            __syncthreads();
+        }
     }
-}
-
-template <int WT>
-__global__ void __launch_bounds__(256) k_dil_count(uint64_t M, uint64_t per, const uint32_t* __restrict__ cjob,
-                                                   const JobGrid* __restrict__ grids,
-                                                   const uint32_t* __restrict__ nbmask, uint32_t F,
-                                                   uint32_t* __restrict__ cnt) {
-    extern __shared__ uint32_t h[];
-    const bool local = F <= kDilHist;
-    if (local)
-        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
-    dil_cells<WT>(z0, z1, cjob, grids, nbmask, nullptr, [&](uint64_t, uint32_t f) {
-        if (local) atomicAdd(&h[f], 1u);
-        else atomicAdd(&cnt[f], 1u);
-    });
-    __syncthreads();
-    if (local)
-        for (uint32_t i = threadIdx.x; i < F; i += blockDim.x)
-            if (h[i]) atomicAdd(&cnt[i], h[i]);
-}
-
-// The same cells per block: count per feature, reserve one range per feature
-// in the lists, write the cells there.
-template <int WT>
-__global__ void __launch_bounds__(256) k_dil_fill(uint64_t M, uint64_t per, const uint32_t* __restrict__ cjob,
-                                                  const JobGrid* __restrict__ grids,
-                                                  const uint32_t* __restrict__ nbmask, uint32_t F,
-                                                  const uint64_t* __restrict__ doff, uint32_t* __restrict__ cursor,
-                                                  uint32_t* __restrict__ dlist, const uint32_t* __restrict__ want) {
-    extern __shared__ unsigned long long hb[];   // F bases, then F counters (32-bit)
-    uint32_t* hc = reinterpret_cast<uint32_t*>(hb + F);
-    const bool local = F <= kDilHist;
-    const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
-    if (!local) {
-        dil_cells<WT>(z0, z1, cjob, grids, nbmask, want,
-                      [&](uint64_t z, uint32_t f) { dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z; });
-        return;
-    }
-    for (uint32_t i = threadIdx.x; i < F; i += blockDim.x) hc[i] = 0;
-    __syncthreads();
-    dil_cells<WT>(z0, z1, cjob, grids, nbmask, want, [&](uint64_t, uint32_t f) { atomicAdd(&hc[f], 1u); });
-    __syncthreads();
-    for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
-        const uint32_t c = hc[f];
-        if (c) hb[f] = doff[f] + atomicAdd(&cursor[f], c);
-        hc[f] = 0;
-    }
-    __syncthreads();
-    dil_cells<WT>(z0, z1, cjob, grids, nbmask, want,
-                  [&](uint64_t z, uint32_t f) { dlist[hb[f] + atomicAdd(&hc[f], 1u)] = (uint32_t)z; });
 }
 
 // Level k >= 3 over the driver lists.  Candidates are grouped by driver
@@ -354,23 +375,6 @@ __global__ void __launch_bounds__(256, (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1))) k_filt
         default: throw StatusError{COLO_ERR_INTERNAL, "mask words not padded to a supported width"}; \
     }
 
-void driver_lists_count(Batch& b, uint32_t* d_cnt) {
-    if (b.M == 0 || b.F == 0) return;
-    cudaStream_t s = b.s;
-    const size_t smem = b.F <= kDilHist ? (size_t)b.F * 4 : 0;
-    uint64_t blocks = std::min<uint64_t>((b.M + 255) / 256, (uint64_t)b.sms * 4);
-    const uint64_t per = (b.M + blocks - 1) / blocks;
-    blocks = (b.M + per - 1) / per;
-    KScope ks("driver_lists");
-#define COLO_DC(WW)                                                                                             \
-    k_dil_count<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
-                                                        b.nbmask.get(), b.F, d_cnt)
-    COLO_W_SWITCH(b.W, COLO_DC)
-#undef COLO_DC
-    COLO_LAUNCH_CHECK();
-    count_launch();
-}
-
 namespace {
 
 // The lists of every feature in `need` (and of those already filled): the lists are filled
@@ -380,7 +384,7 @@ void driver_lists_fill(Batch& b, const std::vector<uint8_t>& need) {
     for (uint32_t f = 0; f < b.F; ++f) missing |= need[f] && !b.dlist_have[f];
     if (!missing) return;
     cudaStream_t s = b.s;
-    std::vector<uint32_t> want((b.F + 31) / 32, 0);
+    std::vector<uint32_t> want((b.F + 31) / 32 + 1, 0);   // one spare word for the kernel's funnel shift
     b.h_doff.assign(b.F + 1, 0);
     for (uint32_t f = 0; f < b.F; ++f) {
         b.dlist_have[f] |= need[f];
@@ -389,7 +393,7 @@ void driver_lists_fill(Batch& b, const std::vector<uint8_t>& need) {
     }
     const uint64_t total = b.h_doff[b.F];
     b.dlist.alloc(total ? total : 1, s);
-    b.doff.alloc(b.F + 1 + want.size() / 2 + 1, s);   // offsets, then the want bitset
+    b.doff.alloc(b.F + 1 + (want.size() + 1) / 2, s);   // offsets, then the want bitset
     uint32_t* d_want = reinterpret_cast<uint32_t*>(b.doff.get() + b.F + 1);
     COLO_CUDA(cudaMemcpyAsync(b.doff.get(), b.h_doff.data(), (b.F + 1) * 8, cudaMemcpyHostToDevice, s));
     COLO_CUDA(cudaMemcpyAsync(d_want, want.data(), want.size() * 4, cudaMemcpyHostToDevice, s));
@@ -397,16 +401,20 @@ void driver_lists_fill(Batch& b, const std::vector<uint8_t>& need) {
     DevBuf<uint32_t> cursor;
     cursor.alloc(b.F, s);
     cursor.zero(s);
-    const size_t smem = b.F <= kDilHist ? (size_t)b.F * 12 : 0;
-    if (smem > 48 * 1024) throw StatusError{COLO_ERR_INTERNAL, "driver-list histogram exceeds 48 KB"};
-    uint64_t blocks = std::min<uint64_t>((b.M + 255) / 256, (uint64_t)b.sms * 4);
-    const uint64_t per = (b.M + blocks - 1) / blocks;
-    blocks = (b.M + per - 1) / per;
+    // one range of consecutive cells per block (a multiple of 256 cells), one wave of resident blocks
     KScope ks("driver_lists");
-#define COLO_DF(WW)                                                                                           \
-    k_dil_fill<WW><<<(unsigned)blocks, 256, smem, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), \
-                                                       b.nbmask.get(), b.F, b.doff.get(), cursor.get(), b.dlist.get(), \
-                                                       d_want)
+#define COLO_DF(WW)                                                                                              \
+    do {                                                                                                         \
+        int per_sm = 1;                                                                                          \
+        COLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dil_fill<WW>, kDilThreads, 0));       \
+        uint64_t blocks = std::min<uint64_t>((b.M + kDilThreads - 1) / kDilThreads,                              \
+                                             (uint64_t)b.sms * (uint64_t)std::max(per_sm, 1));                   \
+        const uint64_t per = ((b.M + blocks - 1) / blocks + kDilThreads - 1) / kDilThreads * kDilThreads;        \
+        blocks = (b.M + per - 1) / per;                                                                          \
+        k_dil_fill<WW><<<(unsigned)blocks, kDilThreads, 0, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr,      \
+                                                               b.grids.get(), b.nbmask.get(), b.F, b.doff.get(), \
+                                                               cursor.get(), b.dlist.get(), d_want);             \
+    } while (0)
     COLO_W_SWITCH(b.W, COLO_DF)
 #undef COLO_DF
     COLO_LAUNCH_CHECK();
@@ -492,8 +500,8 @@ void filter_level(Batch& b, const uint32_t* h_cand, const uint32_t* h_job, uint6
     b.filter_items += nitems;
     if (nitems == 0) return;
     {
-        std::vector<uint8_t> need(b.F, 0);   // every member's list (drivers of this and later levels)
-        for (uint64_t c = 0; c < ncand * k; ++c) need[h_cand[c]] = 1;
+        std::vector<uint8_t> need(b.F, 0);   // the drivers' lists (a later level's new driver refills)
+        for (uint64_t c = 0; c < ncand; ++c) need[drv[c]] = 1;
         driver_lists_fill(b, need);
     }
     // groups (one per driver) and their units: 32 list cells x up to cu candidates

@@ -48,7 +48,7 @@ struct JobGrid {
 struct DevFlags {
     uint32_t out_of_grid;        // points whose cell is outside [0, total)
     uint32_t overflow;           // capacity overflows (learned presize)
-    uint32_t timeout;            // a bounded wait gave up
+    uint32_t timeout;            // a bounded wait gave up (the sort stores its failed pass + 1)
     uint32_t internal;           // consistency checks
 };
 

@@ -186,9 +186,11 @@ void join_neighbors(Batch& b) {
     const uint64_t U = ht[1];
     b.active_anchors = A;
     b.join_pairs = U;
-    DevBuf<uint32_t> act_pos, act_run;
-    act_pos.alloc(A, s);
-    act_run.alloc(A, s);
+    // the active anchors' sorted positions stay with the batch (level 2 walks their lists)
+    DevBuf<uint32_t>& act_pos = b.act_pos;
+    DevBuf<uint32_t> act_run;
+    act_pos.alloc(A ? A : 1, s);
+    act_run.alloc(A ? A : 1, s);
     if (A) {
         KScope ks("join_setup");
         k_expand_active<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rstart.get(), b.rcnt.get(), b.run_L.get(),

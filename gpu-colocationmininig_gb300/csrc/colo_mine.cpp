@@ -883,13 +883,37 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     COLO_CUDA(cudaStreamSynchronize(s));
                 }
             } else {
+                // pairs: counted per anchor (each list entry read once for the level) into
+                // zeroed slots, through a table from (job, pair) to candidate
+                const bool pairs = k == 2 && ns < ncand;
+                DevBuf<unsigned char> cidmem;
+                if (pairs) {
+                    std::vector<uint64_t> cid_off(J + 1, 0);
+                    for (uint32_t j = 0; j < J; ++j) cid_off[j + 1] = cid_off[j] + (uint64_t)js[j].nf * js[j].nf;
+                    std::vector<uint32_t> cid(cid_off[J], 0xFFFFFFFFu);
+                    for (uint64_t q = ns; q < ncand; ++q) {
+                        const JobState& st = js[hd[q].job];
+                        cid[cid_off[hd[q].job] + (uint64_t)(hd[q].m[0] - st.f0) * st.nf + (hd[q].m[1] - st.f0)] =
+                            (uint32_t)q;
+                    }
+                    const size_t o_cid = (J + 1) * 8;
+                    cidmem.alloc(o_cid + cid.size() * 4 + 4, s);
+                    COLO_CUDA(cudaMemcpyAsync(cidmem.get(), cid_off.data(), o_cid, cudaMemcpyHostToDevice, s));
+                    if (!cid.empty())
+                        COLO_CUDA(cudaMemcpyAsync(cidmem.get() + o_cid, cid.data(), cid.size() * 4,
+                                                  cudaMemcpyHostToDevice, s));
+                    COLO_CUDA(cudaMemsetAsync(ar.slots.get(), 0, nslots * 4, s));
+                }
                 if (ns) {
                     LevelWork w{ar.descs.get(), ar.chunk_off.get(), ns, nch_single, d_items.get()};
                     w.chunk_status = ar.status.get();
                     w.ticket = ar.status.get() + nch_single;
                     level_single(b, w, k, ar.overflow.get());
                 }
-                if (ns < ncand) {
+                if (pairs) {
+                    level_pairs_count(b, ar.descs.get(), ncand, reinterpret_cast<const uint64_t*>(cidmem.get()),
+                                      reinterpret_cast<const uint32_t*>(cidmem.get() + (J + 1) * 8), d_items.get());
+                } else if (ns < ncand) {
                     LevelWork w{ar.descs.get() + ns, ar.chunk_off.get() + ns + 1, ncand - ns, nch_count, d_items.get()};
                     w.ticket = ar.tickets.get();
                     level_count(b, w, k);

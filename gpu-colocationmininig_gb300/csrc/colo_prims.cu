@@ -12,25 +12,7 @@ thread_local KTimer* g_ktimer = nullptr;
 namespace {
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kScanThreads * kScanItems;
-
-// A tile of kScanTile items is eight warp segments of 256; a warp reads its
-// segment 32 consecutive items per round (coalesced loads and stores).
-template <class Tin, class Tout>
-__global__ void k_tile_sums(const Tin* __restrict__ in, uint64_t n, Tout* __restrict__ partial) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint64_t seg = (uint64_t)blockIdx.x * kScanTile + (uint64_t)w * (32 * kScanItems);
-    Tout s = 0;
-#pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-        const uint64_t p = seg + (uint64_t)i * 32 + lane;
-        if (p < n) s += (Tout)in[p];
-    }
-    Tout tot;
-    block_excl_scan<Tout>(s, &tot);
-    if (threadIdx.x == 0) partial[blockIdx.x] = tot;
-}
+constexpr int kScanItems = 8;   // per thread in the one-block partials scan
 
 // Single block: exclusive scan of partial[0..m) in place; partial[m] = total.
 template <class T>
@@ -57,31 +39,98 @@ __global__ void k_scan_partials(T* partial, uint64_t m) {
     if (threadIdx.x == 0) partial[m] = carry;
 }
 
+// Single-pass scan (decoupled look-back): a block takes the next tile number
+// from a counter, sums its 4096 items, publishes the sum, and warp 0 reads its
+// predecessors' published words 32 at a time, back to the nearest inclusive
+// prefix; the tile then publishes its own inclusive prefix and writes its
+// items.  Tiles are numbered in the order blocks start, so a tile only waits
+// on tiles whose blocks are already running.  The wait is bounded: past the
+// limit the tile sums its predecessors' items itself (slow, but exact), so a
+// scan never yields a wrong offset.  A warp reads its segment 32 consecutive
+// items per round (coalesced loads and stores).
+constexpr int kScan1Items = 16;
+constexpr int kScan1Tile = kScanThreads * kScan1Items;
+constexpr unsigned long long kScanA = 1ull << 62;   // tile sum published
+constexpr unsigned long long kScanP = 2ull << 62;   // inclusive prefix published
+constexpr unsigned long long kScanVal = (1ull << 62) - 1;
+constexpr uint32_t kScanSpin = 1u << 20;
+
 template <class Tin, class Tout>
-__global__ void k_scan_tiles(const Tin* __restrict__ in, Tout* __restrict__ out, uint64_t n,
-                             const Tout* __restrict__ partial) {
+__global__ void __launch_bounds__(kScanThreads, 4) k_scan_1p(const Tin* __restrict__ in, Tout* __restrict__ out,
+                                                          uint64_t n, unsigned long long* __restrict__ status,
+                                                          uint32_t* __restrict__ ticket, Tout* __restrict__ total) {
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_prefix;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint64_t seg = (uint64_t)blockIdx.x * kScanTile + (uint64_t)w * (32 * kScanItems);
-    Tout v[kScanItems];
-    Tout s = 0;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t seg = (uint64_t)tile * kScan1Tile + (uint64_t)w * (32 * kScan1Items);
+    Tin v[kScan1Items];   // kept in the input type (half the registers for 32-bit counts)
+    Tout sum = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
+    for (int i = 0; i < kScan1Items; ++i) {
         const uint64_t p = seg + (uint64_t)i * 32 + lane;
-        v[i] = p < n ? (Tout)in[p] : Tout(0);
-        s += v[i];
+        v[i] = p < n ? in[p] : Tin(0);
+        sum += (Tout)v[i];
     }
-    // the block's exclusive prefix at this warp's segment: the scan of the
-    // threads' sums, taken at the warp's first lane
     Tout tot;
-    const Tout ex_thread = block_excl_scan<Tout>(s, &tot);
-    Tout carry = __shfl_sync(0xffffffffu, ex_thread, 0) + partial[blockIdx.x];
+    const Tout ex_thread = block_excl_scan<Tout>(sum, &tot);
+    if (w == 0) {
+        unsigned long long prefix = 0;
+        volatile unsigned long long* st = status + tile;
+        if (tile == 0) {
+            if (lane == 0) *st = kScanP | (unsigned long long)tot;
+        } else {
+            if (lane == 0) *st = kScanA | (unsigned long long)tot;
+            int64_t base = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            bool ok = true;
+            while (true) {
+                const int64_t t = base - lane;
+                const unsigned long long sv = t >= 0 ? *(volatile const unsigned long long*)(status + t) : kScanP;
+                const unsigned long long flag = sv & ~kScanVal;
+                const uint32_t pm = __ballot_sync(0xffffffffu, flag == kScanP);
+                const uint32_t zm = __ballot_sync(0xffffffffu, flag == 0);
+                const int fp = pm ? __ffs(pm) - 1 : 32;   // nearest inclusive prefix
+                const uint32_t upto = fp == 32 ? 0xffffffffu : ((2u << fp) - 1u);
+                if (zm & upto) {   // a predecessor has not published yet
+                    if (++spins > kScanSpin) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                unsigned long long add = ((upto >> lane) & 1u) ? (sv & kScanVal) : 0ull;
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-        const Tout inc = warp_incl_scan(v[i]);
+                for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
+                prefix += add;
+                if (fp < 32) break;
+                base -= 32;
+            }
+            if (!ok) {   // the predecessors' items, summed here
+                unsigned long long add = 0;
+                for (uint64_t p = lane; p < (uint64_t)tile * kScan1Tile; p += 32) add += (unsigned long long)(Tout)in[p];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
+                prefix = add;
+            }
+            if (lane == 0) *st = kScanP | (prefix + (unsigned long long)tot);
+        }
+        if (lane == 0) s_prefix = prefix;
+    }
+    __syncthreads();
+    Tout carry = __shfl_sync(0xffffffffu, ex_thread, 0) + (Tout)s_prefix;
+#pragma unroll
+    for (int i = 0; i < kScan1Items; ++i) {
+        const Tout x = (Tout)v[i];
+        const Tout inc = warp_incl_scan(x);
         const uint64_t p = seg + (uint64_t)i * 32 + lane;
-        if (p < n) out[p] = carry + inc - v[i];
+        if (p < n) out[p] = carry + inc - x;
         carry += __shfl_sync(0xffffffffu, inc, 31);
     }
+    if (total && threadIdx.x == 0 && (uint64_t)(tile + 1) * kScan1Tile >= n) *total = (Tout)s_prefix + tot;
 }
 
 __global__ void k_sum_u32(const uint32_t* __restrict__ in, uint64_t n, unsigned long long* __restrict__ out) {
@@ -103,31 +152,22 @@ __global__ void k_sum_u32(const uint32_t* __restrict__ in, uint64_t n, unsigned 
 template <class Tin, class Tout>
 void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total_host, Tout* total_dev) {
     KScope ks("scan");
-    uint64_t tiles = (n + kScanTile - 1) / kScanTile;
-    if (tiles == 0) tiles = 1;
-    DevBuf<Tout> partial;
-    partial.alloc(tiles + 1, s);
-    if (n > 0) {
-        k_tile_sums<Tin, Tout><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, partial.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
-    } else {
-        partial.zero(s);
-    }
-    k_scan_partials<Tout><<<1, 1024, 0, s>>>(partial.get(), n > 0 ? tiles : 0);
-    COLO_LAUNCH_CHECK();
-    count_launch();
-    if (n > 0) {
-        k_scan_tiles<Tin, Tout><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, n, partial.get());
+    const uint64_t tiles = n ? (n + kScan1Tile - 1) / kScan1Tile : 0;
+    if (tiles >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "scan supports < 2^32 tiles"};
+    // status words, then the tile counter and the total: one clear
+    DevBuf<unsigned long long> st;
+    st.alloc(tiles + 2, s);
+    st.zero(s);
+    uint32_t* ticket = reinterpret_cast<uint32_t*>(st.get() + tiles);
+    Tout* tot = reinterpret_cast<Tout*>(st.get() + tiles + 1);
+    if (tiles) {
+        k_scan_1p<Tin, Tout><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, n, st.get(), ticket, tot);
         COLO_LAUNCH_CHECK();
         count_launch();
     }
-    if (total_dev)
-        COLO_CUDA(cudaMemcpyAsync(total_dev, partial.get() + (n > 0 ? tiles : 0), sizeof(Tout),
-                                  cudaMemcpyDeviceToDevice, s));
+    if (total_dev) COLO_CUDA(cudaMemcpyAsync(total_dev, tot, sizeof(Tout), cudaMemcpyDeviceToDevice, s));
     if (total_host) {
-        COLO_CUDA(cudaMemcpyAsync(total_host, partial.get() + (n > 0 ? tiles : 0), sizeof(Tout),
-                                  cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaMemcpyAsync(total_host, tot, sizeof(Tout), cudaMemcpyDeviceToHost, s));
         COLO_CUDA(cudaStreamSynchronize(s));
     }
 }
@@ -250,7 +290,7 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
     uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
     unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err, int bulk,
-    uint32_t spin_limit, int withhold) {
+    uint32_t spin_limit, int withhold, int pass) {
     constexpr int R = 1 << RB;
     constexpr int kSortTile = kSortThreads * kSortRounds;
     constexpr int D = R / kSortThreads;             // digits per thread in the look-back (1 or 2)
@@ -261,14 +301,21 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
     __shared__ alignas(16) KT s_key[kSortTile];
     __shared__ alignas(16) uint32_t s_val[kSortTile];
     __shared__ alignas(8) uint64_t s_bar;
-    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_tile, s_skip;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
+        // an earlier pass that timed out left keys whose digit counts no longer match the
+        // histograms, so its positions could leave the array: every later pass writes nothing
+        // (the word holds the failed pass + 1; the previous launch has finished, so every
+        // block of this pass reads the same value)
+        const uint32_t e = *(volatile const uint32_t*)err;
+        s_skip = e != 0u && e < (uint32_t)pass + 1u;
         s_tile = atomicAdd(ticket, 1u);
-        if (bulk) mbar_init(&s_bar, 1);
+        if (bulk && !s_skip) mbar_init(&s_bar, 1);
     }
     for (int i = threadIdx.x; i < kSortWarps * R; i += blockDim.x) (&wh[0][0])[i] = 0;
     __syncthreads();
+    if (s_skip) return;
     const uint32_t tile = s_tile;
     const uint64_t tile0 = (uint64_t)tile * kSortTile;
     const uint64_t base = tile0 + (uint64_t)w * (32 * kSortRounds);
@@ -284,7 +331,7 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
             // the copy did not complete for every thread in time: report it, give it one
             // more bounded wait (it writes into this block's shared memory) and leave, the
             // whole block together; the host turns err into a timeout
-            if (threadIdx.x == 0) atomicOr(err, 1u);
+            if (threadIdx.x == 0) atomicCAS(err, 0u, (uint32_t)pass + 1u);
             mbar_wait(&s_bar, 0, kSpinLimit);
             return;
         }
@@ -350,8 +397,8 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
                     const unsigned long long v = *(volatile const unsigned long long*)(status + (uint64_t)t * R + d);
                     const unsigned long long flag = v & ~kValMask;
                     if (flag == 0) {
-                        if (++spins > spin_limit) {
-                            atomicOr(err, 1u);
+                        if (++spins > spin_limit) {   // give up: positions from a partial prefix
+                            atomicCAS(err, 0u, (uint32_t)pass + 1u);   // stay below the true ones
                             break;
                         }
                         __nanosleep(64);
@@ -494,7 +541,7 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
                                                                      hist + p * kMaxRadix, status.get(),
                                                                      tickets.get() + p, errp, bulk,
                                                                      test_spin ? test_spin : kSpinLimit,
-                                                                     test_spin && p == 0 ? 1 : 0);
+                                                                     test_spin && p == 0 ? 1 : 0, p);
         COLO_LAUNCH_CHECK();
         count_launch();
         std::swap(ka, kb);
@@ -504,7 +551,9 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         keys.swap(k2);
         vals.swap(v2);
     }
-    if (err_dev) return;   // the caller reads the error word at its next wait
+    // the caller reads the error word at its next wait; until then its kernels read the
+    // output with ids checked against n (a timed-out pass leaves ids unwritten)
+    if (err_dev) return;
     uint32_t herr = 0;
     COLO_CUDA(cudaMemcpyAsync(&herr, err.get(), 4, cudaMemcpyDeviceToHost, s));
     COLO_CUDA(cudaStreamSynchronize(s));

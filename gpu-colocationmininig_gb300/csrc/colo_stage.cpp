@@ -192,6 +192,31 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
     return colo_stage_within(ctx, x1, y1, x2, y2, n, 0.0f, out, nullptr);
 }
 
+colo_status colo_stage_scan(colo_ctx* ctx, const void* in, uint64_t n, int wide, uint64_t* out, uint64_t* total) {
+    if (!ctx || !total || (n && (!in || !out)) || (wide != 0 && wide != 1)) return COLO_ERR_ARG;
+    return run_guarded(ctx, [&]() -> colo_status {
+        cudaStream_t s = ctx->s;
+        DevBuf<uint64_t> o, t;
+        o.alloc(n ? n : 1, s);
+        t.alloc(1, s);
+        if (wide) {
+            DevBuf<uint64_t> a;
+            a.alloc(n ? n : 1, s);
+            if (n) COLO_CUDA(cudaMemcpyAsync(a.get(), in, n * 8, cudaMemcpyHostToDevice, s));
+            scan_u64_to_u64(a.get(), o.get(), n, s, nullptr, t.get());
+        } else {
+            DevBuf<uint32_t> a;
+            a.alloc(n ? n : 1, s);
+            if (n) COLO_CUDA(cudaMemcpyAsync(a.get(), in, n * 4, cudaMemcpyHostToDevice, s));
+            scan_u32_to_u64(reinterpret_cast<const uint32_t*>(a.get()), o.get(), n, s, nullptr, t.get());
+        }
+        if (n) COLO_CUDA(cudaMemcpyAsync(out, o.get(), n * 8, cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaMemcpyAsync(total, t.get(), 8, cudaMemcpyDeviceToHost, s));
+        COLO_CUDA(cudaStreamSynchronize(s));
+        return COLO_OK;
+    });
+}
+
 colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2, const float* y2,
                               uint64_t n, float R2, float* out, uint8_t* within) {
     if (!ctx || (n && (!x1 || !y1 || !x2 || !y2 || (!out && !within)))) return COLO_ERR_ARG;

@@ -231,6 +231,12 @@ colo_status colo_stage_sqdist(colo_ctx* ctx, const float* x1, const float* y1, c
 colo_status colo_stage_within(colo_ctx* ctx, const float* x1, const float* y1, const float* x2,
                               const float* y2, uint64_t n, float R2, float* out, uint8_t* within);
 
+/* The device-wide exclusive scan the mining kernels use for their offsets
+ * (replacing thrust::exclusive_scan, DeviceProcess.cu:342-344), on n host
+ * values: out[i] = in[0] + ... + in[i-1], *total = the sum of all n.  wide = 0:
+ * in is uint32_t, out uint64_t; wide = 1: in and out are uint64_t. */
+colo_status colo_stage_scan(colo_ctx* ctx, const void* in, uint64_t n, int wide, uint64_t* out, uint64_t* total);
+
 /* candidateColocationGeneral (colocationFinder.cpp:517-557) on the device:
  * the level-k candidates of the nprev prevalent (k-1)-patterns in prev
  * (row-major, lexicographic order), with the reference's breaks.  Writes up

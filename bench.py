@@ -557,10 +557,13 @@ def main():
 
     # per-kernel CUDA-event times (a separate profiled pass, so `value` carries no event overhead)
     ms_k, res_k, _, _ = timed(head_mode, True, profile=True)
-    kern = {}
+    kern, gaps, hosts = {}, {}, {}
     for r in res_k:
         for name, (nl, kms) in r.kernels.items():
-            a = kern.setdefault(name, [0, 0.0])
+            # "gap X": stream time between the previous timed scope and X (the GPU waiting for the host);
+            # "host X": host time from the last wait's return to X's launch
+            a = (gaps if name.startswith("gap ") else hosts if name.startswith("host ") else kern).setdefault(
+                name, [0, 0.0])
             a[0] += nl
             a[1] += kms
     counters = dict(res_b[0].counters)
@@ -584,6 +587,10 @@ def main():
         ab = algorithmic_bytes(name, counters, nl / args.steps, words)
         per_kernel[name] = {"ms": round(kms / args.steps, 3), "launches": round(nl / args.steps, 1),
                             "gbs": round(ab / (kms / args.steps / 1e3) / 1e9, 1) if kms > 0 and ab else None}
+    gaps_per_step = {name[4:]: round(kms / args.steps, 3)
+                     for name, (nl, kms) in sorted(gaps.items(), key=lambda kv: -kv[1][1])}
+    host_per_step = {name[5:]: round(kms / args.steps, 3)
+                     for name, (nl, kms) in sorted(hosts.items(), key=lambda kv: -kv[1][1])}
     phases = {k: round(statistics.mean(r.times[k] for r in res_b), 3)
               for k in ("bucket", "join", "filter", "refine", "fill", "apriori", "total")}
     if rank != 0:
@@ -633,6 +640,7 @@ def main():
         "identical_patterns_all_forms": same,
         "gpu_launches": int(sum(r.counters["launches"] for r in res_b)),
         "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,
+        "idle_before_kernel_per_step": gaps_per_step, "host_after_wait_per_step": host_per_step,
         "host_phase_ms": phases,
         "io": io,
         "side_configs": side,

@@ -156,7 +156,7 @@ void apriori_device(cudaStream_t s, const std::vector<const std::vector<uint32_t
         std::vector<uint32_t> hout(total * k), hpar(total);
         COLO_CUDA(cudaMemcpyAsync(hout.data(), dout.get(), hout.size() * 4, cudaMemcpyDeviceToHost, s));
         COLO_CUDA(cudaMemcpyAsync(hpar.data(), dpar.get(), hpar.size() * 4, cudaMemcpyDeviceToHost, s));
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
         for (uint32_t j = 0; j < J; ++j) {
             const uint64_t a = jstart[j] < P ? hoff[jstart[j]] : total;
             const uint64_t b = jstart[j + 1] < P ? hoff[jstart[j + 1]] : total;
@@ -164,7 +164,7 @@ void apriori_device(cudaStream_t s, const std::vector<const std::vector<uint32_t
             parent[j].assign(hpar.begin() + a, hpar.begin() + b);
         }
     } else {
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
     }
 }
 

@@ -81,7 +81,6 @@ struct Batch {
     // (feature, neighbour cell, id) order
     DevBuf<uint64_t> nb_beg;
     DevBuf<uint32_t> nb_cnt, nb;
-    DevBuf<uint32_t> act_pos;        // sorted positions of the join's active anchors (cell order)
     uint64_t E = 0;              // neighbour entries (UINT64_MAX: still on the device in dE)
     DevBuf<unsigned long long> dE;
     uint64_t nb_cap = 0;         // allocated entries (upper bound in single-pass mode)
@@ -156,11 +155,6 @@ struct LevelWork {
 // bitmaps + rows at their count-and-fill positions (overflow recorded per
 // candidate; a look-back that waits too long sets the batch's timeout flag).
 void level_count(Batch& b, const LevelWork& w, uint32_t k);
-// Level 2's count pass per anchor: d_cid[d_cid_off[j] + lf * nf_j + lg] is the index
-// in d_cands of pair (lf, lg) of job j (0xFFFFFFFF: not refined); the candidates'
-// slots must be zero.
-void level_pairs_count(Batch& b, const CandDesc* d_cands, uint64_t ncand, const uint64_t* d_cid_off,
-                       const uint32_t* d_cid, unsigned long long* d_items);
 void level_fill(Batch& b, const LevelWork& w, uint32_t k);
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow);
 // Participation statistics per candidate and member: [A, last, first, full]

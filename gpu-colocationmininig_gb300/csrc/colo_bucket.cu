@@ -925,7 +925,7 @@ void bucket_points(Batch& b) {
             COLO_CUDA(cudaMemcpyAsync(hd.data(), dcnt.get(), b.F * 4, cudaMemcpyDeviceToHost, s));
         }
         COLO_CUDA(cudaMemcpyAsync(&hf, b.flags.get(), sizeof(hf), cudaMemcpyDeviceToHost, s));
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
         b.h_frun_off.assign(b.F + 1, 0);
         for (uint32_t f = 0; f < b.F; ++f) b.h_frun_off[f + 1] = b.h_frun_off[f] + hc[f];
         b.h_dcnt.assign(hd.begin(), hd.end());

@@ -95,6 +95,9 @@ struct colo_ctx {
     int level_queue = 0;        // 1: level count/fill kernels as a persistent work queue
     void* stage = nullptr;      // page-locked staging for the level loop's readbacks
     size_t stage_bytes = 0;
+    void* ustage = nullptr;     // page-locked staging for the level loop's uploads
+    size_t ustage_bytes = 0;
+    size_t ustage_off = 0;      // bytes in use since the stream last drained
 };
 
 struct colo_dataset {

@@ -21,6 +21,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -211,8 +212,25 @@ struct KTimer {
         stats.push_back(KernelStat{name, 0, 0});
         return (int)stats.size() - 1;
     }
+    // Host time from the last wait's return to the next timed launch, charged to
+    // "host <scope>": the part of a gap that the host spends preparing the launch.
+    std::chrono::steady_clock::time_point waited{};
+    bool after_wait = false;
+    void note_wait() {
+        if (!on) return;
+        waited = std::chrono::steady_clock::now();
+        after_wait = true;
+    }
     void begin(const char* name) {
         if (!on || depth++ > 0) return;
+        if (after_wait) {
+            const double ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - waited).count();
+            KernelStat& h = stats[slot((std::string("host ") + name).c_str())];
+            h.ms += ms;
+            h.launches++;
+            after_wait = false;
+        }
         open_slot = slot(name);
         open_a = get();
         COLO_CUDA(cudaEventRecord(open_a, s));
@@ -224,6 +242,10 @@ struct KTimer {
         pend.push_back({open_slot, open_a, b});
         open_slot = -1;
     }
+    // Stream time between the end of one timed scope and the start of the next,
+    // charged to "gap <next scope>": the GPU waiting for the host (a wait and
+    // the launches after it) plus any untimed copy or clear between them.
+    cudaEvent_t last_b = nullptr;
     void resolve() {
         if (pend.empty()) return;
         COLO_CUDA(cudaStreamSynchronize(s));
@@ -232,8 +254,16 @@ struct KTimer {
             COLO_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
             stats[p.slot].ms += ms;
             stats[p.slot].launches++;
+            if (last_b) {
+                float gap = 0;
+                COLO_CUDA(cudaEventElapsedTime(&gap, last_b, p.a));
+                KernelStat& g = stats[slot(("gap " + stats[p.slot].name).c_str())];
+                g.ms += gap;
+                g.launches++;
+                pool.push_back(last_b);
+            }
             pool.push_back(p.a);
-            pool.push_back(p.b);
+            last_b = p.b;
         }
         pend.clear();
     }
@@ -242,10 +272,17 @@ struct KTimer {
             cudaEventDestroy(p.a);
             cudaEventDestroy(p.b);
         }
+        if (last_b) cudaEventDestroy(last_b);
         for (auto e : pool) cudaEventDestroy(e);
     }
 };
 extern thread_local KTimer* g_ktimer;
+
+// A host wait on the stream (noted by the kernel timer in profile mode).
+inline void stream_wait(cudaStream_t s) {
+    COLO_CUDA(cudaStreamSynchronize(s));
+    if (g_ktimer) g_ktimer->note_wait();
+}
 struct KScope {
     explicit KScope(const char* name) {
         if (g_ktimer) g_ktimer->begin(name);

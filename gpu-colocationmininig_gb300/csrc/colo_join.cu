@@ -181,16 +181,14 @@ void join_neighbors(Batch& b) {
     scan_u64_to_u64(cap.get(), cap_off.get(), Rn, s, nullptr, totals.get() + 1);
     uint64_t ht[2] = {0, 0};
     COLO_CUDA(cudaMemcpyAsync(ht, totals.get(), 16, cudaMemcpyDeviceToHost, s));
-    COLO_CUDA(cudaStreamSynchronize(s));
+    stream_wait(s);
     const uint32_t A = (uint32_t)ht[0];
     const uint64_t U = ht[1];
     b.active_anchors = A;
     b.join_pairs = U;
-    // the active anchors' sorted positions stay with the batch (level 2 walks their lists)
-    DevBuf<uint32_t>& act_pos = b.act_pos;
-    DevBuf<uint32_t> act_run;
-    act_pos.alloc(A ? A : 1, s);
-    act_run.alloc(A ? A : 1, s);
+    DevBuf<uint32_t> act_pos, act_run;
+    act_pos.alloc(A, s);
+    act_run.alloc(A, s);
     if (A) {
         KScope ks("join_setup");
         k_expand_active<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rstart.get(), b.rcnt.get(), b.run_L.get(),
@@ -230,7 +228,7 @@ uint64_t neighbor_entries(Batch& b) {
     if (b.E == UINT64_MAX) {
         unsigned long long e = 0;
         COLO_CUDA(cudaMemcpyAsync(&e, b.dE.get(), 8, cudaMemcpyDeviceToHost, b.s));
-        COLO_CUDA(cudaStreamSynchronize(b.s));
+        stream_wait(b.s);
         b.E = e;
     }
     return b.E;

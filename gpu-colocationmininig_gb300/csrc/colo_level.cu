@@ -402,179 +402,6 @@ __global__ void k_level_pi(const CandDesc* __restrict__ cands, uint64_t ncand, u
     }
 }
 
-// Level 2 counted per anchor instead of per candidate row.  The rows of pair
-// (f, g) are the anchors a of f; row a's candidates are the entries of g in
-// N+(a), one contiguous run of the list (it ascends by id, so by feature).
-// Every list entry is read once for the whole level (the per-row form reads
-// each row's list once per candidate of its feature and finds the slice by
-// two binary searches).  Per run of one feature g the pair (f, g) is looked
-// up in the level's pair table (cid: candidate index, or none for a pair the
-// filter removed); for a candidate the run's length goes to the row's slot
-// (a - fstart[f]; the slots of anchors without g stay zero) and to the
-// candidate's rows, and the participation bits of a and of the run's points
-// are set.
-//
-// k_pairs_count walks the join's active anchors (cell order), a lane per
-// anchor, each lane its own list when it is short (independent chains of
-// loads).  A longer list is cut into 32-entry units, listed for
-// k_pairs_units, whose warps take units of any anchor: dense spots, where
-// neighbouring anchors all have long lists, are spread over the GPU instead
-// of one warp.
-constexpr uint32_t kNoCand = 0xFFFFFFFFu;
-constexpr uint32_t kPairsLaneMax = 32;   // entries a lane walks alone
-// Levels with at most this many candidates sum each candidate's rows in shared
-// memory per block (one global atomic per block and candidate at the end):
-// the lanes of a warp are anchors of one cell and mostly add to the same few
-// candidates, which as global atomics serialise on a handful of addresses.
-constexpr uint32_t kPairsBlockRows = 8192;
-
-struct PairsArgs {
-    uint64_t A;                      // active anchors
-    const uint32_t* act_pos;         // their sorted positions
-    const uint32_t* sid;             // sorted position -> point id
-    const uint64_t* nb_beg;
-    const uint32_t* nb_cnt;
-    const uint32_t* nb;
-    uint32_t F;
-    const uint32_t* fstart;
-    const uint32_t* fcount;
-    const uint32_t* fjob;            // nullptr: one job
-    const JobGrid* grids;
-    const uint64_t* cid_off;         // per job: first entry of its pair table
-    const uint32_t* cid;
-    const CandDesc* cands;
-    unsigned long long* items;
-    uint2* units;                    // (anchor, first entry offset) of the long lists' units
-    unsigned long long* nunits;
-    uint32_t ncand;                  // candidates of the level
-    uint32_t block_rows;             // 1: rows are summed per block in shared memory first
-};
-
-__device__ __forceinline__ void pairs_anchor_info(const PairsArgs& P, uint32_t a, const uint32_t*& row_cid,
-                                                  uint32_t& f0, uint32_t& arow, uint32_t& wf) {
-    const uint32_t f = feature_of(a, P.F, P.fstart);
-    const uint32_t j = P.fjob ? P.fjob[f] : 0u;
-    f0 = P.grids[j].f0;
-    row_cid = P.cid + P.cid_off[j] + (uint64_t)(f - f0) * P.grids[j].nf;
-    arow = a - P.fstart[f];
-    wf = (P.fcount[f] + 31u) / 32u;
-}
-
-__device__ __forceinline__ unsigned long long warp_sum_ull(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Adds a row count to candidate c: the block's shared counter or the global one.
-__device__ __forceinline__ void pairs_add_rows(const PairsArgs& P, uint32_t* s_rows, const CandDesc& d, uint32_t c,
-                                               uint32_t len) {
-    if (P.block_rows) atomicAdd(&s_rows[c], len);
-    else atomicAdd(d.rows, (unsigned long long)len);
-}
-
-__device__ __forceinline__ void pairs_rows_init(const PairsArgs& P, uint32_t* s_rows) {
-    if (P.block_rows)
-        for (uint32_t i = threadIdx.x; i < P.ncand; i += blockDim.x) s_rows[i] = 0;
-    __syncthreads();
-}
-
-__device__ __forceinline__ void pairs_rows_flush(const PairsArgs& P, const uint32_t* s_rows) {
-    __syncthreads();
-    if (P.block_rows)
-        for (uint32_t i = threadIdx.x; i < P.ncand; i += blockDim.x)
-            if (s_rows[i]) atomicAdd(P.cands[i].rows, (unsigned long long)s_rows[i]);
-}
-
-__global__ void __launch_bounds__(256) k_pairs_count(PairsArgs P) {
-    extern __shared__ uint32_t s_rows[];
-    pairs_rows_init(P, s_rows);
-    const int lane = threadIdx.x & 31;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    unsigned long long seen = 0;   // entries of candidate runs
-    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < P.A; i0 += stride) {
-        const uint64_t i = i0 + lane;
-        uint32_t a = 0, n = 0;
-        if (i < P.A) {
-            a = P.sid[P.act_pos[i]];
-            n = P.nb_cnt[a];
-        }
-        if (n > kPairsLaneMax) {   // units of 32 entries for k_pairs_units
-            const uint32_t units = (n + 31) / 32;
-            const unsigned long long u0 = atomicAdd(P.nunits, (unsigned long long)units);
-            for (uint32_t u = 0; u < units; ++u) P.units[u0 + u] = make_uint2(a, u * 32);
-        } else if (n) {
-            const uint32_t* row_cid;
-            uint32_t f0, arow, wf;
-            pairs_anchor_info(P, a, row_cid, f0, arow, wf);
-            const uint64_t end = P.nb_beg[a] + n;
-            for (uint64_t p = end - n; p < end;) {
-                const uint32_t g = feature_of(P.nb[p], P.F, P.fstart);
-                const uint32_t gs = P.fstart[g], gend = gs + P.fcount[g];
-                uint64_t q = p + 1;
-                while (q < end && P.nb[q] < gend) ++q;
-                const uint32_t c = row_cid[g - f0];
-                if (c != kNoCand) {
-                    const CandDesc& d = P.cands[c];
-                    const uint32_t len = (uint32_t)(q - p);
-                    d.slots[arow] = len;
-                    pairs_add_rows(P, s_rows, d, c, len);
-                    set_bit(d.bitmap + d.bm_base, arow);
-                    for (uint64_t t = p; t < q; ++t) set_bit(d.bitmap + d.bm_base + wf, P.nb[t] - gs);
-                    seen += len;
-                }
-                p = q;
-            }
-        }
-    }
-    seen = warp_sum_ull(seen);
-    if (P.items && lane == 0 && seen) atomicAdd(P.items, seen);
-    pairs_rows_flush(P, s_rows);
-}
-
-// A unit: up to 32 consecutive entries of one long list, a lane per entry.
-// Lanes of one feature are contiguous; the first of them adds their count to
-// the row's slot (units of one run add up there) and to the candidate's rows.
-__global__ void __launch_bounds__(256) k_pairs_units(PairsArgs P) {
-    extern __shared__ uint32_t s_rows[];
-    pairs_rows_init(P, s_rows);
-    const int lane = threadIdx.x & 31;
-    const unsigned long long nu = *P.nunits;
-    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned long long seen = 0;
-    for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nu; u += warps) {
-        const uint2 un = P.units[u];
-        const uint32_t a = un.x;
-        const uint32_t* row_cid;
-        uint32_t f0, arow, wf;
-        pairs_anchor_info(P, a, row_cid, f0, arow, wf);
-        const uint32_t n = P.nb_cnt[a];
-        const uint64_t t = P.nb_beg[a] + un.y + lane;
-        const bool in = un.y + lane < n;
-        uint32_t g = 0xFFFFFFFFu, c = kNoCand, bpt = 0;
-        if (in) {
-            bpt = P.nb[t];
-            g = feature_of(bpt, P.F, P.fstart);
-            c = row_cid[g - f0];
-        }
-        const uint32_t peers = __match_any_sync(0xffffffffu, g);
-        if (c != kNoCand) {
-            const CandDesc& d = P.cands[c];
-            if (lane == __ffs(peers) - 1) {
-                const uint32_t len = (uint32_t)__popc(peers);
-                atomicAdd(d.slots + arow, len);
-                pairs_add_rows(P, s_rows, d, c, len);
-                set_bit(d.bitmap + d.bm_base, arow);
-                seen += len;
-            }
-            set_bit(d.bitmap + d.bm_base + wf, bpt - P.fstart[g]);
-        }
-    }
-    seen = warp_sum_ull(seen);
-    if (P.items && lane == 0 && seen) atomicAdd(P.items, seen);
-    pairs_rows_flush(P, s_rows);
-}
-
 template <int MODE>
 void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
     if (w.nchunks == 0) return;
@@ -612,30 +439,6 @@ void launch_level(Batch& b, const LevelWork& w, uint32_t k, uint32_t* ovf) {
 }  // namespace
 
 void level_count(Batch& b, const LevelWork& w, uint32_t k) { launch_level<MODE_COUNT>(b, w, k, nullptr); }
-void level_pairs_count(Batch& b, const CandDesc* d_cands, uint64_t ncand, const uint64_t* d_cid_off,
-                       const uint32_t* d_cid, unsigned long long* d_items) {
-    if (b.active_anchors == 0 || ncand == 0) return;
-    KScope ks("level_count");
-    // units of the long lists: at most E / 32 + A of them
-    const uint64_t E = b.nb_cap;
-    DevBuf<uint2> units;
-    DevBuf<unsigned long long> nunits;
-    units.alloc(E / 32 + b.active_anchors + 1, b.s);
-    nunits.alloc(1, b.s);
-    nunits.zero(b.s);
-    PairsArgs P{b.active_anchors, b.act_pos.get(), b.sid.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get(), b.F,
-                b.fstart.get(), b.fcount.get(), b.J > 1 ? b.fjob.get() : nullptr, b.grids.get(), d_cid_off, d_cid,
-                d_cands, d_items, units.get(), nunits.get(), (uint32_t)ncand, ncand <= kPairsBlockRows ? 1u : 0u};
-    const size_t smem = P.block_rows ? (size_t)ncand * 4 : 0;
-    const unsigned grid = (unsigned)std::min<uint64_t>((b.active_anchors + 255) / 256, (uint64_t)b.sms * 8);
-    k_pairs_count<<<grid, 256, smem, b.s>>>(P);
-    COLO_LAUNCH_CHECK();
-    count_launch();
-    k_pairs_units<<<(unsigned)(b.sms * 8), 256, smem, b.s>>>(P);
-    COLO_LAUNCH_CHECK();
-    count_launch();
-}
-
 void level_fill(Batch& b, const LevelWork& w, uint32_t k) { launch_level<MODE_FILL>(b, w, k, nullptr); }
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow) {
     launch_level<MODE_SINGLE>(b, w, k, d_overflow);

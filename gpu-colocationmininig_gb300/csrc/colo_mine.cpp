@@ -106,6 +106,7 @@ void ctx_release(colo_ctx* ctx) {
         cudaStreamDestroy(ctx->s);
     }
     if (ctx->stage) cudaFreeHost(ctx->stage);
+    if (ctx->ustage) cudaFreeHost(ctx->ustage);
     delete ctx;
 }
 
@@ -156,7 +157,7 @@ uint64_t upload_dataset(colo_dataset* ds, cudaStream_t s) {
         COLO_CUDA(cudaMemcpyAsync(ds->dx.get(), ds->hp.x.data(), n * 4, cudaMemcpyHostToDevice, s));
         COLO_CUDA(cudaMemcpyAsync(ds->dy.get(), ds->hp.y.data(), n * 4, cudaMemcpyHostToDevice, s));
     }
-    COLO_CUDA(cudaStreamSynchronize(s));
+    stream_wait(s);
     ds->resident = true;
     return 8 * n;   // bytes copied
 }
@@ -266,7 +267,7 @@ struct Readback {
     Readback(colo_ctx* c, cudaStream_t st, size_t need) : ctx(c), s(st) {
         need += 64 * 16;   // 16-byte alignment of each copy
         if (need > ctx->stage_bytes) {
-            COLO_CUDA(cudaStreamSynchronize(s));
+            stream_wait(s);
             if (ctx->stage) cudaFreeHost(ctx->stage);
             ctx->stage = nullptr;
             ctx->stage_bytes = 0;
@@ -284,12 +285,39 @@ struct Readback {
         off += bytes;
     }
     void finish() {
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
         for (const Item& it : items) std::memcpy(it.dst, static_cast<char*>(ctx->stage) + it.off, it.bytes);
         items.clear();
         off = 0;
+        ctx->ustage_off = 0;   // the stream has drained: every upload staged so far has landed
     }
 };
+
+// Host-to-device copies of the level loop through page-locked staging: the
+// bytes are copied into ctx->ustage and the DMA is queued from there, so the
+// call does not wait as a copy from pageable memory does.  The staging space is
+// reused after the next Readback::finish (the stream has drained by then); it
+// grows, after a drain, when a copy does not fit.
+void upload(colo_ctx* ctx, cudaStream_t s, void* dst, const void* src, size_t bytes) {
+    if (!bytes) return;
+    size_t off = (ctx->ustage_off + 15) & ~(size_t)15;
+    if (off + bytes > ctx->ustage_bytes) {
+        stream_wait(s);
+        off = 0;
+        if (bytes > ctx->ustage_bytes) {
+            if (ctx->ustage) cudaFreeHost(ctx->ustage);
+            ctx->ustage = nullptr;
+            ctx->ustage_bytes = 0;
+            const size_t nb = std::max<size_t>(bytes * 2, (size_t)1 << 20);
+            COLO_CUDA(cudaHostAlloc(&ctx->ustage, nb, cudaHostAllocDefault));
+            ctx->ustage_bytes = nb;
+        }
+    }
+    char* h = static_cast<char*>(ctx->ustage) + off;
+    std::memcpy(h, src, bytes);
+    COLO_CUDA(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, s));
+    ctx->ustage_off = off + bytes;
+}
 
 // A typed view into the level arena's one allocation.
 template <class T>
@@ -306,6 +334,7 @@ struct LevelArena {
     DevBuf<unsigned char> mem;
     ArenaSpan<uint32_t> bitmap;
     ArenaSpan<unsigned long long> rows;
+    ArenaSpan<unsigned long long> items;    // candidate-slice entries examined (work counter)
     ArenaSpan<unsigned long long> status;   // single pass: per chunk look-back word, then the chunk ticket
     ArenaSpan<unsigned long long> tickets;  // chunk tickets of the count and fill launches (persistent queue)
     ArenaSpan<uint32_t> overflow;           // single pass: 1 when the table outgrew its capacity
@@ -313,6 +342,11 @@ struct LevelArena {
     ArenaSpan<CandDesc> descs;
     ArenaSpan<uint64_t> chunk_off;
     ArenaSpan<uint64_t> stats;
+    // the refine's results (rows | items | overflow | stats) and inputs (descs | chunk
+    // prefixes) are each one contiguous block: one copy back, one copy in
+    size_t out_bytes = 0, in_bytes = 0, chunk_at = 0;
+    unsigned char* out = nullptr;
+    unsigned char* in = nullptr;
 
     void init(uint64_t nslots, uint64_t nwords, uint64_t ncand, uint64_t nchunks, uint32_t k, bool single,
               cudaStream_t s) {
@@ -322,28 +356,39 @@ struct LevelArena {
             off += (size_t)((bytes + 255) & ~(uint64_t)255);
             return o;
         };
-        const size_t o_bitmap = take(std::max<uint64_t>(nwords, 1) * 4);
-        const size_t o_rows = take(std::max<uint64_t>(ncand, 1) * 8);
+        const size_t r_items = ncand * 8, r_ovf = r_items + 8, r_stats = (r_ovf + ncand * 4 + 15) & ~(size_t)15;
+        out_bytes = r_stats + ncand * k * 4 * 8;
+        const size_t o_out = take(out_bytes);
         const size_t o_status = single ? take((nchunks + 1) * 8) : 0;
         const size_t o_tickets = take(2 * 8);
-        const size_t o_overflow = single ? take(ncand * 4) : 0;
+        const size_t o_bitmap = take(std::max<uint64_t>(nwords, 1) * 4);
         const size_t zeroed = off;
         const size_t o_slots = take(std::max<uint64_t>(nslots, 1) * 4);
-        const size_t o_descs = take(std::max<uint64_t>(ncand, 1) * sizeof(CandDesc));
-        const size_t o_chunk = take((ncand + 2) * 8);
-        const size_t o_stats = take((ncand * k * 4 + 1) * 8);
+        chunk_at = (std::max<uint64_t>(ncand, 1) * sizeof(CandDesc) + 15) & ~(size_t)15;
+        in_bytes = chunk_at + (ncand + 2) * 8;
+        const size_t o_in = take(in_bytes);
         mem.alloc(off, s);
         unsigned char* b = mem.get();
-        bitmap.p = reinterpret_cast<uint32_t*>(b + o_bitmap);
-        rows.p = reinterpret_cast<unsigned long long*>(b + o_rows);
+        out = b + o_out;
+        in = b + o_in;
+        rows.p = reinterpret_cast<unsigned long long*>(out);
+        items.p = reinterpret_cast<unsigned long long*>(out + r_items);
+        overflow.p = reinterpret_cast<uint32_t*>(out + r_ovf);
+        stats.p = reinterpret_cast<uint64_t*>(out + r_stats);
         status.p = single ? reinterpret_cast<unsigned long long*>(b + o_status) : nullptr;
         tickets.p = reinterpret_cast<unsigned long long*>(b + o_tickets);
-        overflow.p = single ? reinterpret_cast<uint32_t*>(b + o_overflow) : nullptr;
+        bitmap.p = reinterpret_cast<uint32_t*>(b + o_bitmap);
         slots.p = reinterpret_cast<uint32_t*>(b + o_slots);
-        descs.p = reinterpret_cast<CandDesc*>(b + o_descs);
-        chunk_off.p = reinterpret_cast<uint64_t*>(b + o_chunk);
-        stats.p = reinterpret_cast<uint64_t*>(b + o_stats);
+        descs.p = reinterpret_cast<CandDesc*>(in);
+        chunk_off.p = reinterpret_cast<uint64_t*>(in + chunk_at);
         COLO_CUDA(cudaMemsetAsync(b, 0, zeroed, s));
+    }
+    // descs and chunk prefixes in one upload
+    void put_inputs(colo_ctx* ctx, cudaStream_t s, const std::vector<CandDesc>& hd, const std::vector<uint64_t>& ch) {
+        std::vector<unsigned char> h(in_bytes, 0);
+        std::memcpy(h.data(), hd.data(), hd.size() * sizeof(CandDesc));
+        std::memcpy(h.data() + chunk_at, ch.data(), std::min<size_t>(ch.size() * 8, in_bytes - chunk_at));
+        upload(ctx, s, in, h.data(), in_bytes);
     }
 };
 
@@ -412,7 +457,7 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
             COLO_CUDA(cudaMemcpyAsync(ownf[1].get() + off, ds->hp.y.data(), n * 4, cudaMemcpyHostToDevice, s));
             off += n;
         }
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
         b.h2d_points = 8 * N;
         b.x = ownf[0].get();
         b.y = ownf[1].get();
@@ -464,8 +509,8 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
         COLO_CUDA(cudaMemcpyAsync(b.fcount.get(), b.h_fcount.data(), b.F * 4, cudaMemcpyHostToDevice, s));
         COLO_CUDA(cudaMemcpyAsync(b.fjob.get(), b.h_fjob.data(), b.F * 4, cudaMemcpyHostToDevice, s));
     }
+    // (copies from pageable memory return once the source is staged: no wait is needed)
     COLO_CUDA(cudaMemcpyAsync(b.grids.get(), hg.data(), J * sizeof(JobGrid), cudaMemcpyHostToDevice, s));
-    COLO_CUDA(cudaStreamSynchronize(s));
 }
 
 static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J,
@@ -483,8 +528,6 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     uint64_t cnt_items = 0, cnt_parent = 0, cnt_fillw = 0, cnt_bmw = 0, cnt_d2h = 0, cnt_refined = 0, cnt_fcm = 0;
     uint64_t cnt_single = 0, cnt_single_ovf = 0, cnt_fquads = 0, cnt_fcells = 0;
     uint64_t us_pairs_model = 0, us_level_wait = 0;
-    DevBuf<unsigned long long> d_items;
-    d_items.alloc(1, s);
     Batch b;
     const int mode = pv[0].mode;
     const bool plain = (mode == COLO_MODE_PLAIN);
@@ -512,8 +555,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
     double t_bucket = ms_since(t0);
     t0 = Clock::now();
     if (N > 0) join_neighbors(b);
-    COLO_CUDA(cudaStreamSynchronize(s));
-    double t_join = ms_since(t0);
+    double t_join = ms_since(t0);   // host time: the level loop's first wait absorbs the join's tail
 
     double t_filter = 0, t_refine = 0, t_fill = 0, t_apriori = 0;
     uint64_t rows_written = 0;
@@ -571,7 +613,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             filter_pairs(b, ub2, job_off, s);
             std::vector<uint32_t> h(job_off[J]);
             if (!h.empty()) COLO_CUDA(cudaMemcpyAsync(h.data(), ub2.get(), h.size() * 4, cudaMemcpyDeviceToHost, s));
-            COLO_CUDA(cudaStreamSynchronize(s));
+            stream_wait(s);
             for (uint32_t j = 0; j < J; ++j) {
                 if (!tr[j]) continue;
                 LevelTrace& L = *tr[j];
@@ -600,60 +642,69 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             for (uint32_t j = 0; j < J; ++j) rec_all |= tr[j] && (pv[j].reserved[0] & 2) != 0;
             const bool infer = learned_mode && ncand > 0;
             const bool want_x = (rec_all || infer) && ncand;
-            // the level's filter buffers from one allocation: bounds and cell
-            // statistics (zeroed, adjacent), candidates, cost-model inputs and outputs
+            // the level's filter buffers from one allocation: the results (bounds, cell
+            // statistics, predictions: zeroed, one block read back with one copy) and the
+            // inputs (candidates, parent rows, model: one block written with one copy), then
+            // the cost-model inputs
             size_t off = 0;
             auto take = [&](uint64_t bytes) {
                 const size_t o = off;
-                off += (size_t)((bytes + 255) & ~(uint64_t)255);
+                off += (size_t)((bytes + 15) & ~(uint64_t)15);
                 return o;
             };
-            const size_t o_ub = take(ncand * k * 4), o_fs = take(ncand * 2 * 8), zeroed = off;
+            const size_t o_ub = take(ncand * k * 4), o_fs = take(ncand * 2 * 8), o_y = infer ? take(ncand * 4) : 0;
+            const size_t out_bytes = off;
             const size_t o_cand = take(ncand * k * 4);
-            const size_t o_prow = want_x ? take(ncand * 8) : 0, o_x = want_x ? take(ncand * kMlpIn * 4) : 0;
-            const size_t o_par = infer ? take(kMlpParams * 4) : 0, o_y = infer ? take(ncand * 4) : 0;
+            const size_t o_prow = want_x ? take(ncand * 8) : 0, o_par = infer ? take(kMlpParams * 4) : 0;
+            const size_t in_end = off;
+            const size_t o_x = want_x ? take(ncand * kMlpIn * 4) : 0;
             DevBuf<unsigned char> fmem;
             fmem.alloc(off ? off : 256, s);
             unsigned char* fb = fmem.get();
             uint32_t* d_ub = reinterpret_cast<uint32_t*>(fb + o_ub);
             unsigned long long* d_fs = reinterpret_cast<unsigned long long*>(fb + o_fs);
             uint32_t* d_cand = reinterpret_cast<uint32_t*>(fb + o_cand);
-            if (zeroed) COLO_CUDA(cudaMemsetAsync(fb, 0, zeroed, s));
-            COLO_CUDA(cudaMemcpyAsync(d_cand, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
+            if (out_bytes) COLO_CUDA(cudaMemsetAsync(fb, 0, out_bytes, s));
+            {
+                std::vector<unsigned char> hin(in_end - o_cand, 0);
+                std::memcpy(hin.data(), hc.data(), hc.size() * 4);
+                if (want_x) {
+                    uint64_t* hprow = reinterpret_cast<uint64_t*>(hin.data() + (o_prow - o_cand));
+                    for (uint64_t q = 0; q < ncand; ++q) {
+                        const JobState& st = js[owner[q].first];
+                        hprow[q] = st.prev_tables[st.parent[owner[q].second]].rows;
+                    }
+                }
+                if (infer) std::memcpy(hin.data() + (o_par - o_cand), ctx->model.data(), kMlpParams * 4);
+                upload(ctx, s, d_cand, hin.data(), hin.size());
+            }
             filter_level(b, hc.data(), hjob.data(), ncand, k, d_ub, d_fs, d_cand);
             const auto tl0 = Clock::now();
             // cost-model features and predictions on the device, read back with the bounds
-            Readback rb(ctx, s, (rec_all ? ncand * kMlpIn * 4 : 0) + (infer ? ncand * 4 : 0) + ncand * k * 4 +
-                                    ncand * 2 * 8);
+            Readback rb(ctx, s, (rec_all ? ncand * kMlpIn * 4 : 0) + out_bytes);
             std::vector<float> hX, hY;
             if (want_x) {
-                uint64_t* d_prow = reinterpret_cast<uint64_t*>(fb + o_prow);
+                const uint64_t* d_prow = reinterpret_cast<const uint64_t*>(fb + o_prow);
                 float* d_x = reinterpret_cast<float*>(fb + o_x);
-                std::vector<uint64_t> hprow(ncand, 0);
-                for (uint64_t q = 0; q < ncand; ++q) {
-                    const JobState& st = js[owner[q].first];
-                    hprow[q] = st.prev_tables[st.parent[owner[q].second]].rows;
-                }
-                COLO_CUDA(cudaMemcpyAsync(d_prow, hprow.data(), ncand * 8, cudaMemcpyHostToDevice, s));
                 mlp_features(ncand, k, d_cand, d_ub, d_fs, b.fcount.get(), d_prow, d_x, s);
                 if (rec_all) {
                     hX.resize(ncand * kMlpIn);
                     rb.copy(hX.data(), d_x, hX.size() * 4);
                 }
-                if (infer) {
-                    float* d_par = reinterpret_cast<float*>(fb + o_par);
-                    float* d_y = reinterpret_cast<float*>(fb + o_y);
-                    hY.resize(ncand);
-                    COLO_CUDA(cudaMemcpyAsync(d_par, ctx->model.data(), kMlpParams * 4, cudaMemcpyHostToDevice, s));
-                    mlp_forward(d_par, d_x, ncand, d_y, s);
-                    rb.copy(hY.data(), d_y, ncand * 4);
-                }
+                if (infer) mlp_forward(reinterpret_cast<const float*>(fb + o_par), d_x, ncand,
+                                       reinterpret_cast<float*>(fb + o_y), s);
             }
+            std::vector<unsigned char> hout(out_bytes);
+            rb.copy(hout.data(), fb, out_bytes);
+            rb.finish();
             std::vector<uint32_t> hub(ncand * k);
             std::vector<uint64_t> hfs(ncand * 2);
-            rb.copy(hub.data(), d_ub, hub.size() * 4);
-            rb.copy(hfs.data(), d_fs, hfs.size() * 8);
-            rb.finish();
+            std::memcpy(hub.data(), hout.data() + o_ub, hub.size() * 4);
+            std::memcpy(hfs.data(), hout.data() + o_fs, hfs.size() * 8);
+            if (infer) {
+                hY.resize(ncand);
+                std::memcpy(hY.data(), hout.data() + o_y, ncand * 4);
+            }
             us_level_wait += (uint64_t)(ms_since(tl0) * 1000.0);
             for (uint32_t j = 0; j < J; ++j) {
                 if (!tr[j]) continue;
@@ -724,7 +775,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 COLO_CUDA(cudaMemcpyAsync(dx.get(), X.data(), X.size() * 4, cudaMemcpyHostToDevice, s));
                 mlp_forward(dparams.get(), dx.get(), who.size(), dy.get(), s);
                 COLO_CUDA(cudaMemcpyAsync(y.data(), dy.get(), y.size() * 4, cudaMemcpyDeviceToHost, s));
-                COLO_CUDA(cudaStreamSynchronize(s));
+                stream_wait(s);
                 for (uint32_t j = 0; j < J; ++j)
                     if (tr[j]) tr[j]->pred.assign(tr[j]->cand.size() / k, 0.f);
                 for (size_t i = 0; i < who.size(); ++i) tr[who[i].first]->pred[who[i].second] = y[i];
@@ -856,14 +907,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
         }
         std::vector<uint64_t> hstats(ncand * k * 4);
-        Readback rb(ctx, s, hstats.size() * 8 + ncand * 8 + ncand * 4 + 8 + sizeof(DevFlags));
-        d_items.zero(s);
+        Readback rb(ctx, s, ar.out_bytes + sizeof(DevFlags));
         cnt_refined += ncand;
         cnt_bmw += nwords;
         for (uint64_t q = 0; q < ncand; ++q) cnt_parent += (uint64_t)(k - 1) * hd[q].prow;
         if (ncand) {
-            COLO_CUDA(cudaMemcpyAsync(ar.descs.get(), hd.data(), ncand * sizeof(CandDesc), cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(ar.chunk_off.get(), chunk_all.data(), (ncand + 2) * 8, cudaMemcpyHostToDevice, s));
+            ar.put_inputs(ctx, s, hd, chunk_all);
             if (plain) {
                 // per candidate, as the reference refines (one candidate at a time)
                 DevBuf<uint64_t> one_off;
@@ -875,65 +924,45 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), 2 * ncand * 8, cudaMemcpyHostToDevice, s));
                 for (uint64_t q = 0; q < ncand; ++q) {
-                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], d_items.get()};
+                    LevelWork w{ar.descs.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], ar.items.get()};
                     level_count(b, w, k);
                     level_pi(b, ar.descs.get() + q, 1, k, ar.stats.get() + q * k * 4);
                     COLO_CUDA(cudaMemcpyAsync(hstats.data() + q * k * 4, ar.stats.get() + q * k * 4, k * 4 * 8,
                                               cudaMemcpyDeviceToHost, s));
-                    COLO_CUDA(cudaStreamSynchronize(s));
+                    stream_wait(s);
                 }
             } else {
-                // pairs: counted per anchor (each list entry read once for the level) into
-                // zeroed slots, through a table from (job, pair) to candidate
-                const bool pairs = k == 2 && ns < ncand;
-                DevBuf<unsigned char> cidmem;
-                if (pairs) {
-                    std::vector<uint64_t> cid_off(J + 1, 0);
-                    for (uint32_t j = 0; j < J; ++j) cid_off[j + 1] = cid_off[j] + (uint64_t)js[j].nf * js[j].nf;
-                    std::vector<uint32_t> cid(cid_off[J], 0xFFFFFFFFu);
-                    for (uint64_t q = ns; q < ncand; ++q) {
-                        const JobState& st = js[hd[q].job];
-                        cid[cid_off[hd[q].job] + (uint64_t)(hd[q].m[0] - st.f0) * st.nf + (hd[q].m[1] - st.f0)] =
-                            (uint32_t)q;
-                    }
-                    const size_t o_cid = (J + 1) * 8;
-                    cidmem.alloc(o_cid + cid.size() * 4 + 4, s);
-                    COLO_CUDA(cudaMemcpyAsync(cidmem.get(), cid_off.data(), o_cid, cudaMemcpyHostToDevice, s));
-                    if (!cid.empty())
-                        COLO_CUDA(cudaMemcpyAsync(cidmem.get() + o_cid, cid.data(), cid.size() * 4,
-                                                  cudaMemcpyHostToDevice, s));
-                    COLO_CUDA(cudaMemsetAsync(ar.slots.get(), 0, nslots * 4, s));
-                }
                 if (ns) {
-                    LevelWork w{ar.descs.get(), ar.chunk_off.get(), ns, nch_single, d_items.get()};
+                    LevelWork w{ar.descs.get(), ar.chunk_off.get(), ns, nch_single, ar.items.get()};
                     w.chunk_status = ar.status.get();
                     w.ticket = ar.status.get() + nch_single;
                     level_single(b, w, k, ar.overflow.get());
                 }
-                if (pairs) {
-                    level_pairs_count(b, ar.descs.get(), ncand, reinterpret_cast<const uint64_t*>(cidmem.get()),
-                                      reinterpret_cast<const uint32_t*>(cidmem.get() + (J + 1) * 8), d_items.get());
-                } else if (ns < ncand) {
-                    LevelWork w{ar.descs.get() + ns, ar.chunk_off.get() + ns + 1, ncand - ns, nch_count, d_items.get()};
+                if (ns < ncand) {
+                    LevelWork w{ar.descs.get() + ns, ar.chunk_off.get() + ns + 1, ncand - ns, nch_count, ar.items.get()};
                     w.ticket = ar.tickets.get();
                     level_count(b, w, k);
                 }
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
-                rb.copy(hstats.data(), ar.stats.get(), hstats.size() * 8);
             }
         }
-        // row counts, overflow flags and the work counter, with the statistics: one wait
+        // row counts, the work counter, overflow flags and the statistics: one copy, one wait
         std::vector<uint64_t> hrows(ncand);
         std::vector<uint32_t> hovf(ncand, 0);
         unsigned long long h_items = 0;
-        if (ncand) rb.copy(hrows.data(), ar.rows.get(), ncand * 8);
+        std::vector<unsigned char> hout(ar.out_bytes);
+        if (ar.out_bytes) rb.copy(hout.data(), ar.out, ar.out_bytes);
         DevFlags hflags{};
-        if (ns) {
-            rb.copy(hovf.data(), ar.overflow.get(), ns * 4);
-            rb.copy(&hflags, b.flags.get(), sizeof(hflags));
-        }
-        rb.copy(&h_items, d_items.get(), 8);
+        if (ns) rb.copy(&hflags, b.flags.get(), sizeof(hflags));
         rb.finish();
+        if (ncand) {
+            std::memcpy(hrows.data(), hout.data(), ncand * 8);
+            std::memcpy(&h_items, hout.data() + ncand * 8, 8);
+            std::memcpy(hovf.data(), hout.data() + ncand * 8 + 8, ncand * 4);
+            if (!plain)
+                std::memcpy(hstats.data(), hout.data() + (reinterpret_cast<unsigned char*>(ar.stats.get()) - ar.out),
+                            hstats.size() * 8);
+        }
         if (hflags.timeout)
             throw StatusError{COLO_ERR_TIMEOUT, "single-pass tables: a chunk waited too long for its predecessors"};
         // participation index (getParticipationIndex, Codes/DeviceProcess.cu:108-132)
@@ -1076,13 +1105,19 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         rows_written += total_rows;
         cnt_fillw += total_rows * k;
-        DevBuf<CandDesc> dfd;
-        DevBuf<uint64_t> dfc;
+        // the fill's descriptors and chunk prefixes: one allocation, one upload
+        DevBuf<unsigned char> fin;
+        CandDesc* dfd_p = nullptr;
+        uint64_t* dfc_p = nullptr;
         if (!fd.empty()) {
-            dfd.alloc(fd.size(), s);
-            dfc.alloc(fchunk.size(), s);
-            COLO_CUDA(cudaMemcpyAsync(dfd.get(), fd.data(), fd.size() * sizeof(CandDesc), cudaMemcpyHostToDevice, s));
-            COLO_CUDA(cudaMemcpyAsync(dfc.get(), fchunk.data(), fchunk.size() * 8, cudaMemcpyHostToDevice, s));
+            const size_t at = (fd.size() * sizeof(CandDesc) + 15) & ~(size_t)15;
+            std::vector<unsigned char> h(at + fchunk.size() * 8, 0);
+            std::memcpy(h.data(), fd.data(), fd.size() * sizeof(CandDesc));
+            std::memcpy(h.data() + at, fchunk.data(), fchunk.size() * 8);
+            fin.alloc(h.size(), s);
+            dfd_p = reinterpret_cast<CandDesc*>(fin.get());
+            dfc_p = reinterpret_cast<uint64_t*>(fin.get() + at);
+            upload(ctx, s, fin.get(), h.data(), h.size());
             if (plain) {
                 DevBuf<uint64_t> one_off;
                 one_off.alloc(2 * fd.size(), s);
@@ -1093,12 +1128,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 }
                 COLO_CUDA(cudaMemcpyAsync(one_off.get(), hoff.data(), hoff.size() * 8, cudaMemcpyHostToDevice, s));
                 for (size_t q = 0; q < fd.size(); ++q) {
-                    LevelWork w{dfd.get() + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
+                    LevelWork w{dfd_p + q, one_off.get() + 2 * q, 1, hoff[2 * q + 1], nullptr};
                     level_fill(b, w, k);
-                    COLO_CUDA(cudaStreamSynchronize(s));
+                    stream_wait(s);
                 }
             } else {
-                LevelWork w{dfd.get(), dfc.get(), fd.size(), fchunk.back(), nullptr};
+                LevelWork w{dfd_p, dfc_p, fd.size(), fchunk.back(), nullptr};
                 w.ticket = ar.tickets.get() + 1;
                 level_fill(b, w, k);
             }
@@ -1107,7 +1142,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         // the next level's launches queue behind the fill on this stream without a wait
         bool keep_any = false;
         for (uint32_t j = 0; j < J; ++j) keep_any |= pv[j].keep_tables != 0;
-        if (keep_any) COLO_CUDA(cudaStreamSynchronize(s));
+        if (keep_any) stream_wait(s);
         // register the new tables (prefixes of the next level)
         for (uint32_t j = 0; j < J; ++j) {
             js[j].prev_tables.clear();
@@ -1144,7 +1179,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         for (auto& st : js)
             if (st.cands.empty()) st.active = false;
     }
-    COLO_CUDA(cudaStreamSynchronize(s));
+    stream_wait(s);
     kt.resolve();
     for (uint32_t j = 0; j < J; ++j) {
         MineResult* r = outs[j];

@@ -168,7 +168,7 @@ void scan_impl(const Tin* in, Tout* out, uint64_t n, cudaStream_t s, Tout* total
     if (total_dev) COLO_CUDA(cudaMemcpyAsync(total_dev, tot, sizeof(Tout), cudaMemcpyDeviceToDevice, s));
     if (total_host) {
         COLO_CUDA(cudaMemcpyAsync(total_host, tot, sizeof(Tout), cudaMemcpyDeviceToHost, s));
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
     }
 }
 
@@ -443,7 +443,7 @@ void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* 
     count_launch();
     if (total_host) {
         COLO_CUDA(cudaMemcpyAsync(total_host, partial + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-        COLO_CUDA(cudaStreamSynchronize(s));
+        stream_wait(s);
     }
 }
 
@@ -465,7 +465,7 @@ uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
     sum_u32_dev(in, n, s, acc.get());
     unsigned long long h = 0;
     COLO_CUDA(cudaMemcpyAsync(&h, acc.get(), 8, cudaMemcpyDeviceToHost, s));
-    COLO_CUDA(cudaStreamSynchronize(s));
+    stream_wait(s);
     return h;
 }
 
@@ -556,7 +556,7 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
     if (err_dev) return;
     uint32_t herr = 0;
     COLO_CUDA(cudaMemcpyAsync(&herr, err.get(), 4, cudaMemcpyDeviceToHost, s));
-    COLO_CUDA(cudaStreamSynchronize(s));
+    stream_wait(s);
     if (herr) throw StatusError{COLO_ERR_TIMEOUT, "radix sort: a tile waited too long for its predecessors"};
 }
 

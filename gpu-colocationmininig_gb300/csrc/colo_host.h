@@ -95,6 +95,8 @@ struct colo_ctx {
     int level_queue = 0;        // 1: level count/fill kernels as a persistent work queue
     void* stage = nullptr;      // page-locked staging for the level loop's readbacks
     size_t stage_bytes = 0;
+    cudaStream_t s2 = nullptr;  // side stream: the fill's slot scan runs there during the host's level work
+    cudaEvent_t ev_counted = nullptr, ev_scanned = nullptr;
     void* ustage = nullptr;     // page-locked staging for the level loop's uploads
     size_t ustage_bytes = 0;
     size_t ustage_off = 0;      // bytes in use since the stream last drained

@@ -105,6 +105,12 @@ void ctx_release(colo_ctx* ctx) {
         cudaStreamSynchronize(ctx->s);
         cudaStreamDestroy(ctx->s);
     }
+    if (ctx->s2) {
+        cudaStreamSynchronize(ctx->s2);
+        cudaStreamDestroy(ctx->s2);
+    }
+    if (ctx->ev_counted) cudaEventDestroy(ctx->ev_counted);
+    if (ctx->ev_scanned) cudaEventDestroy(ctx->ev_scanned);
     if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->ustage) cudaFreeHost(ctx->ustage);
     delete ctx;
@@ -298,8 +304,9 @@ struct Readback {
 // call does not wait as a copy from pageable memory does.  The staging space is
 // reused after the next Readback::finish (the stream has drained by then); it
 // grows, after a drain, when a copy does not fit.
-void upload(colo_ctx* ctx, cudaStream_t s, void* dst, const void* src, size_t bytes) {
-    if (!bytes) return;
+// Space for `bytes` in the upload staging; the caller writes its data there and
+// queues the copy with upload_from.
+unsigned char* upload_area(colo_ctx* ctx, cudaStream_t s, size_t bytes) {
     size_t off = (ctx->ustage_off + 15) & ~(size_t)15;
     if (off + bytes > ctx->ustage_bytes) {
         stream_wait(s);
@@ -313,10 +320,19 @@ void upload(colo_ctx* ctx, cudaStream_t s, void* dst, const void* src, size_t by
             ctx->ustage_bytes = nb;
         }
     }
-    char* h = static_cast<char*>(ctx->ustage) + off;
-    std::memcpy(h, src, bytes);
-    COLO_CUDA(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, s));
     ctx->ustage_off = off + bytes;
+    return static_cast<unsigned char*>(ctx->ustage) + off;
+}
+
+void upload_from(cudaStream_t s, void* dst, const unsigned char* staged, size_t bytes) {
+    if (bytes) COLO_CUDA(cudaMemcpyAsync(dst, staged, bytes, cudaMemcpyHostToDevice, s));
+}
+
+void upload(colo_ctx* ctx, cudaStream_t s, void* dst, const void* src, size_t bytes) {
+    if (!bytes) return;
+    unsigned char* h = upload_area(ctx, s, bytes);
+    std::memcpy(h, src, bytes);
+    upload_from(s, dst, h, bytes);
 }
 
 // A typed view into the level arena's one allocation.
@@ -385,10 +401,10 @@ struct LevelArena {
     }
     // descs and chunk prefixes in one upload
     void put_inputs(colo_ctx* ctx, cudaStream_t s, const std::vector<CandDesc>& hd, const std::vector<uint64_t>& ch) {
-        std::vector<unsigned char> h(in_bytes, 0);
-        std::memcpy(h.data(), hd.data(), hd.size() * sizeof(CandDesc));
-        std::memcpy(h.data() + chunk_at, ch.data(), std::min<size_t>(ch.size() * 8, in_bytes - chunk_at));
-        upload(ctx, s, in, h.data(), in_bytes);
+        unsigned char* h = upload_area(ctx, s, in_bytes);
+        std::memcpy(h, hd.data(), hd.size() * sizeof(CandDesc));
+        std::memcpy(h + chunk_at, ch.data(), std::min<size_t>(ch.size() * 8, in_bytes - chunk_at));
+        upload_from(s, in, h, in_bytes);
     }
 };
 
@@ -666,17 +682,17 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             uint32_t* d_cand = reinterpret_cast<uint32_t*>(fb + o_cand);
             if (out_bytes) COLO_CUDA(cudaMemsetAsync(fb, 0, out_bytes, s));
             {
-                std::vector<unsigned char> hin(in_end - o_cand, 0);
-                std::memcpy(hin.data(), hc.data(), hc.size() * 4);
+                unsigned char* hin = upload_area(ctx, s, in_end - o_cand);
+                std::memcpy(hin, hc.data(), hc.size() * 4);
                 if (want_x) {
-                    uint64_t* hprow = reinterpret_cast<uint64_t*>(hin.data() + (o_prow - o_cand));
+                    uint64_t* hprow = reinterpret_cast<uint64_t*>(hin + (o_prow - o_cand));
                     for (uint64_t q = 0; q < ncand; ++q) {
                         const JobState& st = js[owner[q].first];
                         hprow[q] = st.prev_tables[st.parent[owner[q].second]].rows;
                     }
                 }
-                if (infer) std::memcpy(hin.data() + (o_par - o_cand), ctx->model.data(), kMlpParams * 4);
-                upload(ctx, s, d_cand, hin.data(), hin.size());
+                if (infer) std::memcpy(hin + (o_par - o_cand), ctx->model.data(), kMlpParams * 4);
+                upload_from(s, d_cand, hin, in_end - o_cand);
             }
             filter_level(b, hc.data(), hjob.data(), ncand, k, d_ub, d_fs, d_cand);
             const auto tl0 = Clock::now();
@@ -788,6 +804,15 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         std::vector<CandDesc> hd;
         std::vector<std::pair<uint32_t, size_t>> owner;
         std::vector<uint64_t> slot_base, chunk_off(1, 0);
+        {
+            size_t most = 0;   // every candidate of the level passes at most
+            for (uint32_t j = 0; j < J; ++j)
+                if (tr[j]) most += tr[j]->cand.size() / k;
+            hd.reserve(most);
+            owner.reserve(most);
+            slot_base.reserve(most);
+            chunk_off.reserve(most + 1);
+        }
         uint64_t nslots = 0, nwords = 0;
         for (uint32_t j = 0; j < J; ++j) {
             if (!tr[j]) continue;
@@ -886,6 +911,17 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         if (ns == ncand) chunk_all.push_back(0);
         const uint64_t nch_single = chunk_all[ns], nch_count = chunk_all.back();
         LevelArena ar;
+        DevBuf<uint64_t> G;   // the fill's output offsets: the scan of every parent row's count
+        // the side stream's scan reads the arena and writes G: the main stream waits for it
+        // before either is freed, also when the level ends by an error
+        struct SideScan {
+            cudaStream_t s;
+            cudaEvent_t ev;
+            bool pending = false;
+            ~SideScan() {
+                if (pending) cudaStreamWaitEvent(s, ev, 0);
+            }
+        } side{s, ctx->ev_scanned};
         ar.init(nslots, nwords, ncand, nch_single, k, ns > 0, s);
         std::unique_ptr<TableBuf> single_cur;
         uint64_t single_words = 0;
@@ -942,6 +978,21 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                     LevelWork w{ar.descs.get() + ns, ar.chunk_off.get() + ns + 1, ncand - ns, nch_count, ar.items.get()};
                     w.ticket = ar.tickets.get();
                     level_count(b, w, k);
+                }
+                // the fill's output offsets (the scan of every row's count) on the side stream,
+                // during the participation kernel, the wait and the host's Apriori; the profiled
+                // pass keeps it on the main stream so that its timers see it
+                if (nslots) {
+                    G.alloc(nslots, s);
+                    if (!kt.on) {
+                        COLO_CUDA(cudaEventRecord(ctx->ev_counted, s));
+                        COLO_CUDA(cudaStreamWaitEvent(ctx->s2, ctx->ev_counted, 0));
+                        scan_u32_to_u64(ar.slots.get(), G.get(), nslots, ctx->s2, nullptr);
+                        COLO_CUDA(cudaEventRecord(ctx->ev_scanned, ctx->s2));
+                        side.pending = true;
+                    } else {
+                        scan_u32_to_u64(ar.slots.get(), G.get(), nslots, s, nullptr);
+                    }
                 }
                 level_pi(b, ar.descs.get(), ncand, k, ar.stats.get());
             }
@@ -1076,16 +1127,16 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         tables_cur.reset(new TableBuf());
         tables_cur->alloc(total_rows * k ? total_rows * k : 1, s, host_tables);
         if (tables_cur->on_host()) cnt_host_table_bytes += total_rows * k * 4;
-        // output offsets of every parent row: exclusive scan of the slots
-        DevBuf<uint64_t> G;
-        if (!fillq.empty()) {
+        // output offsets of every parent row: exclusive scan of the slots (batched: already
+        // launched with the count, on the side stream; the main stream waits for it here)
+        if (side.pending) {
+            COLO_CUDA(cudaStreamWaitEvent(s, ctx->ev_scanned, 0));
+            side.pending = false;
+        }
+        if (!fillq.empty() && plain) {
             G.alloc(nslots, s);
-            if (plain) {
-                for (uint64_t q : fillq)   // one scan per candidate, as the reference does
-                    scan_u32_to_u64(ar.slots.get() + slot_base[q], G.get() + slot_base[q], hd[q].prow, s, nullptr);
-            } else {
-                scan_u32_to_u64(ar.slots.get(), G.get(), nslots, s, nullptr);
-            }
+            for (uint64_t q : fillq)   // one scan per candidate, as the reference does
+                scan_u32_to_u64(ar.slots.get() + slot_base[q], G.get() + slot_base[q], hd[q].prow, s, nullptr);
         }
         std::vector<CandDesc> fd;
         std::vector<uint64_t> fchunk(1, 0);
@@ -1111,13 +1162,14 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         uint64_t* dfc_p = nullptr;
         if (!fd.empty()) {
             const size_t at = (fd.size() * sizeof(CandDesc) + 15) & ~(size_t)15;
-            std::vector<unsigned char> h(at + fchunk.size() * 8, 0);
-            std::memcpy(h.data(), fd.data(), fd.size() * sizeof(CandDesc));
-            std::memcpy(h.data() + at, fchunk.data(), fchunk.size() * 8);
-            fin.alloc(h.size(), s);
+            const size_t bytes = at + fchunk.size() * 8;
+            unsigned char* h = upload_area(ctx, s, bytes);
+            std::memcpy(h, fd.data(), fd.size() * sizeof(CandDesc));
+            std::memcpy(h + at, fchunk.data(), fchunk.size() * 8);
+            fin.alloc(bytes, s);
             dfd_p = reinterpret_cast<CandDesc*>(fin.get());
             dfc_p = reinterpret_cast<uint64_t*>(fin.get() + at);
-            upload(ctx, s, fin.get(), h.data(), h.size());
+            upload_from(s, fin.get(), h, bytes);
             if (plain) {
                 DevBuf<uint64_t> one_off;
                 one_off.alloc(2 * fd.size(), s);
@@ -1264,6 +1316,10 @@ colo_status colo_create(colo_ctx** out, int device) {
     c->device = device;
     if (cudaSetDevice(device) != cudaSuccess) return COLO_ERR_CUDA;
     if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) return COLO_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking) != cudaSuccess) return COLO_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&c->ev_counted, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_scanned, cudaEventDisableTiming) != cudaSuccess)
+        return COLO_ERR_CUDA;
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     // keep freed blocks in the stream-ordered pool between calls
     cudaMemPool_t pool;

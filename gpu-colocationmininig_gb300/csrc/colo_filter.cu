@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t p
 // full quad is counted at its first occupied cell (qfirst).  Sums go to a
 // block-private accumulator when the level's counters fit (acc_n).
 template <int WT>
-__global__ void __launch_bounds__(256, (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1))) k_filter_drv(
+__global__ void __launch_bounds__(256, (WT <= 4 ? 5 : (WT <= 6 ? 4 : (WT <= 8 ? 2 : 1)))) k_filter_drv(
     uint64_t nunits, uint32_t ngroups, const uint64_t* __restrict__ uoff, const uint32_t* __restrict__ gfeat,
     const uint32_t* __restrict__ gstart, const uint32_t* __restrict__ gcount, const uint64_t* __restrict__ doff,
     const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ order, const uint32_t* __restrict__ need_all,

@@ -104,7 +104,12 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+    """nvidia-smi samples during the timed region (clocks and throttle reasons).
+
+    nvidia-smi starts before the timed steps and the steps begin only after its first sample
+    (its start-up then stalls no timed step); every 20 ms a sample, and the summary keeps the
+    samples that arrived while the steps ran (`mark_start`/`mark_end`), or all of them when the
+    steps were shorter than one interval."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -114,21 +119,31 @@ class ClockSampler:
         self.device = device
         self.rows = []
         self.proc = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "20",
                  "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            deadline = time.monotonic() + 5.0
+            while not self.rows and time.monotonic() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, ValueError):
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([v.strip() for v in line.split(",")])
+            self.rows.append((time.monotonic(), [v.strip() for v in line.split(",")]))
+
+    def mark_start(self):
+        self.t0 = time.monotonic()
+
+    def mark_end(self):
+        self.t1 = time.monotonic()
 
     def __exit__(self, *a):
         if self.proc:
@@ -141,7 +156,9 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        rows = [r for t, r in self.rows
+                if self.t0 is not None and self.t1 is not None and self.t0 - 0.02 <= t <= self.t1 + 0.02]
+        for r in rows or [r for _, r in self.rows]:
             try:
                 sm.append(float(r[1]))
                 mx = float(r[2])
@@ -513,11 +530,13 @@ def main():
         barrier_sync()
         tm = StepTimer(torch, dev, stream, 8 * wl.n)
         with ClockSampler(local) as clk:
+            clk.mark_start()
             for _ in range(args.steps):
                 if not resident:
                     ds.evict()
                 results.append(tm.step(lambda: ctx.mine(ds, params)))
             barrier_sync()
+            clk.mark_end()
         ms = tm.ms()
         units = sum(r.num_candidates() for r in results)
         total, ms = replicas.aggregate(dist, units, ms, dev)   # all ranks' candidates, slowest rank's time

@@ -158,7 +158,7 @@ void level_count(Batch& b, const LevelWork& w, uint32_t k);
 void level_fill(Batch& b, const LevelWork& w, uint32_t k);
 void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow);
 // Participation statistics per candidate and member: [A, last, first, full]
-// (A = set bits in [0, n-2]).
+// (A = set bits in [0, n-2]), added into d_stats, which must be zero.
 void level_pi(Batch& b, const CandDesc* d_cands, uint64_t ncand, uint32_t k, uint64_t* d_stats);
 
 // Squared-distance evaluation of the reference expression for n pairs; with

@@ -98,7 +98,7 @@ __device__ __forceinline__ void head_ballots(uint64_t seg, uint64_t n, const KT*
 // (lane 0 reads it).  An id outside the points (only after a sort that timed
 // out; the host then stops the mine) reads point 0.
 template <class KT>
-__global__ void __launch_bounds__(kHeadThreads) k_gather_heads(uint64_t n, uint32_t F, const KT* __restrict__ keys,
+__global__ void __launch_bounds__(kHeadThreads, 8) k_gather_heads(uint64_t n, uint32_t F, const KT* __restrict__ keys,
                                                               const uint32_t* __restrict__ sid,
                                                               const float2* __restrict__ xy,
                                                               const uint32_t* __restrict__ fstart,
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kHeadThreads) k_gather_heads(uint64_t n, uint3
 }
 
 template <class KT>
-__global__ void __launch_bounds__(kHeadThreads) k_head_compact(
+__global__ void __launch_bounds__(kHeadThreads, 8) k_head_compact(
     uint64_t n, const KT* __restrict__ keys, const uint32_t* __restrict__ sfeat, const uint32_t* __restrict__ fjob,
     const uint64_t* __restrict__ partial, uint64_t* __restrict__ ckey, uint32_t* __restrict__ cstart,
     uint32_t* __restrict__ crun, uint32_t* __restrict__ cjob, uint32_t* __restrict__ rfeat,

@@ -353,52 +353,51 @@ __global__ void __launch_bounds__(256, (MODE != MODE_SINGLE && (K == 3 || K == 4
 
 // Participation statistics: per (candidate, member) [A, last, first, full]
 // where A counts set bits in [0, n-2] (the window getParticipationIndex sums,
-// Codes/DeviceProcess.cu:108-132).
-__global__ void k_level_pi(const CandDesc* __restrict__ cands, uint64_t ncand, uint32_t k,
-                           const uint32_t* __restrict__ fcount, uint64_t* __restrict__ stats) {
-    const uint64_t c = blockIdx.x;
-    if (c >= ncand) return;
+// Codes/DeviceProcess.cu:108-132).  A block takes one (candidate, member)
+// pair (blockIdx.x) and one span of kPiSpan bitmap words (blockIdx.y; spans
+// past the member's bitmap leave at once) and adds its counts to the zeroed
+// statistics; the spans holding bit 0 and bit n-1 also record first and last.
+constexpr uint32_t kPiSpan = 16384;
+
+__global__ void __launch_bounds__(256) k_level_pi(const CandDesc* __restrict__ cands, uint32_t k,
+                                                  const uint32_t* __restrict__ fcount, uint64_t* __restrict__ stats) {
+    const uint64_t c = blockIdx.x / k;
+    const uint32_t j = blockIdx.x - (uint32_t)(c * k);
     const CandDesc& d = cands[c];
-    __shared__ unsigned long long red[32];
-    for (uint32_t j = 0; j < k; ++j) {
-        const uint32_t n = fcount[d.m[j]];
-        const uint32_t* w = d.bitmap + bm_offset(d, j, fcount);
-        const uint32_t nw = (n + 31) / 32;
-        unsigned long long cntA = 0, cntFull = 0;
-        for (uint32_t i = threadIdx.x; i < nw; i += blockDim.x) {
-            uint32_t v = w[i];
-            cntFull += __popc(v);
-            // bits [0, n-2]
-            uint32_t lim = n - 1;   // number of bits in the window
-            uint32_t wb = i * 32;
-            uint32_t mask;
-            if (wb + 32 <= lim) mask = 0xffffffffu;
-            else if (wb >= lim) mask = 0u;
-            else mask = (1u << (lim - wb)) - 1u;
-            cntA += __popc(v & mask);
+    const uint32_t n = fcount[d.m[j]];
+    const uint32_t nw = (n + 31) / 32;
+    const uint32_t w0 = blockIdx.y * kPiSpan;
+    if (w0 >= nw) return;
+    const uint32_t w1 = w0 + kPiSpan < nw ? w0 + kPiSpan : nw;
+    const uint32_t* w = d.bitmap + bm_offset(d, j, fcount);
+    const uint32_t lim = n - 1;   // bits in the window [0, n-2]
+    unsigned long long cntA = 0, cntFull = 0;
+    for (uint32_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) {
+        const uint32_t v = w[i];
+        cntFull += __popc(v);
+        const uint32_t wb = i * 32;
+        const uint32_t mask = wb + 32 <= lim ? 0xffffffffu : (wb >= lim ? 0u : (1u << (lim - wb)) - 1u);
+        cntA += __popc(v & mask);
+    }
+    __shared__ unsigned long long red[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        cntA += __shfl_down_sync(0xffffffffu, cntA, o);
+        cntFull += __shfl_down_sync(0xffffffffu, cntFull, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = cntA | (cntFull << 32);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long A = 0, Fu = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+            A += red[q] & 0xffffffffull;
+            Fu += red[q] >> 32;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            cntA += __shfl_down_sync(0xffffffffu, cntA, o);
-            cntFull += __shfl_down_sync(0xffffffffu, cntFull, o);
-        }
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        if (lane == 0) red[wid] = cntA | (cntFull << 32);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long A = 0, Fu = 0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
-                A += red[q] & 0xffffffffull;
-                Fu += red[q] >> 32;
-            }
-            uint32_t last = (w[(n - 1) >> 5] >> ((n - 1) & 31)) & 1u;
-            uint32_t first = w[0] & 1u;
-            uint64_t* o = stats + (c * k + j) * 4;
-            o[0] = A;
-            o[1] = last;
-            o[2] = first;
-            o[3] = Fu;
-        }
-        __syncthreads();
+        uint64_t* o = stats + (c * k + j) * 4;
+        if (A) atomicAdd(reinterpret_cast<unsigned long long*>(o + 0), A);
+        if (Fu) atomicAdd(reinterpret_cast<unsigned long long*>(o + 3), Fu);
+        if (w0 == 0) o[2] = w[0] & 1u;
+        if ((lim >> 5) >= w0 && (lim >> 5) < w1) o[1] = (w[lim >> 5] >> (lim & 31)) & 1u;
     }
 }
 
@@ -446,8 +445,13 @@ void level_single(Batch& b, const LevelWork& w, uint32_t k, uint32_t* d_overflow
 
 void level_pi(Batch& b, const CandDesc* d_cands, uint64_t ncand, uint32_t k, uint64_t* d_stats) {
     if (ncand == 0) return;
+    if (ncand * k >= (1ull << 31)) throw StatusError{COLO_ERR_CAPACITY, "too many candidates in one level"};
     KScope ks("level_pi");
-    k_level_pi<<<(unsigned)ncand, 256, 0, b.s>>>(d_cands, ncand, k, b.fcount.get(), d_stats);
+    // spans per member: enough for the largest feature of the batch
+    uint32_t fmax = 0;
+    for (uint32_t f = 0; f < b.F; ++f) fmax = std::max(fmax, b.h_fcount[f]);
+    const uint32_t spans = std::max<uint32_t>(1, ((fmax + 31) / 32 + kPiSpan - 1) / kPiSpan);
+    k_level_pi<<<dim3((unsigned)(ncand * k), spans), 256, 0, b.s>>>(d_cands, k, b.fcount.get(), d_stats);
     COLO_LAUNCH_CHECK();
     count_launch();
 }

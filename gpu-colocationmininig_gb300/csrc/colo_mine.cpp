@@ -870,6 +870,14 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         bool force_single = false;
         for (uint32_t j = 0; j < J; ++j) force_single |= (pv[j].reserved[0] & 16) != 0;
+        if (learned && !force_single) {   // no table presized large enough: the order stays as it is
+            bool any = false;
+            for (uint64_t q = 0; q < ncand && !any; ++q) any = pc[q] >= kSinglePassMinRows;
+            if (!any) {
+                cap = pc;
+                learned = false;   // nothing takes the single pass
+            }
+        }
         if (learned) {
             // the candidates whose tables are written while counted go first, largest predicted
             // first (their chunks are taken in that order); the others keep their order, which

@@ -244,7 +244,7 @@ __global__ void k_row_starts(uint64_t rows, uint32_t J, uint64_t M, const uint64
 // 0 <= by <= gy-2 are never full and get no bit.
 // rowstart (optional, rows + 1 entries) bounds the search of a row to the
 // cells of that row.
-__global__ void k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
+__global__ void __launch_bounds__(128, 16) k_nb9(uint64_t M, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cjob,
                       const JobGrid* __restrict__ grids, const uint32_t* __restrict__ rowstart,
                       int32_t* __restrict__ nb9, uint8_t* __restrict__ qfirst) {
     uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

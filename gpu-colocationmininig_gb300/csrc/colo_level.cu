@@ -62,10 +62,11 @@ __device__ __forceinline__ uint64_t bm_offset(const CandDesc& d, uint32_t j, con
 // K = pattern size (2..8), or 0 for a runtime size read from the descriptor
 // (members kept in global memory, slower; only reached for k > 8).  The kernel
 // is latency-bound (a chain of dependent loads per warp), so the count and fill
-// forms of sizes 3 and 4 are held to 64 registers: four 256-thread blocks per SM
-// instead of three (larger sizes would spill).
+// forms of sizes 3 and 4 are held to 64 registers (four 256-thread blocks per SM
+// instead of three; larger sizes would spill) and the fill of pairs to 40 (six:
+// 0.173 -> 0.158 ms of fills per step on the 20M workload).
 template <int K, int MODE>
-__global__ void __launch_bounds__(256, (MODE != MODE_SINGLE && (K == 3 || K == 4)) ? 4 : 1) k_level(
+__global__ void __launch_bounds__(256, (MODE == MODE_FILL && K == 2) ? 6 : (MODE != MODE_SINGLE && (K == 3 || K == 4)) ? 4 : 1) k_level(
     const CandDesc* __restrict__ cands, const uint64_t* __restrict__ chunk_off, uint64_t ncand,
     uint64_t nchunks, const uint64_t* __restrict__ nb_beg, const uint32_t* __restrict__ nb_cnt,
     const uint32_t* __restrict__ nb,

@@ -56,7 +56,7 @@ constexpr unsigned long long kScanVal = (1ull << 62) - 1;
 constexpr uint32_t kScanSpin = 1u << 20;
 
 template <class Tin, class Tout>
-__global__ void __launch_bounds__(kScanThreads, 4) k_scan_1p(const Tin* __restrict__ in, Tout* __restrict__ out,
+__global__ void __launch_bounds__(kScanThreads, 5) k_scan_1p(const Tin* __restrict__ in, Tout* __restrict__ out,
                                                           uint64_t n, unsigned long long* __restrict__ status,
                                                           uint32_t* __restrict__ ticket, Tout* __restrict__ total) {
     __shared__ uint32_t s_tile;

@@ -194,7 +194,10 @@ colo_status colo_result_times(const colo_result* r, double* ms8);
  * launches to their readback, [24] bytes of instance tables placed in pinned
  * host memory. */
 colo_status colo_result_counters(const colo_result* r, uint64_t* c, uint32_t n);
-/* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set). */
+/* Per-kernel CUDA-event timing of the mine (with reserved[0] bit 0 set).  Besides the kernel
+ * families, entries named "gap X" give the stream time between the previous timed kernel and
+ * family X (the GPU waiting for the host), and "host X" the host time from the last wait on
+ * the stream to X's launch. */
 uint32_t colo_result_num_kernels(const colo_result* r);
 colo_status colo_result_kernel(const colo_result* r, uint32_t i, char* name, size_t cap, uint64_t* launches,
                                double* ms);

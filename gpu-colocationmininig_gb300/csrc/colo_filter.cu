@@ -168,8 +168,11 @@ __global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t p
                                                           const uint64_t* __restrict__ doff,
                                                           uint32_t* __restrict__ cursor, uint32_t* __restrict__ dlist,
                                                           const uint32_t* __restrict__ want) {
-    __shared__ unsigned long long s_base[kDilHist];
-    __shared__ uint32_t s_cnt[kDilHist], s_touch[kDilHist], s_nt;
+    // F bases, then F counters and F touched features (F <= kDilHist; sized by the launch)
+    extern __shared__ unsigned long long s_base[];
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_base + (F <= kDilHist ? F : 0));
+    uint32_t* s_touch = s_cnt + (F <= kDilHist ? F : 0);
+    __shared__ uint32_t s_nt;
     const bool local = F <= kDilHist;
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t z0 = (uint64_t)blockIdx.x * per, z1 = z0 + per < M ? z0 + per : M;
@@ -401,17 +404,19 @@ void driver_lists_fill(Batch& b, const std::vector<uint8_t>& need) {
     DevBuf<uint32_t> cursor;
     cursor.alloc(b.F, s);
     cursor.zero(s);
-    // one range of consecutive cells per block (a multiple of 256 cells), one wave of resident blocks
+    // one range of consecutive cells per block (a multiple of 256 cells), one wave of resident blocks;
+    // shared memory for the block histogram of the batch's features (none past kDilHist)
+    const size_t dsmem = b.F <= kDilHist ? (size_t)b.F * 16 : 0;
     KScope ks("driver_lists");
 #define COLO_DF(WW)                                                                                              \
     do {                                                                                                         \
         int per_sm = 1;                                                                                          \
-        COLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dil_fill<WW>, kDilThreads, 0));       \
+        COLO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dil_fill<WW>, kDilThreads, dsmem));   \
         uint64_t blocks = std::min<uint64_t>((b.M + kDilThreads - 1) / kDilThreads,                              \
                                              (uint64_t)b.sms * (uint64_t)std::max(per_sm, 1));                   \
         const uint64_t per = ((b.M + blocks - 1) / blocks + kDilThreads - 1) / kDilThreads * kDilThreads;        \
         blocks = (b.M + per - 1) / per;                                                                          \
-        k_dil_fill<WW><<<(unsigned)blocks, kDilThreads, 0, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr,      \
+        k_dil_fill<WW><<<(unsigned)blocks, kDilThreads, dsmem, s>>>(b.M, per, b.J > 1 ? b.cjob.get() : nullptr,  \
                                                                b.grids.get(), b.nbmask.get(), b.F, b.doff.get(), \
                                                                cursor.get(), b.dlist.get(), d_want);             \
     } while (0)

@@ -62,11 +62,13 @@ __device__ __forceinline__ uint64_t bm_offset(const CandDesc& d, uint32_t j, con
 // K = pattern size (2..8), or 0 for a runtime size read from the descriptor
 // (members kept in global memory, slower; only reached for k > 8).  The kernel
 // is latency-bound (a chain of dependent loads per warp), so the count and fill
-// forms of sizes 3 and 4 are held to 64 registers (four 256-thread blocks per SM
-// instead of three; larger sizes would spill) and the fill of pairs to 40 (six:
-// 0.173 -> 0.158 ms of fills per step on the 20M workload).
+// forms are held to fewer registers for more resident warps: pairs' count at
+// eight 256-thread blocks per SM and their fill at six, size 3 at five, size 4
+// at four (a few registers spill; larger sizes would spill more).  On the 20M
+// workload the fills went 0.173 -> 0.158 ms and the counts 0.478 -> 0.466 ms per
+// step.
 template <int K, int MODE>
-__global__ void __launch_bounds__(256, (MODE == MODE_FILL && K == 2) ? 6 : (MODE != MODE_SINGLE && (K == 3 || K == 4)) ? 4 : 1) k_level(
+__global__ void __launch_bounds__(256, (MODE == MODE_COUNT && K == 2) ? 8 : (MODE == MODE_FILL && K == 2) ? 6 : (MODE != MODE_SINGLE && K == 3) ? 5 : (MODE != MODE_SINGLE && K == 4) ? 4 : 1) k_level(
     const CandDesc* __restrict__ cands, const uint64_t* __restrict__ chunk_off, uint64_t ncand,
     uint64_t nchunks, const uint64_t* __restrict__ nb_beg, const uint32_t* __restrict__ nb_cnt,
     const uint32_t* __restrict__ nb,

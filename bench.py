@@ -576,13 +576,14 @@ def main():
 
     # per-kernel CUDA-event times (a separate profiled pass, so `value` carries no event overhead)
     ms_k, res_k, _, _ = timed(head_mode, True, profile=True)
-    kern, gaps, hosts = {}, {}, {}
+    kern, gaps, hosts, parts = {}, {}, {}, {}
     for r in res_k:
         for name, (nl, kms) in r.kernels.items():
             # "gap X": stream time between the previous timed scope and X (the GPU waiting for the host);
             # "host X": host time from the last wait's return to X's launch
-            a = (gaps if name.startswith("gap ") else hosts if name.startswith("host ") else kern).setdefault(
-                name, [0, 0.0])
+            # "part X": host time of one part of the level loop (between two marks)
+            a = (gaps if name.startswith("gap ") else hosts if name.startswith("host ")
+                 else parts if name.startswith("part ") else kern).setdefault(name, [0, 0.0])
             a[0] += nl
             a[1] += kms
     counters = dict(res_b[0].counters)
@@ -610,6 +611,8 @@ def main():
                      for name, (nl, kms) in sorted(gaps.items(), key=lambda kv: -kv[1][1])}
     host_per_step = {name[5:]: round(kms / args.steps, 3)
                      for name, (nl, kms) in sorted(hosts.items(), key=lambda kv: -kv[1][1])}
+    parts_per_step = {name[5:]: round(kms / args.steps, 3)
+                      for name, (nl, kms) in sorted(parts.items(), key=lambda kv: -kv[1][1])}
     phases = {k: round(statistics.mean(r.times[k] for r in res_b), 3)
               for k in ("bucket", "join", "filter", "refine", "fill", "apriori", "total")}
     if rank != 0:
@@ -660,6 +663,7 @@ def main():
         "gpu_launches": int(sum(r.counters["launches"] for r in res_b)),
         "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,
         "idle_before_kernel_per_step": gaps_per_step, "host_after_wait_per_step": host_per_step,
+        "level_loop_host_ms_per_step": parts_per_step,
         "host_phase_ms": phases,
         "io": io,
         "side_configs": side,

@@ -221,6 +221,19 @@ struct KTimer {
         waited = std::chrono::steady_clock::now();
         after_wait = true;
     }
+    // Host time between two marks of the level loop, charged to "part <name>"
+    // (profile mode): where the host spends the time between a wait and a launch.
+    std::chrono::steady_clock::time_point marked{};
+    void mark(const char* name) {
+        if (!on) return;
+        const auto now = std::chrono::steady_clock::now();
+        if (marked.time_since_epoch().count()) {
+            KernelStat& h = stats[slot((std::string("part ") + name).c_str())];
+            h.ms += std::chrono::duration<double, std::milli>(now - marked).count();
+            h.launches++;
+        }
+        marked = now;
+    }
     void begin(const char* name) {
         if (!on || depth++ > 0) return;
         if (after_wait) {

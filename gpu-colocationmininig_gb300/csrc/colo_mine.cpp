@@ -712,7 +712,9 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
             std::vector<unsigned char> hout(out_bytes);
             rb.copy(hout.data(), fb, out_bytes);
+            kt.mark("filter launches");
             rb.finish();
+            kt.mark("filter wait");
             std::vector<uint32_t> hub(ncand * k);
             std::vector<uint64_t> hfs(ncand * 2);
             std::memcpy(hub.data(), hout.data() + o_ub, hub.size() * 4);
@@ -798,6 +800,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
         }
         t_filter += ms_since(t0);
+        kt.mark("filter results");
 
         // ---- refinement: count pass + participation ----
         t0 = Clock::now();
@@ -848,6 +851,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
         }
         const uint64_t ncand = hd.size();
+        kt.mark("refine descriptors");
         // LEARNED: predicted rows presize one-pass tables; the queue runs largest first
         bool learned = mode == COLO_MODE_LEARNED && !ctx->model.empty() && ncand > 0;
         std::vector<uint64_t> cap, pc;
@@ -918,6 +922,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         if (ns == ncand) chunk_all.push_back(0);
         const uint64_t nch_single = chunk_all[ns], nch_count = chunk_all.back();
+        kt.mark("refine presize");
         LevelArena ar;
         DevBuf<uint64_t> G;   // the fill's output offsets: the scan of every parent row's count
         // the side stream's scan reads the arena and writes G: the main stream waits for it
@@ -950,6 +955,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 o += cap[q] * k;
             }
         }
+        kt.mark("refine arena");
         std::vector<uint64_t> hstats(ncand * k * 4);
         Readback rb(ctx, s, ar.out_bytes + sizeof(DevFlags));
         cnt_refined += ncand;
@@ -1013,7 +1019,9 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         if (ar.out_bytes) rb.copy(hout.data(), ar.out, ar.out_bytes);
         DevFlags hflags{};
         if (ns) rb.copy(&hflags, b.flags.get(), sizeof(hflags));
+        kt.mark("refine launches");
         rb.finish();
+        kt.mark("refine wait");
         if (ncand) {
             std::memcpy(hrows.data(), hout.data(), ncand * 8);
             std::memcpy(&h_items, hout.data() + ncand * 8, 8);
@@ -1062,6 +1070,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         for (uint64_t q = 0; q < ncand; ++q) gb[q + 1] = gb[q] + hrows[q];
         for (uint64_t q = 0; q < ncand; ++q) tr[owner[q].first]->rows[owner[q].second] = gb[q + 1] - gb[q];
         t_refine += ms_since(t0);
+        kt.mark("refine results");
 
         // ---- next candidates (Apriori) and the tables they need ----
         t0 = Clock::now();
@@ -1113,6 +1122,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         }
         t_apriori += ms_since(t0);
 
+        kt.mark("apriori");
         // ---- fill pass for the needed prevalent patterns ----
         t0 = Clock::now();
         std::vector<uint64_t> fillq, keepq;   // keepq: tables the single pass already wrote whole
@@ -1234,6 +1244,7 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             }
         }
         t_fill += ms_since(t0);
+        kt.mark("fill launches");
         tables_prev = std::move(tables_cur);
         single_prev = std::move(single_cur);
         for (auto& st : js)

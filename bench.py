@@ -97,6 +97,11 @@ class StepTimer:
         """Total of the steps' times (after a synchronize)."""
         return sum(a.elapsed_time(b) for a, b in self.pairs)
 
+    def spread(self) -> dict:
+        """Fastest, median and slowest step (ms), to show a step that stalled."""
+        t = sorted(a.elapsed_time(b) for a, b in self.pairs)
+        return {"min": round(t[0], 3), "median": round(statistics.median(t), 3), "max": round(t[-1], 3)} if t else {}
+
 
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
@@ -518,6 +523,8 @@ def main():
             dist.barrier()
         torch.cuda.synchronize(dev)
 
+    spreads = {}
+
     def timed(mode, resident, profile=False):
         params = colo.default_params(wl.R, wl.thr, mode, max_size=wl.max_size, profile=profile)
         if resident:
@@ -538,6 +545,7 @@ def main():
             barrier_sync()
             clk.mark_end()
         ms = tm.ms()
+        spreads[(mode, resident, profile)] = tm.spread()
         units = sum(r.num_candidates() for r in results)
         total, ms = replicas.aggregate(dist, units, ms, dev)   # all ranks' candidates, slowest rank's time
         return ms, results, clk.summary(), total
@@ -660,6 +668,9 @@ def main():
                              "overflow_fallback": int(res_b[0].counters["single_pass_overflow"])}
                             if head_mode == colo.MODE_LEARNED else None),
         "identical_patterns_all_forms": same,
+        "step_ms_spread": {"headline": spreads.get((head_mode, True, False)), "e2e": spreads.get((head_mode, False, False)),
+                           "batched": spreads.get((colo.MODE_BATCHED, True, False)),
+                           "plain": spreads.get((colo.MODE_PLAIN, True, False))},
         "gpu_launches": int(sum(r.counters["launches"] for r in res_b)),
         "clocks": clocks, "roofline": roof, "cpu_baseline": cpu, "kernels_per_step": per_kernel,
         "idle_before_kernel_per_step": gaps_per_step, "host_after_wait_per_step": host_per_step,

@@ -204,6 +204,9 @@ struct JobState {
 // candidates are generated on the device (apriori_device); below it the host
 // loop is faster than the launches and copies.
 constexpr uint64_t kDeviceAprioriMin = 4096;
+// Prevalent tables up to this many words (1 GiB) are filled before Apriori decides which
+// of them the next level needs, so that the host's Apriori overlaps the fill.
+constexpr uint64_t kEarlyFillWords = 1ull << 28;
 
 std::vector<uint32_t> apriori_next(const std::vector<uint32_t>& prev, uint32_t km1, std::vector<uint32_t>& parent) {
     std::vector<uint32_t> out;
@@ -1072,64 +1075,84 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         t_refine += ms_since(t0);
         kt.mark("refine results");
 
-        // ---- next candidates (Apriori) and the tables they need ----
+        // ---- next candidates (Apriori), the tables they need, and the fill ----
+        // A table is needed when its pattern is the prefix of a next-level candidate, so Apriori
+        // decides which prevalent tables to fill.  When the prevalent tables are small (and not
+        // filled one at a time, as in the plain form), every prevalent table is filled first and
+        // Apriori runs on the host while the GPU fills; only the needed tables are then recorded
+        // (has_table, the next level's parents, the kept tables) -- the same results either way.
         t0 = Clock::now();
+        bool next_possible = false;
+        for (uint32_t j = 0; j < J; ++j)
+            next_possible |= tr[j] && (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf &&
+                             k + 1 <= (uint32_t)kMaxK;
+        uint64_t prevalent_words = 0;
+        for (uint64_t q = 0; q < ncand; ++q)
+            if (prev_flag[q] && !(q < ns && !hovf[q])) prevalent_words += (gb[q + 1] - gb[q]) * k;
+        const bool early_fill = !plain && !host_tables && next_possible && prevalent_words <= kEarlyFillWords;
+
         // needed[j][c]: candidate c of this level is the prefix of a next-level candidate
         std::vector<std::vector<uint8_t>> needed(J);
-        std::vector<std::vector<uint32_t>> prevs(J), prevcs(J), dnext, dpar;
-        std::vector<const std::vector<uint32_t>*> gen(J, nullptr);
-        uint64_t prev_total = 0;
-        for (uint32_t j = 0; j < J; ++j) {
-            if (!tr[j]) continue;
-            LevelTrace& L = *tr[j];
-            for (size_t c = 0; c < L.cand.size() / k; ++c)
-                if (L.prevalent[c]) {
-                    prevs[j].insert(prevs[j].end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
-                    prevcs[j].push_back((uint32_t)c);
-                }
-            const bool cap_ok = (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf;
-            if (cap_ok) {
-                gen[j] = &prevs[j];
-                prev_total += prevcs[j].size();
-            }
-        }
-        // many prevalent patterns: all jobs' candidates in two device passes
-        bool force_dev = false;
-        for (uint32_t j = 0; j < J; ++j) force_dev |= (pv[j].reserved[0] & 4) != 0;
-        const bool on_device = (prev_total >= kDeviceAprioriMin || (force_dev && prev_total > 0)) &&
-                               k + 1 <= (uint32_t)kMaxK;
-        if (on_device) apriori_device(s, gen, k, dnext, dpar);
-        for (uint32_t j = 0; j < J; ++j) {
-            if (!tr[j]) continue;
-            LevelTrace& L = *tr[j];
-            const std::vector<uint32_t>& prev_c = prevcs[j];
-            std::vector<uint32_t> next, par;
-            if (gen[j]) {
-                if (on_device) {
-                    next = std::move(dnext[j]);
-                    par = std::move(dpar[j]);
-                } else {
-                    next = apriori_next(prevs[j], k, par);
+        auto run_apriori = [&]() {
+            const auto ta = Clock::now();
+            std::vector<std::vector<uint32_t>> prevs(J), prevcs(J), dnext, dpar;
+            std::vector<const std::vector<uint32_t>*> gen(J, nullptr);
+            uint64_t prev_total = 0;
+            for (uint32_t j = 0; j < J; ++j) {
+                if (!tr[j]) continue;
+                LevelTrace& L = *tr[j];
+                for (size_t c = 0; c < L.cand.size() / k; ++c)
+                    if (L.prevalent[c]) {
+                        prevs[j].insert(prevs[j].end(), L.cand.begin() + c * k, L.cand.begin() + (c + 1) * k);
+                        prevcs[j].push_back((uint32_t)c);
+                    }
+                const bool cap_ok = (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf;
+                if (cap_ok) {
+                    gen[j] = &prevs[j];
+                    prev_total += prevcs[j].size();
                 }
             }
-            js[j].cands = next;
-            needed[j].assign(L.cand.size() / k, 0);
-            for (auto& pp : par) {
-                pp = prev_c[pp];        // now an index among this level's candidates
-                needed[j][pp] = 1;
+            // many prevalent patterns: all jobs' candidates in two device passes
+            bool force_dev = false;
+            for (uint32_t j = 0; j < J; ++j) force_dev |= (pv[j].reserved[0] & 4) != 0;
+            const bool on_device = (prev_total >= kDeviceAprioriMin || (force_dev && prev_total > 0)) &&
+                                   k + 1 <= (uint32_t)kMaxK;
+            if (on_device) apriori_device(s, gen, k, dnext, dpar);
+            for (uint32_t j = 0; j < J; ++j) {
+                if (!tr[j]) continue;
+                LevelTrace& L = *tr[j];
+                const std::vector<uint32_t>& prev_c = prevcs[j];
+                std::vector<uint32_t> next, par;
+                if (gen[j]) {
+                    if (on_device) {
+                        next = std::move(dnext[j]);
+                        par = std::move(dpar[j]);
+                    } else {
+                        next = apriori_next(prevs[j], k, par);
+                    }
+                }
+                js[j].cands = next;
+                needed[j].assign(L.cand.size() / k, 0);
+                for (auto& pp : par) {
+                    pp = prev_c[pp];        // now an index among this level's candidates
+                    needed[j][pp] = 1;
+                }
+                js[j].parent = std::move(par);
             }
-            js[j].parent = std::move(par);
+            t_apriori += ms_since(ta);
+            kt.mark("apriori");
+        };
+        if (!early_fill) {
+            run_apriori();
+            t0 = Clock::now();   // the fill's own time
         }
-        t_apriori += ms_since(t0);
 
-        kt.mark("apriori");
-        // ---- fill pass for the needed prevalent patterns ----
-        t0 = Clock::now();
+        // ---- fill pass for the (needed) prevalent patterns ----
         std::vector<uint64_t> fillq, keepq;   // keepq: tables the single pass already wrote whole
         uint64_t total_rows = 0;
         for (uint64_t q = 0; q < ncand; ++q) {
             if (!prev_flag[q]) continue;
-            if (!needed[owner[q].first][owner[q].second]) continue;
+            if (!early_fill && !needed[owner[q].first][owner[q].second]) continue;
             if (q < ns && !hovf[q]) {
                 keepq.push_back(q);
                 continue;
@@ -1168,9 +1191,6 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             obase += rows * k;
             fd.push_back(d);
             fchunk.push_back(fchunk.back() + (d.prow + 31) / 32);
-            LevelTrace& L = *tr[owner[q].first];
-            size_t c = owner[q].second;
-            L.has_table[c] = 1;
         }
         rows_written += total_rows;
         cnt_fillw += total_rows * k;
@@ -1208,6 +1228,12 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
                 level_fill(b, w, k);
             }
         }
+        if (early_fill) run_apriori();   // on the host while the GPU fills
+        // the needed tables among those written
+        for (uint64_t q : fillq) {
+            if (!needed[owner[q].first][owner[q].second]) continue;
+            tr[owner[q].first]->has_table[owner[q].second] = 1;
+        }
         // the tables are read back only when kept in the result (a copy on another stream); else
         // the next level's launches queue behind the fill on this stream without a wait
         bool keep_any = false;
@@ -1219,8 +1245,11 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
             if (tr[j]) js[j].prev_tables.assign(tr[j]->cand.size() / k, TableRef{});
         }
         std::vector<std::pair<uint64_t, TableRef>> made;
-        for (size_t i = 0; i < fillq.size(); ++i) made.push_back({fillq[i], TableRef{fd[i].out, fd[i].out_rows, fd[i].out_rows}});
+        for (size_t i = 0; i < fillq.size(); ++i)
+            if (needed[owner[fillq[i]].first][owner[fillq[i]].second])
+                made.push_back({fillq[i], TableRef{fd[i].out, fd[i].out_rows, fd[i].out_rows}});
         for (uint64_t q : keepq) {
+            if (!needed[owner[q].first][owner[q].second]) continue;
             made.push_back({q, TableRef{hd[q].out, gb[q + 1] - gb[q], cap[q]}});
             tr[owner[q].first]->has_table[owner[q].second] = 1;
         }

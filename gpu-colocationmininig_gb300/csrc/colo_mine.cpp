@@ -1077,19 +1077,39 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
 
         // ---- next candidates (Apriori), the tables they need, and the fill ----
         // A table is needed when its pattern is the prefix of a next-level candidate, so Apriori
-        // decides which prevalent tables to fill.  When the prevalent tables are small (and not
-        // filled one at a time, as in the plain form), every prevalent table is filled first and
-        // Apriori runs on the host while the GPU fills; only the needed tables are then recorded
+        // decides which prevalent tables to fill.  When the tables that can be needed are small
+        // (and not filled one at a time, as in the plain form), they are filled first and Apriori
+        // runs on the host while the GPU fills; only the needed tables are then recorded
         // (has_table, the next level's parents, the kept tables) -- the same results either way.
         t0 = Clock::now();
         bool next_possible = false;
         for (uint32_t j = 0; j < J; ++j)
             next_possible |= tr[j] && (js[j].max_size == 0 || k + 1 <= js[j].max_size) && k + 1 <= js[j].nf &&
                              k + 1 <= (uint32_t)kMaxK;
-        uint64_t prevalent_words = 0;
+        // A next-level candidate joins two prevalent patterns with the same first k-1 members and
+        // its prefix is the first of them (candidateColocationGeneral, colocationFinder.cpp:517-557),
+        // so only a prevalent pattern followed by a prevalent sibling (candidates are in
+        // lexicographic order) can be needed: maybe[j][c] marks those.
+        std::vector<std::vector<uint8_t>> maybe(J);
+        for (uint32_t j = 0; j < J; ++j) {
+            if (!tr[j]) continue;
+            const LevelTrace& L = *tr[j];
+            const size_t C = L.cand.size() / k;
+            maybe[j].assign(C, 0);
+            size_t last = SIZE_MAX;   // the previous prevalent candidate
+            for (size_t c = 0; c < C; ++c) {
+                if (!L.prevalent[c]) continue;
+                if (last != SIZE_MAX && std::equal(L.cand.begin() + last * k, L.cand.begin() + last * k + (k - 1),
+                                                   L.cand.begin() + c * k))
+                    maybe[j][last] = 1;
+                last = c;
+            }
+        }
+        uint64_t maybe_words = 0;
         for (uint64_t q = 0; q < ncand; ++q)
-            if (prev_flag[q] && !(q < ns && !hovf[q])) prevalent_words += (gb[q + 1] - gb[q]) * k;
-        const bool early_fill = !plain && !host_tables && next_possible && prevalent_words <= kEarlyFillWords;
+            if (prev_flag[q] && maybe[owner[q].first][owner[q].second] && !(q < ns && !hovf[q]))
+                maybe_words += (gb[q + 1] - gb[q]) * k;
+        const bool early_fill = !plain && !host_tables && next_possible && maybe_words <= kEarlyFillWords;
 
         // needed[j][c]: candidate c of this level is the prefix of a next-level candidate
         std::vector<std::vector<uint8_t>> needed(J);
@@ -1152,7 +1172,8 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         uint64_t total_rows = 0;
         for (uint64_t q = 0; q < ncand; ++q) {
             if (!prev_flag[q]) continue;
-            if (!early_fill && !needed[owner[q].first][owner[q].second]) continue;
+            if (early_fill ? !maybe[owner[q].first][owner[q].second] : !needed[owner[q].first][owner[q].second])
+                continue;
             if (q < ns && !hovf[q]) {
                 keepq.push_back(q);
                 continue;

@@ -324,6 +324,11 @@ void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t
                      uint32_t* total_host, uint32_t* total_dev = nullptr);
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host, uint64_t* total_dev = nullptr);
+// The join's run scans in one pass: act_r = rcnt[r] if run_L[r] > 0 else 0 and
+// cap_r = act_r * run_L[r], scanned exclusively into act_off and cap_off; the
+// totals land in device memory (no wait).
+void run_scans(const uint32_t* rcnt, const uint32_t* run_L, uint32_t* act_off, uint64_t* cap_off, uint64_t Rn,
+               cudaStream_t s, uint32_t* act_total, uint64_t* cap_total);
 // Digit split of a radix sort: pass p sorts width[p] (<= 8) bits from shift[p].
 constexpr int kRadixDigits = 256;
 constexpr int kRadixMaxPasses = 8;

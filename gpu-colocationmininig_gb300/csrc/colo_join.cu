@@ -25,15 +25,6 @@ namespace {
 
 enum { J_SINGLE = 0, J_COUNT = 1, J_FILL = 2 };
 
-__global__ void k_run_caps(uint64_t Rn, const uint32_t* __restrict__ rcnt, const uint32_t* __restrict__ run_L,
-                           uint32_t* __restrict__ act, uint64_t* __restrict__ cap) {
-    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= Rn) return;
-    uint32_t L = run_L[r];
-    act[r] = L ? rcnt[r] : 0u;
-    cap[r] = L ? (uint64_t)rcnt[r] * L : 0ull;
-}
-
 // thread per run: list the run's anchors (sorted positions) when it has targets
 __global__ void k_expand_active(uint64_t Rn, const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ rcnt,
                                 const uint32_t* __restrict__ run_L, const uint32_t* __restrict__ act_off,
@@ -162,25 +153,17 @@ static const uint64_t kSinglePassCap = 1ull << 30;
 void join_neighbors(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t Rn = b.Rn;
-    DevBuf<uint32_t> act, act_off;
-    DevBuf<uint64_t> cap, cap_off;
-    act.alloc(Rn, s);
-    cap.alloc(Rn, s);
+    DevBuf<uint32_t> act_off;
+    DevBuf<uint64_t> cap_off;
     act_off.alloc(Rn, s);
     cap_off.alloc(Rn, s);
-    {
-        KScope ks("join_setup");
-        k_run_caps<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rcnt.get(), b.run_L.get(), act.get(), cap.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
-    }
-    // active anchors A and the single-pass layout's size U (= pair
-    // evaluations), read back together with one wait
+    // per run: active anchors (its points, when it has targets) and the single-pass layout's
+    // capacity (points x targets), both scanned in one pass; the totals A and U (= pair
+    // evaluations) come back together with one wait
     DevBuf<uint64_t> totals;
     totals.alloc(2, s);
-    totals.zero(s);
-    scan_u32_to_u32(act.get(), act_off.get(), Rn, s, nullptr, reinterpret_cast<uint32_t*>(totals.get()));
-    scan_u64_to_u64(cap.get(), cap_off.get(), Rn, s, nullptr, totals.get() + 1);
+    run_scans(b.rcnt.get(), b.run_L.get(), act_off.get(), cap_off.get(), Rn, s,
+              reinterpret_cast<uint32_t*>(totals.get()), totals.get() + 1);
     uint64_t ht[2] = {0, 0};
     COLO_CUDA(cudaMemcpyAsync(ht, totals.get(), 16, cudaMemcpyDeviceToHost, s));
     stream_wait(s);

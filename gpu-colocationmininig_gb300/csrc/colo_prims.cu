@@ -55,6 +55,52 @@ constexpr unsigned long long kScanP = 2ull << 62;   // inclusive prefix publishe
 constexpr unsigned long long kScanVal = (1ull << 62) - 1;
 constexpr uint32_t kScanSpin = 1u << 20;
 
+// Decoupled look-back by one full warp for tile `tile` of a single-pass scan:
+// publishes the tile's sum `agg`, reads the predecessors' words 32 at a time
+// back to the nearest inclusive prefix, publishes the tile's own inclusive
+// prefix and returns the exclusive one.  Past the poll limit it returns false
+// and publishes nothing more; the caller then computes the prefix itself and
+// publishes it with lookback_publish.
+__device__ __forceinline__ bool warp_lookback(unsigned long long* status, uint32_t tile, unsigned long long agg,
+                                              unsigned long long& prefix) {
+    const int lane = threadIdx.x & 31;
+    prefix = 0;
+    volatile unsigned long long* st = status + tile;
+    if (tile == 0) {
+        if (lane == 0) *st = kScanP | agg;
+        return true;
+    }
+    if (lane == 0) *st = kScanA | agg;
+    int64_t base = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (true) {
+        const int64_t t = base - lane;
+        const unsigned long long sv = t >= 0 ? *(volatile const unsigned long long*)(status + t) : kScanP;
+        const unsigned long long flag = sv & ~kScanVal;
+        const uint32_t pm = __ballot_sync(0xffffffffu, flag == kScanP);
+        const uint32_t zm = __ballot_sync(0xffffffffu, flag == 0);
+        const int fp = pm ? __ffs(pm) - 1 : 32;   // nearest inclusive prefix
+        const uint32_t upto = fp == 32 ? 0xffffffffu : ((2u << fp) - 1u);
+        if (zm & upto) {   // a predecessor has not published yet
+            if (++spins > kScanSpin) return false;
+            __nanosleep(32);
+            continue;
+        }
+        unsigned long long add = ((upto >> lane) & 1u) ? (sv & kScanVal) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
+        prefix += add;
+        if (fp < 32) break;
+        base -= 32;
+    }
+    if (lane == 0) *st = kScanP | (prefix + agg);
+    return true;
+}
+
+__device__ __forceinline__ void lookback_publish(unsigned long long* status, uint32_t tile, unsigned long long incl) {
+    if ((threadIdx.x & 31) == 0) *(volatile unsigned long long*)(status + tile) = kScanP | incl;
+}
+
 template <class Tin, class Tout>
 __global__ void __launch_bounds__(kScanThreads, 5) k_scan_1p(const Tin* __restrict__ in, Tout* __restrict__ out,
                                                           uint64_t n, unsigned long long* __restrict__ status,
@@ -77,46 +123,14 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan_1p(const Tin* __restri
     Tout tot;
     const Tout ex_thread = block_excl_scan<Tout>(sum, &tot);
     if (w == 0) {
-        unsigned long long prefix = 0;
-        volatile unsigned long long* st = status + tile;
-        if (tile == 0) {
-            if (lane == 0) *st = kScanP | (unsigned long long)tot;
-        } else {
-            if (lane == 0) *st = kScanA | (unsigned long long)tot;
-            int64_t base = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            bool ok = true;
-            while (true) {
-                const int64_t t = base - lane;
-                const unsigned long long sv = t >= 0 ? *(volatile const unsigned long long*)(status + t) : kScanP;
-                const unsigned long long flag = sv & ~kScanVal;
-                const uint32_t pm = __ballot_sync(0xffffffffu, flag == kScanP);
-                const uint32_t zm = __ballot_sync(0xffffffffu, flag == 0);
-                const int fp = pm ? __ffs(pm) - 1 : 32;   // nearest inclusive prefix
-                const uint32_t upto = fp == 32 ? 0xffffffffu : ((2u << fp) - 1u);
-                if (zm & upto) {   // a predecessor has not published yet
-                    if (++spins > kScanSpin) {
-                        ok = false;
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                unsigned long long add = ((upto >> lane) & 1u) ? (sv & kScanVal) : 0ull;
+        unsigned long long prefix;
+        if (!warp_lookback(status, tile, (unsigned long long)tot, prefix)) {   // the predecessors' items, summed here
+            unsigned long long add = 0;
+            for (uint64_t p = lane; p < (uint64_t)tile * kScan1Tile; p += 32) add += (unsigned long long)(Tout)in[p];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
-                prefix += add;
-                if (fp < 32) break;
-                base -= 32;
-            }
-            if (!ok) {   // the predecessors' items, summed here
-                unsigned long long add = 0;
-                for (uint64_t p = lane; p < (uint64_t)tile * kScan1Tile; p += 32) add += (unsigned long long)(Tout)in[p];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
-                prefix = add;
-            }
-            if (lane == 0) *st = kScanP | (prefix + (unsigned long long)tot);
+            for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
+            prefix = add;
+            lookback_publish(status, tile, prefix + (unsigned long long)tot);
         }
         if (lane == 0) s_prefix = prefix;
     }
@@ -131,6 +145,87 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan_1p(const Tin* __restri
         carry += __shfl_sync(0xffffffffu, inc, 31);
     }
     if (total && threadIdx.x == 0 && (uint64_t)(tile + 1) * kScan1Tile >= n) *total = (Tout)s_prefix + tot;
+}
+
+// The join's two run scans in one pass: per run r the active anchors
+// act_r = rcnt[r] when the run has targets (run_L[r] > 0) and the single-pass
+// layout's capacity cap_r = rcnt[r] * run_L[r] (both 0 otherwise), scanned
+// exclusively into act_off (32-bit) and cap_off (64-bit), with the totals;
+// warps 0 and 1 look back for the two scans at once.  Tiles of 2048 runs (two
+// values per run in registers).
+constexpr int kRunItems = 8;
+constexpr int kRunTile = kScanThreads * kRunItems;
+
+__global__ void __launch_bounds__(kScanThreads, 4) k_run_scans(uint64_t Rn, const uint32_t* __restrict__ rcnt,
+                                                            const uint32_t* __restrict__ run_L,
+                                                            uint32_t* __restrict__ act_off, uint64_t* __restrict__ cap_off,
+                                                            unsigned long long* __restrict__ status,
+                                                            uint32_t* __restrict__ ticket, uint32_t* __restrict__ act_total,
+                                                            uint64_t* __restrict__ cap_total) {
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_prefix[2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t ntiles = (Rn + kRunTile - 1) / kRunTile;
+    unsigned long long* st_act = status;
+    unsigned long long* st_cap = status + ntiles;
+    const uint64_t seg = (uint64_t)tile * kRunTile + (uint64_t)w * (32 * kRunItems);
+    uint32_t a[kRunItems], L[kRunItems];
+    uint32_t asum = 0;
+    uint64_t csum = 0;
+#pragma unroll
+    for (int i = 0; i < kRunItems; ++i) {
+        const uint64_t p = seg + (uint64_t)i * 32 + lane;
+        const uint32_t l = p < Rn ? run_L[p] : 0u;
+        a[i] = l ? rcnt[p] : 0u;
+        L[i] = l;
+        asum += a[i];
+        csum += (uint64_t)a[i] * l;
+    }
+    uint32_t atot;
+    uint64_t ctot;
+    const uint32_t aex = block_excl_scan<uint32_t>(asum, &atot);
+    const uint64_t cex = block_excl_scan<uint64_t>(csum, &ctot);
+    if (w < 2) {
+        unsigned long long* st = w == 0 ? st_act : st_cap;
+        const unsigned long long agg = w == 0 ? (unsigned long long)atot : (unsigned long long)ctot;
+        unsigned long long prefix;
+        if (!warp_lookback(st, tile, agg, prefix)) {   // the predecessors' runs, summed here
+            unsigned long long add = 0;
+            for (uint64_t p = lane; p < (uint64_t)tile * kRunTile; p += 32) {
+                const uint32_t l = run_L[p];
+                const uint64_t av = l ? rcnt[p] : 0u;
+                add += w == 0 ? av : av * l;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
+            prefix = add;
+            lookback_publish(st, tile, prefix + agg);
+        }
+        if (lane == 0) s_prefix[w] = prefix;
+    }
+    __syncthreads();
+    uint32_t acarry = __shfl_sync(0xffffffffu, aex, 0) + (uint32_t)s_prefix[0];
+    uint64_t ccarry = __shfl_sync(0xffffffffu, cex, 0) + (uint64_t)s_prefix[1];
+#pragma unroll
+    for (int i = 0; i < kRunItems; ++i) {
+        const uint64_t cv = (uint64_t)a[i] * L[i];
+        const uint32_t ainc = warp_incl_scan(a[i]);
+        const uint64_t cinc = warp_incl_scan(cv);
+        const uint64_t p = seg + (uint64_t)i * 32 + lane;
+        if (p < Rn) {
+            act_off[p] = acarry + ainc - a[i];
+            cap_off[p] = ccarry + cinc - cv;
+        }
+        acarry += __shfl_sync(0xffffffffu, ainc, 31);
+        ccarry += __shfl_sync(0xffffffffu, cinc, 31);
+    }
+    if (threadIdx.x == 0 && (uint64_t)(tile + 1) * kRunTile >= Rn) {
+        *act_total = (uint32_t)s_prefix[0] + atot;
+        *cap_total = (uint64_t)s_prefix[1] + ctot;
+    }
 }
 
 __global__ void k_sum_u32(const uint32_t* __restrict__ in, uint64_t n, unsigned long long* __restrict__ out) {
@@ -469,6 +564,26 @@ uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
     COLO_CUDA(cudaMemcpyAsync(&h, acc.get(), 8, cudaMemcpyDeviceToHost, s));
     stream_wait(s);
     return h;
+}
+
+void run_scans(const uint32_t* rcnt, const uint32_t* run_L, uint32_t* act_off, uint64_t* cap_off, uint64_t Rn,
+               cudaStream_t s, uint32_t* act_total, uint64_t* cap_total) {
+    KScope ks("scan");
+    const uint64_t tiles = Rn ? (Rn + kRunTile - 1) / kRunTile : 0;
+    if (tiles >= (1ull << 31)) throw StatusError{COLO_ERR_CAPACITY, "scan supports < 2^31 tiles"};
+    DevBuf<unsigned long long> st;   // two status words per tile, then the tile counter
+    st.alloc(2 * tiles + 1, s);
+    st.zero(s);
+    if (!tiles) {
+        COLO_CUDA(cudaMemsetAsync(act_total, 0, 4, s));
+        COLO_CUDA(cudaMemsetAsync(cap_total, 0, 8, s));
+        return;
+    }
+    k_run_scans<<<(unsigned)tiles, kScanThreads, 0, s>>>(Rn, rcnt, run_L, act_off, cap_off, st.get(),
+                                                          reinterpret_cast<uint32_t*>(st.get() + 2 * tiles), act_total,
+                                                          cap_total);
+    COLO_LAUNCH_CHECK();
+    count_launch();
 }
 
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,

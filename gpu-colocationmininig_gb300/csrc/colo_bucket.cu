@@ -199,15 +199,27 @@ __global__ void k_run_tail(uint64_t Rn, uint64_t M, uint64_t n, const uint32_t* 
     }
 }
 
-__global__ void k_cell_masks(uint64_t Rn, const uint32_t* __restrict__ rfeat,
-                             const uint32_t* __restrict__ rcell, const uint32_t* __restrict__ cjob,
-                             const JobGrid* __restrict__ grids, uint32_t W,
+// Per cell its feature mask (bit lf of word lf / 32 for each of its runs' local
+// features): a thread walks the cell's runs, which ascend by feature, and writes
+// every word of the row (no clearing pass, no atomics).
+__global__ void k_cell_masks(uint64_t M, const uint32_t* __restrict__ crun, const uint32_t* __restrict__ rfeat,
+                             const uint32_t* __restrict__ cjob, const JobGrid* __restrict__ grids, uint32_t W,
                              uint32_t* __restrict__ cmask) {
-    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= Rn) return;
-    uint32_t c = rcell[r];
-    uint32_t lf = rfeat[r] - grids[cjob[c]].f0;
-    atomicOr(&cmask[(uint64_t)c * W + (lf >> 5)], 1u << (lf & 31));
+    const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M) return;
+    const uint32_t f0 = grids[cjob[c]].f0;
+    uint32_t r = crun[c];
+    const uint32_t r1 = crun[c + 1];
+    uint32_t* row = cmask + c * W;
+    for (uint32_t w = 0; w < W; ++w) {
+        uint32_t bits = 0;
+        for (; r < r1; ++r) {
+            const uint32_t lf = rfeat[r] - f0;
+            if ((lf >> 5) != w) break;
+            bits |= 1u << (lf & 31);
+        }
+        row[w] = bits;
+    }
 }
 
 // rowstart[Y] = first occupied cell whose key is at or after the first key of
@@ -833,11 +845,10 @@ void bucket_points(Batch& b) {
     const uint64_t M = b.M, Rn = b.Rn;
 
     b.cmask.alloc((uint64_t)M * b.W, s);
-    b.cmask.zero(s);
     {
         KScope ks("cell_masks");
-        k_cell_masks<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rfeat.get(), b.rcell.get(), b.cjob.get(),
-                                                        b.grids.get(), b.W, b.cmask.get());
+        k_cell_masks<<<grid_for(M, 256), 256, 0, s>>>(M, b.crun.get(), b.rfeat.get(), b.cjob.get(), b.grids.get(),
+                                                       b.W, b.cmask.get());
         COLO_LAUNCH_CHECK();
         count_launch();
     }

@@ -181,9 +181,10 @@ void join_neighbors(Batch& b) {
         COLO_LAUNCH_CHECK();
         count_launch();
     }
+    // a point without targets keeps a zero count; its list start is never read (every
+    // reader takes nb_cnt first), so only the counts are cleared
     b.nb_beg.alloc(b.N ? b.N : 1, s);
     b.nb_cnt.alloc(b.N ? b.N : 1, s);
-    b.nb_beg.zero(s);
     b.nb_cnt.zero(s);
     b.join_single = U <= kSinglePassCap;
     if (b.join_single) {

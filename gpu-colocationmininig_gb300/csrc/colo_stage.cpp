@@ -100,7 +100,7 @@ colo_status colo_stage_neighbors(colo_ctx* ctx, colo_dataset* ds, float R, uint6
             if (nbr && cap < neighbor_entries(b)) return COLO_ERR_CAPACITY;
             uint64_t o = 0;
             for (uint64_t a = 0; a < b.N; ++a) {
-                if (nbr) std::memcpy(nbr + o, all.data() + beg[a], cnt[a] * 4);
+                if (nbr && cnt[a]) std::memcpy(nbr + o, all.data() + beg[a], cnt[a] * 4);
                 o += cnt[a];
                 if (offs) offs[a + 1] = o;
             }

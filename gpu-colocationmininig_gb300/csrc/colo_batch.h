@@ -78,7 +78,7 @@ struct Batch {
     DevBuf<uint32_t> run_qn;
     DevBuf<uint32_t> run_L;
     // neighbour lists N+(a) = nb[nb_beg[a] .. nb_beg[a] + nb_cnt[a]), each in
-    // (feature, neighbour cell, id) order
+    // (feature, neighbour cell, id) order; nb_beg[a] is set only where nb_cnt[a] > 0
     DevBuf<uint64_t> nb_beg;
     DevBuf<uint32_t> nb_cnt, nb;
     uint64_t E = 0;              // neighbour entries (UINT64_MAX: still on the device in dE)

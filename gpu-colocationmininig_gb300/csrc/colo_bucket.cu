@@ -13,9 +13,10 @@
 namespace colo {
 namespace {
 
-// Cell keys, point ids and packed coordinates, and the digit histograms of
-// every radix pass over the keys (block-private counts added to hist once
-// per block), so the sort does not read the keys again to count them.
+// Cell keys, packed coordinates and (vals non-null) point ids, and the digit
+// histograms of every radix pass over the keys (block-private counts added to
+// hist once per block), so the sort does not read the keys again to count
+// them.  When the sort runs a pass its first pass generates the ids itself.
 
 template <class KT>
 __global__ void __launch_bounds__(256) k_cell_keys(
@@ -48,7 +49,7 @@ __global__ void __launch_bounds__(256) k_cell_keys(
         }
         const KT key = (KT)(g.key_base + c);
         keys[i] = key;
-        vals[i] = (uint32_t)i;
+        if (vals) vals[i] = (uint32_t)i;
         for (int p = 0; p < plan.n; ++p)
             atomicAdd(&h[p * kRadixDigits + ((uint32_t)(key >> plan.shift[p]) & ((1u << plan.width[p]) - 1u))], 1u);
     }
@@ -777,14 +778,16 @@ void sort_and_compact(Batch& b) {
     KScope ks("cell_keys");
     b.xy.alloc(n, s);
     const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)b.sms * 8);
+    // the ids are written here only when the sort runs no pass (its first pass makes them)
+    const bool sorted_ids = n > 1 && bits > 0;
     k_cell_keys<KT><<<(unsigned)(blocks ? blocks : 1), 256, 0, s>>>(n, b.x, b.y, b.F, b.fstart.get(), b.fjob.get(), b.grids.get(),
-                                                                    keys.get(), b.sid.get(), b.xy.get(), b.flags.get(),
-                                                                    plan, hist.get());
+                                                                    keys.get(), sorted_ids ? nullptr : b.sid.get(),
+                                                                    b.xy.get(), b.flags.get(), plan, hist.get());
     COLO_LAUNCH_CHECK();
     count_launch();
     }
     // a look-back timeout lands in the batch's flags, read with the compaction totals
-    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get(), &b.flags.get()->timeout, b.test_spin);
+    radix_sort(keys, b.sid, n, bits, s, "radix_sort", hist.get(), &b.flags.get()->timeout, b.test_spin, true);
 
     b.sxy.alloc(n, s);
     b.sfeat.alloc(n, s);

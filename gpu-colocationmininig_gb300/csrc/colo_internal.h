@@ -325,10 +325,13 @@ void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host, uint64_t* total_dev = nullptr);
 // The join's run scans in one pass: act_r = rcnt[r] if run_L[r] > 0 else 0 and
-// cap_r = act_r * run_L[r], scanned exclusively into act_off and cap_off; the
-// totals land in device memory (no wait).
-void run_scans(const uint32_t* rcnt, const uint32_t* run_L, uint32_t* act_off, uint64_t* cap_off, uint64_t Rn,
-               cudaStream_t s, uint32_t* act_total, uint64_t* cap_total);
+// cap_r = act_r * run_L[r]; cap_r is scanned exclusively into cap_off, and the
+// active anchors are listed in run order: act_pos (sorted positions
+// rstart[r] .. rstart[r] + act_r - 1) and act_run (r), which need room for the
+// sum of act_r.  The totals land in device memory (no wait).
+void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rstart, uint64_t* cap_off,
+               uint32_t* act_pos, uint32_t* act_run, uint64_t Rn, cudaStream_t s, uint32_t* act_total,
+               uint64_t* cap_total);
 // Digit split of a radix sort: pass p sorts width[p] (<= 8) bits from shift[p].
 constexpr int kRadixDigits = 256;
 constexpr int kRadixMaxPasses = 8;
@@ -350,11 +353,14 @@ RadixPlan radix_plan(int bits);
 // after test_spin polls, and in the first pass tile 0 withholds its counts,
 // so tile 1's wait runs out; every wait stays bounded and the sort ends with
 // the timeout flag set (its output is discarded by the caller).
+// iota_vals: the values are the positions 0 .. n-1, which the first pass
+// generates instead of reading (vals must still hold n items).  With no pass
+// (n <= 1 or bits <= 0) vals is left as given, so the caller writes them then.
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
                 const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr,
-                uint32_t test_spin = 0);
+                uint32_t test_spin = 0, bool iota_vals = false);
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
                 const char* name = "radix_sort", unsigned long long* hist = nullptr, uint32_t* err_dev = nullptr,
-                uint32_t test_spin = 0);
+                uint32_t test_spin = 0, bool iota_vals = false);
 
 }  // namespace colo

@@ -25,24 +25,10 @@ namespace {
 
 enum { J_SINGLE = 0, J_COUNT = 1, J_FILL = 2 };
 
-// thread per run: list the run's anchors (sorted positions) when it has targets
-__global__ void k_expand_active(uint64_t Rn, const uint32_t* __restrict__ rstart, const uint32_t* __restrict__ rcnt,
-                                const uint32_t* __restrict__ run_L, const uint32_t* __restrict__ act_off,
-                                uint32_t* __restrict__ act_pos, uint32_t* __restrict__ act_run) {
-    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= Rn || run_L[r] == 0) return;
-    uint32_t o = act_off[r], st = rstart[r], n = rcnt[r];
-    for (uint32_t i = 0; i < n; ++i) {
-        act_pos[o + i] = st + i;
-        act_run[o + i] = (uint32_t)r;
-    }
-}
-
-// Six blocks per SM (40 registers): the join is latency-bound, and the sixth block
-// measured 0.398 -> 0.377 ms per step on the 20M workload.
+// One anchor's neighbour list, by its group of T lanes; returns the list length.
 template <int T, int MODE>
-__global__ void __launch_bounds__(256, 6) k_join(
-    uint64_t A, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
+__device__ __forceinline__ uint32_t join_anchor(
+    uint64_t i, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
     const uint32_t* __restrict__ sid, const uint32_t* __restrict__ sfeat, const float2* __restrict__ sxy,
     const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn,
     const uint32_t* __restrict__ run_L, const uint64_t* __restrict__ cap_off, const uint2* __restrict__ nrl_ent,
@@ -52,8 +38,6 @@ __global__ void __launch_bounds__(256, 6) k_join(
     const int gl = lane % T;
     const int gbase = lane - gl;
     const uint32_t gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << gbase);
-    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / T;
-    if (i >= A) return;                 // whole groups leave together
     const uint32_t p = act_pos[i];
     const uint32_t r = act_run[i];
     const uint32_t a = sid[p];
@@ -96,6 +80,42 @@ __global__ void __launch_bounds__(256, 6) k_join(
         nb_cnt[a] = k;
         if (MODE == J_SINGLE) nb_beg[a] = base;
     }
+    return k;
+}
+
+
+// Six blocks per SM (40 registers): the join is latency-bound, and the sixth block
+// measured 0.398 -> 0.377 ms per step on the 20M workload.
+template <int T, int MODE>
+__global__ void __launch_bounds__(256, 6) k_join(
+    uint64_t A, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
+    const uint32_t* __restrict__ sid, const uint32_t* __restrict__ sfeat, const float2* __restrict__ sxy,
+    const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn,
+    const uint32_t* __restrict__ run_L, const uint64_t* __restrict__ cap_off, const uint2* __restrict__ nrl_ent,
+    const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids, uint64_t* __restrict__ nb_beg,
+    uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb, unsigned long long* __restrict__ total) {
+    const int lane = threadIdx.x & 31;
+    const int gl = lane % T;
+    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / T;
+    // groups past the last anchor (whole groups) count nothing but stay for the block sum
+    const uint32_t k = i < A ? join_anchor<T, MODE>(i, act_pos, act_run, sid, sfeat, sxy, rstart, run_sfx, run_qn,
+                                                     run_L, cap_off, nrl_ent, fjob, grids, nb_beg, nb_cnt, nb)
+                             : 0u;
+    if (MODE == J_SINGLE) {
+        // the entries of the block's anchors (each group's count once), one atomic per block:
+        // the list total without another pass over the counts
+        unsigned long long v = gl == 0 ? k : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        __shared__ unsigned long long s_sum[8];
+        if (lane == 0) s_sum[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < 8; ++w) t += s_sum[w];
+            if (t) atomicAdd(total, t);
+        }
+    }
 }
 
 template <int T>
@@ -109,7 +129,7 @@ void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uin
     k_join<T, MD><<<grid, 256, 0, b.s>>>(A, act_pos, act_run, b.sid.get(), b.sfeat.get(), b.sxy.get(),       \
                                          b.rstart.get(), b.run_sfx.get(), b.run_qn.get(), b.run_L.get(),        \
                                          cap_off, b.nrl_ent.get(), b.J > 1 ? b.fjob.get() : nullptr,           \
-                                         b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get())
+                                         b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get(), b.dE.get())
     if (mode == J_SINGLE) COLO_JOIN(J_SINGLE);
     else if (mode == J_COUNT) COLO_JOIN(J_COUNT);
     else COLO_JOIN(J_FILL);
@@ -139,11 +159,6 @@ __global__ void k_sqdist(const float* __restrict__ x1, const float* __restrict__
     if (within) within[i] = ref_within(x1[i], y1[i], x2[i], y2[i], R2, hu) ? 1 : 0;
 }
 
-inline unsigned grid_for(uint64_t n, int threads) {
-    uint64_t g = (n + threads - 1) / threads;
-    return (unsigned)(g == 0 ? 1 : g);
-}
-
 }  // namespace
 
 // Upper bound of the single-pass layout above which the compact two-pass
@@ -153,16 +168,19 @@ static const uint64_t kSinglePassCap = 1ull << 30;
 void join_neighbors(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t Rn = b.Rn;
-    DevBuf<uint32_t> act_off;
     DevBuf<uint64_t> cap_off;
-    act_off.alloc(Rn, s);
     cap_off.alloc(Rn, s);
+    // the active anchors (the points of runs with targets, by run) are listed by the
+    // scan itself, into arrays sized for every point
+    DevBuf<uint32_t> act_pos, act_run;
+    act_pos.alloc(b.N ? b.N : 1, s);
+    act_run.alloc(b.N ? b.N : 1, s);
     // per run: active anchors (its points, when it has targets) and the single-pass layout's
     // capacity (points x targets), both scanned in one pass; the totals A and U (= pair
     // evaluations) come back together with one wait
     DevBuf<uint64_t> totals;
     totals.alloc(2, s);
-    run_scans(b.rcnt.get(), b.run_L.get(), act_off.get(), cap_off.get(), Rn, s,
+    run_scans(b.rcnt.get(), b.run_L.get(), b.rstart.get(), cap_off.get(), act_pos.get(), act_run.get(), Rn, s,
               reinterpret_cast<uint32_t*>(totals.get()), totals.get() + 1);
     uint64_t ht[2] = {0, 0};
     COLO_CUDA(cudaMemcpyAsync(ht, totals.get(), 16, cudaMemcpyDeviceToHost, s));
@@ -171,26 +189,20 @@ void join_neighbors(Batch& b) {
     const uint64_t U = ht[1];
     b.active_anchors = A;
     b.join_pairs = U;
-    DevBuf<uint32_t> act_pos, act_run;
-    act_pos.alloc(A, s);
-    act_run.alloc(A, s);
-    if (A) {
-        KScope ks("join_setup");
-        k_expand_active<<<grid_for(Rn, 256), 256, 0, s>>>(Rn, b.rstart.get(), b.rcnt.get(), b.run_L.get(),
-                                                          act_off.get(), act_pos.get(), act_run.get());
-        COLO_LAUNCH_CHECK();
-        count_launch();
-    }
     // a point without targets keeps a zero count; its list start is never read (every
     // reader takes nb_cnt first), so only the counts are cleared
     b.nb_beg.alloc(b.N ? b.N : 1, s);
     b.nb_cnt.alloc(b.N ? b.N : 1, s);
     b.nb_cnt.zero(s);
+    b.dE.alloc(1, s);
     b.join_single = U <= kSinglePassCap;
     if (b.join_single) {
+        // total entries: summed by the join's blocks and read at the mine's next wait
         b.nb_cap = U;
         b.nb.alloc(U ? U : 1, s);
+        b.dE.zero(s);
         dispatch_join(b, J_SINGLE, A, act_pos.get(), act_run.get(), cap_off.get());
+        b.E = UINT64_MAX;
     } else {
         dispatch_join(b, J_COUNT, A, act_pos.get(), act_run.get(), nullptr);
         uint64_t E = 0;
@@ -198,15 +210,7 @@ void join_neighbors(Batch& b) {
         b.nb_cap = E;
         b.nb.alloc(E ? E : 1, s);
         dispatch_join(b, J_FILL, A, act_pos.get(), act_run.get(), nullptr);
-    }
-    // total entries: known for the two-pass layout; for the single-pass one
-    // summed on the device and read at the mine's next wait (b.dE)
-    b.dE.alloc(1, s);
-    if (b.join_single) {
-        sum_u32_dev(b.nb_cnt.get(), b.N, s, b.dE.get());
-        b.E = UINT64_MAX;
-    } else {
-        b.E = b.nb_cap;
+        b.E = E;
     }
 }
 

@@ -532,9 +532,51 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
     COLO_CUDA(cudaMemcpyAsync(b.grids.get(), hg.data(), J * sizeof(JobGrid), cudaMemcpyHostToDevice, s));
 }
 
+// The stream-ordered pool keeps what it has mapped (its release threshold is
+// "everything"), but a mine whose blocks come and go in a different order than
+// the last one's may find no free block large enough and map more memory in
+// the middle of a step (about a millisecond per growth on the 20M-point
+// workload).  So before a mine the pool gets one free block of twice the most
+// that one earlier mine had in use, if the device has that much to spare
+// (growing the pool by 10 GB took 4.4 ms on a GB300); later mines then carve
+// their blocks out of it.  This happens only for a peak no earlier mine
+// reached, and the pool's high-water mark is read before and reset after the
+// block, so the block itself never counts as a mine's use.
+static void pool_headroom(colo_ctx* ctx) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    uint64_t high = 0, reserved = 0, zero = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    ctx->pool_peak = std::max(ctx->pool_peak, high);
+    size_t free_b = 0, total_b = 0;
+    // only for a new peak (one attempt each, whatever its outcome)
+    const bool grow = ctx->pool_peak > ctx->pool_sized && reserved < 2 * ctx->pool_peak;
+    ctx->pool_sized = ctx->pool_peak;
+    if (grow && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+        const uint64_t want = 2 * ctx->pool_peak;   // one free block that any mine's blocks fit in
+        void* p = nullptr;
+        if (want <= free_b / 2 && cudaMallocAsync(&p, want, ctx->s) == cudaSuccess) {   // most stays free
+            cudaFreeAsync(p, ctx->s);
+            cudaStreamSynchronize(ctx->s);   // the block is back in the pool before the mark is reset
+        }
+    }
+    cudaGetLastError();
+    // from here the mark counts this mine's use only (a reset sets it to the memory in use)
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero);
+    cudaGetLastError();
+}
+
 static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J,
                       MineResult** outs) {
     cudaStream_t s = ctx->s;
+    pool_headroom(ctx);
     const auto t_all = Clock::now();
     g_launches = 0;
     KTimer kt;

@@ -150,15 +150,21 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan_1p(const Tin* __restri
 // The join's two run scans in one pass: per run r the active anchors
 // act_r = rcnt[r] when the run has targets (run_L[r] > 0) and the single-pass
 // layout's capacity cap_r = rcnt[r] * run_L[r] (both 0 otherwise), scanned
-// exclusively into act_off (32-bit) and cap_off (64-bit), with the totals;
-// warps 0 and 1 look back for the two scans at once.  Tiles of 2048 runs (two
-// values per run in registers).
+// exclusively (cap_off, 64-bit), with the totals; warps 0 and 1 look back for
+// the two scans at once.  Tiles of 2048 runs (two values per run in
+// registers).  The anchors are listed in the same pass: the active anchors of
+// a warp's 32 runs fill one contiguous range of act_pos / act_run (their
+// sorted positions and runs), which the warp writes 32 entries at a time, each
+// lane finding its entry's run by a binary search over the warp's inclusive
+// counts.
 constexpr int kRunItems = 8;
 constexpr int kRunTile = kScanThreads * kRunItems;
 
 __global__ void __launch_bounds__(kScanThreads, 4) k_run_scans(uint64_t Rn, const uint32_t* __restrict__ rcnt,
                                                             const uint32_t* __restrict__ run_L,
-                                                            uint32_t* __restrict__ act_off, uint64_t* __restrict__ cap_off,
+                                                            const uint32_t* __restrict__ rstart,
+                                                            uint64_t* __restrict__ cap_off, uint32_t* __restrict__ act_pos,
+                                                            uint32_t* __restrict__ act_run,
                                                             unsigned long long* __restrict__ status,
                                                             uint32_t* __restrict__ ticket, uint32_t* __restrict__ act_total,
                                                             uint64_t* __restrict__ cap_total) {
@@ -215,11 +221,27 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_run_scans(uint64_t Rn, cons
         const uint32_t ainc = warp_incl_scan(a[i]);
         const uint64_t cinc = warp_incl_scan(cv);
         const uint64_t p = seg + (uint64_t)i * 32 + lane;
-        if (p < Rn) {
-            act_off[p] = acarry + ainc - a[i];
-            cap_off[p] = ccarry + cinc - cv;
+        if (p < Rn) cap_off[p] = ccarry + cinc - cv;
+        const uint32_t wa = __shfl_sync(0xffffffffu, ainc, 31);   // the warp's anchors this round
+        if (wa) {
+            const uint32_t st = a[i] ? rstart[p] : 0u;
+            const uint32_t aex = ainc - a[i];
+            for (uint32_t t0 = 0; t0 < wa; t0 += 32) {
+                const uint32_t t = t0 + lane;
+                // j = the number of runs whose inclusive count is <= t: the run of entry t
+                uint32_t j = 0;
+#pragma unroll
+                for (uint32_t step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, ainc, j + step - 1) <= t) j += step;
+                const uint32_t jst = __shfl_sync(0xffffffffu, st, j);
+                const uint32_t jex = __shfl_sync(0xffffffffu, aex, j);
+                if (t < wa) {
+                    act_pos[acarry + t] = jst + (t - jex);
+                    act_run[acarry + t] = (uint32_t)(seg + (uint64_t)i * 32 + j);
+                }
+            }
         }
-        acarry += __shfl_sync(0xffffffffu, ainc, 31);
+        acarry += wa;
         ccarry += __shfl_sync(0xffffffffu, cinc, 31);
     }
     if (threadIdx.x == 0 && (uint64_t)(tile + 1) * kRunTile >= Rn) {
@@ -275,16 +297,34 @@ constexpr int kMaxRadixBits = 8;                        // digits of at most 8 b
 static_assert((1 << kMaxRadixBits) == kRadixDigits, "digit count");
 constexpr int kMaxRadix = kRadixDigits;
 constexpr int kMaxPasses = kRadixMaxPasses;
-constexpr int kSortThreads = 256;
-constexpr int kSortWarps = kSortThreads / 32;
-// Tile shape: 8 items per lane (2048-key tiles) and eight resident blocks per
-// SM (32 registers for 32-bit keys, a few spilled; 8 x 27.8 KB of shared
-// memory).  The pass is latency-bound, so more tiles in flight help: six
-// blocks at 40 registers ran 0.796 ms per sort on the 20M workload, eight
-// 0.774 ms; 4096-key tiles at three blocks per SM measured 4% slower.
+// Tile shape: 512 threads of 8 items (4096-key tiles) and four resident blocks
+// per SM (32 registers for 32-bit keys, a few spilled; 4 x 51 KB of shared
+// memory).  A pass is bound by its look-back: each tile walks back over its
+// predecessors' published counts (about 30 tiles on the 20M workload) one
+// dependent load at a time, so fewer, larger tiles at the same occupancy finish
+// sooner: 0.704 ms per sort against 0.763 ms for 2048-key tiles of 256 threads
+// (eight blocks per SM) and 0.753 ms for 8192-key tiles of 1024 threads (two);
+// 4096-key tiles of 256 threads x 16 items (three blocks per SM, 80 registers)
+// were slower than either.
 template <class KT>
 struct SortShape {
-    static constexpr int rounds = 8, min_blocks = 8;
+    static constexpr int threads = 512, rounds = 8, min_blocks = 4;
+};
+
+// Shared memory of one sort block (dynamic): the tile's keys and ids (bulk-copy
+// targets, 16-byte aligned), each digit's global base, the per-warp digit
+// counts and each digit's tile-local start.
+template <class KT, int RB>
+struct SortSmem {
+    static constexpr int T = SortShape<KT>::threads, W = T / 32, R = 1 << RB;
+    static constexpr int tile = T * SortShape<KT>::rounds;
+    static constexpr size_t key_at = 0;
+    static constexpr size_t val_at = key_at + (size_t)tile * sizeof(KT);
+    static constexpr size_t base_at = val_at + (size_t)tile * sizeof(uint32_t);
+    static constexpr size_t wh_at = base_at + (size_t)R * sizeof(unsigned long long);
+    static constexpr size_t off_at = wh_at + (size_t)W * R * sizeof(uint32_t);
+    static constexpr size_t bytes = off_at + (size_t)R * sizeof(uint32_t);
+    static_assert(val_at % 16 == 0 && base_at % 8 == 0, "alignment");
 };
 
 
@@ -381,22 +421,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
 // A full tile's keys and ids come into shared memory by one bulk copy each
 // (bulk != 0: the host checked that both arrays are 16-byte aligned); the
 // ranking reads them from there, and the same buffers then stage the tile
-// in digit order.
-template <class KT, int RB, int kSortRounds = SortShape<KT>::rounds>
+// in digit order.  vin == nullptr: the ids are the input positions (the first
+// pass over keys in id order), generated rather than read.
+template <class KT, int RB, int kSortThreads = SortShape<KT>::threads, int kSortRounds = SortShape<KT>::rounds>
 __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_onesweep(
     const KT* __restrict__ kin, const uint32_t* __restrict__ vin, KT* __restrict__ kout, uint32_t* __restrict__ vout,
     uint64_t n, int shift, uint32_t dmask, const unsigned long long* __restrict__ gofs,
     unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err, int bulk,
     uint32_t spin_limit, int withhold, int pass) {
     constexpr int R = 1 << RB;
+    constexpr int kSortWarps = kSortThreads / 32;
     constexpr int kSortTile = kSortThreads * kSortRounds;
-    constexpr int D = R / kSortThreads;             // digits per thread in the look-back (1 or 2)
-    static_assert(D >= 1 && D * kSortThreads == R, "digit count");
-    __shared__ uint32_t wh[kSortWarps][R];
-    __shared__ unsigned long long s_base[R];   // global position of the tile's first key of digit d
-    __shared__ uint32_t s_off[R];              // tile-local position of the first key of digit d
-    __shared__ alignas(16) KT s_key[kSortTile];
-    __shared__ alignas(16) uint32_t s_val[kSortTile];
+    // digits per thread in the look-back (1 or 2); with more threads than digits the
+    // first R threads take one each
+    constexpr int D = R >= kSortThreads ? R / kSortThreads : 1;
+    static_assert(R < kSortThreads || D * kSortThreads == R, "digit count");
+    using SM = SortSmem<KT, RB>;
+    static_assert(SM::T == kSortThreads && SM::tile == kSortTile, "shape");
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    KT* s_key = reinterpret_cast<KT*>(s_dyn + SM::key_at);
+    uint32_t* s_val = reinterpret_cast<uint32_t*>(s_dyn + SM::val_at);
+    unsigned long long* s_base = reinterpret_cast<unsigned long long*>(s_dyn + SM::base_at);  // digit's global base
+    uint32_t (*wh)[R] = reinterpret_cast<uint32_t (*)[R]>(s_dyn + SM::wh_at);                 // per-warp digit counts
+    uint32_t* s_off = reinterpret_cast<uint32_t*>(s_dyn + SM::off_at);                       // digit's tile-local start
+    const bool owner = (int)threadIdx.x * D < R;   // this thread owns digits in the look-back
     __shared__ alignas(8) uint64_t s_bar;
     __shared__ uint32_t s_tile, s_skip;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -419,9 +467,9 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
     const bool staged = bulk && n - tile0 >= (uint64_t)kSortTile;   // full tiles only (uniform in the block)
     if (staged) {
         if (threadIdx.x == 0) {
-            mbar_expect_tx(&s_bar, kSortTile * (uint32_t)(sizeof(KT) + sizeof(uint32_t)));
+            mbar_expect_tx(&s_bar, kSortTile * (uint32_t)(sizeof(KT) + (vin ? sizeof(uint32_t) : 0)));
             bulk_g2s(s_key, kin + tile0, kSortTile * (uint32_t)sizeof(KT), &s_bar);
-            bulk_g2s(s_val, vin + tile0, kSortTile * (uint32_t)sizeof(uint32_t), &s_bar);
+            if (vin) bulk_g2s(s_val, vin + tile0, kSortTile * (uint32_t)sizeof(uint32_t), &s_bar);
         }
         const bool done = mbar_wait(&s_bar, 0, kSpinLimit);
         if (!__syncthreads_and(done ? 1 : 0)) {
@@ -443,7 +491,7 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
         const bool ok = i < n;
         const uint32_t li = (uint32_t)(i - tile0);
         key[r] = ok ? (staged ? s_key[li] : kin[i]) : 0;
-        val[r] = ok ? (staged ? s_val[li] : vin[i]) : 0;
+        val[r] = !ok ? 0u : !vin ? (uint32_t)i : staged ? s_val[li] : vin[i];
         const uint32_t d = ok ? ((uint32_t)(key[r] >> shift) & dmask) : 0xFFFFu;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const int leader = __ffs(peers) - 1;
@@ -464,11 +512,12 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
         for (int i = 0; i < D; ++i) {
             const int d = threadIdx.x * D + i;
             uint32_t c = 0;
-            for (int ww = 0; ww < kSortWarps; ++ww) {
-                const uint32_t t = wh[ww][d];
-                wh[ww][d] = c;
-                c += t;
-            }
+            if (owner)
+                for (int ww = 0; ww < kSortWarps; ++ww) {
+                    const uint32_t t = wh[ww][d];
+                    wh[ww][d] = c;
+                    c += t;
+                }
             cnt[i] = c;
             sum += c;
         }
@@ -480,6 +529,7 @@ __global__ void __launch_bounds__(kSortThreads, SortShape<KT>::min_blocks) k_one
 #pragma unroll
         for (int i = 0; i < D; ++i) {
             const int d = threadIdx.x * D + i;
+            if (!owner) break;
             s_off[d] = ex;
             ex += cnt[i];
             if ((uint32_t)d >= nd) continue;
@@ -566,8 +616,9 @@ uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
     return h;
 }
 
-void run_scans(const uint32_t* rcnt, const uint32_t* run_L, uint32_t* act_off, uint64_t* cap_off, uint64_t Rn,
-               cudaStream_t s, uint32_t* act_total, uint64_t* cap_total) {
+void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rstart, uint64_t* cap_off,
+               uint32_t* act_pos, uint32_t* act_run, uint64_t Rn, cudaStream_t s, uint32_t* act_total,
+               uint64_t* cap_total) {
     KScope ks("scan");
     const uint64_t tiles = Rn ? (Rn + kRunTile - 1) / kRunTile : 0;
     if (tiles >= (1ull << 31)) throw StatusError{COLO_ERR_CAPACITY, "scan supports < 2^31 tiles"};
@@ -579,7 +630,7 @@ void run_scans(const uint32_t* rcnt, const uint32_t* run_L, uint32_t* act_off, u
         COLO_CUDA(cudaMemsetAsync(cap_total, 0, 8, s));
         return;
     }
-    k_run_scans<<<(unsigned)tiles, kScanThreads, 0, s>>>(Rn, rcnt, run_L, act_off, cap_off, st.get(),
+    k_run_scans<<<(unsigned)tiles, kScanThreads, 0, s>>>(Rn, rcnt, run_L, rstart, cap_off, act_pos, act_run, st.get(),
                                                           reinterpret_cast<uint32_t*>(st.get() + 2 * tiles), act_total,
                                                           cap_total);
     COLO_LAUNCH_CHECK();
@@ -605,12 +656,13 @@ namespace {
 
 template <class KT>
 void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                     const char* name, unsigned long long* hist_in, uint32_t* err_dev, uint32_t test_spin) {
-    if (n <= 1 || bits <= 0) return;
+                     const char* name, unsigned long long* hist_in, uint32_t* err_dev, uint32_t test_spin,
+                     bool iota_vals) {
+    if (n <= 1 || bits <= 0) return;   // no pass: vals is left as given, iota_vals or not
     if (n >= (1ull << 32)) throw StatusError{COLO_ERR_CAPACITY, "radix sort supports < 2^32 items"};
     const RadixPlan plan = radix_plan(bits);
-    constexpr int kSortTile = kSortThreads * SortShape<KT>::rounds;
-    const uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+    using SM = SortSmem<KT, kMaxRadixBits>;
+    const uint32_t ntiles = (uint32_t)((n + SM::tile - 1) / SM::tile);
     DevBuf<KT> k2;
     DevBuf<uint32_t> v2, tickets, err;
     DevBuf<unsigned long long> ghist, status;
@@ -644,9 +696,11 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
     uint32_t* va = vals.get();
     KT* kb = k2.get();
     uint32_t* vb = v2.get();
-    // six blocks of ~28 KB per SM: ask for the largest shared-memory carveout
+    // several blocks per SM: ask for the largest shared-memory carveout
     COLO_CUDA(cudaFuncSetAttribute((const void*)k_onesweep<KT, kMaxRadixBits>,
                                    cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+    COLO_CUDA(cudaFuncSetAttribute((const void*)k_onesweep<KT, kMaxRadixBits>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::bytes));
     for (int p = 0; p < plan.n; ++p) {
         KScope ks(name);   // one timed launch per digit pass
         const uint32_t dm = (1u << plan.width[p]) - 1u;
@@ -654,7 +708,9 @@ void radix_sort_impl(DevBuf<KT>& keys, DevBuf<uint32_t>& vals, uint64_t n, int b
         // a tile's words stay kMaxRadix apart, which spreads the polled lines over L2)
         COLO_CUDA(cudaMemset2DAsync(status.get(), kMaxRadix * 8, 0, ((size_t)1 << plan.width[p]) * 8, ntiles, s));
         const int bulk = ((uintptr_t)ka % 16 == 0 && (uintptr_t)va % 16 == 0) ? 1 : 0;
-        k_onesweep<KT, kMaxRadixBits><<<ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, plan.shift[p], dm,
+        // the first pass of a sort of positions generates them (no read)
+        const uint32_t* vin = (iota_vals && p == 0) ? nullptr : va;
+        k_onesweep<KT, kMaxRadixBits><<<ntiles, SM::T, SM::bytes, s>>>(ka, vin, kb, vb, n, plan.shift[p], dm,
                                                                      hist + p * kMaxRadix, status.get(),
                                                                      tickets.get() + p, errp, bulk,
                                                                      test_spin ? test_spin : kSpinLimit,
@@ -693,13 +749,13 @@ RadixPlan radix_plan(int bits) {
 }
 
 void radix_sort(DevBuf<uint64_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name, unsigned long long* hist, uint32_t* err_dev, uint32_t test_spin) {
-    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist, err_dev, test_spin);
+                const char* name, unsigned long long* hist, uint32_t* err_dev, uint32_t test_spin, bool iota_vals) {
+    radix_sort_impl<uint64_t>(keys, vals, n, bits, s, name, hist, err_dev, test_spin, iota_vals);
 }
 
 void radix_sort(DevBuf<uint32_t>& keys, DevBuf<uint32_t>& vals, uint64_t n, int bits, cudaStream_t s,
-                const char* name, unsigned long long* hist, uint32_t* err_dev, uint32_t test_spin) {
-    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist, err_dev, test_spin);
+                const char* name, unsigned long long* hist, uint32_t* err_dev, uint32_t test_spin, bool iota_vals) {
+    radix_sort_impl<uint32_t>(keys, vals, n, bits > 32 ? 32 : bits, s, name, hist, err_dev, test_spin, iota_vals);
 }
 
 }  // namespace colo

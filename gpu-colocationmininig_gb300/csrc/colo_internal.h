@@ -325,12 +325,14 @@ void scan_u32_to_u32(const uint32_t* in, uint32_t* out, uint64_t n, cudaStream_t
 void scan_u64_to_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t s,
                      uint64_t* total_host, uint64_t* total_dev = nullptr);
 // The join's run scans in one pass: act_r = rcnt[r] if run_L[r] > 0 else 0 and
-// cap_r = act_r * run_L[r]; cap_r is scanned exclusively into cap_off, and the
-// active anchors are listed in run order: act_pos (sorted positions
-// rstart[r] .. rstart[r] + act_r - 1) and act_run (r), which need room for the
-// sum of act_r.  The totals land in device memory (no wait).
-void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rstart, uint64_t* cap_off,
-               uint32_t* act_pos, uint32_t* act_run, uint64_t Rn, cudaStream_t s, uint32_t* act_total,
+// cap_r = act_r * run_L[r].  The active anchors are listed in run order:
+// act_pos (sorted positions rstart[r] .. rstart[r] + act_r - 1), act_run (r)
+// and act_base (the exclusive scan of cap over the runs before r, plus the
+// anchor's index in its run times run_L[r]: its list start in the single-pass
+// layout); they need room for the sum of act_r.  The totals (sum of act_r,
+// sum of cap_r) land in device memory (no wait).
+void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rstart, uint32_t* act_pos,
+               uint32_t* act_run, uint64_t* act_base, uint64_t Rn, cudaStream_t s, uint32_t* act_total,
                uint64_t* cap_total);
 // Digit split of a radix sort: pass p sorts width[p] (<= 8) bits from shift[p].
 constexpr int kRadixDigits = 256;

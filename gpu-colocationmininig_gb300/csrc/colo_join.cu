@@ -30,10 +30,9 @@ template <int T, int MODE>
 __device__ __forceinline__ uint32_t join_anchor(
     uint64_t i, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
     const uint32_t* __restrict__ sid, const uint32_t* __restrict__ sfeat, const float2* __restrict__ sxy,
-    const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn,
-    const uint32_t* __restrict__ run_L, const uint64_t* __restrict__ cap_off, const uint2* __restrict__ nrl_ent,
-    const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids, uint64_t* __restrict__ nb_beg,
-    uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb) {
+    const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn, const uint64_t* __restrict__ act_base,
+    const uint2* __restrict__ nrl_ent, const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids,
+    uint64_t* __restrict__ nb_beg, uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb) {
     const int lane = threadIdx.x & 31;
     const int gl = lane % T;
     const int gbase = lane - gl;
@@ -47,7 +46,7 @@ __device__ __forceinline__ uint32_t join_anchor(
     const float R2 = g.R2, hu = g.R2hu;
     const uint64_t q0 = run_sfx[r], qend = q0 + run_qn[r];
     uint64_t base = 0;
-    if (MODE == J_SINGLE) base = cap_off[r] + (uint64_t)(p - rstart[r]) * run_L[r];
+    if (MODE == J_SINGLE) base = act_base[i];
     if (MODE == J_FILL) base = nb_beg[a];
     uint32_t k = 0;
     for (uint64_t q = q0; q < qend; ++q) {
@@ -90,16 +89,16 @@ template <int T, int MODE>
 __global__ void __launch_bounds__(256, 6) k_join(
     uint64_t A, const uint32_t* __restrict__ act_pos, const uint32_t* __restrict__ act_run,
     const uint32_t* __restrict__ sid, const uint32_t* __restrict__ sfeat, const float2* __restrict__ sxy,
-    const uint32_t* __restrict__ rstart, const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn,
-    const uint32_t* __restrict__ run_L, const uint64_t* __restrict__ cap_off, const uint2* __restrict__ nrl_ent,
-    const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids, uint64_t* __restrict__ nb_beg,
-    uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb, unsigned long long* __restrict__ total) {
+    const uint64_t* __restrict__ run_sfx, const uint32_t* __restrict__ run_qn, const uint64_t* __restrict__ act_base,
+    const uint2* __restrict__ nrl_ent, const uint32_t* __restrict__ fjob, const JobGrid* __restrict__ grids,
+    uint64_t* __restrict__ nb_beg, uint32_t* __restrict__ nb_cnt, uint32_t* __restrict__ nb,
+    unsigned long long* __restrict__ total) {
     const int lane = threadIdx.x & 31;
     const int gl = lane % T;
     const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / T;
     // groups past the last anchor (whole groups) count nothing but stay for the block sum
-    const uint32_t k = i < A ? join_anchor<T, MODE>(i, act_pos, act_run, sid, sfeat, sxy, rstart, run_sfx, run_qn,
-                                                     run_L, cap_off, nrl_ent, fjob, grids, nb_beg, nb_cnt, nb)
+    const uint32_t k = i < A ? join_anchor<T, MODE>(i, act_pos, act_run, sid, sfeat, sxy, run_sfx, run_qn, act_base,
+                                                     nrl_ent, fjob, grids, nb_beg, nb_cnt, nb)
                              : 0u;
     if (MODE == J_SINGLE) {
         // the entries of the block's anchors (each group's count once), one atomic per block:
@@ -120,15 +119,15 @@ __global__ void __launch_bounds__(256, 6) k_join(
 
 template <int T>
 void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uint32_t* act_run,
-              const uint64_t* cap_off) {
+              const uint64_t* act_base) {
     if (A == 0) return;
     uint64_t threads = A * T;
     unsigned grid = (unsigned)((threads + 255) / 256);
     KScope ks(mode == J_SINGLE ? "join" : mode == J_COUNT ? "join_count" : "join_fill");
 #define COLO_JOIN(MD)                                                                                        \
     k_join<T, MD><<<grid, 256, 0, b.s>>>(A, act_pos, act_run, b.sid.get(), b.sfeat.get(), b.sxy.get(),       \
-                                         b.rstart.get(), b.run_sfx.get(), b.run_qn.get(), b.run_L.get(),        \
-                                         cap_off, b.nrl_ent.get(), b.J > 1 ? b.fjob.get() : nullptr,           \
+                                         b.run_sfx.get(), b.run_qn.get(), act_base, b.nrl_ent.get(),            \
+                                         b.J > 1 ? b.fjob.get() : nullptr,                                      \
                                          b.grids.get(), b.nb_beg.get(), b.nb_cnt.get(), b.nb.get(), b.dE.get())
     if (mode == J_SINGLE) COLO_JOIN(J_SINGLE);
     else if (mode == J_COUNT) COLO_JOIN(J_COUNT);
@@ -139,14 +138,14 @@ void run_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uin
 }
 
 void dispatch_join(Batch& b, int mode, uint64_t A, const uint32_t* act_pos, const uint32_t* act_run,
-                   const uint64_t* cap_off) {
+                   const uint64_t* act_base) {
     switch (b.join_group) {
-        case 1: run_join<1>(b, mode, A, act_pos, act_run, cap_off); break;
-        case 2: run_join<2>(b, mode, A, act_pos, act_run, cap_off); break;
-        case 4: run_join<4>(b, mode, A, act_pos, act_run, cap_off); break;
-        case 16: run_join<16>(b, mode, A, act_pos, act_run, cap_off); break;
-        case 32: run_join<32>(b, mode, A, act_pos, act_run, cap_off); break;
-        default: run_join<8>(b, mode, A, act_pos, act_run, cap_off); break;
+        case 1: run_join<1>(b, mode, A, act_pos, act_run, act_base); break;
+        case 2: run_join<2>(b, mode, A, act_pos, act_run, act_base); break;
+        case 4: run_join<4>(b, mode, A, act_pos, act_run, act_base); break;
+        case 16: run_join<16>(b, mode, A, act_pos, act_run, act_base); break;
+        case 32: run_join<32>(b, mode, A, act_pos, act_run, act_base); break;
+        default: run_join<8>(b, mode, A, act_pos, act_run, act_base); break;
     }
 }
 
@@ -168,19 +167,19 @@ static const uint64_t kSinglePassCap = 1ull << 30;
 void join_neighbors(Batch& b) {
     cudaStream_t s = b.s;
     const uint64_t Rn = b.Rn;
-    DevBuf<uint64_t> cap_off;
-    cap_off.alloc(Rn, s);
     // the active anchors (the points of runs with targets, by run) are listed by the
     // scan itself, into arrays sized for every point
     DevBuf<uint32_t> act_pos, act_run;
+    DevBuf<uint64_t> act_base;
     act_pos.alloc(b.N ? b.N : 1, s);
     act_run.alloc(b.N ? b.N : 1, s);
+    act_base.alloc(b.N ? b.N : 1, s);
     // per run: active anchors (its points, when it has targets) and the single-pass layout's
     // capacity (points x targets), both scanned in one pass; the totals A and U (= pair
     // evaluations) come back together with one wait
     DevBuf<uint64_t> totals;
     totals.alloc(2, s);
-    run_scans(b.rcnt.get(), b.run_L.get(), b.rstart.get(), cap_off.get(), act_pos.get(), act_run.get(), Rn, s,
+    run_scans(b.rcnt.get(), b.run_L.get(), b.rstart.get(), act_pos.get(), act_run.get(), act_base.get(), Rn, s,
               reinterpret_cast<uint32_t*>(totals.get()), totals.get() + 1);
     uint64_t ht[2] = {0, 0};
     COLO_CUDA(cudaMemcpyAsync(ht, totals.get(), 16, cudaMemcpyDeviceToHost, s));
@@ -201,7 +200,7 @@ void join_neighbors(Batch& b) {
         b.nb_cap = U;
         b.nb.alloc(U ? U : 1, s);
         b.dE.zero(s);
-        dispatch_join(b, J_SINGLE, A, act_pos.get(), act_run.get(), cap_off.get());
+        dispatch_join(b, J_SINGLE, A, act_pos.get(), act_run.get(), act_base.get());
         b.E = UINT64_MAX;
     } else {
         dispatch_join(b, J_COUNT, A, act_pos.get(), act_run.get(), nullptr);

@@ -150,21 +150,22 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan_1p(const Tin* __restri
 // The join's two run scans in one pass: per run r the active anchors
 // act_r = rcnt[r] when the run has targets (run_L[r] > 0) and the single-pass
 // layout's capacity cap_r = rcnt[r] * run_L[r] (both 0 otherwise), scanned
-// exclusively (cap_off, 64-bit), with the totals; warps 0 and 1 look back for
-// the two scans at once.  Tiles of 2048 runs (two values per run in
-// registers).  The anchors are listed in the same pass: the active anchors of
-// a warp's 32 runs fill one contiguous range of act_pos / act_run (their
-// sorted positions and runs), which the warp writes 32 entries at a time, each
-// lane finding its entry's run by a binary search over the warp's inclusive
-// counts.
+// exclusively, with the totals; warps 0 and 1 look back for the two scans at
+// once.  Tiles of 2048 runs (two values per run in registers).  The anchors
+// are listed in the same pass: the active anchors of a warp's 32 runs fill one
+// contiguous range of act_pos / act_run / act_base (their sorted positions,
+// runs and single-pass list starts: the run's capacity offset plus the
+// anchor's index in the run times run_L), which the warp writes 32 entries at
+// a time, each lane finding its entry's run by a binary search over the
+// warp's inclusive counts.
 constexpr int kRunItems = 8;
 constexpr int kRunTile = kScanThreads * kRunItems;
 
 __global__ void __launch_bounds__(kScanThreads, 4) k_run_scans(uint64_t Rn, const uint32_t* __restrict__ rcnt,
                                                             const uint32_t* __restrict__ run_L,
                                                             const uint32_t* __restrict__ rstart,
-                                                            uint64_t* __restrict__ cap_off, uint32_t* __restrict__ act_pos,
-                                                            uint32_t* __restrict__ act_run,
+                                                            uint32_t* __restrict__ act_pos, uint32_t* __restrict__ act_run,
+                                                            uint64_t* __restrict__ act_base,
                                                             unsigned long long* __restrict__ status,
                                                             uint32_t* __restrict__ ticket, uint32_t* __restrict__ act_total,
                                                             uint64_t* __restrict__ cap_total) {
@@ -221,11 +222,11 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_run_scans(uint64_t Rn, cons
         const uint32_t ainc = warp_incl_scan(a[i]);
         const uint64_t cinc = warp_incl_scan(cv);
         const uint64_t p = seg + (uint64_t)i * 32 + lane;
-        if (p < Rn) cap_off[p] = ccarry + cinc - cv;
         const uint32_t wa = __shfl_sync(0xffffffffu, ainc, 31);   // the warp's anchors this round
         if (wa) {
             const uint32_t st = a[i] ? rstart[p] : 0u;
             const uint32_t aex = ainc - a[i];
+            const uint64_t cex = ccarry + cinc - cv;
             for (uint32_t t0 = 0; t0 < wa; t0 += 32) {
                 const uint32_t t = t0 + lane;
                 // j = the number of runs whose inclusive count is <= t: the run of entry t
@@ -235,9 +236,12 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_run_scans(uint64_t Rn, cons
                     if (__shfl_sync(0xffffffffu, ainc, j + step - 1) <= t) j += step;
                 const uint32_t jst = __shfl_sync(0xffffffffu, st, j);
                 const uint32_t jex = __shfl_sync(0xffffffffu, aex, j);
+                const uint32_t jL = __shfl_sync(0xffffffffu, L[i], j);
+                const uint64_t jcex = __shfl_sync(0xffffffffu, cex, j);
                 if (t < wa) {
                     act_pos[acarry + t] = jst + (t - jex);
                     act_run[acarry + t] = (uint32_t)(seg + (uint64_t)i * 32 + j);
+                    act_base[acarry + t] = jcex + (uint64_t)(t - jex) * jL;
                 }
             }
         }
@@ -616,8 +620,8 @@ uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s) {
     return h;
 }
 
-void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rstart, uint64_t* cap_off,
-               uint32_t* act_pos, uint32_t* act_run, uint64_t Rn, cudaStream_t s, uint32_t* act_total,
+void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rstart, uint32_t* act_pos,
+               uint32_t* act_run, uint64_t* act_base, uint64_t Rn, cudaStream_t s, uint32_t* act_total,
                uint64_t* cap_total) {
     KScope ks("scan");
     const uint64_t tiles = Rn ? (Rn + kRunTile - 1) / kRunTile : 0;
@@ -630,7 +634,7 @@ void run_scans(const uint32_t* rcnt, const uint32_t* run_L, const uint32_t* rsta
         COLO_CUDA(cudaMemsetAsync(cap_total, 0, 8, s));
         return;
     }
-    k_run_scans<<<(unsigned)tiles, kScanThreads, 0, s>>>(Rn, rcnt, run_L, rstart, cap_off, act_pos, act_run, st.get(),
+    k_run_scans<<<(unsigned)tiles, kScanThreads, 0, s>>>(Rn, rcnt, run_L, rstart, act_pos, act_run, act_base, st.get(),
                                                           reinterpret_cast<uint32_t*>(st.get() + 2 * tiles), act_total,
                                                           cap_total);
     COLO_LAUNCH_CHECK();

@@ -264,8 +264,9 @@ __global__ void __launch_bounds__(128, 16) k_nb9(uint64_t M, const uint64_t* __r
     if (c >= M) return;
     const JobGrid g = grids[cjob[c]];
     const uint64_t key = ckey[c];
-    const uint64_t local = key - g.key_base;
-    const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+    uint64_t ucx, ucy;
+    cell_col_row(key - g.key_base, g.gx, ucx, ucy);
+    const int64_t cx = (int64_t)ucx, cy = (int64_t)ucy;
     const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < (int64_t)g.gx ? cx + 1 : cx;
     int32_t* out = nb9 + c * 9;
     uint32_t occ = 0;   // bit (dy+1)*3 + (dx+1): that neighbour is occupied
@@ -390,8 +391,9 @@ __global__ void __launch_bounds__(kQuadThreads) k_quad_masks(
         if (c < M) {
             const JobGrid g = grids[cjob[c]];
             f0 = g.f0;
-            const uint64_t local = ckey[c] - g.key_base;
-            const int64_t cx = (int64_t)(local % g.gx), cy = (int64_t)(local / g.gx);
+            uint64_t ucx, ucy;
+            cell_col_row(ckey[c] - g.key_base, g.gx, ucx, ucy);
+            const int64_t cx = (int64_t)ucx, cy = (int64_t)ucy;
             int32_t nb[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) nb[q] = nb9[c * 9 + q];
@@ -515,8 +517,9 @@ __device__ __forceinline__ int adjacent_cells(uint64_t c, const uint64_t* ckey, 
                                               const JobGrid* grids, const int32_t* nb9,
                                               int32_t* out) {
     const JobGrid g = grids[cjob[c]];
-    uint64_t local = ckey[c] - g.key_base;
-    uint32_t cx = (uint32_t)(local % g.gx);
+    uint64_t ucx, ucy;
+    cell_col_row(ckey[c] - g.key_base, g.gx, ucx, ucy);
+    const uint32_t cx = (uint32_t)ucx;
     int cnt = 0;
     for (int dy = -1; dy <= 1; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {

@@ -81,6 +81,20 @@ __device__ __forceinline__ uint32_t mask_rank(const uint32_t* __restrict__ m, ui
     return r + __popc(m[wq] & ((1u << (b & 31)) - 1u));
 }
 
+// Column and row of a cell from its id within its grid (id = row * gx + col):
+// a 32-bit division when the id fits, which every grid of fewer than 2^32
+// cells does, else the 64-bit one.
+__device__ __forceinline__ void cell_col_row(uint64_t local, uint32_t gx, uint64_t& cx, uint64_t& cy) {
+    if (local < (1ull << 32)) {
+        const uint32_t l = (uint32_t)local, r = l / gx;
+        cy = r;
+        cx = l - r * gx;
+    } else {
+        cy = local / gx;
+        cx = local - cy * gx;
+    }
+}
+
 // A point's feature is the last feature whose first point is at or before it
 // (points are grouped by feature); the start table stays in L1.
 __device__ __forceinline__ uint32_t feature_of(uint32_t id, uint32_t F, const uint32_t* __restrict__ fstart) {

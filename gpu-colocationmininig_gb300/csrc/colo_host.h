@@ -101,7 +101,6 @@ struct colo_ctx {
     size_t ustage_bytes = 0;
     size_t ustage_off = 0;      // bytes in use since the stream last drained
     uint64_t pool_peak = 0;     // most device-pool memory in use by one earlier mine (bytes)
-    uint64_t pool_sized = 0;    // the peak the pool was last grown for
 };
 
 struct colo_dataset {

@@ -536,47 +536,54 @@ void setup_batch(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv,
 // "everything"), but a mine whose blocks come and go in a different order than
 // the last one's may find no free block large enough and map more memory in
 // the middle of a step (about a millisecond per growth on the 20M-point
-// workload).  So before a mine the pool gets one free block of twice the most
-// that one earlier mine had in use, if the device has that much to spare
-// (growing the pool by 10 GB took 4.4 ms on a GB300); later mines then carve
-// their blocks out of it.  This happens only for a peak no earlier mine
-// reached, and the pool's high-water mark is read before and reset after the
-// block, so the block itself never counts as a mine's use.
-static void pool_headroom(colo_ctx* ctx) {
-    cudaMemPool_t pool;
+// workload).  So after a mine that used more of the pool than any before it,
+// the pool gets one free block of twice that peak, if the device has that
+// much to spare (growing the pool by 10 GB took 4.4 ms on a GB300); later
+// mines carve their blocks out of it.  The growth lands in the mine that set
+// the peak (a warm-up mine, typically), not in the next one.  The pool's
+// high-water mark is reset as a mine starts, so it measures that mine alone.
+static cudaMemPool_t device_pool(colo_ctx* ctx) {
+    cudaMemPool_t pool = nullptr;
     if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) != cudaSuccess) {
         cudaGetLastError();
-        return;
+        return nullptr;
     }
-    uint64_t high = 0, reserved = 0, zero = 0;
+    return pool;
+}
+
+static void pool_reset_mark(colo_ctx* ctx) {
+    cudaMemPool_t pool = device_pool(ctx);
+    uint64_t zero = 0;
+    if (pool && cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero) != cudaSuccess) cudaGetLastError();
+}
+
+static void pool_headroom(colo_ctx* ctx) {
+    cudaMemPool_t pool = device_pool(ctx);
+    if (!pool) return;
+    uint64_t high = 0, reserved = 0;
     if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high) != cudaSuccess ||
         cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
-    ctx->pool_peak = std::max(ctx->pool_peak, high);
+    if (high <= ctx->pool_peak) return;   // no new peak (one attempt per peak, whatever its outcome)
+    ctx->pool_peak = high;
     size_t free_b = 0, total_b = 0;
-    // only for a new peak (one attempt each, whatever its outcome)
-    const bool grow = ctx->pool_peak > ctx->pool_sized && reserved < 2 * ctx->pool_peak;
-    ctx->pool_sized = ctx->pool_peak;
-    if (grow && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-        const uint64_t want = 2 * ctx->pool_peak;   // one free block that any mine's blocks fit in
-        void* p = nullptr;
-        if (want <= free_b / 2 && cudaMallocAsync(&p, want, ctx->s) == cudaSuccess) {   // most stays free
-            cudaFreeAsync(p, ctx->s);
-            cudaStreamSynchronize(ctx->s);   // the block is back in the pool before the mark is reset
-        }
+    if (reserved >= 2 * high || cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return;
     }
-    cudaGetLastError();
-    // from here the mark counts this mine's use only (a reset sets it to the memory in use)
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero);
+    void* p = nullptr;
+    if (2 * high <= free_b / 2 && cudaMallocAsync(&p, 2 * high, ctx->s) == cudaSuccess) {   // most stays free
+        cudaFreeAsync(p, ctx->s);
+        cudaStreamSynchronize(ctx->s);
+    }
     cudaGetLastError();
 }
 
 static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params* pv, uint32_t J,
                       MineResult** outs) {
     cudaStream_t s = ctx->s;
-    pool_headroom(ctx);
     const auto t_all = Clock::now();
     g_launches = 0;
     KTimer kt;
@@ -1632,11 +1639,13 @@ colo_status colo_mine_batch(colo_ctx* ctx, colo_dataset* const* ds, const colo_p
         mr[j] = &res[j]->r;
     }
     colo_status st = guarded(ctx, [&]() {
+        pool_reset_mark(ctx);   // from here the pool's high-water mark is this call's
         if (p[0].mode == COLO_MODE_PLAIN && njobs > 1) {
             for (uint32_t j = 0; j < njobs; ++j) mine_jobs(ctx, &ds[j], &p[j], 1, &mr[j]);
         } else {
             mine_jobs(ctx, ds, p, njobs, mr.data());
         }
+        pool_headroom(ctx);   // the mine's buffers are back in the pool
         return COLO_OK;
     });
     if (st != COLO_OK) return st;

@@ -1,10 +1,11 @@
 """Repeated mines on one context reach a steady device-memory footprint.
 
-Before a mine the library grows the stream-ordered pool once, in one block,
-to twice the most an earlier mine had in use, so that later mines find free
-blocks instead of mapping memory mid-step.  The block must not count as a
-mine's own use, or every mine would grow the pool again: here the device's
-free memory, read between mines, stops changing after the first few.
+After a mine that used more of the stream-ordered pool than any before it,
+the library gives the pool one free block of twice that peak, so that later
+mines find free blocks instead of mapping memory mid-step.  The block must
+not count as a mine's own use, or every mine would grow the pool again: here
+the device's free memory, read between mines, stops changing after the first
+few.
 """
 import pytest
 
@@ -29,5 +30,5 @@ def test_repeated_mines_keep_a_steady_pool():
         assert patterns == first
         torch.cuda.synchronize()
         free.append(torch.cuda.mem_get_info(0)[0])
-    # the first mine sets the peak, the second grows the pool once; from then on nothing moves
+    # the first mine sets the peak and grows the pool once; from then on nothing moves
     assert len(set(free[3:])) == 1, [f >> 20 for f in free]

@@ -16,6 +16,7 @@
 // needed; when the upper bounds would not fit, a count pass + scan + fill
 // pass produces a compact layout instead.
 #include <cmath>
+#include <vector>
 
 #include "colo_batch.h"
 #include "colo_device.cuh"
@@ -24,6 +25,10 @@ namespace colo {
 namespace {
 
 enum { J_SINGLE = 0, J_COUNT = 1, J_FILL = 2 };
+
+// The single pass sums the list total into kEntrySlots counters kEntryStride
+// words apart (one 128-byte line each), added up when the total is read.
+constexpr int kEntrySlots = 64, kEntryStride = 16;
 
 // One anchor's neighbour list, by its group of T lanes; returns the list length.
 template <int T, int MODE>
@@ -101,19 +106,15 @@ __global__ void __launch_bounds__(256, 6) k_join(
                                                      nrl_ent, fjob, grids, nb_beg, nb_cnt, nb)
                              : 0u;
     if (MODE == J_SINGLE) {
-        // the entries of the block's anchors (each group's count once), one atomic per block:
-        // the list total without another pass over the counts
+        // the entries of the warp's anchors (each group's count once), one atomic per warp into
+        // one of kEntrySlots counters on separate lines: the list total without another pass
+        // over the counts, and no block barrier (one made every warp wait for its block's
+        // longest list: the 512-job batch's join ran 10.96 ms against 9.38 ms)
         unsigned long long v = gl == 0 ? k : 0u;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        __shared__ unsigned long long s_sum[8];
-        if (lane == 0) s_sum[threadIdx.x >> 5] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long t = 0;
-            for (int w = 0; w < 8; ++w) t += s_sum[w];
-            if (t) atomicAdd(total, t);
-        }
+        const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        if (lane == 0 && v) atomicAdd(total + (warp % kEntrySlots) * kEntryStride, v);
     }
 }
 
@@ -193,10 +194,10 @@ void join_neighbors(Batch& b) {
     b.nb_beg.alloc(b.N ? b.N : 1, s);
     b.nb_cnt.alloc(b.N ? b.N : 1, s);
     b.nb_cnt.zero(s);
-    b.dE.alloc(1, s);
+    b.dE.alloc(kEntrySlots * kEntryStride, s);
     b.join_single = U <= kSinglePassCap;
     if (b.join_single) {
-        // total entries: summed by the join's blocks and read at the mine's next wait
+        // total entries: summed by the join's warps and read at the mine's next wait
         b.nb_cap = U;
         b.nb.alloc(U ? U : 1, s);
         b.dE.zero(s);
@@ -215,10 +216,12 @@ void join_neighbors(Batch& b) {
 
 uint64_t neighbor_entries(Batch& b) {
     if (b.E == UINT64_MAX) {
-        unsigned long long e = 0;
-        COLO_CUDA(cudaMemcpyAsync(&e, b.dE.get(), 8, cudaMemcpyDeviceToHost, b.s));
+        std::vector<unsigned long long> e(kEntrySlots * kEntryStride);
+        COLO_CUDA(cudaMemcpyAsync(e.data(), b.dE.get(), e.size() * 8, cudaMemcpyDeviceToHost, b.s));
         stream_wait(b.s);
-        b.E = e;
+        uint64_t t = 0;
+        for (int i = 0; i < kEntrySlots; ++i) t += e[(size_t)i * kEntryStride];
+        b.E = t;
     }
     return b.E;
 }

@@ -1158,7 +1158,11 @@ static void mine_jobs(colo_ctx* ctx, colo_dataset* const* dsv, const colo_params
         for (uint64_t q = 0; q < ncand; ++q)
             if (prev_flag[q] && maybe[owner[q].first][owner[q].second] && !(q < ns && !hovf[q]))
                 maybe_words += (gb[q + 1] - gb[q]) * k;
-        const bool early_fill = !plain && !host_tables && next_possible && maybe_words <= kEarlyFillWords;
+        // (one job only: in a batch of many small jobs Apriori's subset test prunes most of
+        // the possible tables -- on the 512-job workload the early fill took 11.3 ms per mine
+        // against 2.7 ms for the needed tables after Apriori)
+        const bool early_fill =
+            !plain && !host_tables && next_possible && maybe_words <= kEarlyFillWords && J == 1;
 
         // needed[j][c]: candidate c of this level is the prefix of a next-level candidate
         std::vector<std::vector<uint8_t>> needed(J);

@@ -312,10 +312,6 @@ struct KScope {
 // In place: exclusive scan of partial[0..m), partial[m] = total (read back
 // when total_host != nullptr).
 void scan_partials_u64(uint64_t* partial, uint64_t m, cudaStream_t s, uint64_t* total_host);
-// Sum of n values (synchronises to read it back).
-uint64_t sum_u32(const uint32_t* in, uint64_t n, cudaStream_t s);
-// Sum of n values into *out (device), without waiting.
-void sum_u32_dev(const uint32_t* in, uint64_t n, cudaStream_t s, unsigned long long* out);
 // out[i] = sum(in[0..i)).  The total is read back (with a wait) when
 // total_host is given, and copied to device memory (no wait) when total_dev is.
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t s,

@@ -35,7 +35,9 @@ constexpr int kMaxW = 32;  // mask words per cell (1024 features per job); rows 
 constexpr uint64_t kAccMax = 16384;   // block-private level sums (64 KB of shared memory)
 
 // One thread per run (C, f); a block owns a contiguous range of runs, so the
-// job changes rarely and the F x F accumulator lives in shared memory.
+// job changes rarely and the F x F accumulator lives in shared memory.  cjob is
+// null for a one-job batch (job 0 everywhere): the mask load then waits on one
+// dependent load (the run's cell) instead of three.
 __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
     uint64_t Rn, const uint32_t* __restrict__ rcell, const uint32_t* __restrict__ cjob,
     const JobGrid* __restrict__ grids, const uint32_t* __restrict__ nbmask,
@@ -47,10 +49,10 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
     const uint64_t r1 = r0 + runs_per_block < Rn ? r0 + runs_per_block : Rn;
     const uint32_t accn = acc_dim * acc_dim;
     for (uint32_t i = threadIdx.x; i < accn; i += blockDim.x) acc[i] = 0;
-    if (threadIdx.x == 0) cur_job = r0 < Rn ? (int32_t)cjob[rcell[r0]] : -1;
+    if (threadIdx.x == 0) cur_job = r0 < Rn ? (cjob ? (int32_t)cjob[rcell[r0]] : 0) : -1;
     __syncthreads();
     for (uint64_t base = r0; base < r1; base += blockDim.x) {
-        int32_t jb = (int32_t)cjob[rcell[base]];
+        const int32_t jb = cjob ? (int32_t)cjob[rcell[base]] : 0;
         if (jb != cur_job) {   // flush the accumulator on a job change (uniform branch)
             __syncthreads();
             uint32_t nf = grids[cur_job].nf;
@@ -66,7 +68,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter_pairs(
         const uint64_t r = base + threadIdx.x;
         if (r < r1) {
             const uint32_t c = rcell[r];
-            const uint32_t job = cjob[c];
+            const uint32_t job = cjob ? cjob[c] : 0u;
             const JobGrid g = grids[job];
             if (g.gx >= 2 && g.gy >= 2) {
                 const bool priv = acc_dim && (int32_t)job == cur_job && g.nf <= acc_dim;
@@ -290,11 +292,19 @@ __global__ void __launch_bounds__(256, (WT <= 4 ? 5 : (WT <= 6 ? 4 : (WT <= 8 ? 
         const uint64_t Z = valid ? __ldg(dlist + l0 + zi) : 0u;
         const uint32_t* q4 = qmask + Z * 4 * W;
         uint32_t qr[kCacheQuads ? 4 : 1][kCacheQuads ? WT : 1];
-        if constexpr (kCacheQuads) {
-            if (valid) {
+        // the cell's own mask and first run, issued with its quads (most list cells are
+        // in U_c of some candidate, and these loads would otherwise wait for the first)
+        uint32_t cm[WT];
+        uint32_t q0 = 0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) cm[w] = 0;
+        if (valid) {
+            if constexpr (kCacheQuads) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) load_row<WT>(q4 + q * W, qr[q]);
             }
+            load_row<WT>(cmask + Z * W, cm);
+            q0 = crun[Z];
         }
         const uint32_t t1 = gc * cu + cu < G ? gc * cu + cu : G;
         for (uint32_t t = gc * cu; t < t1; ++t) {
@@ -316,9 +326,6 @@ __global__ void __launch_bounds__(256, (WT <= 4 ? 5 : (WT <= 6 ? 4 : (WT <= 8 ? 
                 if (ok) full |= 1u << q;
             }
             if (!full) continue;
-            uint32_t cm[WT];
-            load_row<WT>(cmask + Z * W, cm);
-            const uint32_t q0 = crun[Z];
             uint32_t lm[4];
             load_row<4>(lmem + (uint64_t)c * 4, lm);
 #pragma unroll
@@ -457,7 +464,7 @@ void filter_pairs(Batch& b, DevBuf<uint32_t>& ub2, std::vector<uint64_t>& job_of
     blocks = (b.Rn + per - 1) / per;
     KScope ks("filter_pairs");
     k_filter_pairs<<<(unsigned)blocks, kFilterThreads, smem, s>>>(
-        b.Rn, b.rcell.get(), b.cjob.get(), b.grids.get(), b.nbmask.get(), b.W, b.rfeat.get(),
+        b.Rn, b.rcell.get(), b.J > 1 ? b.cjob.get() : nullptr, b.grids.get(), b.nbmask.get(), b.W, b.rfeat.get(),
         b.rcnt.get(), d_job_off.get(), ub2.get(), acc_dim, per);
     COLO_LAUNCH_CHECK();
     count_launch();

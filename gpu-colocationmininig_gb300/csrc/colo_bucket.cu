@@ -280,14 +280,19 @@ __global__ void __launch_bounds__(128, 16) k_nb9(uint64_t M, const uint64_t* __r
         } else if (ny >= 0 && ny < (int64_t)g.gy) {
             const uint64_t k0 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x0;
             const uint64_t k1 = g.key_base + (uint64_t)ny * g.gx + (uint64_t)x1;
-            uint64_t lo = dy < 0 ? 0 : c + 1, hi = dy < 0 ? c : M;
+            // 32-bit positions (M < 2^32): the search is most of this kernel's instructions
+            uint32_t lo = dy < 0 ? 0u : (uint32_t)c + 1u, hi = dy < 0 ? (uint32_t)c : (uint32_t)M;
             if (rowstart) {
                 const uint64_t Y = g.row_base + (uint64_t)ny;
                 lo = rowstart[Y];
                 hi = rowstart[Y + 1];
             }
-            uint64_t pos = lower_bound_dev(ckey, lo, hi, k0);
-            for (; pos < M && ckey[pos] <= k1; ++pos) {
+            while (lo < hi) {
+                const uint32_t mid = lo + ((hi - lo) >> 1);
+                if (ckey[mid] < k0) lo = mid + 1;
+                else hi = mid;
+            }
+            for (uint32_t pos = lo; pos < (uint32_t)M && ckey[pos] <= k1; ++pos) {
                 const int64_t dx = (int64_t)(ckey[pos] - g.key_base - (uint64_t)ny * g.gx) - cx;
                 if (dx < 0) v0 = (int32_t)pos;
                 else if (dx == 0) v1 = (int32_t)pos;

@@ -184,13 +184,15 @@ __global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t p
     __syncthreads();
     for (int pass = local ? 0 : 1; pass < 2; ++pass) {
         for (uint64_t t0 = z0; t0 < z1; t0 += kDilThreads) {
-            const uint64_t z = t0 + threadIdx.x;
-            const uint64_t zw = t0 + (threadIdx.x & ~31u);   // the warp's first cell
+            // cell positions in 32 bits (M < 2^32) inside: the loops below are issue-bound
+            const bool in = t0 + threadIdx.x < z1;
+            const uint32_t z = (uint32_t)(t0 + threadIdx.x);
+            const uint32_t zw = (uint32_t)(t0 + (threadIdx.x & ~31u));   // the warp's first cell
             uint32_t row[WT];
             uint32_t f0 = 0;
-            if (z < z1) {
+            if (in) {
                 f0 = grids[cjob ? cjob[z] : 0u].f0;
-                load_row<WT>(nbmask + z * WT, row);
+                load_row<WT>(nbmask + (uint64_t)z * WT, row);
 #pragma unroll
                 for (int w = 0; w < WT; ++w)   // a nonzero word lies below F, so its bitset words exist
                     if (row[w]) row[w] = dil_wanted(want, f0, w, row[w]);
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t p
                 for (int w = 0; w < WT; ++w) row[w] = 0;
             }
             const uint32_t fl = __shfl_sync(0xffffffffu, f0, 0);
-            if (!__all_sync(0xffffffffu, z >= z1 || f0 == fl)) {
+            if (!__all_sync(0xffffffffu, !in || f0 == fl)) {
                 // the warp straddles a job boundary (batches of several jobs): in pass 1 every
                 // lane writes its own entries, one global atomic each
 #pragma unroll
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t p
                     if (pass == 1)
                         for (uint32_t bits = row[w]; bits; bits &= bits - 1) {
                             const uint32_t f = f0 + (uint32_t)w * 32 + (uint32_t)(__ffs(bits) - 1);
-                            dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = (uint32_t)z;
+                            dlist[doff[f] + atomicAdd(&cursor[f], 1u)] = z;
                         }
                     row[w] = 0;
                 }
@@ -230,7 +232,8 @@ __global__ void __launch_bounds__(kDilThreads) k_dil_fill(uint64_t M, uint64_t p
                 } else {
                     o = doff[f] + atomicAdd(&cursor[f], n);
                 }
-                for (uint32_t bits = col; bits; bits &= bits - 1) dlist[o++] = (uint32_t)(zw + (uint32_t)(__ffs(bits) - 1));
+                uint32_t* dst = dlist + o;
+                for (uint32_t bits = col; bits; bits &= bits - 1) *dst++ = zw + (uint32_t)(__ffs(bits) - 1);
             }
         }
         if (pass == 0) {   // reserve the block's ranges; pass 1 counts again from zero
